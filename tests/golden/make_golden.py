@@ -1,0 +1,65 @@
+"""Extract the reference's regression fixtures used to pin the oracle.
+
+Reads ``samples/<Case>/reference.out`` from a checkout of magic-sph/pizza
+(default: the read-only mount given by --ref) and writes the rows that come
+from the collocation runs into ``tests/golden/<Case>.txt``, together with the
+namelist values of the run that produced them (``tests/golden/cases.json``).
+
+Rows kept per case (the fixture concatenates several chained runs; only the
+first run starts from the namelist and needs no checkpoint):
+  NonRotRa2e3       all 11 rows   (e_kin, coll smat CNAB2, non-rotating)
+  RotE1e3EkPump     rows 0-10     (e_kin_3D, coll smat CNAB2, Ekman pumping)
+  MultistepSchemes  rows 0-200    (e_kin_3D, coll smat SBDF3 + CNAB2 bridge)
+  TimeStepChange    all 21 rows   (e_kin, coll dmat SBDF3, CFL dt changes)
+"""
+import argparse
+import json
+import os
+
+CASES = {
+    "NonRotRa2e3": dict(
+        rows=11, series="e_kin",
+        params=dict(n_r_max=33, n_cheb_max=33, m_max=32, n_time_steps=1000, dtMax=1e-3,
+                    l_non_rot=True, ra=2.0e3, pr=1.0, ek=1.0e-3, radratio=0.35,
+                    g0=1.0, g1=0.0, g2=0.0, init_t=3, amp_t=2.5e-4, n_log_step=100)),
+    "RotE1e3EkPump": dict(
+        rows=11, series="e_kin_3D",
+        params=dict(n_r_max=32, n_cheb_max=32, m_max=32, n_time_steps=1000, dtMax=1e-4,
+                    ra=2.77e4, pr=1.0, ek=1.0e-3, radratio=0.35, g0=0.0, g1=1.0, g2=0.0,
+                    l_ek_pump=True, init_t=4, amp_t=2.5e-4, n_log_step=100)),
+    "MultistepSchemes": dict(
+        rows=201, series="e_kin_3D",
+        params=dict(n_r_max=32, n_cheb_max=32, m_max=32, n_time_steps=200, dtMax=1e-4,
+                    time_scheme="SBDF3", ra=4.0e4, pr=1.0, ek=1.0e-3, radratio=0.35,
+                    g0=0.0, g1=1.0, g2=0.0, l_ek_pump=True, init_t=4, amp_t=2.5e-4,
+                    n_log_step=1)),
+    "TimeStepChange": dict(
+        rows=21, series="e_kin",
+        params=dict(n_r_max=48, n_cheb_max=48, m_max=64, n_time_steps=2000, dtMax=5e-4,
+                    time_scheme="SBDF3", courfac=2.5, l_non_rot=True,
+                    matrix_solve="INFLUENCE", ra=1.0e4, pr=1.0, ek=1.0e-3, radratio=0.35,
+                    g0=1.0, g1=0.0, g2=0.0, init_t=-1, amp_t=1.0e-2, n_log_step=100)),
+}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--ref", default="/root/reference")
+    args = ap.parse_args()
+    here = os.path.dirname(os.path.abspath(__file__))
+    meta = {}
+    for case, spec in CASES.items():
+        src = os.path.join(args.ref, "samples", case, "reference.out")
+        with open(src) as f:
+            lines = [ln for ln in f.read().splitlines() if ln.strip()]
+        keep = lines[:spec["rows"]]
+        with open(os.path.join(here, f"{case}.txt"), "w") as f:
+            f.write("\n".join(keep) + "\n")
+        meta[case] = dict(series=spec["series"], rows=spec["rows"], params=spec["params"],
+                          source=f"samples/{case}/reference.out")
+    with open(os.path.join(here, "cases.json"), "w") as f:
+        json.dump(meta, f, indent=1, sort_keys=True)
+
+
+if __name__ == "__main__":
+    main()
