@@ -1,0 +1,152 @@
+/*
+ * pizza_gpu.h -- C ABI of the GB300 (sm_103a) time step for pizza.
+ *
+ * The library advances one or many independent annulus instances of pizza's
+ * rotating quasi-geostrophic Boussinesq convection problem with the
+ * reference's collocation method.  It replaces, for each instance, the stage
+ * body of pizza's time_loop (src/step_time.f90:216-368): radial_loop
+ * (src/radial_loop.f90:231-394), the m<->r transposes
+ * (src/step_time.f90:550-626), finish_explicit_assembly and mloop
+ * (src/mloop.f90:36-229), the CFL check (src/courant.f90:78-167) and the
+ * IMEX bookkeeping of src/multistep_schemes.f90.
+ *
+ * Conventions
+ *  - FP64 throughout.  Complex arrays are interleaved (re, im) doubles, i.e.
+ *    Fortran complex(8) / C double _Complex / torch.complex128.
+ *  - Spectral arrays use the reference's m-distributed layout f(n_m, n_r),
+ *    n_m fastest (src/fields.f90:42-238): element (n_m, n_r) is at
+ *    2*(n_m + n_r*n_m_max).  n_r = 0 is the outer boundary r_cmb.
+ *  - Host buffers are owned by the caller and copied; device state belongs to
+ *    the library.  All work of one handle is ordered on one CUDA stream.
+ *  - Every entry point returns PZ_OK (0) or a negative PZ_E* code; nothing
+ *    aborts the process (the reference calls abortRun/MPI_Abort instead,
+ *    src/useful.f90:18-44).  pz_last_error() gives the message.
+ *  - One host thread per handle.
+ */
+#ifndef PIZZA_GPU_H
+#define PIZZA_GPU_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define PZ_OK              0
+#define PZ_E_ARG          -1  /* invalid argument or configuration           */
+#define PZ_E_CUDA         -2  /* CUDA runtime error                          */
+#define PZ_E_SINGULAR     -3  /* zero pivot in a matrix (abortRun 'Singular') */
+#define PZ_E_DT_TOO_SMALL -4  /* dt < dtMin (multistep_schemes.f90:335-345)  */
+#define PZ_E_NONFINITE    -5  /* NaN/Inf in the state                        */
+#define PZ_E_UNSUPPORTED  -6  /* option outside the implemented path         */
+#define PZ_E_NOMEM        -7  /* device allocation failed                    */
+
+/* time_scheme values (src/multistep_schemes.f90:35-134) */
+#define PZ_CNAB2   0
+#define PZ_SBDF2   1
+#define PZ_SBDF3   2
+#define PZ_SBDF4   3
+#define PZ_CNLF    4
+#define PZ_MODCNAB 5
+#define PZ_TVB33   6
+
+/* matrix_solve values (src/namelists.f90:416-421) */
+#define PZ_SOLVE_INFLUENCE 0   /* update_psi_coll_dmat: real om/psi solves + 2x2 influence matrix */
+#define PZ_SOLVE_DIRECT    1   /* update_psi_coll_smat: coupled 2N complex solve (not yet on GPU) */
+
+/*
+ * One instance's namelist values.  Mirrors pizza's input.nml groups &grid,
+ * &control, &phys_param (src/namelists.f90:162-189).  Fields not listed take
+ * the reference defaults of src/namelists.f90:530-672 (hdif off, container
+ * 'sphere', beta_shift 0, no forcing, temperature only).  pz_config_default()
+ * fills every field with those defaults.
+ */
+typedef struct pz_config {
+  int    n_r_max;      /* radial collocation points N                       */
+  int    n_cheb_max;   /* Chebyshev truncation (<= n_r_max)                  */
+  int    m_max;        /* azimuthal truncation; n_phi_max = 3*m_max/minc     */
+  int    minc;         /* azimuthal symmetry (1)                            */
+  double ra, ek, pr, radratio;
+  double g0, g1, g2;   /* gravity profile rgrav = g0 + g1 r/r_o + g2 r_o^2/r^2 */
+  int    ktopt, kbott; /* temperature BCs: 1 = fixed temperature            */
+  int    ktopv, kbotv; /* velocity BCs: 1 = stress-free, 2 = rigid           */
+  int    l_ek_pump;    /* Ekman pumping                                     */
+  int    l_non_rot;    /* non-rotating (ek < 0 also selects it)             */
+  int    l_temp_advz;  /* vertical advection of the background temperature  */
+  int    time_scheme;  /* PZ_CNAB2 ...                                      */
+  int    matrix_solve; /* PZ_SOLVE_INFLUENCE / PZ_SOLVE_DIRECT              */
+  int    corio_imp;    /* 1 = 'IMPLICIT' (forced explicit with INFLUENCE)   */
+  int    buo_imp;      /* 1 = 'IMPLICIT' (reference default)                */
+  double dtMax;        /* maximum and initial time step                     */
+  double courfac;      /* >= 1e3 selects the scheme's default CFL factor    */
+  double alpha;        /* Crank-Nicolson weight (0.5)                       */
+  double dt_fac;       /* CFL hysteresis factor (2)                         */
+} pz_config;
+
+typedef struct pz_handle pz_handle;
+
+/* Fill *cfg with the reference defaults (src/namelists.f90:530-672), with
+ * n_cheb_max = n_r_max. */
+void pz_config_default(pz_config* cfg);
+
+/* Create a batch of n_instances independent instances (sizes may differ) on
+ * the current CUDA device.  Builds the radial grids, Chebyshev operators,
+ * phi-FFT plans and the time-independent matrices on the device.
+ * Replaces pizza's init sequence (src/pizza.f90:64-199) up to, not including,
+ * the start fields. */
+int pz_create(const pz_config* cfgs, int n_instances, pz_handle** out);
+
+/* Start fields of one instance (src/init_fields.f90:54-258, no checkpoint):
+ * zero histories, time = 0, dt(:) = dtMax, then the given physical-space
+ * fields us, up, temp (complex (n_m, n_r) arrays, any may be NULL = zero),
+ * from which om, dT/dr and the first implicit state are derived on the
+ * device.  temp is the perturbation on top of the conducting profile. */
+int pz_set_state(pz_handle* h, int inst, const double* us, const double* up,
+                 const double* temp);
+
+/* Same as pz_set_state for all instances at once: each pointer (or NULL)
+ * addresses the concatenation of the instances' arrays in instance order. */
+int pz_set_state_all(pz_handle* h, const double* us, const double* up,
+                     const double* temp);
+
+/* Advance every instance by n_steps time steps: for each step the stage body
+ * of time_loop, with the CFL decision, weight update and matrix rebuild done
+ * on the device.  The step is captured once in a CUDA graph and replayed.
+ * Asynchronous: returns after enqueueing; pz_sync() waits and reports
+ * device-side errors. */
+int pz_step(pz_handle* h, int n_steps);
+
+/* Wait for all enqueued work and check the device status words. */
+int pz_sync(pz_handle* h);
+
+/* Copy one instance's physical state back: complex (n_m, n_r) arrays (any
+ * pointer may be NULL); time and dt(1) scalars (may be NULL). */
+int pz_get_state(pz_handle* h, int inst, double* us, double* up, double* om,
+                 double* psi, double* temp, double* dtemp, double* time,
+                 double* dt);
+
+/* Time series of one instance: one row per completed step plus the start row,
+ * most recent last, at most *n_rows rows (in: capacity, out: count).
+ * Row layout (PZ_SERIES_COLS doubles):
+ *   time, us2_2D, up2_2D, up2_axi_2D,                 (e_kin, outputs.f90:677)
+ *   us2_3D, up2_3D, uz2_3D, up2_axi_3D,               (e_kin_3D, outputs.f90:686)
+ *   NuTop, NuBot, Nu_vol, Nu_int, tTop, tBot, beta_t, (heat, outputs.f90:791)
+ *   dt                                                  (dt(1) of the step) */
+#define PZ_SERIES_COLS 16
+int pz_get_series(pz_handle* h, int inst, double* rows, int* n_rows);
+
+/* Sizes of one instance: n_r_max, n_m_max, n_phi_max. */
+int pz_get_dims(pz_handle* h, int inst, int* n_r_max, int* n_m_max, int* n_phi_max);
+
+/* Number of device kernel launches one time step issues (all instances). */
+int pz_launches_per_step(pz_handle* h);
+
+/* Release all device memory of the handle. */
+int pz_destroy(pz_handle* h);
+
+/* Last error message of the handle (or of the last failed pz_create when h
+ * is NULL).  Never NULL. */
+const char* pz_last_error(pz_handle* h);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* PIZZA_GPU_H */

@@ -1,0 +1,253 @@
+"""GB300 (sm_103a) time step of pizza: Python binding over the C ABI.
+
+The library in ``_lib/libpizza_gb300.so`` (declared in ``include/pizza_gpu.h``)
+advances one or many independent annulus instances of pizza's rotating
+quasi-geostrophic convection problem with the reference's collocation method.
+This module is a thin ctypes layer: configurations mirror pizza's input.nml
+(src/namelists.f90:162-189), spectral arrays use the reference's
+m-distributed layout ``f(n_m, n_r)`` (numpy shape ``(n_m_max, n_r_max)``,
+complex128), and time series rows mirror pizza's e_kin / e_kin_3D / heat files
+(src/outputs.f90:677-793).
+
+There is no CPU fallback: if the library is missing or no GPU is present,
+every call raises.
+"""
+from __future__ import annotations
+
+import ctypes
+import dataclasses
+import os
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "_lib", "libpizza_gb300.so")
+
+SCHEMES = {"CNAB2": 0, "SBDF2": 1, "BDF2AB2": 1, "SBDF3": 2, "BDF3AB3": 2, "SBDF4": 3,
+           "BDF4AB4": 3, "CNLF": 4, "MODCNAB": 5, "TVB33": 6}
+SOLVE_INFLUENCE, SOLVE_DIRECT = 0, 1
+SERIES_COLS = 16
+SERIES_NAMES = ("time", "us2_2D", "up2_2D", "up2_axi_2D", "us2_3D", "up2_3D", "uz2_3D",
+                "up2_axi_3D", "NuTop", "NuBot", "Nu_vol", "Nu_int", "tTop", "tBot", "beta_t", "dt")
+
+PZ_ERRORS = {-1: "invalid argument", -2: "CUDA error", -3: "singular matrix",
+             -4: "time step too small", -5: "non-finite state", -6: "unsupported option",
+             -7: "out of device memory"}
+
+
+class PizzaError(RuntimeError):
+    """Error returned by the library (code < 0)."""
+
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"{PZ_ERRORS.get(code, 'error')} ({code}): {msg}")
+        self.code = code
+
+
+class _CConfig(ctypes.Structure):
+    _fields_ = [("n_r_max", ctypes.c_int), ("n_cheb_max", ctypes.c_int), ("m_max", ctypes.c_int),
+                ("minc", ctypes.c_int), ("ra", ctypes.c_double), ("ek", ctypes.c_double),
+                ("pr", ctypes.c_double), ("radratio", ctypes.c_double), ("g0", ctypes.c_double),
+                ("g1", ctypes.c_double), ("g2", ctypes.c_double), ("ktopt", ctypes.c_int),
+                ("kbott", ctypes.c_int), ("ktopv", ctypes.c_int), ("kbotv", ctypes.c_int),
+                ("l_ek_pump", ctypes.c_int), ("l_non_rot", ctypes.c_int), ("l_temp_advz", ctypes.c_int),
+                ("time_scheme", ctypes.c_int), ("matrix_solve", ctypes.c_int), ("corio_imp", ctypes.c_int),
+                ("buo_imp", ctypes.c_int), ("dtMax", ctypes.c_double), ("courfac", ctypes.c_double),
+                ("alpha", ctypes.c_double), ("dt_fac", ctypes.c_double)]
+
+
+@dataclasses.dataclass
+class Config:
+    """One instance's namelist values (defaults: src/namelists.f90:530-672,
+    except matrix_solve, which defaults to the influence-matrix path that the
+    GPU implements)."""
+    n_r_max: int = 32
+    n_cheb_max: int | None = None
+    m_max: int = 32
+    minc: int = 1
+    ra: float = 1.0e5
+    ek: float = 1.0e-3
+    pr: float = 1.0
+    radratio: float = 0.35
+    g0: float = 0.0
+    g1: float = 1.0
+    g2: float = 0.0
+    ktopt: int = 1
+    kbott: int = 1
+    ktopv: int = 2
+    kbotv: int = 2
+    l_ek_pump: bool = False
+    l_non_rot: bool = False
+    l_temp_advz: bool = False
+    time_scheme: str = "CNAB2"
+    matrix_solve: str = "INFLUENCE"
+    corio_term: str = "IMPLICIT"
+    buo_term: str = "IMPLICIT"
+    dtMax: float = 1.0e-5
+    courfac: float = 1.0e3
+    alpha: float = 0.5
+    dt_fac: float = 2.0
+
+    def to_c(self) -> _CConfig:
+        c = _CConfig()
+        for f in ("n_r_max", "m_max", "minc", "ra", "ek", "pr", "radratio", "g0", "g1", "g2",
+                  "ktopt", "kbott", "ktopv", "kbotv", "dtMax", "courfac", "alpha", "dt_fac"):
+            setattr(c, f, getattr(self, f))
+        c.n_cheb_max = self.n_r_max if self.n_cheb_max is None else self.n_cheb_max
+        c.l_ek_pump = int(bool(self.l_ek_pump))
+        c.l_non_rot = int(bool(self.l_non_rot))
+        c.l_temp_advz = int(bool(self.l_temp_advz))
+        ts = self.time_scheme.upper()
+        if ts not in SCHEMES:
+            raise ValueError(f"time integrator {self.time_scheme} not found")
+        c.time_scheme = SCHEMES[ts]
+        c.matrix_solve = SOLVE_DIRECT if "DIRECT" in self.matrix_solve.upper() else SOLVE_INFLUENCE
+        c.corio_imp = int("IMP" in self.corio_term.upper())
+        c.buo_imp = int("IMP" in self.buo_term.upper())
+        return c
+
+    @property
+    def n_m_max(self) -> int:
+        return self.m_max // self.minc + 1
+
+    @property
+    def n_phi_max(self) -> int:
+        return 3 * self.m_max // self.minc
+
+
+_lib = None
+
+
+def load_library(path: str | None = None):
+    """Load the CUDA library (raises if it is absent: there is no fallback)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    p = path or LIB_PATH
+    if not os.path.exists(p):
+        raise RuntimeError(f"pizza_gb300 CUDA library not built: {p} (run `python -m pizza_gb300.build`)")
+    lib = ctypes.CDLL(p)
+    dp = ctypes.POINTER(ctypes.c_double)
+    lib.pz_config_default.argtypes = [ctypes.POINTER(_CConfig)]
+    lib.pz_config_default.restype = None
+    lib.pz_create.argtypes = [ctypes.POINTER(_CConfig), ctypes.c_int, ctypes.POINTER(ctypes.c_void_p)]
+    lib.pz_set_state.argtypes = [ctypes.c_void_p, ctypes.c_int, dp, dp, dp]
+    lib.pz_set_state_all.argtypes = [ctypes.c_void_p, dp, dp, dp]
+    lib.pz_step.argtypes = [ctypes.c_void_p, ctypes.c_int]
+    lib.pz_sync.argtypes = [ctypes.c_void_p]
+    lib.pz_get_state.argtypes = [ctypes.c_void_p, ctypes.c_int, dp, dp, dp, dp, dp, dp, dp, dp]
+    lib.pz_get_series.argtypes = [ctypes.c_void_p, ctypes.c_int, dp, ctypes.POINTER(ctypes.c_int)]
+    lib.pz_get_dims.argtypes = [ctypes.c_void_p, ctypes.c_int] + [ctypes.POINTER(ctypes.c_int)] * 3
+    lib.pz_launches_per_step.argtypes = [ctypes.c_void_p]
+    lib.pz_destroy.argtypes = [ctypes.c_void_p]
+    lib.pz_last_error.argtypes = [ctypes.c_void_p]
+    lib.pz_last_error.restype = ctypes.c_char_p
+    for f in ("pz_create", "pz_set_state", "pz_set_state_all", "pz_step", "pz_sync", "pz_get_state",
+              "pz_get_series", "pz_get_dims", "pz_launches_per_step", "pz_destroy"):
+        getattr(lib, f).restype = ctypes.c_int
+    _lib = lib
+    return lib
+
+
+def _dptr(a):
+    if a is None:
+        return None
+    return a.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+
+
+def _carr(a, shape):
+    """(n_m, n_r) complex array -> C-contiguous complex128 in Fortran (n_m fastest) order."""
+    if a is None:
+        return None
+    a = np.asarray(a, dtype=np.complex128)
+    if a.shape != shape:
+        raise ValueError(f"expected shape {shape}, got {a.shape}")
+    # (n_m, n_r) with n_m fastest == row-major (n_r, n_m)
+    return np.ascontiguousarray(a.T)
+
+
+class Ensemble:
+    """A batch of independent pizza instances advanced together on one GPU."""
+
+    def __init__(self, configs):
+        if isinstance(configs, Config):
+            configs = [configs]
+        self.configs = list(configs)
+        self.lib = load_library()
+        arr = (_CConfig * len(self.configs))(*[c.to_c() for c in self.configs])
+        h = ctypes.c_void_p()
+        rc = self.lib.pz_create(arr, len(self.configs), ctypes.byref(h))
+        if rc != 0:
+            raise PizzaError(rc, self.lib.pz_last_error(None).decode())
+        self._h = h
+        self.dims = []
+        for i in range(len(self.configs)):
+            a, b, c = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
+            self._check(self.lib.pz_get_dims(self._h, i, ctypes.byref(a), ctypes.byref(b), ctypes.byref(c)))
+            self.dims.append((a.value, b.value, c.value))
+
+    def _check(self, rc):
+        if rc != 0:
+            raise PizzaError(rc, self.lib.pz_last_error(self._h).decode())
+
+    def __len__(self):
+        return len(self.configs)
+
+    def shape(self, i):
+        n, m, _ = self.dims[i]
+        return (m, n)
+
+    def set_state(self, i, us=None, up=None, temp=None):
+        """pizza's start fields (src/init_fields.f90:54-258) from physical fields."""
+        shp = self.shape(i)
+        a, b, c = _carr(us, shp), _carr(up, shp), _carr(temp, shp)
+        self._check(self.lib.pz_set_state(self._h, i, _dptr(a), _dptr(b), _dptr(c)))
+
+    def set_state_all(self, temps, us=None, up=None):
+        """Start fields of every instance; ``temps`` is a list of (n_m, n_r) arrays."""
+        def cat(lst):
+            if lst is None:
+                return None
+            return np.concatenate([_carr(x, self.shape(i)).ravel() for i, x in enumerate(lst)])
+        a, b, c = cat(us), cat(up), cat(temps)
+        self._check(self.lib.pz_set_state_all(self._h, _dptr(a), _dptr(b), _dptr(c)))
+
+    def step(self, n_steps=1, sync=True):
+        self._check(self.lib.pz_step(self._h, int(n_steps)))
+        if sync:
+            self.sync()
+
+    def sync(self):
+        self._check(self.lib.pz_sync(self._h))
+
+    def get_state(self, i):
+        """Physical fields of instance i as (n_m, n_r) complex arrays, plus time and dt."""
+        n, m, _ = self.dims[i]
+        bufs = {k: np.zeros((n, m), np.complex128) for k in ("us", "up", "om", "psi", "temp", "dtemp")}
+        t, dt = ctypes.c_double(), ctypes.c_double()
+        self._check(self.lib.pz_get_state(self._h, i, *[_dptr(bufs[k]) for k in ("us", "up", "om", "psi", "temp", "dtemp")],
+                                          ctypes.byref(t), ctypes.byref(dt)))
+        out = {k: v.T.copy() for k, v in bufs.items()}
+        out["time"] = t.value
+        out["dt"] = dt.value
+        return out
+
+    def series(self, i, max_rows=1024):
+        """Time series rows of instance i (columns: SERIES_NAMES)."""
+        rows = np.zeros((max_rows, SERIES_COLS))
+        n = ctypes.c_int(max_rows)
+        self._check(self.lib.pz_get_series(self._h, i, _dptr(rows), ctypes.byref(n)))
+        return rows[: n.value].copy()
+
+    def launches_per_step(self):
+        return self.lib.pz_launches_per_step(self._h)
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self.lib.pz_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

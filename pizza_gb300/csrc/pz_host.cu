@@ -1,0 +1,650 @@
+// Host side of the GB300 pizza time step: configuration, radial grid and
+// Chebyshev operators, device pool layout and the C ABI of pizza_gpu.h.
+//
+// What runs here is set-up work of pizza's init sequence (src/pizza.f90:64-199):
+// read_namelists' derived switches (src/namelists.f90:271-526), the
+// Gauss-Lobatto grid and collocation matrices (src/chebyshev.f90:222-383),
+// the radial functions (src/radial.f90:115-282) and the integration weights
+// (src/integration.f90).  Everything per time step runs on the device.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <string>
+#include <vector>
+
+#include "pizza_gpu.h"
+#include "pz_internal.h"
+
+namespace {
+
+thread_local std::string g_create_error = "no error";
+
+struct HostInst {
+  pz_config c;
+  PzInst I;
+};
+
+}  // namespace
+
+struct pz_handle {
+  int n_inst = 0;
+  std::vector<HostInst> hin;
+  std::vector<PzInst> inst;
+  double* pool = nullptr;
+  long long pool_size = 0;
+  PzInst* d_inst = nullptr;
+  PzState* d_state = nullptr;
+  PzItem* d_ritems = nullptr;
+  PzItem* d_mitems = nullptr;
+  PzDev dev{};
+  cudaStream_t stream = nullptr;
+  cudaGraphExec_t graph = nullptr;
+  double* h_stage = nullptr;   // pinned staging buffer
+  long long h_stage_size = 0;
+  std::string err = "no error";
+};
+
+namespace {
+
+int fail(pz_handle* h, int code, const std::string& msg) {
+  if (h) h->err = msg; else g_create_error = msg;
+  return code;
+}
+
+int cuda_fail(pz_handle* h, cudaError_t e, const char* what) {
+  return fail(h, PZ_E_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+// -------------------------------------------------------------------------
+// Chebyshev operators for N Gauss-Lobatto points (chebyshev.f90:222-383,
+// dct_fftw.f90:46-397).  All column-major N x N.
+// -------------------------------------------------------------------------
+struct Basis {
+  int N;
+  std::vector<double> x, C, D1c, D2c, D1p, D2p, rMat, drMat, d2rMat;
+};
+
+Basis make_basis(int N, double r_icb, double r_cmb) {
+  Basis b;
+  b.N = N;
+  const long double pi = 3.141592653589793238462643383279502884L;
+  b.x.resize(N);
+  for (int k = 0; k < N; ++k) b.x[k] = (double)cosl(pi * (long double)k / (long double)(N - 1));
+  const double drx = 2.0 / (r_cmb - r_icb), ddrx = 0.0;
+  // recursion over the polynomial degree (get_der_mat), stored as (grid i, degree n)
+  std::vector<double> rM(N * N), drM(N * N), d2rM(N * N);
+  auto at = [N](std::vector<double>& A, int i, int n) -> double& { return A[i + (size_t)n * N]; };
+  for (int i = 0; i < N; ++i) {
+    at(rM, i, 0) = 1.0; at(rM, i, 1) = b.x[i];
+    at(drM, i, 0) = 0.0; at(drM, i, 1) = drx;
+    at(d2rM, i, 0) = 0.0; at(d2rM, i, 1) = ddrx;
+    for (int n = 2; n < N; ++n) {
+      at(rM, i, n) = 2.0 * b.x[i] * at(rM, i, n - 1) - at(rM, i, n - 2);
+      at(drM, i, n) = 2.0 * drx * at(rM, i, n - 1) + 2.0 * b.x[i] * at(drM, i, n - 1) - at(drM, i, n - 2);
+      at(d2rM, i, n) = 2.0 * ddrx * at(rM, i, n - 1) + 4.0 * drx * at(drM, i, n - 1) +
+                       2.0 * b.x[i] * at(d2rM, i, n - 1) - at(d2rM, i, n - 2);
+    }
+  }
+  b.rMat = rM; b.drMat = drM; b.d2rMat = d2rM;
+  const double rnorm = std::sqrt(2.0 / (double)(N - 1));
+  const double cheb_fac = std::sqrt(0.5 / (double)(N - 1));
+  // costf1 as a matrix: out_k = cheb_fac * sum_j w_j cos(pi j k/(N-1)) f_j
+  b.C.assign((size_t)N * N, 0.0);
+  const long long L = 2LL * (N - 1);
+  for (int k = 0; k < N; ++k)
+    for (int j = 0; j < N; ++j) {
+      const long long q = ((long long)j * k) % L;
+      const double cs = (double)cosl(pi * (long double)q / (long double)(N - 1));
+      const double w = (j == 0 || j == N - 1) ? 1.0 : 2.0;
+      b.C[k + (size_t)j * N] = cheb_fac * w * cs;
+    }
+  // Chebyshev -> physical derivatives: rnorm * bfac_k * T_k^(p)(x_i)
+  b.D1c.resize((size_t)N * N);
+  b.D2c.resize((size_t)N * N);
+  for (int i = 0; i < N; ++i)
+    for (int k = 0; k < N; ++k) {
+      const double bf = (k == 0 || k == N - 1) ? 0.5 : 1.0;
+      b.D1c[i + (size_t)k * N] = rnorm * bf * at(drM, i, k);
+      b.D2c[i + (size_t)k * N] = rnorm * bf * at(d2rM, i, k);
+    }
+  // physical -> physical: D = Dc * C (accumulated in long double)
+  auto matmul = [N](const std::vector<double>& A, const std::vector<double>& B) {
+    std::vector<double> R((size_t)N * N);
+    for (int i = 0; i < N; ++i)
+      for (int j = 0; j < N; ++j) {
+        long double s = 0.0L;
+        for (int k = 0; k < N; ++k) s += (long double)A[i + (size_t)k * N] * (long double)B[k + (size_t)j * N];
+        R[i + (size_t)j * N] = (double)s;
+      }
+    return R;
+  };
+  b.D1p = matmul(b.D1c, b.C);
+  b.D2p = matmul(b.D2c, b.C);
+  return b;
+}
+
+bool factor_fft(int P, int* radix, int* nrad) {
+  int n = P, k = 0;
+  while (n % 4 == 0) { if (k >= PZ_MAX_RADIX) return false; radix[k++] = 4; n /= 4; }
+  while (n % 2 == 0) { if (k >= PZ_MAX_RADIX) return false; radix[k++] = 2; n /= 2; }
+  const int odd[3] = {3, 5, 7};
+  for (int t = 0; t < 3; ++t)
+    while (n % odd[t] == 0) { if (k >= PZ_MAX_RADIX) return false; radix[k++] = odd[t]; n /= odd[t]; }
+  *nrad = k;
+  return n == 1;
+}
+
+int scheme_counts(int scheme, int* nold, int* nimp, int* nexp, double* cf, int* imp_calc) {
+  // multistep_schemes.f90:53-106
+  *imp_calc = 1;
+  switch (scheme) {
+    case PZ_CNAB2: *nimp = 1; *nold = 1; *nexp = 2; *cf = 3.0; break;
+    case PZ_MODCNAB: *nold = 2; *nimp = 2; *nexp = 2; *cf = 2.9; break;
+    case PZ_CNLF: *nold = 2; *nimp = 2; *nexp = 2; *cf = 3.0; break;
+    case PZ_SBDF2: *nold = 2; *nimp = 1; *nexp = 2; *cf = 2.8; *imp_calc = 0; break;
+    case PZ_SBDF3: *nold = 3; *nimp = 1; *nexp = 3; *cf = 4.0; *imp_calc = 0; break;
+    case PZ_TVB33: *nold = 3; *nimp = 3; *nexp = 3; *cf = 4.0; break;
+    case PZ_SBDF4: *nold = 4; *nimp = 1; *nexp = 4; *cf = 5.5; *imp_calc = 0; break;
+    default: return -1;
+  }
+  return 0;
+}
+
+// simps (integration.f90:104-152) applied to f, as a linear functional
+double simps(const std::vector<double>& f, const std::vector<double>& r) {
+  const int n = (int)f.size();
+  double s = 0.0;
+  auto seg = [&](int i) {
+    const double h2 = r[i + 1] - r[i], h1 = r[i] - r[i - 1];
+    return (h1 + h2) / 6.0 * (f[i - 1] * (2 * h1 - h2) / h1 + f[i] * (h1 + h2) * (h1 + h2) / (h1 * h2) +
+                             f[i + 1] * (2 * h2 - h1) / h2);
+  };
+  if (n % 2 == 1) {
+    for (int i = 1; i < n - 1; i += 2) s += seg(i);
+    return -s;
+  }
+  s = 0.5 * (r[1] - r[0]) * (f[1] + f[0]);
+  for (int i = 2; i < n - 1; i += 2) s += seg(i);
+  s += 0.5 * (r[n - 1] - r[n - 2]) * (f[n - 1] + f[n - 2]);
+  for (int i = 1; i < n - 1; i += 2) s += seg(i);
+  return -0.5 * s;
+}
+
+int validate(const pz_config& c, std::string* why) {
+  auto bad = [&](const char* m) { *why = m; return PZ_E_ARG; };
+  auto uns = [&](const char* m) { *why = m; return PZ_E_UNSUPPORTED; };
+  if (c.n_r_max < 5 || c.n_r_max > 128) return bad("n_r_max must be in [5, 128]");
+  if (c.n_cheb_max < 2 || c.n_cheb_max > c.n_r_max) return bad("n_cheb_max must be in [2, n_r_max]");
+  if (c.minc != 1) return uns("minc != 1 is not implemented");
+  if (c.m_max < 2 || c.m_max > 512) return bad("m_max must be in [2, 512]");
+  if (c.ra == 0.0) return uns("ra = 0 (no temperature equation) is not implemented");
+  if (c.pr <= 0.0) return bad("pr must be > 0");
+  if (!(c.radratio > 0.0 && c.radratio < 1.0)) return uns("radratio must be in (0, 1): the full disk is not implemented");
+  if (c.ktopt != 1 || c.kbott != 1) return uns("only fixed-temperature boundaries (ktopt = kbott = 1)");
+  if (c.ktopv != 2 || c.kbotv != 2) return uns("only rigid boundaries (ktopv = kbotv = 2)");
+  if (c.matrix_solve != PZ_SOLVE_INFLUENCE) return uns("matrix_solve DIRECT is not on the GPU yet; use INFLUENCE");
+  if (c.dtMax <= 0.0) return bad("dtMax must be > 0");
+  if (c.alpha <= 0.0 || c.alpha > 1.0) return bad("alpha must be in (0, 1]");
+  if (c.dt_fac <= 1.0) return bad("dt_fac must be > 1");
+  int a, b, d, e; double f;
+  if (scheme_counts(c.time_scheme, &a, &b, &d, &f, &e) != 0) return bad("unknown time_scheme");
+  int radix[PZ_MAX_RADIX], nr;
+  if (!factor_fft(3 * c.m_max / c.minc, radix, &nr)) return uns("n_phi_max must factor into 2, 3, 5, 7");
+  return PZ_OK;
+}
+
+}  // namespace
+
+// ===========================================================================
+// C ABI
+// ===========================================================================
+extern "C" void pz_config_default(pz_config* c) {
+  if (!c) return;
+  std::memset(c, 0, sizeof(*c));
+  // src/namelists.f90:530-672
+  c->n_r_max = 32; c->n_cheb_max = 32; c->m_max = 32; c->minc = 1;
+  c->ra = 1.0e5; c->ek = 1.0e-3; c->pr = 1.0; c->radratio = 0.35;
+  c->g0 = 0.0; c->g1 = 1.0; c->g2 = 0.0;
+  c->ktopt = 1; c->kbott = 1; c->ktopv = 2; c->kbotv = 2;
+  c->l_ek_pump = 0; c->l_non_rot = 0; c->l_temp_advz = 0;
+  c->time_scheme = PZ_CNAB2; c->matrix_solve = PZ_SOLVE_DIRECT;
+  c->corio_imp = 1; c->buo_imp = 1;
+  c->dtMax = 1.0e-5; c->courfac = 1.0e3; c->alpha = 0.5; c->dt_fac = 2.0;
+}
+
+extern "C" int pz_create(const pz_config* cfgs, int n, pz_handle** out) {
+  if (!cfgs || n <= 0 || !out) return fail(nullptr, PZ_E_ARG, "pz_create: bad arguments");
+  *out = nullptr;
+  for (int i = 0; i < n; ++i) {
+    std::string why;
+    const int rc = validate(cfgs[i], &why);
+    if (rc != PZ_OK) return fail(nullptr, rc, "instance " + std::to_string(i) + ": " + why);
+  }
+  pz_handle* h = new pz_handle();
+  h->n_inst = n;
+  h->hin.resize(n);
+  h->inst.resize(n);
+
+  long long off = 0;
+  auto take = [&off](long long nd) { long long o = off; off += (nd + 1) & ~1LL; return o; };
+  std::map<int, long long> basis_off;    // by N
+  std::map<int, Basis> bases;
+  std::map<int, long long> tw_off;       // by P
+  std::vector<std::vector<double>> rad(n);
+  int maxN = 0, maxP = 0, maxM = 0;
+  for (int i = 0; i < n; ++i) {
+    const pz_config& c = cfgs[i];
+    PzInst I;
+    std::memset(&I, 0, sizeof(I));
+    I.N = c.n_r_max; I.n_max = c.n_cheb_max; I.mmax = c.m_max; I.minc = c.minc;
+    I.M = c.m_max / c.minc + 1;                   // truncation.f90:28
+    I.P = 3 * c.m_max / c.minc;                   // truncation.f90:30-31
+    factor_fft(I.P, I.radix, &I.nrad);
+    double cf;
+    int imp_calc;
+    scheme_counts(c.time_scheme, &I.nold, &I.nimp, &I.nexp, &cf, &imp_calc);
+    I.scheme = c.time_scheme;
+    I.courfac = std::fabs(c.courfac) >= 1.0e3 ? cf : c.courfac;
+    // derived switches (namelists.f90:271-526)
+    double ek = c.ek;
+    const bool non_rot = c.l_non_rot || ek < 0.0;
+    if (non_rot) ek = -1.0;
+    I.ek = ek;
+    I.tadvz = c.l_temp_advz ? 1.0 : 0.0;
+    I.alpha = c.alpha;
+    I.dtMax = c.dtMax; I.dtMin = c.dtMax / 1.0e6;   // pre_calculations.f90:33
+    I.dt_fac = c.dt_fac;
+    if (non_rot) { I.CorFac = 0.0; I.BuoFac = c.ra / c.pr; I.TdiffFac = 1.0 / c.pr; I.ViscFac = 1.0; }
+    else { I.CorFac = 2.0 / ek; I.BuoFac = c.ra / c.pr; I.TdiffFac = 1.0 / c.pr; I.ViscFac = 1.0; }
+    I.flags = 0;
+    if (c.buo_imp) I.flags |= PZF_BUO_IMP;
+    if (c.l_ek_pump) I.flags |= PZF_EK_PUMP;
+    if (non_rot) I.flags |= PZF_NON_ROT;
+    if (imp_calc) I.flags |= PZF_IMP_CALC;
+    const int N = I.N;
+    I.rnorm = std::sqrt(2.0 / (double)(N - 1));
+    I.r_cmb = 1.0 / (1.0 - c.radratio);
+    I.r_icb = I.r_cmb - 1.0;
+    if (!bases.count(N)) {
+      bases[N] = make_basis(N, I.r_icb, I.r_cmb);
+      basis_off[N] = take((long long)BM_COUNT * N * N);
+    }
+    I.o_basis = basis_off[N];
+    if (!tw_off.count(I.P)) tw_off[I.P] = take(2LL * I.P);
+    I.o_tw = tw_off[I.P];
+    // radial functions (radial.f90:115-282)
+    const Basis& B = bases[N];
+    std::vector<double>& R = rad[i];
+    R.assign((size_t)RV_COUNT * N, 0.0);
+    auto rv = [&R, N](int k, int r) -> double& { return R[(size_t)k * N + r]; };
+    const double bma = 0.5 * (I.r_cmb - I.r_icb), bpa = 0.5 * (I.r_icb + I.r_cmb);
+    std::vector<double> r(N);
+    for (int k = 0; k < N; ++k) r[k] = bma * B.x[k] + bpa;
+    const double ek_pump_fac = (c.l_ek_pump && !non_rot) ? 1.0 : 0.0;
+    const double rc = I.r_cmb, ri = I.r_icb;
+    const double m_R = (double)c.m_max;
+    const double twopi3 = 2.0 * 3.14159265358979323846 / 3.0;
+    for (int k = 0; k < N; ++k) {
+      rv(RV_R, k) = r[k];
+      rv(RV_OR1, k) = 1.0 / r[k];
+      rv(RV_OR2, k) = rv(RV_OR1, k) * rv(RV_OR1, k);
+      rv(RV_RGRAV, k) = c.g0 + c.g1 * r[k] / rc + c.g2 * rc * rc * rv(RV_OR2, k);
+      rv(RV_TCOND, k) = std::log(r[k] / rc) / std::log(c.radratio);
+      rv(RV_DTCOND, k) = rv(RV_OR1, k) / std::log(c.radratio);
+      if (non_rot) {
+        rv(RV_HEIGHT, k) = 1.0;
+      } else if (k > 0) {
+        const double s2 = rc * rc - r[k] * r[k];
+        rv(RV_HEIGHT, k) = 2.0 * std::sqrt(s2);
+        const double oh = 0.5 / std::sqrt(s2);
+        rv(RV_BETA, k) = -r[k] / s2;
+        rv(RV_DBETA, k) = -(rc * rc + r[k] * r[k]) / (s2 * s2);
+        rv(RV_EKPUMP, k) = 0.5 * ek_pump_fac * std::sqrt(ek * rc) / std::pow(s2, 0.75);
+        rv(RV_EKP_UP, k) = -0.5 * rv(RV_BETA, k);
+        rv(RV_EKP_US, k) = -5.0 * rc * rv(RV_BETA, k) * oh;
+        rv(RV_EKP_DUSDP, k) = rv(RV_BETA, k);
+      }
+      // Courant lengths (radial.f90:164-173)
+      if (k == 0) {
+        rv(RV_DELXH2, k) = std::pow(twopi3 / m_R * rc, 2);
+        rv(RV_DELXR2, k) = std::pow(r[0] - r[1], 2);
+      } else if (k == N - 1) {
+        rv(RV_DELXH2, k) = std::pow(twopi3 / m_R * ri, 2);
+        rv(RV_DELXR2, k) = std::pow(r[N - 2] - r[N - 1], 2);
+      } else {
+        rv(RV_DELXH2, k) = std::pow(twopi3 / m_R * r[k], 2);
+        const double dmin = std::min(r[k - 1] - r[k], r[k] - r[k + 1]);
+        rv(RV_DELXR2, k) = dmin * dmin;
+      }
+    }
+    // rInt_R weights: rInt(f) = 2 sqrt(2/(N-1)) sum_k q_k (C f/drx)_k
+    std::vector<double> q(N, 0.0);
+    q[0] = 0.5;
+    for (int nc = 3; nc <= N; nc += 2) q[nc - 1] = -1.0 / (double)(nc * (nc - 2));
+    if ((N - 1) % 2 == 0) q[N - 1] *= 0.5;   // f2(n_r_max) halved before the sum
+    const double drx = 2.0 / (rc - ri);
+    const double pre = 2.0 * std::sqrt(2.0 / (double)(N - 1));
+    for (int j = 0; j < N; ++j) {
+      long double s = 0.0L;
+      for (int k = 0; k < N; ++k) s += (long double)q[k] * (long double)B.C[k + (size_t)j * N];
+      rv(RV_WINT, j) = pre * (double)s / drx;
+    }
+    // simps over colatitude theta = asin(r/r_cmb) (outputs.f90:768-783)
+    std::vector<double> th(N), e(N, 0.0);
+    for (int k = 0; k < N; ++k) th[k] = std::asin(std::min(1.0, r[k] / rc));
+    for (int j = 0; j < N; ++j) {
+      std::fill(e.begin(), e.end(), 0.0);
+      e[j] = 1.0;
+      rv(RV_WSIMP, j) = simps(e, th);
+    }
+    // influence-matrix boundary rows, rigid walls: rnorm * bfac * drMat
+    for (int k = 0; k < N; ++k) {
+      const double bf = (k == 0 || k == N - 1) ? 0.5 : 1.0;
+      rv(RV_BCTOP, k) = I.rnorm * bf * B.drMat[0 + (size_t)k * N];
+      rv(RV_BCBOT, k) = I.rnorm * bf * B.drMat[(N - 1) + (size_t)k * N];
+    }
+    // denominators of Nu_vol and Nu_int
+    double sv = 0.0, sf = 0.0, sfs = 0.0;
+    std::vector<double> tmp(N);
+    for (int k = 0; k < N; ++k) {
+      sv += rv(RV_WINT, k) * rv(RV_DTCOND, k) * rv(RV_DTCOND, k) * rv(RV_HEIGHT, k) * r[k];
+      sf += rv(RV_WINT, k) * (-I.TdiffFac * rv(RV_DTCOND, k) * r[k]);
+      tmp[k] = -I.TdiffFac * rv(RV_DTCOND, k) * (r[k] / rc) * (r[k] / rc);
+    }
+    sfs = simps(tmp, th);
+    I.nu_vol_den = sv;
+    I.nu_int_fac = non_rot ? sf : sfs;
+    I.o_rad = take((long long)RV_COUNT * N);
+    h->hin[i].c = c;
+    h->inst[i] = I;
+    maxN = std::max(maxN, N);
+    maxP = std::max(maxP, I.P);
+    maxM = std::max(maxM, I.M);
+  }
+  // per-instance operators and state
+  for (int i = 0; i < n; ++i) {
+    PzInst& I = h->inst[i];
+    const long long N = I.N, M = I.M;
+    I.o_gt = take(M * N * N);
+    I.o_gom = take(M * N * N);
+    I.o_guphi = take(N * N);
+    I.o_gpsi = take(M * N * N);
+    I.o_aux = take(4 * M * N + 4 * M);
+    I.o_fld = take(2LL * F_COUNT * M * N);
+    I.o_hist = take(2LL * 2 * (I.nold + I.nimp + I.nexp) * M * N);
+    I.o_cfl = take(2 * N);
+    I.o_series = take((long long)PZ_SERIES_CAP * PZ_SERIES_COLS);
+  }
+  h->pool_size = off;
+  cudaError_t e;
+  if ((e = pz_setup_kernels())) { int rc = cuda_fail(nullptr, e, "kernel setup"); delete h; return rc; }
+  if ((e = cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking))) {
+    int rc = cuda_fail(nullptr, e, "stream"); delete h; return rc;
+  }
+  if ((e = cudaMalloc(&h->pool, (size_t)off * sizeof(double)))) {
+    g_create_error = std::string("device pool allocation: ") + cudaGetErrorString(e);
+    pz_destroy(h);
+    return PZ_E_NOMEM;
+  }
+  // host image of the constant parts, uploaded in one copy
+  std::vector<double> img;
+  {
+    long long hi = 0;
+    for (auto& kv : basis_off) hi = std::max(hi, kv.second + (long long)BM_COUNT * kv.first * kv.first);
+    for (auto& kv : tw_off) hi = std::max(hi, kv.second + 2LL * kv.first);
+    for (int i = 0; i < n; ++i) hi = std::max(hi, h->inst[i].o_rad + (long long)RV_COUNT * h->inst[i].N);
+    img.assign((size_t)hi, 0.0);
+    for (auto& kv : bases) {
+      const Basis& B = kv.second;
+      const long long NN = (long long)B.N * B.N;
+      double* dst = img.data() + basis_off[kv.first];
+      const std::vector<double>* mats[BM_COUNT] = {&B.C, &B.D1c, &B.D2c, &B.D1p, &B.D2p, &B.rMat, &B.drMat, &B.d2rMat};
+      for (int k = 0; k < BM_COUNT; ++k) std::memcpy(dst + k * NN, mats[k]->data(), NN * sizeof(double));
+    }
+    const long double pi = 3.141592653589793238462643383279502884L;
+    for (auto& kv : tw_off) {
+      const int P = kv.first;
+      double* dst = img.data() + kv.second;
+      for (int k = 0; k < P; ++k) {
+        const long double a = 2.0L * pi * (long double)k / (long double)P;
+        dst[2 * k] = (double)cosl(a);
+        dst[2 * k + 1] = -(double)sinl(a);
+      }
+    }
+    for (int i = 0; i < n; ++i) std::memcpy(img.data() + h->inst[i].o_rad, rad[i].data(), rad[i].size() * sizeof(double));
+  }
+  if ((e = cudaMemsetAsync(h->pool, 0, (size_t)off * sizeof(double), h->stream)) ||
+      (e = cudaMemcpyAsync(h->pool, img.data(), img.size() * sizeof(double), cudaMemcpyHostToDevice, h->stream))) {
+    g_create_error = std::string("pool upload: ") + cudaGetErrorString(e);
+    pz_destroy(h);
+    return PZ_E_CUDA;
+  }
+  // work lists: radii and m, largest instances first
+  std::vector<int> order(n);
+  for (int i = 0; i < n; ++i) order[i] = i;
+  std::stable_sort(order.begin(), order.end(), [&](int a, int b) {
+    return (long long)h->inst[a].N * h->inst[a].M > (long long)h->inst[b].N * h->inst[b].M;
+  });
+  std::vector<PzItem> ritems, mitems;
+  for (int i : order) {
+    for (int r = 0; r < h->inst[i].N; ++r) ritems.push_back({i, r});
+    for (int m = 0; m < h->inst[i].M; ++m) mitems.push_back({i, m});
+  }
+  if ((e = cudaMalloc(&h->d_inst, n * sizeof(PzInst))) || (e = cudaMalloc(&h->d_state, n * sizeof(PzState))) ||
+      (e = cudaMalloc(&h->d_ritems, ritems.size() * sizeof(PzItem))) ||
+      (e = cudaMalloc(&h->d_mitems, mitems.size() * sizeof(PzItem)))) {
+    g_create_error = std::string("device allocation: ") + cudaGetErrorString(e);
+    pz_destroy(h);
+    return PZ_E_NOMEM;
+  }
+  cudaMemcpyAsync(h->d_inst, h->inst.data(), n * sizeof(PzInst), cudaMemcpyHostToDevice, h->stream);
+  cudaMemcpyAsync(h->d_ritems, ritems.data(), ritems.size() * sizeof(PzItem), cudaMemcpyHostToDevice, h->stream);
+  cudaMemcpyAsync(h->d_mitems, mitems.data(), mitems.size() * sizeof(PzItem), cudaMemcpyHostToDevice, h->stream);
+  cudaMemsetAsync(h->d_state, 0, n * sizeof(PzState), h->stream);
+  h->dev.inst = h->d_inst;
+  h->dev.state = h->d_state;
+  h->dev.pool = h->pool;
+  h->dev.ritems = h->d_ritems; h->dev.n_ritems = (int)ritems.size();
+  h->dev.mitems = h->d_mitems; h->dev.n_mitems = (int)mitems.size();
+  h->dev.n_inst = n;
+  h->dev.maxN = maxN; h->dev.maxP = maxP; h->dev.maxM = maxM;
+  if ((e = pz_launch_init_state(h->dev, -1, h->stream)) || (e = pz_launch_build_static(h->dev, h->stream)) ||
+      (e = cudaStreamSynchronize(h->stream))) {
+    g_create_error = std::string("static operators: ") + cudaGetErrorString(e);
+    pz_destroy(h);
+    return PZ_E_CUDA;
+  }
+  std::vector<PzState> st(n);
+  cudaMemcpy(st.data(), h->d_state, n * sizeof(PzState), cudaMemcpyDeviceToHost);
+  for (int i = 0; i < n; ++i)
+    if (st[i].status != 0) {
+      g_create_error = "instance " + std::to_string(i) + ": singular psi matrix";
+      pz_destroy(h);
+      return PZ_E_SINGULAR;
+    }
+  *out = h;
+  return PZ_OK;
+}
+
+namespace {
+
+// (n_m, n_r) n_m-fastest host array <-> device m-major field of instance i
+int upload_field(pz_handle* h, int i, int f, const double* src) {
+  const PzInst& I = h->inst[i];
+  const long long MN = (long long)I.M * I.N;
+  std::vector<double> buf(2 * MN, 0.0);
+  if (src)
+    for (int r = 0; r < I.N; ++r)
+      for (int m = 0; m < I.M; ++m) {
+        buf[2 * ((long long)m * I.N + r)] = src[2 * (m + (long long)r * I.M)];
+        buf[2 * ((long long)m * I.N + r) + 1] = src[2 * (m + (long long)r * I.M) + 1];
+      }
+  cudaError_t e = cudaMemcpyAsync(h->pool + I.o_fld + 2LL * f * MN, buf.data(), 2 * MN * sizeof(double),
+                                  cudaMemcpyHostToDevice, h->stream);
+  if (e) return cuda_fail(h, e, "set_state upload");
+  e = cudaStreamSynchronize(h->stream);   // buf is pageable and local
+  if (e) return cuda_fail(h, e, "set_state upload");
+  return PZ_OK;
+}
+
+int check_status(pz_handle* h) {
+  std::vector<PzState> st(h->n_inst);
+  cudaError_t e = cudaMemcpyAsync(st.data(), h->d_state, h->n_inst * sizeof(PzState), cudaMemcpyDeviceToHost, h->stream);
+  if (!e) e = cudaStreamSynchronize(h->stream);
+  if (e) return cuda_fail(h, e, "device state");
+  for (int i = 0; i < h->n_inst; ++i) {
+    const int s = st[i].status;
+    if (s == 0) continue;
+    const char* what = s == PZ_E_SINGULAR ? "singular matrix" : s == PZ_E_DT_TOO_SMALL ? "time step too small (dt < dtMin)"
+                       : s == PZ_E_NONFINITE ? "non-finite value in the state" : "device error";
+    return fail(h, s, "instance " + std::to_string(i) + ": " + what + " after step " + std::to_string(st[i].n_step));
+  }
+  return PZ_OK;
+}
+
+}  // namespace
+
+extern "C" int pz_set_state(pz_handle* h, int inst, const double* us, const double* up, const double* temp) {
+  if (!h) return fail(nullptr, PZ_E_ARG, "pz_set_state: null handle");
+  if (inst < 0 || inst >= h->n_inst) return fail(h, PZ_E_ARG, "pz_set_state: instance out of range");
+  int rc;
+  if ((rc = upload_field(h, inst, F_US, us)) || (rc = upload_field(h, inst, F_UP, up)) ||
+      (rc = upload_field(h, inst, F_TEMP, temp)))
+    return rc;
+  cudaError_t e;
+  if ((e = pz_launch_init_state(h->dev, inst, h->stream)) || (e = pz_launch_start(h->dev, inst, h->stream)) ||
+      (e = pz_launch_obs(h->dev, inst, h->stream)))
+    return cuda_fail(h, e, "pz_set_state");
+  return check_status(h);
+}
+
+extern "C" int pz_set_state_all(pz_handle* h, const double* us, const double* up, const double* temp) {
+  if (!h) return fail(nullptr, PZ_E_ARG, "pz_set_state_all: null handle");
+  long long o = 0;
+  for (int i = 0; i < h->n_inst; ++i) {
+    const PzInst& I = h->inst[i];
+    int rc;
+    if ((rc = upload_field(h, i, F_US, us ? us + o : nullptr)) || (rc = upload_field(h, i, F_UP, up ? up + o : nullptr)) ||
+        (rc = upload_field(h, i, F_TEMP, temp ? temp + o : nullptr)))
+      return rc;
+    o += 2LL * I.M * I.N;
+  }
+  cudaError_t e;
+  if ((e = pz_launch_init_state(h->dev, -1, h->stream)) || (e = pz_launch_start(h->dev, -1, h->stream)) ||
+      (e = pz_launch_obs(h->dev, -1, h->stream)))
+    return cuda_fail(h, e, "pz_set_state_all");
+  return check_status(h);
+}
+
+extern "C" int pz_step(pz_handle* h, int n_steps) {
+  if (!h) return fail(nullptr, PZ_E_ARG, "pz_step: null handle");
+  if (n_steps < 0) return fail(h, PZ_E_ARG, "pz_step: n_steps < 0");
+  cudaError_t e;
+  if (!h->graph) {
+    cudaGraph_t g;
+    if ((e = cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal))) return cuda_fail(h, e, "capture");
+    e = pz_launch_step(h->dev, h->stream);
+    cudaError_t e2 = cudaStreamEndCapture(h->stream, &g);
+    if (e || e2) return cuda_fail(h, e ? e : e2, "capture");
+    e = cudaGraphInstantiate(&h->graph, g, 0);
+    cudaGraphDestroy(g);
+    if (e) { h->graph = nullptr; return cuda_fail(h, e, "graph instantiate"); }
+  }
+  for (int s = 0; s < n_steps; ++s)
+    if ((e = cudaGraphLaunch(h->graph, h->stream))) return cuda_fail(h, e, "graph launch");
+  return PZ_OK;
+}
+
+extern "C" int pz_sync(pz_handle* h) {
+  if (!h) return fail(nullptr, PZ_E_ARG, "pz_sync: null handle");
+  cudaError_t e = cudaStreamSynchronize(h->stream);
+  if (e) return cuda_fail(h, e, "pz_sync");
+  return check_status(h);
+}
+
+extern "C" int pz_get_state(pz_handle* h, int inst, double* us, double* up, double* om, double* psi, double* temp,
+                            double* dtemp, double* time, double* dt) {
+  if (!h) return fail(nullptr, PZ_E_ARG, "pz_get_state: null handle");
+  if (inst < 0 || inst >= h->n_inst) return fail(h, PZ_E_ARG, "pz_get_state: instance out of range");
+  const PzInst& I = h->inst[inst];
+  const long long MN = (long long)I.M * I.N;
+  std::vector<double> buf(2 * MN * F_COUNT);
+  cudaError_t e = cudaMemcpyAsync(buf.data(), h->pool + I.o_fld, buf.size() * sizeof(double), cudaMemcpyDeviceToHost,
+                                  h->stream);
+  PzState st;
+  if (!e) e = cudaMemcpyAsync(&st, h->d_state + inst, sizeof(PzState), cudaMemcpyDeviceToHost, h->stream);
+  if (!e) e = cudaStreamSynchronize(h->stream);
+  if (e) return cuda_fail(h, e, "pz_get_state");
+  double* outs[6] = {us, up, om, psi, temp, dtemp};
+  const int fids[6] = {F_US, F_UP, F_OM, F_PSI, F_TEMP, F_DTEMP};
+  for (int k = 0; k < 6; ++k) {
+    if (!outs[k]) continue;
+    const double* src = buf.data() + 2 * MN * fids[k];
+    for (int r = 0; r < I.N; ++r)
+      for (int m = 0; m < I.M; ++m) {
+        outs[k][2 * (m + (long long)r * I.M)] = src[2 * ((long long)m * I.N + r)];
+        outs[k][2 * (m + (long long)r * I.M) + 1] = src[2 * ((long long)m * I.N + r) + 1];
+      }
+  }
+  if (time) *time = st.time;
+  if (dt) *dt = st.dt[0];
+  return st.status ? check_status(h) : PZ_OK;
+}
+
+extern "C" int pz_get_series(pz_handle* h, int inst, double* rows, int* n_rows) {
+  if (!h) return fail(nullptr, PZ_E_ARG, "pz_get_series: null handle");
+  if (inst < 0 || inst >= h->n_inst || !n_rows) return fail(h, PZ_E_ARG, "pz_get_series: bad arguments");
+  const PzInst& I = h->inst[inst];
+  PzState st;
+  std::vector<double> buf((size_t)PZ_SERIES_CAP * PZ_SERIES_COLS);
+  cudaError_t e = cudaMemcpyAsync(&st, h->d_state + inst, sizeof(PzState), cudaMemcpyDeviceToHost, h->stream);
+  if (!e) e = cudaMemcpyAsync(buf.data(), h->pool + I.o_series, buf.size() * sizeof(double), cudaMemcpyDeviceToHost,
+                              h->stream);
+  if (!e) e = cudaStreamSynchronize(h->stream);
+  if (e) return cuda_fail(h, e, "pz_get_series");
+  const int have = std::min(st.series_count, PZ_SERIES_CAP);
+  const int want = std::min(have, *n_rows);
+  for (int k = 0; k < want; ++k) {
+    const int idx = (st.series_count - want + k) % PZ_SERIES_CAP;
+    if (rows) std::memcpy(rows + (size_t)k * PZ_SERIES_COLS, buf.data() + (size_t)idx * PZ_SERIES_COLS,
+                          PZ_SERIES_COLS * sizeof(double));
+  }
+  *n_rows = want;
+  return PZ_OK;
+}
+
+extern "C" int pz_get_dims(pz_handle* h, int inst, int* n_r_max, int* n_m_max, int* n_phi_max) {
+  if (!h) return fail(nullptr, PZ_E_ARG, "pz_get_dims: null handle");
+  if (inst < 0 || inst >= h->n_inst) return fail(h, PZ_E_ARG, "pz_get_dims: instance out of range");
+  if (n_r_max) *n_r_max = h->inst[inst].N;
+  if (n_m_max) *n_m_max = h->inst[inst].M;
+  if (n_phi_max) *n_phi_max = h->inst[inst].P;
+  return PZ_OK;
+}
+
+extern "C" int pz_launches_per_step(pz_handle* h) {
+  (void)h;
+  return pz_step_launch_count();
+}
+
+extern "C" int pz_destroy(pz_handle* h) {
+  if (!h) return PZ_OK;
+  if (h->stream) cudaStreamSynchronize(h->stream);
+  if (h->graph) cudaGraphExecDestroy(h->graph);
+  cudaFree(h->pool);
+  cudaFree(h->d_inst);
+  cudaFree(h->d_state);
+  cudaFree(h->d_ritems);
+  cudaFree(h->d_mitems);
+  if (h->stream) cudaStreamDestroy(h->stream);
+  delete h;
+  return PZ_OK;
+}
+
+extern "C" const char* pz_last_error(pz_handle* h) {
+  return h ? h->err.c_str() : g_create_error.c_str();
+}

@@ -1,0 +1,132 @@
+// Internal data layout shared by the host setup (pz_host.cu) and the
+// device kernels (pz_kernels.cu).
+//
+// Everything of a handle lives in one FP64 device pool.  Offsets are counted
+// in doubles; complex arrays occupy two doubles per element and start on an
+// even offset (16-byte aligned).
+//
+// Spectral arrays are stored per m: element (m, r) of an instance's field is
+// at complex index m*N + r ("m-major": the N radial values of one azimuthal
+// wavenumber are contiguous), which is what the per-m solve kernel streams.
+// The per-radius phi-transform kernel gathers the same arrays with a stride
+// of N and scatters its outputs back: this is the on-device form of pizza's
+// m<->r transposes (src/mpi_transpose.f90:209-318).
+//
+// Matrices are stored column-major (Fortran order): A(i, j) at i + j*n, so
+// that thread i of a matrix-vector product reads consecutive addresses.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#define PZ_MAX_RADIX 8
+#define PZ_SERIES_CAP 1024
+
+// flag bits of PzInst::flags
+enum {
+  PZF_DIRECT   = 1,    // smat (not on the GPU yet)
+  PZF_BUO_IMP  = 2,    // implicit buoyancy (buo_term='IMPLICIT')
+  PZF_COR_IMP  = 4,    // implicit Coriolis (direct solve only)
+  PZF_EK_PUMP  = 8,    // Ekman pumping
+  PZF_NON_ROT  = 16,   // non-rotating
+  PZF_IMP_CALC = 32,   // scheme computes the implicit term each step
+};
+
+// radial vectors, each N doubles, at o_rad + RV_xxx*N
+enum {
+  RV_R = 0, RV_OR1, RV_OR2, RV_BETA, RV_DBETA, RV_EKPUMP, RV_EKP_UP, RV_EKP_US,
+  RV_EKP_DUSDP, RV_RGRAV, RV_TCOND, RV_DTCOND, RV_HEIGHT, RV_DELXR2, RV_DELXH2,
+  RV_WINT,    // rInt_R(f) = sum_r WINT[r] f[r]       (integration.f90:18-55)
+  RV_WSIMP,   // simps(f, theta) = sum_r WSIMP[r] f[r] (integration.f90:104-152)
+  RV_BCTOP,   // influence-matrix boundary row at r_cmb (update_psi_coll_dmat.f90:1302-1376)
+  RV_BCBOT,   // ... at r_icb
+  RV_COUNT
+};
+
+// per-N Chebyshev operator block at o_basis + BM_xxx*N*N (column-major)
+enum {
+  BM_C = 0,   // costf1: physical <-> Chebyshev (DCT-I, self-inverse), dct_fftw.f90:175-238
+  BM_D1C,     // Chebyshev coefficients -> physical d/dr       (get_dr, l_dct_in=.false.)
+  BM_D2C,     // Chebyshev coefficients -> physical d2/dr2
+  BM_D1P,     // physical -> physical d/dr                     (get_dr, l_dct_in=.true.)
+  BM_D2P,     // physical -> physical d2/dr2
+  BM_RMAT,    // T_k(x_i)    rMat of chebyshev.f90:281-383 (matrix builders)
+  BM_DRMAT,   // T_k'(x_i)   drMat
+  BM_D2RMAT,  // T_k''(x_i)  d2rMat
+  BM_COUNT
+};
+
+// complex fields per instance, each M*N complex, at o_fld + 2*F_xxx*M*N
+enum {
+  F_US = 0, F_UP, F_OM, F_PSI, F_TEMP, F_DTEMP, F_DVST, F_DVSOM, F_COUNT
+};
+
+struct PzInst {
+  int N, M, P, mmax, minc, n_max;
+  int scheme, nold, nimp, nexp;
+  int flags;
+  int nrad;                 // number of phi-FFT stages
+  int radix[PZ_MAX_RADIX];
+  double CorFac, BuoFac, TdiffFac, ViscFac, ek, tadvz, alpha;
+  double dtMax, dtMin, courfac, dt_fac, rnorm;
+  double r_cmb, r_icb;
+  double nu_vol_den;        // rInt_R(dtcond^2 height r)
+  double nu_int_fac;        // denominator of Nu_int
+  long long o_rad;          // RV_COUNT*N
+  long long o_basis;        // BM_COUNT*N*N (shared by instances of equal N)
+  long long o_tw;           // 2*P: exp(-2 pi i k/P), shared by equal P
+  long long o_gt;           // M*N*N   temperature operator per m
+  long long o_gom;          // M*N*N   vorticity operator per m (influence)
+  long long o_guphi;        // N*N     m=0 u_phi operator
+  long long o_gpsi;         // M*N*N   streamfunction operator per m (dt independent)
+  long long o_aux;          // 4*M*N: om2, om3, psi2, psi3 (Chebyshev space) ; then 4*M infl
+  long long o_fld;          // 2*F_COUNT*M*N
+  long long o_hist;         // 2*(2*(nold+nimp+nexp))*M*N
+  long long o_cfl;          // 2*N: dtr, dth
+  long long o_series;       // PZ_SERIES_CAP*16
+};
+
+struct PzState {
+  double time;
+  double dt[4];
+  double wimp[4], wimp_lin[5], wexp[4];
+  int n_step;
+  int lMatNext, lMat;
+  int bridge;               // start_from_another_scheme active this step
+  int l_calc_lin;           // implicit term computed this step
+  int b_old, b_impl, b_expl;          // ring base of logical slot 1 (next write)
+  int r_old, r_impl, r_expl;          // ring base used by this step's rhs
+  int status;               // 0 or a negative PZ_E_* code
+  int series_count;
+  int pad;
+};
+
+// history ring accessors: field f in {0: temperature, 1: psi/omega},
+// kind in {0: old, 1: impl, 2: expl}
+__host__ __device__ inline long long pz_hist_off(const PzInst& I, int f, int kind, int phys) {
+  long long mn2 = 2LL * I.M * I.N;
+  int per = I.nold + I.nimp + I.nexp;
+  int base = (kind == 0) ? 0 : (kind == 1 ? I.nold : I.nold + I.nimp);
+  return I.o_hist + mn2 * ((long long)f * per + base + phys);
+}
+
+struct PzItem { int inst; int idx; };   // (instance, r) or (instance, m index)
+
+// launchers (pz_kernels.cu)
+struct PzDev {
+  const PzInst* inst;       // device array
+  PzState* state;           // device array
+  double* pool;
+  const PzItem* ritems; int n_ritems;     // (inst, r)
+  const PzItem* mitems; int n_mitems;     // (inst, m index)
+  int n_inst;
+  int maxN, maxP, maxM;
+};
+
+// `only` selects one instance (>= 0) or all of them (-1).
+cudaError_t pz_launch_build_static(const PzDev& d, cudaStream_t s);
+cudaError_t pz_launch_init_state(const PzDev& d, int only, cudaStream_t s);
+cudaError_t pz_launch_start(const PzDev& d, int only, cudaStream_t s);
+cudaError_t pz_launch_step(const PzDev& d, cudaStream_t s);
+cudaError_t pz_launch_obs(const PzDev& d, int only, cudaStream_t s);
+cudaError_t pz_setup_kernels();
+int pz_step_launch_count();

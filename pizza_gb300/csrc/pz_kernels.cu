@@ -1,0 +1,1254 @@
+// Device kernels of the pizza time step (collocation, influence-matrix
+// solve, multistep IMEX schemes) for sm_103a.  FP64 throughout.
+//
+// One time step of every instance of the batch is five launches:
+//   k_rloop  (instance, r)  radial_loop: phi-FFTs, nonlinear products, CFL
+//   k_cfl    (instance)     dt_courant, dt roll, IMEX weights, rebuild flag
+//   k_build  (instance, m)  LU-equivalent operators when dt changed
+//   k_mloop  (instance, m)  finish_explicit_assembly + mloop solves
+//   k_obs    (instance)     time series (e_kin, e_kin_3D, heat)
+// Work lists of (instance, r) and (instance, m) items make one launch cover a
+// ragged batch of instances of different sizes.
+#include <cuda_runtime.h>
+#include <math.h>
+
+#include "pizza_gpu.h"
+#include "pz_internal.h"
+
+#define PZ_THREADS 128
+
+namespace {
+
+// ---------------------------------------------------------------------------
+// small helpers
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ double2 cadd(double2 a, double2 b) { return make_double2(a.x + b.x, a.y + b.y); }
+__device__ __forceinline__ double2 csub(double2 a, double2 b) { return make_double2(a.x - b.x, a.y - b.y); }
+__device__ __forceinline__ double2 cmul(double2 a, double2 b) {
+  return make_double2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+}
+__device__ __forceinline__ double2 cscale(double s, double2 a) { return make_double2(s * a.x, s * a.y); }
+// (i*m) * a
+__device__ __forceinline__ double2 cim(double m, double2 a) { return make_double2(-m * a.y, m * a.x); }
+
+__device__ __forceinline__ double warp_sum(double v) {
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+__device__ __forceinline__ double warp_max(double v) {
+  for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
+  return v;
+}
+__device__ __forceinline__ double warp_min(double v) {
+  for (int o = 16; o > 0; o >>= 1) v = fmin(v, __shfl_xor_sync(0xffffffffu, v, o));
+  return v;
+}
+
+// block-wide reductions; `red` holds >= 32 doubles of shared scratch
+__device__ double block_sum(double v, double* red) {
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
+  v = warp_sum(v);
+  __syncthreads();
+  if (lane == 0) red[wid] = v;
+  __syncthreads();
+  double t = (threadIdx.x < nw) ? red[threadIdx.x] : 0.0;
+  if (wid == 0) t = warp_sum(t);
+  if (threadIdx.x == 0) red[0] = t;
+  __syncthreads();
+  t = red[0];
+  __syncthreads();
+  return t;
+}
+__device__ double block_max(double v, double* red) {
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
+  v = warp_max(v);
+  __syncthreads();
+  if (lane == 0) red[wid] = v;
+  __syncthreads();
+  double t = (threadIdx.x < nw) ? red[threadIdx.x] : -1.0e300;
+  if (wid == 0) t = warp_max(t);
+  if (threadIdx.x == 0) red[0] = t;
+  __syncthreads();
+  t = red[0];
+  __syncthreads();
+  return t;
+}
+
+// Instance view: pointers into the pool.
+struct View {
+  const PzInst* I;
+  double* pool;
+  __device__ const double* rad(int k) const { return pool + I->o_rad + (long long)k * I->N; }
+  __device__ const double* basis(int k) const { return pool + I->o_basis + (long long)k * I->N * I->N; }
+  __device__ double2* fld(int f, int mi) const {
+    return reinterpret_cast<double2*>(pool + I->o_fld) + ((long long)f * I->M + mi) * I->N;
+  }
+  __device__ double2* hist(int f, int kind, int phys, int mi) const {
+    return reinterpret_cast<double2*>(pool + pz_hist_off(*I, f, kind, phys)) + (long long)mi * I->N;
+  }
+};
+
+// ---------------------------------------------------------------------------
+// dense operators: y = A x with A column-major (nr x nc) real, x complex
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ void mv1(const double* __restrict__ A, int nr, int nc,
+                                    const double2* __restrict__ x, double2* __restrict__ y) {
+  for (int i = threadIdx.x; i < nr; i += blockDim.x) {
+    double re = 0.0, im = 0.0;
+    const double* a = A + i;
+#pragma unroll 4
+    for (int j = 0; j < nc; ++j) {
+      const double aij = __ldg(a + (long long)j * nr);
+      const double2 v = x[j];
+      re = fma(aij, v.x, re);
+      im = fma(aij, v.y, im);
+    }
+    y[i] = make_double2(re, im);
+  }
+}
+__device__ __forceinline__ void mv2(const double* __restrict__ A, const double* __restrict__ B, int n,
+                                    const double2* __restrict__ x, double2* __restrict__ ya,
+                                    double2* __restrict__ yb) {
+  for (int i = threadIdx.x; i < n; i += blockDim.x) {
+    double ar = 0.0, ai = 0.0, br = 0.0, bi = 0.0;
+#pragma unroll 4
+    for (int j = 0; j < n; ++j) {
+      const double a = __ldg(A + i + (long long)j * n);
+      const double b = __ldg(B + i + (long long)j * n);
+      const double2 v = x[j];
+      ar = fma(a, v.x, ar); ai = fma(a, v.y, ai);
+      br = fma(b, v.x, br); bi = fma(b, v.y, bi);
+    }
+    ya[i] = make_double2(ar, ai);
+    yb[i] = make_double2(br, bi);
+  }
+}
+__device__ __forceinline__ void mv3(const double* __restrict__ A, const double* __restrict__ B,
+                                    const double* __restrict__ C, int n, const double2* __restrict__ x,
+                                    double2* __restrict__ ya, double2* __restrict__ yb,
+                                    double2* __restrict__ yc) {
+  for (int i = threadIdx.x; i < n; i += blockDim.x) {
+    double ar = 0.0, ai = 0.0, br = 0.0, bi = 0.0, cr = 0.0, ci = 0.0;
+#pragma unroll 2
+    for (int j = 0; j < n; ++j) {
+      const double a = __ldg(A + i + (long long)j * n);
+      const double b = __ldg(B + i + (long long)j * n);
+      const double c = __ldg(C + i + (long long)j * n);
+      const double2 v = x[j];
+      ar = fma(a, v.x, ar); ai = fma(a, v.y, ai);
+      br = fma(b, v.x, br); bi = fma(b, v.y, bi);
+      cr = fma(c, v.x, cr); ci = fma(c, v.y, ci);
+    }
+    ya[i] = make_double2(ar, ai);
+    yb[i] = make_double2(br, bi);
+    yc[i] = make_double2(cr, ci);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// IMEX weights of the multistep family (src/multistep_schemes.f90:137-306)
+// ---------------------------------------------------------------------------
+__device__ bool set_weights(const PzInst& I, PzState& S) {
+  const double wimp_old = S.wimp_lin[0];
+  const double* dt = S.dt;
+  const double one = 1.0, half = 0.5, two = 2.0;
+  switch (I.scheme) {
+    case PZ_CNAB2:
+      S.wimp[0] = one;
+      S.wimp_lin[0] = I.alpha * dt[0];
+      S.wimp_lin[1] = (1.0 - I.alpha) * dt[0];
+      S.wexp[0] = (one + half * dt[0] / dt[1]) * dt[0];
+      S.wexp[1] = -half * dt[0] * dt[0] / dt[1];
+      break;
+    case PZ_CNLF: {
+      const double delta = dt[0] / dt[1];
+      S.wimp[0] = (one - delta) * (one + delta);
+      S.wimp[1] = delta * delta;
+      S.wimp_lin[0] = half * (one + delta) / delta * dt[0];
+      S.wimp_lin[1] = half * (one + delta) * (delta - one) / delta * dt[0];
+      S.wimp_lin[2] = half * (one + delta) * dt[0];
+      S.wexp[0] = (one + delta) * dt[0];
+      S.wexp[1] = 0.0;
+    } break;
+    case PZ_MODCNAB: {
+      const double delta = dt[0] / dt[1];
+      S.wimp[0] = one;
+      S.wimp[1] = 0.0;
+      S.wimp_lin[0] = (half + 1.0 / delta / 16.0) * dt[0];
+      S.wimp_lin[1] = (7.0 / 16.0 - 1.0 / delta / 16.0) * dt[0];
+      S.wimp_lin[2] = 1.0 / 16.0 * dt[0];
+      S.wexp[0] = (one + half * delta) * dt[0];
+      S.wexp[1] = -half * delta * dt[0];
+    } break;
+    case PZ_SBDF2: {
+      const double delta = dt[0] / dt[1];
+      S.wimp_lin[0] = (one + delta) / (one + two * delta) * dt[0];
+      S.wimp_lin[1] = 0.0;
+      S.wimp[0] = (one + delta) * (one + delta) / (one + two * delta);
+      S.wimp[1] = -delta * delta / (one + two * delta);
+      S.wexp[0] = (one + delta) * (one + delta) * dt[0] / (one + two * delta);
+      S.wexp[1] = -delta * (one + delta) * dt[0] / (one + two * delta);
+    } break;
+    case PZ_SBDF3: {
+      const double dn = dt[1] / dt[0], dn1 = dt[2] / dt[0];
+      const double a0 = one + one / (one + dn) + one / (one + dn + dn1);
+      const double a1 = (one + dn) * (one + dn + dn1) / (dn * (dn + dn1));
+      const double a2 = -(one + dn + dn1) / (dn * dn1 * (one + dn));
+      const double a3 = (one + dn) / (dn1 * (dn + dn1) * (one + dn + dn1));
+      const double b0 = (one + dn) * (one + dn + dn1) / (dn * (dn + dn1));
+      const double b1 = -(one + dn + dn1) / (dn * dn1);
+      const double b2 = (one + dn) / (dn1 * (dn + dn1));
+      S.wimp_lin[0] = one / a0 * dt[0];
+      S.wimp_lin[1] = 0.0;
+      S.wimp[0] = a1 / a0; S.wimp[1] = a2 / a0; S.wimp[2] = a3 / a0;
+      S.wexp[0] = b0 / a0 * dt[0]; S.wexp[1] = b1 / a0 * dt[0]; S.wexp[2] = b2 / a0 * dt[0];
+    } break;
+    case PZ_TVB33: {
+      const double gam = (2619.0 - sqrt(5995281.0)) / 345.0;
+      const double theta = (3525.0 * gam * gam - 3118.0 * gam - 5084.0) / 5468.0;
+      const double c = (2178.0 * theta - 959.0 * gam * gam + 130.0 * gam + 726.0) / 4096.0;
+      const double dn = dt[0] / dt[1], dn1 = dt[1] / dt[2];
+      const double a3 = -pow(dn1, 3) * dn * dn * (3.0 * gam * gam * dn + two * gam * (one - dn) - one) /
+                        (one + dn1) / (one + dn1 * (one + dn));
+      const double a2 = -dn * dn * (gam * dn * dn1 * (two - 3.0 * gam) + (one - two * gam) * (one + dn1)) / (one + dn);
+      const double a1 = -(dn1 * (one + gam * dn) * (1 + dn * (3.0 * gam - two)) + dn * (two * gam - one) + one) /
+                            (one + dn1) - theta;
+      const double a0 = theta + (one + two * gam * dn + dn1 * (one + gam * dn) * (one + 3.0 * gam * dn)) /
+                                    (one + dn) / (one + dn1 * (one + dn));
+      const double b2 = dn1 * dn1 * dn * (6.0 * gam * (one + gam * dn) + theta * (3.0 + two * dn)) / (6.0 * (one + dn1));
+      const double b1 = -gam * dn * (one + dn1 * (one + gam * dn)) - theta / 6.0 * dn * (3.0 + dn1 * (3.0 + two * dn));
+      const double b0 = (one + gam * dn) * (one + dn1 * (one + gam * dn)) / (one + dn1) +
+                        theta * (one + 0.5 * dn + dn1 * dn * (3.0 + two * dn) / (6.0 * (one + dn1)));
+      const double c3 = theta * dn1 * dn1 * dn * (3.0 + two * dn) / (6.0 * (one + dn1)) - c;
+      const double c2 = (c * (one + dn1) * (one + dn1 * (one + dn)) - dn1 * dn1 * dn * dn * gam * (one - gam)) /
+                            (dn1 * dn1 * (one + dn)) - theta * dn * (3.0 + dn1 * (3.0 + 2.0 * dn)) / 6.0;
+      const double c1 = (dn1 * dn1 * dn * (one - gam) * (one + gam * dn) - c * (one + dn1 * (one + dn))) / (dn1 * dn1) / dn +
+                        theta * (one + 0.5 * dn + dn1 * dn * (3.0 + two * dn) / (6.0 * (one + dn1)));
+      const double c0 = (dn1 * dn1 * dn * gam * (one + gam * dn) + c * (one + dn1)) / (dn1 * dn1 * dn * (one + dn));
+      S.wimp_lin[0] = c0 / a0 * dt[0]; S.wimp_lin[1] = c1 / a0 * dt[0];
+      S.wimp_lin[2] = c2 / a0 * dt[0]; S.wimp_lin[3] = c3 / a0 * dt[0];
+      S.wimp[0] = -a1 / a0; S.wimp[1] = -a2 / a0; S.wimp[2] = -a3 / a0;
+      S.wexp[0] = b0 / a0 * dt[0]; S.wexp[1] = b1 / a0 * dt[0]; S.wexp[2] = b2 / a0 * dt[0];
+    } break;
+    case PZ_SBDF4: {
+      const double dn = dt[0] / dt[1], dn1 = dt[1] / dt[2], dn2 = dt[2] / dt[3];
+      const double c1 = one + dn2 * (one + dn1);
+      const double c2 = one + dn1 * (one + dn);
+      const double c3 = one + dn2 * c2;
+      const double a4 = (one + dn) / (one + dn2) * c2 / c1 / c3 * (pow(dn2, 4) * pow(dn1, 3) * dn * dn);
+      const double a3 = -pow(dn1, 3) * dn * dn * (one + dn) / (one + dn1) * c3 / c2;
+      const double a2 = dn * (dn / (one + dn) + dn1 * dn * (c3 + dn2) / (one + dn2));
+      const double a1 = -one - dn * (one + dn1 * (one + dn) * (one + dn2 * c2 / c1) / (one + dn1));
+      const double a0 = one + dn / (one + dn) + dn1 * dn / c2 + dn2 * dn1 * dn / c3;
+      const double b3 = -pow(dn2, 3) * dn1 * dn1 * dn * (one + dn) / (one + dn2) * c2 / c1;
+      const double b2 = dn1 * dn1 * dn * (one + dn) / (one + dn1) * c3;
+      const double b1 = -c2 * c3 * dn / (one + dn2);
+      const double b0 = dn1 * (one + dn) / (one + dn1) * ((one + dn) * (c3 + dn2) + (one + dn2) / dn1) / c1;
+      S.wimp_lin[0] = one / a0 * dt[0];
+      S.wimp_lin[1] = 0.0;
+      S.wimp[0] = -a1 / a0; S.wimp[1] = -a2 / a0; S.wimp[2] = -a3 / a0; S.wimp[3] = -a4 / a0;
+      S.wexp[0] = b0 / a0 * dt[0]; S.wexp[1] = b1 / a0 * dt[0];
+      S.wexp[2] = b2 / a0 * dt[0]; S.wexp[3] = b3 / a0 * dt[0];
+    } break;
+    default:
+      break;
+  }
+  return S.wimp_lin[0] != wimp_old;
+}
+
+// bridge_with_cnab2 (multistep_schemes.f90:500-522)
+__device__ void bridge_with_cnab2(const PzInst& I, PzState& S) {
+  PzInst J = I;
+  J.scheme = PZ_CNAB2;
+  set_weights(J, S);
+  for (int k = 1; k < I.nold; ++k) S.wimp[k] = 0.0;
+  for (int k = 2; k < I.nimp + 1; ++k) S.wimp_lin[k] = 0.0;
+  for (int k = 2; k < I.nexp; ++k) S.wexp[k] = 0.0;
+}
+
+// ---------------------------------------------------------------------------
+// phi-FFT: mixed-radix Stockham autosort on nb transforms in shared memory
+// ---------------------------------------------------------------------------
+// One stage of radix R with running product p (product of earlier radices).
+// tw[k] = exp(-2 pi i k / P); sgn = +1 selects the backward transform.
+__device__ void fft_stage(const double2* __restrict__ x, double2* __restrict__ y, int P, int R, int p,
+                          const double2* __restrict__ tw, int nb, bool backward) {
+  const int T = P / R;
+  const int tstep = P / (p * R);
+  const int rstep = P / R;
+  for (int w = threadIdx.x; w < nb * T; w += blockDim.x) {
+    const int b = w / T, i = w - b * T;
+    const int k = i % p;
+    const double2* xb = x + b * P;
+    double2* yb = y + b * P;
+    double2 u[PZ_MAX_RADIX];
+#pragma unroll
+    for (int q = 0; q < PZ_MAX_RADIX; ++q) {
+      if (q < R) {
+        double2 t = tw[(q * k * tstep) % P];
+        if (backward) t.y = -t.y;
+        u[q] = cmul(xb[i + q * T], t);
+      }
+    }
+    const int base = (i - k) * R + k;
+    if (R == 2) {
+      yb[base] = cadd(u[0], u[1]);
+      yb[base + p] = csub(u[0], u[1]);
+    } else if (R == 4) {
+      const double2 s02 = cadd(u[0], u[2]), d02 = csub(u[0], u[2]);
+      const double2 s13 = cadd(u[1], u[3]), d13 = csub(u[1], u[3]);
+      // forward: W = -i ; backward: W = +i
+      const double2 jd13 = backward ? make_double2(-d13.y, d13.x) : make_double2(d13.y, -d13.x);
+      yb[base] = cadd(s02, s13);
+      yb[base + p] = cadd(d02, jd13);
+      yb[base + 2 * p] = csub(s02, s13);
+      yb[base + 3 * p] = csub(d02, jd13);
+    } else {
+      for (int s = 0; s < R; ++s) {
+        double2 acc = u[0];
+        for (int q = 1; q < R; ++q) {
+          double2 t = tw[((s * q) % R) * rstep];
+          if (backward) t.y = -t.y;
+          acc = cadd(acc, cmul(u[q], t));
+        }
+        yb[base + s * p] = acc;
+      }
+    }
+  }
+}
+
+// Full transform; returns the buffer holding the result (a or b).
+__device__ double2* fft_run(double2* a, double2* b, const PzInst& I, const double2* tw, int nb, bool backward) {
+  int p = 1;
+  double2* src = a;
+  double2* dst = b;
+  for (int s = 0; s < I.nrad; ++s) {
+    const int R = I.radix[s];
+    fft_stage(src, dst, I.P, R, p, tw, nb, backward);
+    __syncthreads();
+    p *= R;
+    double2* t = src; src = dst; dst = t;
+  }
+  return src;
+}
+
+// ---------------------------------------------------------------------------
+// k_rloop: radial_loop for one radius of one instance
+// (src/radial_loop.f90:231-394 with ifft/fft of src/fft_fftw.f90:44-90)
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(PZ_THREADS) k_rloop(PzDev d) {
+  extern __shared__ double2 sh[];
+  __shared__ double red[32];
+  const PzItem it = d.ritems[blockIdx.x];
+  const PzInst& I = d.inst[it.inst];
+  PzState& S = d.state[it.inst];
+  if (S.status != 0) return;
+  const View V{&I, d.pool};
+  const int N = I.N, M = I.M, P = I.P, r = it.idx;
+  double2* tw = sh;              // P
+  double2* za = sh + P;          // 2P: z1 | z2
+  double2* zb = sh + 3 * P;      // 2P
+  const double2* gtw = reinterpret_cast<const double2*>(d.pool + I.o_tw);
+  for (int k = threadIdx.x; k < P; k += blockDim.x) tw[k] = gtw[k];
+  for (int k = threadIdx.x; k < 2 * P; k += blockDim.x) za[k] = make_double2(0.0, 0.0);
+  __syncthreads();
+
+  const double rr = V.rad(RV_R)[r];
+  const double or1 = V.rad(RV_OR1)[r];
+  const double beta = V.rad(RV_BETA)[r];
+  const double ekpump = V.rad(RV_EKPUMP)[r];
+  const double2* us = V.fld(F_US, 0);
+  const double2* up = V.fld(F_UP, 0);
+  const double2* om = V.fld(F_OM, 0);
+  const double2* T = V.fld(F_TEMP, 0);
+  // Hermitian spectra of the pairs (us + i up) and (om + i T); Reynolds stress
+  double usom = 0.0;
+  for (int m = threadIdx.x; m < M; m += blockDim.x) {
+    double2 a = us[(long long)m * N + r], b = up[(long long)m * N + r];
+    double2 c = om[(long long)m * N + r], e = T[(long long)m * N + r];
+    if (m == 0) {
+      const double usf = 0.5 * I.ek * I.CorFac * ekpump * b.x;  // us_fluct(m=0)
+      usom += usf * c.x;
+      a.y = 0.0; b.y = 0.0; c.y = 0.0; e.y = 0.0;   // c2r ignores Im of the DC term
+    } else {
+      usom += 2.0 * (a.x * c.x + a.y * c.y);
+    }
+    const int mm = m;   // FFT index n_m (fft_fftw.f90:55-62)
+    za[mm] = make_double2(a.x - b.y, a.y + b.x);
+    za[P + mm] = make_double2(c.x - e.y, c.y + e.x);
+    if (mm > 0) {
+      za[P - mm] = make_double2(a.x + b.y, -a.y + b.x);
+      za[2 * P - mm] = make_double2(c.x + e.y, -c.y + e.x);
+    }
+  }
+  usom = block_sum(usom, red);
+  double2* g = fft_run(za, zb, I, tw, 2, true);   // g[0..P): us + i up, g[P..2P): om + i T
+  double2* h = (g == za) ? zb : za;
+  // CFL and products
+  double vr = 0.0, vh = 0.0;
+  for (int j = threadIdx.x; j < P; j += blockDim.x) {
+    const double2 z1 = g[j], z2 = g[P + j];
+    const double usg = z1.x, upg = z1.y, omg = z2.x, Tg = z2.y;
+    vr = fmax(vr, usg * usg);
+    vh = fmax(vh, upg * upg);
+    h[j] = make_double2(rr * usg * Tg, upg * Tg);            // usT + i upT
+    h[P + j] = make_double2(rr * usg * omg, upg * omg);      // usOm + i upOm
+  }
+  vr = block_max(vr, red);
+  vh = block_max(vh, red);
+  if (threadIdx.x == 0) {
+    // courant (src/courant.f90:41-76)
+    double* cfl = d.pool + I.o_cfl;
+    const double vr2 = I.courfac * I.courfac * vr, vh2 = I.courfac * I.courfac * vh;
+    double dtr = 1.0e10, dth = 1.0e10;
+    if (vr2 != 0.0) dtr = fmin(dtr, sqrt(V.rad(RV_DELXR2)[r] / vr2));
+    if (vh2 != 0.0) dth = fmin(dth, sqrt(V.rad(RV_DELXH2)[r] / vh2));
+    cfl[r] = dtr;
+    cfl[N + r] = dth;
+  }
+  __syncthreads();
+  double2* f = fft_run(h, g, I, tw, 2, false);
+  double2* eT = V.hist(0, 2, S.b_expl, 0);
+  double2* eP = V.hist(1, 2, S.b_expl, 0);
+  double2* dVsT = V.fld(F_DVST, 0);
+  double2* dVsOm = V.fld(F_DVSOM, 0);
+  const double tfac = (1.0 - I.tadvz) * beta * or1;
+  for (int m = threadIdx.x; m < M; m += blockDim.x) {
+    const int mm = m;
+    const int mc = (P - mm) % P;
+    const double dm = (double)(m * I.minc);
+    // split the two real transforms packed in one complex FFT
+    const double2 Z = f[mm], Zc = f[mc];
+    const double2 A = make_double2(0.5 * (Z.x + Zc.x), 0.5 * (Z.y - Zc.y));   // FFT(usT)
+    const double2 B = make_double2(0.5 * (Z.y + Zc.y), -0.5 * (Z.x - Zc.x));  // FFT(upT)
+    const double2 Y = f[P + mm], Yc = f[P + mc];
+    const double2 C = make_double2(0.5 * (Y.x + Yc.x), 0.5 * (Y.y - Yc.y));   // FFT(usOm)
+    const double2 D = make_double2(0.5 * (Y.y + Yc.y), -0.5 * (Y.x - Yc.x));  // FFT(upOm)
+    const double2 vsT = make_double2(A.x / (double)P, A.y / (double)P);
+    const double2 upT = make_double2(B.x / (double)P, B.y / (double)P);
+    const double2 vsOm = make_double2(C.x / (double)P, C.y / (double)P);
+    const double2 upOm = make_double2(D.x / (double)P, D.y / (double)P);
+    const double t = or1 * dm;
+    const double2 dtdt = make_double2(t * upT.y - tfac * vsT.x, -t * upT.x - tfac * vsT.y);
+    const double2 dpdt = (m == 0) ? make_double2(-usom, 0.0) : make_double2(t * upOm.y, -t * upOm.x);
+    const long long o = (long long)m * N + r;
+    eT[o] = dtdt;
+    dVsT[o] = vsT;
+    eP[o] = dpdt;
+    dVsOm[o] = vsOm;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// k_cfl: dt_courant, set_dt_array, set_weights, lMat, bridge, ring bases
+// (src/courant.f90:78-167, src/step_time.f90:281-329)
+// ---------------------------------------------------------------------------
+__global__ void k_cfl(PzDev d) {
+  const int inst = blockIdx.x;
+  const PzInst& I = d.inst[inst];
+  PzState& S = d.state[inst];
+  if (S.status != 0) return;
+  const double* cfl = d.pool + I.o_cfl;
+  double dtr = 1000.0 * I.dtMax, dth = dtr;
+  for (int r = threadIdx.x; r < I.N; r += 32) {
+    dtr = fmin(dtr, cfl[r]);
+    dth = fmin(dth, cfl[I.N + r]);
+  }
+  dtr = warp_min(dtr);
+  dth = warp_min(dth);
+  if (threadIdx.x != 0) return;
+  const double dt = S.dt[0];
+  const double dt_rh = fmin(dtr, dth);
+  const double dt_2 = fmin(0.5 * (1.0 / I.dt_fac + 1.0) * dt_rh, I.dtMax);
+  bool l_new_dt;
+  double dt_new;
+  if (dt > I.dtMax) { l_new_dt = true; dt_new = I.dtMax; }
+  else if (dt > dt_rh) { l_new_dt = true; dt_new = dt_2; }
+  else if (I.dt_fac * dt < dt_rh && dt < I.dtMax) { l_new_dt = true; dt_new = dt_2; }
+  else { l_new_dt = false; dt_new = dt; }
+  for (int k = I.nexp - 1; k > 0; --k) S.dt[k] = S.dt[k - 1];
+  S.dt[0] = dt_new;
+  if (dt_new < I.dtMin) { S.status = PZ_E_DT_TOO_SMALL; return; }
+  if (set_weights(I, S)) S.lMatNext = 1;
+  S.time = S.time + S.dt[0];
+  S.lMat = (S.lMatNext || l_new_dt) ? 1 : 0;
+  S.lMatNext = 0;
+  S.n_step += 1;
+  S.bridge = (I.scheme != PZ_CNAB2 && S.n_step <= I.nold - 1) ? 1 : 0;
+  if (S.bridge) bridge_with_cnab2(I, S);
+  S.l_calc_lin = (I.flags & PZF_IMP_CALC) ? 1 : 0;
+  // rotate_imex on rings: this step reads slots from r_*, writes logical slot 1 at b_*
+  S.r_old = S.b_old; S.r_impl = S.b_impl; S.r_expl = S.b_expl;
+  S.b_old = (S.b_old + I.nold - 1) % I.nold;
+  S.b_impl = (S.b_impl + I.nimp - 1) % I.nimp;
+  S.b_expl = (S.b_expl + I.nexp - 1) % I.nexp;
+}
+
+// ---------------------------------------------------------------------------
+// Gauss-Jordan inversion with partial pivoting of a row-major n x n matrix in
+// shared memory (in place).  Returns 0, or -1 on a zero pivot.
+// ---------------------------------------------------------------------------
+__device__ int gj_invert(double* A, int n, int* piv, double* colk, double* red, int* redi) {
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
+  for (int k = 0; k < n; ++k) {
+    // pivot: first index of max |A(i,k)|, i >= k (idamax semantics)
+    double best = -1.0;
+    int bi = n;
+    for (int i = k + threadIdx.x; i < n; i += blockDim.x) {
+      const double v = fabs(A[i * n + k]);
+      if (v > best) { best = v; bi = i; }
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+      const double ov = __shfl_xor_sync(0xffffffffu, best, o);
+      const int oi = __shfl_xor_sync(0xffffffffu, bi, o);
+      if (ov > best || (ov == best && oi < bi)) { best = ov; bi = oi; }
+    }
+    if (lane == 0) { red[wid] = best; redi[wid] = bi; }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      double b = red[0];
+      int ib = redi[0];
+      for (int w = 1; w < nw; ++w)
+        if (red[w] > b || (red[w] == b && redi[w] < ib)) { b = red[w]; ib = redi[w]; }
+      piv[k] = ib;
+    }
+    __syncthreads();
+    const int p = piv[k];
+    if (p >= n || A[p * n + k] == 0.0) return -1;
+    if (p != k) {
+      for (int j = threadIdx.x; j < n; j += blockDim.x) {
+        const double t = A[k * n + j]; A[k * n + j] = A[p * n + j]; A[p * n + j] = t;
+      }
+      __syncthreads();
+    }
+    const double pv = A[k * n + k];
+    for (int i = threadIdx.x; i < n; i += blockDim.x) colk[i] = A[i * n + k];
+    __syncthreads();
+    for (int j = threadIdx.x; j < n; j += blockDim.x) A[k * n + j] = (j == k ? 1.0 : A[k * n + j]) / pv;
+    __syncthreads();
+    for (int idx = threadIdx.x; idx < n * n; idx += blockDim.x) {
+      const int i = idx / n, j = idx - i * n;
+      if (i != k) A[idx] = (j == k ? 0.0 : A[idx]) - colk[i] * A[k * n + j];
+    }
+    __syncthreads();
+  }
+  for (int k = n - 1; k >= 0; --k) {
+    const int p = piv[k];
+    if (p != k) {
+      for (int i = threadIdx.x; i < n; i += blockDim.x) {
+        const double t = A[i * n + k]; A[i * n + k] = A[i * n + p]; A[i * n + p] = t;
+      }
+    }
+    __syncthreads();
+  }
+  return 0;
+}
+
+// Boundary rows and the Chebyshev boundary factor of the collocation builders.
+// Row i of the matrix is written to A (row-major); `rowfn` gives interior rows.
+struct BuildCtx {
+  const PzInst* I;
+  const double* rM; const double* drM; const double* d2rM;   // column-major N x N
+  int N;
+  __device__ double rm(int i, int k) const { return rM[i + (long long)k * N]; }
+  __device__ double drm(int i, int k) const { return drM[i + (long long)k * N]; }
+  __device__ double d2rm(int i, int k) const { return d2rM[i + (long long)k * N]; }
+};
+
+// Write G (= X in shared row-major, scaled) to global column-major, rows >=
+// n_max zeroed (dealiasing): G(i,j) = rs[i] * X(i,j) * cs[j].
+__device__ void store_op(double* G, const double* X, int n, int n_max, const double* rs, const double* cs) {
+  for (int idx = threadIdx.x; idx < n * n; idx += blockDim.x) {
+    const int j = idx / n, i = idx - j * n;
+    double v = 0.0;
+    if (i < n_max) {
+      v = X[i * n + j];
+      if (rs) v = rs[i] * v;
+      if (cs) v = v * cs[j];
+    }
+    G[idx] = v;
+  }
+}
+
+// Row and column equilibration of get_omMat/get_psiMat
+// (update_psi_coll_dmat.f90:881-897): f1 = 1/max|row|, then f2 = 1/max|col|.
+__device__ void equilibrate(double* A, int n, double* f1, double* f2, bool cols) {
+  for (int i = threadIdx.x; i < n; i += blockDim.x) {
+    double mx = 0.0;
+    for (int j = 0; j < n; ++j) mx = fmax(mx, fabs(A[i * n + j]));
+    f1[i] = 1.0 / mx;
+  }
+  __syncthreads();
+  for (int idx = threadIdx.x; idx < n * n; idx += blockDim.x) A[idx] *= f1[idx / n];
+  __syncthreads();
+  if (!cols) return;
+  for (int j = threadIdx.x; j < n; j += blockDim.x) {
+    double mx = 0.0;
+    for (int i = 0; i < n; ++i) mx = fmax(mx, fabs(A[i * n + j]));
+    f2[j] = 1.0 / mx;
+  }
+  __syncthreads();
+  for (int idx = threadIdx.x; idx < n * n; idx += blockDim.x) A[idx] *= f2[idx - (idx / n) * n];
+  __syncthreads();
+}
+
+// kind: 0 temperature (get_tempMat), 1 omega (get_omMat), 2 psi (get_psiMat),
+// 3 uphi (get_uphiMat).  Fills A (row-major) before scaling.
+__device__ void fill_matrix(double* A, const BuildCtx& B, const View& V, int kind, int m, double wlin) {
+  const PzInst& I = *B.I;
+  const int n = B.N, n_max = I.n_max;
+  const double rn = I.rnorm, dm2 = (double)m * (double)m;
+  const double* or1 = V.rad(RV_OR1);
+  const double* or2 = V.rad(RV_OR2);
+  const double* beta = V.rad(RV_BETA);
+  const double* dbeta = V.rad(RV_DBETA);
+  const double* ekp = V.rad(RV_EKPUMP);
+  for (int idx = threadIdx.x; idx < n * n; idx += blockDim.x) {
+    const int i = idx / n, k = idx - i * n;
+    double v;
+    if (i == 0 || i == n - 1) {
+      if (k >= n_max) {
+        v = 0.0;
+      } else {
+        // fixed temperature (ktopt=kbott=1), non-penetration, rigid u_phi
+        // (ktopv=kbotv=2): rnorm*rMat on both boundary rows
+        v = rn * B.rm(i, k);
+      }
+    } else {
+      const double r0 = B.rm(i, k), r1 = B.drm(i, k), r2 = B.d2rm(i, k);
+      if (kind == 0) {
+        v = rn * (r0 - wlin * I.TdiffFac * (r2 + or1[i] * r1 - dm2 * or2[i] * r0));
+      } else if (kind == 1) {
+        v = rn * (r0 - wlin * I.ViscFac * (r2 + or1[i] * r1 - dm2 * or2[i] * r0));
+      } else if (kind == 2) {
+        v = rn * (r2 + (or1[i] + beta[i]) * r1 + (or1[i] * beta[i] + dbeta[i] - dm2 * or2[i]) * r0);
+      } else {
+        v = rn * (r0 - wlin * (I.ViscFac * (r2 + or1[i] * r1 - or2[i] * r0) - I.CorFac * ekp[i] * r0));
+      }
+    }
+    if (k == 0 || k == n - 1) v = 0.5 * v;   // boundary_fac
+    A[idx] = v;
+  }
+  __syncthreads();
+}
+
+struct BuildSmem {
+  double* A; double* f1; double* f2; double* colk; double* red; int* redi; int* piv;
+  double2* va; double2* vb;
+};
+// shared-memory layout of the builders, in doubles; see build_smem_bytes()
+__device__ BuildSmem build_smem(int n) {
+  extern __shared__ double shb[];
+  BuildSmem s;
+  long long off = 0;
+  s.A = shb + off; off += (long long)n * n;
+  s.f1 = shb + off; off += n;
+  s.f2 = shb + off; off += n;
+  s.colk = shb + off; off += n;
+  s.red = shb + off; off += 32;
+  s.redi = reinterpret_cast<int*>(shb + off); off += 16;
+  s.piv = reinterpret_cast<int*>(shb + off); off += (n + 1) / 2;
+  off = (off + 1) & ~1LL;
+  s.va = reinterpret_cast<double2*>(shb + off); off += 2 * n;
+  s.vb = reinterpret_cast<double2*>(shb + off);
+  return s;
+}
+
+__device__ void flag_status(PzState& S, int code) {
+  if (threadIdx.x == 0) atomicCAS(&S.status, 0, code);
+}
+
+// dt independent streamfunction operators (update_psi_coll_dmat.f90:94-98)
+__global__ void __launch_bounds__(PZ_THREADS) k_build_static(PzDev d) {
+  const PzItem it = d.mitems[blockIdx.x];
+  const PzInst& I = d.inst[it.inst];
+  PzState& S = d.state[it.inst];
+  if (it.idx == 0 || (I.flags & PZF_DIRECT)) return;
+  const View V{&I, d.pool};
+  const int n = I.N, m = it.idx * I.minc;
+  BuildSmem s = build_smem(n);
+  BuildCtx B{&I, V.basis(BM_RMAT), V.basis(BM_DRMAT), V.basis(BM_D2RMAT), n};
+  fill_matrix(s.A, B, V, 2, m, 0.0);
+  equilibrate(s.A, n, s.f1, s.f2, true);
+  if (gj_invert(s.A, n, s.piv, s.colk, s.red, s.redi) != 0) { flag_status(S, PZ_E_SINGULAR); return; }
+  store_op(d.pool + I.o_gpsi + (long long)it.idx * n * n, s.A, n, I.n_max, s.f2, s.f1);
+}
+
+// dt dependent operators, rebuilt when lMat (step_time.f90:296-303):
+// temperature, omega and u_phi, plus the influence-matrix ingredients.
+__global__ void __launch_bounds__(PZ_THREADS) k_build(PzDev d) {
+  const PzItem it = d.mitems[blockIdx.x];
+  const PzInst& I = d.inst[it.inst];
+  PzState& S = d.state[it.inst];
+  if (S.status != 0 || !S.lMat) return;
+  const View V{&I, d.pool};
+  const int n = I.N, mi = it.idx, m = mi * I.minc;
+  const double wlin = S.wimp_lin[0];
+  BuildSmem s = build_smem(n);
+  BuildCtx B{&I, V.basis(BM_RMAT), V.basis(BM_DRMAT), V.basis(BM_D2RMAT), n};
+  // temperature (get_tempMat with WITH_PRECOND_S: row scaling only)
+  fill_matrix(s.A, B, V, 0, m, wlin);
+  equilibrate(s.A, n, s.f1, s.f2, false);
+  if (gj_invert(s.A, n, s.piv, s.colk, s.red, s.redi) != 0) { flag_status(S, PZ_E_SINGULAR); return; }
+  store_op(d.pool + I.o_gt + (long long)mi * n * n, s.A, n, I.n_max, nullptr, s.f1);
+  __syncthreads();
+  if (m == 0) {
+    fill_matrix(s.A, B, V, 3, 0, wlin);
+    if (gj_invert(s.A, n, s.piv, s.colk, s.red, s.redi) != 0) { flag_status(S, PZ_E_SINGULAR); return; }
+    store_op(d.pool + I.o_guphi, s.A, n, I.n_max, nullptr, nullptr);
+    return;
+  }
+  // omega (get_omMat: row and column scaling)
+  fill_matrix(s.A, B, V, 1, m, wlin);
+  equilibrate(s.A, n, s.f1, s.f2, true);
+  if (gj_invert(s.A, n, s.piv, s.colk, s.red, s.redi) != 0) { flag_status(S, PZ_E_SINGULAR); return; }
+  double* Gom = d.pool + I.o_gom + (long long)mi * n * n;
+  store_op(Gom, s.A, n, I.n_max, s.f2, s.f1);
+  __syncthreads();
+  // intermediate solutions (get_intermediate_om/psi, update_psi_coll_dmat.f90:1136-1218):
+  // om2 = G_om e_{N-1}, om3 = G_om e_0 ; psi_k = G_psi (-C om_k) on interior rows
+  double* aux = d.pool + I.o_aux;
+  const long long MN = (long long)I.M * n;
+  double* om2 = aux + 0 * MN + (long long)mi * n;
+  double* om3 = aux + 1 * MN + (long long)mi * n;
+  double* psi2 = aux + 2 * MN + (long long)mi * n;
+  double* psi3 = aux + 3 * MN + (long long)mi * n;
+  for (int i = threadIdx.x; i < n; i += blockDim.x) {
+    const double a2 = Gom[i + (long long)(n - 1) * n];
+    const double a3 = Gom[i];
+    om2[i] = a2; om3[i] = a3;
+    s.va[i] = make_double2(a2, a3);
+  }
+  __syncthreads();
+  mv1(V.basis(BM_C), n, n, s.va, s.vb);
+  __syncthreads();
+  for (int i = threadIdx.x; i < n; i += blockDim.x) {
+    const bool bd = (i == 0 || i == n - 1);
+    s.va[i] = bd ? make_double2(0.0, 0.0) : make_double2(-s.vb[i].x, -s.vb[i].y);
+  }
+  __syncthreads();
+  mv1(d.pool + I.o_gpsi + (long long)mi * n * n, n, n, s.va, s.vb);
+  __syncthreads();
+  double t2 = 0.0, t3 = 0.0, b2 = 0.0, b3 = 0.0;
+  const double* bct = V.rad(RV_BCTOP);
+  const double* bcb = V.rad(RV_BCBOT);
+  for (int i = threadIdx.x; i < n; i += blockDim.x) {
+    psi2[i] = s.vb[i].x;
+    psi3[i] = s.vb[i].y;
+    t2 += bct[i] * s.vb[i].x; t3 += bct[i] * s.vb[i].y;
+    b2 += bcb[i] * s.vb[i].x; b3 += bcb[i] * s.vb[i].y;
+  }
+  t2 = block_sum(t2, s.red); t3 = block_sum(t3, s.red);
+  b2 = block_sum(b2, s.red); b3 = block_sum(b3, s.red);
+  if (threadIdx.x == 0) {
+    // get_influence_matrix (update_psi_coll_dmat.f90:1220-1254)
+    double* infl = aux + 4 * MN + 4LL * mi;
+    const double det = t2 * b3 - t3 * b2;
+    infl[0] = b3 / det; infl[1] = -t3 / det; infl[2] = -b2 / det; infl[3] = t2 / det;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// implicit terms from physical-space fields: get_temp_rhs_imp_coll and
+// get_psi_rhs_imp_coll_dmat with l_in_cheb_space=.false. (used by the start
+// fields, init_fields.f90:228-255, and by start_from_another_scheme,
+// step_time.f90:417-516).  Writes old/impl logical slot 1 at ring bases bo/bi.
+// ---------------------------------------------------------------------------
+struct MS {   // per-m vectors in shared memory
+  double2 *a, *b, *c, *e, *f, *g, *h, *k;
+  double* red;
+};
+
+__device__ void imp_from_physical(const View& V, const PzInst& I, int mi, int bo, int bi, bool calc, MS& s) {
+  const int n = I.N;
+  const int m = mi * I.minc;
+  const double dm = (double)m, dm2 = dm * dm;
+  const double* or1 = V.rad(RV_OR1);
+  const double* or2 = V.rad(RV_OR2);
+  const double* rgrav = V.rad(RV_RGRAV);
+  const double* ekpump = V.rad(RV_EKPUMP);
+  double2* T = V.fld(F_TEMP, mi);
+  double2* om = V.fld(F_OM, mi);
+  double2* up = V.fld(F_UP, mi);
+  for (int i = threadIdx.x; i < n; i += blockDim.x) s.a[i] = T[i];
+  __syncthreads();
+  mv2(V.basis(BM_D1P), V.basis(BM_D2P), n, s.a, s.b, s.c);
+  __syncthreads();
+  double2* oT = V.hist(0, 0, bo, mi);
+  double2* iT = V.hist(0, 1, bi, mi);
+  double2* dT = V.fld(F_DTEMP, mi);
+  for (int i = threadIdx.x; i < n; i += blockDim.x) {
+    const double2 t = s.a[i], d1 = s.b[i], d2 = s.c[i];
+    oT[i] = t;
+    dT[i] = d1;
+    if (calc) {
+      const double f = I.TdiffFac;
+      iT[i] = make_double2(f * (d2.x + or1[i] * d1.x - dm2 * or2[i] * t.x),
+                           f * (d2.y + or1[i] * d1.y - dm2 * or2[i] * t.y));
+    }
+  }
+  __syncthreads();
+  double2* oP = V.hist(1, 0, bo, mi);
+  double2* iP = V.hist(1, 1, bi, mi);
+  if (m == 0) {
+    for (int i = threadIdx.x; i < n; i += blockDim.x) s.a[i] = make_double2(up[i].x, 0.0);
+  } else {
+    for (int i = threadIdx.x; i < n; i += blockDim.x) s.a[i] = om[i];
+  }
+  __syncthreads();
+  mv2(V.basis(BM_D1P), V.basis(BM_D2P), n, s.a, s.b, s.c);
+  __syncthreads();
+  for (int i = threadIdx.x; i < n; i += blockDim.x) {
+    const double2 x = s.a[i], d1 = s.b[i], d2 = s.c[i];
+    if (m == 0) {
+      oP[i] = up[i];
+      if (calc) {
+        const double u = x.x;
+        iP[i] = make_double2(I.ViscFac * (d2.x + or1[i] * d1.x - or2[i] * u) - I.CorFac * ekpump[i] * u, 0.0);
+      }
+    } else {
+      oP[i] = x;
+      if (calc) {
+        double2 v = make_double2(I.ViscFac * (d2.x + or1[i] * d1.x - dm2 * or2[i] * x.x),
+                                 I.ViscFac * (d2.y + or1[i] * d1.y - dm2 * or2[i] * x.y));
+        if (I.flags & PZF_BUO_IMP) {
+          const double2 b = cim(dm, T[i]);
+          const double c = rgrav[i] * or1[i] * I.BuoFac;
+          v.x -= c * b.x; v.y -= c * b.y;
+        }
+        iP[i] = v;
+      }
+    }
+  }
+  __syncthreads();
+}
+
+__device__ MS ms_smem(int n) {
+  extern __shared__ double2 shm[];
+  MS s;
+  s.a = shm; s.b = s.a + n; s.c = s.b + n; s.e = s.c + n; s.f = s.e + n; s.g = s.f + n; s.h = s.g + n; s.k = s.h + n;
+  s.red = reinterpret_cast<double*>(s.k + n);
+  return s;
+}
+
+// start fields (init_fields.f90:54-258, no checkpoint)
+__global__ void __launch_bounds__(PZ_THREADS) k_start(PzDev d, int only) {
+  const PzItem it = d.mitems[blockIdx.x];
+  if (only >= 0 && it.inst != only) return;
+  const PzInst& I = d.inst[it.inst];
+  PzState& S = d.state[it.inst];
+  const View V{&I, d.pool};
+  const int n = I.N, mi = it.idx, m = mi * I.minc;
+  const double dm = (double)m;
+  MS s = ms_smem(n);
+  // zero the history rings of this m
+  for (int f = 0; f < 2; ++f)
+    for (int kind = 0; kind < 3; ++kind) {
+      const int ns = kind == 0 ? I.nold : (kind == 1 ? I.nimp : I.nexp);
+      for (int ph = 0; ph < ns; ++ph) {
+        double2* h = V.hist(f, kind, ph, mi);
+        for (int i = threadIdx.x; i < n; i += blockDim.x) h[i] = make_double2(0.0, 0.0);
+      }
+    }
+  double2* us = V.fld(F_US, mi);
+  double2* up = V.fld(F_UP, mi);
+  double2* om = V.fld(F_OM, mi);
+  double2* psi = V.fld(F_PSI, mi);
+  const double* or1 = V.rad(RV_OR1);
+  for (int i = threadIdx.x; i < n; i += blockDim.x) { s.a[i] = up[i]; psi[i] = make_double2(0.0, 0.0); }
+  __syncthreads();
+  mv1(V.basis(BM_D1P), n, n, s.a, s.b);
+  __syncthreads();
+  for (int i = threadIdx.x; i < n; i += blockDim.x) {
+    // om = d(up)/dr + up/r - (i m / r) us
+    const double2 u = up[i], w = s.b[i], vs = cim(dm, us[i]);
+    om[i] = make_double2(w.x + or1[i] * u.x - or1[i] * vs.x, w.y + or1[i] * u.y - or1[i] * vs.y);
+  }
+  __syncthreads();
+  imp_from_physical(V, I, mi, S.b_old, S.b_impl, true, s);
+}
+
+// ---------------------------------------------------------------------------
+// k_mloop: finish_explicit_assembly + update_temp_co + update_om_coll_dmat
+// for one m of one instance (src/mloop.f90:36-229)
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ double2 imex_rhs(const View& V, const PzInst& I, const PzState& S, int f, int mi, int i) {
+  double2 acc;
+  {
+    const double2 v = V.hist(f, 0, S.r_old, mi)[i];
+    acc = make_double2(S.wimp[0] * v.x, S.wimp[0] * v.y);
+  }
+  for (int k = 1; k < I.nold; ++k) {
+    const double2 v = V.hist(f, 0, (S.r_old + k) % I.nold, mi)[i];
+    acc.x += S.wimp[k] * v.x; acc.y += S.wimp[k] * v.y;
+  }
+  for (int k = 0; k < I.nimp; ++k) {
+    const double2 v = V.hist(f, 1, (S.r_impl + k) % I.nimp, mi)[i];
+    acc.x += S.wimp_lin[k + 1] * v.x; acc.y += S.wimp_lin[k + 1] * v.y;
+  }
+  for (int k = 0; k < I.nexp; ++k) {
+    const double2 v = V.hist(f, 2, (S.r_expl + k) % I.nexp, mi)[i];
+    acc.x += S.wexp[k] * v.x; acc.y += S.wexp[k] * v.y;
+  }
+  return acc;
+}
+
+__global__ void __launch_bounds__(PZ_THREADS) k_mloop(PzDev d) {
+  const PzItem it = d.mitems[blockIdx.x];
+  const PzInst& I = d.inst[it.inst];
+  PzState& Sg = d.state[it.inst];
+  if (Sg.status != 0) return;
+  const PzState S = Sg;
+  const View V{&I, d.pool};
+  const int n = I.N, mi = it.idx, m = mi * I.minc;
+  const double dm = (double)m, dm2 = dm * dm;
+  MS s = ms_smem(n);
+  const double* or1 = V.rad(RV_OR1);
+  const double* or2 = V.rad(RV_OR2);
+  const double* beta = V.rad(RV_BETA);
+  const double* rgrav = V.rad(RV_RGRAV);
+  const double* tcond = V.rad(RV_TCOND);
+  const double* dtcond = V.rad(RV_DTCOND);
+  const double* ekpump = V.rad(RV_EKPUMP);
+  const double* ekp_up = V.rad(RV_EKP_UP);
+  const double* ekp_us = V.rad(RV_EKP_US);
+  const double* ekp_dusdp = V.rad(RV_EKP_DUSDP);
+  double2* us = V.fld(F_US, mi);
+  double2* up = V.fld(F_UP, mi);
+  double2* om = V.fld(F_OM, mi);
+  double2* psi = V.fld(F_PSI, mi);
+  double2* T = V.fld(F_TEMP, mi);
+  double2* dT = V.fld(F_DTEMP, mi);
+  const bool buo_imp = (I.flags & PZF_BUO_IMP) != 0;
+
+  // -- finish_exp_temp_coll (update_temp_coll.f90:152-176)
+  for (int i = threadIdx.x; i < n; i += blockDim.x) {
+    s.a[i] = V.fld(F_DVST, mi)[i];
+    s.e[i] = V.fld(F_DVSOM, mi)[i];
+  }
+  __syncthreads();
+  mv1(V.basis(BM_D1P), n, n, s.a, s.b);
+  mv1(V.basis(BM_D1P), n, n, s.e, s.f);
+  __syncthreads();
+  {
+    double2* eT = V.hist(0, 2, S.r_expl, mi);
+    double2* eP = V.hist(1, 2, S.r_expl, mi);
+    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+      double2 e = eT[i];
+      const double2 u = us[i];
+      const double c = dtcond[i] - I.tadvz * beta[i] * tcond[i];
+      e.x = e.x - or1[i] * s.b[i].x - u.x * c;
+      e.y = e.y - or1[i] * s.b[i].y - u.y * c;
+      eT[i] = e;
+      // finish_exp_psi_coll_dmat (update_psi_coll_dmat.f90:468-552), m /= 0
+      if (m != 0) {
+        double2 p = eP[i];
+        p.x -= or1[i] * s.f[i].x;
+        p.y -= or1[i] * s.f[i].y;
+        if (!(I.flags & PZF_NON_ROT)) {
+          p.x += I.CorFac * beta[i] * u.x;
+          p.y += I.CorFac * beta[i] * u.y;
+        }
+        if (!buo_imp) {
+          const double2 b = cim(dm, T[i]);
+          const double cb = I.BuoFac * rgrav[i] * or1[i];
+          p.x -= cb * b.x; p.y -= cb * b.y;
+        }
+        if (I.flags & PZF_EK_PUMP) {
+          const double2 o = om[i], w = up[i];
+          const double2 q = make_double2(ekp_us[i] * u.x - ekp_dusdp[i] * dm * u.y,
+                                         ekp_us[i] * u.y + ekp_dusdp[i] * dm * u.x);
+          const double ce = I.CorFac * ekpump[i];
+          p.x -= ce * (o.x + ekp_up[i] * w.x + q.x);
+          p.y -= ce * (o.y + ekp_up[i] * w.y + q.y);
+        }
+        eP[i] = p;
+      }
+    }
+  }
+  __syncthreads();
+  // -- start_from_another_scheme (step_time.f90:417-516)
+  if (S.bridge) imp_from_physical(V, I, mi, S.r_old, S.r_impl, true, s);
+
+  // -- update_temp_co (update_temp_coll.f90:66-150)
+  for (int i = threadIdx.x; i < n; i += blockDim.x) {
+    const double2 v = imex_rhs(V, I, S, 0, mi, i);
+    s.a[i] = (i == 0 || i == n - 1) ? make_double2(0.0, 0.0) : v;   // topt = bott = 0
+  }
+  __syncthreads();
+  mv1(d.pool + I.o_gt + (long long)mi * n * n, n, n, s.a, s.b);           // Chebyshev T
+  __syncthreads();
+  mv3(V.basis(BM_D1C), V.basis(BM_D2C), V.basis(BM_C), n, s.b, s.c, s.e, s.f);
+  __syncthreads();
+  bool bad = false;
+  {
+    double2* oT = V.hist(0, 0, S.b_old, mi);
+    double2* iT = V.hist(0, 1, S.b_impl, mi);
+    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+      const double2 t = s.f[i], d1 = s.c[i], d2 = s.e[i];
+      T[i] = t;
+      dT[i] = d1;
+      oT[i] = t;
+      bad |= !isfinite(t.x) || !isfinite(t.y);
+      if (S.l_calc_lin) {
+        const double f = I.TdiffFac;
+        iT[i] = make_double2(f * (d2.x + or1[i] * d1.x - dm2 * or2[i] * t.x),
+                             f * (d2.y + or1[i] * d1.y - dm2 * or2[i] * t.y));
+      }
+    }
+  }
+  // s.f keeps the new physical temperature
+  // -- update_om_coll_dmat (update_psi_coll_dmat.f90:126-466)
+  for (int i = threadIdx.x; i < n; i += blockDim.x) {
+    double2 v = imex_rhs(V, I, S, 1, mi, i);
+    if (m != 0 && buo_imp) {
+      const double2 b = cim(dm, s.f[i]);
+      const double c = S.wimp_lin[0] * I.BuoFac * rgrav[i] * or1[i];
+      v.x -= c * b.x; v.y -= c * b.y;
+    }
+    if (m == 0) v.y = 0.0;
+    s.a[i] = (i == 0 || i == n - 1) ? make_double2(0.0, 0.0) : v;
+  }
+  __syncthreads();
+  double2* oP = V.hist(1, 0, S.b_old, mi);
+  double2* iP = V.hist(1, 1, S.b_impl, mi);
+  if (m == 0) {
+    mv1(d.pool + I.o_guphi, n, n, s.a, s.b);            // uphi, Chebyshev
+    __syncthreads();
+    mv3(V.basis(BM_D1C), V.basis(BM_D2C), V.basis(BM_C), n, s.b, s.c, s.e, s.g);
+    __syncthreads();
+    const double* ekp = ekpump;
+    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+      const double u = s.g[i].x, du = s.c[i].x, d2u = s.e[i].x;
+      us[i] = make_double2(0.0, 0.0);
+      up[i] = make_double2(u, 0.0);
+      om[i] = make_double2(du + or1[i] * u, 0.0);
+      psi[i] = make_double2(0.0, 0.0);
+      oP[i] = make_double2(u, 0.0);
+      bad |= !isfinite(u);
+      if (S.l_calc_lin)
+        iP[i] = make_double2(I.ViscFac * (d2u + or1[i] * du - or2[i] * u) - I.CorFac * ekp[i] * u, 0.0);
+    }
+  } else {
+    mv1(d.pool + I.o_gom + (long long)mi * n * n, n, n, s.a, s.b);   // omega, Chebyshev
+    __syncthreads();
+    mv1(V.basis(BM_C), n, n, s.b, s.c);                             // omega, physical
+    __syncthreads();
+    for (int i = threadIdx.x; i < n; i += blockDim.x)
+      s.a[i] = (i == 0 || i == n - 1) ? make_double2(0.0, 0.0) : make_double2(-s.c[i].x, -s.c[i].y);
+    __syncthreads();
+    mv1(d.pool + I.o_gpsi + (long long)mi * n * n, n, n, s.a, s.e);  // psi, Chebyshev
+    __syncthreads();
+    // influence-matrix correction (update_psi_coll_dmat.f90:1256-1300)
+    const double* bct = V.rad(RV_BCTOP);
+    const double* bcb = V.rad(RV_BCBOT);
+    double tr = 0.0, ti = 0.0, br = 0.0, bi = 0.0;
+    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+      tr += bct[i] * s.e[i].x; ti += bct[i] * s.e[i].y;
+      br += bcb[i] * s.e[i].x; bi += bcb[i] * s.e[i].y;
+    }
+    tr = block_sum(tr, s.red); ti = block_sum(ti, s.red);
+    br = block_sum(br, s.red); bi = block_sum(bi, s.red);
+    const long long MN = (long long)I.M * n;
+    const double* aux = d.pool + I.o_aux;
+    const double* infl = aux + 4 * MN + 4LL * mi;
+    const double c1r = -infl[0] * tr - infl[1] * br, c1i = -infl[0] * ti - infl[1] * bi;
+    const double c2r = -infl[2] * tr - infl[3] * br, c2i = -infl[2] * ti - infl[3] * bi;
+    const double* om2 = aux + 0 * MN + (long long)mi * n;
+    const double* om3 = aux + 1 * MN + (long long)mi * n;
+    const double* psi2 = aux + 2 * MN + (long long)mi * n;
+    const double* psi3 = aux + 3 * MN + (long long)mi * n;
+    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+      double2 p = s.e[i], o = s.b[i];
+      p.x += c1r * psi2[i] + c2r * psi3[i];
+      p.y += c1i * psi2[i] + c2i * psi3[i];
+      o.x += c1r * om2[i] + c2r * om3[i];
+      o.y += c1i * om2[i] + c2i * om3[i];
+      s.e[i] = p;
+      s.b[i] = o;
+    }
+    __syncthreads();
+    mv2(V.basis(BM_D1C), V.basis(BM_C), n, s.e, s.g, s.h);            // dpsi/dr, psi
+    __syncthreads();
+    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+      const double2 p = s.h[i], dp = s.g[i];
+      psi[i] = p;
+      us[i] = cscale(or1[i], cim(dm, p));
+      up[i] = make_double2(-dp.x - beta[i] * p.x, -dp.y - beta[i] * p.y);
+    }
+    mv3(V.basis(BM_D1C), V.basis(BM_D2C), V.basis(BM_C), n, s.b, s.c, s.a, s.k);   // dom, d2om, om
+    __syncthreads();
+    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+      const double2 o = s.k[i], d1 = s.c[i], d2 = s.a[i];
+      om[i] = o;
+      oP[i] = o;
+      bad |= !isfinite(o.x) || !isfinite(o.y);
+      if (S.l_calc_lin) {
+        double2 v = make_double2(I.ViscFac * (d2.x + or1[i] * d1.x - dm2 * or2[i] * o.x),
+                                 I.ViscFac * (d2.y + or1[i] * d1.y - dm2 * or2[i] * o.y));
+        if (buo_imp) {
+          const double2 b = cim(dm, s.f[i]);
+          const double c = rgrav[i] * or1[i] * I.BuoFac;
+          v.x -= c * b.x; v.y -= c * b.y;
+        }
+        iP[i] = v;
+      }
+    }
+  }
+  if (__syncthreads_or(bad)) flag_status(Sg, PZ_E_NONFINITE);
+}
+
+// ---------------------------------------------------------------------------
+// k_obs: time series of one instance (src/outputs.f90:418-830)
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ double round_off(double x) { return fabs(x) < 1.0e-20 ? 0.0 : x; }
+
+__global__ void k_obs(PzDev d, int only) {
+  const int inst = blockIdx.x;
+  if (only >= 0 && inst != only) return;
+  const PzInst& I = d.inst[inst];
+  PzState& S = d.state[inst];
+  const View V{&I, d.pool};
+  __shared__ double red[32];
+  const int n = I.N, M = I.M;
+  const double* rr = V.rad(RV_R);
+  const double* or2 = V.rad(RV_OR2);
+  const double* h = V.rad(RV_HEIGHT);
+  const double* beta = V.rad(RV_BETA);
+  const double* dtcond = V.rad(RV_DTCOND);
+  const double* wint = V.rad(RV_WINT);
+  const double* wsimp = V.rad(RV_WSIMP);
+  const double2* us = V.fld(F_US, 0);
+  const double2* up = V.fld(F_UP, 0);
+  const double2* T = V.fld(F_TEMP, 0);
+  const double2* dT = V.fld(F_DTEMP, 0);
+  const bool rot = !(I.flags & PZF_NON_ROT);
+  double s_us = 0, s_up = 0, s_ax = 0, s_us3 = 0, s_up3 = 0, s_uz3 = 0, s_ax3 = 0, s_nu = 0, s_fl = 0;
+  for (int r = threadIdx.x; r < n; r += blockDim.x) {
+    double us2 = 0, up2 = 0, nu = 0, fl = 0, ax = 0;
+    for (int mi = 0; mi < M; ++mi) {
+      const long long o = (long long)mi * n + r;
+      const double2 a = us[o], b = up[o], t = T[o], dt = dT[o];
+      const double mm = (double)(mi * I.minc);
+      if (mi == 0) {
+        us2 += a.x * a.x;
+        up2 += b.x * b.x;
+        ax = b.x * b.x;
+        nu += dt.x * dt.x + mm * mm * or2[r] * (t.x * t.x);
+        fl += a.x * t.x;
+        fl = fl - I.TdiffFac * dt.x - I.TdiffFac * dtcond[r];
+      } else {
+        us2 += 2.0 * (a.x * a.x + a.y * a.y);
+        up2 += 2.0 * (b.x * b.x + b.y * b.y);
+        nu += 2.0 * (dt.x * dt.x + dt.y * dt.y) + mm * mm * or2[r] * 2.0 * (t.x * t.x + t.y * t.y);
+        fl += 2.0 * (a.x * t.x + a.y * t.y);
+      }
+    }
+    nu = nu * rr[r] * h[r];
+    s_us += wint[r] * us2 * rr[r];
+    s_up += wint[r] * up2 * rr[r];
+    s_ax += wint[r] * ax * rr[r];
+    if (rot) {
+      s_us3 += wint[r] * us2 * rr[r] * h[r];
+      s_up3 += wint[r] * up2 * rr[r] * h[r];
+      s_uz3 += wint[r] * us2 * beta[r] * beta[r] * rr[r] * h[r] * h[r] * h[r] / 12.0;
+      s_ax3 += wint[r] * ax * rr[r] * h[r];
+      const double x = rr[r] / I.r_cmb;
+      s_fl += wsimp[r] * fl * x * x;
+    } else {
+      s_fl += wint[r] * fl * rr[r];
+    }
+    s_nu += wint[r] * nu;
+  }
+  s_us = block_sum(s_us, red); s_up = block_sum(s_up, red); s_ax = block_sum(s_ax, red);
+  s_us3 = block_sum(s_us3, red); s_up3 = block_sum(s_up3, red); s_uz3 = block_sum(s_uz3, red);
+  s_ax3 = block_sum(s_ax3, red); s_nu = block_sum(s_nu, red); s_fl = block_sum(s_fl, red);
+  if (threadIdx.x != 0) return;
+  const double pi = 3.14159265358979323846;
+  double* row = d.pool + I.o_series + (long long)(S.series_count % PZ_SERIES_CAP) * PZ_SERIES_COLS;
+  row[0] = S.time;
+  row[1] = round_off(pi * s_us);
+  row[2] = round_off(pi * s_up);
+  row[3] = round_off(pi * s_ax);
+  row[4] = rot ? round_off(pi * s_us3) : 0.0;
+  row[5] = rot ? round_off(pi * s_up3) : 0.0;
+  row[6] = rot ? round_off(pi * s_uz3) : 0.0;
+  row[7] = rot ? round_off(pi * s_ax3) : 0.0;
+  const double* tcond = V.rad(RV_TCOND);
+  row[8] = round_off(1.0 + dT[0].x / dtcond[0]);
+  row[9] = round_off(1.0 + dT[n - 1].x / dtcond[n - 1]);
+  row[10] = round_off(1.0 + s_nu / I.nu_vol_den);
+  row[11] = round_off(s_fl / I.nu_int_fac);
+  row[12] = round_off(T[0].x + tcond[0]);
+  row[13] = round_off(T[n - 1].x + tcond[n - 1]);
+  row[14] = round_off(dtcond[n / 2 - 1] + dT[n / 2 - 1].x);
+  row[15] = S.dt[0];
+  S.series_count += 1;
+}
+
+__global__ void k_init_state(PzDev d, int only) {
+  const int inst = blockIdx.x * blockDim.x + threadIdx.x;
+  if (inst >= d.n_inst || (only >= 0 && inst != only)) return;
+  const PzInst& I = d.inst[inst];
+  PzState S;
+  memset(&S, 0, sizeof(S));
+  for (int k = 0; k < 4; ++k) S.dt[k] = I.dtMax;
+  set_weights(I, S);
+  S.lMatNext = 1;
+  S.l_calc_lin = 1;
+  d.state[inst] = S;
+}
+
+size_t build_smem_bytes(int n) {
+  long long off = (long long)n * n + 3LL * n + 32 + 16 + (n + 1) / 2;
+  off = (off + 1) & ~1LL;
+  off += 4LL * n;
+  return (size_t)off * sizeof(double);
+}
+size_t ms_smem_bytes(int n) { return 8 * (size_t)n * sizeof(double2) + 64 * sizeof(double); }
+size_t rloop_smem_bytes(int P) { return 5 * (size_t)P * sizeof(double2); }
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+// launchers
+// ---------------------------------------------------------------------------
+cudaError_t pz_setup_kernels() {
+  cudaError_t e;
+  const int big = 200 * 1024;
+  if ((e = cudaFuncSetAttribute(k_build, cudaFuncAttributeMaxDynamicSharedMemorySize, big))) return e;
+  if ((e = cudaFuncSetAttribute(k_build_static, cudaFuncAttributeMaxDynamicSharedMemorySize, big))) return e;
+  if ((e = cudaFuncSetAttribute(k_rloop, cudaFuncAttributeMaxDynamicSharedMemorySize, 64 * 1024))) return e;
+  return cudaSuccess;
+}
+
+cudaError_t pz_launch_build_static(const PzDev& d, cudaStream_t s) {
+  k_build_static<<<d.n_mitems, PZ_THREADS, build_smem_bytes(d.maxN), s>>>(d);
+  return cudaGetLastError();
+}
+
+cudaError_t pz_launch_init_state(const PzDev& d, int only, cudaStream_t s) {
+  k_init_state<<<(d.n_inst + 63) / 64, 64, 0, s>>>(d, only);
+  return cudaGetLastError();
+}
+
+cudaError_t pz_launch_start(const PzDev& d, int only, cudaStream_t s) {
+  k_start<<<d.n_mitems, PZ_THREADS, ms_smem_bytes(d.maxN), s>>>(d, only);
+  return cudaGetLastError();
+}
+
+cudaError_t pz_launch_obs(const PzDev& d, int only, cudaStream_t s) {
+  k_obs<<<d.n_inst, PZ_THREADS, 0, s>>>(d, only);
+  return cudaGetLastError();
+}
+
+int pz_step_launch_count() { return 5; }
+
+cudaError_t pz_launch_step(const PzDev& d, cudaStream_t s) {
+  k_rloop<<<d.n_ritems, PZ_THREADS, rloop_smem_bytes(d.maxP), s>>>(d);
+  k_cfl<<<d.n_inst, 32, 0, s>>>(d);
+  k_build<<<d.n_mitems, PZ_THREADS, build_smem_bytes(d.maxN), s>>>(d);
+  k_mloop<<<d.n_mitems, PZ_THREADS, ms_smem_bytes(d.maxN), s>>>(d);
+  k_obs<<<d.n_inst, PZ_THREADS, 0, s>>>(d, -1);
+  return cudaGetLastError();
+}

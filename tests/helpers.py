@@ -1,0 +1,43 @@
+"""Shared helpers of the test suite: one workload description drives both
+the oracle (oracle.pizza_oracle.Params) and the CUDA library
+(pizza_gb300.Config)."""
+import numpy as np
+
+from oracle.pizza_oracle import Params, Pizza, seeded_temperature
+
+ORACLE_ONLY = {"n_time_steps", "n_log_step", "init_t", "amp_t", "init_u", "amp_u"}
+
+
+def gpu_config(spec):
+    import pizza_gb300 as pz
+    kw = {k: v for k, v in spec.items() if k not in ORACLE_ONLY}
+    return pz.Config(**kw)
+
+
+def oracle(spec, temp0=None):
+    sim = Pizza(Params(**spec))
+    sim.start(temp0=temp0)
+    return sim
+
+
+def seeded(spec, seed, amp=1e-3):
+    sim = Pizza(Params(**spec))
+    return seeded_temperature(sim.M, sim.r, sim.d["r_icb"], amp, seed)
+
+
+def rel_err(a, b):
+    """max |a - b| / max |b| (norm-wise relative error of a field)."""
+    a = np.asarray(a)
+    b = np.asarray(b)
+    den = np.max(np.abs(b))
+    return float(np.max(np.abs(a - b)) / (den if den > 0 else 1.0))
+
+
+def series_from_oracle(sim):
+    """Oracle time-series row in the library's column order."""
+    rows = sim.time_series()
+    ek = rows["e_kin"]
+    e3 = rows.get("e_kin_3D", [ek[0], 0.0, 0.0, 0.0, 0.0])
+    ht = rows["heat"]
+    return np.array([ek[0], ek[1], ek[2], ek[3], e3[1], e3[2], e3[3], e3[4],
+                     ht[1], ht[2], ht[3], ht[4], ht[5], ht[6], ht[7], sim.ts.dt[0]])
