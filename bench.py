@@ -1,0 +1,402 @@
+"""Benchmark of the GB300 pizza time step.
+
+Workload (configs[2] shape, the configuration the headline metric is quoted
+on): a batched ensemble of B independent annulus instances of uneven size,
+n_r_max in {33, 49, 65}, n_phi_max in {96, 192, 288} (m_max = n_phi_max/3),
+log10 Ra ~ U[5, 7], E in {1e-3, 1e-4}, Pr = 1, radius ratio 0.35, Ekman
+pumping, CNAB2 with per-instance CFL time steps (courfac 0.5, dtMax =
+min(1e-4, 0.03/sqrt(Ra))), collocation with the influence-matrix solve, each
+instance started from its own seeded temperature perturbation of amplitude
+1e-3 (synthetic data: the reference publishes no dataset).  One step advances
+every instance by one time step.
+
+Metric: aggregate instance-steps/s of the batched step (``value``), next to the
+plain one-instance-per-handle GPU step of the same instances
+(``plain_steps_per_s``); their ratio is the reference's headline quantity.
+
+Usage: python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+if ROOT not in sys.path:
+    sys.path.insert(0, ROOT)
+
+METRIC = "aggregate steps/s batched vs plain GPU step at 1e-10 rel err; adjoint/forward time"
+UNIT = "instance-steps/s"
+NS = (33, 49, 65)
+PS = (96, 192, 288)
+
+
+def ensemble_specs(n_inst: int, seed: int = 1234):
+    """The batched workload: per-instance namelist values and seeds."""
+    rng = np.random.default_rng(seed)
+    specs = []
+    for i in range(n_inst):
+        N = int(rng.choice(NS))
+        P = int(rng.choice(PS))
+        ra = float(10.0 ** rng.uniform(5.0, 7.0))
+        ek = float(rng.choice([1e-3, 1e-4]))
+        specs.append(dict(n_r_max=N, n_cheb_max=N, m_max=P // 3, ra=ra, ek=ek, pr=1.0, radratio=0.35,
+                          l_ek_pump=True, time_scheme="CNAB2", courfac=0.5,
+                          dtMax=min(1e-4, 0.03 / math.sqrt(ra)), matrix_solve="INFLUENCE",
+                          seed=int(seed * 1000 + i)))
+    return specs
+
+
+def seeded_temp(spec, amp=1e-3):
+    """Seeded perturbation T(m,r) = amp g_m e^{i theta_m} sin(pi (r - r_i)), m >= 1."""
+    N, M = spec["n_r_max"], spec["m_max"] + 1
+    r_cmb = 1.0 / (1.0 - spec["radratio"])
+    r_icb = r_cmb - 1.0
+    x = np.cos(np.pi * np.arange(N) / (N - 1))
+    r = 0.5 * (r_cmb - r_icb) * x + 0.5 * (r_cmb + r_icb)
+    rng = np.random.default_rng(spec["seed"])
+    g = rng.standard_normal(M - 1)
+    th = rng.uniform(0.0, 2.0 * np.pi, M - 1)
+    T = np.zeros((M, N), complex)
+    T[1:, :] = (amp * g * np.exp(1j * th))[:, None] * np.sin(np.pi * (r - r_icb))[None, :]
+    return T
+
+
+def gpu_cfg(spec):
+    import pizza_gb300 as pz
+    kw = {k: v for k, v in spec.items() if k != "seed"}
+    return pz.Config(**kw)
+
+
+# ---------------------------------------------------------------------------
+# algorithmic work per launch of the per-m solve kernel (k_mloop)
+# ---------------------------------------------------------------------------
+def mloop_work(specs, nold=1, nimp=1, nexp=2):
+    """Algorithmic HBM bytes and FP64 flops of one k_mloop launch over the batch.
+
+    Per (instance, m): the three per-m operators (temperature, vorticity,
+    streamfunction; N x N FP64 each, m = 0: temperature and u_phi), the
+    influence vectors (4N + 4 doubles), the state it reads (dVsT, dVsOm, us, up,
+    om, T: 6 complex N-vectors) and the history slots of both equations
+    (2 (nold + nimp + nexp) complex N-vectors), and what it writes (T, dT/dr,
+    us, up, om, psi, two explicit, two old and two implicit slots: 12 complex
+    N-vectors).  The Chebyshev operators shared by all m of one size are
+    counted once per size.  Flops: 14 real-operator x complex-vector products
+    of 4N^2 flops per m (m = 0: 10), elementwise work neglected.
+    """
+    byts = 0.0
+    flops = 0.0
+    sizes = set()
+    for s in specs:
+        N, M = s["n_r_max"], s["m_max"] + 1
+        sizes.add(N)
+        per_m = 8.0 * 3 * N * N + 8.0 * (4 * N + 4) + 16.0 * N * (6 + 2 * (nold + nimp + nexp) + 12)
+        m0 = 8.0 * 2 * N * N + 16.0 * N * (6 + 2 * (nold + nimp + nexp) + 12)
+        byts += (M - 1) * per_m + m0
+        flops += (M - 1) * 14 * 4.0 * N * N + 10 * 4.0 * N * N
+    for N in sizes:
+        byts += 8.0 * 4 * N * N
+    return byts, flops
+
+
+# ---------------------------------------------------------------------------
+# clocks during the timed region
+# ---------------------------------------------------------------------------
+class Clocks:
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self):
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        try:
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            self.proc = subprocess.Popen(["nvidia-smi", f"--query-gpu={self.QUERY}", "--format=csv,noheader,nounits",
+                                          "-lms", "100"], stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        dev = int(os.environ.get("LOCAL_RANK", "0"))
+        for line in open(self.path):
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                if int(f[0]) != dev:
+                    continue
+                sm.append(float(f[1]))
+                mx.append(float(f[2]))
+            except ValueError:
+                continue
+            for k, nm in enumerate(names):
+                if f[5 + k].lower().startswith("active"):
+                    reasons.add(nm)
+        os.unlink(self.path)
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def measured_peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            j = json.load(f)
+        return float(j["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def fp64_gemm_peak():
+    """FP64 throughput of cuBLAS DGEMM on this GPU (TFLOP/s), the FP64 ceiling."""
+    import torch
+    n = 4096
+    a = torch.randn(n, n, dtype=torch.float64, device="cuda")
+    b = torch.randn(n, n, dtype=torch.float64, device="cuda")
+    torch.matmul(a, b)
+    torch.cuda.synchronize()
+    best = 1e30
+    for _ in range(3):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        torch.matmul(a, b)
+        e1.record()
+        e1.synchronize()
+        best = min(best, e0.elapsed_time(e1))
+    return 2.0 * n ** 3 / (best * 1e-3) / 1e12
+
+
+# ---------------------------------------------------------------------------
+# CPU baselines (oracle port)
+# ---------------------------------------------------------------------------
+def _cpu_class_time(args):
+    spec, nsteps = args
+    from oracle.pizza_oracle import Params, Pizza
+    kw = {k: v for k, v in spec.items() if k != "seed"}
+    sim = Pizza(Params(**kw))
+    sim.start(temp0=seeded_temp(spec))
+    sim.advance()                       # builds the matrices
+    t0 = time.perf_counter()
+    for _ in range(nsteps):
+        sim.advance()
+    return (time.perf_counter() - t0) / nsteps
+
+
+def cpu_baseline(specs, nsteps=4):
+    """Single-core oracle, one instance per size class, scaled to the batch."""
+    classes = {}
+    for s in specs:
+        classes.setdefault((s["n_r_max"], s["m_max"]), []).append(s)
+    t_class = {k: _cpu_class_time((v[0], nsteps)) for k, v in classes.items()}
+    t_step = sum(t_class[(s["n_r_max"], s["m_max"])] for s in specs)
+    return {"value": len(specs) / t_step, "unit": UNIT, "cores": 1, "kind": "port",
+            "sample": f"oracle (NumPy/SciPy FP64) {nsteps} steps of one instance per (n_r_max, m_max) class "
+                      f"({len(classes)} classes), scaled by the class counts of the {len(specs)}-instance batch"}
+
+
+def reference_arm(args, specs):
+    """--impl reference: the oracle port of the reference's CPU algorithm on all host cores."""
+    import multiprocessing as mp
+    cores = os.cpu_count() or 1
+    sample = specs[: min(len(specs), max(cores, 32))]
+    steps = max(1, min(args.steps, 3))
+    ctx = mp.get_context("spawn")
+    t0 = time.perf_counter()
+    with ctx.Pool(cores) as pool:
+        per = pool.map(_cpu_class_time, [(s, steps) for s in sample])
+    wall = time.perf_counter() - t0
+    # aggregate rate of `cores` workers each stepping its own instances
+    rate = len(sample) / (sum(per) / cores)
+    line = {"impl": "reference", "metric": METRIC, "value": rate, "unit": UNIT, "n_gpus": 0,
+            "steps": steps, "warmup": 1, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f64", "data": "synthetic",
+            "config": {"workload": f"batched ensemble of {len(specs)} instances (configs[2] shape)",
+                       "instances_sampled": len(sample)},
+            "cpu_baseline": {"value": rate, "unit": UNIT, "cores": cores, "kind": "port",
+                             "sample": f"{len(sample)} instances x {steps} steps of the oracle port, one process "
+                                       f"per core; wall {wall:.1f}s incl. matrix set-up"},
+            "e2e": {"value": rate, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+
+
+# ---------------------------------------------------------------------------
+# GPU arm
+# ---------------------------------------------------------------------------
+def time_steps(ens, k, torch):
+    s = torch.cuda.ExternalStream(ens.stream_ptr)
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(s)
+    ens.step(k, sync=False)
+    e1.record(s)
+    e1.synchronize()
+    ens.sync()
+    return e0.elapsed_time(e1)
+
+
+def plain_rate(specs, steps, warmup, torch):
+    """Plain GPU step: one instance per handle, stepped one after another.
+    One instance per (n_r_max, m_max) class is timed; the batch time is the
+    sum over instances of their class's per-step time."""
+    import pizza_gb300 as pz
+    classes = {}
+    for s in specs:
+        classes.setdefault((s["n_r_max"], s["m_max"]), s)
+    t_class = {}
+    for key, s in classes.items():
+        e = pz.Ensemble(gpu_cfg(s))
+        e.set_state(0, temp=seeded_temp(s))
+        e.step(warmup)
+        t_class[key] = time_steps(e, steps, torch) / steps
+        e.close()
+    t_step_ms = sum(t_class[(s["n_r_max"], s["m_max"])] for s in specs)
+    return len(specs) / (t_step_ms * 1e-3), {f"{k[0]}x{3 * k[1]}": v for k, v in t_class.items()}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=50)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--instances", type=int, default=256)
+    ap.add_argument("--seed", type=int, default=1234)
+    ap.add_argument("--no-plain", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    args.warmup = max(3, args.warmup)
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    specs = ensemble_specs(args.instances, seed=args.seed + 7919 * rank)
+
+    if args.impl == "reference":
+        if rank == 0:
+            reference_arm(args, specs)
+        return
+
+    import torch
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    from __graft_entry__ import build
+    build()
+    import pizza_gb300 as pz
+
+    ens = pz.Ensemble([gpu_cfg(s) for s in specs])
+    temps = [seeded_temp(s) for s in specs]
+    ens.set_state_all(temps)
+    ens.step(args.warmup)
+
+    # ---- device-resident timed region
+    clocks = Clocks()
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    clocks.start()
+    ms = time_steps(ens, args.steps, torch)
+    clk = clocks.stop()
+    if dist:
+        t = torch.tensor([ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    value = world * len(specs) * args.steps / (ms * 1e-3)
+
+    # ---- per-kernel device times (launched one by one, CUDA events)
+    kms = ens.profile_steps(max(3, min(10, args.steps)))
+    dom = max(kms, key=kms.get)
+    byts, flops = mloop_work(specs)
+    peak, peak_kind = measured_peaks()
+    mloop_ms = kms["k_mloop"]
+    achieved = byts / (mloop_ms * 1e-3) / 1e9
+    try:
+        fp64_peak = fp64_gemm_peak()
+    except Exception:
+        fp64_peak = None
+
+    # ---- e2e through the C ABI with host buffers
+    ens2 = pz.Ensemble([gpu_cfg(s) for s in specs])
+    rows = np.zeros((len(specs), pz.SERIES_COLS))
+    state_bytes = sum(t.size * 16 for t in temps)
+    t0 = time.perf_counter()
+    ens2.set_state_all(temps)
+    for _ in range(args.steps):
+        ens2.step(1, sync=False)
+        ens2.latest_rows(rows)
+    ens2.sync()
+    e2e_wall = time.perf_counter() - t0
+    ens2.close()
+    e2e = {"value": world * len(specs) * args.steps / e2e_wall, "unit": UNIT,
+           "h2d_bytes_per_step": int(state_bytes // args.steps),
+           "d2h_bytes_per_step": int(rows.nbytes),
+           "note": "set_state_all from host arrays, then per step pz_step + pz_latest_rows (one D2H of every "
+                   "instance's e_kin/heat row); wall clock"}
+
+    plain = None
+    if not args.no_plain:
+        plain_v, t_class = plain_rate(specs, max(5, min(args.steps, 20)), args.warmup, torch)
+        plain = {"value": plain_v, "per_step_ms_by_class": t_class}
+
+    if rank != 0:
+        return
+    cpu = None
+    if not args.no_cpu:
+        cpu = cpu_baseline(specs)
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": f"batched ensemble of {len(specs)} annulus instances per GPU (configs[2] shape): "
+                               "n_r_max in {33,49,65}, n_phi_max in {96,192,288}, Ra log-uniform [1e5,1e7], "
+                               "E in {1e-3,1e-4}, CNAB2, CFL 0.5, collocation + influence matrix",
+                   "instances": len(specs), "l2": "working set (operators + state, GBs) far larger than L2",
+                   "solve": "INFLUENCE"},
+        "plain_steps_per_s": plain["value"] if plain else None,
+        "batched_over_plain": (value / world / plain["value"]) if plain else None,
+        "plain_detail": plain,
+        "kernel_ms_per_step": kms,
+        "roofline": {"bound": "hbm", "kernel": "k_mloop", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak, "peak_kind": peak_kind, "traffic": None,
+                     "algorithmic_bytes": byts,
+                     "fp64": {"achieved_tflops": flops / (mloop_ms * 1e-3) / 1e12, "peak_tflops": fp64_peak,
+                              "peak_kind": "cuBLAS DGEMM 4096^3 measured in this run",
+                              "frac": (flops / (mloop_ms * 1e-3) / 1e12 / fp64_peak) if fp64_peak else None}},
+        "dominant_kernel": dom,
+        "cpu_baseline": cpu,
+        "e2e": e2e,
+        "gpu_launches": ens.launches_per_step() * args.steps,
+        "clocks": clk,
+    }
+    print(json.dumps(line))
+    if dist:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -139,6 +139,21 @@ int pz_get_dims(pz_handle* h, int inst, int* n_r_max, int* n_m_max, int* n_phi_m
 /* Number of device kernel launches one time step issues (all instances). */
 int pz_launches_per_step(pz_handle* h);
 
+/* Latest time-series row of every instance: n_instances x PZ_SERIES_COLS
+ * doubles, one device-to-host copy. */
+int pz_latest_rows(pz_handle* h, double* rows);
+
+/* The CUDA stream (cudaStream_t) all work of the handle is ordered on, for
+ * callers that time with CUDA events or order their own work after it. */
+void* pz_stream(pz_handle* h);
+
+/* Run n_steps steps launching the kernels one by one (no graph), with CUDA
+ * events between them on the handle's stream; kernel_ms[k] receives the mean
+ * device time per step of kernel k (k < pz_launches_per_step), names in
+ * pz_kernel_name(k).  Synchronises. */
+int pz_step_profile(pz_handle* h, int n_steps, double* kernel_ms);
+const char* pz_kernel_name(int k);
+
 /* Release all device memory of the handle. */
 int pz_destroy(pz_handle* h);
 

@@ -138,11 +138,18 @@ def load_library(path: str | None = None):
     lib.pz_get_series.argtypes = [ctypes.c_void_p, ctypes.c_int, dp, ctypes.POINTER(ctypes.c_int)]
     lib.pz_get_dims.argtypes = [ctypes.c_void_p, ctypes.c_int] + [ctypes.POINTER(ctypes.c_int)] * 3
     lib.pz_launches_per_step.argtypes = [ctypes.c_void_p]
+    lib.pz_latest_rows.argtypes = [ctypes.c_void_p, dp]
+    lib.pz_stream.argtypes = [ctypes.c_void_p]
+    lib.pz_stream.restype = ctypes.c_void_p
+    lib.pz_step_profile.argtypes = [ctypes.c_void_p, ctypes.c_int, dp]
+    lib.pz_kernel_name.argtypes = [ctypes.c_int]
+    lib.pz_kernel_name.restype = ctypes.c_char_p
     lib.pz_destroy.argtypes = [ctypes.c_void_p]
     lib.pz_last_error.argtypes = [ctypes.c_void_p]
     lib.pz_last_error.restype = ctypes.c_char_p
     for f in ("pz_create", "pz_set_state", "pz_set_state_all", "pz_step", "pz_sync", "pz_get_state",
-              "pz_get_series", "pz_get_dims", "pz_launches_per_step", "pz_destroy"):
+              "pz_get_series", "pz_get_dims", "pz_launches_per_step", "pz_latest_rows",
+              "pz_step_profile", "pz_destroy"):
         getattr(lib, f).restype = ctypes.c_int
     _lib = lib
     return lib
@@ -240,6 +247,25 @@ class Ensemble:
 
     def launches_per_step(self):
         return self.lib.pz_launches_per_step(self._h)
+
+    def latest_rows(self, out=None):
+        """Latest time-series row of every instance, shape (n_instances, 16)."""
+        if out is None:
+            out = np.zeros((len(self), SERIES_COLS))
+        self._check(self.lib.pz_latest_rows(self._h, _dptr(out)))
+        return out
+
+    @property
+    def stream_ptr(self) -> int:
+        """cudaStream_t of the handle (for torch.cuda.ExternalStream)."""
+        return int(self.lib.pz_stream(self._h) or 0)
+
+    def profile_steps(self, n_steps):
+        """Mean device ms per step of each kernel, launched one by one."""
+        nk = self.launches_per_step()
+        ms = np.zeros(nk)
+        self._check(self.lib.pz_step_profile(self._h, int(n_steps), _dptr(ms)))
+        return {self.lib.pz_kernel_name(k).decode(): float(ms[k]) for k in range(nk)}
 
     def close(self):
         if getattr(self, "_h", None):

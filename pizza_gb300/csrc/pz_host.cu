@@ -43,8 +43,7 @@ struct pz_handle {
   PzDev dev{};
   cudaStream_t stream = nullptr;
   cudaGraphExec_t graph = nullptr;
-  double* h_stage = nullptr;   // pinned staging buffer
-  long long h_stage_size = 0;
+  double* d_rows = nullptr;    // n_inst x PZ_SERIES_COLS gather buffer
   std::string err = "no error";
 };
 
@@ -436,7 +435,8 @@ extern "C" int pz_create(const pz_config* cfgs, int n, pz_handle** out) {
   }
   if ((e = cudaMalloc(&h->d_inst, n * sizeof(PzInst))) || (e = cudaMalloc(&h->d_state, n * sizeof(PzState))) ||
       (e = cudaMalloc(&h->d_ritems, ritems.size() * sizeof(PzItem))) ||
-      (e = cudaMalloc(&h->d_mitems, mitems.size() * sizeof(PzItem)))) {
+      (e = cudaMalloc(&h->d_mitems, mitems.size() * sizeof(PzItem))) ||
+      (e = cudaMalloc(&h->d_rows, (size_t)n * PZ_SERIES_COLS * sizeof(double)))) {
     g_create_error = std::string("device allocation: ") + cudaGetErrorString(e);
     pz_destroy(h);
     return PZ_E_NOMEM;
@@ -631,6 +631,47 @@ extern "C" int pz_launches_per_step(pz_handle* h) {
   return pz_step_launch_count();
 }
 
+extern "C" int pz_latest_rows(pz_handle* h, double* rows) {
+  if (!h || !rows) return fail(h, PZ_E_ARG, "pz_latest_rows: bad arguments");
+  cudaError_t e = pz_launch_gather_rows(h->dev, h->d_rows, h->stream);
+  if (!e) e = cudaMemcpyAsync(rows, h->d_rows, (size_t)h->n_inst * PZ_SERIES_COLS * sizeof(double),
+                              cudaMemcpyDeviceToHost, h->stream);
+  if (!e) e = cudaStreamSynchronize(h->stream);
+  if (e) return cuda_fail(h, e, "pz_latest_rows");
+  return PZ_OK;
+}
+
+extern "C" void* pz_stream(pz_handle* h) { return h ? (void*)h->stream : nullptr; }
+
+extern "C" int pz_step_profile(pz_handle* h, int n_steps, double* kernel_ms) {
+  if (!h || n_steps <= 0 || !kernel_ms) return fail(h, PZ_E_ARG, "pz_step_profile: bad arguments");
+  const int nk = pz_step_launch_count();
+  std::vector<cudaEvent_t> ev((size_t)n_steps * (nk + 1));
+  cudaError_t e = cudaSuccess;
+  for (auto& x : ev) if (!e) e = cudaEventCreate(&x);
+  if (e) return cuda_fail(h, e, "pz_step_profile events");
+  for (int s = 0; s < n_steps && !e; ++s) {
+    e = cudaEventRecord(ev[(size_t)s * (nk + 1)], h->stream);
+    for (int k = 0; k < nk && !e; ++k) {
+      e = pz_launch_step_kernel(h->dev, k, h->stream);
+      if (!e) e = cudaEventRecord(ev[(size_t)s * (nk + 1) + k + 1], h->stream);
+    }
+  }
+  if (!e) e = cudaStreamSynchronize(h->stream);
+  for (int k = 0; k < nk; ++k) kernel_ms[k] = 0.0;
+  for (int s = 0; s < n_steps && !e; ++s)
+    for (int k = 0; k < nk && !e; ++k) {
+      float ms = 0.f;
+      e = cudaEventElapsedTime(&ms, ev[(size_t)s * (nk + 1) + k], ev[(size_t)s * (nk + 1) + k + 1]);
+      kernel_ms[k] += ms / n_steps;
+    }
+  for (auto& x : ev) cudaEventDestroy(x);
+  if (e) return cuda_fail(h, e, "pz_step_profile");
+  return check_status(h);
+}
+
+extern "C" const char* pz_kernel_name(int k) { return pz_step_kernel_name(k); }
+
 extern "C" int pz_destroy(pz_handle* h) {
   if (!h) return PZ_OK;
   if (h->stream) cudaStreamSynchronize(h->stream);
@@ -640,6 +681,7 @@ extern "C" int pz_destroy(pz_handle* h) {
   cudaFree(h->d_state);
   cudaFree(h->d_ritems);
   cudaFree(h->d_mitems);
+  cudaFree(h->d_rows);
   if (h->stream) cudaStreamDestroy(h->stream);
   delete h;
   return PZ_OK;

@@ -127,6 +127,9 @@ cudaError_t pz_launch_build_static(const PzDev& d, cudaStream_t s);
 cudaError_t pz_launch_init_state(const PzDev& d, int only, cudaStream_t s);
 cudaError_t pz_launch_start(const PzDev& d, int only, cudaStream_t s);
 cudaError_t pz_launch_step(const PzDev& d, cudaStream_t s);
+cudaError_t pz_launch_step_kernel(const PzDev& d, int k, cudaStream_t s);
+const char* pz_step_kernel_name(int k);
 cudaError_t pz_launch_obs(const PzDev& d, int only, cudaStream_t s);
+cudaError_t pz_launch_gather_rows(const PzDev& d, double* out, cudaStream_t s);
 cudaError_t pz_setup_kernels();
 int pz_step_launch_count();

@@ -1199,6 +1199,17 @@ __global__ void k_init_state(PzDev d, int only) {
   d.state[inst] = S;
 }
 
+// latest time-series row of every instance into a contiguous buffer
+__global__ void k_gather_rows(PzDev d, double* out) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  const int inst = t / PZ_SERIES_COLS, c = t - inst * PZ_SERIES_COLS;
+  if (inst >= d.n_inst) return;
+  const PzInst& I = d.inst[inst];
+  const int cnt = d.state[inst].series_count;
+  const int idx = (cnt + PZ_SERIES_CAP - 1) % PZ_SERIES_CAP;
+  out[t] = d.pool[I.o_series + (long long)idx * PZ_SERIES_COLS + c];
+}
+
 size_t build_smem_bytes(int n) {
   long long off = (long long)n * n + 3LL * n + 32 + 16 + (n + 1) / 2;
   off = (off + 1) & ~1LL;
@@ -1244,11 +1255,33 @@ cudaError_t pz_launch_obs(const PzDev& d, int only, cudaStream_t s) {
 
 int pz_step_launch_count() { return 5; }
 
-cudaError_t pz_launch_step(const PzDev& d, cudaStream_t s) {
-  k_rloop<<<d.n_ritems, PZ_THREADS, rloop_smem_bytes(d.maxP), s>>>(d);
-  k_cfl<<<d.n_inst, 32, 0, s>>>(d);
-  k_build<<<d.n_mitems, PZ_THREADS, build_smem_bytes(d.maxN), s>>>(d);
-  k_mloop<<<d.n_mitems, PZ_THREADS, ms_smem_bytes(d.maxN), s>>>(d);
-  k_obs<<<d.n_inst, PZ_THREADS, 0, s>>>(d, -1);
+cudaError_t pz_launch_gather_rows(const PzDev& d, double* out, cudaStream_t s) {
+  const int n = d.n_inst * PZ_SERIES_COLS;
+  k_gather_rows<<<(n + 127) / 128, 128, 0, s>>>(d, out);
   return cudaGetLastError();
+}
+
+cudaError_t pz_launch_step_kernel(const PzDev& d, int k, cudaStream_t s) {
+  switch (k) {
+    case 0: k_rloop<<<d.n_ritems, PZ_THREADS, rloop_smem_bytes(d.maxP), s>>>(d); break;
+    case 1: k_cfl<<<d.n_inst, 32, 0, s>>>(d); break;
+    case 2: k_build<<<d.n_mitems, PZ_THREADS, build_smem_bytes(d.maxN), s>>>(d); break;
+    case 3: k_mloop<<<d.n_mitems, PZ_THREADS, ms_smem_bytes(d.maxN), s>>>(d); break;
+    case 4: k_obs<<<d.n_inst, PZ_THREADS, 0, s>>>(d, -1); break;
+    default: return cudaErrorInvalidValue;
+  }
+  return cudaGetLastError();
+}
+
+const char* pz_step_kernel_name(int k) {
+  static const char* names[5] = {"k_rloop", "k_cfl", "k_build", "k_mloop", "k_obs"};
+  return (k >= 0 && k < 5) ? names[k] : "";
+}
+
+cudaError_t pz_launch_step(const PzDev& d, cudaStream_t s) {
+  for (int k = 0; k < 5; ++k) {
+    const cudaError_t e = pz_launch_step_kernel(d, k, s);
+    if (e) return e;
+  }
+  return cudaSuccess;
 }

@@ -114,9 +114,9 @@ def test_multistep_schemes(pz, scheme):
 
 def test_dt_change_rebuilds_operators(pz):
     """CFL-driven dt changes (hysteresis, dt_fac) rebuild the dt-dependent operators."""
-    spec = dict(n_r_max=33, m_max=32, ek=1e-3, ra=3e5, l_ek_pump=True, dtMax=3e-4, courfac=0.5,
+    spec = dict(n_r_max=33, m_max=32, ek=1e-3, ra=3e5, l_ek_pump=True, dtMax=1e-4, courfac=10.0,
                 matrix_solve="INFLUENCE")
-    sim, ens, out = run_pair(pz, spec, 150, seed=2, amp=3e-3)
+    sim, ens, out = run_pair(pz, spec, 150, seed=2, amp=3e-3)   # dt changes 3 times
     g = out[-1][2]
     assert g["dt"] != spec["dtMax"], "the run must change dt"
     assert abs(g["dt"] - sim.ts.dt[0]) <= 1e-12 * sim.ts.dt[0]
