@@ -154,6 +154,21 @@ void* pz_stream(pz_handle* h);
 int pz_step_profile(pz_handle* h, int n_steps, double* kernel_ms);
 const char* pz_kernel_name(int k);
 
+/* Explicit (nonlinear) terms of instance `inst` for one stage, from caller
+ * device arrays: replaces transp_Mloc_to_Rloc, radial_loop,
+ * transp_Rloc_to_Mloc and finish_explicit_assembly of the collocation
+ * influence-matrix path (src/step_time.f90:222-269, src/radial_loop.f90:231-394,
+ * src/mloop.f90:169-229).  us, up, om, temp: physical-space complex (n_m, n_r)
+ * device arrays (n_m fastest, like the reference's *_Mloc).  Outputs:
+ * dTdt_expl and dpsidt_expl, complex (n_m, n_r) device arrays, and dtr, dth,
+ * n_r_max doubles each (the per-radius Courant steps of src/courant.f90:41-76,
+ * evaluated with the instance's courfac).  Ordered on the handle's stream,
+ * asynchronous; device memory for 2*n_m_max*n_r_max complex intermediates is
+ * taken with cudaMallocAsync on that stream and released after the call. */
+int pz_explicit_terms(pz_handle* h, int inst, const double* us, const double* up,
+                      const double* om, const double* temp, double* dTdt_expl,
+                      double* dpsidt_expl, double* dtr, double* dth);
+
 /* Release all device memory of the handle. */
 int pz_destroy(pz_handle* h);
 

@@ -18,6 +18,7 @@
 
 #include "pizza_gpu.h"
 #include "pz_internal.h"
+#include "pz_stage.h"
 
 namespace {
 
@@ -671,6 +672,38 @@ extern "C" int pz_step_profile(pz_handle* h, int n_steps, double* kernel_ms) {
 }
 
 extern "C" const char* pz_kernel_name(int k) { return pz_step_kernel_name(k); }
+
+extern "C" int pz_explicit_terms(pz_handle* h, int inst, const double* us, const double* up, const double* om,
+                                 const double* temp, double* dTdt_expl, double* dpsidt_expl, double* dtr,
+                                 double* dth) {
+  if (!h) return fail(nullptr, PZ_E_ARG, "pz_explicit_terms: null handle");
+  if (inst < 0 || inst >= h->n_inst) return fail(h, PZ_E_ARG, "pz_explicit_terms: instance out of range");
+  if (!us || !up || !om || !temp || !dTdt_expl || !dpsidt_expl || !dtr || !dth)
+    return fail(h, PZ_E_ARG, "pz_explicit_terms: null array");
+  const PzInst& I = h->inst[inst];
+  void* scratch = nullptr;
+  const size_t bytes = pz_expl_scratch_bytes(I.N, I.M);
+  cudaError_t e = cudaMallocAsync(&scratch, bytes, h->stream);
+  if (e) return cuda_fail(h, e, "pz_explicit_terms scratch");
+  PzExplArgs a;
+  a.inst = h->d_inst + inst;
+  a.pool = h->pool;
+  a.us = reinterpret_cast<const double2*>(us);
+  a.up = reinterpret_cast<const double2*>(up);
+  a.om = reinterpret_cast<const double2*>(om);
+  a.temp = reinterpret_cast<const double2*>(temp);
+  a.dTdt = reinterpret_cast<double2*>(dTdt_expl);
+  a.dpsidt = reinterpret_cast<double2*>(dpsidt_expl);
+  a.dtr = dtr;
+  a.dth = dth;
+  a.s_dVsT = reinterpret_cast<double2*>(scratch);
+  a.s_dVsOm = a.s_dVsT + (size_t)I.N * I.M;
+  e = pz_launch_explicit_terms(a, I.N, I.M, I.P, h->stream);
+  const cudaError_t e2 = cudaFreeAsync(scratch, h->stream);
+  if (e) return cuda_fail(h, e, "pz_explicit_terms");
+  if (e2) return cuda_fail(h, e2, "pz_explicit_terms scratch release");
+  return PZ_OK;
+}
 
 extern "C" int pz_destroy(pz_handle* h) {
   if (!h) return PZ_OK;

@@ -1,0 +1,23 @@
+// Arguments and launcher of the stage-level explicit-terms kernels (pz_stage.cu).
+#pragma once
+#include <cuda_runtime.h>
+
+#include "pz_internal.h"
+
+struct PzExplArgs {
+  const PzInst* inst;      // device pointer to the instance descriptor
+  double* pool;            // the handle's pool (operators, radial functions)
+  const double2* us;       // (n_m, n_r), n_m fastest, physical space
+  const double2* up;
+  const double2* om;
+  const double2* temp;
+  double2* dTdt;           // out: dTdt%expl(:,:,istage)   (n_m, n_r)
+  double2* dpsidt;         // out: dpsidt%expl(:,:,istage) (n_m, n_r)
+  double* dtr;             // out: radial Courant step per radius
+  double* dth;             // out: horizontal Courant step per radius
+  double2* s_dVsT;         // scratch: n_m_max * n_r_max complex
+  double2* s_dVsOm;        // scratch: n_m_max * n_r_max complex
+};
+
+size_t pz_expl_scratch_bytes(int n_r_max, int n_m_max);
+cudaError_t pz_launch_explicit_terms(const PzExplArgs& a, int N, int M, int P, cudaStream_t s);

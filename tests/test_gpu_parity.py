@@ -163,3 +163,29 @@ def test_nonfinite_state_is_reported(pz):
         ens.set_state(0, temp=t)
         ens.step(1)
     assert e.value.code == -5
+
+
+def test_explicit_terms_entry_point_matches_oracle(pz):
+    """pz_explicit_terms on caller device arrays = the oracle's radial_loop +
+    finish_explicit_assembly for the same state."""
+    import torch
+    spec = C0
+    sim = oracle(spec, temp0=seeded(spec, 4))
+    for _ in range(3):
+        sim.advance()
+    state = {f: getattr(sim, f).copy() for f in ("us", "up", "om", "temp")}
+    sim.ts.istage = 1                       # stage 1 of the next step
+    dtempdt, dVsT, dpsidt, dVsOm = sim.radial_loop()
+    sim.dTdt.expl[0] = dtempdt
+    sim.dpsidt.expl[0] = dpsidt
+    sim.finish_explicit(dVsT, dVsOm)
+    ens = pz.Ensemble(gpu_config(spec))
+    dev = {f: torch.from_numpy(np.ascontiguousarray(state[f].T)).cuda() for f in state}
+    torch.cuda.synchronize()
+    for _ in range(2):
+        out = ens.explicit_terms(0, dev["us"], dev["up"], dev["om"], dev["temp"])
+        ens.sync()
+        assert rel_err(out[0].cpu().numpy().T, sim.dTdt.expl[0]) < 1e-12
+        assert rel_err(out[1].cpu().numpy().T, sim.dpsidt.expl[0]) < 1e-12
+        np.testing.assert_allclose(out[2].cpu().numpy(), sim.dtr, rtol=1e-12)
+        np.testing.assert_allclose(out[3].cpu().numpy(), sim.dth, rtol=1e-12)
