@@ -169,6 +169,26 @@ int pz_explicit_terms(pz_handle* h, int inst, const double* us, const double* up
                       const double* om, const double* temp, double* dTdt_expl,
                       double* dpsidt_expl, double* dtr, double* dth);
 
+/* No counterpart in the reference.  pz_explicit_terms without any device
+ * allocation, for callers that cannot allocate when they need the explicit
+ * terms: a host capturing its own CUDA graph, or one whose device memory is all
+ * handed out by its own pool allocator.  Same arguments, results and stream
+ * as pz_explicit_terms; its intermediates live in a static device array of
+ * 2*PZ_NOALLOC_MAX_MN complex values (1 MiB) that every GPU loading the library
+ * keeps until the process exits.  Limits and rules:
+ *  - n_m_max*n_r_max of the instance must not exceed PZ_NOALLOC_MAX_MN, else
+ *    PZ_E_ARG with a message;
+ *  - call it with the handle's device current; the first call on a device
+ *    looks up the array's device address (cudaGetSymbolAddress), so make that
+ *    first call before any stream capture;
+ *  - all calls on a device share the array: calls that overlap on the GPU
+ *    race, so order them (one stream, or events).  Nothing needs clearing
+ *    between calls. */
+#define PZ_NOALLOC_MAX_MN 32768
+int pz_explicit_terms_noalloc(pz_handle* h, int inst, const double* us, const double* up,
+                              const double* om, const double* temp, double* dTdt_expl,
+                              double* dpsidt_expl, double* dtr, double* dth);
+
 /* Release all device memory of the handle. */
 int pz_destroy(pz_handle* h);
 

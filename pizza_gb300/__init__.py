@@ -146,12 +146,13 @@ def load_library(path: str | None = None):
     lib.pz_kernel_name.restype = ctypes.c_char_p
     vp = ctypes.c_void_p
     lib.pz_explicit_terms.argtypes = [vp, ctypes.c_int, vp, vp, vp, vp, vp, vp, vp, vp]
+    lib.pz_explicit_terms_noalloc.argtypes = [vp, ctypes.c_int, vp, vp, vp, vp, vp, vp, vp, vp]
     lib.pz_destroy.argtypes = [ctypes.c_void_p]
     lib.pz_last_error.argtypes = [ctypes.c_void_p]
     lib.pz_last_error.restype = ctypes.c_char_p
     for f in ("pz_create", "pz_set_state", "pz_set_state_all", "pz_step", "pz_sync", "pz_get_state",
               "pz_get_series", "pz_get_dims", "pz_launches_per_step", "pz_latest_rows",
-              "pz_step_profile", "pz_explicit_terms", "pz_destroy"):
+              "pz_step_profile", "pz_explicit_terms", "pz_explicit_terms_noalloc", "pz_destroy"):
         getattr(lib, f).restype = ctypes.c_int
     _lib = lib
     return lib
@@ -247,12 +248,15 @@ class Ensemble:
         self._check(self.lib.pz_get_series(self._h, i, _dptr(rows), ctypes.byref(n)))
         return rows[: n.value].copy()
 
-    def explicit_terms(self, i, us, up, om, temp, out=None):
+    def explicit_terms(self, i, us, up, om, temp, out=None, noalloc=False):
         """Explicit terms of instance i from device tensors (anything with
         ``data_ptr()``, e.g. torch complex128 CUDA tensors of shape
         (n_r_max, n_m_max) row-major, i.e. the reference's (n_m, n_r) layout
         with n_m fastest).  Returns (dTdt_expl, dpsidt_expl, dtr, dth) in the
-        given or newly created torch tensors; ordered on the handle's stream."""
+        given or newly created torch tensors; ordered on the handle's stream.
+        ``noalloc=True`` calls pz_explicit_terms_noalloc, which takes no device
+        memory (its intermediates live in a static device array shared by all
+        calls on the device; overlapping calls race)."""
         import torch
         n, m, _ = self.dims[i]
         dev = us.device
@@ -264,9 +268,9 @@ class Ensemble:
         for t in (us, up, om, temp) + tuple(out[:2]):
             if tuple(t.shape) != (n, m) or t.dtype != torch.complex128 or not t.is_contiguous():
                 raise ValueError(f"expected contiguous complex128 tensors of shape {(n, m)}")
-        self._check(self.lib.pz_explicit_terms(self._h, i, us.data_ptr(), up.data_ptr(), om.data_ptr(),
-                                               temp.data_ptr(), out[0].data_ptr(), out[1].data_ptr(),
-                                               out[2].data_ptr(), out[3].data_ptr()))
+        fn = self.lib.pz_explicit_terms_noalloc if noalloc else self.lib.pz_explicit_terms
+        self._check(fn(self._h, i, us.data_ptr(), up.data_ptr(), om.data_ptr(), temp.data_ptr(),
+                       out[0].data_ptr(), out[1].data_ptr(), out[2].data_ptr(), out[3].data_ptr()))
         return out
 
     def launches_per_step(self):

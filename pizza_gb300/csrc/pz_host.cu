@@ -705,6 +705,35 @@ extern "C" int pz_explicit_terms(pz_handle* h, int inst, const double* us, const
   return PZ_OK;
 }
 
+int pz_expl_args(pz_handle* h, int inst, const double* us, const double* up, const double* om, const double* temp,
+                 double* dTdt_expl, double* dpsidt_expl, double* dtr, double* dth, PzExplArgs* a, int* N, int* M,
+                 int* P, cudaStream_t* s) {
+  if (!h) return fail(nullptr, PZ_E_ARG, "null handle");
+  if (inst < 0 || inst >= h->n_inst) return fail(h, PZ_E_ARG, "instance out of range");
+  if (!us || !up || !om || !temp || !dTdt_expl || !dpsidt_expl || !dtr || !dth)
+    return fail(h, PZ_E_ARG, "null array");
+  const PzInst& I = h->inst[inst];
+  a->inst = h->d_inst + inst;
+  a->pool = h->pool;
+  a->us = reinterpret_cast<const double2*>(us);
+  a->up = reinterpret_cast<const double2*>(up);
+  a->om = reinterpret_cast<const double2*>(om);
+  a->temp = reinterpret_cast<const double2*>(temp);
+  a->dTdt = reinterpret_cast<double2*>(dTdt_expl);
+  a->dpsidt = reinterpret_cast<double2*>(dpsidt_expl);
+  a->dtr = dtr;
+  a->dth = dth;
+  a->s_dVsT = nullptr;
+  a->s_dVsOm = nullptr;
+  *N = I.N;
+  *M = I.M;
+  *P = I.P;
+  *s = h->stream;
+  return PZ_OK;
+}
+
+int pz_record_error(pz_handle* h, int code, const char* msg) { return fail(h, code, msg); }
+
 extern "C" int pz_destroy(pz_handle* h) {
   if (!h) return PZ_OK;
   if (h->stream) cudaStreamSynchronize(h->stream);

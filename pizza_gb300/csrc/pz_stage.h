@@ -21,3 +21,13 @@ struct PzExplArgs {
 
 size_t pz_expl_scratch_bytes(int n_r_max, int n_m_max);
 cudaError_t pz_launch_explicit_terms(const PzExplArgs& a, int N, int M, int P, cudaStream_t s);
+
+// Arguments of instance `inst` of a handle for the explicit-terms kernels,
+// without scratch (the caller sets s_dVsT / s_dVsOm), plus its sizes and
+// stream.  Validates the handle, the instance index and the array pointers;
+// on error returns a PZ_E_* code and records the message in the handle.
+struct pz_handle;
+int pz_expl_args(pz_handle* h, int inst, const double* us, const double* up, const double* om,
+                 const double* temp, double* dTdt_expl, double* dpsidt_expl, double* dtr, double* dth,
+                 PzExplArgs* a, int* N, int* M, int* P, cudaStream_t* s);
+int pz_record_error(pz_handle* h, int code, const char* msg);
