@@ -3,12 +3,15 @@
 Workload (configs[2] shape, the configuration the headline metric is quoted
 on): a batched ensemble of B independent annulus instances of uneven size,
 n_r_max in {33, 49, 65}, n_phi_max in {96, 192, 288} (m_max = n_phi_max/3),
-log10 Ra ~ U[5, 7], E in {1e-3, 1e-4}, Pr = 1, radius ratio 0.35, Ekman
-pumping, CNAB2 with per-instance CFL time steps (courfac 0.5, dtMax =
-min(1e-4, 0.03/sqrt(Ra))), collocation with the influence-matrix solve, each
-instance started from its own seeded temperature perturbation of amplitude
-1e-3 (synthetic data: the reference publishes no dataset).  One step advances
-every instance by one time step.
+log10 Ra ~ U[5, log10 Ra_max(n_r_max)] with Ra_max = 1e6, 3e6, 1e7 for
+n_r_max = 33, 49, 65 (the resolution that keeps a 500-step run stable; 1e7 at
+n_r_max = 33 is not), E in {1e-3, 1e-4}, Pr = 1, radius ratio 0.35, Ekman
+pumping, CNAB2 with per-instance CFL time steps at CFL number 0.5 (pizza's
+courfac = 2: dt = dr / (courfac |u|)), dtMax = min(1e-4, 0.03/sqrt(Ra)),
+collocation with the influence-matrix solve, each instance started from its
+own seeded temperature perturbation of amplitude 1e-3 (synthetic data: the
+reference publishes no dataset).  One step advances every instance by one
+time step; the default timed region is configs[2]'s 500 steps.
 
 Metric: aggregate instance-steps/s of the batched step (``value``), next to the
 plain one-instance-per-handle GPU step of the same instances
@@ -38,6 +41,7 @@ METRIC = "aggregate steps/s batched vs plain GPU step at 1e-10 rel err; adjoint/
 UNIT = "instance-steps/s"
 NS = (33, 49, 65)
 PS = (96, 192, 288)
+RA_MAX = {33: 1.0e6, 49: 3.0e6, 65: 1.0e7}
 
 
 def ensemble_specs(n_inst: int, seed: int = 1234):
@@ -47,10 +51,10 @@ def ensemble_specs(n_inst: int, seed: int = 1234):
     for i in range(n_inst):
         N = int(rng.choice(NS))
         P = int(rng.choice(PS))
-        ra = float(10.0 ** rng.uniform(5.0, 7.0))
+        ra = float(10.0 ** rng.uniform(5.0, math.log10(RA_MAX[N])))
         ek = float(rng.choice([1e-3, 1e-4]))
         specs.append(dict(n_r_max=N, n_cheb_max=N, m_max=P // 3, ra=ra, ek=ek, pr=1.0, radratio=0.35,
-                          l_ek_pump=True, time_scheme="CNAB2", courfac=0.5,
+                          l_ek_pump=True, time_scheme="CNAB2", courfac=2.0,
                           dtMax=min(1e-4, 0.03 / math.sqrt(ra)), matrix_solve="INFLUENCE",
                           seed=int(seed * 1000 + i)))
     return specs
@@ -90,8 +94,10 @@ def mloop_work(specs, nold=1, nimp=1, nexp=2):
     (2 (nold + nimp + nexp) complex N-vectors), and what it writes (T, dT/dr,
     us, up, om, psi, two explicit, two old and two implicit slots: 12 complex
     N-vectors).  The Chebyshev operators shared by all m of one size are
-    counted once per size.  Flops: 14 real-operator x complex-vector products
-    of 4N^2 flops per m (m = 0: 10), elementwise work neglected.
+    counted once per size.  Flops: per m, 3 dense real-operator x complex-vector
+    products (4N^2 flops each: the per-m operators) and 11 products with the
+    parity-compact Chebyshev operators (2N^2 flops each); m = 0: 2 dense and 8
+    compact.  Elementwise work is neglected.
     """
     byts = 0.0
     flops = 0.0
@@ -102,7 +108,7 @@ def mloop_work(specs, nold=1, nimp=1, nexp=2):
         per_m = 8.0 * 3 * N * N + 8.0 * (4 * N + 4) + 16.0 * N * (6 + 2 * (nold + nimp + nexp) + 12)
         m0 = 8.0 * 2 * N * N + 16.0 * N * (6 + 2 * (nold + nimp + nexp) + 12)
         byts += (M - 1) * per_m + m0
-        flops += (M - 1) * 14 * 4.0 * N * N + 10 * 4.0 * N * N
+        flops += (M - 1) * (3 * 4.0 + 11 * 2.0) * N * N + (2 * 4.0 + 8 * 2.0) * N * N
     for N in sizes:
         byts += 8.0 * 4 * N * N
     return byts, flops
@@ -279,8 +285,8 @@ def plain_rate(specs, steps, warmup, torch):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=50)
-    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--steps", type=int, default=500)
+    ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--instances", type=int, default=256)
     ap.add_argument("--seed", type=int, default=1234)
@@ -373,8 +379,9 @@ def main():
         "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64", "data": "synthetic",
         "config": {"workload": f"batched ensemble of {len(specs)} annulus instances per GPU (configs[2] shape): "
-                               "n_r_max in {33,49,65}, n_phi_max in {96,192,288}, Ra log-uniform [1e5,1e7], "
-                               "E in {1e-3,1e-4}, CNAB2, CFL 0.5, collocation + influence matrix",
+                               "n_r_max in {33,49,65}, n_phi_max in {96,192,288}, Ra log-uniform [1e5, Ra_max(N)] "
+                               "with Ra_max = 1e6/3e6/1e7 for N = 33/49/65, E in {1e-3,1e-4}, CNAB2, CFL 0.5, "
+                               "collocation + influence matrix",
                    "instances": len(specs), "l2": "working set (operators + state, GBs) far larger than L2",
                    "solve": "INFLUENCE"},
         "plain_steps_per_s": plain["value"] if plain else None,

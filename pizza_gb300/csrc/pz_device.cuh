@@ -202,4 +202,146 @@ __device__ double2* fft_run(double2* a, double2* b, const PzInst& I, const doubl
   return src;
 }
 
+// ---------------------------------------------------------------------------
+// operator products with one (row, re/im) task per lane
+// ---------------------------------------------------------------------------
+// y = A x, A column-major n x n, x complex: lane t computes component (t & 1)
+// of row (t >> 1).  Two lanes share each matrix element (broadcast load).
+__device__ __forceinline__ void mv_lanes(const double* __restrict__ A, int n, const double2* __restrict__ x,
+                                         double2* __restrict__ y) {
+  const double* xs = reinterpret_cast<const double*>(x);
+  double* ys = reinterpret_cast<double*>(y);
+  for (int t = threadIdx.x; t < 2 * n; t += blockDim.x) {
+    const int row = t >> 1, c = t & 1;
+    const double* a = A + row;
+    double acc = 0.0;
+#pragma unroll 4
+    for (int j = 0; j < n; ++j) acc = fma(__ldg(a + (long long)j * n), xs[2 * j + c], acc);
+    ys[t] = acc;
+  }
+}
+
+// Parity-compact products.  Rows of the compact matrix A (nrow x L,
+// column-major) take their input from v0 (even row) or v1 (odd row); lane t
+// computes component (t & 1) of row (t >> 1) into out[t].
+__device__ __forceinline__ void sym_dot(const double* __restrict__ A, int nrow, int L,
+                                        const double2* __restrict__ v0, const double2* __restrict__ v1,
+                                        double* __restrict__ out) {
+  for (int t = threadIdx.x; t < 2 * nrow; t += blockDim.x) {
+    const int row = t >> 1, c = t & 1;
+    const double* v = reinterpret_cast<const double*>((row & 1) ? v1 : v0) + c;
+    const double* a = A + row;
+    double acc = 0.0;
+#pragma unroll 4
+    for (int j = 0; j < L; ++j) acc = fma(__ldg(a + (long long)j * nrow), v[2 * j], acc);
+    out[t] = acc;
+  }
+}
+__device__ __forceinline__ void sym_dot2(const double* __restrict__ A, const double* __restrict__ B, int nrow,
+                                         int L, const double2* __restrict__ v0, const double2* __restrict__ v1,
+                                         double* __restrict__ outA, double* __restrict__ outB) {
+  for (int t = threadIdx.x; t < 2 * nrow; t += blockDim.x) {
+    const int row = t >> 1, c = t & 1;
+    const double* v = reinterpret_cast<const double*>((row & 1) ? v1 : v0) + c;
+    double acca = 0.0, accb = 0.0;
+#pragma unroll 4
+    for (int j = 0; j < L; ++j) {
+      const double x = v[2 * j];
+      acca = fma(__ldg(A + row + (long long)j * nrow), x, acca);
+      accb = fma(__ldg(B + row + (long long)j * nrow), x, accb);
+    }
+    outA[t] = acca;
+    outB[t] = accb;
+  }
+}
+
+// s_j = x_j + x_{n-1-j}, a_j = x_j - x_{n-1-j} (j < n/2); odd n: s_h = x_h, a_h = 0
+__device__ __forceinline__ void prep_sa(const double2* __restrict__ x, int n, double2* __restrict__ s,
+                                        double2* __restrict__ a) {
+  const int h = n / 2, h2 = (n + 1) / 2;
+  for (int j = threadIdx.x; j < h2; j += blockDim.x) {
+    if (j < h) {
+      const double2 p = x[j], q = x[n - 1 - j];
+      s[j] = make_double2(p.x + q.x, p.y + q.y);
+      a[j] = make_double2(p.x - q.x, p.y - q.y);
+    } else {
+      s[j] = x[j];
+      a[j] = make_double2(0.0, 0.0);
+    }
+  }
+}
+// xe_k = x_{2k}, xo_k = x_{2k+1} (zero past the end)
+__device__ __forceinline__ void prep_eo(const double2* __restrict__ x, int n, double2* __restrict__ xe,
+                                        double2* __restrict__ xo) {
+  const int h2 = (n + 1) / 2;
+  for (int k = threadIdx.x; k < h2; k += blockDim.x) {
+    xe[k] = x[2 * k];
+    xo[k] = (2 * k + 1 < n) ? x[2 * k + 1] : make_double2(0.0, 0.0);
+  }
+}
+// out holds rows (2i: E or u, 2i+1: O or v) x (re, im); y_i = E + O and
+// y_{n-1-i} = se*E + so*O (i < n/2)
+__device__ __forceinline__ void sym_combine(const double* __restrict__ out, int n, double se, double so,
+                                            double2* __restrict__ y) {
+  const int h = n / 2, h2 = (n + 1) / 2;
+  for (int i = threadIdx.x; i < h2; i += blockDim.x) {
+    const double er = out[4 * i], ei = out[4 * i + 1], orr = out[4 * i + 2], oi = out[4 * i + 3];
+    y[i] = make_double2(er + orr, ei + oi);
+    if (i < h) y[n - 1 - i] = make_double2(se * er + so * orr, se * ei + so * oi);
+  }
+}
+
+// Scratch of the parity products: s, a (h2 complex each) and two task
+// buffers of 4*h2 doubles.
+struct SymScratch {
+  double2* s; double2* a; double* t1; double* t2;
+};
+
+// y = C x (DCT-I, costf1)
+__device__ void op_C(const View& V, int n, const double2* x, double2* y, SymScratch& w) {
+  const int h2 = (n + 1) / 2;
+  prep_sa(x, n, w.s, w.a);
+  __syncthreads();
+  sym_dot(V.basis(BM_CS), n, h2, w.s, w.a, reinterpret_cast<double*>(y));
+}
+// (y1, y2) = (D1c x, D2c x): Chebyshev coefficients -> physical derivatives
+__device__ void op_Dc2(const View& V, int n, const double2* x, double2* y1, double2* y2, SymScratch& w) {
+  const int h2 = (n + 1) / 2;
+  prep_eo(x, n, w.s, w.a);
+  __syncthreads();
+  sym_dot2(V.basis(BM_D1CS), V.basis(BM_D2CS), 2 * h2, h2, w.s, w.a, w.t1, w.t2);
+  __syncthreads();
+  sym_combine(w.t1, n, -1.0, 1.0, y1);
+  sym_combine(w.t2, n, 1.0, -1.0, y2);
+}
+// y1 = D1c x
+__device__ void op_D1c(const View& V, int n, const double2* x, double2* y1, SymScratch& w) {
+  const int h2 = (n + 1) / 2;
+  prep_eo(x, n, w.s, w.a);
+  __syncthreads();
+  sym_dot(V.basis(BM_D1CS), 2 * h2, h2, w.s, w.a, w.t1);
+  __syncthreads();
+  sym_combine(w.t1, n, -1.0, 1.0, y1);
+}
+// (y1, y2) = (D1p x, D2p x): physical -> physical derivatives
+__device__ void op_Dp2(const View& V, int n, const double2* x, double2* y1, double2* y2, SymScratch& w) {
+  const int h2 = (n + 1) / 2;
+  prep_sa(x, n, w.s, w.a);
+  __syncthreads();
+  sym_dot2(V.basis(BM_D1PS), V.basis(BM_D2PS), 2 * h2, h2, w.s, w.a, w.t1, w.t2);
+  __syncthreads();
+  // y_i = u + v ; y_{n-1-i} = sigma (u - v), sigma = -1 (D1p), +1 (D2p)
+  sym_combine(w.t1, n, -1.0, 1.0, y1);
+  sym_combine(w.t2, n, 1.0, -1.0, y2);
+}
+// y1 = D1p x
+__device__ void op_D1p(const View& V, int n, const double2* x, double2* y1, SymScratch& w) {
+  const int h2 = (n + 1) / 2;
+  prep_sa(x, n, w.s, w.a);
+  __syncthreads();
+  sym_dot(V.basis(BM_D1PS), 2 * h2, h2, w.s, w.a, w.t1);
+  __syncthreads();
+  sym_combine(w.t1, n, -1.0, 1.0, y1);
+}
+
 }  // namespace

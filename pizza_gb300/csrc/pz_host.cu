@@ -66,7 +66,44 @@ int cuda_fail(pz_handle* h, cudaError_t e, const char* what) {
 struct Basis {
   int N;
   std::vector<double> x, C, D1c, D2c, D1p, D2p, rMat, drMat, d2rMat;
+  std::vector<double> Cs, D1cs, D2cs, D1ps, D2ps;   // parity-compact forms
 };
+
+// Parity-compact operators (see BM_CS..BM_D2PS in pz_internal.h).  The
+// Gauss-Lobatto grid is symmetric, x_{N-1-i} = -x_i, so
+//   C(k, N-1-j)      = (-1)^k C(k, j),
+//   D1c(N-1-i, k)    = (-1)^(k+1) D1c(i, k),   D2c(N-1-i, k) = (-1)^k D2c(i, k),
+//   D1p(N-1-i,N-1-j) = -D1p(i, j),             D2p(N-1-i,N-1-j) = D2p(i, j),
+// and each product needs about half the multiply-adds of the dense form.
+void make_compact(Basis& b) {
+  const int N = b.N, h = N / 2, h2 = (N + 1) / 2, R = 2 * h2;
+  auto A = [N](const std::vector<double>& M, int i, int j) { return M[i + (size_t)j * N]; };
+  b.Cs.assign((size_t)N * h2, 0.0);
+  for (int k = 0; k < N; ++k)
+    for (int j = 0; j < h2; ++j) b.Cs[k + (size_t)j * N] = A(b.C, k, j);
+  for (int w = 0; w < 2; ++w) {
+    const std::vector<double>& D = w == 0 ? b.D1c : b.D2c;
+    std::vector<double>& out = w == 0 ? b.D1cs : b.D2cs;
+    out.assign((size_t)R * h2, 0.0);
+    for (int i = 0; i < h2; ++i)
+      for (int kk = 0; kk < h2; ++kk) {
+        out[(2 * i) + (size_t)kk * R] = A(D, i, 2 * kk);
+        if (2 * kk + 1 < N) out[(2 * i + 1) + (size_t)kk * R] = A(D, i, 2 * kk + 1);
+      }
+  }
+  for (int w = 0; w < 2; ++w) {
+    const std::vector<double>& D = w == 0 ? b.D1p : b.D2p;
+    std::vector<double>& out = w == 0 ? b.D1ps : b.D2ps;
+    out.assign((size_t)R * h2, 0.0);
+    for (int i = 0; i < h2; ++i) {
+      for (int j = 0; j < h; ++j) {
+        out[(2 * i) + (size_t)j * R] = 0.5 * (A(D, i, j) + A(D, i, N - 1 - j));
+        out[(2 * i + 1) + (size_t)j * R] = 0.5 * (A(D, i, j) - A(D, i, N - 1 - j));
+      }
+      if (N % 2 == 1) out[(2 * i) + (size_t)h * R] = A(D, i, h);
+    }
+  }
+}
 
 Basis make_basis(int N, double r_icb, double r_cmb) {
   Basis b;
@@ -124,6 +161,7 @@ Basis make_basis(int N, double r_icb, double r_cmb) {
   };
   b.D1p = matmul(b.D1c, b.C);
   b.D2p = matmul(b.D2c, b.C);
+  make_compact(b);
   return b;
 }
 
@@ -402,8 +440,9 @@ extern "C" int pz_create(const pz_config* cfgs, int n, pz_handle** out) {
       const Basis& B = kv.second;
       const long long NN = (long long)B.N * B.N;
       double* dst = img.data() + basis_off[kv.first];
-      const std::vector<double>* mats[BM_COUNT] = {&B.C, &B.D1c, &B.D2c, &B.D1p, &B.D2p, &B.rMat, &B.drMat, &B.d2rMat};
-      for (int k = 0; k < BM_COUNT; ++k) std::memcpy(dst + k * NN, mats[k]->data(), NN * sizeof(double));
+      const std::vector<double>* mats[BM_COUNT] = {&B.C,    &B.D1c,  &B.D2c,  &B.D1p,  &B.D2p,  &B.rMat, &B.drMat,
+                                                   &B.d2rMat, &B.Cs, &B.D1cs, &B.D2cs, &B.D1ps, &B.D2ps};
+      for (int k = 0; k < BM_COUNT; ++k) std::memcpy(dst + k * NN, mats[k]->data(), mats[k]->size() * sizeof(double));
     }
     const long double pi = 3.141592653589793238462643383279502884L;
     for (auto& kv : tw_off) {

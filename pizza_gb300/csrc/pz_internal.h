@@ -52,6 +52,14 @@ enum {
   BM_RMAT,    // T_k(x_i)    rMat of chebyshev.f90:281-383 (matrix builders)
   BM_DRMAT,   // T_k'(x_i)   drMat
   BM_D2RMAT,  // T_k''(x_i)  d2rMat
+  // parity-compact forms (h = N/2, h2 = (N+1)/2), used by the sym_* products:
+  BM_CS,      // C, N x h2: column j < h pairs with s_j = x_j + x_{N-1-j} (even k) or
+              // a_j = x_j - x_{N-1-j} (odd k); column h (odd N) is the middle point
+  BM_D1CS,    // D1c, 2*h2 x h2: row 2i = even-degree columns of row i, 2i+1 = odd
+  BM_D2CS,    // D2c, same layout
+  BM_D1PS,    // D1p, 2*h2 x h2: row 2i = (D(i,j)+D(i,N-1-j))/2 (j<h), D(i,h) (odd N);
+              //      row 2i+1 = (D(i,j)-D(i,N-1-j))/2 (j<h), 0
+  BM_D2PS,    // D2p, same layout
   BM_COUNT
 };
 

@@ -563,6 +563,7 @@ __global__ void __launch_bounds__(PZ_THREADS) k_build(PzDev d) {
 // ---------------------------------------------------------------------------
 struct MS {   // per-m vectors in shared memory
   double2 *a, *b, *c, *e, *f, *g, *h, *k;
+  SymScratch w;
   double* red;
 };
 
@@ -579,7 +580,7 @@ __device__ void imp_from_physical(const View& V, const PzInst& I, int mi, int bo
   double2* up = V.fld(F_UP, mi);
   for (int i = threadIdx.x; i < n; i += blockDim.x) s.a[i] = T[i];
   __syncthreads();
-  mv2(V.basis(BM_D1P), V.basis(BM_D2P), n, s.a, s.b, s.c);
+  op_Dp2(V, n, s.a, s.b, s.c, s.w);
   __syncthreads();
   double2* oT = V.hist(0, 0, bo, mi);
   double2* iT = V.hist(0, 1, bi, mi);
@@ -603,7 +604,7 @@ __device__ void imp_from_physical(const View& V, const PzInst& I, int mi, int bo
     for (int i = threadIdx.x; i < n; i += blockDim.x) s.a[i] = om[i];
   }
   __syncthreads();
-  mv2(V.basis(BM_D1P), V.basis(BM_D2P), n, s.a, s.b, s.c);
+  op_Dp2(V, n, s.a, s.b, s.c, s.w);
   __syncthreads();
   for (int i = threadIdx.x; i < n; i += blockDim.x) {
     const double2 x = s.a[i], d1 = s.b[i], d2 = s.c[i];
@@ -632,9 +633,14 @@ __device__ void imp_from_physical(const View& V, const PzInst& I, int mi, int bo
 
 __device__ MS ms_smem(int n) {
   extern __shared__ double2 shm[];
+  const int h2 = (n + 1) / 2;
   MS s;
   s.a = shm; s.b = s.a + n; s.c = s.b + n; s.e = s.c + n; s.f = s.e + n; s.g = s.f + n; s.h = s.g + n; s.k = s.h + n;
-  s.red = reinterpret_cast<double*>(s.k + n);
+  s.w.s = s.k + n;
+  s.w.a = s.w.s + h2;
+  s.w.t1 = reinterpret_cast<double*>(s.w.a + h2);
+  s.w.t2 = s.w.t1 + 4 * h2;
+  s.red = s.w.t2 + 4 * h2;
   return s;
 }
 
@@ -664,7 +670,7 @@ __global__ void __launch_bounds__(PZ_THREADS) k_start(PzDev d, int only) {
   const double* or1 = V.rad(RV_OR1);
   for (int i = threadIdx.x; i < n; i += blockDim.x) { s.a[i] = up[i]; psi[i] = make_double2(0.0, 0.0); }
   __syncthreads();
-  mv1(V.basis(BM_D1P), n, n, s.a, s.b);
+  op_D1p(V, n, s.a, s.b, s.w);
   __syncthreads();
   for (int i = threadIdx.x; i < n; i += blockDim.x) {
     // om = d(up)/dr + up/r - (i m / r) us
@@ -700,7 +706,7 @@ __device__ __forceinline__ double2 imex_rhs(const View& V, const PzInst& I, cons
   return acc;
 }
 
-__global__ void __launch_bounds__(PZ_THREADS) k_mloop(PzDev d) {
+__global__ void __launch_bounds__(256) k_mloop(PzDev d) {
   const PzItem it = d.mitems[blockIdx.x];
   const PzInst& I = d.inst[it.inst];
   PzState& Sg = d.state[it.inst];
@@ -734,8 +740,9 @@ __global__ void __launch_bounds__(PZ_THREADS) k_mloop(PzDev d) {
     s.e[i] = V.fld(F_DVSOM, mi)[i];
   }
   __syncthreads();
-  mv1(V.basis(BM_D1P), n, n, s.a, s.b);
-  mv1(V.basis(BM_D1P), n, n, s.e, s.f);
+  op_D1p(V, n, s.a, s.b, s.w);
+  __syncthreads();
+  op_D1p(V, n, s.e, s.f, s.w);
   __syncthreads();
   {
     double2* eT = V.hist(0, 2, S.r_expl, mi);
@@ -783,9 +790,11 @@ __global__ void __launch_bounds__(PZ_THREADS) k_mloop(PzDev d) {
     s.a[i] = (i == 0 || i == n - 1) ? make_double2(0.0, 0.0) : v;   // topt = bott = 0
   }
   __syncthreads();
-  mv1(d.pool + I.o_gt + (long long)mi * n * n, n, n, s.a, s.b);           // Chebyshev T
+  mv_lanes(d.pool + I.o_gt + (long long)mi * n * n, n, s.a, s.b);        // Chebyshev T
   __syncthreads();
-  mv3(V.basis(BM_D1C), V.basis(BM_D2C), V.basis(BM_C), n, s.b, s.c, s.e, s.f);
+  op_Dc2(V, n, s.b, s.c, s.e, s.w);                                       // dT/dr, d2T/dr2
+  __syncthreads();
+  op_C(V, n, s.b, s.f, s.w);                                              // T (physical)
   __syncthreads();
   bool bad = false;
   {
@@ -820,9 +829,11 @@ __global__ void __launch_bounds__(PZ_THREADS) k_mloop(PzDev d) {
   double2* oP = V.hist(1, 0, S.b_old, mi);
   double2* iP = V.hist(1, 1, S.b_impl, mi);
   if (m == 0) {
-    mv1(d.pool + I.o_guphi, n, n, s.a, s.b);            // uphi, Chebyshev
+    mv_lanes(d.pool + I.o_guphi, n, s.a, s.b);           // uphi, Chebyshev
     __syncthreads();
-    mv3(V.basis(BM_D1C), V.basis(BM_D2C), V.basis(BM_C), n, s.b, s.c, s.e, s.g);
+    op_Dc2(V, n, s.b, s.c, s.e, s.w);
+    __syncthreads();
+    op_C(V, n, s.b, s.g, s.w);
     __syncthreads();
     const double* ekp = ekpump;
     for (int i = threadIdx.x; i < n; i += blockDim.x) {
@@ -837,14 +848,14 @@ __global__ void __launch_bounds__(PZ_THREADS) k_mloop(PzDev d) {
         iP[i] = make_double2(I.ViscFac * (d2u + or1[i] * du - or2[i] * u) - I.CorFac * ekp[i] * u, 0.0);
     }
   } else {
-    mv1(d.pool + I.o_gom + (long long)mi * n * n, n, n, s.a, s.b);   // omega, Chebyshev
+    mv_lanes(d.pool + I.o_gom + (long long)mi * n * n, n, s.a, s.b);  // omega, Chebyshev
     __syncthreads();
-    mv1(V.basis(BM_C), n, n, s.b, s.c);                             // omega, physical
+    op_C(V, n, s.b, s.c, s.w);                                       // omega, physical
     __syncthreads();
     for (int i = threadIdx.x; i < n; i += blockDim.x)
       s.a[i] = (i == 0 || i == n - 1) ? make_double2(0.0, 0.0) : make_double2(-s.c[i].x, -s.c[i].y);
     __syncthreads();
-    mv1(d.pool + I.o_gpsi + (long long)mi * n * n, n, n, s.a, s.e);  // psi, Chebyshev
+    mv_lanes(d.pool + I.o_gpsi + (long long)mi * n * n, n, s.a, s.e);  // psi, Chebyshev
     __syncthreads();
     // influence-matrix correction (update_psi_coll_dmat.f90:1256-1300)
     const double* bct = V.rad(RV_BCTOP);
@@ -875,7 +886,9 @@ __global__ void __launch_bounds__(PZ_THREADS) k_mloop(PzDev d) {
       s.b[i] = o;
     }
     __syncthreads();
-    mv2(V.basis(BM_D1C), V.basis(BM_C), n, s.e, s.g, s.h);            // dpsi/dr, psi
+    op_D1c(V, n, s.e, s.g, s.w);                                     // dpsi/dr
+    __syncthreads();
+    op_C(V, n, s.e, s.h, s.w);                                       // psi
     __syncthreads();
     for (int i = threadIdx.x; i < n; i += blockDim.x) {
       const double2 p = s.h[i], dp = s.g[i];
@@ -883,7 +896,9 @@ __global__ void __launch_bounds__(PZ_THREADS) k_mloop(PzDev d) {
       us[i] = cscale(or1[i], cim(dm, p));
       up[i] = make_double2(-dp.x - beta[i] * p.x, -dp.y - beta[i] * p.y);
     }
-    mv3(V.basis(BM_D1C), V.basis(BM_D2C), V.basis(BM_C), n, s.b, s.c, s.a, s.k);   // dom, d2om, om
+    op_Dc2(V, n, s.b, s.c, s.a, s.w);                                // dom, d2om
+    __syncthreads();
+    op_C(V, n, s.b, s.k, s.w);                                       // om
     __syncthreads();
     for (int i = threadIdx.x; i < n; i += blockDim.x) {
       const double2 o = s.k[i], d1 = s.c[i], d2 = s.a[i];
@@ -1023,7 +1038,17 @@ size_t build_smem_bytes(int n) {
   off += 4LL * n;
   return (size_t)off * sizeof(double);
 }
-size_t ms_smem_bytes(int n) { return 8 * (size_t)n * sizeof(double2) + 64 * sizeof(double); }
+size_t ms_smem_bytes(int n) {
+  const size_t h2 = (size_t)(n + 1) / 2;
+  return 8 * (size_t)n * sizeof(double2) + 2 * h2 * sizeof(double2) + 8 * h2 * sizeof(double) + 64 * sizeof(double);
+}
+// threads of the per-m kernels: one lane per (row, re/im) task of the
+// widest product, rounded up to whole warps
+int mloop_threads(int maxN) {
+  const int h2 = (maxN + 1) / 2;
+  const int t = 2 * maxN > 4 * h2 ? 2 * maxN : 4 * h2;
+  return ((t + 31) / 32) * 32;
+}
 size_t rloop_smem_bytes(int P) { return 5 * (size_t)P * sizeof(double2); }
 
 }  // namespace
@@ -1073,7 +1098,7 @@ cudaError_t pz_launch_step_kernel(const PzDev& d, int k, cudaStream_t s) {
     case 0: k_rloop<<<d.n_ritems, PZ_THREADS, rloop_smem_bytes(d.maxP), s>>>(d); break;
     case 1: k_cfl<<<d.n_inst, 32, 0, s>>>(d); break;
     case 2: k_build<<<d.n_mitems, PZ_THREADS, build_smem_bytes(d.maxN), s>>>(d); break;
-    case 3: k_mloop<<<d.n_mitems, PZ_THREADS, ms_smem_bytes(d.maxN), s>>>(d); break;
+    case 3: k_mloop<<<d.n_mitems, mloop_threads(d.maxN), ms_smem_bytes(d.maxN), s>>>(d); break;
     case 4: k_obs<<<d.n_inst, PZ_THREADS, 0, s>>>(d, -1); break;
     default: return cudaErrorInvalidValue;
   }
