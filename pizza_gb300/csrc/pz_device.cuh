@@ -140,24 +140,32 @@ __device__ __forceinline__ void mv3(const double* __restrict__ A, const double* 
 // phi-FFT: mixed-radix Stockham autosort on nb transforms in shared memory
 // ---------------------------------------------------------------------------
 // One stage of radix R with running product p (product of earlier radices).
-// tw[k] = exp(-2 pi i k / P); sgn = +1 selects the backward transform.
+// tw[k] = exp(-2 pi i k / P) in global memory; `backward` selects the
+// conjugate twiddles.  Twiddles of the first stage (p = 1) are all 1.
 __device__ void fft_stage(const double2* __restrict__ x, double2* __restrict__ y, int P, int R, int p,
                           const double2* __restrict__ tw, int nb, bool backward) {
   const int T = P / R;
   const int tstep = P / (p * R);
   const int rstep = P / R;
+  const double sg = backward ? -1.0 : 1.0;
   for (int w = threadIdx.x; w < nb * T; w += blockDim.x) {
     const int b = w / T, i = w - b * T;
     const int k = i % p;
     const double2* xb = x + b * P;
     double2* yb = y + b * P;
     double2 u[PZ_MAX_RADIX];
+    u[0] = xb[i];
 #pragma unroll
-    for (int q = 0; q < PZ_MAX_RADIX; ++q) {
+    for (int q = 1; q < PZ_MAX_RADIX; ++q) {
       if (q < R) {
-        double2 t = tw[(q * k * tstep) % P];
-        if (backward) t.y = -t.y;
-        u[q] = cmul(xb[i + q * T], t);
+        const double2 v = xb[i + q * T];
+        if (k == 0) {
+          u[q] = v;
+        } else {
+          double2 t = __ldg(tw + (q * k * tstep) % P);
+          t.y *= sg;
+          u[q] = cmul(v, t);
+        }
       }
     }
     const int base = (i - k) * R + k;
@@ -173,15 +181,25 @@ __device__ void fft_stage(const double2* __restrict__ x, double2* __restrict__ y
       yb[base + p] = cadd(d02, jd13);
       yb[base + 2 * p] = csub(s02, s13);
       yb[base + 3 * p] = csub(d02, jd13);
+    } else if (R == 3) {
+      // W = c - i sg*sn with c = cos(2 pi/3), sn = sin(2 pi/3) from the table
+      const double2 w1 = __ldg(tw + rstep);
+      const double c = w1.x, sn = -w1.y * sg;
+      const double2 s12 = cadd(u[1], u[2]), d12 = csub(u[1], u[2]);
+      const double2 m = make_double2(u[0].x + c * s12.x, u[0].y + c * s12.y);
+      const double2 jd = make_double2(sn * d12.y, -sn * d12.x);   // -i sn d
+      yb[base] = cadd(u[0], s12);
+      yb[base + p] = cadd(m, jd);
+      yb[base + 2 * p] = csub(m, jd);
     } else {
-      for (int s = 0; s < R; ++s) {
+      for (int s2 = 0; s2 < R; ++s2) {
         double2 acc = u[0];
         for (int q = 1; q < R; ++q) {
-          double2 t = tw[((s * q) % R) * rstep];
-          if (backward) t.y = -t.y;
+          double2 t = __ldg(tw + ((s2 * q) % R) * rstep);
+          t.y *= sg;
           acc = cadd(acc, cmul(u[q], t));
         }
-        yb[base + s * p] = acc;
+        yb[base + s2 * p] = acc;
       }
     }
   }
@@ -200,6 +218,106 @@ __device__ double2* fft_run(double2* a, double2* b, const PzInst& I, const doubl
     double2* t = src; src = dst; dst = t;
   }
   return src;
+}
+
+// ---------------------------------------------------------------------------
+// radial_loop for a group of radii of one instance (src/radial_loop.f90:231-394,
+// ifft/fft of src/fft_fftw.f90:44-90).  IO supplies the inputs (us, up, om, T
+// at (m, r)) and takes the outputs (dT/dt, dVsT, dpsi/dt, dVsOm at (m, r), and
+// the Courant steps of radius r).  The two real fields of each pair are packed
+// into one complex FFT (us + i up, om + i T on the way to the grid; the
+// products r us T + i up T and r us om + i up om on the way back).
+// Shared memory: 4*G*P complex (two ping-pong buffers of 2*G transforms) and
+// 3*G + G*M doubles.
+template <class IO>
+__device__ void rloop_group(const PzInst& I, const View& V, int r0, IO& io, double2* sh, double* rsh) {
+  const int N = I.N, M = I.M, P = I.P;
+  const int G = min(PZ_RLOOP_G, N - r0);
+  const double2* tw = reinterpret_cast<const double2*>(V.pool + I.o_tw);
+  double2* za = sh;                  // [g][2][P]
+  double2* zb = sh + 2 * G * P;
+  double* usom = rsh;                // [G]
+  double* vr = rsh + G;              // [G]
+  double* vh = rsh + 2 * G;          // [G]
+  double* prod = rsh + 3 * G;        // [G][M] Reynolds-stress terms
+  for (int k = threadIdx.x; k < 2 * G * P; k += blockDim.x) za[k] = make_double2(0.0, 0.0);
+  for (int k = threadIdx.x; k < 3 * G; k += blockDim.x) rsh[k] = 0.0;
+  __syncthreads();
+  // spectra at the G radii; Reynolds stress of the m=0 equation
+  for (int t = threadIdx.x; t < G * M; t += blockDim.x) {
+    const int g = t / M, m = t - g * M, r = r0 + g;
+    double2 a = io.in(0, m, r), b = io.in(1, m, r), c = io.in(2, m, r), e = io.in(3, m, r);
+    double us_om;
+    if (m == 0) {
+      // us_fluct(m=0) = E CorFac ekpump up(m=0) / 2 (radial_loop.f90:267-278)
+      us_om = 0.5 * I.ek * I.CorFac * V.rad(RV_EKPUMP)[r] * b.x * c.x;
+      a.y = 0.0; b.y = 0.0; c.y = 0.0; e.y = 0.0;   // c2r ignores Im of the DC term
+    } else {
+      us_om = 2.0 * (a.x * c.x + a.y * c.y);
+    }
+    prod[g * M + m] = us_om;
+    double2* z1 = za + (2 * g) * P;
+    double2* z2 = za + (2 * g + 1) * P;
+    z1[m] = make_double2(a.x - b.y, a.y + b.x);
+    z2[m] = make_double2(c.x - e.y, c.y + e.x);
+    if (m > 0) {
+      z1[P - m] = make_double2(a.x + b.y, -a.y + b.x);
+      z2[P - m] = make_double2(c.x + e.y, -c.y + e.x);
+    }
+  }
+  __syncthreads();
+  {
+    // deterministic sum over m of the Reynolds-stress terms, one warp per radius
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    for (int g = wid; g < G; g += nw) {
+      double acc = 0.0;
+      for (int m = lane; m < M; m += 32) acc += prod[g * M + m];
+      acc = warp_sum(acc);
+      if (lane == 0) usom[g] = acc;
+    }
+  }
+  double2* g1 = fft_run(za, zb, I, tw, 2 * G, true);
+  double2* h = (g1 == za) ? zb : za;
+  // Courant velocities and the nonlinear products on the grid
+  for (int t = threadIdx.x; t < G * P; t += blockDim.x) {
+    const int g = t / P, j = t - g * P;
+    const double rr = V.rad(RV_R)[r0 + g];
+    const double2 z1 = g1[(2 * g) * P + j], z2 = g1[(2 * g + 1) * P + j];
+    const double usg = z1.x, upg = z1.y, omg = z2.x, Tg = z2.y;
+    // squares are >= 0: their bit patterns order like unsigned integers
+    atomicMax(reinterpret_cast<unsigned long long*>(&vr[g]), (unsigned long long)__double_as_longlong(usg * usg));
+    atomicMax(reinterpret_cast<unsigned long long*>(&vh[g]), (unsigned long long)__double_as_longlong(upg * upg));
+    h[(2 * g) * P + j] = make_double2(rr * usg * Tg, upg * Tg);
+    h[(2 * g + 1) * P + j] = make_double2(rr * usg * omg, upg * omg);
+  }
+  __syncthreads();
+  for (int g = threadIdx.x; g < G; g += blockDim.x) {
+    // courant (src/courant.f90:41-76)
+    const int r = r0 + g;
+    const double vr2 = I.courfac * I.courfac * vr[g], vh2 = I.courfac * I.courfac * vh[g];
+    double dtr = 1.0e10, dth = 1.0e10;
+    if (vr2 != 0.0) dtr = fmin(dtr, sqrt(V.rad(RV_DELXR2)[r] / vr2));
+    if (vh2 != 0.0) dth = fmin(dth, sqrt(V.rad(RV_DELXH2)[r] / vh2));
+    io.cfl(r, dtr, dth);
+  }
+  double2* f = fft_run(h, g1, I, tw, 2 * G, false);
+  for (int t = threadIdx.x; t < G * M; t += blockDim.x) {
+    const int g = t / M, m = t - g * M, r = r0 + g;
+    const double or1 = V.rad(RV_OR1)[r];
+    const double tfac = (1.0 - I.tadvz) * V.rad(RV_BETA)[r] * or1;
+    const int mc = (P - m) % P;
+    const double2* f1 = f + (2 * g) * P;
+    const double2* f2 = f + (2 * g + 1) * P;
+    // split the two real transforms packed in one complex FFT
+    const double2 Z = f1[m], Zc = f1[mc], Y = f2[m], Yc = f2[mc];
+    const double2 vsT = make_double2(0.5 * (Z.x + Zc.x) / (double)P, 0.5 * (Z.y - Zc.y) / (double)P);
+    const double2 upT = make_double2(0.5 * (Z.y + Zc.y) / (double)P, -0.5 * (Z.x - Zc.x) / (double)P);
+    const double2 vsOm = make_double2(0.5 * (Y.x + Yc.x) / (double)P, 0.5 * (Y.y - Yc.y) / (double)P);
+    const double2 upOm = make_double2(0.5 * (Y.y + Yc.y) / (double)P, -0.5 * (Y.x - Yc.x) / (double)P);
+    const double tm = or1 * (double)(m * I.minc);
+    io.out(m, r, make_double2(tm * upT.y - tfac * vsT.x, -tm * upT.x - tfac * vsT.y), vsT,
+           (m == 0) ? make_double2(-usom[g], 0.0) : make_double2(tm * upOm.y, -tm * upOm.x), vsOm);
+  }
 }
 
 // ---------------------------------------------------------------------------

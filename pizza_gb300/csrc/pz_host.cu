@@ -218,7 +218,7 @@ int validate(const pz_config& c, std::string* why) {
   if (c.n_r_max < 5 || c.n_r_max > 128) return bad("n_r_max must be in [5, 128]");
   if (c.n_cheb_max < 2 || c.n_cheb_max > c.n_r_max) return bad("n_cheb_max must be in [2, n_r_max]");
   if (c.minc != 1) return uns("minc != 1 is not implemented");
-  if (c.m_max < 2 || c.m_max > 512) return bad("m_max must be in [2, 512]");
+  if (c.m_max < 2 || c.m_max > 256) return bad("m_max must be in [2, 256]");
   if (c.ra == 0.0) return uns("ra = 0 (no temperature equation) is not implemented");
   if (c.pr <= 0.0) return bad("pr must be > 0");
   if (!(c.radratio > 0.0 && c.radratio < 1.0)) return uns("radratio must be in (0, 1): the full disk is not implemented");
@@ -303,6 +303,10 @@ extern "C" int pz_create(const pz_config* cfgs, int n, pz_handle** out) {
     if (c.l_ek_pump) I.flags |= PZF_EK_PUMP;
     if (non_rot) I.flags |= PZF_NON_ROT;
     if (imp_calc) I.flags |= PZF_IMP_CALC;
+    // get_tempMat and get_omMat (update_temp_coll.f90:310-393,
+    // update_psi_coll_dmat.f90:829-911) build the same rows when
+    // TdiffFac*hdif_T == ViscFac*hdif_V and both use fixed/no-slip boundary rows
+    if (I.TdiffFac == I.ViscFac) I.flags |= PZF_T_IS_OM;
     const int N = I.N;
     I.rnorm = std::sqrt(2.0 / (double)(N - 1));
     I.r_cmb = 1.0 / (1.0 - c.radratio);
@@ -470,7 +474,7 @@ extern "C" int pz_create(const pz_config* cfgs, int n, pz_handle** out) {
   });
   std::vector<PzItem> ritems, mitems;
   for (int i : order) {
-    for (int r = 0; r < h->inst[i].N; ++r) ritems.push_back({i, r});
+    for (int r = 0; r < h->inst[i].N; r += PZ_RLOOP_G) ritems.push_back({i, r});
     for (int m = 0; m < h->inst[i].M; ++m) mitems.push_back({i, m});
   }
   if ((e = cudaMalloc(&h->d_inst, n * sizeof(PzInst))) || (e = cudaMalloc(&h->d_state, n * sizeof(PzState))) ||

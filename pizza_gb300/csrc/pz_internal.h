@@ -20,6 +20,8 @@
 
 #define PZ_MAX_RADIX 8
 #define PZ_SERIES_CAP 1024
+#define PZ_RLOOP_G 4        // radii per block of the phi-transform kernels
+#define PZ_SMEM_MAX (227 * 1024)
 
 // flag bits of PzInst::flags
 enum {
@@ -29,6 +31,9 @@ enum {
   PZF_EK_PUMP  = 8,    // Ekman pumping
   PZF_NON_ROT  = 16,   // non-rotating
   PZF_IMP_CALC = 32,   // scheme computes the implicit term each step
+  PZF_T_IS_OM  = 64,   // TdiffFac == ViscFac (Pr = 1, no hyperdiffusion): the
+                       // temperature and vorticity operators of each m /= 0 are
+                       // the same matrix; one inverse serves both solves
 };
 
 // radial vectors, each N doubles, at o_rad + RV_xxx*N

@@ -140,110 +140,50 @@ __device__ void bridge_with_cnab2(const PzInst& I, PzState& S) {
 }
 
 // ---------------------------------------------------------------------------
-// k_rloop: radial_loop for one radius of one instance
-// (src/radial_loop.f90:231-394 with ifft/fft of src/fft_fftw.f90:44-90)
+// k_rloop: radial_loop for PZ_RLOOP_G radii of one instance, reading the
+// m-major step state and writing the explicit slot, dVsT, dVsOm and the
+// Courant steps (src/radial_loop.f90:231-394)
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(PZ_THREADS) k_rloop(PzDev d) {
-  extern __shared__ double2 sh[];
-  __shared__ double red[32];
-  const PzItem it = d.ritems[blockIdx.x];
-  const PzInst& I = d.inst[it.inst];
-  PzState& S = d.state[it.inst];
-  if (S.status != 0) return;
-  const View V{&I, d.pool};
-  const int N = I.N, M = I.M, P = I.P, r = it.idx;
-  double2* tw = sh;              // P
-  double2* za = sh + P;          // 2P: z1 | z2
-  double2* zb = sh + 3 * P;      // 2P
-  const double2* gtw = reinterpret_cast<const double2*>(d.pool + I.o_tw);
-  for (int k = threadIdx.x; k < P; k += blockDim.x) tw[k] = gtw[k];
-  for (int k = threadIdx.x; k < 2 * P; k += blockDim.x) za[k] = make_double2(0.0, 0.0);
-  __syncthreads();
-
-  const double rr = V.rad(RV_R)[r];
-  const double or1 = V.rad(RV_OR1)[r];
-  const double beta = V.rad(RV_BETA)[r];
-  const double ekpump = V.rad(RV_EKPUMP)[r];
-  const double2* us = V.fld(F_US, 0);
-  const double2* up = V.fld(F_UP, 0);
-  const double2* om = V.fld(F_OM, 0);
-  const double2* T = V.fld(F_TEMP, 0);
-  // Hermitian spectra of the pairs (us + i up) and (om + i T); Reynolds stress
-  double usom = 0.0;
-  for (int m = threadIdx.x; m < M; m += blockDim.x) {
-    double2 a = us[(long long)m * N + r], b = up[(long long)m * N + r];
-    double2 c = om[(long long)m * N + r], e = T[(long long)m * N + r];
-    if (m == 0) {
-      const double usf = 0.5 * I.ek * I.CorFac * ekpump * b.x;  // us_fluct(m=0)
-      usom += usf * c.x;
-      a.y = 0.0; b.y = 0.0; c.y = 0.0; e.y = 0.0;   // c2r ignores Im of the DC term
-    } else {
-      usom += 2.0 * (a.x * c.x + a.y * c.y);
-    }
-    const int mm = m;   // FFT index n_m (fft_fftw.f90:55-62)
-    za[mm] = make_double2(a.x - b.y, a.y + b.x);
-    za[P + mm] = make_double2(c.x - e.y, c.y + e.x);
-    if (mm > 0) {
-      za[P - mm] = make_double2(a.x + b.y, -a.y + b.x);
-      za[2 * P - mm] = make_double2(c.x + e.y, -c.y + e.x);
-    }
+struct StepIO {
+  View V;
+  int N;
+  double2 *us, *up, *om, *T, *eT, *eP, *vsT, *vsOm;
+  double* cflv;
+  __device__ double2 in(int f, int m, int r) const {
+    const long long o = (long long)m * N + r;
+    return f == 0 ? us[o] : f == 1 ? up[o] : f == 2 ? om[o] : T[o];
   }
-  usom = block_sum(usom, red);
-  double2* g = fft_run(za, zb, I, tw, 2, true);   // g[0..P): us + i up, g[P..2P): om + i T
-  double2* h = (g == za) ? zb : za;
-  // CFL and products
-  double vr = 0.0, vh = 0.0;
-  for (int j = threadIdx.x; j < P; j += blockDim.x) {
-    const double2 z1 = g[j], z2 = g[P + j];
-    const double usg = z1.x, upg = z1.y, omg = z2.x, Tg = z2.y;
-    vr = fmax(vr, usg * usg);
-    vh = fmax(vh, upg * upg);
-    h[j] = make_double2(rr * usg * Tg, upg * Tg);            // usT + i upT
-    h[P + j] = make_double2(rr * usg * omg, upg * omg);      // usOm + i upOm
-  }
-  vr = block_max(vr, red);
-  vh = block_max(vh, red);
-  if (threadIdx.x == 0) {
-    // courant (src/courant.f90:41-76)
-    double* cfl = d.pool + I.o_cfl;
-    const double vr2 = I.courfac * I.courfac * vr, vh2 = I.courfac * I.courfac * vh;
-    double dtr = 1.0e10, dth = 1.0e10;
-    if (vr2 != 0.0) dtr = fmin(dtr, sqrt(V.rad(RV_DELXR2)[r] / vr2));
-    if (vh2 != 0.0) dth = fmin(dth, sqrt(V.rad(RV_DELXH2)[r] / vh2));
-    cfl[r] = dtr;
-    cfl[N + r] = dth;
-  }
-  __syncthreads();
-  double2* f = fft_run(h, g, I, tw, 2, false);
-  double2* eT = V.hist(0, 2, S.b_expl, 0);
-  double2* eP = V.hist(1, 2, S.b_expl, 0);
-  double2* dVsT = V.fld(F_DVST, 0);
-  double2* dVsOm = V.fld(F_DVSOM, 0);
-  const double tfac = (1.0 - I.tadvz) * beta * or1;
-  for (int m = threadIdx.x; m < M; m += blockDim.x) {
-    const int mm = m;
-    const int mc = (P - mm) % P;
-    const double dm = (double)(m * I.minc);
-    // split the two real transforms packed in one complex FFT
-    const double2 Z = f[mm], Zc = f[mc];
-    const double2 A = make_double2(0.5 * (Z.x + Zc.x), 0.5 * (Z.y - Zc.y));   // FFT(usT)
-    const double2 B = make_double2(0.5 * (Z.y + Zc.y), -0.5 * (Z.x - Zc.x));  // FFT(upT)
-    const double2 Y = f[P + mm], Yc = f[P + mc];
-    const double2 C = make_double2(0.5 * (Y.x + Yc.x), 0.5 * (Y.y - Yc.y));   // FFT(usOm)
-    const double2 D = make_double2(0.5 * (Y.y + Yc.y), -0.5 * (Y.x - Yc.x));  // FFT(upOm)
-    const double2 vsT = make_double2(A.x / (double)P, A.y / (double)P);
-    const double2 upT = make_double2(B.x / (double)P, B.y / (double)P);
-    const double2 vsOm = make_double2(C.x / (double)P, C.y / (double)P);
-    const double2 upOm = make_double2(D.x / (double)P, D.y / (double)P);
-    const double t = or1 * dm;
-    const double2 dtdt = make_double2(t * upT.y - tfac * vsT.x, -t * upT.x - tfac * vsT.y);
-    const double2 dpdt = (m == 0) ? make_double2(-usom, 0.0) : make_double2(t * upOm.y, -t * upOm.x);
+  __device__ void out(int m, int r, double2 dtdt, double2 vst, double2 dpdt, double2 vsom) const {
     const long long o = (long long)m * N + r;
     eT[o] = dtdt;
-    dVsT[o] = vsT;
+    vsT[o] = vst;
     eP[o] = dpdt;
-    dVsOm[o] = vsOm;
+    vsOm[o] = vsom;
   }
+  __device__ void cfl(int r, double dtr, double dth) const {
+    cflv[r] = dtr;
+    cflv[N + r] = dth;
+  }
+};
+
+__global__ void __launch_bounds__(256) k_rloop(PzDev d) {
+  extern __shared__ double2 sh[];
+  const PzItem it = d.ritems[blockIdx.x];
+  const PzInst& I = d.inst[it.inst];
+  const PzState& S = d.state[it.inst];
+  if (S.status != 0) return;
+  const View V{&I, d.pool};
+  StepIO io;
+  io.V = V;
+  io.N = I.N;
+  io.us = V.fld(F_US, 0); io.up = V.fld(F_UP, 0); io.om = V.fld(F_OM, 0); io.T = V.fld(F_TEMP, 0);
+  io.eT = V.hist(0, 2, S.b_expl, 0);
+  io.eP = V.hist(1, 2, S.b_expl, 0);
+  io.vsT = V.fld(F_DVST, 0);
+  io.vsOm = V.fld(F_DVSOM, 0);
+  io.cflv = d.pool + I.o_cfl;
+  double* rsh = reinterpret_cast<double*>(sh + 4 * PZ_RLOOP_G * I.P);
+  rloop_group(I, V, it.idx, io, sh, rsh);
 }
 
 // ---------------------------------------------------------------------------
@@ -493,12 +433,15 @@ __global__ void __launch_bounds__(PZ_THREADS) k_build(PzDev d) {
   const double wlin = S.wimp_lin[0];
   BuildSmem s = build_smem(n);
   BuildCtx B{&I, V.basis(BM_RMAT), V.basis(BM_DRMAT), V.basis(BM_D2RMAT), n};
-  // temperature (get_tempMat with WITH_PRECOND_S: row scaling only)
-  fill_matrix(s.A, B, V, 0, m, wlin);
-  equilibrate(s.A, n, s.f1, s.f2, false);
-  if (gj_invert(s.A, n, s.piv, s.colk, s.red, s.redi) != 0) { flag_status(S, PZ_E_SINGULAR); return; }
-  store_op(d.pool + I.o_gt + (long long)mi * n * n, s.A, n, I.n_max, nullptr, s.f1);
-  __syncthreads();
+  const bool shared = (I.flags & PZF_T_IS_OM) && m != 0;
+  if (!shared) {
+    // temperature (get_tempMat with WITH_PRECOND_S: row scaling only)
+    fill_matrix(s.A, B, V, 0, m, wlin);
+    equilibrate(s.A, n, s.f1, s.f2, false);
+    if (gj_invert(s.A, n, s.piv, s.colk, s.red, s.redi) != 0) { flag_status(S, PZ_E_SINGULAR); return; }
+    store_op(d.pool + I.o_gt + (long long)mi * n * n, s.A, n, I.n_max, nullptr, s.f1);
+    __syncthreads();
+  }
   if (m == 0) {
     fill_matrix(s.A, B, V, 3, 0, wlin);
     if (gj_invert(s.A, n, s.piv, s.colk, s.red, s.redi) != 0) { flag_status(S, PZ_E_SINGULAR); return; }
@@ -790,7 +733,9 @@ __global__ void __launch_bounds__(256) k_mloop(PzDev d) {
     s.a[i] = (i == 0 || i == n - 1) ? make_double2(0.0, 0.0) : v;   // topt = bott = 0
   }
   __syncthreads();
-  mv_lanes(d.pool + I.o_gt + (long long)mi * n * n, n, s.a, s.b);        // Chebyshev T
+  const double* GT = ((I.flags & PZF_T_IS_OM) && m != 0) ? d.pool + I.o_gom + (long long)mi * n * n
+                                                         : d.pool + I.o_gt + (long long)mi * n * n;
+  mv_lanes(GT, n, s.a, s.b);                                              // Chebyshev T
   __syncthreads();
   op_Dc2(V, n, s.b, s.c, s.e, s.w);                                       // dT/dr, d2T/dr2
   __syncthreads();
@@ -1049,7 +994,9 @@ int mloop_threads(int maxN) {
   const int t = 2 * maxN > 4 * h2 ? 2 * maxN : 4 * h2;
   return ((t + 31) / 32) * 32;
 }
-size_t rloop_smem_bytes(int P) { return 5 * (size_t)P * sizeof(double2); }
+size_t rloop_smem_bytes(int P, int M) {
+  return 4 * (size_t)PZ_RLOOP_G * P * sizeof(double2) + (3 + (size_t)M) * PZ_RLOOP_G * sizeof(double);
+}
 
 }  // namespace
 
@@ -1061,7 +1008,7 @@ cudaError_t pz_setup_kernels() {
   const int big = 200 * 1024;
   if ((e = cudaFuncSetAttribute(k_build, cudaFuncAttributeMaxDynamicSharedMemorySize, big))) return e;
   if ((e = cudaFuncSetAttribute(k_build_static, cudaFuncAttributeMaxDynamicSharedMemorySize, big))) return e;
-  if ((e = cudaFuncSetAttribute(k_rloop, cudaFuncAttributeMaxDynamicSharedMemorySize, 64 * 1024))) return e;
+  if ((e = cudaFuncSetAttribute(k_rloop, cudaFuncAttributeMaxDynamicSharedMemorySize, PZ_SMEM_MAX))) return e;
   return cudaSuccess;
 }
 
@@ -1095,7 +1042,7 @@ cudaError_t pz_launch_gather_rows(const PzDev& d, double* out, cudaStream_t s) {
 
 cudaError_t pz_launch_step_kernel(const PzDev& d, int k, cudaStream_t s) {
   switch (k) {
-    case 0: k_rloop<<<d.n_ritems, PZ_THREADS, rloop_smem_bytes(d.maxP), s>>>(d); break;
+    case 0: k_rloop<<<d.n_ritems, 256, rloop_smem_bytes(d.maxP, d.maxM), s>>>(d); break;
     case 1: k_cfl<<<d.n_inst, 32, 0, s>>>(d); break;
     case 2: k_build<<<d.n_mitems, PZ_THREADS, build_smem_bytes(d.maxN), s>>>(d); break;
     case 3: k_mloop<<<d.n_mitems, mloop_threads(d.maxN), ms_smem_bytes(d.maxN), s>>>(d); break;

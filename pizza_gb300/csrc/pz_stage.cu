@@ -17,77 +17,35 @@
 
 namespace {
 
-// radial_loop for one radius, reading and writing (n_m, n_r) arrays, n_m fastest
-__global__ void __launch_bounds__(PZ_THREADS) k_expl_rloop(PzExplArgs a) {
+// radial_loop for PZ_RLOOP_G radii, reading and writing (n_m, n_r) arrays,
+// n_m fastest, with dVsT and dVsOm to the m-major scratch
+struct ExplIO {
+  const PzExplArgs* a;
+  int N, M;
+  __device__ double2 in(int f, int m, int r) const {
+    const long long o = (long long)r * M + m;
+    return f == 0 ? a->us[o] : f == 1 ? a->up[o] : f == 2 ? a->om[o] : a->temp[o];
+  }
+  __device__ void out(int m, int r, double2 dtdt, double2 vst, double2 dpdt, double2 vsom) const {
+    const long long o = (long long)r * M + m;
+    a->dTdt[o] = dtdt;
+    a->dpsidt[o] = dpdt;
+    a->s_dVsT[(long long)m * N + r] = vst;
+    a->s_dVsOm[(long long)m * N + r] = vsom;
+  }
+  __device__ void cfl(int r, double dtr, double dth) const {
+    a->dtr[r] = dtr;
+    a->dth[r] = dth;
+  }
+};
+
+__global__ void __launch_bounds__(256) k_expl_rloop(PzExplArgs a) {
   extern __shared__ double2 sh[];
-  __shared__ double red[32];
   const PzInst& I = *a.inst;
   const View V{&I, a.pool};
-  const int N = I.N, M = I.M, P = I.P, r = blockIdx.x;
-  double2* tw = sh;
-  double2* za = sh + P;
-  double2* zb = sh + 3 * P;
-  const double2* gtw = reinterpret_cast<const double2*>(a.pool + I.o_tw);
-  for (int k = threadIdx.x; k < P; k += blockDim.x) tw[k] = gtw[k];
-  for (int k = threadIdx.x; k < 2 * P; k += blockDim.x) za[k] = make_double2(0.0, 0.0);
-  __syncthreads();
-  const double rr = V.rad(RV_R)[r], or1 = V.rad(RV_OR1)[r], beta = V.rad(RV_BETA)[r];
-  const double ekpump = V.rad(RV_EKPUMP)[r];
-  double usom = 0.0;
-  for (int m = threadIdx.x; m < M; m += blockDim.x) {
-    const long long o = (long long)r * M + m;
-    double2 u = a.us[o], w = a.up[o], c = a.om[o], e = a.temp[o];
-    if (m == 0) {
-      usom += 0.5 * I.ek * I.CorFac * ekpump * w.x * c.x;   // us_fluct(m=0) * om
-      u.y = 0.0; w.y = 0.0; c.y = 0.0; e.y = 0.0;
-    } else {
-      usom += 2.0 * (u.x * c.x + u.y * c.y);
-    }
-    za[m] = make_double2(u.x - w.y, u.y + w.x);
-    za[P + m] = make_double2(c.x - e.y, c.y + e.x);
-    if (m > 0) {
-      za[P - m] = make_double2(u.x + w.y, -u.y + w.x);
-      za[2 * P - m] = make_double2(c.x + e.y, -c.y + e.x);
-    }
-  }
-  usom = block_sum(usom, red);
-  double2* g = fft_run(za, zb, I, tw, 2, true);
-  double2* h = (g == za) ? zb : za;
-  double vr = 0.0, vh = 0.0;
-  for (int j = threadIdx.x; j < P; j += blockDim.x) {
-    const double2 z1 = g[j], z2 = g[P + j];
-    vr = fmax(vr, z1.x * z1.x);
-    vh = fmax(vh, z1.y * z1.y);
-    h[j] = make_double2(rr * z1.x * z2.y, z1.y * z2.y);
-    h[P + j] = make_double2(rr * z1.x * z2.x, z1.y * z2.x);
-  }
-  vr = block_max(vr, red);
-  vh = block_max(vh, red);
-  if (threadIdx.x == 0) {
-    const double vr2 = I.courfac * I.courfac * vr, vh2 = I.courfac * I.courfac * vh;
-    double dtr = 1.0e10, dth = 1.0e10;
-    if (vr2 != 0.0) dtr = fmin(dtr, sqrt(V.rad(RV_DELXR2)[r] / vr2));
-    if (vh2 != 0.0) dth = fmin(dth, sqrt(V.rad(RV_DELXH2)[r] / vh2));
-    a.dtr[r] = dtr;
-    a.dth[r] = dth;
-  }
-  __syncthreads();
-  double2* f = fft_run(h, g, I, tw, 2, false);
-  const double tfac = (1.0 - I.tadvz) * beta * or1;
-  for (int m = threadIdx.x; m < M; m += blockDim.x) {
-    const int mc = (P - m) % P;
-    const double2 Z = f[m], Zc = f[mc], Y = f[P + m], Yc = f[P + mc];
-    const double2 vsT = make_double2(0.5 * (Z.x + Zc.x) / (double)P, 0.5 * (Z.y - Zc.y) / (double)P);
-    const double2 upT = make_double2(0.5 * (Z.y + Zc.y) / (double)P, -0.5 * (Z.x - Zc.x) / (double)P);
-    const double2 vsOm = make_double2(0.5 * (Y.x + Yc.x) / (double)P, 0.5 * (Y.y - Yc.y) / (double)P);
-    const double2 upOm = make_double2(0.5 * (Y.y + Yc.y) / (double)P, -0.5 * (Y.x - Yc.x) / (double)P);
-    const double t = or1 * (double)(m * I.minc);
-    const long long o = (long long)r * M + m;
-    a.dTdt[o] = make_double2(t * upT.y - tfac * vsT.x, -t * upT.x - tfac * vsT.y);
-    a.dpsidt[o] = (m == 0) ? make_double2(-usom, 0.0) : make_double2(t * upOm.y, -t * upOm.x);
-    a.s_dVsT[(long long)m * N + r] = vsT;
-    a.s_dVsOm[(long long)m * N + r] = vsOm;
-  }
+  ExplIO io{&a, I.N, I.M};
+  double* rsh = reinterpret_cast<double*>(sh + 4 * PZ_RLOOP_G * I.P);
+  rloop_group(I, V, blockIdx.x * PZ_RLOOP_G, io, sh, rsh);
 }
 
 // finish_exp_temp_coll and finish_exp_psi_coll_dmat for one m
@@ -160,9 +118,10 @@ size_t pz_expl_scratch_bytes(int n_r_max, int n_m_max) {
 }
 
 cudaError_t pz_launch_explicit_terms(const PzExplArgs& a, int N, int M, int P, cudaStream_t s) {
-  cudaError_t e = cudaFuncSetAttribute(k_expl_rloop, cudaFuncAttributeMaxDynamicSharedMemorySize, 64 * 1024);
+  cudaError_t e = cudaFuncSetAttribute(k_expl_rloop, cudaFuncAttributeMaxDynamicSharedMemorySize, PZ_SMEM_MAX);
   if (e) return e;
-  k_expl_rloop<<<N, PZ_THREADS, 5 * (size_t)P * sizeof(double2), s>>>(a);
+  const size_t smem = 4 * (size_t)PZ_RLOOP_G * P * sizeof(double2) + (3 + (size_t)M) * PZ_RLOOP_G * sizeof(double);
+  k_expl_rloop<<<(N + PZ_RLOOP_G - 1) / PZ_RLOOP_G, 256, smem, s>>>(a);
   if ((e = cudaGetLastError())) return e;
   k_expl_finish<<<M, PZ_THREADS, 4 * (size_t)N * sizeof(double2), s>>>(a);
   return cudaGetLastError();

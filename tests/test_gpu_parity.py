@@ -189,3 +189,19 @@ def test_explicit_terms_entry_point_matches_oracle(pz):
         assert rel_err(out[1].cpu().numpy().T, sim.dpsidt.expl[0]) < 1e-12
         np.testing.assert_allclose(out[2].cpu().numpy(), sim.dtr, rtol=1e-12)
         np.testing.assert_allclose(out[3].cpu().numpy(), sim.dth, rtol=1e-12)
+
+
+def test_prandtl_not_one_uses_separate_temperature_operator(pz):
+    """Pr != 1: the temperature and vorticity operators differ (TdiffFac != ViscFac)."""
+    spec = dict(C0, pr=0.7)
+    sim, ens, out = run_pair(pz, spec, 40, seed=8)
+    check_fields(sim, out[-1][2], TOL, "Pr=0.7")
+
+
+def test_odd_and_even_grids_and_phi_sizes(pz):
+    """Parity-compact operators on even N, and FFT lengths with radix 2, 3, 5, 7."""
+    for spec in (dict(C0, n_r_max=32, n_cheb_max=32, m_max=30),     # P = 90 = 2*3*3*5
+                 dict(C0, n_r_max=40, n_cheb_max=40, m_max=42),     # P = 126 = 2*3*3*7
+                 dict(C0, n_r_max=33, n_cheb_max=30, m_max=32)):    # dealiased n_cheb_max < n_r_max
+        sim, ens, out = run_pair(pz, spec, 15, seed=9)
+        check_fields(sim, out[-1][2], TOL, str(spec["n_r_max"]))
