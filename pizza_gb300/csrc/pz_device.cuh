@@ -323,54 +323,109 @@ __device__ void rloop_group(const PzInst& I, const View& V, int r0, IO& io, doub
 // ---------------------------------------------------------------------------
 // operator products with one (row, re/im) task per lane
 // ---------------------------------------------------------------------------
-// y = A x, A column-major n x n, x complex: lane t computes component (t & 1)
-// of row (t >> 1).  Two lanes share each matrix element (broadcast load).
-__device__ __forceinline__ void mv_lanes(const double* __restrict__ A, int n, const double2* __restrict__ x,
-                                         double2* __restrict__ y) {
-  const double* xs = reinterpret_cast<const double*>(x);
-  double* ys = reinterpret_cast<double*>(y);
-  for (int t = threadIdx.x; t < 2 * n; t += blockDim.x) {
-    const int row = t >> 1, c = t & 1;
-    const double* a = A + row;
+// Dot products of T tasks of length L, one task per lane.  Whole warps of
+// tasks run one task per lane; the last r < 32 tasks (T is 2N or 4*ceil(N/2),
+// two or four past a multiple of 32 for N = 2^k + 1) are split across the
+// lanes of one warp, G = 32/r (rounded down to a power of 2) lanes per task,
+// and reduced with shuffles, so no warp issues FP64 work for a few lanes.
+// Policy P supplies fma(task, j, acc) and store(task, value).
+template <class P>
+__device__ __forceinline__ void lane_dots(const P& p, int T, int L) {
+  const int full = T & ~31;
+  for (int t = threadIdx.x; t < full; t += blockDim.x) {
     double acc = 0.0;
 #pragma unroll 4
-    for (int j = 0; j < n; ++j) acc = fma(__ldg(a + (long long)j * n), xs[2 * j + c], acc);
-    ys[t] = acc;
+    for (int j = 0; j < L; ++j) acc = p.fma(t, j, acc);
+    p.store(t, acc);
+  }
+  const int r = T - full;
+  if (r > 0 && (threadIdx.x >> 5) == ((full >> 5) % (blockDim.x >> 5))) {
+    const int lane = threadIdx.x & 31;
+    int G = 32;
+    while (G * r > 32) G >>= 1;
+    const int task = lane / G, sub = lane & (G - 1);
+    double acc = 0.0;
+    if (task < r)
+      for (int j = sub; j < L; j += G) acc = p.fma(full + task, j, acc);
+    for (int o = G >> 1; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o, G);
+    if (task < r && sub == 0) p.store(full + task, acc);
+  }
+}
+template <class P>
+__device__ __forceinline__ void lane_dots2(const P& p, int T, int L) {
+  const int full = T & ~31;
+  for (int t = threadIdx.x; t < full; t += blockDim.x) {
+    double a = 0.0, b = 0.0;
+#pragma unroll 4
+    for (int j = 0; j < L; ++j) p.fma2(t, j, a, b);
+    p.store2(t, a, b);
+  }
+  const int r = T - full;
+  if (r > 0 && (threadIdx.x >> 5) == ((full >> 5) % (blockDim.x >> 5))) {
+    const int lane = threadIdx.x & 31;
+    int G = 32;
+    while (G * r > 32) G >>= 1;
+    const int task = lane / G, sub = lane & (G - 1);
+    double a = 0.0, b = 0.0;
+    if (task < r)
+      for (int j = sub; j < L; j += G) p.fma2(full + task, j, a, b);
+    for (int o = G >> 1; o > 0; o >>= 1) {
+      a += __shfl_down_sync(0xffffffffu, a, o, G);
+      b += __shfl_down_sync(0xffffffffu, b, o, G);
+    }
+    if (task < r && sub == 0) p.store2(full + task, a, b);
   }
 }
 
-// Parity-compact products.  Rows of the compact matrix A (nrow x L,
-// column-major) take their input from v0 (even row) or v1 (odd row); lane t
-// computes component (t & 1) of row (t >> 1) into out[t].
+// dense: task t = component (t & 1) of row (t >> 1) of A x, A column-major n x n
+struct DenseDot {
+  const double* __restrict__ A; int n; const double* __restrict__ x; double* __restrict__ y;
+  __device__ __forceinline__ double fma(int t, int j, double acc) const {
+    return ::fma(__ldg(A + (t >> 1) + (long long)j * n), x[2 * j + (t & 1)], acc);
+  }
+  __device__ __forceinline__ void store(int t, double v) const { y[t] = v; }
+};
+// parity-compact: rows of A (nrow x L) take input v0 (even row) or v1 (odd row)
+struct SymDot {
+  const double* __restrict__ A; int nrow; const double* __restrict__ v0; const double* __restrict__ v1;
+  double* __restrict__ out;
+  __device__ __forceinline__ double fma(int t, int j, double acc) const {
+    const int row = t >> 1;
+    const double* v = (row & 1) ? v1 : v0;
+    return ::fma(__ldg(A + row + (long long)j * nrow), v[2 * j + (t & 1)], acc);
+  }
+  __device__ __forceinline__ void store(int t, double v) const { out[t] = v; }
+};
+struct SymDot2 {
+  const double* __restrict__ A; const double* __restrict__ B; int nrow;
+  const double* __restrict__ v0; const double* __restrict__ v1; double* __restrict__ oa; double* __restrict__ ob;
+  __device__ __forceinline__ void fma2(int t, int j, double& a, double& b) const {
+    const int row = t >> 1;
+    const double x = ((row & 1) ? v1 : v0)[2 * j + (t & 1)];
+    a = ::fma(__ldg(A + row + (long long)j * nrow), x, a);
+    b = ::fma(__ldg(B + row + (long long)j * nrow), x, b);
+  }
+  __device__ __forceinline__ void store2(int t, double a, double b) const { oa[t] = a; ob[t] = b; }
+};
+
+// y = A x, A column-major n x n real, x complex
+__device__ __forceinline__ void mv_lanes(const double* __restrict__ A, int n, const double2* __restrict__ x,
+                                         double2* __restrict__ y) {
+  lane_dots(DenseDot{A, n, reinterpret_cast<const double*>(x), reinterpret_cast<double*>(y)}, 2 * n, n);
+}
+
 __device__ __forceinline__ void sym_dot(const double* __restrict__ A, int nrow, int L,
                                         const double2* __restrict__ v0, const double2* __restrict__ v1,
                                         double* __restrict__ out) {
-  for (int t = threadIdx.x; t < 2 * nrow; t += blockDim.x) {
-    const int row = t >> 1, c = t & 1;
-    const double* v = reinterpret_cast<const double*>((row & 1) ? v1 : v0) + c;
-    const double* a = A + row;
-    double acc = 0.0;
-#pragma unroll 4
-    for (int j = 0; j < L; ++j) acc = fma(__ldg(a + (long long)j * nrow), v[2 * j], acc);
-    out[t] = acc;
-  }
+  lane_dots(SymDot{A, nrow, reinterpret_cast<const double*>(v0), reinterpret_cast<const double*>(v1), out},
+            2 * nrow, L);
 }
 __device__ __forceinline__ void sym_dot2(const double* __restrict__ A, const double* __restrict__ B, int nrow,
                                          int L, const double2* __restrict__ v0, const double2* __restrict__ v1,
                                          double* __restrict__ outA, double* __restrict__ outB) {
-  for (int t = threadIdx.x; t < 2 * nrow; t += blockDim.x) {
-    const int row = t >> 1, c = t & 1;
-    const double* v = reinterpret_cast<const double*>((row & 1) ? v1 : v0) + c;
-    double acca = 0.0, accb = 0.0;
-#pragma unroll 4
-    for (int j = 0; j < L; ++j) {
-      const double x = v[2 * j];
-      acca = fma(__ldg(A + row + (long long)j * nrow), x, acca);
-      accb = fma(__ldg(B + row + (long long)j * nrow), x, accb);
-    }
-    outA[t] = acca;
-    outB[t] = accb;
-  }
+  lane_dots2(SymDot2{A, B, nrow, reinterpret_cast<const double*>(v0), reinterpret_cast<const double*>(v1), outA,
+                     outB},
+             2 * nrow, L);
 }
 
 // s_j = x_j + x_{n-1-j}, a_j = x_j - x_{n-1-j} (j < n/2); odd n: s_h = x_h, a_h = 0

@@ -90,7 +90,7 @@ struct PzInst {
   long long o_gt;           // M*N*N   temperature operator per m
   long long o_gom;          // M*N*N   vorticity operator per m (influence)
   long long o_guphi;        // N*N     m=0 u_phi operator
-  long long o_gpsi;         // M*N*N   streamfunction operator per m (dt independent)
+  long long o_gpsi;         // M*N*N   K = G_psi P C per m: psi_cheb = -K om_cheb (dt independent)
   long long o_aux;          // 4*M*N: om2, om3, psi2, psi3 (Chebyshev space) ; then 4*M infl
   long long o_fld;          // 2*F_COUNT*M*N
   long long o_hist;         // 2*(2*(nold+nimp+nexp))*M*N

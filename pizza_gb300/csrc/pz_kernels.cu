@@ -418,7 +418,22 @@ __global__ void __launch_bounds__(PZ_THREADS) k_build_static(PzDev d) {
   fill_matrix(s.A, B, V, 2, m, 0.0);
   equilibrate(s.A, n, s.f1, s.f2, true);
   if (gj_invert(s.A, n, s.piv, s.colk, s.red, s.redi) != 0) { flag_status(S, PZ_E_SINGULAR); return; }
-  store_op(d.pool + I.o_gpsi + (long long)it.idx * n * n, s.A, n, I.n_max, s.f2, s.f1);
+  // K = G_psi P C with G_psi = diag(f2) A_s^-1 diag(f1) and P the projection
+  // on the interior rows: the streamfunction solve psi = G_psi (-omega_phys)
+  // of update_om_coll_dmat (update_psi_coll_dmat.f90:309-366) applied to the
+  // Chebyshev coefficients of omega in one operator, psi = -K omega_cheb
+  const double* C = V.basis(BM_C);
+  double* K = d.pool + I.o_gpsi + (long long)it.idx * n * n;
+  for (int idx = threadIdx.x; idx < n * n; idx += blockDim.x) {
+    const int j = idx / n, i = idx - j * n;
+    double v = 0.0;
+    if (i < I.n_max) {
+      double acc = 0.0;
+      for (int l = 1; l < n - 1; ++l) acc = fma(s.A[i * n + l] * s.f1[l], C[l + (long long)j * n], acc);
+      v = s.f2[i] * acc;
+    }
+    K[idx] = v;
+  }
 }
 
 // dt dependent operators, rebuilt when lMat (step_time.f90:296-303):
@@ -470,14 +485,9 @@ __global__ void __launch_bounds__(PZ_THREADS) k_build(PzDev d) {
     s.va[i] = make_double2(a2, a3);
   }
   __syncthreads();
-  mv1(V.basis(BM_C), n, n, s.va, s.vb);
+  mv_lanes(d.pool + I.o_gpsi + (long long)mi * n * n, n, s.va, s.vb);   // K (om2, om3)
   __syncthreads();
-  for (int i = threadIdx.x; i < n; i += blockDim.x) {
-    const bool bd = (i == 0 || i == n - 1);
-    s.va[i] = bd ? make_double2(0.0, 0.0) : make_double2(-s.vb[i].x, -s.vb[i].y);
-  }
-  __syncthreads();
-  mv1(d.pool + I.o_gpsi + (long long)mi * n * n, n, n, s.va, s.vb);
+  for (int i = threadIdx.x; i < n; i += blockDim.x) s.vb[i] = make_double2(-s.vb[i].x, -s.vb[i].y);
   __syncthreads();
   double t2 = 0.0, t3 = 0.0, b2 = 0.0, b3 = 0.0;
   const double* bct = V.rad(RV_BCTOP);
@@ -795,12 +805,9 @@ __global__ void __launch_bounds__(256) k_mloop(PzDev d) {
   } else {
     mv_lanes(d.pool + I.o_gom + (long long)mi * n * n, n, s.a, s.b);  // omega, Chebyshev
     __syncthreads();
-    op_C(V, n, s.b, s.c, s.w);                                       // omega, physical
+    mv_lanes(d.pool + I.o_gpsi + (long long)mi * n * n, n, s.b, s.e);  // -psi, Chebyshev (psi = -K om)
     __syncthreads();
-    for (int i = threadIdx.x; i < n; i += blockDim.x)
-      s.a[i] = (i == 0 || i == n - 1) ? make_double2(0.0, 0.0) : make_double2(-s.c[i].x, -s.c[i].y);
-    __syncthreads();
-    mv_lanes(d.pool + I.o_gpsi + (long long)mi * n * n, n, s.a, s.e);  // psi, Chebyshev
+    for (int i = threadIdx.x; i < n; i += blockDim.x) s.e[i] = make_double2(-s.e[i].x, -s.e[i].y);
     __syncthreads();
     // influence-matrix correction (update_psi_coll_dmat.f90:1256-1300)
     const double* bct = V.rad(RV_BCTOP);
