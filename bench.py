@@ -87,17 +87,19 @@ def gpu_cfg(spec):
 def mloop_work(specs, nold=1, nimp=1, nexp=2):
     """Algorithmic HBM bytes and FP64 flops of one k_mloop launch over the batch.
 
-    Per (instance, m): the three per-m operators (temperature, vorticity,
-    streamfunction; N x N FP64 each, m = 0: temperature and u_phi), the
+    Per (instance, m): the per-m operators (the vorticity operator, which at
+    Pr = 1 is also the temperature operator, and the streamfunction operator;
+    N x N FP64 each; m = 0: temperature and u_phi), the
     influence vectors (4N + 4 doubles), the state it reads (dVsT, dVsOm, us, up,
     om, T: 6 complex N-vectors) and the history slots of both equations
     (2 (nold + nimp + nexp) complex N-vectors), and what it writes (T, dT/dr,
     us, up, om, psi, two explicit, two old and two implicit slots: 12 complex
     N-vectors).  The Chebyshev operators shared by all m of one size are
     counted once per size.  Flops: per m, 3 dense real-operator x complex-vector
-    products (4N^2 flops each: the per-m operators) and 11 products with the
-    parity-compact Chebyshev operators (2N^2 flops each); m = 0: 2 dense and 8
-    compact.  Elementwise work is neglected.
+    products (4N^2 flops each: temperature/vorticity operator twice, the
+    streamfunction operator K once) and 10 products with the parity-compact
+    Chebyshev operators (2N^2 flops each); m = 0: 2 dense and 8 compact.
+    Elementwise work is neglected.
     """
     byts = 0.0
     flops = 0.0
@@ -105,10 +107,10 @@ def mloop_work(specs, nold=1, nimp=1, nexp=2):
     for s in specs:
         N, M = s["n_r_max"], s["m_max"] + 1
         sizes.add(N)
-        per_m = 8.0 * 3 * N * N + 8.0 * (4 * N + 4) + 16.0 * N * (6 + 2 * (nold + nimp + nexp) + 12)
+        per_m = 8.0 * 2 * N * N + 8.0 * (4 * N + 4) + 16.0 * N * (6 + 2 * (nold + nimp + nexp) + 12)
         m0 = 8.0 * 2 * N * N + 16.0 * N * (6 + 2 * (nold + nimp + nexp) + 12)
         byts += (M - 1) * per_m + m0
-        flops += (M - 1) * (3 * 4.0 + 11 * 2.0) * N * N + (2 * 4.0 + 8 * 2.0) * N * N
+        flops += (M - 1) * (3 * 4.0 + 10 * 2.0) * N * N + (2 * 4.0 + 8 * 2.0) * N * N
     for N in sizes:
         byts += 8.0 * 4 * N * N
     return byts, flops
