@@ -190,6 +190,38 @@ int pz_explicit_terms_noalloc(pz_handle* h, int inst, const double* us, const do
                               double* dpsidt_expl, double* dtr, double* dth);
 
 /* Release all device memory of the handle. */
+/* ---- discrete adjoint (the gradient path of the benchmark spec) ----------
+ * pizza itself has no adjoint; these entry points back the PyTorch
+ * autograd.Function of the binding.  The objective of every instance is
+ *   J = (1/n_window) * sum over the last n_window states k of
+ *       (us2_3D + up2_3D + uz2_3D)(k)          (e_kin_3D, outputs.f90:553-570)
+ * and the gradient is taken with respect to the initial temperature
+ * perturbation (the temp argument of pz_set_state) and Ra, for a fixed
+ * time-step sequence.  Only CNAB2 with the influence-matrix solve is covered.
+ *
+ * pz_adjoint_forward: run n_steps steps from the start state set by
+ * pz_set_state/pz_set_state_all (every instance must be at step 0), storing a
+ * checkpoint every checkpoint_every steps (<= 0: store every step, no
+ * recomputation).  dt_sched (n_inst x n_steps, row per instance, or NULL)
+ * prescribes dt of every step; NULL lets the Courant controller choose and
+ * records its choice.  J (n_inst) receives the objective, dt_used (n_inst x
+ * n_steps, or NULL) the sequence used.  No time-series rows are written.
+ * Leaves the handle at the final state. */
+int pz_adjoint_forward(pz_handle* h, int n_steps, int n_window, int checkpoint_every,
+                       const double* dt_sched, double* J, double* dt_used);
+
+/* pz_adjoint_backward: gradient of the last forward sweep's objective.
+ * dJ_dtemp: per instance a complex (n_m, n_r) array (m fastest, the layout of
+ * pz_set_state), instances concatenated, with dJ = Re(sum conj(g) dtemp);
+ * dJ_dra (n_inst).  Either may be NULL.  Leaves the handle at the final
+ * state of the forward sweep.  Any pz_step, pz_set_state* or pz_set_ra call
+ * in between discards the stored sweep. */
+int pz_adjoint_backward(pz_handle* h, double* dJ_dtemp, double* dJ_dra);
+
+/* Change Ra of one instance (BuoFac = Ra/Pr); the operators do not depend on
+ * it.  Used for finite-difference checks of dJ/dRa. */
+int pz_set_ra(pz_handle* h, int inst, double ra);
+
 int pz_destroy(pz_handle* h);
 
 /* Last error message of the handle (or of the last failed pz_create when h

@@ -147,12 +147,16 @@ def load_library(path: str | None = None):
     vp = ctypes.c_void_p
     lib.pz_explicit_terms.argtypes = [vp, ctypes.c_int, vp, vp, vp, vp, vp, vp, vp, vp]
     lib.pz_explicit_terms_noalloc.argtypes = [vp, ctypes.c_int, vp, vp, vp, vp, vp, vp, vp, vp]
+    lib.pz_adjoint_forward.argtypes = [vp, ctypes.c_int, ctypes.c_int, ctypes.c_int, dp, dp, dp]
+    lib.pz_adjoint_backward.argtypes = [vp, dp, dp]
+    lib.pz_set_ra.argtypes = [vp, ctypes.c_int, ctypes.c_double]
     lib.pz_destroy.argtypes = [ctypes.c_void_p]
     lib.pz_last_error.argtypes = [ctypes.c_void_p]
     lib.pz_last_error.restype = ctypes.c_char_p
     for f in ("pz_create", "pz_set_state", "pz_set_state_all", "pz_step", "pz_sync", "pz_get_state",
               "pz_get_series", "pz_get_dims", "pz_launches_per_step", "pz_latest_rows",
-              "pz_step_profile", "pz_explicit_terms", "pz_explicit_terms_noalloc", "pz_destroy"):
+              "pz_step_profile", "pz_explicit_terms", "pz_explicit_terms_noalloc", "pz_adjoint_forward",
+              "pz_adjoint_backward", "pz_set_ra", "pz_destroy"):
         getattr(lib, f).restype = ctypes.c_int
     _lib = lib
     return lib
@@ -275,6 +279,41 @@ class Ensemble:
 
     def launches_per_step(self):
         return self.lib.pz_launches_per_step(self._h)
+
+    # -- discrete adjoint -------------------------------------------------
+    def set_ra(self, i, ra):
+        """Change Ra of instance i (BuoFac = Ra/Pr)."""
+        self._check(self.lib.pz_set_ra(self._h, i, float(ra)))
+        self.configs[i] = dataclasses.replace(self.configs[i], ra=float(ra))
+
+    def adjoint_forward(self, n_steps, n_window, checkpoint_every=0, dt_sched=None):
+        """Forward sweep of the kinetic-energy objective from the start state
+        of every instance (pz_adjoint_forward).  ``dt_sched`` (n_instances,
+        n_steps) prescribes the time steps; None lets the Courant controller
+        choose.  Returns (J, dt_used) as numpy arrays."""
+        nI = len(self)
+        J = np.zeros(nI)
+        dt_used = np.zeros((nI, int(n_steps)))
+        sched = None
+        if dt_sched is not None:
+            sched = np.ascontiguousarray(np.broadcast_to(np.asarray(dt_sched, np.float64), (nI, int(n_steps))))
+        self._check(self.lib.pz_adjoint_forward(self._h, int(n_steps), int(n_window), int(checkpoint_every),
+                                                _dptr(sched), _dptr(J), _dptr(dt_used)))
+        return J, dt_used
+
+    def adjoint_backward(self):
+        """Gradient of the last forward sweep's objective: a list of
+        (n_m, n_r) complex arrays dJ/dtemp (dJ = Re sum conj(g) dtemp) and an
+        array dJ/dRa."""
+        sizes = [m * n for (n, m, _) in self.dims]
+        g = np.zeros(sum(sizes), np.complex128)
+        dra = np.zeros(len(self))
+        self._check(self.lib.pz_adjoint_backward(self._h, _dptr(g.view(np.float64)), _dptr(dra)))
+        out, o = [], 0
+        for i, (n, m, _) in enumerate(self.dims):
+            out.append(g[o:o + m * n].reshape(n, m).T.copy())
+            o += m * n
+        return out, dra
 
     def latest_rows(self, out=None):
         """Latest time-series row of every instance, shape (n_instances, 16)."""

@@ -1,0 +1,938 @@
+// Discrete adjoint of the CNAB2 collocation step (influence-matrix solve):
+// gradient of a time-averaged 3-D kinetic energy with respect to the initial
+// temperature perturbation and to BuoFac (hence Ra).
+//
+// The step of k_rloop/k_cfl/k_build/k_mloop is, per instance, a map of the
+// state S_n = (Tc, oc, pc, uc) -- the Chebyshev coefficients of temperature,
+// vorticity and streamfunction (m /= 0) and of u_phi (m = 0) -- plus the
+// explicit terms E_{n-1} of the previous step:
+//   fields f_n   = L(S_n)                 T, us, up, om, implicit terms iT, iP
+//                                         (get_temp_rhs_imp_coll, get_psi_rhs_imp_coll_dmat)
+//   nonlinear    = NL(f_n)                radial_loop.f90:231-394
+//   E_n          = FIN(f_n, NL)           finish_exp_temp_coll / finish_exp_psi_coll_dmat
+//   S_{n+1}      = SOLVE(f_n, E_n, E_{n-1})   update_temp_co, update_om_coll_dmat
+// with SOLVE linear in its inputs for a fixed time-step sequence.  The backward
+// step is the exact transpose of each piece, in reverse order:
+//   k_adj_solve  (instance, m)  SOLVE^T and FIN^T (local part): influence
+//                               correction, K^T, G_om^T / G_uphi^T, buoyancy,
+//                               G_T^T, IMEX weights, D1p^T
+//   k_adj_rloop  (instance, r)  NL^T: phi-FFT adjoints and product rule
+//   k_adj_lin    (instance, m)  L^T plus the kinetic-energy source:
+//                               C^T, D1c^T, D2c^T
+// Complex numbers are treated as pairs of reals: the adjoint of y = a x is
+// x_bar = conj(a) y_bar, and a real matrix transposes.  The gradient g of a
+// real J with respect to a complex z is the one with dJ = Re(conj(g) dz).
+//
+// The time-step sequence is held fixed: the sweep either takes it from the
+// caller or records the one chosen by the Courant controller, and the
+// gradient is that of J for the recorded sequence (dt_courant's choices are
+// piecewise constant in the state; the value picked at a change point is
+// not differentiated).
+//
+// Memory: the forward sweep stores a checkpoint (fields, history rings and
+// step state) every `checkpoint_every` steps and the physical fields
+// (T, us, up, om) of every step of the last segment; the backward sweep
+// recomputes each earlier segment from its checkpoint before running it
+// backwards.  Operators are rebuilt in the backward sweep wherever the
+// recorded weights change.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <string>
+#include <vector>
+
+#include "pizza_gpu.h"
+#include "pz_device.cuh"
+#include "pz_handle.h"
+#include "pz_internal.h"
+
+namespace {
+
+// planes of M*N complex per instance in the adjoint workspace
+enum {
+  AP_TCB = 0, AP_OCB, AP_PCB, AP_UCB,   // adjoint of the state (row 0 of AP_UCB: u_phi, m = 0)
+  AP_CT, AP_CP,                          // adjoint of E_n carried from step n+1 (we1 * rhs adjoint)
+  AP_RTB, AP_RPB,                        // adjoint of the solve right-hand sides of step n
+  AP_ETB, AP_EPB,                        // adjoint of E_n (temperature, vorticity)
+  AP_VTB, AP_VOB,                        // adjoint of dVsT, dVsOm
+  AP_AUS, AP_AUP, AP_AOM, AP_AT,         // adjoint of us, up, om, T through the nonlinear terms
+  AP_DB,                                 // dJ/dBuoFac partial sums per m (first M doubles)
+  AP_SNAP                                // snapshots, 4 planes each (T, us, up, om)
+};
+enum { SN_T = 0, SN_US, SN_UP, SN_OM };
+
+struct PzAdjDev {
+  PzDev d;                  // forward launch parameters
+  double* ws;               // workspace
+  const long long* o_ws;    // per-instance offset (doubles)
+  const PzState* rec;       // [inst][n_steps] state of every step after its dt/weight update
+  PzState* ck_state;        // [inst][n_ck]
+  PzState* bstate;          // [inst] state handed to k_build in the backward sweep
+  double* J;                // [inst] objective
+  double* out;              // gradient output, ABI layout, instances concatenated
+  const long long* o_out;   // per-instance offset into out (doubles)
+  int n_steps, n_snap, n_ck, ck_planes;
+  int win0;                 // first state index of the averaging window
+  double inv_window;
+};
+
+struct AdjView {
+  const PzInst* I;
+  double* base;
+  __device__ double2* plane(long long k, int mi) const {
+    return reinterpret_cast<double2*>(base) + (k * I->M + mi) * I->N;
+  }
+  __device__ double2* snap(int slot, int f, int mi) const { return plane(AP_SNAP + 4LL * slot + f, mi); }
+  __device__ double2* ck(int n_snap, int ck_planes, int c, int k, int mi) const {
+    return plane(AP_SNAP + 4LL * n_snap + (long long)c * ck_planes + k, mi);
+  }
+  __device__ double* db() const { return reinterpret_cast<double*>(plane(AP_DB, 0)); }
+};
+
+__device__ __forceinline__ AdjView adj_view(const PzAdjDev& a, int inst) {
+  return AdjView{&a.d.inst[inst], a.ws + a.o_ws[inst]};
+}
+
+// per-m scratch: 12 vectors of n complex, the parity-product scratch and a
+// reduction buffer
+struct AS {
+  double2* v[12];
+  SymScratch w;
+  double* red;
+};
+__device__ AS as_smem(int n) {
+  extern __shared__ double2 shm[];
+  const int h2 = (n + 1) / 2;
+  AS s;
+  for (int k = 0; k < 12; ++k) s.v[k] = shm + k * n;
+  s.w.s = shm + 12 * n;
+  s.w.a = s.w.s + h2;
+  s.w.t1 = reinterpret_cast<double*>(s.w.a + h2);
+  s.w.t2 = s.w.t1 + 4 * h2;
+  s.red = s.w.t2 + 4 * h2;
+  return s;
+}
+size_t as_smem_bytes(int n) {
+  const size_t h2 = (size_t)(n + 1) / 2;
+  return 12 * (size_t)n * sizeof(double2) + 2 * h2 * sizeof(double2) + 8 * h2 * sizeof(double) + 64 * sizeof(double);
+}
+int adj_threads(int maxN) {
+  const int h2 = (maxN + 1) / 2;
+  const int t = 2 * maxN > 4 * h2 ? 2 * maxN : 4 * h2;
+  return ((t + 31) / 32) * 32;
+}
+size_t adj_rloop_smem_bytes(int P) {
+  return 6 * (size_t)PZ_RLOOP_G * P * sizeof(double2) + PZ_RLOOP_G * sizeof(double);
+}
+
+__device__ __forceinline__ double2 cz() { return make_double2(0.0, 0.0); }
+__device__ __forceinline__ double2 caxpy(double s, double2 x, double2 y) {
+  return make_double2(fma(s, x.x, y.x), fma(s, x.y, y.y));
+}
+// Re(conj(x) y)
+__device__ __forceinline__ double cdotr(double2 x, double2 y) { return x.x * y.x + x.y * y.y; }
+
+// ---------------------------------------------------------------------------
+// forward-sweep helpers
+// ---------------------------------------------------------------------------
+// physical fields of the current state -> snapshot `slot`
+__global__ void k_adj_snap(PzAdjDev a, int slot) {
+  const PzItem it = a.d.mitems[blockIdx.x];
+  const PzInst& I = a.d.inst[it.inst];
+  const View V{&I, a.d.pool};
+  const AdjView A = adj_view(a, it.inst);
+  const int n = I.N, mi = it.idx;
+  const double2* src[4] = {V.fld(F_TEMP, mi), V.fld(F_US, mi), V.fld(F_UP, mi), V.fld(F_OM, mi)};
+  for (int f = 0; f < 4; ++f) {
+    double2* dst = A.snap(slot, f, mi);
+    for (int i = threadIdx.x; i < n; i += blockDim.x) dst[i] = src[f][i];
+  }
+}
+
+// checkpoint c: save (dir 0) or restore (dir 1) fields, history rings and the
+// step state.  A restored state rebuilds its operators at its next step.
+__global__ void k_adj_ckpt(PzAdjDev a, int c, int dir) {
+  const PzItem it = a.d.mitems[blockIdx.x];
+  const int inst = it.inst;
+  const PzInst& I = a.d.inst[inst];
+  const AdjView A = adj_view(a, inst);
+  const int n = I.N, mi = it.idx;
+  const long long MN = (long long)I.M * n;
+  const int nh = 2 * (I.nold + I.nimp + I.nexp);
+  for (int k = 0; k < F_COUNT + nh; ++k) {
+    double2* p = reinterpret_cast<double2*>(a.d.pool + (k < F_COUNT ? I.o_fld + 2LL * k * MN
+                                                                      : I.o_hist + 2LL * (k - F_COUNT) * MN)) +
+                 (long long)mi * n;
+    double2* q = A.ck(a.n_snap, a.ck_planes, c, k, mi);
+    if (dir == 0)
+      for (int i = threadIdx.x; i < n; i += blockDim.x) q[i] = p[i];
+    else
+      for (int i = threadIdx.x; i < n; i += blockDim.x) p[i] = q[i];
+  }
+  if (mi == 0 && threadIdx.x == 0) {
+    PzState* cs = a.ck_state + (long long)inst * a.n_ck + c;
+    if (dir == 0) {
+      *cs = a.d.state[inst];
+    } else {
+      PzState S = *cs;
+      S.lMatNext = 1;
+      a.d.state[inst] = S;
+    }
+  }
+}
+
+// J += (us2_3D + up2_3D + uz2_3D) / n_window of the current state
+// (the e_kin_3D sums of outputs.f90:553-570, as k_obs forms them)
+__global__ void k_adj_ke(PzAdjDev a) {
+  const int inst = blockIdx.x;
+  const PzInst& I = a.d.inst[inst];
+  const View V{&I, a.d.pool};
+  __shared__ double red[32];
+  const int n = I.N, M = I.M;
+  const double* rr = V.rad(RV_R);
+  const double* h = V.rad(RV_HEIGHT);
+  const double* beta = V.rad(RV_BETA);
+  const double* wint = V.rad(RV_WINT);
+  const double2* us = V.fld(F_US, 0);
+  const double2* up = V.fld(F_UP, 0);
+  double s3 = 0.0;
+  if (!(I.flags & PZF_NON_ROT)) {
+    for (int r = threadIdx.x; r < n; r += blockDim.x) {
+      double us2 = 0.0, up2 = 0.0;
+      for (int mi = 0; mi < M; ++mi) {
+        const double2 x = us[(long long)mi * n + r], y = up[(long long)mi * n + r];
+        if (mi == 0) { us2 += x.x * x.x; up2 += y.x * y.x; }
+        else { us2 += 2.0 * (x.x * x.x + x.y * x.y); up2 += 2.0 * (y.x * y.x + y.y * y.y); }
+      }
+      s3 += wint[r] * us2 * rr[r] * h[r] + wint[r] * up2 * rr[r] * h[r] +
+            wint[r] * us2 * beta[r] * beta[r] * rr[r] * h[r] * h[r] * h[r] / 12.0;
+    }
+  }
+  s3 = block_sum(s3, red);
+  if (threadIdx.x == 0) a.J[inst] += 3.14159265358979323846 * s3 * a.inv_window;
+}
+
+// ---------------------------------------------------------------------------
+// backward-sweep kernels
+// ---------------------------------------------------------------------------
+__global__ void k_adj_zero(PzAdjDev a) {
+  const PzItem it = a.d.mitems[blockIdx.x];
+  const PzInst& I = a.d.inst[it.inst];
+  const AdjView A = adj_view(a, it.inst);
+  for (int k = 0; k <= AP_DB; ++k) {
+    double2* p = A.plane(k, it.idx);
+    for (int i = threadIdx.x; i < I.N; i += blockDim.x) p[i] = cz();
+  }
+}
+
+// operators of step n for k_build: lMat where the weights differ from step n+1's
+__global__ void k_adj_bstate(PzAdjDev a, int n) {
+  const int inst = blockIdx.x * blockDim.x + threadIdx.x;
+  if (inst >= a.d.n_inst) return;
+  const PzState* r = a.rec + (long long)inst * a.n_steps;
+  PzState S = r[n];
+  S.lMat = (n + 1 >= a.n_steps || r[n].wimp_lin[0] != r[n + 1].wimp_lin[0]) ? 1 : 0;
+  S.status = 0;
+  a.bstate[inst] = S;
+}
+
+// SOLVE^T and the local part of FIN^T for step n (snapshot `slot` = state n)
+__global__ void __launch_bounds__(256) k_adj_solve(PzAdjDev a, int n, int slot) {
+  const PzItem it = a.d.mitems[blockIdx.x];
+  const int inst = it.inst;
+  const PzInst& I = a.d.inst[inst];
+  const PzState& S = a.rec[(long long)inst * a.n_steps + n];
+  const View V{&I, a.d.pool};
+  const AdjView A = adj_view(a, inst);
+  const int N = I.N, mi = it.idx, m = mi * I.minc;
+  const double dm = (double)m;
+  AS s = as_smem(N);
+  const double w0 = S.wimp[0], wl0 = S.wimp_lin[0], wl1 = S.wimp_lin[1];
+  const double we0 = S.wexp[0], we1 = S.wexp[1];
+  const bool buo_imp = (I.flags & PZF_BUO_IMP) != 0;
+  (void)w0;
+  const double* or1 = V.rad(RV_OR1);
+  const double* rgrav = V.rad(RV_RGRAV);
+  double2 *Tc = s.v[0], *oc = s.v[1], *pc = s.v[2], *x = s.v[3], *y = s.v[4];
+  double2 *rT = s.v[5], *rP = s.v[6], *eT = s.v[7], *eP = s.v[8], *t = s.v[9];
+  for (int i = threadIdx.x; i < N; i += blockDim.x) {
+    Tc[i] = A.plane(AP_TCB, mi)[i];
+    oc[i] = (m == 0) ? A.plane(AP_UCB, 0)[i] : A.plane(AP_OCB, mi)[i];
+    pc[i] = (m == 0) ? cz() : A.plane(AP_PCB, mi)[i];
+  }
+  __syncthreads();
+  if (m != 0) {
+    // influence correction (update_psi_coll_dmat.f90:1256-1300), transposed
+    const long long MN = (long long)I.M * N;
+    const double* aux = a.d.pool + I.o_aux;
+    const double* om2 = aux + 0 * MN + (long long)mi * N;
+    const double* om3 = aux + 1 * MN + (long long)mi * N;
+    const double* psi2 = aux + 2 * MN + (long long)mi * N;
+    const double* psi3 = aux + 3 * MN + (long long)mi * N;
+    const double* infl = aux + 4 * MN + 4LL * mi;
+    const double* bct = V.rad(RV_BCTOP);
+    const double* bcb = V.rad(RV_BCBOT);
+    double c1r = 0.0, c1i = 0.0, c2r = 0.0, c2i = 0.0;
+    for (int i = threadIdx.x; i < N; i += blockDim.x) {
+      c1r += psi2[i] * pc[i].x + om2[i] * oc[i].x;
+      c1i += psi2[i] * pc[i].y + om2[i] * oc[i].y;
+      c2r += psi3[i] * pc[i].x + om3[i] * oc[i].x;
+      c2i += psi3[i] * pc[i].y + om3[i] * oc[i].y;
+    }
+    c1r = block_sum(c1r, s.red); c1i = block_sum(c1i, s.red);
+    c2r = block_sum(c2r, s.red); c2i = block_sum(c2i, s.red);
+    const double ttr = -infl[0] * c1r - infl[2] * c2r, tti = -infl[0] * c1i - infl[2] * c2i;
+    const double tbr = -infl[1] * c1r - infl[3] * c2r, tbi = -infl[1] * c1i - infl[3] * c2i;
+    for (int i = threadIdx.x; i < N; i += blockDim.x)
+      x[i] = make_double2(pc[i].x + ttr * bct[i] + tbr * bcb[i], pc[i].y + tti * bct[i] + tbi * bcb[i]);
+    __syncthreads();
+    // psi = -K om  ->  om_bar -= K^T psi_bar
+    mvT_lanes(a.d.pool + I.o_gpsi + (long long)mi * N * N, N, x, y);
+    __syncthreads();
+    for (int i = threadIdx.x; i < N; i += blockDim.x) x[i] = csub(oc[i], y[i]);
+    __syncthreads();
+    mvT_lanes(a.d.pool + I.o_gom + (long long)mi * N * N, N, x, rP);
+    __syncthreads();
+    // implicit buoyancy of the new temperature in the vorticity rhs
+    for (int i = threadIdx.x; i < N; i += blockDim.x) {
+      if (i == 0 || i == N - 1) rP[i] = cz();
+      x[i] = buo_imp ? cscale(wl0 * I.BuoFac * rgrav[i] * or1[i], cim(dm, rP[i])) : cz();
+    }
+    __syncthreads();
+    if (buo_imp) {
+      op_CT(V, N, x, y, s.w);
+      __syncthreads();
+      for (int i = threadIdx.x; i < N; i += blockDim.x) Tc[i] = cadd(Tc[i], y[i]);
+      __syncthreads();
+    }
+  } else {
+    mvT_lanes(a.d.pool + I.o_guphi, N, oc, rP);
+    __syncthreads();
+    for (int i = threadIdx.x; i < N; i += blockDim.x)
+      if (i == 0 || i == N - 1) rP[i] = cz(); else rP[i].y = 0.0;
+    __syncthreads();
+  }
+  const double* GT = ((I.flags & PZF_T_IS_OM) && m != 0) ? a.d.pool + I.o_gom + (long long)mi * N * N
+                                                         : a.d.pool + I.o_gt + (long long)mi * N * N;
+  mvT_lanes(GT, N, Tc, rT);
+  __syncthreads();
+  double2* cT = A.plane(AP_CT, mi);
+  double2* cP = A.plane(AP_CP, mi);
+  for (int i = threadIdx.x; i < N; i += blockDim.x) {
+    const double2 rt = (i == 0 || i == N - 1) ? cz() : rT[i];
+    const double2 rp = rP[i];
+    rT[i] = rt;
+    const double2 et = caxpy(we0, rt, cT[i]), ep = caxpy(we0, rp, cP[i]);
+    eT[i] = et; eP[i] = ep;
+    cT[i] = cscale(we1, rt);
+    cP[i] = cscale(we1, rp);
+    A.plane(AP_RTB, mi)[i] = rt;
+    A.plane(AP_RPB, mi)[i] = rp;
+    A.plane(AP_ETB, mi)[i] = et;
+    A.plane(AP_EPB, mi)[i] = ep;
+    x[i] = cscale(-or1[i], et);
+    y[i] = cscale(-or1[i], ep);
+  }
+  __syncthreads();
+  // dVsT_bar = D1p^T (-or1 eT_bar), dVsOm_bar likewise (m /= 0)
+  op_D1pT(V, N, x, t, s.w);
+  __syncthreads();
+  for (int i = threadIdx.x; i < N; i += blockDim.x) A.plane(AP_VTB, mi)[i] = t[i];
+  __syncthreads();
+  if (m != 0) {
+    op_D1pT(V, N, y, t, s.w);
+    __syncthreads();
+    for (int i = threadIdx.x; i < N; i += blockDim.x) A.plane(AP_VOB, mi)[i] = t[i];
+    // dJ/dBuoFac: buoyancy in the rhs (new temperature) and in the implicit
+    // term of state n, or the explicit buoyancy of FIN
+    const double2* Tn = A.snap(slot, SN_T, mi);
+    const double2* Tn1 = A.snap(slot + 1, SN_T, mi);
+    double acc = 0.0;
+    for (int i = threadIdx.x; i < N; i += blockDim.x) {
+      const double c = rgrav[i] * or1[i];
+      if (buo_imp) {
+        acc += cdotr(rP[i], cscale(-wl0 * c, cim(dm, Tn1[i])));
+        acc += wl1 * cdotr(rP[i], cscale(-c, cim(dm, Tn[i])));
+      } else {
+        acc += cdotr(eP[i], cscale(-c, cim(dm, Tn[i])));
+      }
+    }
+    acc = block_sum(acc, s.red);
+    if (threadIdx.x == 0) A.db()[mi] += acc;
+  } else {
+    for (int i = threadIdx.x; i < N; i += blockDim.x) A.plane(AP_VOB, mi)[i] = cz();
+  }
+}
+
+// NL^T for PZ_RLOOP_G radii: the adjoint of
+//   A = fft(r us T), B = fft(up T), C = fft(r us om), D = fft(up om)
+//   ET = -(i m/r) B - tfac A,  EP = -(i m/r) D (m > 0),  EP(0) = -sum_m us_fluct om
+// with fft = rfft/P truncated to M and the grids from c2r of the spectra.
+// The adjoint of fft is a c2r of the spectrum scaled by 1/(2P) (1/P and the
+// real part at m = 0); the adjoint of the c2r is an r2c scaled by 2 (1 and
+// the real part at m = 0).  Shared memory: three buffers of 2*G transforms.
+__global__ void __launch_bounds__(256) k_adj_rloop(PzAdjDev a, int slot) {
+  extern __shared__ double2 sh[];
+  const PzItem it = a.d.ritems[blockIdx.x];
+  const int inst = it.inst, r0 = it.idx;
+  const PzInst& I = a.d.inst[inst];
+  const View V{&I, a.d.pool};
+  const AdjView A = adj_view(a, inst);
+  const int N = I.N, M = I.M, P = I.P;
+  const int G = min(PZ_RLOOP_G, N - r0);
+  const double2* tw = reinterpret_cast<const double2*>(V.pool + I.o_tw);
+  double2* b0 = sh;
+  double2* b1 = sh + 2 * G * P;
+  double2* b2 = sh + 4 * G * P;
+  double* ep0 = reinterpret_cast<double*>(sh + 6 * G * P);
+  for (int k = threadIdx.x; k < 2 * G * P; k += blockDim.x) { b0[k] = cz(); b2[k] = cz(); }
+  __syncthreads();
+  const double inv2P = 0.5 / (double)P, invP = 1.0 / (double)P;
+  for (int t = threadIdx.x; t < G * M; t += blockDim.x) {
+    const int g = t / M, mi = t - g * M, r = r0 + g;
+    const double dm = (double)(mi * I.minc);
+    const long long o = (long long)mi * N + r;
+    // grids of the state (as k_rloop)
+    double2 us = A.snap(slot, SN_US, 0)[o], up = A.snap(slot, SN_UP, 0)[o];
+    double2 om = A.snap(slot, SN_OM, 0)[o], T = A.snap(slot, SN_T, 0)[o];
+    // spectra of the adjoint products
+    const double or1 = V.rad(RV_OR1)[r];
+    const double tfac = (1.0 - I.tadvz) * V.rad(RV_BETA)[r] * or1;
+    const double2 et = A.plane(AP_ETB, 0)[o], ep = A.plane(AP_EPB, 0)[o];
+    double2 hA = csub(A.plane(AP_VTB, 0)[o], cscale(tfac, et));
+    double2 hB = cscale(or1, cim(dm, et));
+    double2 hC = A.plane(AP_VOB, 0)[o];
+    double2 hD = (mi == 0) ? cz() : cscale(or1, cim(dm, ep));
+    if (mi == 0) {
+      us.y = 0.0; up.y = 0.0; om.y = 0.0; T.y = 0.0;
+      hA = make_double2(hA.x * invP, 0.0); hB = make_double2(hB.x * invP, 0.0);
+      hC = make_double2(hC.x * invP, 0.0); hD = cz();
+      ep0[g] = ep.x;
+    } else {
+      hA = cscale(inv2P, hA); hB = cscale(inv2P, hB); hC = cscale(inv2P, hC); hD = cscale(inv2P, hD);
+    }
+    double2* z1 = b0 + (2 * g) * P;
+    double2* z2 = b0 + (2 * g + 1) * P;
+    double2* z3 = b2 + (2 * g) * P;
+    double2* z4 = b2 + (2 * g + 1) * P;
+    z1[mi] = make_double2(us.x - up.y, us.y + up.x);
+    z2[mi] = make_double2(om.x - T.y, om.y + T.x);
+    z3[mi] = make_double2(hA.x - hB.y, hA.y + hB.x);
+    z4[mi] = make_double2(hC.x - hD.y, hC.y + hD.x);
+    if (mi > 0) {
+      z1[P - mi] = make_double2(us.x + up.y, -us.y + up.x);
+      z2[P - mi] = make_double2(om.x + T.y, -om.y + T.x);
+      z3[P - mi] = make_double2(hA.x + hB.y, -hA.y + hB.x);
+      z4[P - mi] = make_double2(hC.x + hD.y, -hC.y + hD.x);
+    }
+  }
+  __syncthreads();
+  double2* X = fft_run(b0, b1, I, tw, 2 * G, true);
+  double2* fr = (X == b0) ? b1 : b0;
+  double2* Y = fft_run(b2, fr, I, tw, 2 * G, true);
+  double2* W = (Y == b2) ? fr : b2;
+  // product rule on the grid
+  for (int t = threadIdx.x; t < G * P; t += blockDim.x) {
+    const int g = t / P, j = t - g * P;
+    const double rr = V.rad(RV_R)[r0 + g];
+    const double2 x1 = X[(2 * g) * P + j], x2 = X[(2 * g + 1) * P + j];
+    const double2 y1 = Y[(2 * g) * P + j], y2 = Y[(2 * g + 1) * P + j];
+    const double usg = x1.x, upg = x1.y, omg = x2.x, Tg = x2.y;
+    const double ab = y1.x, bb = y1.y, cb = y2.x, db = y2.y;
+    const double usgb = rr * (Tg * ab + omg * cb);
+    const double upgb = Tg * bb + omg * db;
+    const double omgb = rr * usg * cb + upg * db;
+    const double Tgb = rr * usg * ab + upg * bb;
+    Y[(2 * g) * P + j] = make_double2(usgb, upgb);
+    Y[(2 * g + 1) * P + j] = make_double2(omgb, Tgb);
+  }
+  __syncthreads();
+  double2* F = fft_run(Y, W, I, tw, 2 * G, false);
+  for (int t = threadIdx.x; t < G * M; t += blockDim.x) {
+    const int g = t / M, mi = t - g * M, r = r0 + g;
+    const long long o = (long long)mi * N + r;
+    const int mc = (P - mi) % P;
+    const double2* f1 = F + (2 * g) * P;
+    const double2* f2 = F + (2 * g + 1) * P;
+    const double2 Z = f1[mi], Zc = f1[mc], Yv = f2[mi], Yc = f2[mc];
+    double2 a_us = make_double2(0.5 * (Z.x + Zc.x), 0.5 * (Z.y - Zc.y));
+    double2 a_up = make_double2(0.5 * (Z.y + Zc.y), -0.5 * (Z.x - Zc.x));
+    double2 a_om = make_double2(0.5 * (Yv.x + Yc.x), 0.5 * (Yv.y - Yc.y));
+    double2 a_T = make_double2(0.5 * (Yv.y + Yc.y), -0.5 * (Yv.x - Yc.x));
+    const double e0 = ep0[g];
+    if (mi == 0) {
+      a_us = make_double2(a_us.x, 0.0);
+      a_up = make_double2(a_up.x, 0.0);
+      a_om = make_double2(a_om.x, 0.0);
+      a_T = make_double2(a_T.x, 0.0);
+      // us_fluct(m=0) = E CorFac ekpump up(m=0) / 2 in the Reynolds stress
+      const double f = 0.5 * I.ek * I.CorFac * V.rad(RV_EKPUMP)[r];
+      a_up.x -= e0 * f * A.snap(slot, SN_OM, 0)[o].x;
+      a_om.x -= e0 * f * A.snap(slot, SN_UP, 0)[o].x;
+    } else {
+      a_us = cscale(2.0, a_us); a_up = cscale(2.0, a_up);
+      a_om = cscale(2.0, a_om); a_T = cscale(2.0, a_T);
+      a_us = caxpy(-2.0 * e0, A.snap(slot, SN_OM, 0)[o], a_us);
+      a_om = caxpy(-2.0 * e0, A.snap(slot, SN_US, 0)[o], a_om);
+    }
+    A.plane(AP_AUS, 0)[o] = a_us;
+    A.plane(AP_AUP, 0)[o] = a_up;
+    A.plane(AP_AOM, 0)[o] = a_om;
+    A.plane(AP_AT, 0)[o] = a_T;
+  }
+}
+
+// L^T for step n: field adjoints of state n -> adjoint of S_n.  `terminal`
+// handles the final state (only the kinetic-energy source), `ke` adds the
+// source of the averaging window.
+__global__ void __launch_bounds__(256) k_adj_lin(PzAdjDev a, int n, int slot, int terminal, int ke) {
+  const PzItem it = a.d.mitems[blockIdx.x];
+  const int inst = it.inst;
+  const PzInst& I = a.d.inst[inst];
+  const View V{&I, a.d.pool};
+  const AdjView A = adj_view(a, inst);
+  const int N = I.N, mi = it.idx, m = mi * I.minc;
+  const double dm = (double)m, dm2 = dm * dm;
+  AS s = as_smem(N);
+  double w0 = 0.0, wl1 = 0.0;
+  if (!terminal) {
+    const PzState& S = a.rec[(long long)inst * a.n_steps + n];
+    w0 = S.wimp[0];
+    wl1 = S.wimp_lin[1];
+  }
+  const bool buo_imp = (I.flags & PZF_BUO_IMP) != 0;
+  const bool rot = !(I.flags & PZF_NON_ROT);
+  const bool ek = (I.flags & PZF_EK_PUMP) != 0;
+  const double TdF = I.TdiffFac, Vis = I.ViscFac;
+  const double* rr = V.rad(RV_R);
+  const double* or1 = V.rad(RV_OR1);
+  const double* or2 = V.rad(RV_OR2);
+  const double* beta = V.rad(RV_BETA);
+  const double* rgrav = V.rad(RV_RGRAV);
+  const double* tcond = V.rad(RV_TCOND);
+  const double* dtcond = V.rad(RV_DTCOND);
+  const double* ekpump = V.rad(RV_EKPUMP);
+  const double* ekp_up = V.rad(RV_EKP_UP);
+  const double* ekp_us = V.rad(RV_EKP_US);
+  const double* ekp_dusdp = V.rad(RV_EKP_DUSDP);
+  const double* h = V.rad(RV_HEIGHT);
+  const double* wint = V.rad(RV_WINT);
+  const double pi = 3.14159265358979323846;
+  double2** v = s.v;
+  for (int i = threadIdx.x; i < N; i += blockDim.x) {
+    double2 rT = cz(), rP = cz(), eT = cz(), eP = cz(), aus = cz(), aup = cz(), aom = cz(), aT = cz();
+    if (!terminal) {
+      rT = A.plane(AP_RTB, mi)[i]; rP = A.plane(AP_RPB, mi)[i];
+      eT = A.plane(AP_ETB, mi)[i]; eP = A.plane(AP_EPB, mi)[i];
+      aus = A.plane(AP_AUS, mi)[i]; aup = A.plane(AP_AUP, mi)[i];
+      aom = A.plane(AP_AOM, mi)[i]; aT = A.plane(AP_AT, mi)[i];
+    }
+    double2 Tb = caxpy(w0, rT, aT);
+    const double2 iTb = cscale(wl1, rT), oldPb = cscale(w0, rP), iPb = cscale(wl1, rP);
+    // FIN^T (update_temp_coll.f90:152-176, update_psi_coll_dmat.f90:468-552)
+    const double gT = dtcond[i] - I.tadvz * beta[i] * tcond[i];
+    double2 usb = caxpy(-gT, eT, aus), upb = aup, omb = aom;
+    if (m != 0) {
+      if (rot) usb = caxpy(I.CorFac * beta[i], eP, usb);
+      if (ek) {
+        const double ce = I.CorFac * ekpump[i];
+        // (i m ekp_dusdp + ekp_us) us  ->  conj(.) eP
+        usb = csub(usb, cscale(ce, csub(cscale(ekp_us[i], eP), cscale(ekp_dusdp[i], cim(dm, eP)))));
+        upb = caxpy(-ce * ekp_up[i], eP, upb);
+        omb = caxpy(-ce, eP, omb);
+      }
+      if (!buo_imp) Tb = cadd(Tb, cscale(I.BuoFac * rgrav[i] * or1[i], cim(dm, eP)));
+    }
+    if (ke) {
+      // d(us2_3D + up2_3D + uz2_3D)/d(us, up) of the state, averaged
+      const double W1 = pi * wint[i] * (rr[i] * h[i] + beta[i] * beta[i] * rr[i] * h[i] * h[i] * h[i] / 12.0);
+      const double W2 = pi * wint[i] * rr[i] * h[i];
+      const double2 us = A.snap(slot, SN_US, mi)[i], up = A.snap(slot, SN_UP, mi)[i];
+      if (m != 0) {
+        usb = caxpy(4.0 * W1 * a.inv_window, us, usb);
+        upb = caxpy(4.0 * W2 * a.inv_window, up, upb);
+      } else {
+        usb.x += 2.0 * W1 * a.inv_window * us.x;
+        upb.x += 2.0 * W2 * a.inv_window * up.x;
+      }
+    }
+    // L^T: temperature, vorticity / u_phi, streamfunction
+    v[1][i] = cscale(TdF, iTb);
+    v[2][i] = cscale(TdF * or1[i], iTb);
+    if (m != 0) {
+      double2 Tt = caxpy(-TdF * dm2 * or2[i], iTb, Tb);
+      if (buo_imp) Tt = cadd(Tt, cscale(I.BuoFac * rgrav[i] * or1[i], cim(dm, iPb)));
+      v[0][i] = Tt;
+      omb = cadd(omb, oldPb);
+      v[3][i] = caxpy(-Vis * dm2 * or2[i], iPb, omb);
+      v[4][i] = cscale(Vis, iPb);
+      v[5][i] = cscale(Vis * or1[i], iPb);
+      // us = (i m / r) psi, up = -dpsi/dr - beta psi
+      v[6][i] = csub(cscale(-or1[i], cim(dm, usb)), cscale(beta[i], upb));
+      v[7][i] = upb;
+    } else {
+      v[0][i] = Tb;
+      // up(0) = u, om(0) = du/dr + u/r, old = u,
+      // iP(0) = Vis (u'' + u'/r - u/r^2) - CorFac ekpump u
+      const double u0b = upb.x + oldPb.x + or1[i] * omb.x + (-Vis * or2[i] - I.CorFac * ekpump[i]) * iPb.x;
+      v[3][i] = make_double2(u0b, 0.0);
+      v[4][i] = make_double2(Vis * iPb.x, 0.0);
+      v[5][i] = make_double2(omb.x + Vis * or1[i] * iPb.x, 0.0);
+    }
+  }
+  __syncthreads();
+  double2 *t0 = v[8], *t1 = v[9], *t2 = v[10];
+  // Tc_bar = C^T Tt + D2c^T (TdF iT_bar) + D1c^T (TdF/r iT_bar)
+  op_CT(V, N, v[0], t0, s.w);
+  __syncthreads();
+  op_D2cT(V, N, v[1], t1, s.w);
+  __syncthreads();
+  op_D1cT(V, N, v[2], t2, s.w);
+  __syncthreads();
+  for (int i = threadIdx.x; i < N; i += blockDim.x) A.plane(AP_TCB, mi)[i] = cadd(t0[i], cadd(t1[i], t2[i]));
+  __syncthreads();
+  op_CT(V, N, v[3], t0, s.w);
+  __syncthreads();
+  op_D2cT(V, N, v[4], t1, s.w);
+  __syncthreads();
+  op_D1cT(V, N, v[5], t2, s.w);
+  __syncthreads();
+  if (m != 0) {
+    for (int i = threadIdx.x; i < N; i += blockDim.x) A.plane(AP_OCB, mi)[i] = cadd(t0[i], cadd(t1[i], t2[i]));
+    __syncthreads();
+    op_CT(V, N, v[6], t0, s.w);
+    __syncthreads();
+    op_D1cT(V, N, v[7], t1, s.w);
+    __syncthreads();
+    for (int i = threadIdx.x; i < N; i += blockDim.x) A.plane(AP_PCB, mi)[i] = csub(t0[i], t1[i]);
+  } else {
+    for (int i = threadIdx.x; i < N; i += blockDim.x) {
+      A.plane(AP_UCB, 0)[i] = make_double2(t0[i].x + t1[i].x + t2[i].x, 0.0);
+      A.plane(AP_OCB, 0)[i] = cz();
+      A.plane(AP_PCB, 0)[i] = cz();
+    }
+  }
+}
+
+// dJ/dT0 = C^T Tc_bar(0), in the ABI layout (m fastest)
+__global__ void __launch_bounds__(256) k_adj_out(PzAdjDev a) {
+  const PzItem it = a.d.mitems[blockIdx.x];
+  const int inst = it.inst;
+  const PzInst& I = a.d.inst[inst];
+  const View V{&I, a.d.pool};
+  const AdjView A = adj_view(a, inst);
+  const int N = I.N, mi = it.idx;
+  AS s = as_smem(N);
+  for (int i = threadIdx.x; i < N; i += blockDim.x) s.v[0][i] = A.plane(AP_TCB, mi)[i];
+  __syncthreads();
+  op_CT(V, N, s.v[0], s.v[1], s.w);
+  __syncthreads();
+  double2* out = reinterpret_cast<double2*>(a.out + a.o_out[inst]);
+  for (int i = threadIdx.x; i < N; i += blockDim.x) out[mi + (long long)i * I.M] = s.v[1][i];
+}
+
+// dJ/dBuoFac per instance (sum over m in a fixed order)
+__global__ void k_adj_db(PzAdjDev a, double* out) {
+  const int inst = blockIdx.x * blockDim.x + threadIdx.x;
+  if (inst >= a.d.n_inst) return;
+  const AdjView A = adj_view(a, inst);
+  const double* db = A.db();
+  double acc = 0.0;
+  for (int mi = 0; mi < a.d.inst[inst].M; ++mi) acc += db[mi];
+  out[inst] = acc;
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+// host driver
+// ---------------------------------------------------------------------------
+struct PzAdjoint {
+  int n_steps = 0, K = 0, n_seg = 0, n_window = 0, n_snap = 0, n_ck = 0, ck_planes = 0;
+  bool ready = false;        // a forward sweep is stored
+  bool last_valid = false;   // snapshots of the last segment are those of the forward sweep
+  double* ws = nullptr;
+  long long* d_ows = nullptr;
+  long long* d_oout = nullptr;
+  PzState* d_rec = nullptr;
+  PzState* d_ck = nullptr;
+  PzState* d_bstate = nullptr;
+  double* d_dt = nullptr;
+  double* d_J = nullptr;
+  double* d_out = nullptr;
+  size_t cap_ws = 0, cap_out = 0, cap_ows = 0, cap_oout = 0, cap_rec = 0, cap_ck = 0, cap_b = 0, cap_dt = 0, cap_J = 0;
+  size_t out_doubles = 0;    // gradient output of the current layout
+  std::vector<PzState> h_rec;
+};
+
+void pz_adjoint_free(pz_handle* h) {
+  if (!h || !h->adj) return;
+  PzAdjoint* A = h->adj;
+  cudaFree(A->ws); cudaFree(A->d_ows); cudaFree(A->d_oout); cudaFree(A->d_rec); cudaFree(A->d_ck);
+  cudaFree(A->d_bstate); cudaFree(A->d_dt); cudaFree(A->d_J); cudaFree(A->d_out);
+  delete A;
+  h->adj = nullptr;
+}
+
+void pz_adjoint_invalidate(pz_handle* h) {
+  if (h && h->adj) h->adj->ready = false;
+}
+
+namespace {
+
+int acuda(pz_handle* h, cudaError_t e, const char* what) {
+  return pz_fail(h, PZ_E_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+PzAdjDev adj_dev(pz_handle* h) {
+  PzAdjoint* A = h->adj;
+  PzAdjDev a{};
+  a.d = h->dev;
+  a.ws = A->ws;
+  a.o_ws = A->d_ows;
+  a.rec = A->d_rec;
+  a.ck_state = A->d_ck;
+  a.bstate = A->d_bstate;
+  a.J = A->d_J;
+  a.out = A->d_out;
+  a.o_out = A->d_oout;
+  a.n_steps = A->n_steps;
+  a.n_snap = A->n_snap;
+  a.n_ck = A->n_ck;
+  a.ck_planes = A->ck_planes;
+  a.win0 = A->n_steps - A->n_window + 1;
+  a.inv_window = A->n_window > 0 ? 1.0 / A->n_window : 0.0;
+  return a;
+}
+
+cudaError_t launch_snap(const PzAdjDev& a, int slot, cudaStream_t s) {
+  k_adj_snap<<<a.d.n_mitems, 64, 0, s>>>(a, slot);
+  return cudaGetLastError();
+}
+cudaError_t launch_ckpt(const PzAdjDev& a, int c, int dir, cudaStream_t s) {
+  k_adj_ckpt<<<a.d.n_mitems, 64, 0, s>>>(a, c, dir);
+  return cudaGetLastError();
+}
+// one forward step without the time series: k_rloop, k_cfl, k_build, k_mloop
+cudaError_t launch_fwd(const PzDev& d, cudaStream_t s) {
+  for (int k = 0; k < 4; ++k) {
+    const cudaError_t e = pz_launch_step_kernel(d, k, s);
+    if (e) return e;
+  }
+  return cudaSuccess;
+}
+
+template <class T>
+cudaError_t grow(T** p, size_t* cap, size_t n) {
+  if (*p && *cap >= n) return cudaSuccess;
+  cudaFree(*p);
+  *p = nullptr;
+  *cap = 0;
+  cudaError_t e = cudaMalloc(reinterpret_cast<void**>(p), n * sizeof(T));
+  if (!e) *cap = n;
+  return e;
+}
+
+}  // namespace
+
+extern "C" int pz_set_ra(pz_handle* h, int inst, double ra) {
+  if (!h) return pz_fail(nullptr, PZ_E_ARG, "pz_set_ra: null handle");
+  if (inst < 0 || inst >= h->n_inst) return pz_fail(h, PZ_E_ARG, "pz_set_ra: instance out of range");
+  if (!(ra > 0.0)) return pz_fail(h, PZ_E_ARG, "pz_set_ra: ra must be positive");
+  HostInst& hi = h->hin[inst];
+  const double buo = ra / hi.c.pr;   // BuoFac = Ra / Pr (namelists.f90, time_scale 'VISC')
+  hi.c.ra = ra;
+  hi.I.BuoFac = buo;
+  h->inst[inst].BuoFac = buo;
+  cudaError_t e = cudaMemcpyAsync(&h->d_inst[inst].BuoFac, &h->inst[inst].BuoFac, sizeof(double),
+                                  cudaMemcpyHostToDevice, h->stream);
+  if (!e) e = cudaStreamSynchronize(h->stream);
+  if (e) return acuda(h, e, "pz_set_ra");
+  pz_adjoint_invalidate(h);
+  return PZ_OK;
+}
+
+extern "C" int pz_adjoint_forward(pz_handle* h, int n_steps, int n_window, int checkpoint_every,
+                                  const double* dt_sched, double* J, double* dt_used) {
+  if (!h) return pz_fail(nullptr, PZ_E_ARG, "pz_adjoint_forward: null handle");
+  if (n_steps < 1) return pz_fail(h, PZ_E_ARG, "pz_adjoint_forward: n_steps < 1");
+  if (n_window < 0 || n_window > n_steps) return pz_fail(h, PZ_E_ARG, "pz_adjoint_forward: n_window outside [0, n_steps]");
+  for (int i = 0; i < h->n_inst; ++i) {
+    const PzInst& I = h->inst[i];
+    if (I.scheme != PZ_CNAB2 || (I.flags & PZF_DIRECT))
+      return pz_fail(h, PZ_E_UNSUPPORTED, "pz_adjoint_forward: the adjoint covers CNAB2 with the influence-matrix solve");
+    if (adj_rloop_smem_bytes(I.P) > PZ_SMEM_MAX)
+      return pz_fail(h, PZ_E_UNSUPPORTED, "pz_adjoint_forward: n_phi_max too large for the adjoint transform kernel");
+  }
+  cudaError_t e;
+  std::vector<PzState> st(h->n_inst);
+  if ((e = cudaMemcpyAsync(st.data(), h->d_state, h->n_inst * sizeof(PzState), cudaMemcpyDeviceToHost, h->stream)) ||
+      (e = cudaStreamSynchronize(h->stream)))
+    return acuda(h, e, "pz_adjoint_forward");
+  for (int i = 0; i < h->n_inst; ++i)
+    if (st[i].n_step != 0 || st[i].status != 0)
+      return pz_fail(h, PZ_E_ARG, "pz_adjoint_forward: instance " + std::to_string(i) +
+                                      " is not at a start state (call pz_set_state first)");
+  if (dt_sched)
+    for (long long k = 0; k < (long long)h->n_inst * n_steps; ++k)
+      if (!(dt_sched[k] > 0.0)) return pz_fail(h, PZ_E_ARG, "pz_adjoint_forward: dt_sched must be positive");
+
+  if (!h->adj) h->adj = new PzAdjoint();
+  PzAdjoint* A = h->adj;
+  A->ready = false;
+  A->n_steps = n_steps;
+  A->n_window = n_window;
+  A->K = (checkpoint_every <= 0 || checkpoint_every > n_steps) ? n_steps : checkpoint_every;
+  A->n_seg = (n_steps + A->K - 1) / A->K;
+  A->n_snap = A->K + 1;
+  A->n_ck = A->n_seg + 1;             // one per segment start, plus the final state
+  A->ck_planes = F_COUNT + 2 * (1 + 1 + 2);
+  std::vector<long long> ows(h->n_inst), oout(h->n_inst);
+  long long tot = 0, tout = 0;
+  const long long planes = AP_SNAP + 4LL * A->n_snap + (long long)A->n_ck * A->ck_planes;
+  for (int i = 0; i < h->n_inst; ++i) {
+    const long long MN = (long long)h->inst[i].M * h->inst[i].N;
+    ows[i] = tot;
+    tot += planes * 2 * MN;
+    oout[i] = tout;
+    tout += 2 * MN;
+  }
+  // buffers grow and are kept for later calls
+  if ((e = grow(&A->ws, &A->cap_ws, (size_t)tot)) || (e = grow(&A->d_out, &A->cap_out, (size_t)tout)) ||
+      (e = grow(&A->d_ows, &A->cap_ows, (size_t)h->n_inst)) || (e = grow(&A->d_oout, &A->cap_oout, (size_t)h->n_inst)) ||
+      (e = grow(&A->d_rec, &A->cap_rec, (size_t)h->n_inst * n_steps)) ||
+      (e = grow(&A->d_ck, &A->cap_ck, (size_t)h->n_inst * A->n_ck)) ||
+      (e = grow(&A->d_bstate, &A->cap_b, (size_t)h->n_inst)) ||
+      (e = grow(&A->d_dt, &A->cap_dt, (size_t)h->n_inst * n_steps)) || (e = grow(&A->d_J, &A->cap_J, (size_t)h->n_inst))) {
+    pz_adjoint_free(h);
+    return pz_fail(h, PZ_E_NOMEM, std::string("pz_adjoint_forward: device allocation: ") + cudaGetErrorString(e));
+  }
+  A->out_doubles = (size_t)tout;
+  cudaStream_t s = h->stream;
+  if ((e = cudaMemcpyAsync(A->d_ows, ows.data(), ows.size() * sizeof(long long), cudaMemcpyHostToDevice, s)) ||
+      (e = cudaMemcpyAsync(A->d_oout, oout.data(), oout.size() * sizeof(long long), cudaMemcpyHostToDevice, s)) ||
+      (e = cudaMemsetAsync(A->d_J, 0, h->n_inst * sizeof(double), s)))
+    return acuda(h, e, "pz_adjoint_forward");
+  if (dt_sched &&
+      (e = cudaMemcpyAsync(A->d_dt, dt_sched, (size_t)h->n_inst * n_steps * sizeof(double), cudaMemcpyHostToDevice, s)))
+    return acuda(h, e, "pz_adjoint_forward");
+
+  PzAdjDev a = adj_dev(h);
+  PzDev dF = h->dev;
+  dF.dt_io = A->d_dt;
+  dF.rec = A->d_rec;
+  dF.sched_n = n_steps;
+  dF.sched_mode = dt_sched ? 1 : 2;
+  const int k0_last = (A->n_seg - 1) * A->K;
+  for (int n = 0; n < n_steps; ++n) {
+    if (n % A->K == 0 && (e = launch_ckpt(a, n / A->K, 0, s))) return acuda(h, e, "checkpoint");
+    if (n >= k0_last && (e = launch_snap(a, n - k0_last, s))) return acuda(h, e, "snapshot");
+    if ((e = launch_fwd(dF, s))) return acuda(h, e, "forward step");
+    if (n_window > 0 && n + 1 >= a.win0) {
+      k_adj_ke<<<h->n_inst, PZ_THREADS, 0, s>>>(a);
+      if ((e = cudaGetLastError())) return acuda(h, e, "objective");
+    }
+  }
+  if ((e = launch_snap(a, n_steps - k0_last, s)) || (e = launch_ckpt(a, A->n_seg, 0, s)))
+    return acuda(h, e, "final state");
+  int rc = pz_check_status(h);
+  if (rc) return rc;
+  A->h_rec.resize((size_t)h->n_inst * n_steps);
+  if ((e = cudaMemcpyAsync(A->h_rec.data(), A->d_rec, A->h_rec.size() * sizeof(PzState), cudaMemcpyDeviceToHost, s)))
+    return acuda(h, e, "pz_adjoint_forward");
+  if (J && (e = cudaMemcpyAsync(J, A->d_J, h->n_inst * sizeof(double), cudaMemcpyDeviceToHost, s)))
+    return acuda(h, e, "pz_adjoint_forward");
+  if ((e = cudaStreamSynchronize(s))) return acuda(h, e, "pz_adjoint_forward");
+  if (dt_used)
+    for (size_t k = 0; k < A->h_rec.size(); ++k) dt_used[k] = A->h_rec[k].dt[0];
+  A->ready = true;
+  A->last_valid = true;
+  return PZ_OK;
+}
+
+extern "C" int pz_adjoint_backward(pz_handle* h, double* dJ_dtemp, double* dJ_dra) {
+  if (!h) return pz_fail(nullptr, PZ_E_ARG, "pz_adjoint_backward: null handle");
+  PzAdjoint* A = h->adj;
+  if (!A || !A->ready)
+    return pz_fail(h, PZ_E_ARG, "pz_adjoint_backward: no forward sweep stored (call pz_adjoint_forward first)");
+  cudaStream_t s = h->stream;
+  cudaError_t e;
+  PzAdjDev a = adj_dev(h);
+  PzDev dR = h->dev;          // recompute: prescribed (recorded) dt, nothing recorded
+  dR.dt_io = A->d_dt;
+  dR.rec = nullptr;
+  dR.sched_n = A->n_steps;
+  dR.sched_mode = 1;
+  PzDev dB = h->dev;          // operator rebuilds of the backward sweep
+  dB.state = A->d_bstate;
+  const int n_steps = A->n_steps, K = A->K;
+  const int k0_last = (A->n_seg - 1) * K;
+  const int threads = adj_threads(h->dev.maxN);
+  const size_t smem = as_smem_bytes(h->dev.maxN);
+  const size_t rsmem = adj_rloop_smem_bytes(h->dev.maxP);
+  if ((e = cudaFuncSetAttribute(k_adj_rloop, cudaFuncAttributeMaxDynamicSharedMemorySize, PZ_SMEM_MAX)))
+    return acuda(h, e, "pz_adjoint_backward");
+  k_adj_zero<<<h->dev.n_mitems, 64, 0, s>>>(a);
+  if ((e = cudaGetLastError()) || (e = cudaMemsetAsync(A->d_bstate, 0, h->n_inst * sizeof(PzState), s)))
+    return acuda(h, e, "adjoint init");
+  if (!A->last_valid) {
+    // snapshots and operators of the last segment were overwritten: recompute
+    if ((e = launch_ckpt(a, A->n_seg - 1, 1, s))) return acuda(h, e, "restore");
+    for (int n = k0_last; n < n_steps; ++n)
+      if ((e = launch_snap(a, n - k0_last, s)) || (e = launch_fwd(dR, s))) return acuda(h, e, "recompute");
+    if ((e = launch_snap(a, n_steps - k0_last, s))) return acuda(h, e, "recompute");
+  }
+  if (A->n_window > 0) {
+    k_adj_lin<<<h->dev.n_mitems, threads, smem, s>>>(a, n_steps, n_steps - k0_last, 1, 1);
+    if ((e = cudaGetLastError())) return acuda(h, e, "adjoint terminal");
+  }
+  for (int sg = A->n_seg - 1; sg >= 0; --sg) {
+    const int k0 = sg * K, k1 = std::min(k0 + K, n_steps);
+    if (sg != A->n_seg - 1) {
+      if ((e = launch_ckpt(a, sg, 1, s))) return acuda(h, e, "restore");
+      for (int n = k0; n < k1; ++n)
+        if ((e = launch_snap(a, n - k0, s)) || (e = launch_fwd(dR, s))) return acuda(h, e, "recompute");
+      if ((e = launch_snap(a, k1 - k0, s))) return acuda(h, e, "recompute");
+    }
+    for (int n = k1 - 1; n >= k0; --n) {
+      bool rebuild = false;
+      if (n < k1 - 1)
+        for (int i = 0; i < h->n_inst && !rebuild; ++i) {
+          const PzState* r = &A->h_rec[(size_t)i * n_steps];
+          rebuild = r[n].wimp_lin[0] != r[n + 1].wimp_lin[0];
+        }
+      if (rebuild) {
+        k_adj_bstate<<<(h->n_inst + 63) / 64, 64, 0, s>>>(a, n);
+        if ((e = cudaGetLastError()) || (e = pz_launch_step_kernel(dB, 2, s))) return acuda(h, e, "rebuild");
+      }
+      const int slot = n - k0;
+      k_adj_solve<<<h->dev.n_mitems, threads, smem, s>>>(a, n, slot);
+      k_adj_rloop<<<h->dev.n_ritems, 256, rsmem, s>>>(a, slot);
+      k_adj_lin<<<h->dev.n_mitems, threads, smem, s>>>(a, n, slot, 0, n >= a.win0 ? 1 : 0);
+      if ((e = cudaGetLastError())) return acuda(h, e, "adjoint step");
+    }
+  }
+  A->last_valid = false;
+  k_adj_out<<<h->dev.n_mitems, threads, smem, s>>>(a);
+  k_adj_db<<<(h->n_inst + 63) / 64, 64, 0, s>>>(a, A->d_J);
+  if ((e = cudaGetLastError())) return acuda(h, e, "adjoint output");
+  // leave the handle at the final state of the forward sweep
+  if ((e = launch_ckpt(a, A->n_seg, 1, s))) return acuda(h, e, "restore final state");
+  std::vector<double> db(h->n_inst);
+  std::vector<PzState> bst(h->n_inst);
+  if ((e = cudaMemcpyAsync(db.data(), A->d_J, h->n_inst * sizeof(double), cudaMemcpyDeviceToHost, s)) ||
+      (e = cudaMemcpyAsync(bst.data(), A->d_bstate, h->n_inst * sizeof(PzState), cudaMemcpyDeviceToHost, s)))
+    return acuda(h, e, "pz_adjoint_backward");
+  if (dJ_dtemp &&
+      (e = cudaMemcpyAsync(dJ_dtemp, A->d_out, A->out_doubles * sizeof(double), cudaMemcpyDeviceToHost, s)))
+    return acuda(h, e, "pz_adjoint_backward");
+  if ((e = cudaStreamSynchronize(s))) return acuda(h, e, "pz_adjoint_backward");
+  // k_adj_db reused d_J; the objective values are not needed any more
+  for (int i = 0; i < h->n_inst; ++i)
+    if (bst[i].status != 0) return pz_fail(h, bst[i].status, "pz_adjoint_backward: operator rebuild failed");
+  int rc = pz_check_status(h);
+  if (rc) return rc;
+  if (dJ_dra)
+    for (int i = 0; i < h->n_inst; ++i) dJ_dra[i] = db[i] / h->hin[i].c.pr;   // dBuoFac/dRa = 1/Pr
+  return PZ_OK;
+}

@@ -517,4 +517,50 @@ __device__ void op_D1p(const View& V, int n, const double2* x, double2* y1, SymS
   sym_combine(w.t1, n, -1.0, 1.0, y1);
 }
 
+// ---- transposes (discrete adjoint) -----------------------------------------
+// y = C^T x
+__device__ void op_CT(const View& V, int n, const double2* x, double2* y, SymScratch& w) {
+  const int h2 = (n + 1) / 2;
+  prep_eo(x, n, w.s, w.a);
+  __syncthreads();
+  sym_dot(V.basis(BM_CTS), 2 * h2, h2, w.s, w.a, w.t1);
+  __syncthreads();
+  sym_combine(w.t1, n, 1.0, -1.0, y);
+}
+// y = D1c^T x
+__device__ void op_D1cT(const View& V, int n, const double2* x, double2* y, SymScratch& w) {
+  const int h2 = (n + 1) / 2;
+  prep_sa(x, n, w.s, w.a);
+  __syncthreads();
+  sym_dot(V.basis(BM_D1CTS), n, h2, w.a, w.s, reinterpret_cast<double*>(y));
+}
+// y = D2c^T x
+__device__ void op_D2cT(const View& V, int n, const double2* x, double2* y, SymScratch& w) {
+  const int h2 = (n + 1) / 2;
+  prep_sa(x, n, w.s, w.a);
+  __syncthreads();
+  sym_dot(V.basis(BM_D2CTS), n, h2, w.s, w.a, reinterpret_cast<double*>(y));
+}
+// y = D1p^T x
+__device__ void op_D1pT(const View& V, int n, const double2* x, double2* y, SymScratch& w) {
+  const int h2 = (n + 1) / 2;
+  prep_sa(x, n, w.s, w.a);
+  __syncthreads();
+  sym_dot(V.basis(BM_D1PTS), 2 * h2, h2, w.s, w.a, w.t1);
+  __syncthreads();
+  sym_combine(w.t1, n, -1.0, 1.0, y);
+}
+// y = A^T x, A column-major n x n real (dense per-m operators)
+struct DenseDotT {
+  const double* __restrict__ A; int n; const double* __restrict__ x; double* __restrict__ y;
+  __device__ __forceinline__ double fma(int t, int i, double acc) const {
+    return ::fma(__ldg(A + i + (long long)(t >> 1) * n), x[2 * i + (t & 1)], acc);
+  }
+  __device__ __forceinline__ void store(int t, double v) const { y[t] = v; }
+};
+__device__ __forceinline__ void mvT_lanes(const double* __restrict__ A, int n, const double2* __restrict__ x,
+                                          double2* __restrict__ y) {
+  lane_dots(DenseDotT{A, n, reinterpret_cast<const double*>(x), reinterpret_cast<double*>(y)}, 2 * n, n);
+}
+
 }  // namespace

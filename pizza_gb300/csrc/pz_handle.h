@@ -1,0 +1,40 @@
+// The handle of the C ABI (shared by the host-side translation units).
+#pragma once
+#include <cuda_runtime.h>
+
+#include <string>
+#include <vector>
+
+#include "pizza_gpu.h"
+#include "pz_internal.h"
+
+struct HostInst {
+  pz_config c;
+  PzInst I;
+};
+
+struct PzAdjoint;   // adjoint workspace (pz_adjoint.cu)
+
+struct pz_handle {
+  int n_inst = 0;
+  std::vector<HostInst> hin;
+  std::vector<PzInst> inst;
+  double* pool = nullptr;
+  long long pool_size = 0;
+  PzInst* d_inst = nullptr;
+  PzState* d_state = nullptr;
+  PzItem* d_ritems = nullptr;
+  PzItem* d_mitems = nullptr;
+  PzDev dev{};
+  cudaStream_t stream = nullptr;
+  cudaGraphExec_t graph = nullptr;
+  double* d_rows = nullptr;    // n_inst x PZ_SERIES_COLS gather buffer
+  std::string err = "no error";
+  PzAdjoint* adj = nullptr;   // allocated by the first adjoint call
+};
+
+// host helpers of pz_host.cu
+int pz_fail(pz_handle* h, int code, const std::string& msg);
+int pz_check_status(pz_handle* h);
+void pz_adjoint_free(pz_handle* h);
+void pz_adjoint_invalidate(pz_handle* h);   // a stored forward sweep no longer matches the state

@@ -17,6 +17,7 @@
 #include <vector>
 
 #include "pizza_gpu.h"
+#include "pz_handle.h"
 #include "pz_internal.h"
 #include "pz_stage.h"
 
@@ -24,29 +25,11 @@ namespace {
 
 thread_local std::string g_create_error = "no error";
 
-struct HostInst {
-  pz_config c;
-  PzInst I;
-};
+
 
 }  // namespace
 
-struct pz_handle {
-  int n_inst = 0;
-  std::vector<HostInst> hin;
-  std::vector<PzInst> inst;
-  double* pool = nullptr;
-  long long pool_size = 0;
-  PzInst* d_inst = nullptr;
-  PzState* d_state = nullptr;
-  PzItem* d_ritems = nullptr;
-  PzItem* d_mitems = nullptr;
-  PzDev dev{};
-  cudaStream_t stream = nullptr;
-  cudaGraphExec_t graph = nullptr;
-  double* d_rows = nullptr;    // n_inst x PZ_SERIES_COLS gather buffer
-  std::string err = "no error";
-};
+
 
 namespace {
 
@@ -55,6 +38,10 @@ int fail(pz_handle* h, int code, const std::string& msg) {
   return code;
 }
 
+int cuda_fail(pz_handle* h, cudaError_t e, const char* what);
+}  // namespace
+int pz_fail(pz_handle* h, int code, const std::string& msg) { return fail(h, code, msg); }
+namespace {
 int cuda_fail(pz_handle* h, cudaError_t e, const char* what) {
   return fail(h, PZ_E_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
 }
@@ -67,6 +54,7 @@ struct Basis {
   int N;
   std::vector<double> x, C, D1c, D2c, D1p, D2p, rMat, drMat, d2rMat;
   std::vector<double> Cs, D1cs, D2cs, D1ps, D2ps;   // parity-compact forms
+  std::vector<double> CTs, D1cTs, D2cTs, D1pTs;     // ... of the transposes
 };
 
 // Parity-compact operators (see BM_CS..BM_D2PS in pz_internal.h).  The
@@ -75,34 +63,55 @@ struct Basis {
 //   D1c(N-1-i, k)    = (-1)^(k+1) D1c(i, k),   D2c(N-1-i, k) = (-1)^k D2c(i, k),
 //   D1p(N-1-i,N-1-j) = -D1p(i, j),             D2p(N-1-i,N-1-j) = D2p(i, j),
 // and each product needs about half the multiply-adds of the dense form.
-void make_compact(Basis& b) {
-  const int N = b.N, h = N / 2, h2 = (N + 1) / 2, R = 2 * h2;
-  auto A = [N](const std::vector<double>& M, int i, int j) { return M[i + (size_t)j * N]; };
-  b.Cs.assign((size_t)N * h2, 0.0);
+// in-sym: column j < h2 of M (N x N), N x h2
+static std::vector<double> compact_in(const std::vector<double>& M, int N) {
+  const int h2 = (N + 1) / 2;
+  std::vector<double> out((size_t)N * h2, 0.0);
   for (int k = 0; k < N; ++k)
-    for (int j = 0; j < h2; ++j) b.Cs[k + (size_t)j * N] = A(b.C, k, j);
-  for (int w = 0; w < 2; ++w) {
-    const std::vector<double>& D = w == 0 ? b.D1c : b.D2c;
-    std::vector<double>& out = w == 0 ? b.D1cs : b.D2cs;
-    out.assign((size_t)R * h2, 0.0);
-    for (int i = 0; i < h2; ++i)
-      for (int kk = 0; kk < h2; ++kk) {
-        out[(2 * i) + (size_t)kk * R] = A(D, i, 2 * kk);
-        if (2 * kk + 1 < N) out[(2 * i + 1) + (size_t)kk * R] = A(D, i, 2 * kk + 1);
-      }
-  }
-  for (int w = 0; w < 2; ++w) {
-    const std::vector<double>& D = w == 0 ? b.D1p : b.D2p;
-    std::vector<double>& out = w == 0 ? b.D1ps : b.D2ps;
-    out.assign((size_t)R * h2, 0.0);
-    for (int i = 0; i < h2; ++i) {
-      for (int j = 0; j < h; ++j) {
-        out[(2 * i) + (size_t)j * R] = 0.5 * (A(D, i, j) + A(D, i, N - 1 - j));
-        out[(2 * i + 1) + (size_t)j * R] = 0.5 * (A(D, i, j) - A(D, i, N - 1 - j));
-      }
-      if (N % 2 == 1) out[(2 * i) + (size_t)h * R] = A(D, i, h);
+    for (int j = 0; j < h2; ++j) out[k + (size_t)j * N] = M[k + (size_t)j * N];
+  return out;
+}
+// out-sym: rows 2i (even columns of row i) and 2i+1 (odd columns), 2*h2 x h2
+static std::vector<double> compact_out(const std::vector<double>& M, int N) {
+  const int h2 = (N + 1) / 2, R = 2 * h2;
+  std::vector<double> out((size_t)R * h2, 0.0);
+  for (int i = 0; i < h2; ++i)
+    for (int kk = 0; kk < h2; ++kk) {
+      out[(2 * i) + (size_t)kk * R] = M[i + (size_t)(2 * kk) * N];
+      if (2 * kk + 1 < N) out[(2 * i + 1) + (size_t)kk * R] = M[i + (size_t)(2 * kk + 1) * N];
     }
+  return out;
+}
+// centro: rows 2i = (M(i,j)+M(i,N-1-j))/2 (and the middle column), 2i+1 = (M(i,j)-M(i,N-1-j))/2
+static std::vector<double> compact_centro(const std::vector<double>& M, int N) {
+  const int h = N / 2, h2 = (N + 1) / 2, R = 2 * h2;
+  std::vector<double> out((size_t)R * h2, 0.0);
+  for (int i = 0; i < h2; ++i) {
+    for (int j = 0; j < h; ++j) {
+      out[(2 * i) + (size_t)j * R] = 0.5 * (M[i + (size_t)j * N] + M[i + (size_t)(N - 1 - j) * N]);
+      out[(2 * i + 1) + (size_t)j * R] = 0.5 * (M[i + (size_t)j * N] - M[i + (size_t)(N - 1 - j) * N]);
+    }
+    if (N % 2 == 1) out[(2 * i) + (size_t)h * R] = M[i + (size_t)h * N];
   }
+  return out;
+}
+static std::vector<double> transpose(const std::vector<double>& M, int N) {
+  std::vector<double> T((size_t)N * N);
+  for (int i = 0; i < N; ++i)
+    for (int j = 0; j < N; ++j) T[j + (size_t)i * N] = M[i + (size_t)j * N];
+  return T;
+}
+void make_compact(Basis& b) {
+  const int N = b.N;
+  b.Cs = compact_in(b.C, N);
+  b.D1cs = compact_out(b.D1c, N);
+  b.D2cs = compact_out(b.D2c, N);
+  b.D1ps = compact_centro(b.D1p, N);
+  b.D2ps = compact_centro(b.D2p, N);
+  b.CTs = compact_out(transpose(b.C, N), N);
+  b.D1cTs = compact_in(transpose(b.D1c, N), N);
+  b.D2cTs = compact_in(transpose(b.D2c, N), N);
+  b.D1pTs = compact_centro(transpose(b.D1p, N), N);
 }
 
 Basis make_basis(int N, double r_icb, double r_cmb) {
@@ -444,8 +453,9 @@ extern "C" int pz_create(const pz_config* cfgs, int n, pz_handle** out) {
       const Basis& B = kv.second;
       const long long NN = (long long)B.N * B.N;
       double* dst = img.data() + basis_off[kv.first];
-      const std::vector<double>* mats[BM_COUNT] = {&B.C,    &B.D1c,  &B.D2c,  &B.D1p,  &B.D2p,  &B.rMat, &B.drMat,
-                                                   &B.d2rMat, &B.Cs, &B.D1cs, &B.D2cs, &B.D1ps, &B.D2ps};
+      const std::vector<double>* mats[BM_COUNT] = {&B.C,    &B.D1c,  &B.D2c,  &B.D1p,   &B.D2p,   &B.rMat,
+                                                   &B.drMat, &B.d2rMat, &B.Cs, &B.D1cs, &B.D2cs, &B.D1ps,
+                                                   &B.D2ps, &B.CTs, &B.D1cTs, &B.D2cTs, &B.D1pTs};
       for (int k = 0; k < BM_COUNT; ++k) std::memcpy(dst + k * NN, mats[k]->data(), mats[k]->size() * sizeof(double));
     }
     const long double pi = 3.141592653589793238462643383279502884L;
@@ -552,8 +562,11 @@ int check_status(pz_handle* h) {
 
 }  // namespace
 
+int pz_check_status(pz_handle* h) { return check_status(h); }
+
 extern "C" int pz_set_state(pz_handle* h, int inst, const double* us, const double* up, const double* temp) {
   if (!h) return fail(nullptr, PZ_E_ARG, "pz_set_state: null handle");
+  pz_adjoint_invalidate(h);
   if (inst < 0 || inst >= h->n_inst) return fail(h, PZ_E_ARG, "pz_set_state: instance out of range");
   int rc;
   if ((rc = upload_field(h, inst, F_US, us)) || (rc = upload_field(h, inst, F_UP, up)) ||
@@ -568,6 +581,7 @@ extern "C" int pz_set_state(pz_handle* h, int inst, const double* us, const doub
 
 extern "C" int pz_set_state_all(pz_handle* h, const double* us, const double* up, const double* temp) {
   if (!h) return fail(nullptr, PZ_E_ARG, "pz_set_state_all: null handle");
+  pz_adjoint_invalidate(h);
   long long o = 0;
   for (int i = 0; i < h->n_inst; ++i) {
     const PzInst& I = h->inst[i];
@@ -586,6 +600,7 @@ extern "C" int pz_set_state_all(pz_handle* h, const double* us, const double* up
 
 extern "C" int pz_step(pz_handle* h, int n_steps) {
   if (!h) return fail(nullptr, PZ_E_ARG, "pz_step: null handle");
+  pz_adjoint_invalidate(h);
   if (n_steps < 0) return fail(h, PZ_E_ARG, "pz_step: n_steps < 0");
   cudaError_t e;
   if (!h->graph) {
@@ -780,6 +795,7 @@ int pz_record_error(pz_handle* h, int code, const char* msg) { return fail(h, co
 extern "C" int pz_destroy(pz_handle* h) {
   if (!h) return PZ_OK;
   if (h->stream) cudaStreamSynchronize(h->stream);
+  pz_adjoint_free(h);
   if (h->graph) cudaGraphExecDestroy(h->graph);
   cudaFree(h->pool);
   cudaFree(h->d_inst);

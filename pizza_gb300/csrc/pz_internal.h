@@ -65,6 +65,11 @@ enum {
   BM_D1PS,    // D1p, 2*h2 x h2: row 2i = (D(i,j)+D(i,N-1-j))/2 (j<h), D(i,h) (odd N);
               //      row 2i+1 = (D(i,j)-D(i,N-1-j))/2 (j<h), 0
   BM_D2PS,    // D2p, same layout
+  // transposes, for the discrete adjoint (same parity structure):
+  BM_CTS,     // C^T, 2*h2 x h2 (layout of BM_D1CS; mirror row = E - O)
+  BM_D1CTS,   // D1c^T, N x h2 (layout of BM_CS; even rows pair with a, odd with s)
+  BM_D2CTS,   // D2c^T, N x h2 (layout of BM_CS)
+  BM_D1PTS,   // D1p^T, 2*h2 x h2 (layout of BM_D1PS)
   BM_COUNT
 };
 
@@ -133,6 +138,13 @@ struct PzDev {
   const PzItem* mitems; int n_mitems;     // (inst, m index)
   int n_inst;
   int maxN, maxP, maxM;
+  // time-step schedule of the adjoint sweeps (null on the plain step):
+  // sched_mode 1 takes dt of step k (0-based n_step) from dt_io[inst*sched_n + k]
+  // instead of the Courant estimate, 2 records the chosen dt there; rec (if
+  // set) receives the state after the dt/weight update of every step.
+  double* dt_io;
+  PzState* rec;
+  int sched_n, sched_mode;
 };
 
 // `only` selects one instance (>= 0) or all of them (-1).

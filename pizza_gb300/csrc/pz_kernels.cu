@@ -213,6 +213,13 @@ __global__ void k_cfl(PzDev d) {
   else if (dt > dt_rh) { l_new_dt = true; dt_new = dt_2; }
   else if (I.dt_fac * dt < dt_rh && dt < I.dtMax) { l_new_dt = true; dt_new = dt_2; }
   else { l_new_dt = false; dt_new = dt; }
+  const long long ks = (long long)inst * d.sched_n + S.n_step;
+  if (d.sched_mode == 1 && S.n_step < d.sched_n) {
+    dt_new = d.dt_io[ks];
+    l_new_dt = dt_new != dt;
+  } else if (d.sched_mode == 2 && S.n_step < d.sched_n) {
+    d.dt_io[ks] = dt_new;
+  }
   for (int k = I.nexp - 1; k > 0; --k) S.dt[k] = S.dt[k - 1];
   S.dt[0] = dt_new;
   if (dt_new < I.dtMin) { S.status = PZ_E_DT_TOO_SMALL; return; }
@@ -229,6 +236,7 @@ __global__ void k_cfl(PzDev d) {
   S.b_old = (S.b_old + I.nold - 1) % I.nold;
   S.b_impl = (S.b_impl + I.nimp - 1) % I.nimp;
   S.b_expl = (S.b_expl + I.nexp - 1) % I.nexp;
+  if (d.rec && ks < (long long)(inst + 1) * d.sched_n) d.rec[ks] = S;
 }
 
 // ---------------------------------------------------------------------------
