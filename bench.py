@@ -284,6 +284,47 @@ def plain_rate(specs, steps, warmup, torch):
     return len(specs) / (t_step_ms * 1e-3), {f"{k[0]}x{3 * k[1]}": v for k, v in t_class.items()}
 
 
+ADJ_SPEC = dict(n_r_max=65, n_cheb_max=65, m_max=64, ek=1e-4, ra=2e6, pr=1.0, radratio=0.35, l_ek_pump=True,
+                time_scheme="CNAB2", dtMax=5e-5, matrix_solve="INFLUENCE", seed=1)
+ADJ_STEPS, ADJ_WINDOW, ADJ_CK = 500, 250, 50
+
+
+def adjoint_ratio(torch, reps=3, checkpoint_every=ADJ_CK, n_steps=ADJ_STEPS, n_window=ADJ_WINDOW):
+    """Cost of the kinetic-energy gradient (forward sweep with checkpoints +
+    backward sweep with recomputation) over a plain forward run of the same
+    500 steps, single instance N=65, n_phi=192, E=1e-4, Ra=2e6.  Both are
+    wall-clock times from pz_set_state to the result on the host (J and the
+    gradient, or the synchronised final state)."""
+    import pizza_gb300 as pz
+    spec = ADJ_SPEC
+    t0 = seeded_temp(spec)
+    ens = pz.Ensemble(gpu_cfg(spec))
+    fw, gr, sw, bw = [], [], [], []
+    for rep in range(reps + 1):
+        torch.cuda.synchronize()
+        a = time.perf_counter()
+        ens.set_state(0, temp=t0)
+        ens.step(n_steps)
+        b = time.perf_counter()
+        ens.set_state(0, temp=t0)
+        J, dt = ens.adjoint_forward(n_steps, n_window, checkpoint_every)
+        c = time.perf_counter()
+        g, dra = ens.adjoint_backward()
+        d = time.perf_counter()
+        if rep == 0:
+            continue          # warm-up: graph capture, workspace allocation
+        fw.append(b - a); gr.append(d - b); sw.append(c - b); bw.append(d - c)
+    ens.close()
+    med = lambda x: float(np.median(x))
+    return {"workload": "adjoint gradient: N=65, n_phi=192, E=1e-4, Ra=2e6, CNAB2, dtMax=5e-5 under the Courant "
+                        f"controller, {n_steps} steps, J = mean e_kin_3D over the last {n_window} states, "
+                        f"checkpoint every {checkpoint_every if checkpoint_every > 0 else n_steps} steps",
+            "forward_ms": 1e3 * med(fw), "gradient_ms": 1e3 * med(gr),
+            "sweep_ms": 1e3 * med(sw), "backward_ms": 1e3 * med(bw),
+            "adjoint_over_forward": med(gr) / med(fw),
+            "J": float(J[0]), "dJ_dra": float(dra[0]), "distinct_dt": int(len(np.unique(dt)))}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -294,6 +335,10 @@ def main():
     ap.add_argument("--seed", type=int, default=1234)
     ap.add_argument("--no-plain", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-adjoint", action="store_true")
+    ap.add_argument("--adjoint-only", action="store_true", help="print only the adjoint/forward measurement")
+    ap.add_argument("--adj-steps", type=int, default=ADJ_STEPS)
+    ap.add_argument("--adj-reps", type=int, default=3)
     args = ap.parse_args()
     args.warmup = max(3, args.warmup)
 
@@ -316,6 +361,13 @@ def main():
     from __graft_entry__ import build
     build()
     import pizza_gb300 as pz
+
+    if args.adjoint_only:
+        if rank == 0:
+            n, w = args.adj_steps, max(1, args.adj_steps // 2)
+            print(json.dumps({"adjoint": adjoint_ratio(torch, args.adj_reps, ADJ_CK, n, w),
+                              "adjoint_no_recompute": adjoint_ratio(torch, args.adj_reps, 0, n, w)}))
+        return
 
     ens = pz.Ensemble([gpu_cfg(s) for s in specs])
     temps = [seeded_temp(s) for s in specs]
@@ -373,6 +425,9 @@ def main():
 
     if rank != 0:
         return
+    adj = None
+    if not args.no_adjoint:
+        adj = {"checkpointed": adjoint_ratio(torch), "stored_trajectory": adjoint_ratio(torch, checkpoint_every=0)}
     cpu = None
     if not args.no_cpu:
         cpu = cpu_baseline(specs)
@@ -397,6 +452,7 @@ def main():
                               "peak_kind": "cuBLAS DGEMM 4096^3 measured in this run",
                               "frac": (flops / (mloop_ms * 1e-3) / 1e12 / fp64_peak) if fp64_peak else None}},
         "dominant_kernel": dom,
+        "adjoint": adj,
         "cpu_baseline": cpu,
         "e2e": e2e,
         "gpu_launches": ens.launches_per_step() * args.steps,
