@@ -57,9 +57,9 @@ class _CConfig(ctypes.Structure):
 
 @dataclasses.dataclass
 class Config:
-    """One instance's namelist values (defaults: src/namelists.f90:530-672,
-    except matrix_solve, which defaults to the influence-matrix path that the
-    GPU implements)."""
+    """One instance's namelist values (defaults: src/namelists.f90:530-672).
+    matrix_solve 'DIRECT' is pizza's coupled smat solve, 'INFLUENCE' the dmat
+    influence-matrix solve (the one the adjoint covers)."""
     n_r_max: int = 32
     n_cheb_max: int | None = None
     m_max: int = 32
@@ -79,7 +79,7 @@ class Config:
     l_non_rot: bool = False
     l_temp_advz: bool = False
     time_scheme: str = "CNAB2"
-    matrix_solve: str = "INFLUENCE"
+    matrix_solve: str = "DIRECT"
     corio_term: str = "IMPLICIT"
     buo_term: str = "IMPLICIT"
     dtMax: float = 1.0e-5

@@ -550,6 +550,29 @@ __device__ void op_D1pT(const View& V, int n, const double2* x, double2* y, SymS
   __syncthreads();
   sym_combine(w.t1, n, -1.0, 1.0, y);
 }
+// (y0, y1) = G x with G complex 2n x n, column-major with leading dimension 2n,
+// x complex: rows < n go to y0, the others to y1 (the smat (omega, psi) solve)
+struct CDenseDot {
+  const double2* __restrict__ G; int n; const double* __restrict__ x; double* __restrict__ y0;
+  double* __restrict__ y1;
+  __device__ __forceinline__ double fma(int t, int j, double acc) const {
+    const double2 g = __ldg(G + (t >> 1) + (long long)j * 2 * n);
+    const double xr = x[2 * j], xi = x[2 * j + 1];
+    return (t & 1) ? ::fma(g.x, xi, ::fma(g.y, xr, acc)) : ::fma(g.x, xr, ::fma(-g.y, xi, acc));
+  }
+  __device__ __forceinline__ void store(int t, double v) const {
+    const int row = t >> 1;
+    if (row < n) y0[2 * row + (t & 1)] = v;
+    else y1[2 * (row - n) + (t & 1)] = v;
+  }
+};
+__device__ __forceinline__ void cmv_lanes(const double2* __restrict__ G, int n, const double2* __restrict__ x,
+                                          double2* __restrict__ y0, double2* __restrict__ y1) {
+  lane_dots(CDenseDot{G, n, reinterpret_cast<const double*>(x), reinterpret_cast<double*>(y0),
+                      reinterpret_cast<double*>(y1)},
+            4 * n, n);
+}
+
 // y = A^T x, A column-major n x n real (dense per-m operators)
 struct DenseDotT {
   const double* __restrict__ A; int n; const double* __restrict__ x; double* __restrict__ y;

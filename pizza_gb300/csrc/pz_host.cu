@@ -233,7 +233,9 @@ int validate(const pz_config& c, std::string* why) {
   if (!(c.radratio > 0.0 && c.radratio < 1.0)) return uns("radratio must be in (0, 1): the full disk is not implemented");
   if (c.ktopt != 1 || c.kbott != 1) return uns("only fixed-temperature boundaries (ktopt = kbott = 1)");
   if (c.ktopv != 2 || c.kbotv != 2) return uns("only rigid boundaries (ktopv = kbotv = 2)");
-  if (c.matrix_solve != PZ_SOLVE_INFLUENCE) return uns("matrix_solve DIRECT is not on the GPU yet; use INFLUENCE");
+  if (c.matrix_solve != PZ_SOLVE_INFLUENCE && c.matrix_solve != PZ_SOLVE_DIRECT) return bad("unknown matrix_solve");
+  if (c.matrix_solve == PZ_SOLVE_DIRECT && pz_build_smem_bytes(c.n_r_max, true) > PZ_SMEM_MAX)
+    return uns("matrix_solve DIRECT needs n_r_max <= 97 (the coupled operator build is staged in shared memory)");
   if (c.dtMax <= 0.0) return bad("dtMax must be > 0");
   if (c.alpha <= 0.0 || c.alpha > 1.0) return bad("alpha must be in (0, 1]");
   if (c.dt_fac <= 1.0) return bad("dt_fac must be > 1");
@@ -312,10 +314,14 @@ extern "C" int pz_create(const pz_config* cfgs, int n, pz_handle** out) {
     if (c.l_ek_pump) I.flags |= PZF_EK_PUMP;
     if (non_rot) I.flags |= PZF_NON_ROT;
     if (imp_calc) I.flags |= PZF_IMP_CALC;
+    const bool direct = c.matrix_solve == PZ_SOLVE_DIRECT;
+    if (direct) I.flags |= PZF_DIRECT;
+    // corio_term='IMPLICIT' only with the direct solve (namelists.f90:448-457)
+    if (direct && c.corio_imp && !non_rot) I.flags |= PZF_COR_IMP;
     // get_tempMat and get_omMat (update_temp_coll.f90:310-393,
     // update_psi_coll_dmat.f90:829-911) build the same rows when
     // TdiffFac*hdif_T == ViscFac*hdif_V and both use fixed/no-slip boundary rows
-    if (I.TdiffFac == I.ViscFac) I.flags |= PZF_T_IS_OM;
+    if (!direct && I.TdiffFac == I.ViscFac) I.flags |= PZF_T_IS_OM;
     const int N = I.N;
     I.rnorm = std::sqrt(2.0 / (double)(N - 1));
     I.r_cmb = 1.0 / (1.0 - c.radratio);
@@ -421,10 +427,16 @@ extern "C" int pz_create(const pz_config* cfgs, int n, pz_handle** out) {
     PzInst& I = h->inst[i];
     const long long N = I.N, M = I.M;
     I.o_gt = take(M * N * N);
-    I.o_gom = take(M * N * N);
     I.o_guphi = take(N * N);
-    I.o_gpsi = take(M * N * N);
-    I.o_aux = take(4 * M * N + 4 * M);
+    if (I.flags & PZF_DIRECT) {
+      I.o_gsm = take(4 * M * N * N);
+      I.o_gom = I.o_gpsi = I.o_aux = 0;   // influence-matrix operators unused
+    } else {
+      I.o_gom = take(M * N * N);
+      I.o_gpsi = take(M * N * N);
+      I.o_aux = take(4 * M * N + 4 * M);
+      I.o_gsm = 0;
+    }
     I.o_fld = take(2LL * F_COUNT * M * N);
     I.o_hist = take(2LL * 2 * (I.nold + I.nimp + I.nexp) * M * N);
     I.o_cfl = take(2 * N);
@@ -506,6 +518,10 @@ extern "C" int pz_create(const pz_config* cfgs, int n, pz_handle** out) {
   h->dev.mitems = h->d_mitems; h->dev.n_mitems = (int)mitems.size();
   h->dev.n_inst = n;
   h->dev.maxN = maxN; h->dev.maxP = maxP; h->dev.maxM = maxM;
+  size_t sb = 0;
+  for (int i = 0; i < n; ++i)
+    sb = std::max(sb, pz_build_smem_bytes(h->inst[i].N, (h->inst[i].flags & PZF_DIRECT) != 0));
+  h->dev.smem_build = (int)sb;
   if ((e = pz_launch_init_state(h->dev, -1, h->stream)) || (e = pz_launch_build_static(h->dev, h->stream)) ||
       (e = cudaStreamSynchronize(h->stream))) {
     g_create_error = std::string("static operators: ") + cudaGetErrorString(e);

@@ -25,7 +25,7 @@
 
 // flag bits of PzInst::flags
 enum {
-  PZF_DIRECT   = 1,    // smat (not on the GPU yet)
+  PZF_DIRECT   = 1,    // smat: coupled (omega, psi) solve per m
   PZF_BUO_IMP  = 2,    // implicit buoyancy (buo_term='IMPLICIT')
   PZF_COR_IMP  = 4,    // implicit Coriolis (direct solve only)
   PZF_EK_PUMP  = 8,    // Ekman pumping
@@ -97,6 +97,9 @@ struct PzInst {
   long long o_guphi;        // N*N     m=0 u_phi operator
   long long o_gpsi;         // M*N*N   K = G_psi P C per m: psi_cheb = -K om_cheb (dt independent)
   long long o_aux;          // 4*M*N: om2, om3, psi2, psi3 (Chebyshev space) ; then 4*M infl
+  long long o_gsm;          // DIRECT (smat): 4*M*N*N, per m the first N columns of the
+                            // inverse of the coupled 2N x 2N operator, complex, column-major
+                            // with leading dimension 2N: (omega, psi)_cheb = G rhs
   long long o_fld;          // 2*F_COUNT*M*N
   long long o_hist;         // 2*(2*(nold+nimp+nexp))*M*N
   long long o_cfl;          // 2*N: dtr, dth
@@ -138,6 +141,7 @@ struct PzDev {
   const PzItem* mitems; int n_mitems;     // (inst, m index)
   int n_inst;
   int maxN, maxP, maxM;
+  int smem_build;           // dynamic shared memory of k_build (bytes)
   // time-step schedule of the adjoint sweeps (null on the plain step):
   // sched_mode 1 takes dt of step k (0-based n_step) from dt_io[inst*sched_n + k]
   // instead of the Courant estimate, 2 records the chosen dt there; rec (if
@@ -157,4 +161,5 @@ const char* pz_step_kernel_name(int k);
 cudaError_t pz_launch_obs(const PzDev& d, int only, cudaStream_t s);
 cudaError_t pz_launch_gather_rows(const PzDev& d, double* out, cudaStream_t s);
 cudaError_t pz_setup_kernels();
+size_t pz_build_smem_bytes(int n, bool direct);   // k_build shared memory for one instance
 int pz_step_launch_count();

@@ -387,6 +387,198 @@ __device__ void fill_matrix(double* A, const BuildCtx& B, const View& V, int kin
   __syncthreads();
 }
 
+// Entry (R, C) of the coupled operator of get_psiMat in
+// update_psi_coll_smat.f90:674-837 before equilibration.  Rows 0..N-1 are the
+// vorticity equation (boundary rows: psi = 0), rows N..2N-1 the streamfunction
+// equation (boundary rows: dpsi/dr = 0, rigid walls); columns 0..N-1 are the
+// Chebyshev coefficients of omega, N..2N-1 those of psi.  Ekman pumping and
+// (corio_term='IMPLICIT') the Coriolis term couple omega to psi.
+__device__ double2 smat_entry(const BuildCtx& B, const View& V, int m, double wlin, int R, int C) {
+  const PzInst& I = *B.I;
+  const int n = B.N;
+  const double rn = I.rnorm, dm = (double)m, dm2 = dm * dm;
+  const bool top = R < n, wcol = C < n;
+  const int i = top ? R : R - n, k = wcol ? C : C - n;
+  double re = 0.0, im = 0.0;
+  if (i == 0 || i == n - 1) {
+    if (!wcol && k < I.n_max) re = rn * (top ? B.rm(i, k) : B.drm(i, k));
+  } else {
+    const double r0 = B.rm(i, k), r1 = B.drm(i, k), r2 = B.d2rm(i, k);
+    const double or1 = V.rad(RV_OR1)[i], or2 = V.rad(RV_OR2)[i], beta = V.rad(RV_BETA)[i];
+    if (top && wcol) {
+      const double ekp = V.rad(RV_EKPUMP)[i];
+      re = rn * (r0 - wlin * (I.ViscFac * (r2 + or1 * r1 - dm2 * or2 * r0) - I.CorFac * ekp * r0));
+    } else if (top) {
+      const double ekp = V.rad(RV_EKPUMP)[i], eup = V.rad(RV_EKP_UP)[i];
+      const double eus = V.rad(RV_EKP_US)[i], edp = V.rad(RV_EKP_DUSDP)[i];
+      // -rn w CorFac ekp (eup d/dr + eup beta - (i m edp + eus) i m / r) - rn w CorFac beta i m / r
+      re = -rn * wlin * I.CorFac * ekp * (eup * r1 + (eup * beta + edp * dm2 * or1) * r0);
+      const double cor = (I.flags & PZF_COR_IMP) ? beta : 0.0;
+      im = rn * wlin * I.CorFac * or1 * dm * (ekp * eus - cor) * r0;
+    } else if (wcol) {
+      re = rn * r0;
+    } else {
+      re = rn * (r2 + (or1 + beta) * r1 + (or1 * beta + V.rad(RV_DBETA)[i] - dm2 * or2) * r0);
+    }
+  }
+  if (k == 0 || k == n - 1) { re *= 0.5; im *= 0.5; }   // boundary_fac
+  return make_double2(re, im);
+}
+
+// Gauss-Jordan inversion with partial pivoting (pivot: max |re| + |im|, the
+// cabs1 of izamax) of a complex row-major n x n matrix in shared memory.
+__device__ int gj_invert_c(double2* A, int n, int* piv, double2* colk, double* red, int* redi) {
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
+  for (int k = 0; k < n; ++k) {
+    double best = -1.0;
+    int bi = n;
+    for (int i = k + threadIdx.x; i < n; i += blockDim.x) {
+      const double v = fabs(A[i * n + k].x) + fabs(A[i * n + k].y);
+      if (v > best) { best = v; bi = i; }
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+      const double ov = __shfl_xor_sync(0xffffffffu, best, o);
+      const int oi = __shfl_xor_sync(0xffffffffu, bi, o);
+      if (ov > best || (ov == best && oi < bi)) { best = ov; bi = oi; }
+    }
+    if (lane == 0) { red[wid] = best; redi[wid] = bi; }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      double b = red[0];
+      int ib = redi[0];
+      for (int w = 1; w < nw; ++w)
+        if (red[w] > b || (red[w] == b && redi[w] < ib)) { b = red[w]; ib = redi[w]; }
+      piv[k] = ib;
+    }
+    __syncthreads();
+    const int p = piv[k];
+    if (p >= n || (A[p * n + k].x == 0.0 && A[p * n + k].y == 0.0)) return -1;
+    if (p != k) {
+      for (int j = threadIdx.x; j < n; j += blockDim.x) {
+        const double2 t = A[k * n + j]; A[k * n + j] = A[p * n + j]; A[p * n + j] = t;
+      }
+      __syncthreads();
+    }
+    const double2 pv = A[k * n + k];
+    const double den = pv.x * pv.x + pv.y * pv.y;
+    const double2 inv = make_double2(pv.x / den, -pv.y / den);
+    for (int i = threadIdx.x; i < n; i += blockDim.x) colk[i] = A[i * n + k];
+    __syncthreads();
+    for (int j = threadIdx.x; j < n; j += blockDim.x)
+      A[k * n + j] = cmul(j == k ? make_double2(1.0, 0.0) : A[k * n + j], inv);
+    __syncthreads();
+    for (int idx = threadIdx.x; idx < n * n; idx += blockDim.x) {
+      const int i = idx / n, j = idx - i * n;
+      if (i != k) A[idx] = csub(j == k ? make_double2(0.0, 0.0) : A[idx], cmul(colk[i], A[k * n + j]));
+    }
+    __syncthreads();
+  }
+  for (int k = n - 1; k >= 0; --k) {
+    const int p = piv[k];
+    if (p != k) {
+      for (int i = threadIdx.x; i < n; i += blockDim.x) {
+        const double2 t = A[i * n + k]; A[i * n + k] = A[i * n + p]; A[i * n + p] = t;
+      }
+    }
+    __syncthreads();
+  }
+  return 0;
+}
+
+// smat operator of one m /= 0 by block elimination of the equilibrated
+// system As = diag(f1) A diag(f2) = [[A11, A12], [A21, D]] (f1 = 1/max|row|,
+// then f2 = 1/max|col|, update_psi_coll_smat.f90:810-826): with E = D^-1 A21
+// and the Schur complement S = A11 - A12 E (complex),
+//   As^-1 [:, :N] = [S^-1 ; -E S^-1],
+// so G = diag(f2) As^-1[:, :N] diag(f1[:N]) gives (omega, psi)_cheb = G rhs.
+// Shared memory: S (complex N^2) | E (N^2, padded to an even count) | f1, f2,
+// pivot column (2N each) | reductions | pivots; D^-1 occupies the first N^2
+// doubles before S is formed.
+__device__ int build_smat(double* G, const BuildCtx& B, const View& V, int m, double wlin) {
+  extern __shared__ double shb[];
+  const PzInst& I = *B.I;
+  const int n = B.N, n2 = 2 * n;
+  double* X = shb;
+  double2* Sx = reinterpret_cast<double2*>(X);
+  double* E = X + 2LL * n * n;
+  double* f1 = E + (((long long)n * n + 1) & ~1LL);   // even offset: colk below is read as double2
+  double* f2 = f1 + n2;
+  double* colk = f2 + n2;
+  double* red = colk + n2;
+  int* redi = reinterpret_cast<int*>(red + 32);
+  int* piv = redi + 32;
+  for (int R = threadIdx.x; R < n2; R += blockDim.x) {
+    double mx = 0.0;
+    for (int C = 0; C < n2; ++C) {
+      const double2 a = smat_entry(B, V, m, wlin, R, C);
+      mx = fmax(mx, hypot(a.x, a.y));
+    }
+    f1[R] = 1.0 / mx;
+  }
+  __syncthreads();
+  for (int C = threadIdx.x; C < n2; C += blockDim.x) {
+    double mx = 0.0;
+    for (int R = 0; R < n2; ++R) {
+      const double2 a = smat_entry(B, V, m, wlin, R, C);
+      mx = fmax(mx, hypot(f1[R] * a.x, f1[R] * a.y));
+    }
+    f2[C] = 1.0 / mx;
+  }
+  __syncthreads();
+  // D (real), then D^-1
+  for (int idx = threadIdx.x; idx < n * n; idx += blockDim.x) {
+    const int k = idx / n, j = idx - k * n;
+    X[idx] = f1[n + k] * smat_entry(B, V, m, wlin, n + k, n + j).x * f2[n + j];
+  }
+  __syncthreads();
+  if (gj_invert(X, n, piv, colk, red, redi) != 0) return -1;
+  // E = D^-1 A21 with A21(k, j) = f1[N+k] rnorm rMat(k, j) bf(j) f2[j] on interior rows
+  for (int idx = threadIdx.x; idx < n * n; idx += blockDim.x) {
+    const int i = idx / n, j = idx - i * n;
+    double acc = 0.0;
+    for (int k = 1; k < n - 1; ++k) acc = fma(X[i * n + k] * f1[n + k], B.rm(k, j), acc);
+    const double bf = (j == 0 || j == n - 1) ? 0.5 : 1.0;
+    E[idx] = acc * I.rnorm * bf * f2[j];
+  }
+  __syncthreads();
+  // S = A11 - A12 E
+  for (int idx = threadIdx.x; idx < n * n; idx += blockDim.x) {
+    const int i = idx / n, j = idx - i * n;
+    const double2 a = smat_entry(B, V, m, wlin, i, j);
+    double re = f1[i] * a.x * f2[j], im = 0.0;
+    for (int k = 0; k < n; ++k) {
+      const double2 b = smat_entry(B, V, m, wlin, i, n + k);
+      const double w = f1[i] * f2[n + k] * E[k * n + j];
+      re = fma(-b.x, w, re);
+      im = fma(-b.y, w, im);
+    }
+    Sx[idx] = make_double2(re, im);
+  }
+  __syncthreads();
+  if (gj_invert_c(Sx, n, piv, reinterpret_cast<double2*>(colk), red, redi) != 0) return -1;
+  double2* Gc = reinterpret_cast<double2*>(G);
+  for (int idx = threadIdx.x; idx < n2 * n; idx += blockDim.x) {
+    const int c = idx / n2, r = idx - c * n2;
+    double2 v = make_double2(0.0, 0.0);
+    if (r < n) {
+      if (r < I.n_max) v = cscale(f2[r] * f1[c], Sx[r * n + c]);
+    } else {
+      const int i = r - n;
+      if (i < I.n_max) {
+        double vr = 0.0, vi = 0.0;
+        for (int k = 0; k < n; ++k) {
+          const double e = E[i * n + k];
+          vr = fma(e, Sx[k * n + c].x, vr);
+          vi = fma(e, Sx[k * n + c].y, vi);
+        }
+        v = make_double2(-f2[r] * vr * f1[c], -f2[r] * vi * f1[c]);
+      }
+    }
+    Gc[idx] = v;
+  }
+  return 0;
+}
+
 struct BuildSmem {
   double* A; double* f1; double* f2; double* colk; double* red; int* redi; int* piv;
   double2* va; double2* vb;
@@ -471,6 +663,12 @@ __global__ void __launch_bounds__(PZ_THREADS) k_build(PzDev d) {
     store_op(d.pool + I.o_guphi, s.A, n, I.n_max, nullptr, nullptr);
     return;
   }
+  if (I.flags & PZF_DIRECT) {
+    // coupled (omega, psi) operator of update_om_coll_smat
+    __syncthreads();
+    if (build_smat(d.pool + I.o_gsm + 4LL * mi * n * n, B, V, m, wlin) != 0) flag_status(S, PZ_E_SINGULAR);
+    return;
+  }
   // omega (get_omMat: row and column scaling)
   fill_matrix(s.A, B, V, 1, m, wlin);
   equilibrate(s.A, n, s.f1, s.f2, true);
@@ -522,6 +720,22 @@ __global__ void __launch_bounds__(PZ_THREADS) k_build(PzDev d) {
 // fields, init_fields.f90:228-255, and by start_from_another_scheme,
 // step_time.f90:417-516).  Writes old/impl logical slot 1 at ring bases bo/bi.
 // ---------------------------------------------------------------------------
+// implicit Ekman pumping and Coriolis terms of the smat vorticity equation,
+// get_psi_rhs_imp_coll_smat (update_psi_coll_smat.f90:380-527), m /= 0:
+//   -CorFac ekpump (om + ekp_up up + (i m ekp_dusdp + ekp_us) us) [+ CorFac beta us]
+__device__ __forceinline__ double2 smat_imp_extra(const PzInst& I, const View& V, int i, double dm, double2 om,
+                                                  double2 up, double2 us) {
+  const double ce = I.CorFac * V.rad(RV_EKPUMP)[i];
+  const double eus = V.rad(RV_EKP_US)[i], edp = V.rad(RV_EKP_DUSDP)[i], eup = V.rad(RV_EKP_UP)[i];
+  const double2 q = make_double2(eus * us.x - edp * dm * us.y, eus * us.y + edp * dm * us.x);
+  double2 v = make_double2(-ce * (om.x + eup * up.x + q.x), -ce * (om.y + eup * up.y + q.y));
+  if (I.flags & PZF_COR_IMP) {
+    const double cb = I.CorFac * V.rad(RV_BETA)[i];
+    v.x += cb * us.x; v.y += cb * us.y;
+  }
+  return v;
+}
+
 struct MS {   // per-m vectors in shared memory
   double2 *a, *b, *c, *e, *f, *g, *h, *k;
   SymScratch w;
@@ -580,6 +794,7 @@ __device__ void imp_from_physical(const View& V, const PzInst& I, int mi, int bo
       if (calc) {
         double2 v = make_double2(I.ViscFac * (d2.x + or1[i] * d1.x - dm2 * or2[i] * x.x),
                                  I.ViscFac * (d2.y + or1[i] * d1.y - dm2 * or2[i] * x.y));
+        if (I.flags & PZF_DIRECT) v = cadd(v, smat_imp_extra(I, V, i, dm, x, up[i], V.fld(F_US, mi)[i]));
         if (I.flags & PZF_BUO_IMP) {
           const double2 b = cim(dm, T[i]);
           const double c = rgrav[i] * or1[i] * I.BuoFac;
@@ -694,6 +909,7 @@ __global__ void __launch_bounds__(256) k_mloop(PzDev d) {
   double2* T = V.fld(F_TEMP, mi);
   double2* dT = V.fld(F_DTEMP, mi);
   const bool buo_imp = (I.flags & PZF_BUO_IMP) != 0;
+  const bool direct = (I.flags & PZF_DIRECT) != 0;
 
   // -- finish_exp_temp_coll (update_temp_coll.f90:152-176)
   for (int i = threadIdx.x; i < n; i += blockDim.x) {
@@ -720,7 +936,9 @@ __global__ void __launch_bounds__(256) k_mloop(PzDev d) {
         double2 p = eP[i];
         p.x -= or1[i] * s.f[i].x;
         p.y -= or1[i] * s.f[i].y;
-        if (!(I.flags & PZF_NON_ROT)) {
+        // explicit Coriolis: always with dmat, unless implicit with smat
+        // (update_psi_coll_smat.f90:323-378)
+        if (direct ? !(I.flags & PZF_COR_IMP) : !(I.flags & PZF_NON_ROT)) {
           p.x += I.CorFac * beta[i] * u.x;
           p.y += I.CorFac * beta[i] * u.y;
         }
@@ -729,7 +947,7 @@ __global__ void __launch_bounds__(256) k_mloop(PzDev d) {
           const double cb = I.BuoFac * rgrav[i] * or1[i];
           p.x -= cb * b.x; p.y -= cb * b.y;
         }
-        if (I.flags & PZF_EK_PUMP) {
+        if (!direct && (I.flags & PZF_EK_PUMP)) {
           const double2 o = om[i], w = up[i];
           const double2 q = make_double2(ekp_us[i] * u.x - ekp_dusdp[i] * dm * u.y,
                                          ekp_us[i] * u.y + ekp_dusdp[i] * dm * u.x);
@@ -811,6 +1029,11 @@ __global__ void __launch_bounds__(256) k_mloop(PzDev d) {
         iP[i] = make_double2(I.ViscFac * (d2u + or1[i] * du - or2[i] * u) - I.CorFac * ekp[i] * u, 0.0);
     }
   } else {
+    if (direct) {
+      // update_om_coll_smat (update_psi_coll_smat.f90:88-321): one coupled solve
+      cmv_lanes(reinterpret_cast<const double2*>(d.pool + I.o_gsm) + 2LL * mi * n * n, n, s.a, s.b, s.e);
+      __syncthreads();
+    } else {
     mv_lanes(d.pool + I.o_gom + (long long)mi * n * n, n, s.a, s.b);  // omega, Chebyshev
     __syncthreads();
     mv_lanes(d.pool + I.o_gpsi + (long long)mi * n * n, n, s.b, s.e);  // -psi, Chebyshev (psi = -K om)
@@ -846,6 +1069,7 @@ __global__ void __launch_bounds__(256) k_mloop(PzDev d) {
       s.b[i] = o;
     }
     __syncthreads();
+    }
     op_D1c(V, n, s.e, s.g, s.w);                                     // dpsi/dr
     __syncthreads();
     op_C(V, n, s.e, s.h, s.w);                                       // psi
@@ -868,6 +1092,7 @@ __global__ void __launch_bounds__(256) k_mloop(PzDev d) {
       if (S.l_calc_lin) {
         double2 v = make_double2(I.ViscFac * (d2.x + or1[i] * d1.x - dm2 * or2[i] * o.x),
                                  I.ViscFac * (d2.y + or1[i] * d1.y - dm2 * or2[i] * o.y));
+        if (direct) v = cadd(v, smat_imp_extra(I, V, i, dm, o, up[i], us[i]));
         if (buo_imp) {
           const double2 b = cim(dm, s.f[i]);
           const double c = rgrav[i] * or1[i] * I.BuoFac;
@@ -992,6 +1217,9 @@ __global__ void k_gather_rows(PzDev d, double* out) {
   out[t] = d.pool[I.o_series + (long long)idx * PZ_SERIES_COLS + c];
 }
 
+size_t build_smat_smem_bytes(int n) {
+  return (3 * (size_t)n * n + 1 + 6 * (size_t)n + 32 + 16 + (size_t)(n + 1) / 2) * sizeof(double);
+}
 size_t build_smem_bytes(int n) {
   long long off = (long long)n * n + 3LL * n + 32 + 16 + (n + 1) / 2;
   off = (off + 1) & ~1LL;
@@ -1021,10 +1249,17 @@ size_t rloop_smem_bytes(int P, int M) {
 cudaError_t pz_setup_kernels() {
   cudaError_t e;
   const int big = 200 * 1024;
-  if ((e = cudaFuncSetAttribute(k_build, cudaFuncAttributeMaxDynamicSharedMemorySize, big))) return e;
+  if ((e = cudaFuncSetAttribute(k_build, cudaFuncAttributeMaxDynamicSharedMemorySize, PZ_SMEM_MAX))) return e;
   if ((e = cudaFuncSetAttribute(k_build_static, cudaFuncAttributeMaxDynamicSharedMemorySize, big))) return e;
   if ((e = cudaFuncSetAttribute(k_rloop, cudaFuncAttributeMaxDynamicSharedMemorySize, PZ_SMEM_MAX))) return e;
   return cudaSuccess;
+}
+
+size_t pz_build_smem_bytes(int n, bool direct) {
+  const size_t a = build_smem_bytes(n);
+  if (!direct) return a;
+  const size_t b = build_smat_smem_bytes(n);
+  return a > b ? a : b;
 }
 
 cudaError_t pz_launch_build_static(const PzDev& d, cudaStream_t s) {
@@ -1059,7 +1294,7 @@ cudaError_t pz_launch_step_kernel(const PzDev& d, int k, cudaStream_t s) {
   switch (k) {
     case 0: k_rloop<<<d.n_ritems, 256, rloop_smem_bytes(d.maxP, d.maxM), s>>>(d); break;
     case 1: k_cfl<<<d.n_inst, 32, 0, s>>>(d); break;
-    case 2: k_build<<<d.n_mitems, PZ_THREADS, build_smem_bytes(d.maxN), s>>>(d); break;
+    case 2: k_build<<<d.n_mitems, PZ_THREADS, d.smem_build, s>>>(d); break;
     case 3: k_mloop<<<d.n_mitems, mloop_threads(d.maxN), ms_smem_bytes(d.maxN), s>>>(d); break;
     case 4: k_obs<<<d.n_inst, PZ_THREADS, 0, s>>>(d, -1); break;
     default: return cudaErrorInvalidValue;

@@ -48,8 +48,9 @@ __global__ void __launch_bounds__(256) k_expl_rloop(PzExplArgs a) {
   rloop_group(I, V, blockIdx.x * PZ_RLOOP_G, io, sh, rsh);
 }
 
-// finish_exp_temp_coll and finish_exp_psi_coll_dmat for one m
-// (src/update_temp_coll.f90:152-176, src/update_psi_coll_dmat.f90:468-552)
+// finish_exp_temp_coll and finish_exp_psi_coll_{dmat,smat} for one m
+// (src/update_temp_coll.f90:152-176, src/update_psi_coll_dmat.f90:468-552,
+// src/update_psi_coll_smat.f90:323-378)
 __global__ void __launch_bounds__(PZ_THREADS) k_expl_finish(PzExplArgs a) {
   extern __shared__ double2 shm[];
   const PzInst& I = *a.inst;
@@ -89,7 +90,10 @@ __global__ void __launch_bounds__(PZ_THREADS) k_expl_finish(PzExplArgs a) {
       double2 p = a.dpsidt[o];
       p.x -= or1[i] * sf[i].x;
       p.y -= or1[i] * sf[i].y;
-      if (!(I.flags & PZF_NON_ROT)) {
+      const bool direct = (I.flags & PZF_DIRECT) != 0;
+      // explicit Coriolis: always with dmat, unless implicit with smat
+      // (update_psi_coll_smat.f90:323-378)
+      if (direct ? !(I.flags & PZF_COR_IMP) : !(I.flags & PZF_NON_ROT)) {
         p.x += I.CorFac * beta[i] * u.x;
         p.y += I.CorFac * beta[i] * u.y;
       }
@@ -98,7 +102,7 @@ __global__ void __launch_bounds__(PZ_THREADS) k_expl_finish(PzExplArgs a) {
         const double cb = I.BuoFac * rgrav[i] * or1[i];
         p.x -= cb * b.x; p.y -= cb * b.y;
       }
-      if (I.flags & PZF_EK_PUMP) {
+      if (!direct && (I.flags & PZF_EK_PUMP)) {   // implicit with smat
         const double2 w = a.om[o], v = a.up[o];
         const double2 q = make_double2(ekp_us[i] * u.x - ekp_dusdp[i] * dm * u.y,
                                        ekp_us[i] * u.y + ekp_dusdp[i] * dm * u.x);

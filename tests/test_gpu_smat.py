@@ -1,0 +1,121 @@
+"""The coupled (omega, psi) solve of matrix_solve='DIRECT' (pizza's default,
+update_psi_coll_smat.f90) on the GPU against the oracle and the reference
+fixtures (needs a GB300).
+
+The GPU applies, per m, the first N columns of the inverse of the
+equilibrated 2N x 2N operator, formed by block elimination through the real
+streamfunction block; pizza solves the same system with zgetrf/zgetrs.  The
+two agree to ~1e-12 (N=33) .. 2e-10 (N=97) per solve relative to the
+solution's magnitude, so the field tolerance over many steps is 1e-10 for
+N <= 33 and 1e-9 above.
+"""
+import json
+import os
+
+import numpy as np
+import pytest
+
+from tests.helpers import gpu_config, oracle, rel_err, seeded, series_from_oracle
+from tests.test_gpu_parity import run_pair, check_fields
+
+pytestmark = pytest.mark.gpu
+HERE = os.path.dirname(os.path.abspath(__file__))
+
+C0D = dict(n_r_max=33, n_cheb_max=33, m_max=32, ek=1e-3, ra=1e5, pr=1.0, radratio=0.35,
+           l_ek_pump=True, time_scheme="CNAB2", dtMax=1e-4, matrix_solve="DIRECT")
+
+
+@pytest.fixture(scope="module")
+def pz():
+    import torch
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    from pizza_gb300 import build as b
+    b.build()
+    import pizza_gb300
+    return pizza_gb300
+
+
+def test_c0_direct_cnab2_200_steps(pz):
+    sim, ens, out = run_pair(pz, C0D, 200, checkpoints=(1, 10))
+    for k, s, g in out:
+        check_fields(s, g, 1e-10, f"smat step {k}")
+    ref = series_from_oracle(sim)
+    np.testing.assert_allclose(ens.series(0)[-1, :15], ref[:15], rtol=1e-10, atol=1e-14)
+
+
+@pytest.mark.parametrize("case", ["RotE1e3EkPump", "MultistepSchemes"])
+def test_golden_smat_fixtures_on_gpu(pz, case):
+    """Reference fixtures written by pizza.exe with the default smat solve."""
+    with open(os.path.join(HERE, "golden", "cases.json")) as f:
+        spec = json.load(f)[case]
+    p = dict(spec["params"])
+    ref = np.loadtxt(os.path.join(HERE, "golden", f"{case}.txt"))
+    sim = oracle(p)                          # init_t > 0 start field built by the oracle
+    temp0 = sim.temp.copy()
+    ens = pz.Ensemble(gpu_config(p))
+    ens.set_state(0, temp=temp0)
+    n, nlog = p["n_time_steps"], p["n_log_step"]
+    ens.step(n)
+    rows = ens.series(0, n + 1)[::nlog]
+    got = rows[:, [0, 4, 5, 6, 7]]           # e_kin_3D columns
+    assert got.shape == ref.shape
+    np.testing.assert_allclose(got, ref, rtol=1e-8, atol=1e-14)
+
+
+@pytest.mark.parametrize("variant", [
+    dict(corio_term="EXPLICIT"),
+    dict(l_ek_pump=False),
+    dict(time_scheme="SBDF3"),
+    dict(pr=0.7),
+    dict(l_non_rot=True, ra=2e4),
+    dict(buo_term="EXPLICIT"),
+])
+def test_direct_variants(pz, variant):
+    spec = dict(C0D, **variant)
+    sim, ens, out = run_pair(pz, spec, 30, seed=7)
+    check_fields(sim, out[-1][2], 1e-10, str(variant))
+
+
+def test_direct_larger_grids(pz):
+    for spec in (dict(C0D, n_r_max=65, n_cheb_max=65, m_max=64, ek=1e-4, ra=2e6, dtMax=2e-5),
+                 dict(C0D, n_r_max=97, n_cheb_max=97, m_max=42, ek=1e-4, ra=1e6, dtMax=2e-5)):
+        sim, ens, out = run_pair(pz, spec, 10, seed=9)
+        check_fields(sim, out[-1][2], 1e-9, f"N={spec['n_r_max']}")
+
+
+def test_mixed_direct_and_influence_batch(pz):
+    specs = [C0D, dict(C0D, matrix_solve="INFLUENCE"), dict(C0D, n_r_max=49, m_max=64, ek=1e-4, ra=1e6, dtMax=2e-5)]
+    temps = [seeded(s, 20 + i) for i, s in enumerate(specs)]
+    ens = pz.Ensemble([gpu_config(s) for s in specs])
+    ens.set_state_all(temps)
+    ens.step(15)
+    for i, s in enumerate(specs):
+        sim = oracle(s, temp0=temps[i])
+        for _ in range(15):
+            sim.advance()
+        check_fields(sim, ens.get_state(i), 1e-10, f"instance {i}")
+
+
+def test_direct_explicit_terms_entry_point(pz):
+    """The stage entry point finishes the vorticity terms the smat way
+    (Ekman pumping implicit, Coriolis implicit)."""
+    import torch
+    spec = C0D
+    t0 = seeded(spec, 4)
+    sim = oracle(spec, temp0=t0)
+    for _ in range(3):
+        sim.advance()
+    ens = pz.Ensemble(gpu_config(spec))
+    dev = torch.device("cuda")
+    f = {k: torch.tensor(getattr(sim, k).T.copy(), dtype=torch.complex128, device=dev)
+         for k in ("us", "up", "om", "temp")}
+    dT, dP, dtr, dth = ens.explicit_terms(0, f["us"], f["up"], f["om"], f["temp"])
+    torch.cuda.synchronize()
+    sim.ts.istage = 1
+    dtempdt, dVsT, dpsidt, dVsOm = sim.radial_loop()
+    sim.dTdt.expl[0] = dtempdt
+    sim.dpsidt.expl[0] = dpsidt
+    sim.finish_explicit(dVsT, dVsOm)
+    assert rel_err(dT.cpu().numpy().T, sim.dTdt.expl[0]) < 1e-12
+    assert rel_err(dP.cpu().numpy().T, sim.dpsidt.expl[0]) < 1e-12
