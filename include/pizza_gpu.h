@@ -47,10 +47,26 @@ extern "C" {
 #define PZ_CNLF    4
 #define PZ_MODCNAB 5
 #define PZ_TVB33   6
+/* DIRK IMEX Runge-Kutta schemes (src/dirk_schemes.f90:35-244); those marked
+ * (A) end with an assembly stage (assemble_stage, src/step_time.f90:370-384) */
+#define PZ_ARS222    10
+#define PZ_ARS232    11   /* (A) */
+#define PZ_ARS233    12   /* (A) */
+#define PZ_SSP222    13   /* (A) */
+#define PZ_LSDIRK222 14   /* (A) */
+#define PZ_LZ232     15
+#define PZ_CK232     16
+#define PZ_ARS443    17
+#define PZ_BPR353    18
+#define PZ_PC2       19
+#define PZ_ARS343    20   /* (A) */
+#define PZ_MARS343   21   /* (A) */
+#define PZ_SSP322    22   /* (A) */
+#define PZ_SSP332    23   /* (A) */
 
 /* matrix_solve values (src/namelists.f90:416-421) */
 #define PZ_SOLVE_INFLUENCE 0   /* update_psi_coll_dmat: real om/psi solves + 2x2 influence matrix */
-#define PZ_SOLVE_DIRECT    1   /* update_psi_coll_smat: coupled 2N complex solve (not yet on GPU) */
+#define PZ_SOLVE_DIRECT    1   /* update_psi_coll_smat: coupled 2N complex solve */
 
 /*
  * One instance's namelist values.  Mirrors pizza's input.nml groups &grid,
@@ -149,8 +165,9 @@ void* pz_stream(pz_handle* h);
 
 /* Run n_steps steps launching the kernels one by one (no graph), with CUDA
  * events between them on the handle's stream; kernel_ms[k] receives the mean
- * device time per step of kernel k (k < pz_launches_per_step), names in
- * pz_kernel_name(k).  Synchronises. */
+ * device time per step of kernel kind k (k < PZ_KERNEL_KINDS, summed over the
+ * stages of a DIRK step), names in pz_kernel_name(k).  Synchronises. */
+#define PZ_KERNEL_KINDS 6
 int pz_step_profile(pz_handle* h, int n_steps, double* kernel_ms);
 const char* pz_kernel_name(int k);
 

@@ -310,6 +310,189 @@ class Multistep:
         self.nimp = old_order
 
 
+def dirk_tableau(name: str):
+    """Unscaled tableaux of the DIRK IMEX schemes (src/dirk_schemes.f90:35-244
+    for the stage counts and flags, :246-707 for the coefficients).
+
+    Returns nstages, l_assembly, gamma (the diagonal implicit weight), the
+    implicit and explicit Butcher matrices (sizet x sizet, sizet = nstages + 1
+    without an assembly stage, nstages with one), the assembly rows, the
+    per-stage flags l_exp_calc and l_imp_calc_rhs and the default courfac."""
+    r2, r3 = math.sqrt(2.0), math.sqrt(3.0)
+    n = name.upper()
+    exp_calc = None
+    imp1 = False              # l_imp_calc_rhs(1)
+    bai = bae = None
+    if n == "ARS222":
+        g = 0.5 * (2.0 - r2); d = 1.0 - 0.5 / g
+        ns, ass, cf = 2, False, 1.35
+        bi = [[0, 0, 0], [0, g, 0], [0, 1 - g, g]]
+        be = [[0, 0, 0], [g, 0, 0], [d, 1 - d, 0]]
+    elif n == "ARS232":
+        g = 0.5 * (2.0 - r2); d = -2.0 * r2 / 3.0
+        ns, ass, cf = 3, True, 1.35
+        bi = [[0, 0, 0], [0, g, 0], [0, 1 - g, g]]
+        be = [[0, 0, 0], [g, 0, 0], [d, 1 - d, 0]]
+        bai = bae = [0, 1 - g, g]
+    elif n == "ARS233":
+        g = (3.0 + r3) / 6.0
+        ns, ass, cf = 3, True, 1.35
+        bi = [[0, 0, 0], [0, g, 0], [0, 1 - 2 * g, g]]
+        be = [[0, 0, 0], [g, 0, 0], [g - 1, 2 * (1 - g), 0]]
+        bai = bae = [0, 0.5, 0.5]
+    elif n == "SSP222":
+        g = 1.0 - 1.0 / r2
+        ns, ass, cf = 3, True, 1.35
+        bi = [[0, 0, 0], [0, g, 0], [0, 1 - 2 * g, g]]
+        be = [[0, 0, 0], [0, 0, 0], [0, 1, 0]]
+        bai = bae = [0, 0.5, 0.5]
+    elif n == "LSDIRK222":
+        g = 1.0 - 1.0 / r2; ch = 1.0 / (2.0 * g)
+        ns, ass, cf = 3, True, 1.35
+        bi = [[0, 0, 0], [0, g, 0], [0, 1 - g, g]]
+        be = [[0, 0, 0], [0, 0, 0], [0, ch, 0]]
+        bai = bae = [0, 1 - g, g]
+    elif n == "LZ232":
+        g = 0.5
+        ns, ass, cf, imp1 = 2, False, 1.25, True
+        bi = [[0, 0, 0], [-0.25, 0.5, 0], [0.5, 0, 0.5]]
+        be = [[0, 0, 0], [0.25, 0, 0], [-1, 2, 0]]
+    elif n == "CK232":
+        g = 1.0 - 0.5 * r2
+        ns, ass, cf, imp1 = 2, False, 1.25, True
+        bi = [[0, 0, 0], [-1.0 / 3.0 + 0.5 * r2, g, 0], [0.75 - 0.25 * r2, -0.75 + 0.75 * r2, g]]
+        be = [[0, 0, 0], [2.0 / 3.0, 0, 0], [0.25, 0.75, 0]]
+    elif n == "ARS443":
+        g = 0.5
+        ns, ass, cf = 4, False, 0.9
+        bi = [[0, 0, 0, 0, 0], [0, 0.5, 0, 0, 0], [0, 1.0 / 6.0, 0.5, 0, 0], [0, -0.5, 0.5, 0.5, 0],
+              [0, 1.5, -1.5, 0.5, 0.5]]
+        be = [[0, 0, 0, 0, 0], [0.5, 0, 0, 0, 0], [11.0 / 18.0, 1.0 / 18.0, 0, 0, 0],
+              [5.0 / 6.0, -5.0 / 6.0, 0.5, 0, 0], [0.25, 1.75, 0.75, -1.75, 0]]
+    elif n == "BPR353":
+        g = 0.5
+        ns, ass, cf, imp1 = 4, False, 1.0, True
+        bi = [[0, 0, 0, 0, 0], [0.5, 0.5, 0, 0, 0], [5.0 / 18.0, -1.0 / 9.0, 0.5, 0, 0], [0.5, 0, 0, 0.5, 0],
+              [0.25, 0, 0.75, -0.5, 0.5]]
+        be = [[0, 0, 0, 0, 0], [1, 0, 0, 0, 0], [4.0 / 9.0, 2.0 / 9.0, 0, 0, 0], [0.25, 0, 0.75, 0, 0],
+              [0.25, 0, 0.75, 0, 0]]
+        exp_calc = [True, True, True, False]
+    elif n == "PC2":
+        g = 0.5
+        ns, ass, cf, imp1 = 3, False, 0.8, True
+        bi = [[0, 0, 0, 0], [0.5, 0.5, 0, 0], [0.5, 0, 0.5, 0], [0.5, 0, 0, 0.5]]
+        be = [[0, 0, 0, 0], [1, 0, 0, 0], [0.5, 0.5, 0, 0], [0.5, 0, 0.5, 0]]
+    elif n in ("ARS343", "MARS343"):
+        if n == "ARS343":
+            g = 0.435866521508459
+            b1 = -1.5 * g * g + 4.0 * g - 0.25
+            b2 = 1.5 * g * g - 5.0 * g + 1.25
+            cf = 0.7
+            be = [[0, 0, 0, 0], [g, 0, 0, 0], [0.3212788860286278, 0.3966543747256017, 0, 0],
+                  [-0.1058582960718797, 0.5529291480359398, 0.5529291480359398, 0]]
+        else:
+            g = 0.435866521508458
+            b1, b2 = 1.20849664917601, -0.64436317068446
+            cf = 0.5
+            be = [[0, 0, 0, 0], [0.877173304301691, 0, 0, 0], [0.535396540307354, 0.182536720446875, 0, 0],
+                  [0.63041255815287, -0.83193390106308, 1.20152134291021, 0]]
+        ns, ass = 4, True
+        bi = [[0, 0, 0, 0], [0, g, 0, 0], [0, 0.5 * (1 - g), g, 0], [0, b1, b2, g]]
+        bai = bae = [0, b1, b2, g]
+    elif n == "SSP322":
+        g = 0.5
+        ns, ass, cf = 4, True, 1.35
+        bi = [[0, 0, 0, 0], [0, 0.5, 0, 0], [0, -0.5, 0.5, 0], [0, 0, 0.5, 0.5]]
+        be = [[0, 0, 0, 0], [0, 0, 0, 0], [0, 0, 0, 0], [0, 0, 1, 0]]
+        bai = bae = [0, 0, 0.5, 0.5]
+    elif n == "SSP332":
+        g = 1.0 - 1.0 / r2
+        ns, ass, cf = 4, True, 1.35
+        bi = [[0, 0, 0, 0], [0, g, 0, 0], [0, 1 - 2 * g, g, 0], [0, 0.5 - g, 0, g]]
+        be = [[0, 0, 0, 0], [0, 0, 0, 0], [0, 1, 0, 0], [0, 0.25, 0.25, 0]]
+        bai = bae = [0, 1.0 / 6.0, 1.0 / 6.0, 2.0 / 3.0]
+    else:
+        return None
+    bi = np.array(bi, float)
+    be = np.array(be, float)
+    sizet = bi.shape[0]
+    assert sizet == (ns if ass else ns + 1)
+    return dict(nstages=ns, l_assembly=ass, gamma=g, bimp=bi, bexp=be,
+                bass_imp=np.array(bai if bai is not None else np.zeros(sizet), float),
+                bass_exp=np.array(bae if bae is not None else np.zeros(sizet), float),
+                l_exp_calc=exp_calc if exp_calc is not None else [True] * ns,
+                l_imp_calc_rhs=[imp1] + [True] * (ns - 1), courfac=cf)
+
+
+DIRK_SCHEMES = ("ARS222", "ARS232", "ARS233", "SSP222", "LSDIRK222", "LZ232", "CK232", "ARS443",
+                "BPR353", "PC2", "ARS343", "MARS343", "SSP322", "SSP332")
+
+
+class Dirk:
+    """type_dirk (src/dirk_schemes.f90): Butcher weights scaled by dt, the
+    stage right-hand side and the assembly stage."""
+
+    def __init__(self, time_scheme: str, courfac_nml: float):
+        t = dirk_tableau(time_scheme)
+        if t is None:
+            raise ValueError(f"time integrator {time_scheme} not found")
+        self.time_scheme = time_scheme.upper()
+        self.family = "DIRK"
+        self.tab = t
+        self.nstages = t["nstages"]
+        self.nold, self.nimp, self.nexp = 1, t["nstages"], t["nstages"]
+        self.l_assembly = t["l_assembly"]
+        self.l_exp_calc = list(t["l_exp_calc"])
+        self.l_imp_calc_rhs = list(t["l_imp_calc_rhs"])
+        self.istage = 1
+        self.courfac = t["courfac"] if abs(courfac_nml) >= 1.0e3 else courfac_nml
+        self.dt = np.zeros(1)
+        self.wimp_lin = np.zeros(1)
+
+    def set_weights(self) -> bool:
+        """set_weights (dirk_schemes.f90:275-712): everything scaled by dt(1).
+        Unlike the multistep family it never requests a matrix rebuild."""
+        dt = self.dt[0]
+        t = self.tab
+        self.wimp_lin[0] = dt * t["gamma"]
+        self.butcher_imp = dt * t["bimp"]
+        self.butcher_exp = dt * t["bexp"]
+        self.butcher_ass_imp = dt * t["bass_imp"]
+        self.butcher_ass_exp = dt * t["bass_exp"]
+        return False
+
+    def set_dt_array(self, dt_new: float, dt_min: float):
+        """set_dt_array (dirk_schemes.f90:714-760)."""
+        self.dt[0] = dt_new
+        if dt_new < dt_min:
+            raise FloatingPointError(f"time step too small, dt={dt_new!r}")
+
+    def set_imex_rhs(self, ta: "TArray") -> np.ndarray:
+        """set_imex_rhs (dirk_schemes.f90:762-795): stage istage."""
+        s = self.istage
+        rhs = ta.old[0].copy()
+        for k in range(s):
+            rhs = rhs + self.butcher_exp[s, k] * ta.expl[k]
+        for k in range(s):
+            rhs = rhs + self.butcher_imp[s, k] * ta.impl[k]
+        return rhs
+
+    def rotate_imex(self, ta: "TArray"):
+        """rotate_imex (dirk_schemes.f90:833-838): nothing to rotate."""
+
+    def bridge_with_cnab2(self):
+        """bridge_with_cnab2 (dirk_schemes.f90:840-844): nothing to bridge."""
+
+    def assemble_imex(self, ta: "TArray") -> np.ndarray:
+        """assemble_imex (dirk_schemes.f90:852-882)."""
+        rhs = ta.old[0].copy()
+        for k in range(self.nstages):
+            rhs = rhs + self.butcher_ass_exp[k] * ta.expl[k]
+        for k in range(self.nstages):
+            rhs = rhs + self.butcher_ass_imp[k] * ta.impl[k]
+        return rhs
+
+
 class TArray:
     """type_tarray (src/time_array.f90:11-71): old/impl/expl history slots."""
 
@@ -588,7 +771,10 @@ class Pizza:
         self.l_direct = d["l_direct_solve"]
         self.cheb = Cheb(N, N, d["r_icb"], d["r_cmb"])
         self._radial()
-        self.ts = Multistep(p.time_scheme, p.courfac, p.alpha)
+        if p.time_scheme.upper() in DIRK_SCHEMES:
+            self.ts = Dirk(p.time_scheme, p.courfac)
+        else:
+            self.ts = Multistep(p.time_scheme, p.courfac, p.alpha)
         shp = (self.M, N)
         ts = self.ts
         # dt_fieldsLast.f90:35-215: histories, explicit containers (1 stage)
@@ -1119,9 +1305,9 @@ class Pizza:
         self.temp = temp
         ts.rotate_imex(self.dTdt)
         if ts.istage == ts.nstages:
-            self._temp_rhs_imp(1, ts.l_imp_calc_rhs, l_in_cheb=True)
+            self._temp_rhs_imp(1, self._calc_rhs(1), l_in_cheb=True)
         else:
-            self._temp_rhs_imp(ts.istage + 1, ts.l_imp_calc_rhs, l_in_cheb=True)
+            self._temp_rhs_imp(ts.istage + 1, self._calc_rhs(ts.istage + 1), l_in_cheb=True)
         if l_log_next:
             self.dtemp = self.cheb.get_dr(self.temp)
 
@@ -1193,13 +1379,125 @@ class Pizza:
         self.psi, self.us, self.up, self.om = psi, us, up, om
         ts.rotate_imex(self.dpsidt)
         if ts.istage == ts.nstages:
-            self._psi_rhs_imp(1, ts.l_imp_calc_rhs, l_in_cheb=True)
+            self._psi_rhs_imp(1, self._calc_rhs(1), l_in_cheb=True)
         else:
-            self._psi_rhs_imp(ts.istage + 1, ts.l_imp_calc_rhs, l_in_cheb=True)
+            self._psi_rhs_imp(ts.istage + 1, self._calc_rhs(ts.istage + 1), l_in_cheb=True)
+
+    def _calc_rhs(self, stage):
+        """l_imp_calc_rhs of the stage whose implicit term is formed next: one
+        flag for the multistep family, one per stage for DIRK."""
+        f = self.ts.l_imp_calc_rhs
+        return f[stage - 1] if isinstance(f, list) else f
+
+    def _ass_mat(self, m):
+        """get_assMat (update_psi_coll_smat.f90:839-917 = dmat:1056-1134): the
+        streamfunction from the assembled vorticity, psi = dpsi/dr = 0 on both
+        rigid walls; dt independent, not equilibrated."""
+        c = self.cheb
+        N, n_max = self.N, self.n_max
+        A = np.zeros((N, N))
+        rn = c.rnorm
+        A[0, :n_max] = rn * c.rMat[0, :n_max]
+        A[N - 1, :n_max] = rn * c.rMat[N - 1, :n_max]
+        A[1, :n_max] = rn * c.drMat[0, :n_max]                 # ktopv = 2
+        A[N - 2, :n_max] = rn * c.drMat[N - 1, :n_max]         # kbotv = 2
+        dm2 = float(m) * float(m)
+        i = slice(2, N - 2)
+        or1, or2 = self.or1[i, None], self.or2[i, None]
+        be, dbe = self.beta[i, None], self.dbeta[i, None]
+        A[i, :] = -rn * (c.d2rMat[i] + (or1 + be) * c.drMat[i] + (or1 * be + dbe - dm2 * or2) * c.rMat[i])
+        self._bfac_cols(A, (0, N - 1))
+        return self._lu(A, "assMat")
+
+    def assemble_stage(self, l_log_next=True):
+        """assemble_stage (mloop.f90): assemble_temp_coll
+        (update_temp_coll.f90:238-307) and assemble_psi_coll_{smat,dmat}
+        (update_psi_coll_smat.f90:529-672)."""
+        c, ts = self.cheb, self.ts
+        N, M, n_max = self.N, self.M, self.n_max
+        m = self.mvec
+        # temperature: interior from the assembled rhs, Dirichlet rows (robin_bc)
+        work = ts.assemble_imex(self.dTdt)
+        temp = self.temp.copy()
+        temp[:, 1:N - 1] = work[:, 1:N - 1]
+        temp[0, 1:N - 1] = work[0, 1:N - 1].real + 0j
+        temp[:, 0] = self.topt
+        temp[:, N - 1] = self.bott
+        self.temp = temp
+        self._temp_rhs_imp(1, self._calc_rhs(1), l_in_cheb=False)
+        if l_log_next:
+            self.dtemp = c.get_dr(self.temp)
+        # streamfunction from the assembled vorticity
+        work = ts.assemble_imex(self.dpsidt)
+        up0 = np.zeros(N)
+        up0[1:N - 1] = work[0, 1:N - 1].real                   # rigid walls: u_phi = 0
+        if not hasattr(self, "_assmats"):
+            self._assmats = [None] + [self._ass_mat(int(m[i])) for i in range(1, M)]
+        psi = np.zeros((M, N), complex)
+        for i in range(1, M):
+            rhs1 = np.zeros(N, complex)
+            rhs1[2:N - 2] = work[i, 2:N - 2]
+            x = self._solve_real(self._assmats[i], rhs1)
+            psi[i, :n_max] = x[:n_max]
+        om0 = c.get_dr_real(up0)
+        dpsi, d2psi = c.get_ddr(psi, l_dct=False)
+        psi = c.costf1(psi)
+        mm = m[:, None].astype(float)
+        us = 1j * mm * self.or1 * psi
+        up = -dpsi - self.beta * psi
+        om = -(d2psi + (self.or1 + self.beta) * dpsi
+               + (self.or1 * self.beta + self.dbeta - mm ** 2 * self.or2) * psi)
+        us[0] = 0.0
+        up[0] = up0
+        om[0] = om0 + self.or1 * up0
+        self.psi, self.us, self.up, self.om = psi, us, up, om
+        self._psi_rhs_imp(1, self._calc_rhs(1), l_in_cheb=False)
+
+    def _advance_dirk(self, l_log_next=True):
+        """One time step of a DIRK scheme: the stage loop of time_loop
+        (step_time.f90:210-368) and the assembly stage (:370-384)."""
+        ts, p = self.ts, self.p
+        self.n_time_step += 1
+        n_time_step = self.n_time_step
+        ts.istage = 1
+        lMat = False
+        for n_stage in range(1, ts.nstages + 1):
+            if ts.l_exp_calc[n_stage - 1]:
+                dtempdt, dVsT, dpsidt, dVsOm = self.radial_loop()
+                self.dTdt.expl[ts.istage - 1] = dtempdt
+                self.dpsidt.expl[ts.istage - 1] = dpsidt
+                self.finish_explicit(dVsT, dVsOm)
+            l_new_dt = False
+            if ts.istage == 1:
+                l_new_dt, dt_new = self.dt_courant()
+                sched = getattr(self, "dt_schedule", None)
+                if sched is not None and n_time_step - 1 < len(sched):
+                    dt_new = float(sched[n_time_step - 1])
+                    l_new_dt = dt_new != ts.dt[0]
+                self.l_new_dt = l_new_dt
+                ts.set_dt_array(dt_new, self.dtMin)
+                if ts.set_weights():
+                    self.lMatNext = True
+                self.time = self.time + ts.dt[0]
+            lMat = self.lMatNext
+            if (l_new_dt or lMat) and ts.istage == 1:
+                lMat = True
+            self.lMatNext = False
+            if (not ts.l_assembly) or ts.istage != ts.nstages:
+                if lMat or not self._mats_built:
+                    self.build_matrices()
+                self.update_temp(lMat, l_log_next)
+                self.update_om()
+                ts.istage += 1
+        if ts.l_assembly:
+            self.assemble_stage(l_log_next)
+        return lMat
 
     # -- one iteration of the outer loop (src/step_time.f90:139-406) ----------
     def advance(self, l_log_next=True):
         """One time step (stage body, multistep family: one stage)."""
+        if self.ts.family == "DIRK":
+            return self._advance_dirk(l_log_next)
         ts, p = self.ts, self.p
         self.n_time_step += 1
         n_time_step = self.n_time_step

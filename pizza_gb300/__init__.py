@@ -24,7 +24,12 @@ _HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(_HERE, "_lib", "libpizza_gb300.so")
 
 SCHEMES = {"CNAB2": 0, "SBDF2": 1, "BDF2AB2": 1, "SBDF3": 2, "BDF3AB3": 2, "SBDF4": 3,
-           "BDF4AB4": 3, "CNLF": 4, "MODCNAB": 5, "TVB33": 6}
+           "BDF4AB4": 3, "CNLF": 4, "MODCNAB": 5, "TVB33": 6,
+           # DIRK IMEX Runge-Kutta (src/dirk_schemes.f90)
+           "ARS222": 10, "ARS232": 11, "ARS233": 12, "SSP222": 13, "LSDIRK222": 14, "LZ232": 15,
+           "CK232": 16, "ARS443": 17, "BPR353": 18, "PC2": 19, "ARS343": 20, "MARS343": 21,
+           "SSP322": 22, "SSP332": 23}
+KERNEL_KINDS = 6
 SOLVE_INFLUENCE, SOLVE_DIRECT = 0, 1
 SERIES_COLS = 16
 SERIES_NAMES = ("time", "us2_2D", "up2_2D", "up2_axi_2D", "us2_3D", "up2_3D", "uz2_3D",
@@ -329,10 +334,9 @@ class Ensemble:
 
     def profile_steps(self, n_steps):
         """Mean device ms per step of each kernel, launched one by one."""
-        nk = self.launches_per_step()
-        ms = np.zeros(nk)
+        ms = np.zeros(KERNEL_KINDS)
         self._check(self.lib.pz_step_profile(self._h, int(n_steps), _dptr(ms)))
-        return {self.lib.pz_kernel_name(k).decode(): float(ms[k]) for k in range(nk)}
+        return {self.lib.pz_kernel_name(k).decode(): float(ms[k]) for k in range(KERNEL_KINDS)}
 
     def close(self):
         if getattr(self, "_h", None):

@@ -716,7 +716,7 @@ cudaError_t launch_ckpt(const PzAdjDev& a, int c, int dir, cudaStream_t s) {
 // one forward step without the time series: k_rloop, k_cfl, k_build, k_mloop
 cudaError_t launch_fwd(const PzDev& d, cudaStream_t s) {
   for (int k = 0; k < 4; ++k) {
-    const cudaError_t e = pz_launch_step_kernel(d, k, s);
+    const cudaError_t e = pz_launch_step_kernel(d, k, 1, s);
     if (e) return e;
   }
   return cudaSuccess;
@@ -903,7 +903,7 @@ extern "C" int pz_adjoint_backward(pz_handle* h, double* dJ_dtemp, double* dJ_dr
         }
       if (rebuild) {
         k_adj_bstate<<<(h->n_inst + 63) / 64, 64, 0, s>>>(a, n);
-        if ((e = cudaGetLastError()) || (e = pz_launch_step_kernel(dB, 2, s))) return acuda(h, e, "rebuild");
+        if ((e = cudaGetLastError()) || (e = pz_launch_step_kernel(dB, PZK_BUILD, 1, s))) return acuda(h, e, "rebuild");
       }
       const int slot = n - k0;
       k_adj_solve<<<h->dev.n_mitems, threads, smem, s>>>(a, n, slot);

@@ -31,6 +31,7 @@ struct pz_handle {
   double* d_rows = nullptr;    // n_inst x PZ_SERIES_COLS gather buffer
   std::string err = "no error";
   PzAdjoint* adj = nullptr;   // allocated by the first adjoint call
+  std::vector<PzLaunch> plan;  // kernel launches of one step, in order
 };
 
 // host helpers of pz_host.cu

@@ -12,6 +12,7 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <initializer_list>
 #include <map>
 #include <string>
 #include <vector>
@@ -185,9 +186,153 @@ bool factor_fft(int P, int* radix, int* nrad) {
   return n == 1;
 }
 
+// DIRK tableau (dirk_schemes.f90:35-244 for the stage counts and flags,
+// :246-707 for the coefficients): unscaled Butcher matrices of size sizet
+// (nstages+1, or nstages with an assembly stage), the assembly rows, the
+// diagonal weight gamma, per-stage l_exp_calc / l_imp_calc_rhs bits and the
+// default courfac.
+struct DirkTab {
+  int nstages = 0, assembly = 0, sizet = 0, exp_mask = 0, imp_mask = 0;
+  double gamma = 0.0, courfac = 0.0;
+  double bimp[PZ_BT_LD][PZ_BT_LD] = {}, bexp[PZ_BT_LD][PZ_BT_LD] = {};
+  double bai[PZ_BT_LD] = {}, bae[PZ_BT_LD] = {};
+};
+bool dirk_tableau(int scheme, DirkTab* t) {
+  const double r2 = std::sqrt(2.0), r3 = std::sqrt(3.0);
+  bool imp1 = false;
+  auto rows = [&](std::initializer_list<std::initializer_list<double>> bi,
+                  std::initializer_list<std::initializer_list<double>> be) {
+    int i = 0;
+    for (auto& r : bi) { int j = 0; for (double v : r) t->bimp[i][j++] = v; ++i; }
+    t->sizet = i;
+    i = 0;
+    for (auto& r : be) { int j = 0; for (double v : r) t->bexp[i][j++] = v; ++i; }
+  };
+  auto ass = [&](std::initializer_list<double> a) {
+    int j = 0;
+    for (double v : a) { t->bai[j] = v; t->bae[j] = v; ++j; }
+  };
+  double g, d;
+  switch (scheme) {
+    case PZ_ARS222:
+      g = 0.5 * (2.0 - r2); d = 1.0 - 0.5 / g;
+      t->nstages = 2; t->assembly = 0; t->courfac = 1.35;
+      rows({{0, 0, 0}, {0, g, 0}, {0, 1 - g, g}}, {{0, 0, 0}, {g, 0, 0}, {d, 1 - d, 0}});
+      break;
+    case PZ_ARS232:
+      g = 0.5 * (2.0 - r2); d = -2.0 * r2 / 3.0;
+      t->nstages = 3; t->assembly = 1; t->courfac = 1.35;
+      rows({{0, 0, 0}, {0, g, 0}, {0, 1 - g, g}}, {{0, 0, 0}, {g, 0, 0}, {d, 1 - d, 0}});
+      ass({0, 1 - g, g});
+      break;
+    case PZ_ARS233:
+      g = (3.0 + r3) / 6.0;
+      t->nstages = 3; t->assembly = 1; t->courfac = 1.35;
+      rows({{0, 0, 0}, {0, g, 0}, {0, 1 - 2 * g, g}}, {{0, 0, 0}, {g, 0, 0}, {g - 1, 2 * (1 - g), 0}});
+      ass({0, 0.5, 0.5});
+      break;
+    case PZ_SSP222:
+      g = 1.0 - 1.0 / r2;
+      t->nstages = 3; t->assembly = 1; t->courfac = 1.35;
+      rows({{0, 0, 0}, {0, g, 0}, {0, 1 - 2 * g, g}}, {{0, 0, 0}, {0, 0, 0}, {0, 1, 0}});
+      ass({0, 0.5, 0.5});
+      break;
+    case PZ_LSDIRK222:
+      g = 1.0 - 1.0 / r2; d = 1.0 / (2.0 * g);
+      t->nstages = 3; t->assembly = 1; t->courfac = 1.35;
+      rows({{0, 0, 0}, {0, g, 0}, {0, 1 - g, g}}, {{0, 0, 0}, {0, 0, 0}, {0, d, 0}});
+      ass({0, 1 - g, g});
+      break;
+    case PZ_LZ232:
+      g = 0.5; imp1 = true;
+      t->nstages = 2; t->assembly = 0; t->courfac = 1.25;
+      rows({{0, 0, 0}, {-0.25, 0.5, 0}, {0.5, 0, 0.5}}, {{0, 0, 0}, {0.25, 0, 0}, {-1, 2, 0}});
+      break;
+    case PZ_CK232:
+      g = 1.0 - 0.5 * r2; imp1 = true;
+      t->nstages = 2; t->assembly = 0; t->courfac = 1.25;
+      rows({{0, 0, 0}, {-1.0 / 3.0 + 0.5 * r2, g, 0}, {0.75 - 0.25 * r2, -0.75 + 0.75 * r2, g}},
+           {{0, 0, 0}, {2.0 / 3.0, 0, 0}, {0.25, 0.75, 0}});
+      break;
+    case PZ_ARS443:
+      g = 0.5;
+      t->nstages = 4; t->assembly = 0; t->courfac = 0.9;
+      rows({{0, 0, 0, 0, 0}, {0, 0.5, 0, 0, 0}, {0, 1.0 / 6.0, 0.5, 0, 0}, {0, -0.5, 0.5, 0.5, 0},
+            {0, 1.5, -1.5, 0.5, 0.5}},
+           {{0, 0, 0, 0, 0}, {0.5, 0, 0, 0, 0}, {11.0 / 18.0, 1.0 / 18.0, 0, 0, 0},
+            {5.0 / 6.0, -5.0 / 6.0, 0.5, 0, 0}, {0.25, 1.75, 0.75, -1.75, 0}});
+      break;
+    case PZ_BPR353:
+      g = 0.5; imp1 = true;
+      t->nstages = 4; t->assembly = 0; t->courfac = 1.0;
+      rows({{0, 0, 0, 0, 0}, {0.5, 0.5, 0, 0, 0}, {5.0 / 18.0, -1.0 / 9.0, 0.5, 0, 0}, {0.5, 0, 0, 0.5, 0},
+            {0.25, 0, 0.75, -0.5, 0.5}},
+           {{0, 0, 0, 0, 0}, {1, 0, 0, 0, 0}, {4.0 / 9.0, 2.0 / 9.0, 0, 0, 0}, {0.25, 0, 0.75, 0, 0},
+            {0.25, 0, 0.75, 0, 0}});
+      t->exp_mask = 0x7;   // no explicit terms at stage 4
+      break;
+    case PZ_PC2:
+      g = 0.5; imp1 = true;
+      t->nstages = 3; t->assembly = 0; t->courfac = 0.8;
+      rows({{0, 0, 0, 0}, {0.5, 0.5, 0, 0}, {0.5, 0, 0.5, 0}, {0.5, 0, 0, 0.5}},
+           {{0, 0, 0, 0}, {1, 0, 0, 0}, {0.5, 0.5, 0, 0}, {0.5, 0, 0.5, 0}});
+      break;
+    case PZ_ARS343:
+    case PZ_MARS343: {
+      double b1, b2;
+      if (scheme == PZ_ARS343) {
+        g = 0.435866521508459;
+        b1 = -1.5 * g * g + 4.0 * g - 0.25;
+        b2 = 1.5 * g * g - 5.0 * g + 1.25;
+        t->courfac = 0.7;
+        rows({{0, 0, 0, 0}, {0, g, 0, 0}, {0, 0.5 * (1 - g), g, 0}, {0, b1, b2, g}},
+             {{0, 0, 0, 0}, {g, 0, 0, 0}, {0.3212788860286278, 0.3966543747256017, 0, 0},
+              {-0.1058582960718797, 0.5529291480359398, 0.5529291480359398, 0}});
+      } else {
+        g = 0.435866521508458;
+        b1 = 1.20849664917601;
+        b2 = -0.64436317068446;
+        t->courfac = 0.5;
+        rows({{0, 0, 0, 0}, {0, g, 0, 0}, {0, 0.5 * (1 - g), g, 0}, {0, b1, b2, g}},
+             {{0, 0, 0, 0}, {0.877173304301691, 0, 0, 0}, {0.535396540307354, 0.182536720446875, 0, 0},
+              {0.63041255815287, -0.83193390106308, 1.20152134291021, 0}});
+      }
+      t->nstages = 4; t->assembly = 1;
+      ass({0, b1, b2, g});
+    } break;
+    case PZ_SSP322:
+      g = 0.5;
+      t->nstages = 4; t->assembly = 1; t->courfac = 1.35;
+      rows({{0, 0, 0, 0}, {0, 0.5, 0, 0}, {0, -0.5, 0.5, 0}, {0, 0, 0.5, 0.5}},
+           {{0, 0, 0, 0}, {0, 0, 0, 0}, {0, 0, 0, 0}, {0, 0, 1, 0}});
+      ass({0, 0, 0.5, 0.5});
+      break;
+    case PZ_SSP332:
+      g = 1.0 - 1.0 / r2;
+      t->nstages = 4; t->assembly = 1; t->courfac = 1.35;
+      rows({{0, 0, 0, 0}, {0, g, 0, 0}, {0, 1 - 2 * g, g, 0}, {0, 0.5 - g, 0, g}},
+           {{0, 0, 0, 0}, {0, 0, 0, 0}, {0, 1, 0, 0}, {0, 0.25, 0.25, 0}});
+      ass({0, 1.0 / 6.0, 1.0 / 6.0, 2.0 / 3.0});
+      break;
+    default:
+      return false;
+  }
+  t->gamma = g;
+  if (!t->exp_mask) t->exp_mask = (1 << t->nstages) - 1;
+  t->imp_mask = ((1 << t->nstages) - 1) & ~1;
+  if (imp1) t->imp_mask |= 1;
+  return true;
+}
+
 int scheme_counts(int scheme, int* nold, int* nimp, int* nexp, double* cf, int* imp_calc) {
-  // multistep_schemes.f90:53-106
+  // multistep_schemes.f90:53-106; DIRK: one old slot, one explicit and one
+  // implicit slot per stage (dirk_schemes.f90:35-244)
   *imp_calc = 1;
+  DirkTab t;
+  if (dirk_tableau(scheme, &t)) {
+    *nold = 1; *nimp = t.nstages; *nexp = t.nstages; *cf = t.courfac;
+    return 0;
+  }
   switch (scheme) {
     case PZ_CNAB2: *nimp = 1; *nold = 1; *nexp = 2; *cf = 3.0; break;
     case PZ_MODCNAB: *nold = 2; *nimp = 2; *nexp = 2; *cf = 2.9; break;
@@ -297,6 +442,16 @@ extern "C" int pz_create(const pz_config* cfgs, int n, pz_handle** out) {
     int imp_calc;
     scheme_counts(c.time_scheme, &I.nold, &I.nimp, &I.nexp, &cf, &imp_calc);
     I.scheme = c.time_scheme;
+    {
+      DirkTab tab;
+      const bool dirk = dirk_tableau(c.time_scheme, &tab);
+      I.dirk = dirk ? 1 : 0;
+      I.nstages = dirk ? tab.nstages : 1;
+      I.assembly = dirk ? tab.assembly : 0;
+      I.exp_mask = dirk ? tab.exp_mask : 1;
+      I.imp_mask = dirk ? tab.imp_mask : 1;
+      I.dirk_gamma = dirk ? tab.gamma : 0.0;
+    }
     I.courfac = std::fabs(c.courfac) >= 1.0e3 ? cf : c.courfac;
     // derived switches (namelists.f90:271-526)
     double ek = c.ek;
@@ -437,6 +592,8 @@ extern "C" int pz_create(const pz_config* cfgs, int n, pz_handle** out) {
       I.o_aux = take(4 * M * N + 4 * M);
       I.o_gsm = 0;
     }
+    I.o_bt = I.dirk ? take(PZ_BT_SIZE) : 0;
+    I.o_gass = (I.dirk && I.assembly) ? take(M * N * N) : 0;
     I.o_fld = take(2LL * F_COUNT * M * N);
     I.o_hist = take(2LL * 2 * (I.nold + I.nimp + I.nexp) * M * N);
     I.o_cfl = take(2 * N);
@@ -460,7 +617,23 @@ extern "C" int pz_create(const pz_config* cfgs, int n, pz_handle** out) {
     for (auto& kv : basis_off) hi = std::max(hi, kv.second + (long long)BM_COUNT * kv.first * kv.first);
     for (auto& kv : tw_off) hi = std::max(hi, kv.second + 2LL * kv.first);
     for (int i = 0; i < n; ++i) hi = std::max(hi, h->inst[i].o_rad + (long long)RV_COUNT * h->inst[i].N);
+    for (int i = 0; i < n; ++i)
+      if (h->inst[i].dirk) hi = std::max(hi, h->inst[i].o_bt + (long long)PZ_BT_SIZE);
     img.assign((size_t)hi, 0.0);
+    for (int i = 0; i < n; ++i) {
+      DirkTab tab;
+      if (!h->inst[i].dirk || !dirk_tableau(h->inst[i].scheme, &tab)) continue;
+      double* bt = img.data() + h->inst[i].o_bt;
+      for (int r = 0; r < PZ_BT_LD; ++r)
+        for (int q = 0; q < PZ_BT_LD; ++q) {
+          bt[PZ_BT_IMP + r * PZ_BT_LD + q] = tab.bimp[r][q];
+          bt[PZ_BT_EXP + r * PZ_BT_LD + q] = tab.bexp[r][q];
+        }
+      for (int q = 0; q < PZ_BT_LD; ++q) {
+        bt[PZ_BT_AIMP + q] = tab.bai[q];
+        bt[PZ_BT_AEXP + q] = tab.bae[q];
+      }
+    }
     for (auto& kv : bases) {
       const Basis& B = kv.second;
       const long long NN = (long long)B.N * B.N;
@@ -522,6 +695,25 @@ extern "C" int pz_create(const pz_config* cfgs, int n, pz_handle** out) {
   for (int i = 0; i < n; ++i)
     sb = std::max(sb, pz_build_smem_bytes(h->inst[i].N, (h->inst[i].flags & PZF_DIRECT) != 0));
   h->dev.smem_build = (int)sb;
+  // launch plan of one step: per stage k_rloop [k_cfl, k_build] k_mloop, then
+  // the assembly stage and the time series (step_time.f90:139-406)
+  int smax = 1;
+  bool any_assembly = false;
+  for (int i = 0; i < n; ++i) {
+    smax = std::max(smax, h->inst[i].nstages);
+    any_assembly |= h->inst[i].assembly != 0;
+  }
+  h->plan.clear();
+  for (int st = 1; st <= smax; ++st) {
+    h->plan.push_back({PZK_RLOOP, st});
+    if (st == 1) {
+      h->plan.push_back({PZK_CFL, 1});
+      h->plan.push_back({PZK_BUILD, 1});
+    }
+    h->plan.push_back({PZK_MLOOP, st});
+  }
+  if (any_assembly) h->plan.push_back({PZK_ASSEMBLE, 0});
+  h->plan.push_back({PZK_OBS, 0});
   if ((e = pz_launch_init_state(h->dev, -1, h->stream)) || (e = pz_launch_build_static(h->dev, h->stream)) ||
       (e = cudaStreamSynchronize(h->stream))) {
     g_create_error = std::string("static operators: ") + cudaGetErrorString(e);
@@ -622,7 +814,8 @@ extern "C" int pz_step(pz_handle* h, int n_steps) {
   if (!h->graph) {
     cudaGraph_t g;
     if ((e = cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal))) return cuda_fail(h, e, "capture");
-    e = pz_launch_step(h->dev, h->stream);
+    for (const PzLaunch& L : h->plan)
+      if (!e) e = pz_launch_step_kernel(h->dev, L.kind, L.stage, h->stream);
     cudaError_t e2 = cudaStreamEndCapture(h->stream, &g);
     if (e || e2) return cuda_fail(h, e ? e : e2, "capture");
     e = cudaGraphInstantiate(&h->graph, g, 0);
@@ -703,7 +896,7 @@ extern "C" int pz_get_dims(pz_handle* h, int inst, int* n_r_max, int* n_m_max, i
 
 extern "C" int pz_launches_per_step(pz_handle* h) {
   (void)h;
-  return pz_step_launch_count();
+  return (int)h->plan.size();
 }
 
 extern "C" int pz_latest_rows(pz_handle* h, double* rows) {
@@ -720,7 +913,8 @@ extern "C" void* pz_stream(pz_handle* h) { return h ? (void*)h->stream : nullptr
 
 extern "C" int pz_step_profile(pz_handle* h, int n_steps, double* kernel_ms) {
   if (!h || n_steps <= 0 || !kernel_ms) return fail(h, PZ_E_ARG, "pz_step_profile: bad arguments");
-  const int nk = pz_step_launch_count();
+  pz_adjoint_invalidate(h);
+  const int nk = (int)h->plan.size();
   std::vector<cudaEvent_t> ev((size_t)n_steps * (nk + 1));
   cudaError_t e = cudaSuccess;
   for (auto& x : ev) if (!e) e = cudaEventCreate(&x);
@@ -728,17 +922,17 @@ extern "C" int pz_step_profile(pz_handle* h, int n_steps, double* kernel_ms) {
   for (int s = 0; s < n_steps && !e; ++s) {
     e = cudaEventRecord(ev[(size_t)s * (nk + 1)], h->stream);
     for (int k = 0; k < nk && !e; ++k) {
-      e = pz_launch_step_kernel(h->dev, k, h->stream);
+      e = pz_launch_step_kernel(h->dev, h->plan[k].kind, h->plan[k].stage, h->stream);
       if (!e) e = cudaEventRecord(ev[(size_t)s * (nk + 1) + k + 1], h->stream);
     }
   }
   if (!e) e = cudaStreamSynchronize(h->stream);
-  for (int k = 0; k < nk; ++k) kernel_ms[k] = 0.0;
+  for (int k = 0; k < PZ_KERNEL_KINDS; ++k) kernel_ms[k] = 0.0;
   for (int s = 0; s < n_steps && !e; ++s)
     for (int k = 0; k < nk && !e; ++k) {
       float ms = 0.f;
       e = cudaEventElapsedTime(&ms, ev[(size_t)s * (nk + 1) + k], ev[(size_t)s * (nk + 1) + k + 1]);
-      kernel_ms[k] += ms / n_steps;
+      kernel_ms[h->plan[k].kind] += ms / n_steps;
     }
   for (auto& x : ev) cudaEventDestroy(x);
   if (e) return cuda_fail(h, e, "pz_step_profile");

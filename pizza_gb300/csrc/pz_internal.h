@@ -22,6 +22,15 @@
 #define PZ_SERIES_CAP 1024
 #define PZ_RLOOP_G 4        // radii per block of the phi-transform kernels
 #define PZ_SMEM_MAX (227 * 1024)
+#define PZ_MAX_STAGES 8     // DIRK stages
+#define PZ_BT_LD (PZ_MAX_STAGES + 1)
+// DIRK tables at o_bt (unscaled, row-major with leading dimension PZ_BT_LD):
+// butcher_imp, butcher_exp, then the assembly rows butcher_ass_imp/exp
+#define PZ_BT_IMP 0
+#define PZ_BT_EXP (PZ_BT_LD * PZ_BT_LD)
+#define PZ_BT_AIMP (2 * PZ_BT_LD * PZ_BT_LD)
+#define PZ_BT_AEXP (2 * PZ_BT_LD * PZ_BT_LD + PZ_BT_LD)
+#define PZ_BT_SIZE (2 * PZ_BT_LD * PZ_BT_LD + 2 * PZ_BT_LD)
 
 // flag bits of PzInst::flags
 enum {
@@ -82,6 +91,11 @@ struct PzInst {
   int N, M, P, mmax, minc, n_max;
   int scheme, nold, nimp, nexp;
   int flags;
+  int nstages;              // 1 for the multistep family
+  int dirk;                 // DIRK family (src/dirk_schemes.f90)
+  int assembly;             // DIRK scheme with an assembly stage
+  int exp_mask, imp_mask;   // bit s-1: l_exp_calc(s), l_imp_calc_rhs(s)
+  double dirk_gamma;        // wimp_lin(1)/dt
   int nrad;                 // number of phi-FFT stages
   int radix[PZ_MAX_RADIX];
   double CorFac, BuoFac, TdiffFac, ViscFac, ek, tadvz, alpha;
@@ -100,6 +114,8 @@ struct PzInst {
   long long o_gsm;          // DIRECT (smat): 4*M*N*N, per m the first N columns of the
                             // inverse of the coupled 2N x 2N operator, complex, column-major
                             // with leading dimension 2N: (omega, psi)_cheb = G rhs
+  long long o_bt;           // DIRK tables, PZ_BT_SIZE doubles
+  long long o_gass;         // DIRK assembly: M*N*N, psi_cheb = G_ass rhs (get_assMat, dt independent)
   long long o_fld;          // 2*F_COUNT*M*N
   long long o_hist;         // 2*(2*(nold+nimp+nexp))*M*N
   long long o_cfl;          // 2*N: dtr, dth
@@ -155,11 +171,14 @@ struct PzDev {
 cudaError_t pz_launch_build_static(const PzDev& d, cudaStream_t s);
 cudaError_t pz_launch_init_state(const PzDev& d, int only, cudaStream_t s);
 cudaError_t pz_launch_start(const PzDev& d, int only, cudaStream_t s);
-cudaError_t pz_launch_step(const PzDev& d, cudaStream_t s);
-cudaError_t pz_launch_step_kernel(const PzDev& d, int k, cudaStream_t s);
-const char* pz_step_kernel_name(int k);
+// kernel kinds of a step; a step launches, for stage s = 1..max_stages,
+// k_rloop(s) [k_cfl, k_build after stage 1] k_mloop(s), then k_assemble (if
+// any instance has an assembly stage) and k_obs
+enum { PZK_RLOOP = 0, PZK_CFL, PZK_BUILD, PZK_MLOOP, PZK_OBS, PZK_ASSEMBLE, PZK_KINDS };
+struct PzLaunch { int kind, stage; };
+cudaError_t pz_launch_step_kernel(const PzDev& d, int kind, int stage, cudaStream_t s);
+const char* pz_step_kernel_name(int kind);
 cudaError_t pz_launch_obs(const PzDev& d, int only, cudaStream_t s);
 cudaError_t pz_launch_gather_rows(const PzDev& d, double* out, cudaStream_t s);
 cudaError_t pz_setup_kernels();
 size_t pz_build_smem_bytes(int n, bool direct);   // k_build shared memory for one instance
-int pz_step_launch_count();

@@ -22,6 +22,12 @@ namespace {
 // IMEX weights of the multistep family (src/multistep_schemes.f90:137-306)
 // ---------------------------------------------------------------------------
 __device__ bool set_weights(const PzInst& I, PzState& S) {
+  if (I.dirk) {
+    // DIRK (dirk_schemes.f90:275-712): the Butcher tables are scaled by dt(1)
+    // where they are used; no rebuild request of its own
+    S.wimp_lin[0] = I.dirk_gamma * S.dt[0];
+    return false;
+  }
   const double wimp_old = S.wimp_lin[0];
   const double* dt = S.dt;
   const double one = 1.0, half = 0.5, two = 2.0;
@@ -166,19 +172,21 @@ struct StepIO {
   }
 };
 
-__global__ void __launch_bounds__(256) k_rloop(PzDev d) {
+__global__ void __launch_bounds__(256) k_rloop(PzDev d, int stage) {
   extern __shared__ double2 sh[];
   const PzItem it = d.ritems[blockIdx.x];
   const PzInst& I = d.inst[it.inst];
   const PzState& S = d.state[it.inst];
-  if (S.status != 0) return;
+  if (S.status != 0 || stage > I.nstages) return;
+  if (I.dirk && !((I.exp_mask >> (stage - 1)) & 1)) return;   // l_exp_calc(stage)
+  const int eslot = I.dirk ? stage - 1 : S.b_expl;
   const View V{&I, d.pool};
   StepIO io;
   io.V = V;
   io.N = I.N;
   io.us = V.fld(F_US, 0); io.up = V.fld(F_UP, 0); io.om = V.fld(F_OM, 0); io.T = V.fld(F_TEMP, 0);
-  io.eT = V.hist(0, 2, S.b_expl, 0);
-  io.eP = V.hist(1, 2, S.b_expl, 0);
+  io.eT = V.hist(0, 2, eslot, 0);
+  io.eP = V.hist(1, 2, eslot, 0);
   io.vsT = V.fld(F_DVST, 0);
   io.vsOm = V.fld(F_DVSOM, 0);
   io.cflv = d.pool + I.o_cfl;
@@ -220,7 +228,8 @@ __global__ void k_cfl(PzDev d) {
   } else if (d.sched_mode == 2 && S.n_step < d.sched_n) {
     d.dt_io[ks] = dt_new;
   }
-  for (int k = I.nexp - 1; k > 0; --k) S.dt[k] = S.dt[k - 1];
+  if (!I.dirk)
+    for (int k = I.nexp - 1; k > 0; --k) S.dt[k] = S.dt[k - 1];
   S.dt[0] = dt_new;
   if (dt_new < I.dtMin) { S.status = PZ_E_DT_TOO_SMALL; return; }
   if (set_weights(I, S)) S.lMatNext = 1;
@@ -228,14 +237,16 @@ __global__ void k_cfl(PzDev d) {
   S.lMat = (S.lMatNext || l_new_dt) ? 1 : 0;
   S.lMatNext = 0;
   S.n_step += 1;
-  S.bridge = (I.scheme != PZ_CNAB2 && S.n_step <= I.nold - 1) ? 1 : 0;
+  S.bridge = (!I.dirk && I.scheme != PZ_CNAB2 && S.n_step <= I.nold - 1) ? 1 : 0;
   if (S.bridge) bridge_with_cnab2(I, S);
   S.l_calc_lin = (I.flags & PZF_IMP_CALC) ? 1 : 0;
-  // rotate_imex on rings: this step reads slots from r_*, writes logical slot 1 at b_*
-  S.r_old = S.b_old; S.r_impl = S.b_impl; S.r_expl = S.b_expl;
-  S.b_old = (S.b_old + I.nold - 1) % I.nold;
-  S.b_impl = (S.b_impl + I.nimp - 1) % I.nimp;
-  S.b_expl = (S.b_expl + I.nexp - 1) % I.nexp;
+  if (!I.dirk) {
+    // rotate_imex on rings: this step reads slots from r_*, writes logical slot 1 at b_*
+    S.r_old = S.b_old; S.r_impl = S.b_impl; S.r_expl = S.b_expl;
+    S.b_old = (S.b_old + I.nold - 1) % I.nold;
+    S.b_impl = (S.b_impl + I.nimp - 1) % I.nimp;
+    S.b_expl = (S.b_expl + I.nexp - 1) % I.nexp;
+  }   // DIRK: slots are stages, nothing rotates (dirk_schemes.f90:833-838)
   if (d.rec && ks < (long long)(inst + 1) * d.sched_n) d.rec[ks] = S;
 }
 
@@ -348,7 +359,8 @@ __device__ void equilibrate(double* A, int n, double* f1, double* f2, bool cols)
 }
 
 // kind: 0 temperature (get_tempMat), 1 omega (get_omMat), 2 psi (get_psiMat),
-// 3 uphi (get_uphiMat).  Fills A (row-major) before scaling.
+// 3 uphi (get_uphiMat), 4 DIRK assembly psi (get_assMat).  Fills A
+// (row-major) before scaling.
 __device__ void fill_matrix(double* A, const BuildCtx& B, const View& V, int kind, int m, double wlin) {
   const PzInst& I = *B.I;
   const int n = B.N, n_max = I.n_max;
@@ -361,7 +373,11 @@ __device__ void fill_matrix(double* A, const BuildCtx& B, const View& V, int kin
   for (int idx = threadIdx.x; idx < n * n; idx += blockDim.x) {
     const int i = idx / n, k = idx - i * n;
     double v;
-    if (i == 0 || i == n - 1) {
+    if (kind == 4 && (i == 1 || i == n - 2)) {
+      // get_assMat: dpsi/dr = 0 on the rigid walls in the second and
+      // second-last rows (update_psi_coll_smat.f90:839-917)
+      v = (k >= n_max) ? 0.0 : rn * B.drm(i == 1 ? 0 : n - 1, k);
+    } else if (i == 0 || i == n - 1) {
       if (k >= n_max) {
         v = 0.0;
       } else {
@@ -377,6 +393,8 @@ __device__ void fill_matrix(double* A, const BuildCtx& B, const View& V, int kin
         v = rn * (r0 - wlin * I.ViscFac * (r2 + or1[i] * r1 - dm2 * or2[i] * r0));
       } else if (kind == 2) {
         v = rn * (r2 + (or1[i] + beta[i]) * r1 + (or1[i] * beta[i] + dbeta[i] - dm2 * or2[i]) * r0);
+      } else if (kind == 4) {
+        v = -rn * (r2 + (or1[i] + beta[i]) * r1 + (or1[i] * beta[i] + dbeta[i] - dm2 * or2[i]) * r0);
       } else {
         v = rn * (r0 - wlin * (I.ViscFac * (r2 + or1[i] * r1 - or2[i] * r0) - I.CorFac * ekp[i] * r0));
       }
@@ -610,11 +628,19 @@ __global__ void __launch_bounds__(PZ_THREADS) k_build_static(PzDev d) {
   const PzItem it = d.mitems[blockIdx.x];
   const PzInst& I = d.inst[it.inst];
   PzState& S = d.state[it.inst];
-  if (it.idx == 0 || (I.flags & PZF_DIRECT)) return;
+  if (it.idx == 0) return;
   const View V{&I, d.pool};
   const int n = I.N, m = it.idx * I.minc;
   BuildSmem s = build_smem(n);
   BuildCtx B{&I, V.basis(BM_RMAT), V.basis(BM_DRMAT), V.basis(BM_D2RMAT), n};
+  if (I.dirk && I.assembly) {
+    // assembly-stage streamfunction operator (plain LU in the reference: no scaling)
+    fill_matrix(s.A, B, V, 4, m, 0.0);
+    if (gj_invert(s.A, n, s.piv, s.colk, s.red, s.redi) != 0) { flag_status(S, PZ_E_SINGULAR); return; }
+    store_op(d.pool + I.o_gass + (long long)it.idx * n * n, s.A, n, I.n_max, nullptr, nullptr);
+    __syncthreads();
+  }
+  if (I.flags & PZF_DIRECT) return;
   fill_matrix(s.A, B, V, 2, m, 0.0);
   equilibrate(s.A, n, s.f1, s.f2, true);
   if (gj_invert(s.A, n, s.piv, s.colk, s.red, s.redi) != 0) { flag_status(S, PZ_E_SINGULAR); return; }
@@ -882,12 +908,44 @@ __device__ __forceinline__ double2 imex_rhs(const View& V, const PzInst& I, cons
   return acc;
 }
 
-__global__ void __launch_bounds__(256) k_mloop(PzDev d) {
+// IMEX rhs of DIRK stage `stage` (set_imex_rhs, dirk_schemes.f90:762-795):
+// old + sum_{k<=stage} dt (b_exp(stage+1,k) expl_k + b_imp(stage+1,k) impl_k)
+__device__ __forceinline__ double2 dirk_rhs(const View& V, const PzInst& I, const PzState& S, int f, int mi, int i,
+                                           int stage) {
+  const double* bt = V.pool + I.o_bt;
+  const double dt = S.dt[0];
+  double2 acc = V.hist(f, 0, 0, mi)[i];
+  for (int k = 0; k < stage; ++k) {
+    const double w = dt * bt[PZ_BT_EXP + stage * PZ_BT_LD + k];
+    const double2 v = V.hist(f, 2, k, mi)[i];
+    acc.x += w * v.x; acc.y += w * v.y;
+  }
+  for (int k = 0; k < stage; ++k) {
+    const double w = dt * bt[PZ_BT_IMP + stage * PZ_BT_LD + k];
+    const double2 v = V.hist(f, 1, k, mi)[i];
+    acc.x += w * v.x; acc.y += w * v.y;
+  }
+  return acc;
+}
+
+__global__ void __launch_bounds__(256) k_mloop(PzDev d, int stage) {
   const PzItem it = d.mitems[blockIdx.x];
   const PzInst& I = d.inst[it.inst];
   PzState& Sg = d.state[it.inst];
-  if (Sg.status != 0) return;
+  if (Sg.status != 0 || stage > I.nstages) return;
   const PzState S = Sg;
+  // stage bookkeeping: the explicit slot of this stage, whether this stage
+  // solves (not the last stage of an assembly scheme), and where the solution's
+  // implicit term goes (stage+1, or 1 after the last stage, which also sets old)
+  const bool dirk = I.dirk != 0;
+  const int eslot = dirk ? stage - 1 : S.r_expl;
+  const bool do_finish = !dirk || ((I.exp_mask >> (stage - 1)) & 1);
+  const bool do_solve = !(dirk && I.assembly && stage == I.nstages);
+  const int tgt = (!dirk || stage == I.nstages) ? 1 : stage + 1;
+  const int oslot = dirk ? 0 : S.b_old;
+  const int islot = dirk ? tgt - 1 : S.b_impl;
+  const bool wold = tgt == 1;
+  const bool calc = dirk ? ((I.imp_mask >> (tgt - 1)) & 1) != 0 : S.l_calc_lin != 0;
   const View V{&I, d.pool};
   const int n = I.N, mi = it.idx, m = mi * I.minc;
   const double dm = (double)m, dm2 = dm * dm;
@@ -912,6 +970,7 @@ __global__ void __launch_bounds__(256) k_mloop(PzDev d) {
   const bool direct = (I.flags & PZF_DIRECT) != 0;
 
   // -- finish_exp_temp_coll (update_temp_coll.f90:152-176)
+  if (do_finish) {
   for (int i = threadIdx.x; i < n; i += blockDim.x) {
     s.a[i] = V.fld(F_DVST, mi)[i];
     s.e[i] = V.fld(F_DVSOM, mi)[i];
@@ -922,8 +981,8 @@ __global__ void __launch_bounds__(256) k_mloop(PzDev d) {
   op_D1p(V, n, s.e, s.f, s.w);
   __syncthreads();
   {
-    double2* eT = V.hist(0, 2, S.r_expl, mi);
-    double2* eP = V.hist(1, 2, S.r_expl, mi);
+    double2* eT = V.hist(0, 2, eslot, mi);
+    double2* eP = V.hist(1, 2, eslot, mi);
     for (int i = threadIdx.x; i < n; i += blockDim.x) {
       double2 e = eT[i];
       const double2 u = us[i];
@@ -960,12 +1019,14 @@ __global__ void __launch_bounds__(256) k_mloop(PzDev d) {
     }
   }
   __syncthreads();
+  }
+  if (!do_solve) return;   // assembly follows (k_assemble)
   // -- start_from_another_scheme (step_time.f90:417-516)
   if (S.bridge) imp_from_physical(V, I, mi, S.r_old, S.r_impl, true, s);
 
   // -- update_temp_co (update_temp_coll.f90:66-150)
   for (int i = threadIdx.x; i < n; i += blockDim.x) {
-    const double2 v = imex_rhs(V, I, S, 0, mi, i);
+    const double2 v = dirk ? dirk_rhs(V, I, S, 0, mi, i, stage) : imex_rhs(V, I, S, 0, mi, i);
     s.a[i] = (i == 0 || i == n - 1) ? make_double2(0.0, 0.0) : v;   // topt = bott = 0
   }
   __syncthreads();
@@ -979,15 +1040,15 @@ __global__ void __launch_bounds__(256) k_mloop(PzDev d) {
   __syncthreads();
   bool bad = false;
   {
-    double2* oT = V.hist(0, 0, S.b_old, mi);
-    double2* iT = V.hist(0, 1, S.b_impl, mi);
+    double2* oT = V.hist(0, 0, oslot, mi);
+    double2* iT = V.hist(0, 1, islot, mi);
     for (int i = threadIdx.x; i < n; i += blockDim.x) {
       const double2 t = s.f[i], d1 = s.c[i], d2 = s.e[i];
       T[i] = t;
       dT[i] = d1;
-      oT[i] = t;
+      if (wold) oT[i] = t;
       bad |= !isfinite(t.x) || !isfinite(t.y);
-      if (S.l_calc_lin) {
+      if (calc) {
         const double f = I.TdiffFac;
         iT[i] = make_double2(f * (d2.x + or1[i] * d1.x - dm2 * or2[i] * t.x),
                              f * (d2.y + or1[i] * d1.y - dm2 * or2[i] * t.y));
@@ -997,7 +1058,7 @@ __global__ void __launch_bounds__(256) k_mloop(PzDev d) {
   // s.f keeps the new physical temperature
   // -- update_om_coll_dmat (update_psi_coll_dmat.f90:126-466)
   for (int i = threadIdx.x; i < n; i += blockDim.x) {
-    double2 v = imex_rhs(V, I, S, 1, mi, i);
+    double2 v = dirk ? dirk_rhs(V, I, S, 1, mi, i, stage) : imex_rhs(V, I, S, 1, mi, i);
     if (m != 0 && buo_imp) {
       const double2 b = cim(dm, s.f[i]);
       const double c = S.wimp_lin[0] * I.BuoFac * rgrav[i] * or1[i];
@@ -1007,8 +1068,8 @@ __global__ void __launch_bounds__(256) k_mloop(PzDev d) {
     s.a[i] = (i == 0 || i == n - 1) ? make_double2(0.0, 0.0) : v;
   }
   __syncthreads();
-  double2* oP = V.hist(1, 0, S.b_old, mi);
-  double2* iP = V.hist(1, 1, S.b_impl, mi);
+  double2* oP = V.hist(1, 0, oslot, mi);
+  double2* iP = V.hist(1, 1, islot, mi);
   if (m == 0) {
     mv_lanes(d.pool + I.o_guphi, n, s.a, s.b);           // uphi, Chebyshev
     __syncthreads();
@@ -1023,9 +1084,9 @@ __global__ void __launch_bounds__(256) k_mloop(PzDev d) {
       up[i] = make_double2(u, 0.0);
       om[i] = make_double2(du + or1[i] * u, 0.0);
       psi[i] = make_double2(0.0, 0.0);
-      oP[i] = make_double2(u, 0.0);
+      if (wold) oP[i] = make_double2(u, 0.0);
       bad |= !isfinite(u);
-      if (S.l_calc_lin)
+      if (calc)
         iP[i] = make_double2(I.ViscFac * (d2u + or1[i] * du - or2[i] * u) - I.CorFac * ekp[i] * u, 0.0);
     }
   } else {
@@ -1087,9 +1148,9 @@ __global__ void __launch_bounds__(256) k_mloop(PzDev d) {
     for (int i = threadIdx.x; i < n; i += blockDim.x) {
       const double2 o = s.k[i], d1 = s.c[i], d2 = s.a[i];
       om[i] = o;
-      oP[i] = o;
+      if (wold) oP[i] = o;
       bad |= !isfinite(o.x) || !isfinite(o.y);
-      if (S.l_calc_lin) {
+      if (calc) {
         double2 v = make_double2(I.ViscFac * (d2.x + or1[i] * d1.x - dm2 * or2[i] * o.x),
                                  I.ViscFac * (d2.y + or1[i] * d1.y - dm2 * or2[i] * o.y));
         if (direct) v = cadd(v, smat_imp_extra(I, V, i, dm, o, up[i], us[i]));
@@ -1102,6 +1163,98 @@ __global__ void __launch_bounds__(256) k_mloop(PzDev d) {
       }
     }
   }
+  if (__syncthreads_or(bad)) flag_status(Sg, PZ_E_NONFINITE);
+}
+
+// ---------------------------------------------------------------------------
+// k_assemble: the assembly stage of a DIRK scheme (assemble_stage, mloop.f90;
+// assemble_temp_coll, update_temp_coll.f90:238-307; assemble_psi_coll_{smat,dmat},
+// update_psi_coll_smat.f90:529-672) for one m of one instance:
+//   X = old + sum_k dt (b_ass_exp(k) expl_k + b_ass_imp(k) impl_k)   (assemble_imex)
+// temperature: interior from X, fixed walls; u_phi(m=0): interior from Re X,
+// rigid walls; m /= 0: psi from the assembled vorticity through get_assMat,
+// then us, up and om from psi; finally the first-stage old/implicit terms
+// from the physical fields (get_*_rhs_imp_coll with l_in_cheb_space=.false.).
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ double2 assemble_imex(const View& V, const PzInst& I, const PzState& S, int f, int mi,
+                                                int i) {
+  const double* bt = V.pool + I.o_bt;
+  const double dt = S.dt[0];
+  double2 acc = V.hist(f, 0, 0, mi)[i];
+  for (int k = 0; k < I.nstages; ++k) {
+    const double w = dt * bt[PZ_BT_AEXP + k];
+    const double2 v = V.hist(f, 2, k, mi)[i];
+    acc.x += w * v.x; acc.y += w * v.y;
+  }
+  for (int k = 0; k < I.nstages; ++k) {
+    const double w = dt * bt[PZ_BT_AIMP + k];
+    const double2 v = V.hist(f, 1, k, mi)[i];
+    acc.x += w * v.x; acc.y += w * v.y;
+  }
+  return acc;
+}
+
+__global__ void __launch_bounds__(256) k_assemble(PzDev d) {
+  const PzItem it = d.mitems[blockIdx.x];
+  const PzInst& I = d.inst[it.inst];
+  PzState& Sg = d.state[it.inst];
+  if (Sg.status != 0 || !I.dirk || !I.assembly) return;
+  const PzState S = Sg;
+  const View V{&I, d.pool};
+  const int n = I.N, mi = it.idx, m = mi * I.minc;
+  const double dm = (double)m, dm2 = dm * dm;
+  MS s = ms_smem(n);
+  const double* or1 = V.rad(RV_OR1);
+  const double* or2 = V.rad(RV_OR2);
+  const double* beta = V.rad(RV_BETA);
+  const double* dbeta = V.rad(RV_DBETA);
+  double2* T = V.fld(F_TEMP, mi);
+  double2* us = V.fld(F_US, mi);
+  double2* up = V.fld(F_UP, mi);
+  double2* om = V.fld(F_OM, mi);
+  double2* psi = V.fld(F_PSI, mi);
+  bool bad = false;
+  for (int i = threadIdx.x; i < n; i += blockDim.x) {
+    double2 t = assemble_imex(V, I, S, 0, mi, i);
+    if (m == 0) t.y = 0.0;
+    if (i == 0 || i == n - 1) t = make_double2(0.0, 0.0);   // robin_bc, Dirichlet: topt = bott = 0
+    T[i] = t;
+    bad |= !isfinite(t.x) || !isfinite(t.y);
+    const double2 w = assemble_imex(V, I, S, 1, mi, i);
+    if (m == 0) s.a[i] = (i == 0 || i == n - 1) ? make_double2(0.0, 0.0) : make_double2(w.x, 0.0);
+    else s.a[i] = (i < 2 || i > n - 3) ? make_double2(0.0, 0.0) : w;
+  }
+  __syncthreads();
+  if (m == 0) {
+    op_D1p(V, n, s.a, s.b, s.w);                                      // d u_phi / dr
+    __syncthreads();
+    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+      const double u = s.a[i].x;
+      us[i] = make_double2(0.0, 0.0);
+      up[i] = make_double2(u, 0.0);
+      om[i] = make_double2(s.b[i].x + or1[i] * u, 0.0);
+      psi[i] = make_double2(0.0, 0.0);
+      bad |= !isfinite(u);
+    }
+  } else {
+    mv_lanes(d.pool + I.o_gass + (long long)mi * n * n, n, s.a, s.b);   // psi, Chebyshev
+    __syncthreads();
+    op_Dc2(V, n, s.b, s.c, s.e, s.w);                                   // dpsi, d2psi
+    __syncthreads();
+    op_C(V, n, s.b, s.f, s.w);                                          // psi
+    __syncthreads();
+    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+      const double2 p = s.f[i], d1 = s.c[i], d2 = s.e[i];
+      const double c1 = or1[i] + beta[i], c0 = or1[i] * beta[i] + dbeta[i] - dm2 * or2[i];
+      psi[i] = p;
+      us[i] = cscale(or1[i], cim(dm, p));
+      up[i] = make_double2(-d1.x - beta[i] * p.x, -d1.y - beta[i] * p.y);
+      om[i] = make_double2(-(d2.x + c1 * d1.x + c0 * p.x), -(d2.y + c1 * d1.y + c0 * p.y));
+      bad |= !isfinite(p.x) || !isfinite(p.y);
+    }
+  }
+  __syncthreads();
+  imp_from_physical(V, I, mi, 0, 0, (I.imp_mask & 1) != 0, s);
   if (__syncthreads_or(bad)) flag_status(Sg, PZ_E_NONFINITE);
 }
 
@@ -1282,35 +1435,26 @@ cudaError_t pz_launch_obs(const PzDev& d, int only, cudaStream_t s) {
   return cudaGetLastError();
 }
 
-int pz_step_launch_count() { return 5; }
-
 cudaError_t pz_launch_gather_rows(const PzDev& d, double* out, cudaStream_t s) {
   const int n = d.n_inst * PZ_SERIES_COLS;
   k_gather_rows<<<(n + 127) / 128, 128, 0, s>>>(d, out);
   return cudaGetLastError();
 }
 
-cudaError_t pz_launch_step_kernel(const PzDev& d, int k, cudaStream_t s) {
-  switch (k) {
-    case 0: k_rloop<<<d.n_ritems, 256, rloop_smem_bytes(d.maxP, d.maxM), s>>>(d); break;
-    case 1: k_cfl<<<d.n_inst, 32, 0, s>>>(d); break;
-    case 2: k_build<<<d.n_mitems, PZ_THREADS, d.smem_build, s>>>(d); break;
-    case 3: k_mloop<<<d.n_mitems, mloop_threads(d.maxN), ms_smem_bytes(d.maxN), s>>>(d); break;
-    case 4: k_obs<<<d.n_inst, PZ_THREADS, 0, s>>>(d, -1); break;
+cudaError_t pz_launch_step_kernel(const PzDev& d, int kind, int stage, cudaStream_t s) {
+  switch (kind) {
+    case PZK_RLOOP: k_rloop<<<d.n_ritems, 256, rloop_smem_bytes(d.maxP, d.maxM), s>>>(d, stage); break;
+    case PZK_CFL: k_cfl<<<d.n_inst, 32, 0, s>>>(d); break;
+    case PZK_BUILD: k_build<<<d.n_mitems, PZ_THREADS, d.smem_build, s>>>(d); break;
+    case PZK_MLOOP: k_mloop<<<d.n_mitems, mloop_threads(d.maxN), ms_smem_bytes(d.maxN), s>>>(d, stage); break;
+    case PZK_OBS: k_obs<<<d.n_inst, PZ_THREADS, 0, s>>>(d, -1); break;
+    case PZK_ASSEMBLE: k_assemble<<<d.n_mitems, mloop_threads(d.maxN), ms_smem_bytes(d.maxN), s>>>(d); break;
     default: return cudaErrorInvalidValue;
   }
   return cudaGetLastError();
 }
 
-const char* pz_step_kernel_name(int k) {
-  static const char* names[5] = {"k_rloop", "k_cfl", "k_build", "k_mloop", "k_obs"};
-  return (k >= 0 && k < 5) ? names[k] : "";
-}
-
-cudaError_t pz_launch_step(const PzDev& d, cudaStream_t s) {
-  for (int k = 0; k < 5; ++k) {
-    const cudaError_t e = pz_launch_step_kernel(d, k, s);
-    if (e) return e;
-  }
-  return cudaSuccess;
+const char* pz_step_kernel_name(int kind) {
+  static const char* names[PZK_KINDS] = {"k_rloop", "k_cfl", "k_build", "k_mloop", "k_obs", "k_assemble"};
+  return (kind >= 0 && kind < PZK_KINDS) ? names[kind] : "";
 }

@@ -11,6 +11,7 @@ first run starts from the namelist and needs no checkpoint):
   RotE1e3EkPump     rows 0-10     (e_kin_3D, coll smat CNAB2, Ekman pumping)
   MultistepSchemes  rows 0-200    (e_kin_3D, coll smat SBDF3 + CNAB2 bridge)
   TimeStepChange    all 21 rows   (e_kin, coll dmat SBDF3, CFL dt changes)
+  DIRKSchemes       rows 0-10     (e_kin_3D, coll smat ARS222, a DIRK scheme)
 """
 import argparse
 import json
@@ -39,6 +40,12 @@ CASES = {
                     time_scheme="SBDF3", courfac=2.5, l_non_rot=True,
                     matrix_solve="INFLUENCE", ra=1.0e4, pr=1.0, ek=1.0e-3, radratio=0.35,
                     g0=1.0, g1=0.0, g2=0.0, init_t=-1, amp_t=1.0e-2, n_log_step=100)),
+    "DIRKSchemes": dict(
+        rows=11, series="e_kin_3D",
+        params=dict(n_r_max=33, n_cheb_max=33, m_max=32, n_time_steps=100, dtMax=1e-5,
+                    time_scheme="ARS222", courfac=1.0, ra=6.0e4, pr=1.0, ek=1.0e-3,
+                    radratio=0.35, g0=0.0, g1=1.0, g2=0.0, l_ek_pump=False, init_t=4,
+                    amp_t=2.5e-4, n_log_step=10)),
 }
 
 
