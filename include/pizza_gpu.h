@@ -216,6 +216,9 @@ int pz_explicit_terms_noalloc(pz_handle* h, int inst, const double* us, const do
  * perturbation (the temp argument of pz_set_state) and Ra, for a fixed
  * time-step sequence.  Only CNAB2 with the influence-matrix solve is covered.
  *
+ * The objective is selected per sweep: PZ_OBJ_EKIN3D (above) or
+ * PZ_OBJ_NUTOP, the mean of NuTop = 1 + dT/dr(m=0, r_cmb)/dtcond(r_cmb).
+ *
  * pz_adjoint_forward: run n_steps steps from the start state set by
  * pz_set_state/pz_set_state_all (every instance must be at step 0), storing a
  * checkpoint every checkpoint_every steps (<= 0: store every step, no
@@ -224,7 +227,9 @@ int pz_explicit_terms_noalloc(pz_handle* h, int inst, const double* us, const do
  * records its choice.  J (n_inst) receives the objective, dt_used (n_inst x
  * n_steps, or NULL) the sequence used.  No time-series rows are written.
  * Leaves the handle at the final state. */
-int pz_adjoint_forward(pz_handle* h, int n_steps, int n_window, int checkpoint_every,
+#define PZ_OBJ_EKIN3D 0   /* us2_3D + up2_3D + uz2_3D                 */
+#define PZ_OBJ_NUTOP  1   /* NuTop (outputs.f90:742-746), r(1) = r_cmb */
+int pz_adjoint_forward(pz_handle* h, int objective, int n_steps, int n_window, int checkpoint_every,
                        const double* dt_sched, double* J, double* dt_used);
 
 /* pz_adjoint_backward: gradient of the last forward sweep's objective.

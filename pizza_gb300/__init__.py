@@ -152,7 +152,7 @@ def load_library(path: str | None = None):
     vp = ctypes.c_void_p
     lib.pz_explicit_terms.argtypes = [vp, ctypes.c_int, vp, vp, vp, vp, vp, vp, vp, vp]
     lib.pz_explicit_terms_noalloc.argtypes = [vp, ctypes.c_int, vp, vp, vp, vp, vp, vp, vp, vp]
-    lib.pz_adjoint_forward.argtypes = [vp, ctypes.c_int, ctypes.c_int, ctypes.c_int, dp, dp, dp]
+    lib.pz_adjoint_forward.argtypes = [vp, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, dp, dp, dp]
     lib.pz_adjoint_backward.argtypes = [vp, dp, dp]
     lib.pz_set_ra.argtypes = [vp, ctypes.c_int, ctypes.c_double]
     lib.pz_destroy.argtypes = [ctypes.c_void_p]
@@ -291,18 +291,20 @@ class Ensemble:
         self._check(self.lib.pz_set_ra(self._h, i, float(ra)))
         self.configs[i] = dataclasses.replace(self.configs[i], ra=float(ra))
 
-    def adjoint_forward(self, n_steps, n_window, checkpoint_every=0, dt_sched=None):
-        """Forward sweep of the kinetic-energy objective from the start state
-        of every instance (pz_adjoint_forward).  ``dt_sched`` (n_instances,
-        n_steps) prescribes the time steps; None lets the Courant controller
-        choose.  Returns (J, dt_used) as numpy arrays."""
+    def adjoint_forward(self, n_steps, n_window, checkpoint_every=0, dt_sched=None, objective="ekin3d"):
+        """Forward sweep of the objective ('ekin3d': us2_3D+up2_3D+uz2_3D, or
+        'nutop': NuTop) averaged over the last n_window states, from the start
+        state of every instance (pz_adjoint_forward).  ``dt_sched``
+        (n_instances, n_steps) prescribes the time steps; None lets the
+        Courant controller choose.  Returns (J, dt_used) as numpy arrays."""
+        obj = {"ekin3d": 0, "nutop": 1}[objective]
         nI = len(self)
         J = np.zeros(nI)
         dt_used = np.zeros((nI, int(n_steps)))
         sched = None
         if dt_sched is not None:
             sched = np.ascontiguousarray(np.broadcast_to(np.asarray(dt_sched, np.float64), (nI, int(n_steps))))
-        self._check(self.lib.pz_adjoint_forward(self._h, int(n_steps), int(n_window), int(checkpoint_every),
+        self._check(self.lib.pz_adjoint_forward(self._h, obj, int(n_steps), int(n_window), int(checkpoint_every),
                                                 _dptr(sched), _dptr(J), _dptr(dt_used)))
         return J, dt_used
 

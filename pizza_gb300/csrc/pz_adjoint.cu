@@ -1,6 +1,7 @@
 // Discrete adjoint of the CNAB2 collocation step (influence-matrix solve):
-// gradient of a time-averaged 3-D kinetic energy with respect to the initial
-// temperature perturbation and to BuoFac (hence Ra).
+// gradient of a time-averaged 3-D kinetic energy or outer-boundary Nusselt
+// number with respect to the initial temperature perturbation and to BuoFac
+// (hence Ra).
 //
 // The step of k_rloop/k_cfl/k_build/k_mloop is, per instance, a map of the
 // state S_n = (Tc, oc, pc, uc) -- the Chebyshev coefficients of temperature,
@@ -74,6 +75,7 @@ struct PzAdjDev {
   int n_steps, n_snap, n_ck, ck_planes;
   int win0;                 // first state index of the averaging window
   double inv_window;
+  int objective;            // PZ_OBJ_EKIN3D or PZ_OBJ_NUTOP
 };
 
 struct AdjView {
@@ -181,13 +183,19 @@ __global__ void k_adj_ckpt(PzAdjDev a, int c, int dir) {
   }
 }
 
-// J += (us2_3D + up2_3D + uz2_3D) / n_window of the current state
-// (the e_kin_3D sums of outputs.f90:553-570, as k_obs forms them)
+// J += objective(current state) / n_window: us2_3D + up2_3D + uz2_3D (the
+// e_kin_3D sums of outputs.f90:553-570, as k_obs forms them) or NuTop
+// = 1 + dT/dr(m=0, r_cmb) / dtcond(r_cmb) (outputs.f90:742-746)
 __global__ void k_adj_ke(PzAdjDev a) {
   const int inst = blockIdx.x;
   const PzInst& I = a.d.inst[inst];
   const View V{&I, a.d.pool};
   __shared__ double red[32];
+  if (a.objective == PZ_OBJ_NUTOP) {
+    if (threadIdx.x == 0)
+      a.J[inst] += (1.0 + V.fld(F_DTEMP, 0)[0].x / V.rad(RV_DTCOND)[0]) * a.inv_window;
+    return;
+  }
   const int n = I.N, M = I.M;
   const double* rr = V.rad(RV_R);
   const double* h = V.rad(RV_HEIGHT);
@@ -485,7 +493,7 @@ __global__ void __launch_bounds__(256) k_adj_rloop(PzAdjDev a, int slot) {
 // L^T for step n: field adjoints of state n -> adjoint of S_n.  `terminal`
 // handles the final state (only the kinetic-energy source), `ke` adds the
 // source of the averaging window.
-__global__ void __launch_bounds__(256) k_adj_lin(PzAdjDev a, int n, int slot, int terminal, int ke) {
+__global__ void __launch_bounds__(256) k_adj_lin(PzAdjDev a, int n, int slot, int terminal, int src) {
   const PzItem it = a.d.mitems[blockIdx.x];
   const int inst = it.inst;
   const PzInst& I = a.d.inst[inst];
@@ -543,7 +551,7 @@ __global__ void __launch_bounds__(256) k_adj_lin(PzAdjDev a, int n, int slot, in
       }
       if (!buo_imp) Tb = cadd(Tb, cscale(I.BuoFac * rgrav[i] * or1[i], cim(dm, eP)));
     }
-    if (ke) {
+    if (src && a.objective == PZ_OBJ_EKIN3D) {
       // d(us2_3D + up2_3D + uz2_3D)/d(us, up) of the state, averaged
       const double W1 = pi * wint[i] * (rr[i] * h[i] + beta[i] * beta[i] * rr[i] * h[i] * h[i] * h[i] / 12.0);
       const double W2 = pi * wint[i] * rr[i] * h[i];
@@ -589,7 +597,17 @@ __global__ void __launch_bounds__(256) k_adj_lin(PzAdjDev a, int n, int slot, in
   __syncthreads();
   op_D1cT(V, N, v[2], t2, s.w);
   __syncthreads();
-  for (int i = threadIdx.x; i < N; i += blockDim.x) A.plane(AP_TCB, mi)[i] = cadd(t0[i], cadd(t1[i], t2[i]));
+  {
+    // NuTop source: d/dTc of dT/dr(m=0, r_cmb) / dtcond(r_cmb) = D1c(0, k) / dtcond(0)
+    const bool nu = src && a.objective == PZ_OBJ_NUTOP && m == 0;
+    const double cnu = nu ? a.inv_window / V.rad(RV_DTCOND)[0] : 0.0;
+    const double* d1c = V.basis(BM_D1C);
+    for (int i = threadIdx.x; i < N; i += blockDim.x) {
+      double2 v = cadd(t0[i], cadd(t1[i], t2[i]));
+      if (nu) v.x += cnu * d1c[(long long)i * N];
+      A.plane(AP_TCB, mi)[i] = v;
+    }
+  }
   __syncthreads();
   op_CT(V, N, v[3], t0, s.w);
   __syncthreads();
@@ -648,7 +666,7 @@ __global__ void k_adj_db(PzAdjDev a, double* out) {
 // host driver
 // ---------------------------------------------------------------------------
 struct PzAdjoint {
-  int n_steps = 0, K = 0, n_seg = 0, n_window = 0, n_snap = 0, n_ck = 0, ck_planes = 0;
+  int n_steps = 0, K = 0, n_seg = 0, n_window = 0, n_snap = 0, n_ck = 0, ck_planes = 0, objective = 0;
   bool ready = false;        // a forward sweep is stored
   bool last_valid = false;   // snapshots of the last segment are those of the forward sweep
   double* ws = nullptr;
@@ -702,6 +720,7 @@ PzAdjDev adj_dev(pz_handle* h) {
   a.ck_planes = A->ck_planes;
   a.win0 = A->n_steps - A->n_window + 1;
   a.inv_window = A->n_window > 0 ? 1.0 / A->n_window : 0.0;
+  a.objective = A->objective;
   return a;
 }
 
@@ -752,9 +771,11 @@ extern "C" int pz_set_ra(pz_handle* h, int inst, double ra) {
   return PZ_OK;
 }
 
-extern "C" int pz_adjoint_forward(pz_handle* h, int n_steps, int n_window, int checkpoint_every,
+extern "C" int pz_adjoint_forward(pz_handle* h, int objective, int n_steps, int n_window, int checkpoint_every,
                                   const double* dt_sched, double* J, double* dt_used) {
   if (!h) return pz_fail(nullptr, PZ_E_ARG, "pz_adjoint_forward: null handle");
+  if (objective != PZ_OBJ_EKIN3D && objective != PZ_OBJ_NUTOP)
+    return pz_fail(h, PZ_E_ARG, "pz_adjoint_forward: unknown objective");
   if (n_steps < 1) return pz_fail(h, PZ_E_ARG, "pz_adjoint_forward: n_steps < 1");
   if (n_window < 0 || n_window > n_steps) return pz_fail(h, PZ_E_ARG, "pz_adjoint_forward: n_window outside [0, n_steps]");
   for (int i = 0; i < h->n_inst; ++i) {
@@ -780,6 +801,7 @@ extern "C" int pz_adjoint_forward(pz_handle* h, int n_steps, int n_window, int c
   if (!h->adj) h->adj = new PzAdjoint();
   PzAdjoint* A = h->adj;
   A->ready = false;
+  A->objective = objective;
   A->n_steps = n_steps;
   A->n_window = n_window;
   A->K = (checkpoint_every <= 0 || checkpoint_every > n_steps) ? n_steps : checkpoint_every;

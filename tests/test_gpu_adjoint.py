@@ -9,6 +9,8 @@ Ra for a fixed time-step sequence.  Checks:
   * directional derivatives against FP64 central finite differences of the
     GPU forward, eps = 1e-6 relative (agreement 1e-6 relative, the bar the
     gradient path is held to), and against finite differences of the oracle;
+  * the dot-product test against the tangent-linear run of the oracle's step
+    (oracle/pizza_tangent.py): <tangent(d), 1> = Re<g, d> to 1e-8;
   * dJ/dRa against finite differences;
   * independence of the checkpoint interval (recomputation is exact);
   * the torch.autograd.Function path.
@@ -199,3 +201,90 @@ def test_c3_gradient_16_directions(pz):
     fd = (jp - jm) / (2 * h)
     assert abs(fd - dra[0]) <= GRAD_TOL * abs(fd), (fd, dra[0])
     print("c3 FD rel errors: max %.2e, dJ/dRa rel %.2e" % (max(errs), abs(fd - dra[0]) / abs(fd)))
+
+
+def test_dot_product_with_oracle_tangent_linear_run(pz):
+    """The GPU gradient against exact directional derivatives from the
+    tangent-linear run of the oracle's step (no finite-difference error)."""
+    from oracle import pizza_tangent as pt
+    from oracle.pizza_oracle import Params
+    t0 = seeded(SMALL, 8, 1e-2)
+    ens = pz.Ensemble(gpu_config(SMALL))
+    fwd(ens, t0, 12, 7, SCHED, ck=4)
+    g, dra = ens.adjoint_backward()
+    o = pt.StepOps(Params(**SMALL))
+    rng = np.random.default_rng(21)
+    for _ in range(3):
+        d = rng.standard_normal(t0.shape) + 1j * rng.standard_normal(t0.shape)
+        dr = 1e3 * rng.standard_normal()
+        _, dJ = pt.tangent(o, t0, d, SCHED, SMALL["ra"], dr, range(6, 13))
+        ad = directional(g[0], d) + dra[0] * dr
+        assert abs(dJ - ad) <= 1e-8 * abs(dJ), (dJ, ad)
+
+
+def test_nutop_objective_vs_fd(pz):
+    t0 = seeded(SMALL, 12, 1e-2)
+    ens = pz.Ensemble(gpu_config(SMALL))
+    ens.set_state(0, temp=t0)
+    J, _ = ens.adjoint_forward(12, 12, 4, SCHED[None, :], objective="nutop")
+    # the objective is the mean of the NuTop column of the time series
+    sim = oracle(SMALL, temp0=t0)
+    sim.dt_schedule = SCHED
+    vals = []
+    for _ in range(12):
+        sim.advance()
+        vals.append(series_from_oracle(sim)[8])
+    assert abs(J[0] - np.mean(vals)) <= 1e-10 * abs(np.mean(vals))
+    g, dra = ens.adjoint_backward()
+    rng = np.random.default_rng(13)
+    for _ in range(3):
+        d = rng.standard_normal(t0.shape) + 1j * rng.standard_normal(t0.shape)
+        eps = 1e-6 * np.max(np.abs(t0)) / np.max(np.abs(d))
+        js = []
+        for sgn in (1, -1):
+            ens.set_state(0, temp=t0 + sgn * eps * d)
+            js.append(ens.adjoint_forward(12, 12, 0, SCHED[None, :], objective="nutop")[0][0])
+        fd = (js[0] - js[1]) / (2 * eps)
+        assert abs(fd - directional(g[0], d)) <= GRAD_TOL * abs(fd), (fd, directional(g[0], d))
+
+
+def test_batched_nutop_gradient_ensemble(pz):
+    """The batched adjoint workload's shape: 64 instances, N in {49, 65},
+    n_phi in {126, 192}, E=1e-4, Ra log-uniform, dtMax=5e-5 under the
+    Courant controller, 300 steps, checkpoint every 30, gradient of the mean
+    NuTop in one forward+backward sweep; FD on 4 instances (all instances are
+    perturbed in the same two batched runs).  Time scheme CNAB2 (the adjoint
+    covers the multistep CNAB2 step)."""
+    rng = np.random.default_rng(64)
+    specs = []
+    for i in range(64):
+        N = (49, 65)[i % 2]
+        mmax = (42, 64)[(i // 2) % 2]
+        lo, hi = 6.0, (6.5 if N == 49 else 7.0)
+        specs.append(dict(n_r_max=N, n_cheb_max=N, m_max=mmax, ek=1e-4, ra=float(10 ** rng.uniform(lo, hi)),
+                          pr=1.0, radratio=0.35, l_ek_pump=True, time_scheme="CNAB2", dtMax=5e-5,
+                          matrix_solve="INFLUENCE"))
+    temps = [seeded(s, 100 + i, 1e-3) for i, s in enumerate(specs)]
+    ens = pz.Ensemble([gpu_config(s) for s in specs])
+    ens.set_state_all(temps)
+    J, dt = ens.adjoint_forward(300, 300, 30, objective="nutop")
+    g, dra = ens.adjoint_backward()
+    assert np.all(np.isfinite(J))
+    check = [0, 1, 2, 3]
+    ds = [rng.standard_normal(t.shape) + 1j * rng.standard_normal(t.shape) for t in temps]
+    # at these Rayleigh numbers the 300-step forward amplifies rounding: central
+    # differences are taken at two step sizes (rounding error falls, truncation
+    # error grows with eps) and the better one is held to the bar
+    errs = {}
+    for rel in (1e-6, 1e-5):
+        eps = [rel * np.max(np.abs(t)) / np.max(np.abs(d)) for t, d in zip(temps, ds)]
+        js = []
+        for sgn in (1, -1):
+            ens.set_state_all([t + sgn * e * d for t, e, d in zip(temps, eps, ds)])
+            js.append(ens.adjoint_forward(300, 300, 0, dt, objective="nutop")[0])
+        for i in check:
+            fd = (js[0][i] - js[1][i]) / (2 * eps[i])
+            errs.setdefault(i, []).append(abs(fd - directional(g[i], ds[i])) / abs(fd))
+    print("batched NuTop FD rel errors (eps 1e-6, 1e-5):", errs)
+    for i in check:
+        assert min(errs[i]) <= GRAD_TOL, (i, errs[i])
