@@ -169,6 +169,14 @@ class Clocks:
                 "samples": len(sm)}
 
 
+# DRAM bytes (read + write) of one k_mloop launch over its algorithmic bytes,
+# from an ncu capture of the 16-instance ensemble (same generator and seed):
+# 77.4 MB measured for 81.9 MB algorithmic.  The 256-instance launch is too
+# large to capture under the profiling rules; its traffic is this ratio times
+# its algorithmic bytes (traffic grows with the (instance, m) items processed).
+MLOOP_TRAFFIC_PER_ALGO_BYTE = 77.40e6 / 81868128.0
+
+
 def measured_peaks():
     try:
         with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
@@ -406,9 +414,13 @@ def main():
     state_bytes = sum(t.size * 16 for t in temps)
     t0 = time.perf_counter()
     ens2.set_state_all(temps)
+    n_dt_changes, prev_dt = 0, None
     for _ in range(args.steps):
         ens2.step(1, sync=False)
         ens2.latest_rows(rows)
+        if prev_dt is not None:
+            n_dt_changes += int(np.count_nonzero(rows[:, 15] != prev_dt))
+        prev_dt = rows[:, 15].copy()
     ens2.sync()
     e2e_wall = time.perf_counter() - t0
     ens2.close()
@@ -446,12 +458,16 @@ def main():
         "plain_detail": plain,
         "kernel_ms_per_step": kms,
         "roofline": {"bound": "hbm", "kernel": "k_mloop", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                     "frac": achieved / peak, "peak_kind": peak_kind, "traffic": None,
+                     "frac": achieved / peak, "peak_kind": peak_kind,
+                     "traffic": MLOOP_TRAFFIC_PER_ALGO_BYTE * byts,
+                     "traffic_note": "DRAM bytes per launch, ncu capture of the 16-instance ensemble scaled by "
+                                     "algorithmic bytes",
                      "algorithmic_bytes": byts,
                      "fp64": {"achieved_tflops": flops / (mloop_ms * 1e-3) / 1e12, "peak_tflops": fp64_peak,
                               "peak_kind": "cuBLAS DGEMM 4096^3 measured in this run",
                               "frac": (flops / (mloop_ms * 1e-3) / 1e12 / fp64_peak) if fp64_peak else None}},
         "dominant_kernel": dom,
+        "operator_rebuilds_per_step": n_dt_changes / max(1, args.steps - 1),
         "adjoint": adj,
         "cpu_baseline": cpu,
         "e2e": e2e,

@@ -1284,24 +1284,28 @@ __global__ void k_obs(PzDev d, int only) {
   const double2* dT = V.fld(F_DTEMP, 0);
   const bool rot = !(I.flags & PZF_NON_ROT);
   double s_us = 0, s_up = 0, s_ax = 0, s_us3 = 0, s_up3 = 0, s_uz3 = 0, s_ax3 = 0, s_nu = 0, s_fl = 0;
-  for (int r = threadIdx.x; r < n; r += blockDim.x) {
+  // thread (r, c) sums the m = c, c + nc, ... terms of radius r; the radial
+  // weights are applied to those partial sums (their sum over c is the sum
+  // over m of outputs.f90:418-830)
+  const int nc = max(1, (int)blockDim.x / n);
+  for (int t = threadIdx.x; t < nc * n; t += blockDim.x) {
+    const int r = t % n, c = t / n;
     double us2 = 0, up2 = 0, nu = 0, fl = 0, ax = 0;
-    for (int mi = 0; mi < M; ++mi) {
+    for (int mi = c; mi < M; mi += nc) {
       const long long o = (long long)mi * n + r;
-      const double2 a = us[o], b = up[o], t = T[o], dt = dT[o];
+      const double2 a = us[o], b = up[o], tt = T[o], dt = dT[o];
       const double mm = (double)(mi * I.minc);
       if (mi == 0) {
         us2 += a.x * a.x;
         up2 += b.x * b.x;
         ax = b.x * b.x;
-        nu += dt.x * dt.x + mm * mm * or2[r] * (t.x * t.x);
-        fl += a.x * t.x;
-        fl = fl - I.TdiffFac * dt.x - I.TdiffFac * dtcond[r];
+        nu += dt.x * dt.x + mm * mm * or2[r] * (tt.x * tt.x);
+        fl += a.x * tt.x - I.TdiffFac * dt.x - I.TdiffFac * dtcond[r];
       } else {
         us2 += 2.0 * (a.x * a.x + a.y * a.y);
         up2 += 2.0 * (b.x * b.x + b.y * b.y);
-        nu += 2.0 * (dt.x * dt.x + dt.y * dt.y) + mm * mm * or2[r] * 2.0 * (t.x * t.x + t.y * t.y);
-        fl += 2.0 * (a.x * t.x + a.y * t.y);
+        nu += 2.0 * (dt.x * dt.x + dt.y * dt.y) + mm * mm * or2[r] * 2.0 * (tt.x * tt.x + tt.y * tt.y);
+        fl += 2.0 * (a.x * tt.x + a.y * tt.y);
       }
     }
     nu = nu * rr[r] * h[r];
@@ -1431,7 +1435,7 @@ cudaError_t pz_launch_start(const PzDev& d, int only, cudaStream_t s) {
 }
 
 cudaError_t pz_launch_obs(const PzDev& d, int only, cudaStream_t s) {
-  k_obs<<<d.n_inst, PZ_THREADS, 0, s>>>(d, only);
+  k_obs<<<d.n_inst, 256, 0, s>>>(d, only);
   return cudaGetLastError();
 }
 
@@ -1447,7 +1451,7 @@ cudaError_t pz_launch_step_kernel(const PzDev& d, int kind, int stage, cudaStrea
     case PZK_CFL: k_cfl<<<d.n_inst, 32, 0, s>>>(d); break;
     case PZK_BUILD: k_build<<<d.n_mitems, PZ_THREADS, d.smem_build, s>>>(d); break;
     case PZK_MLOOP: k_mloop<<<d.n_mitems, mloop_threads(d.maxN), ms_smem_bytes(d.maxN), s>>>(d, stage); break;
-    case PZK_OBS: k_obs<<<d.n_inst, PZ_THREADS, 0, s>>>(d, -1); break;
+    case PZK_OBS: k_obs<<<d.n_inst, 256, 0, s>>>(d, -1); break;
     case PZK_ASSEMBLE: k_assemble<<<d.n_mitems, mloop_threads(d.maxN), ms_smem_bytes(d.maxN), s>>>(d); break;
     default: return cudaErrorInvalidValue;
   }
