@@ -139,6 +139,25 @@ int pz_get_state(pz_handle* h, int inst, double* us, double* up, double* om,
                  double* psi, double* temp, double* dtemp, double* time,
                  double* dt);
 
+/* History slots of the IMEX time arrays (type_tarray, src/time_array.f90:11-71)
+ * at a step boundary, in the layout of pz_set_state: field 0 temperature,
+ * 1 vorticity (u_phi for m = 0); kind 0 old, 1 impl, 2 expl; slot 1-based
+ * as in dfdt%old(:,:,slot).  Slot 1 of old/impl is the current state's
+ * (recomputed from the fields by pz_set_state); expl slot 1 is formed by the
+ * next step.  These carry a multistep run across a checkpoint
+ * (src/checkpoints.f90:868-924 writes slots 2..n).  pz_set_history
+ * overwrites the slot on the device. */
+int pz_get_history(pz_handle* h, int inst, int field, int kind, int slot, double* out);
+int pz_set_history(pz_handle* h, int inst, int field, int kind, int slot, const double* in);
+
+/* Time, dt history (nexp values for the multistep family, 1 for DIRK) and
+ * step count of one instance.  pz_set_step_state restores them after
+ * pz_set_state; n_step >= nold - 1 skips the CNAB2 bridge of the first steps
+ * (a restart with a full history), and the operators are rebuilt at the next
+ * step. */
+int pz_get_step_state(pz_handle* h, int inst, double* time, double* dt, int* n_step);
+int pz_set_step_state(pz_handle* h, int inst, double time, const double* dt, int n_step);
+
 /* Time series of one instance: one row per completed step plus the start row,
  * most recent last, at most *n_rows rows (in: capacity, out: count).
  * Row layout (PZ_SERIES_COLS doubles):

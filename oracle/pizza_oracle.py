@@ -876,6 +876,40 @@ class Pizza:
         self._temp_rhs_imp(1, True, l_in_cheb=False)
         self._psi_rhs_imp(1, True, l_in_cheb=False)
 
+    def start_from_checkpoint(self, ck):
+        """get_start_fields with l_start_file (init_fields.f90:54-258) for a
+        version-7 checkpoint of the same grid and scheme (read_checkpoint,
+        checkpoints.f90:185-860, without grid mapping): fields, the history
+        slots 2..n, dt and time; then om and the first old/implicit slots as
+        for a fresh start.  Same scheme and Ekman number: no bridge, no AB1
+        (checkpoints.f90:398-416).  ``ck`` is a dict with header, us, up,
+        temp, hist_P, hist_T (expl 2..nexp, impl 2..nimp, old 2..nold)."""
+        ts, h = self.ts, ck["header"]
+        self.time = h["time"]
+        nd = len(h["dt"])
+        ts.dt[:nd] = h["dt"]
+        if nd < len(ts.dt):
+            ts.dt[nd:] = h["dt"][-1]
+        ts.set_weights()
+        self.us = np.array(ck["us"], complex)
+        self.up = np.array(ck["up"], complex)
+        self.temp = np.array(ck["temp"], complex)
+        if ts.family == "MULTISTEP":
+            order = ([("expl", k) for k in range(2, ts.nexp + 1)] + [("impl", k) for k in range(2, ts.nimp + 1)]
+                     + [("old", k) for k in range(2, ts.nold + 1)])
+            for (kind, k), aP, aT in zip(order, ck["hist_P"], ck["hist_T"]):
+                getattr(self.dpsidt, kind)[k - 1] = np.array(aP, complex)
+                getattr(self.dTdt, kind)[k - 1] = np.array(aT, complex)
+        c = self.cheb
+        self.dtemp = c.get_dr(self.temp)
+        work = c.get_dr(self.up)
+        m = self.mvec[:, None]
+        self.om = work + self.or1 * self.up - self.or1 * 1j * m * self.us
+        self._temp_rhs_imp(1, True, l_in_cheb=False)
+        self._psi_rhs_imp(1, True, l_in_cheb=False)
+        self.l_bridge_step = False
+        self.l_AB1 = False
+
     def _init_prop(self, init_t, amp):
         """initProp (init_fields.f90:260-376), modes init_t>0 and -1."""
         N, M = self.N, self.M

@@ -155,13 +155,18 @@ def load_library(path: str | None = None):
     lib.pz_adjoint_forward.argtypes = [vp, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, dp, dp, dp]
     lib.pz_adjoint_backward.argtypes = [vp, dp, dp]
     lib.pz_set_ra.argtypes = [vp, ctypes.c_int, ctypes.c_double]
+    lib.pz_get_history.argtypes = [vp, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, dp]
+    lib.pz_set_history.argtypes = [vp, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, dp]
+    lib.pz_get_step_state.argtypes = [vp, ctypes.c_int, dp, dp, ctypes.POINTER(ctypes.c_int)]
+    lib.pz_set_step_state.argtypes = [vp, ctypes.c_int, ctypes.c_double, dp, ctypes.c_int]
     lib.pz_destroy.argtypes = [ctypes.c_void_p]
     lib.pz_last_error.argtypes = [ctypes.c_void_p]
     lib.pz_last_error.restype = ctypes.c_char_p
     for f in ("pz_create", "pz_set_state", "pz_set_state_all", "pz_step", "pz_sync", "pz_get_state",
               "pz_get_series", "pz_get_dims", "pz_launches_per_step", "pz_latest_rows",
               "pz_step_profile", "pz_explicit_terms", "pz_explicit_terms_noalloc", "pz_adjoint_forward",
-              "pz_adjoint_backward", "pz_set_ra", "pz_destroy"):
+              "pz_adjoint_backward", "pz_set_ra", "pz_get_history", "pz_set_history", "pz_get_step_state",
+              "pz_set_step_state", "pz_destroy"):
         getattr(lib, f).restype = ctypes.c_int
     _lib = lib
     return lib
@@ -284,6 +289,33 @@ class Ensemble:
 
     def launches_per_step(self):
         return self.lib.pz_launches_per_step(self._h)
+
+    # -- history and step state (checkpoints) ------------------------------
+    def get_history(self, i, field, kind, slot):
+        """History slot (1-based) of the time arrays: field 0 temperature, 1
+        vorticity; kind 0 old, 1 impl, 2 expl.  (n_m, n_r) complex."""
+        n, m, _ = self.dims[i]
+        buf = np.zeros((n, m), np.complex128)
+        self._check(self.lib.pz_get_history(self._h, i, int(field), int(kind), int(slot), _dptr(buf.view(np.float64))))
+        return buf.T.copy()
+
+    def set_history(self, i, field, kind, slot, arr):
+        a = _carr(arr, self.shape(i))
+        self._check(self.lib.pz_set_history(self._h, i, int(field), int(kind), int(slot), _dptr(a.view(np.float64))))
+
+    def get_step_state(self, i):
+        """(time, dt history, n_step) of instance i."""
+        t = ctypes.c_double()
+        dt = np.zeros(4)
+        ns = ctypes.c_int()
+        self._check(self.lib.pz_get_step_state(self._h, i, ctypes.byref(t), _dptr(dt), ctypes.byref(ns)))
+        return t.value, dt, ns.value
+
+    def set_step_state(self, i, time, dt, n_step):
+        d = np.zeros(4)
+        dt = np.atleast_1d(np.asarray(dt, np.float64))
+        d[:len(dt)] = dt
+        self._check(self.lib.pz_set_step_state(self._h, i, float(time), _dptr(d), int(n_step)))
 
     # -- discrete adjoint -------------------------------------------------
     def set_ra(self, i, ra):

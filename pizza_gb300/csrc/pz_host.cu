@@ -863,6 +863,110 @@ extern "C" int pz_get_state(pz_handle* h, int inst, double* us, double* up, doub
   return st.status ? check_status(h) : PZ_OK;
 }
 
+namespace {
+// physical ring slot of logical history slot `slot` (1-based) at a step boundary
+int hist_phys(const PzInst& I, const PzState& st, int kind, int slot) {
+  const int n = kind == 0 ? I.nold : (kind == 1 ? I.nimp : I.nexp);
+  if (I.dirk) return slot - 1;
+  const int base = kind == 0 ? st.b_old : (kind == 1 ? st.b_impl : st.b_expl);
+  return (base + slot - 1) % n;
+}
+int hist_args(pz_handle* h, int inst, int field, int kind, int slot, const char* who) {
+  if (!h) return fail(nullptr, PZ_E_ARG, std::string(who) + ": null handle");
+  if (inst < 0 || inst >= h->n_inst) return fail(h, PZ_E_ARG, std::string(who) + ": instance out of range");
+  const PzInst& I = h->inst[inst];
+  const int n = kind == 0 ? I.nold : (kind == 1 ? I.nimp : (kind == 2 ? I.nexp : 0));
+  if (field < 0 || field > 1 || kind < 0 || kind > 2 || slot < 1 || slot > n)
+    return fail(h, PZ_E_ARG, std::string(who) + ": field, kind or slot out of range");
+  return PZ_OK;
+}
+}  // namespace
+
+extern "C" int pz_get_history(pz_handle* h, int inst, int field, int kind, int slot, double* out) {
+  int rc = hist_args(h, inst, field, kind, slot, "pz_get_history");
+  if (rc) return rc;
+  if (!out) return fail(h, PZ_E_ARG, "pz_get_history: null output");
+  const PzInst& I = h->inst[inst];
+  const long long MN = (long long)I.M * I.N;
+  PzState st;
+  std::vector<double> buf(2 * MN);
+  cudaError_t e = cudaMemcpyAsync(&st, h->d_state + inst, sizeof(PzState), cudaMemcpyDeviceToHost, h->stream);
+  if (!e) e = cudaStreamSynchronize(h->stream);
+  if (e) return cuda_fail(h, e, "pz_get_history");
+  const long long off = pz_hist_off(I, field, kind, hist_phys(I, st, kind, slot));
+  e = cudaMemcpyAsync(buf.data(), h->pool + off, buf.size() * sizeof(double), cudaMemcpyDeviceToHost, h->stream);
+  if (!e) e = cudaStreamSynchronize(h->stream);
+  if (e) return cuda_fail(h, e, "pz_get_history");
+  for (int r = 0; r < I.N; ++r)
+    for (int m = 0; m < I.M; ++m) {
+      out[2 * (m + (long long)r * I.M)] = buf[2 * ((long long)m * I.N + r)];
+      out[2 * (m + (long long)r * I.M) + 1] = buf[2 * ((long long)m * I.N + r) + 1];
+    }
+  return PZ_OK;
+}
+
+extern "C" int pz_set_history(pz_handle* h, int inst, int field, int kind, int slot, const double* in) {
+  int rc = hist_args(h, inst, field, kind, slot, "pz_set_history");
+  if (rc) return rc;
+  if (!in) return fail(h, PZ_E_ARG, "pz_set_history: null input");
+  pz_adjoint_invalidate(h);
+  const PzInst& I = h->inst[inst];
+  const long long MN = (long long)I.M * I.N;
+  PzState st;
+  std::vector<double> buf(2 * MN);
+  cudaError_t e = cudaMemcpyAsync(&st, h->d_state + inst, sizeof(PzState), cudaMemcpyDeviceToHost, h->stream);
+  if (!e) e = cudaStreamSynchronize(h->stream);
+  if (e) return cuda_fail(h, e, "pz_set_history");
+  for (int r = 0; r < I.N; ++r)
+    for (int m = 0; m < I.M; ++m) {
+      buf[2 * ((long long)m * I.N + r)] = in[2 * (m + (long long)r * I.M)];
+      buf[2 * ((long long)m * I.N + r) + 1] = in[2 * (m + (long long)r * I.M) + 1];
+    }
+  const long long off = pz_hist_off(I, field, kind, hist_phys(I, st, kind, slot));
+  e = cudaMemcpyAsync(h->pool + off, buf.data(), buf.size() * sizeof(double), cudaMemcpyHostToDevice, h->stream);
+  if (!e) e = cudaStreamSynchronize(h->stream);   // buf is pageable and local
+  if (e) return cuda_fail(h, e, "pz_set_history");
+  return PZ_OK;
+}
+
+extern "C" int pz_get_step_state(pz_handle* h, int inst, double* time, double* dt, int* n_step) {
+  if (!h) return fail(nullptr, PZ_E_ARG, "pz_get_step_state: null handle");
+  if (inst < 0 || inst >= h->n_inst) return fail(h, PZ_E_ARG, "pz_get_step_state: instance out of range");
+  PzState st;
+  cudaError_t e = cudaMemcpyAsync(&st, h->d_state + inst, sizeof(PzState), cudaMemcpyDeviceToHost, h->stream);
+  if (!e) e = cudaStreamSynchronize(h->stream);
+  if (e) return cuda_fail(h, e, "pz_get_step_state");
+  const PzInst& I = h->inst[inst];
+  if (time) *time = st.time;
+  if (dt)
+    for (int k = 0; k < (I.dirk ? 1 : I.nexp); ++k) dt[k] = st.dt[k];
+  if (n_step) *n_step = st.n_step;
+  return PZ_OK;
+}
+
+extern "C" int pz_set_step_state(pz_handle* h, int inst, double time, const double* dt, int n_step) {
+  if (!h) return fail(nullptr, PZ_E_ARG, "pz_set_step_state: null handle");
+  if (inst < 0 || inst >= h->n_inst || !dt || n_step < 0)
+    return fail(h, PZ_E_ARG, "pz_set_step_state: bad arguments");
+  pz_adjoint_invalidate(h);
+  const PzInst& I = h->inst[inst];
+  const int nd = I.dirk ? 1 : I.nexp;
+  for (int k = 0; k < nd; ++k)
+    if (!(dt[k] > 0.0)) return fail(h, PZ_E_ARG, "pz_set_step_state: dt must be positive");
+  PzState st;
+  cudaError_t e = cudaMemcpyAsync(&st, h->d_state + inst, sizeof(PzState), cudaMemcpyDeviceToHost, h->stream);
+  if (!e) e = cudaStreamSynchronize(h->stream);
+  if (e) return cuda_fail(h, e, "pz_set_step_state");
+  st.time = time;
+  for (int k = 0; k < nd; ++k) st.dt[k] = dt[k];
+  st.n_step = n_step;
+  st.lMatNext = 1;   // operators for the restored dt at the next step
+  e = cudaMemcpyAsync(h->d_state + inst, &st, sizeof(PzState), cudaMemcpyHostToDevice, h->stream);
+  if (!e) e = cudaStreamSynchronize(h->stream);
+  if (e) return cuda_fail(h, e, "pz_set_step_state");
+  return PZ_OK;
+}
+
 extern "C" int pz_get_series(pz_handle* h, int inst, double* rows, int* n_rows) {
   if (!h) return fail(nullptr, PZ_E_ARG, "pz_get_series: null handle");
   if (inst < 0 || inst >= h->n_inst || !n_rows) return fail(h, PZ_E_ARG, "pz_get_series: bad arguments");

@@ -1,0 +1,229 @@
+"""pizza's files on the host side of the GPU step: the time series it writes
+(e_kin.TAG, e_kin_3D.TAG, heat.TAG; src/outputs.f90:677-793) and its
+version-7 checkpoints (src/checkpoints.f90:33-183 write, :185-860 read).
+
+A run on the GPU can therefore leave the same text series a pizza.exe run
+leaves (python/pizza reads them), save a checkpoint pizza.exe can restart
+from, and restart from a checkpoint pizza.exe wrote -- for the same grid and
+time-scheme family (pizza's own reader also interpolates between grids and
+bridges between schemes; that mapping is not restated here).
+"""
+from __future__ import annotations
+
+import os
+
+import numpy as np
+
+# columns of Ensemble.series rows written to each file
+SERIES_FILES = {
+    "e_kin": (0, 1, 2, 3),                    # time, us2_2D, up2_2D, up2_axi_2D
+    "e_kin_3D": (0, 4, 5, 6, 7),              # time, us2_3D, up2_3D, uz2_3D, up2_axi_3D
+    "heat": (0, 8, 9, 10, 11, 12, 13, 14),    # time, NuTop, NuBot, Nu_vol, Nu_int, tTop, tBot, beta_t
+}
+
+
+def fortran_es(x: float, w: int, d: int) -> str:
+    """The Fortran ESw.d edit descriptor: one nonzero digit before the point,
+    d after it, a two-digit signed exponent after 'E' (three digits replace
+    the 'E' when |exponent| >= 100), right-justified in w columns."""
+    s = f"{float(x):.{d}E}"
+    mant, exp = s.split("E")
+    e = int(exp)
+    if abs(e) >= 100:
+        s = f"{mant}{'+' if e >= 0 else '-'}{abs(e):03d}"
+    else:
+        s = f"{mant}E{'+' if e >= 0 else '-'}{abs(e):02d}"
+    if len(s) > w:
+        return "*" * w
+    return s.rjust(w)
+
+
+def format_series_line(values) -> str:
+    """'(1P, ES20.12, kES16.8)' as pizza writes its time series."""
+    return fortran_es(values[0], 20, 12) + "".join(fortran_es(v, 16, 8) for v in values[1:])
+
+
+def write_series(ens, i: int, tag: str, directory: str = ".", rows=None):
+    """Write e_kin.TAG, heat.TAG and (rotating runs) e_kin_3D.TAG of instance i
+    from its time-series rows (Ensemble.series: at most the last 1024).
+    Returns the paths written."""
+    if rows is None:
+        rows = ens.series(i)
+    rot = not ens.configs[i].l_non_rot and ens.configs[i].ek >= 0.0
+    paths = []
+    for name, cols in SERIES_FILES.items():
+        if name == "e_kin_3D" and not rot:
+            continue
+        p = os.path.join(directory, f"{name}.{tag}")
+        with open(p, "w") as f:
+            for row in rows:
+                f.write(format_series_line([row[c] for c in cols]) + "\n")
+        paths.append(p)
+    return paths
+
+
+# ---------------------------------------------------------------------------
+# version-7 checkpoints (stream-unformatted, native byte order)
+# ---------------------------------------------------------------------------
+_I4, _F8 = np.dtype("<i4"), np.dtype("<f8")
+
+
+def _grid_r(n_r_max: int, radratio: float) -> np.ndarray:
+    """Gauss-Lobatto radii (src/chebyshev.f90, no mapping): r(1) = r_cmb."""
+    r_cmb = 1.0 / (1.0 - radratio)
+    r_icb = r_cmb - 1.0
+    x = np.cos(np.pi * np.arange(n_r_max) / (n_r_max - 1))
+    return 0.5 * (r_cmb - r_icb) * x + 0.5 * (r_cmb + r_icb)
+
+
+def write_checkpoint(path: str, header: dict, fields: dict):
+    """Write a version-7 checkpoint (write_checkpoint_mloc).
+
+    header: time, family ('MULTISTEP' or 'DIRK'), nexp, nimp, nold, dt (array),
+    ra, pr, ek, radratio, n_r_max, m_max, minc, n_max, r (n_r_max radii).
+    fields: us, up, temp ((n_m_max, n_r_max) complex) and, for MULTISTEP,
+    lists hist_P and hist_T of the slots written after up and temp: expl
+    2..nexp, impl 2..nimp, old 2..nold, in that order."""
+    h = header
+    with open(path, "wb") as f:
+        f.write(np.array([7], _I4).tobytes())
+        f.write(np.array([h["time"]], _F8).tobytes())
+        f.write(np.array([1], _I4).tobytes())                            # l_cheb_coll
+        f.write(h["family"].ljust(10)[:10].encode())
+        f.write(np.array([h["nexp"], h["nimp"], h["nold"]], _I4).tobytes())
+        f.write(np.asarray(h["dt"], _F8).tobytes())
+        f.write(np.array([h["ra"], h["pr"], 0.0, 0.0, h["ek"], 0.0, h["radratio"]], _F8).tobytes())
+        f.write(np.array([h["n_r_max"], h["m_max"], h["minc"]], _I4).tobytes())
+        f.write("cheb".ljust(72).encode())
+        f.write(np.array([h["n_max"], h.get("order_boundary", 0)], _I4).tobytes())
+        f.write(np.array([0.0, 0.0], _F8).tobytes())                     # alph1, alph2 (no mapping)
+        f.write(np.asarray(h["r"], _F8).tobytes())
+        f.write(np.array([1, 0, 0], _I4).tobytes())                      # l_heat, l_chem, l_phase_field
+
+        def put(a):
+            # (n_m_max, n_r_max) Fortran order: m fastest
+            f.write(np.asfortranarray(np.asarray(a, np.complex128)).tobytes(order="F"))
+
+        put(fields["us"])
+        put(fields["up"])
+        for a in fields.get("hist_P", []):
+            put(a)
+        put(fields["temp"])
+        for a in fields.get("hist_T", []):
+            put(a)
+
+
+def read_checkpoint(path: str) -> dict:
+    """Read a version-7 checkpoint written by pizza.exe or write_checkpoint."""
+    with open(path, "rb") as f:
+        buf = f.read()
+    pos = 0
+
+    def take(dtype, n=1):
+        nonlocal pos
+        a = np.frombuffer(buf, dtype=dtype, count=n, offset=pos)
+        pos += a.nbytes
+        return a
+
+    def chars(n):
+        nonlocal pos
+        s = buf[pos:pos + n].decode(errors="replace")
+        pos += n
+        return s.strip()
+
+    version = int(take(_I4)[0])
+    if version != 7:
+        raise ValueError(f"checkpoint version {version}: only version 7 is read")
+    h = {"version": version, "time": float(take(_F8)[0]), "l_cheb_coll": bool(take(_I4)[0])}
+    h["family"] = chars(10)
+    h["nexp"], h["nimp"], h["nold"] = (int(v) for v in take(_I4, 3))
+    h["dt"] = take(_F8, h["nexp"] if h["family"] == "MULTISTEP" else 1).copy()
+    ra, pr, raxi, sc, ek, stef, radratio = take(_F8, 7)
+    h.update(ra=float(ra), pr=float(pr), raxi=float(raxi), sc=float(sc), ek=float(ek), stef=float(stef),
+             radratio=float(radratio))
+    h["n_r_max"], h["m_max"], h["minc"] = (int(v) for v in take(_I4, 3))
+    h["rscheme"] = chars(72)
+    h["n_max"], h["order_boundary"] = (int(v) for v in take(_I4, 2))
+    h["alph1"], h["alph2"] = (float(v) for v in take(_F8, 2))
+    h["r"] = take(_F8, h["n_r_max"]).copy()
+    h["l_heat"], h["l_chem"], h["l_phase_field"] = (bool(v) for v in take(_I4, 3))
+    M = h["m_max"] // h["minc"] + 1
+    N = h["n_r_max"]
+    nh = (h["nexp"] - 1) + (h["nimp"] - 1) + (h["nold"] - 1) if h["family"] == "MULTISTEP" else 0
+
+    def field():
+        return take(np.dtype("<c16"), M * N).reshape((M, N), order="F").copy()
+
+    out = {"header": h, "us": field(), "up": field()}
+    out["hist_P"] = [field() for _ in range(nh)]
+    if h["l_heat"]:
+        out["temp"] = field()
+        out["hist_T"] = [field() for _ in range(nh)]
+    if pos != len(buf):
+        raise ValueError(f"checkpoint {path}: {len(buf) - pos} trailing bytes (chemistry or phase field?)")
+    return out
+
+
+def _hist_order(nexp, nimp, nold):
+    """(kind, slot) of the history arrays in checkpoint order (write_one_field_mpi)."""
+    return ([(2, k) for k in range(2, nexp + 1)] + [(1, k) for k in range(2, nimp + 1)]
+            + [(0, k) for k in range(2, nold + 1)])
+
+
+def save_checkpoint(ens, i: int, path: str):
+    """Checkpoint of instance i at the current step boundary."""
+    c = ens.configs[i]
+    st = ens.get_state(i)
+    time, dt, _ = ens.get_step_state(i)
+    nexp, nimp, nold, family = _scheme_counts(ens, i)
+    n, m, _ = ens.dims[i]
+    header = dict(time=time, family=family, nexp=nexp, nimp=nimp, nold=nold,
+                  dt=dt[:nexp] if family == "MULTISTEP" else dt[:1], ra=c.ra, pr=c.pr, ek=c.ek,
+                  radratio=c.radratio, n_r_max=n, m_max=c.m_max, minc=c.minc,
+                  n_max=c.n_cheb_max if c.n_cheb_max is not None else n, r=_grid_r(n, c.radratio))
+    fields = dict(us=st["us"], up=st["up"], temp=st["temp"])
+    if family == "MULTISTEP":
+        order = _hist_order(nexp, nimp, nold)
+        fields["hist_P"] = [ens.get_history(i, 1, k, s) for k, s in order]
+        fields["hist_T"] = [ens.get_history(i, 0, k, s) for k, s in order]
+    write_checkpoint(path, header, fields)
+
+
+def restart_from_checkpoint(ens, i: int, path: str):
+    """Start instance i from a checkpoint of the same grid and scheme family:
+    the fields (getStartFields recomputes the first old/implicit slots from
+    them), the history slots 2..n, time and dt."""
+    ck = read_checkpoint(path)
+    h = ck["header"]
+    n, m, _ = ens.dims[i]
+    c = ens.configs[i]
+    if (h["n_r_max"], h["m_max"], h["minc"]) != (n, c.m_max, c.minc):
+        raise ValueError("checkpoint grid differs from the instance's (grid mapping is not restated)")
+    nexp, nimp, nold, family = _scheme_counts(ens, i)
+    if h["family"] != family or (family == "MULTISTEP" and (h["nexp"], h["nimp"], h["nold"]) != (nexp, nimp, nold)):
+        raise ValueError("checkpoint time scheme differs from the instance's (scheme bridging is not restated)")
+    if not h["l_heat"]:
+        raise ValueError("checkpoint without temperature")
+    ens.set_state(i, us=ck["us"], up=ck["up"], temp=ck["temp"])
+    if family == "MULTISTEP":
+        for (k, s), aP, aT in zip(_hist_order(nexp, nimp, nold), ck["hist_P"], ck["hist_T"]):
+            ens.set_history(i, 1, k, s, aP)
+            ens.set_history(i, 0, k, s, aT)
+    ens.set_step_state(i, h["time"], h["dt"], max(nold, 1))
+    return h
+
+
+def _scheme_counts(ens, i):
+    """(nexp, nimp, nold, family) of instance i's time scheme
+    (multistep_schemes.f90:53-106, dirk_schemes.f90:35-244)."""
+    ts = ens.configs[i].time_scheme.upper()
+    multistep = {"CNAB2": (2, 1, 1), "SBDF2": (2, 1, 2), "BDF2AB2": (2, 1, 2), "SBDF3": (3, 1, 3),
+                 "BDF3AB3": (3, 1, 3), "SBDF4": (4, 1, 4), "BDF4AB4": (4, 1, 4), "CNLF": (2, 2, 2),
+                 "MODCNAB": (2, 2, 2), "TVB33": (3, 3, 3)}
+    if ts in multistep:
+        nexp, nimp, nold = multistep[ts]
+        return nexp, nimp, nold, "MULTISTEP"
+    stages = {"ARS222": 2, "ARS232": 3, "ARS233": 3, "SSP222": 3, "LSDIRK222": 3, "LZ232": 2, "CK232": 2,
+              "ARS443": 4, "BPR353": 4, "PC2": 3, "ARS343": 4, "MARS343": 4, "SSP322": 4, "SSP332": 4}
+    ns = stages[ts]
+    return ns, ns, 1, "DIRK"

@@ -1,0 +1,80 @@
+"""Time series files and checkpoint restarts of GPU runs (needs a GB300)."""
+import json
+import os
+
+import numpy as np
+import pytest
+
+from tests.helpers import gpu_config, oracle, seeded
+from tests.test_gpu_parity import check_fields
+
+pytestmark = pytest.mark.gpu
+HERE = os.path.dirname(os.path.abspath(__file__))
+C0 = dict(n_r_max=33, n_cheb_max=33, m_max=32, ek=1e-3, ra=1e5, pr=1.0, radratio=0.35, l_ek_pump=True,
+          dtMax=1e-4)
+
+
+@pytest.fixture(scope="module")
+def pz():
+    import torch
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    from pizza_gb300 import build as b
+    b.build()
+    import pizza_gb300
+    return pizza_gb300
+
+
+def test_series_files_match_pizza_fixture(pz, tmp_path):
+    """e_kin_3D.TAG of a GPU run of RotE1e3EkPump, written in pizza's format,
+    against the file pizza.exe wrote (values to 1e-8, same line layout)."""
+    from pizza_gb300.pizza_io import write_series
+    with open(os.path.join(HERE, "golden", "cases.json")) as f:
+        p = dict(json.load(f)["RotE1e3EkPump"]["params"])
+    sim = oracle(p)
+    ens = pz.Ensemble(gpu_config(p))
+    ens.set_state(0, temp=sim.temp.copy())
+    ens.step(p["n_time_steps"])
+    rows = ens.series(0, p["n_time_steps"] + 1)[::p["n_log_step"]]
+    paths = write_series(ens, 0, "gpu", str(tmp_path), rows=rows)
+    assert {os.path.basename(x) for x in paths} == {"e_kin.gpu", "e_kin_3D.gpu", "heat.gpu"}
+    with open(os.path.join(HERE, "golden", "RotE1e3EkPump.txt")) as f:
+        ref_lines = [ln.rstrip("\n") for ln in f if ln.strip()]
+    with open(tmp_path / "e_kin_3D.gpu") as f:
+        got_lines = [ln.rstrip("\n") for ln in f]
+    assert [len(x) for x in got_lines] == [len(x) for x in ref_lines]
+    np.testing.assert_allclose(np.loadtxt(tmp_path / "e_kin_3D.gpu"), np.loadtxt(os.path.join(HERE, "golden",
+                               "RotE1e3EkPump.txt")), rtol=1e-8, atol=1e-14)
+
+
+@pytest.mark.parametrize("scheme,solve", [("CNAB2", "INFLUENCE"), ("SBDF3", "DIRECT"), ("TVB33", "INFLUENCE"),
+                                          ("ARS222", "DIRECT")])
+def test_checkpoint_restart_matches_pizza_restart(pz, tmp_path, scheme, solve):
+    """10 steps, a version-7 checkpoint, a restart in a new handle and 10 more
+    steps, against the oracle restarting from the same file.
+
+    A checkpoint holds us and up, not the vorticity; a restart recomputes om
+    from the velocities (getStartFields), so a run with the influence-matrix
+    solve, whose wall vorticity is not the velocities', continues differently
+    from an uninterrupted run -- in pizza as here.  The parity bar is the
+    restart pizza makes."""
+    from oracle.pizza_oracle import Params, Pizza
+    from pizza_gb300.pizza_io import read_checkpoint, restart_from_checkpoint, save_checkpoint
+    spec = dict(C0, time_scheme=scheme, matrix_solve=solve)
+    t0 = seeded(spec, 50)
+    a = pz.Ensemble(gpu_config(spec))
+    a.set_state(0, temp=t0)
+    a.step(10)
+    ck = str(tmp_path / "checkpoint_t=10.test")
+    save_checkpoint(a, 0, ck)
+    b = pz.Ensemble(gpu_config(spec))
+    h = restart_from_checkpoint(b, 0, ck)
+    assert h["family"] == ("DIRK" if scheme == "ARS222" else "MULTISTEP")
+    b.step(10)
+    sim = Pizza(Params(**spec))
+    sim.start_from_checkpoint(read_checkpoint(ck))
+    for _ in range(10):
+        sim.advance()
+    gb = b.get_state(0)
+    check_fields(sim, gb, 1e-10, f"{scheme} restarted")
+    assert abs(gb["time"] - sim.time) < 1e-15

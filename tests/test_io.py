@@ -1,0 +1,54 @@
+"""pizza's time-series text format and version-7 checkpoint layout
+(pizza_gb300/pizza_io.py), on the CPU."""
+import os
+
+import numpy as np
+import pytest
+
+from pizza_gb300.pizza_io import fortran_es, format_series_line, read_checkpoint, write_checkpoint, _grid_r
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+
+
+@pytest.mark.parametrize("case", ["RotE1e3EkPump", "DIRKSchemes", "NonRotRa2e3", "MultistepSchemes"])
+def test_series_format_reproduces_pizza_lines(case):
+    """Every line pizza.exe printed, re-printed from its values, is identical."""
+    with open(os.path.join(HERE, "golden", f"{case}.txt")) as f:
+        lines = [ln.rstrip("\n") for ln in f if ln.strip()]
+    for ln in lines:
+        vals = [float(v) for v in ln.split()]
+        assert format_series_line(vals) == ln
+
+
+def test_fortran_es_edge_cases():
+    assert fortran_es(0.0, 16, 8) == "  0.00000000E+00"
+    assert fortran_es(-1.5e-7, 16, 8) == " -1.50000000E-07"
+    assert fortran_es(2.5e123, 16, 8) == "  2.50000000+123"
+    assert fortran_es(1.0, 20, 12) == "  1.000000000000E+00"
+
+
+def test_checkpoint_roundtrip(tmp_path):
+    rng = np.random.default_rng(0)
+    N, m_max = 17, 8
+    M = m_max + 1
+
+    def c():
+        return rng.standard_normal((M, N)) + 1j * rng.standard_normal((M, N))
+
+    header = dict(time=0.125, family="MULTISTEP", nexp=3, nimp=1, nold=3, dt=np.array([1e-4, 2e-4, 3e-4]),
+                  ra=1e5, pr=1.0, ek=1e-3, radratio=0.35, n_r_max=N, m_max=m_max, minc=1, n_max=N,
+                  r=_grid_r(N, 0.35))
+    fields = dict(us=c(), up=c(), temp=c(), hist_P=[c() for _ in range(4)], hist_T=[c() for _ in range(4)])
+    p = str(tmp_path / "checkpoint_end.test")
+    write_checkpoint(p, header, fields)
+    # header bytes as written by write_checkpoint_mloc, then us and (1 + 4) each for up and temp
+    hdr = 4 + 8 + 4 + 10 + 12 + 8 * 3 + 8 * 7 + 12 + 72 + 8 + 16 + 8 * N + 12
+    assert os.path.getsize(p) == hdr + 11 * M * N * 16
+    ck = read_checkpoint(p)
+    h = ck["header"]
+    assert h["family"] == "MULTISTEP" and (h["nexp"], h["nimp"], h["nold"]) == (3, 1, 3)
+    assert np.array_equal(h["dt"], header["dt"]) and h["time"] == 0.125 and h["rscheme"] == "cheb"
+    for k in ("us", "up", "temp"):
+        assert np.array_equal(ck[k], fields[k])
+    for k in ("hist_P", "hist_T"):
+        assert all(np.array_equal(a, b) for a, b in zip(ck[k], fields[k]))
