@@ -7,7 +7,11 @@ the hot path: the stage body of ``time_loop`` (src/step_time.f90:139-368) with
 streamfunction/vorticity system, both the coupled direct solve
 (src/update_psi_coll_smat.f90) and the influence-matrix solve
 (src/update_psi_coll_dmat.f90), with the multistep IMEX schemes of
-src/multistep_schemes.f90.
+src/multistep_schemes.f90 and the DIRK schemes of src/dirk_schemes.f90.
+With ``cheb_method="INTEG"`` the stage routines are those of the sparse
+Chebyshev-integration method with tau boundary rows and the direct
+streamfunction solve (src/update_temp_integ.f90,
+src/update_psi_integ_smat.f90), restated in oracle/pizza_integ.py.
 
 It is the checker for the CUDA library and nothing else: only ``tests/``,
 ``__graft_entry__.smoke()`` and the ``cpu_baseline`` / ``--impl reference``
@@ -15,7 +19,8 @@ legs of ``bench.py`` import it.  The product path never calls it.
 
 Parity pin: the oracle reproduces the reference's own regression fixtures
 (``samples/*/reference.out``: NonRotRa2e3, RotE1e3EkPump first run,
-MultistepSchemes first run, TimeStepChange) at the fixtures' rtol=1e-8, see
+MultistepSchemes first run, TimeStepChange, DIRKSchemes first run, RotInteg
+first run) at the fixtures' rtol=1e-8, atol=1e-20, see
 ``tests/test_oracle_golden.py``.  Third-party arithmetic the reference calls
 (FFTW3 r2c/c2r/dft, LAPACK dgetrf/dgetrs/zgetrf/zgetrs; not vendored, versions
 unpinned in src/CMakeLists.txt) is restated with numpy.fft (pocketfft) and
@@ -36,7 +41,7 @@ import scipy.linalg as sla
 
 __all__ = ["Params", "Pizza", "seeded_temperature", "l_correct_step"]
 
-TINY_NUMBER = 1.0e-20  # src/constants.f90 (tiny_number used by round_off)
+TINY_NUMBER = 10.0 * np.finfo(float).eps  # tiny_number, src/constants.f90:21 (used by round_off)
 
 
 # ---------------------------------------------------------------------------
@@ -56,6 +61,9 @@ class Params:
     dt_fac: float = 2.0
     time_scheme: str = "CNAB2"
     matrix_solve: str = "DIRECT"      # DIRECT -> smat, INFLUENCE -> dmat
+    cheb_method: str = "COLL"         # COLL -> collocation, INTEG -> sparse integration
+    l_rerror_fix: bool = False
+    rerror_fac: float = 500.0
     corio_term: str = "IMPLICIT"
     buo_term: str = "IMPLICIT"
     time_scale: str = "VISC"
@@ -97,6 +105,7 @@ class Params:
         d["r_cmb"] = 1.0 / (1.0 - self.radratio)
         d["r_icb"] = d["r_cmb"] - 1.0
         d["l_direct_solve"] = "DIRECT" in self.matrix_solve.upper()
+        d["l_cheb_coll"] = "COLL" in self.cheb_method.upper()   # namelists.f90:379-384
         l_cor_imp = "IMP" in self.corio_term.upper()
         if (not d["l_direct_solve"]) and l_cor_imp and (not l_non_rot):
             l_cor_imp = False  # namelists.f90:448-457
@@ -622,25 +631,33 @@ class Cheb:
         return df, ddf
 
     # -- real 1d derivatives via the Chebyshev recursion ---------------------
+    # round-off threshold of the real recursions (radial_derivatives.f90:51-66):
+    # rerror_fac * epsilon with l_rerror_fix, else 0
+    thr = 0.0
+
     def _dcheb(self, c):
-        """get_dcheb_real_1d (radial_derivatives.f90:143-185), thr=0."""
+        """get_dcheb_real_1d (radial_derivatives.f90:143-185): a coefficient
+        below the threshold zeroes that derivative coefficient."""
         N = self.N
+        t = np.max(np.abs(c)) * self.thr
         df = np.zeros(N)
-        df[N - 2] = (N - 1) * c[N - 1]
+        df[N - 2] = (N - 1) * c[N - 1] if abs(c[N - 1]) >= t else 0.0
         for n in range(N - 3, -1, -1):
-            df[n] = df[n + 2] + 2.0 * (n + 1) * c[n + 1]
+            df[n] = df[n + 2] + 2.0 * (n + 1) * c[n + 1] if abs(c[n + 1]) >= t else 0.0
         return df
 
     def _ddcheb(self, c):
-        """get_ddcheb_real_1d (radial_derivatives.f90:259-311), thr=0."""
+        """get_ddcheb_real_1d (radial_derivatives.f90:259-311): terms below the
+        threshold are skipped."""
         N = self.N
+        t = np.max(np.abs(c)) * self.thr
         df = np.zeros(N)
         ddf = np.zeros(N)
-        df[N - 2] = (N - 1) * c[N - 1]
+        df[N - 2] = (N - 1) * c[N - 1] if abs(c[N - 1]) >= t else 0.0
         for n in range(N - 3, -1, -1):
             fac = 2.0 * (n + 1)
-            df[n] = df[n + 2] + fac * c[n + 1]
-            ddf[n] = ddf[n + 2] + fac * df[n + 1]
+            df[n] = df[n + 2] + fac * c[n + 1] if abs(c[n + 1]) >= t else df[n + 2]
+            ddf[n] = ddf[n + 2] + fac * df[n + 1] if abs(df[n + 1]) >= t else ddf[n + 2]
         return df, ddf
 
     def get_dr_real(self, f, l_dct=True):
@@ -802,6 +819,16 @@ class Pizza:
         self.l_bridge_step = True
         self.l_AB1 = False
         self.rows = {"e_kin": [], "e_kin_3D": [], "heat": []}
+        if p.l_rerror_fix:
+            self.cheb.thr = p.rerror_fac * np.finfo(float).eps
+        self.l_integ = not d["l_cheb_coll"]
+        self.temp_hat = np.zeros(shp, complex)
+        self.psi_hat = np.zeros(shp, complex)
+        if self.l_integ:
+            if not self.l_direct:
+                raise NotImplementedError("integ with the influence-matrix solve is not restated")
+            from .pizza_integ import IntegScheme
+            self.integ = IntegScheme(self)
 
     # -- radial functions (src/radial.f90:115-282) ---------------------------
     def _radial(self):
@@ -873,6 +900,9 @@ class Pizza:
         work = c.get_dr(self.up)
         m = self.mvec[:, None]
         self.om = work + self.or1 * self.up - self.or1 * 1j * m * self.us
+        if self.l_integ:
+            self.integ.start()
+            return
         self._temp_rhs_imp(1, True, l_in_cheb=False)
         self._psi_rhs_imp(1, True, l_in_cheb=False)
 
@@ -900,13 +930,18 @@ class Pizza:
             for (kind, k), aP, aT in zip(order, ck["hist_P"], ck["hist_T"]):
                 getattr(self.dpsidt, kind)[k - 1] = np.array(aP, complex)
                 getattr(self.dTdt, kind)[k - 1] = np.array(aT, complex)
+        if self.l_integ:
+            self.psi = self.integ.psi_from_us()
         c = self.cheb
         self.dtemp = c.get_dr(self.temp)
         work = c.get_dr(self.up)
         m = self.mvec[:, None]
         self.om = work + self.or1 * self.up - self.or1 * 1j * m * self.us
-        self._temp_rhs_imp(1, True, l_in_cheb=False)
-        self._psi_rhs_imp(1, True, l_in_cheb=False)
+        if self.l_integ:
+            self.integ.start()
+        else:
+            self._temp_rhs_imp(1, True, l_in_cheb=False)
+            self._psi_rhs_imp(1, True, l_in_cheb=False)
         self.l_bridge_step = False
         self.l_AB1 = False
 
@@ -1018,6 +1053,8 @@ class Pizza:
 
     # -- explicit assembly (src/mloop.f90:169-229) ---------------------------
     def finish_explicit(self, dVsT, dVsOm):
+        if self.l_integ:
+            return self.integ.finish_explicit(dVsT, dVsOm)
         d = self.d
         c = self.cheb
         ist = self.ts.istage - 1
@@ -1203,6 +1240,10 @@ class Pizza:
         """All dt dependent LU factors, plus the dt independent dmat psi ones
         on first use (update_psi_coll_dmat.f90:94-98)."""
         M = self.M
+        if self.l_integ:
+            self.integ.build_matrices()
+            self._mats_built = True
+            return
         self.tmats = [self._temp_mat(int(self.mvec[i])) for i in range(M)]
         self.uphi = self._uphi_mat()
         if self.l_direct:
@@ -1270,6 +1311,8 @@ class Pizza:
     # -- implicit terms ------------------------------------------------------
     def _temp_rhs_imp(self, istage, l_calc_lin, l_in_cheb):
         """get_temp_rhs_imp_coll (update_temp_coll.f90:178-236)."""
+        if self.l_integ:
+            return self.integ.temp_rhs_imp(istage, l_calc_lin)
         c, d = self.cheb, self.d
         if l_calc_lin:
             self.dtemp, work = c.get_ddr(self.temp, l_dct=not l_in_cheb)
@@ -1288,6 +1331,8 @@ class Pizza:
     def _psi_rhs_imp(self, istage, l_calc_lin, l_in_cheb):
         """get_psi_rhs_imp_coll_{dmat,smat} (update_psi_coll_dmat.f90:554-682,
         update_psi_coll_smat.f90:380-527)."""
+        if self.l_integ:
+            return self.integ.psi_rhs_imp(istage, l_calc_lin)
         c, d = self.cheb, self.d
         om0 = self.om[0].real.copy()
         if l_calc_lin:
@@ -1323,6 +1368,8 @@ class Pizza:
     # -- solves (mloop) ------------------------------------------------------
     def update_temp(self, lMat, l_log_next):
         """update_temp_co (update_temp_coll.f90:66-150)."""
+        if self.l_integ:
+            return self.integ.update_temp(l_log_next)
         N, M, n_max = self.N, self.M, self.n_max
         ts = self.ts
         work = ts.set_imex_rhs(self.dTdt)
@@ -1348,6 +1395,8 @@ class Pizza:
     def update_om(self):
         """update_om_coll_dmat (update_psi_coll_dmat.f90:126-466) or
         update_om_coll_smat (update_psi_coll_smat.f90:88-321)."""
+        if self.l_integ:
+            return self.integ.update_psi()
         c, d = self.cheb, self.d
         N, M, n_max = self.N, self.M, self.n_max
         ts = self.ts

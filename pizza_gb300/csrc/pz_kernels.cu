@@ -1261,7 +1261,9 @@ __global__ void __launch_bounds__(256) k_assemble(PzDev d) {
 // ---------------------------------------------------------------------------
 // k_obs: time series of one instance (src/outputs.f90:418-830)
 // ---------------------------------------------------------------------------
-__device__ __forceinline__ double round_off(double x) { return fabs(x) < 1.0e-20 ? 0.0 : x; }
+// round_off (src/useful.f90:222-233) with tiny_number = 10 epsilon(1.0_cp)
+// (src/constants.f90:21)
+__device__ __forceinline__ double round_off(double x) { return fabs(x) < 10.0 * 2.220446049250313e-16 ? 0.0 : x; }
 
 __global__ void k_obs(PzDev d, int only) {
   const int inst = blockIdx.x;

@@ -12,6 +12,7 @@ first run starts from the namelist and needs no checkpoint):
   MultistepSchemes  rows 0-200    (e_kin_3D, coll smat SBDF3 + CNAB2 bridge)
   TimeStepChange    all 21 rows   (e_kin, coll dmat SBDF3, CFL dt changes)
   DIRKSchemes       rows 0-10     (e_kin_3D, coll smat ARS222, a DIRK scheme)
+  RotInteg          rows 0-200    (e_kin_3D, integ smat CNAB2, tau boundary rows)
 """
 import argparse
 import json
@@ -46,6 +47,13 @@ CASES = {
                     time_scheme="ARS222", courfac=1.0, ra=6.0e4, pr=1.0, ek=1.0e-3,
                     radratio=0.35, g0=0.0, g1=1.0, g2=0.0, l_ek_pump=False, init_t=4,
                     amp_t=2.5e-4, n_log_step=10)),
+    "RotInteg": dict(
+        rows=201, series="e_kin_3D",
+        params=dict(n_r_max=49, n_cheb_max=32, m_max=32, n_time_steps=4000, dtMax=1e-1,
+                    cheb_method="INTEG", matrix_solve="DIRECT", l_rerror_fix=True, rerror_fac=5e2,
+                    courfac=4.0, time_scale="ROT", ra=5.0e4, pr=1.0, ek=1.0e-3, radratio=0.35,
+                    g0=0.0, g1=1.0, g2=0.0, ktopv=2, kbotv=2, l_ek_pump=False, init_t=-1,
+                    amp_t=1.0e-2, n_log_step=20)),
 }
 
 
