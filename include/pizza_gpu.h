@@ -68,6 +68,15 @@ extern "C" {
 #define PZ_SOLVE_INFLUENCE 0   /* update_psi_coll_dmat: real om/psi solves + 2x2 influence matrix */
 #define PZ_SOLVE_DIRECT    1   /* update_psi_coll_smat: coupled 2N complex solve */
 
+/* cheb_method values (src/namelists.f90:379-384) */
+#define PZ_CHEB_COLL  0   /* collocation (update_*_coll)                            */
+#define PZ_CHEB_INTEG 1   /* sparse Chebyshev integration with tau rows
+                             (update_temp_integ, update_psi_integ_smat)             */
+
+/* time_scale values (src/namelists.f90:472-510) */
+#define PZ_TS_VISC 0      /* viscous time unit (default)                            */
+#define PZ_TS_ROT  1      /* rotation time unit: CorFac = 2, ViscFac = ek           */
+
 /*
  * One instance's namelist values.  Mirrors pizza's input.nml groups &grid,
  * &control, &phys_param (src/namelists.f90:162-189).  Fields not listed take
@@ -95,6 +104,11 @@ typedef struct pz_config {
   double courfac;      /* >= 1e3 selects the scheme's default CFL factor    */
   double alpha;        /* Crank-Nicolson weight (0.5)                       */
   double dt_fac;       /* CFL hysteresis factor (2)                         */
+  int    cheb_method;  /* PZ_CHEB_COLL / PZ_CHEB_INTEG                      */
+  int    time_scale;   /* PZ_TS_VISC / PZ_TS_ROT                            */
+  int    l_rerror_fix; /* round-off threshold in the real m = 0 Chebyshev
+                          derivative recursions (radial_derivatives.f90)   */
+  double rerror_fac;   /* threshold = rerror_fac * epsilon (500)            */
 } pz_config;
 
 typedef struct pz_handle pz_handle;
@@ -186,7 +200,7 @@ void* pz_stream(pz_handle* h);
  * events between them on the handle's stream; kernel_ms[k] receives the mean
  * device time per step of kernel kind k (k < PZ_KERNEL_KINDS, summed over the
  * stages of a DIRK step), names in pz_kernel_name(k).  Synchronises. */
-#define PZ_KERNEL_KINDS 6
+#define PZ_KERNEL_KINDS 7
 int pz_step_profile(pz_handle* h, int n_steps, double* kernel_ms);
 const char* pz_kernel_name(int k);
 
@@ -262,6 +276,18 @@ int pz_adjoint_backward(pz_handle* h, double* dJ_dtemp, double* dJ_dra);
 /* Change Ra of one instance (BuoFac = Ra/Pr); the operators do not depend on
  * it.  Used for finite-difference checks of dJ/dRa. */
 int pz_set_ra(pz_handle* h, int inst, double ra);
+
+/* No counterpart in the reference (its stencils are closed-form functions of
+ * src/chebsparselib.f90).  One banded operator of the integration method,
+ * as pz_create derives it for a grid (host only, no device needed):
+ * `which` in 0..PZ_INTEG_OPS-1 selects I2[r f], I2[r^2 f], I2[f],
+ * I2[r^2 f'' + r f'], I2[r^2 f'' + r f' - f], I4[r^3 f], I4[r^4 f], then
+ * Q0, Q1 (intcheb4rmult4laplrot = Q0 + m^2 Q1) and S0, S1, S2
+ * (intcheb4rmult4laplrot2 = S0 + m^2 S1 + m^4 S2); all times rnorm with the
+ * tau rows zero.  out: n_r_max^2 doubles, column-major; *bandwidth: max |i-j|
+ * of a nonzero entry. */
+#define PZ_INTEG_OPS 12
+int pz_integ_operator(int n_r_max, double radratio, int which, double* out, int* bandwidth);
 
 int pz_destroy(pz_handle* h);
 

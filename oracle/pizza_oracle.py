@@ -1496,6 +1496,9 @@ class Pizza:
         """assemble_stage (mloop.f90): assemble_temp_coll
         (update_temp_coll.f90:238-307) and assemble_psi_coll_{smat,dmat}
         (update_psi_coll_smat.f90:529-672)."""
+        if self.l_integ:
+            # mloop.f90:162-164: abortRun for the integration method
+            raise NotImplementedError("Assembly stage with integration method not implemented")
         c, ts = self.cheb, self.ts
         N, M, n_max = self.N, self.M, self.n_max
         m = self.mvec

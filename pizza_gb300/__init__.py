@@ -29,8 +29,10 @@ SCHEMES = {"CNAB2": 0, "SBDF2": 1, "BDF2AB2": 1, "SBDF3": 2, "BDF3AB3": 2, "SBDF
            "ARS222": 10, "ARS232": 11, "ARS233": 12, "SSP222": 13, "LSDIRK222": 14, "LZ232": 15,
            "CK232": 16, "ARS443": 17, "BPR353": 18, "PC2": 19, "ARS343": 20, "MARS343": 21,
            "SSP322": 22, "SSP332": 23}
-KERNEL_KINDS = 6
+KERNEL_KINDS = 7
 SOLVE_INFLUENCE, SOLVE_DIRECT = 0, 1
+CHEB_COLL, CHEB_INTEG = 0, 1
+TS_VISC, TS_ROT = 0, 1
 SERIES_COLS = 16
 SERIES_NAMES = ("time", "us2_2D", "up2_2D", "up2_axi_2D", "us2_3D", "up2_3D", "uz2_3D",
                 "up2_axi_3D", "NuTop", "NuBot", "Nu_vol", "Nu_int", "tTop", "tBot", "beta_t", "dt")
@@ -57,14 +59,17 @@ class _CConfig(ctypes.Structure):
                 ("l_ek_pump", ctypes.c_int), ("l_non_rot", ctypes.c_int), ("l_temp_advz", ctypes.c_int),
                 ("time_scheme", ctypes.c_int), ("matrix_solve", ctypes.c_int), ("corio_imp", ctypes.c_int),
                 ("buo_imp", ctypes.c_int), ("dtMax", ctypes.c_double), ("courfac", ctypes.c_double),
-                ("alpha", ctypes.c_double), ("dt_fac", ctypes.c_double)]
+                ("alpha", ctypes.c_double), ("dt_fac", ctypes.c_double), ("cheb_method", ctypes.c_int),
+                ("time_scale", ctypes.c_int), ("l_rerror_fix", ctypes.c_int), ("rerror_fac", ctypes.c_double)]
 
 
 @dataclasses.dataclass
 class Config:
     """One instance's namelist values (defaults: src/namelists.f90:530-672).
     matrix_solve 'DIRECT' is pizza's coupled smat solve, 'INFLUENCE' the dmat
-    influence-matrix solve (the one the adjoint covers)."""
+    influence-matrix solve (the one the adjoint covers).  cheb_method 'COLL'
+    is the collocation method, 'INTEG' the sparse Chebyshev integration
+    method with tau boundary rows (direct solve, rotating runs)."""
     n_r_max: int = 32
     n_cheb_max: int | None = None
     m_max: int = 32
@@ -91,6 +96,10 @@ class Config:
     courfac: float = 1.0e3
     alpha: float = 0.5
     dt_fac: float = 2.0
+    cheb_method: str = "COLL"
+    time_scale: str = "VISC"
+    l_rerror_fix: bool = False
+    rerror_fac: float = 500.0
 
     def to_c(self) -> _CConfig:
         c = _CConfig()
@@ -108,6 +117,10 @@ class Config:
         c.matrix_solve = SOLVE_DIRECT if "DIRECT" in self.matrix_solve.upper() else SOLVE_INFLUENCE
         c.corio_imp = int("IMP" in self.corio_term.upper())
         c.buo_imp = int("IMP" in self.buo_term.upper())
+        c.cheb_method = CHEB_COLL if "COLL" in self.cheb_method.upper() else CHEB_INTEG
+        c.time_scale = TS_ROT if "ROT" in self.time_scale.upper() else TS_VISC
+        c.l_rerror_fix = int(bool(self.l_rerror_fix))
+        c.rerror_fac = float(self.rerror_fac)
         return c
 
     @property
@@ -159,6 +172,7 @@ def load_library(path: str | None = None):
     lib.pz_set_history.argtypes = [vp, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, dp]
     lib.pz_get_step_state.argtypes = [vp, ctypes.c_int, dp, dp, ctypes.POINTER(ctypes.c_int)]
     lib.pz_set_step_state.argtypes = [vp, ctypes.c_int, ctypes.c_double, dp, ctypes.c_int]
+    lib.pz_integ_operator.argtypes = [ctypes.c_int, ctypes.c_double, ctypes.c_int, dp, ctypes.POINTER(ctypes.c_int)]
     lib.pz_destroy.argtypes = [ctypes.c_void_p]
     lib.pz_last_error.argtypes = [ctypes.c_void_p]
     lib.pz_last_error.restype = ctypes.c_char_p
@@ -166,10 +180,25 @@ def load_library(path: str | None = None):
               "pz_get_series", "pz_get_dims", "pz_launches_per_step", "pz_latest_rows",
               "pz_step_profile", "pz_explicit_terms", "pz_explicit_terms_noalloc", "pz_adjoint_forward",
               "pz_adjoint_backward", "pz_set_ra", "pz_get_history", "pz_set_history", "pz_get_step_state",
-              "pz_set_step_state", "pz_destroy"):
+              "pz_set_step_state", "pz_integ_operator", "pz_destroy"):
         getattr(lib, f).restype = ctypes.c_int
     _lib = lib
     return lib
+
+
+INTEG_OPERATORS = ("I2R1", "I2R2", "I2", "LT0", "ULAP", "I4R3", "I4R4", "Q0", "Q1", "S0", "S1", "S2")
+
+
+def integ_operator(n_r_max: int, radratio: float, name: str):
+    """One banded operator of the integration method as the library derives
+    it (host code, no GPU needed): (n_r_max, n_r_max) array and bandwidth."""
+    lib = load_library()
+    out = np.zeros(n_r_max * n_r_max)
+    bw = ctypes.c_int(0)
+    rc = lib.pz_integ_operator(n_r_max, float(radratio), INTEG_OPERATORS.index(name), _dptr(out), ctypes.byref(bw))
+    if rc != 0:
+        raise RuntimeError(lib.pz_last_error(None).decode())
+    return out.reshape(n_r_max, n_r_max, order="F"), bw.value
 
 
 def _dptr(a):

@@ -379,8 +379,21 @@ int validate(const pz_config& c, std::string* why) {
   if (c.ktopt != 1 || c.kbott != 1) return uns("only fixed-temperature boundaries (ktopt = kbott = 1)");
   if (c.ktopv != 2 || c.kbotv != 2) return uns("only rigid boundaries (ktopv = kbotv = 2)");
   if (c.matrix_solve != PZ_SOLVE_INFLUENCE && c.matrix_solve != PZ_SOLVE_DIRECT) return bad("unknown matrix_solve");
-  if (c.matrix_solve == PZ_SOLVE_DIRECT && pz_build_smem_bytes(c.n_r_max, true) > PZ_SMEM_MAX)
+  if (c.cheb_method != PZ_CHEB_COLL && c.cheb_method != PZ_CHEB_INTEG) return bad("unknown cheb_method");
+  if (c.time_scale != PZ_TS_VISC && c.time_scale != PZ_TS_ROT) return bad("unknown time_scale");
+  if (c.l_rerror_fix && !(c.rerror_fac > 0.0)) return bad("rerror_fac must be > 0");
+  if (c.cheb_method == PZ_CHEB_INTEG) {
+    if (c.matrix_solve != PZ_SOLVE_DIRECT)
+      return uns("cheb_method 'integ' is implemented with matrix_solve 'DIRECT' (update_psi_integ_smat)");
+    if (c.l_non_rot || c.ek < 0.0) return uns("cheb_method 'integ' is implemented for rotating runs");
+    if (pz_build_smem_bytes(c.n_r_max, true, true) > PZ_SMEM_MAX)
+      return uns("cheb_method 'integ' needs n_r_max <= 118 (the operator build is staged in shared memory)");
+    DirkTab t;
+    if (dirk_tableau(c.time_scheme, &t) && t.assembly)
+      return uns("cheb_method 'integ' has no assembly stage (mloop.f90:162-164 aborts)");
+  } else if (c.matrix_solve == PZ_SOLVE_DIRECT && pz_build_smem_bytes(c.n_r_max, true, false) > PZ_SMEM_MAX) {
     return uns("matrix_solve DIRECT needs n_r_max <= 97 (the coupled operator build is staged in shared memory)");
+  }
   if (c.dtMax <= 0.0) return bad("dtMax must be > 0");
   if (c.alpha <= 0.0 || c.alpha > 1.0) return bad("alpha must be in (0, 1]");
   if (c.dt_fac <= 1.0) return bad("dt_fac must be > 1");
@@ -408,6 +421,8 @@ extern "C" void pz_config_default(pz_config* c) {
   c->time_scheme = PZ_CNAB2; c->matrix_solve = PZ_SOLVE_DIRECT;
   c->corio_imp = 1; c->buo_imp = 1;
   c->dtMax = 1.0e-5; c->courfac = 1.0e3; c->alpha = 0.5; c->dt_fac = 2.0;
+  c->cheb_method = PZ_CHEB_COLL; c->time_scale = PZ_TS_VISC;
+  c->l_rerror_fix = 0; c->rerror_fac = 500.0;
 }
 
 extern "C" int pz_create(const pz_config* cfgs, int n, pz_handle** out) {
@@ -428,6 +443,9 @@ extern "C" int pz_create(const pz_config* cfgs, int n, pz_handle** out) {
   std::map<int, long long> basis_off;    // by N
   std::map<int, Basis> bases;
   std::map<int, long long> tw_off;       // by P
+  struct IntegBlock { std::vector<double> ops; int band[IM_COUNT]; };
+  std::map<std::pair<int, double>, long long> integ_off;   // by (N, radratio)
+  std::map<std::pair<int, double>, IntegBlock> integ_blocks;
   std::vector<std::vector<double>> rad(n);
   int maxN = 0, maxP = 0, maxM = 0;
   for (int i = 0; i < n; ++i) {
@@ -463,7 +481,9 @@ extern "C" int pz_create(const pz_config* cfgs, int n, pz_handle** out) {
     I.dtMax = c.dtMax; I.dtMin = c.dtMax / 1.0e6;   // pre_calculations.f90:33
     I.dt_fac = c.dt_fac;
     if (non_rot) { I.CorFac = 0.0; I.BuoFac = c.ra / c.pr; I.TdiffFac = 1.0 / c.pr; I.ViscFac = 1.0; }
-    else { I.CorFac = 2.0 / ek; I.BuoFac = c.ra / c.pr; I.TdiffFac = 1.0 / c.pr; I.ViscFac = 1.0; }
+    else if (c.time_scale == PZ_TS_ROT) {   // namelists.f90:491-500
+      I.CorFac = 2.0; I.BuoFac = c.ra * ek * ek / c.pr; I.TdiffFac = ek / c.pr; I.ViscFac = ek;
+    } else { I.CorFac = 2.0 / ek; I.BuoFac = c.ra / c.pr; I.TdiffFac = 1.0 / c.pr; I.ViscFac = 1.0; }
     I.flags = 0;
     if (c.buo_imp) I.flags |= PZF_BUO_IMP;
     if (c.l_ek_pump) I.flags |= PZF_EK_PUMP;
@@ -477,6 +497,11 @@ extern "C" int pz_create(const pz_config* cfgs, int n, pz_handle** out) {
     // update_psi_coll_dmat.f90:829-911) build the same rows when
     // TdiffFac*hdif_T == ViscFac*hdif_V and both use fixed/no-slip boundary rows
     if (!direct && I.TdiffFac == I.ViscFac) I.flags |= PZF_T_IS_OM;
+    if (c.cheb_method == PZ_CHEB_INTEG) I.flags |= PZF_INTEG;
+    if (c.l_rerror_fix) {   // radial_derivatives.f90:51-66
+      I.flags |= PZF_RERR;
+      I.rerr_thr = c.rerror_fac * 2.220446049250313e-16;
+    }
     const int N = I.N;
     I.rnorm = std::sqrt(2.0 / (double)(N - 1));
     I.r_cmb = 1.0 / (1.0 - c.radratio);
@@ -486,6 +511,17 @@ extern "C" int pz_create(const pz_config* cfgs, int n, pz_handle** out) {
       basis_off[N] = take((long long)BM_COUNT * N * N);
     }
     I.o_basis = basis_off[N];
+    if (I.flags & PZF_INTEG) {
+      // integration-method operators, shared by equal (N, radratio)
+      const std::pair<int, double> key(N, c.radratio);
+      if (!integ_off.count(key)) {
+        IntegBlock& ib = integ_blocks[key];
+        pz_integ_operators(N, I.r_icb, I.r_cmb, I.rnorm, ib.ops, ib.band);
+        integ_off[key] = take((long long)IM_COUNT * N * N);
+      }
+      I.o_integ = integ_off[key];
+      std::memcpy(I.im_band, integ_blocks[key].band, sizeof(I.im_band));
+    }
     if (!tw_off.count(I.P)) tw_off[I.P] = take(2LL * I.P);
     I.o_tw = tw_off[I.P];
     // radial functions (radial.f90:115-282)
@@ -583,7 +619,10 @@ extern "C" int pz_create(const pz_config* cfgs, int n, pz_handle** out) {
     const long long N = I.N, M = I.M;
     I.o_gt = take(M * N * N);
     I.o_guphi = take(N * N);
-    if (I.flags & PZF_DIRECT) {
+    if (I.flags & PZF_INTEG) {
+      I.o_gsm = take(2 * M * N * N);      // complex N x N streamfunction inverse per m
+      I.o_gom = I.o_gpsi = I.o_aux = 0;
+    } else if (I.flags & PZF_DIRECT) {
       I.o_gsm = take(4 * M * N * N);
       I.o_gom = I.o_gpsi = I.o_aux = 0;   // influence-matrix operators unused
     } else {
@@ -616,6 +655,7 @@ extern "C" int pz_create(const pz_config* cfgs, int n, pz_handle** out) {
     long long hi = 0;
     for (auto& kv : basis_off) hi = std::max(hi, kv.second + (long long)BM_COUNT * kv.first * kv.first);
     for (auto& kv : tw_off) hi = std::max(hi, kv.second + 2LL * kv.first);
+    for (auto& kv : integ_off) hi = std::max(hi, kv.second + (long long)IM_COUNT * kv.first.first * kv.first.first);
     for (int i = 0; i < n; ++i) hi = std::max(hi, h->inst[i].o_rad + (long long)RV_COUNT * h->inst[i].N);
     for (int i = 0; i < n; ++i)
       if (h->inst[i].dirk) hi = std::max(hi, h->inst[i].o_bt + (long long)PZ_BT_SIZE);
@@ -654,6 +694,10 @@ extern "C" int pz_create(const pz_config* cfgs, int n, pz_handle** out) {
       }
     }
     for (int i = 0; i < n; ++i) std::memcpy(img.data() + h->inst[i].o_rad, rad[i].data(), rad[i].size() * sizeof(double));
+    for (auto& kv : integ_off) {
+      const std::vector<double>& ops = integ_blocks[kv.first].ops;
+      std::memcpy(img.data() + kv.second, ops.data(), ops.size() * sizeof(double));
+    }
   }
   if ((e = cudaMemsetAsync(h->pool, 0, (size_t)off * sizeof(double), h->stream)) ||
       (e = cudaMemcpyAsync(h->pool, img.data(), img.size() * sizeof(double), cudaMemcpyHostToDevice, h->stream))) {
@@ -693,15 +737,19 @@ extern "C" int pz_create(const pz_config* cfgs, int n, pz_handle** out) {
   h->dev.maxN = maxN; h->dev.maxP = maxP; h->dev.maxM = maxM;
   size_t sb = 0;
   for (int i = 0; i < n; ++i)
-    sb = std::max(sb, pz_build_smem_bytes(h->inst[i].N, (h->inst[i].flags & PZF_DIRECT) != 0));
+    sb = std::max(sb, pz_build_smem_bytes(h->inst[i].N, (h->inst[i].flags & PZF_DIRECT) != 0,
+                                          (h->inst[i].flags & PZF_INTEG) != 0));
   h->dev.smem_build = (int)sb;
   // launch plan of one step: per stage k_rloop [k_cfl, k_build] k_mloop, then
   // the assembly stage and the time series (step_time.f90:139-406)
   int smax = 1;
-  bool any_assembly = false;
+  bool any_assembly = false, any_integ = false, any_coll = false;
   for (int i = 0; i < n; ++i) {
     smax = std::max(smax, h->inst[i].nstages);
     any_assembly |= h->inst[i].assembly != 0;
+    const bool integ = (h->inst[i].flags & PZF_INTEG) != 0;
+    any_integ |= integ;
+    any_coll |= !integ;
   }
   h->plan.clear();
   for (int st = 1; st <= smax; ++st) {
@@ -710,7 +758,8 @@ extern "C" int pz_create(const pz_config* cfgs, int n, pz_handle** out) {
       h->plan.push_back({PZK_CFL, 1});
       h->plan.push_back({PZK_BUILD, 1});
     }
-    h->plan.push_back({PZK_MLOOP, st});
+    if (any_coll) h->plan.push_back({PZK_MLOOP, st});
+    if (any_integ) h->plan.push_back({PZK_MLOOP_INTEG, st});
   }
   if (any_assembly) h->plan.push_back({PZK_ASSEMBLE, 0});
   h->plan.push_back({PZK_OBS, 0});
@@ -1045,6 +1094,21 @@ extern "C" int pz_step_profile(pz_handle* h, int n_steps, double* kernel_ms) {
 
 extern "C" const char* pz_kernel_name(int k) { return pz_step_kernel_name(k); }
 
+extern "C" int pz_integ_operator(int n_r_max, double radratio, int which, double* out, int* bandwidth) {
+  static_assert(PZ_INTEG_OPS == IM_COUNT, "operator count");
+  if (n_r_max < 5 || n_r_max > 1024 || !(radratio > 0.0 && radratio < 1.0) || which < 0 || which >= IM_COUNT ||
+      !out || !bandwidth)
+    return fail(nullptr, PZ_E_ARG, "pz_integ_operator: bad arguments");
+  const double r_cmb = 1.0 / (1.0 - radratio), r_icb = r_cmb - 1.0;
+  std::vector<double> ops;
+  int band[IM_COUNT];
+  pz_integ_operators(n_r_max, r_icb, r_cmb, std::sqrt(2.0 / (double)(n_r_max - 1)), ops, band);
+  const size_t nn = (size_t)n_r_max * n_r_max;
+  std::memcpy(out, ops.data() + (size_t)which * nn, nn * sizeof(double));
+  *bandwidth = band[which];
+  return PZ_OK;
+}
+
 extern "C" int pz_explicit_terms(pz_handle* h, int inst, const double* us, const double* up, const double* om,
                                  const double* temp, double* dTdt_expl, double* dpsidt_expl, double* dtr,
                                  double* dth) {
@@ -1085,6 +1149,8 @@ int pz_expl_args(pz_handle* h, int inst, const double* us, const double* up, con
   if (!us || !up || !om || !temp || !dTdt_expl || !dpsidt_expl || !dtr || !dth)
     return fail(h, PZ_E_ARG, "null array");
   const PzInst& I = h->inst[inst];
+  if (I.flags & PZF_INTEG)
+    return fail(h, PZ_E_UNSUPPORTED, "explicit terms entry point: collocation instances only (cheb_method 'integ')");
   a->inst = h->d_inst + inst;
   a->pool = h->pool;
   a->us = reinterpret_cast<const double2*>(us);

@@ -1,0 +1,508 @@
+// Chebyshev integration method ("integ", tau boundary rows, direct solve):
+// the per-m device code of update_temp_int (src/update_temp_integ.f90) and
+// update_psi_int_smat (src/update_psi_integ_smat.f90).  Included by
+// pz_kernels.cu after the collocation helpers it reuses (View, MS, op_*,
+// mv_lanes, imex_rhs, dirk_rhs, gj_invert, gj_invert_c, store_op).
+//
+// Unknowns are Chebyshev coefficients: T_hat per m, psi_hat per m /= 0 and
+// the m = 0 azimuthal velocity's coefficients.  The equations are multiplied
+// by r^2 (temperature, u_phi) or r^4 (streamfunction) and integrated twice
+// (four times) in r, which makes every operator except the tau rows banded:
+// the banded operators (IM_*) are applied with band_mv over their band
+// only, the dt dependent left-hand sides are inverted per m in k_build and
+// applied as dense products, like the collocation path.
+#pragma once
+
+// -- banded products ---------------------------------------------------------
+// y_i = sum_{|j-i|<=bw} (sum_k c_k A_k(i,j)) x_j, A_k column-major n x n;
+// one thread per row.
+struct Band3 {
+  const double* A[3];
+  double c[3];
+  int na, bw;
+};
+__device__ __forceinline__ void band_mv(const Band3& B, int n, const double2* __restrict__ x,
+                                        double2* __restrict__ y) {
+  for (int i = threadIdx.x; i < n; i += blockDim.x) {
+    const int j0 = max(0, i - B.bw), j1 = min(n - 1, i + B.bw);
+    double re = 0.0, im = 0.0;
+    for (int j = j0; j <= j1; ++j) {
+      double a = 0.0;
+      for (int k = 0; k < B.na; ++k) a = fma(B.c[k], __ldg(B.A[k] + i + (long long)j * n), a);
+      re = fma(a, x[j].x, re);
+      im = fma(a, x[j].y, im);
+    }
+    y[i] = make_double2(re, im);
+  }
+}
+
+__device__ __forceinline__ const double* im_op(const View& V, int k) {
+  return V.pool + V.I->o_integ + (long long)k * V.I->N * V.I->N;
+}
+__device__ __forceinline__ Band3 band1(const View& V, int k, double c = 1.0) {
+  Band3 b;
+  b.A[0] = im_op(V, k); b.c[0] = c; b.na = 1; b.bw = V.I->im_band[k];
+  b.A[1] = b.A[2] = nullptr; b.c[1] = b.c[2] = 0.0;
+  return b;
+}
+// intcheb2rmult2lapl(m) = LT0 - m^2 I2, times f
+__device__ __forceinline__ Band3 band_tlap(const View& V, double dm2, double f) {
+  Band3 b;
+  b.A[0] = im_op(V, IM_LT0); b.c[0] = f;
+  b.A[1] = im_op(V, IM_I2); b.c[1] = -dm2 * f;
+  b.A[2] = nullptr; b.c[2] = 0.0;
+  b.na = 2; b.bw = max(V.I->im_band[IM_LT0], V.I->im_band[IM_I2]);
+  return b;
+}
+// intcheb4rmult4laplrot(m) = Q0 + m^2 Q1
+__device__ __forceinline__ Band3 band_rot(const View& V, double dm2) {
+  Band3 b;
+  b.A[0] = im_op(V, IM_Q0); b.c[0] = 1.0;
+  b.A[1] = im_op(V, IM_Q1); b.c[1] = dm2;
+  b.A[2] = nullptr; b.c[2] = 0.0;
+  b.na = 2; b.bw = max(V.I->im_band[IM_Q0], V.I->im_band[IM_Q1]);
+  return b;
+}
+// f * intcheb4rmult4laplrot2(m) = f (S0 + m^2 S1 + m^4 S2)
+__device__ __forceinline__ Band3 band_rot2(const View& V, double dm2, double f) {
+  Band3 b;
+  b.A[0] = im_op(V, IM_S0); b.c[0] = f;
+  b.A[1] = im_op(V, IM_S1); b.c[1] = f * dm2;
+  b.A[2] = im_op(V, IM_S2); b.c[2] = f * dm2 * dm2;
+  b.na = 3; b.bw = max(V.I->im_band[IM_S0], max(V.I->im_band[IM_S1], V.I->im_band[IM_S2]));
+  return b;
+}
+
+// y = G x, G complex n x n column-major (the integ streamfunction inverse)
+struct CDenseDotN {
+  const double2* __restrict__ G; int n; const double* __restrict__ x; double* __restrict__ y;
+  __device__ __forceinline__ double fma(int t, int j, double acc) const {
+    const double2 g = __ldg(G + (t >> 1) + (long long)j * n);
+    const double xr = x[2 * j], xi = x[2 * j + 1];
+    return (t & 1) ? ::fma(g.x, xi, ::fma(g.y, xr, acc)) : ::fma(g.x, xr, ::fma(-g.y, xi, acc));
+  }
+  __device__ __forceinline__ void store(int t, double v) const { y[t] = v; }
+};
+__device__ __forceinline__ void cmvn_lanes(const double2* __restrict__ G, int n, const double2* __restrict__ x,
+                                           double2* __restrict__ y) {
+  lane_dots(CDenseDotN{G, n, reinterpret_cast<const double*>(x), reinterpret_cast<double*>(y)}, 2 * n, n);
+}
+
+// -- m = 0 derivative with the round-off threshold ---------------------------
+// get_dcheb_real_1d (src/radial_derivatives.f90:143-185) on the real parts of
+// the Chebyshev coefficients c: with thr > 0, a coefficient below
+// thr*max|c| zeroes the derivative coefficient it feeds.  Output: derivative
+// coefficients in df (imaginary parts zero).  One thread; the block syncs.
+__device__ void dcheb_thr(const double2* c, double2* df, int n, double thr) {
+  if (threadIdx.x == 0) {
+    double mx = 0.0;
+    for (int i = 0; i < n; ++i) mx = fmax(mx, fabs(c[i].x));
+    const double t = mx * thr;
+    df[n - 1] = make_double2(0.0, 0.0);
+    df[n - 2] = make_double2(fabs(c[n - 1].x) >= t ? (double)(n - 1) * c[n - 1].x : 0.0, 0.0);
+    for (int k = n - 3; k >= 0; --k)
+      df[k] = make_double2(fabs(c[k + 1].x) >= t ? df[k + 2].x + 2.0 * (k + 1) * c[k + 1].x : 0.0, 0.0);
+  }
+  __syncthreads();
+}
+// get_ddcheb_real_1d (src/radial_derivatives.f90:259-311): terms below the
+// threshold are skipped.
+__device__ void ddcheb_thr(const double2* c, double2* df, double2* ddf, int n, double thr) {
+  if (threadIdx.x == 0) {
+    double mx = 0.0;
+    for (int i = 0; i < n; ++i) mx = fmax(mx, fabs(c[i].x));
+    const double t = mx * thr;
+    df[n - 1] = ddf[n - 1] = ddf[n - 2] = make_double2(0.0, 0.0);
+    df[n - 2] = make_double2(fabs(c[n - 1].x) >= t ? (double)(n - 1) * c[n - 1].x : 0.0, 0.0);
+    for (int k = n - 3; k >= 0; --k) {
+      const double fac = 2.0 * (k + 1);
+      const double d = fabs(c[k + 1].x) >= t ? df[k + 2].x + fac * c[k + 1].x : df[k + 2].x;
+      df[k] = make_double2(d, 0.0);
+      ddf[k] = make_double2(fabs(df[k + 1].x) >= t ? ddf[k + 2].x + fac * df[k + 1].x : ddf[k + 2].x, 0.0);
+    }
+  }
+  __syncthreads();
+}
+
+// -- dt dependent left-hand sides (get_lhs_mat_tau) ----------------------------
+// k_build for one m of an integ instance: the temperature operator
+// (update_temp_integ.f90:631-776), the m = 0 u_phi operator or the m /= 0
+// streamfunction operator (update_psi_integ_smat.f90:1286-1581), each with its
+// tau rows (boundary_fac on column 0) and the row preconditioning
+// 1/max|row|, inverted by Gauss-Jordan and stored as G = A_s^-1 diag(fac) so
+// that x = G rhs.  Unlike the collocation builders nothing is truncated: the
+// integration method keeps all n_r_max coefficients of the solution.
+// Shared memory: see pz_build_smem_bytes (integ).
+__device__ int integ_build(const PzDev& d, const PzInst& I, const View& V, int mi, double wlin) {
+  extern __shared__ double shb[];
+  const int n = I.N, m = mi * I.minc;
+  const double dm = (double)m, dm2 = dm * dm, rn = I.rnorm;
+  double* A = shb;
+  double2* Ac = reinterpret_cast<double2*>(shb);
+  double* f1 = shb + 2LL * n * n;
+  double* colk = f1 + ((n + 1) & ~1);          // even offset: read as double2 by gj_invert_c
+  double* red = colk + 2 * n;
+  int* redi = reinterpret_cast<int*>(red + 32);
+  int* piv = redi + 32;
+  const double* I2R2 = im_op(V, IM_I2R2);
+  for (int pass = 0; pass < 2; ++pass) {
+    // pass 0: temperature; pass 1: u_phi (m = 0) -- the m /= 0 streamfunction
+    // operator is complex and built below
+    if (pass == 1 && m != 0) break;
+    const double* L0 = im_op(V, pass == 0 ? IM_LT0 : IM_ULAP);
+    const double* L1 = im_op(V, IM_I2);
+    const double c0 = wlin * (pass == 0 ? I.TdiffFac : I.ViscFac);
+    const double c1 = pass == 0 ? -dm2 * c0 : 0.0;
+    for (int idx = threadIdx.x; idx < n * n; idx += blockDim.x) {
+      const int i = idx / n, j = idx - i * n;
+      double v;
+      if (i < 2) {
+        // fixed temperature / rigid u_phi: T_j(+-1) = 1, (-1)^j
+        v = rn * ((i == 1 && (j & 1)) ? -1.0 : 1.0);
+        if (j == 0) v *= 0.5;                       // boundary_fac
+      } else {
+        const long long c = i + (long long)j * n;
+        v = I2R2[c] - c0 * L0[c] - c1 * L1[c];
+      }
+      A[idx] = v;
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+      double mx = 0.0;
+      for (int j = 0; j < n; ++j) mx = fmax(mx, fabs(A[i * n + j]));
+      f1[i] = 1.0 / mx;
+    }
+    __syncthreads();
+    for (int idx = threadIdx.x; idx < n * n; idx += blockDim.x) A[idx] *= f1[idx / n];
+    __syncthreads();
+    if (gj_invert(A, n, piv, colk, red, redi) != 0) return -1;
+    double* G = d.pool + (pass == 0 ? I.o_gt + (long long)mi * n * n : I.o_guphi);
+    store_op(G, A, n, n, nullptr, f1);
+    __syncthreads();
+  }
+  if (m == 0) return 0;
+  // streamfunction, m /= 0: Q0 + m^2 Q1 - wlin ViscFac (S0 + m^2 S1 + m^4 S2)
+  // + i wlin CorFac m I4R4 (implicit Coriolis), tau rows psi(r_o) = psi(r_i) = 0,
+  // d3psi/dx3(r_o) = 0 (rigid, rotating) and dpsi/dr(r_i) = 0
+  const double* Q0 = im_op(V, IM_Q0);
+  const double* Q1 = im_op(V, IM_Q1);
+  const double* S0 = im_op(V, IM_S0);
+  const double* S1 = im_op(V, IM_S1);
+  const double* S2 = im_op(V, IM_S2);
+  const double* R4 = im_op(V, IM_I4R4);
+  const double cv = wlin * I.ViscFac;
+  const double cc = (I.flags & PZF_COR_IMP) ? wlin * I.CorFac * dm : 0.0;
+  for (int idx = threadIdx.x; idx < n * n; idx += blockDim.x) {
+    const int i = idx / n, j = idx - i * n;
+    double re = 0.0, im = 0.0;
+    if (i < 4) {
+      const double dj = (double)j, dn2 = dj * dj, sg = (j & 1) ? -1.0 : 1.0;
+      if (i == 0) re = 1.0;
+      else if (i == 1) re = sg;
+      else if (i == 2) re = 8.0 / 15.0 * dn2 * (dn2 - 1.0) * (dn2 - 4.0);   // update_psi_integ_smat.f90:1303-1306
+      else re = -2.0 * dn2 * sg;                                           // drMat(2,:), chebyshev.f90:363-379
+      re *= rn;
+      if (j == 0) re *= 0.5;                                               // boundary_fac
+    } else {
+      const long long c = i + (long long)j * n;
+      re = Q0[c] + dm2 * Q1[c] - cv * (S0[c] + dm2 * (S1[c] + dm2 * S2[c]));
+      im = cc * R4[c];
+    }
+    Ac[idx] = make_double2(re, im);
+  }
+  __syncthreads();
+  for (int i = threadIdx.x; i < n; i += blockDim.x) {
+    double mx = 0.0;
+    for (int j = 0; j < n; ++j) mx = fmax(mx, hypot(Ac[i * n + j].x, Ac[i * n + j].y));
+    f1[i] = 1.0 / mx;
+  }
+  __syncthreads();
+  for (int idx = threadIdx.x; idx < n * n; idx += blockDim.x) Ac[idx] = cscale(f1[idx / n], Ac[idx]);
+  __syncthreads();
+  if (gj_invert_c(Ac, n, piv, reinterpret_cast<double2*>(colk), red, redi) != 0) return -1;
+  double2* G = reinterpret_cast<double2*>(d.pool + I.o_gsm) + (long long)mi * n * n;
+  for (int idx = threadIdx.x; idx < n * n; idx += blockDim.x) {
+    const int j = idx / n, i = idx - j * n;
+    G[idx] = cscale(f1[j], Ac[i * n + j]);
+  }
+  return 0;
+}
+
+// -- implicit terms from the physical fields ------------------------------------
+// get_temp_rhs_imp_int and get_psi_rhs_imp_int_smat with l_calc_lin
+// (update_temp_integ.f90:471-536, update_psi_integ_smat.f90:960-1115) from
+// T_hat = C T and psi_hat = C psi: the start fields (init_fields.f90:207-251)
+// and start_from_another_scheme (step_time.f90:488-500).  With from_us the
+// streamfunction is first rebuilt from u_s, psi = -i r u_s / (m h^2)
+// (init_fields.f90:73-91).  Writes old/impl logical slot 1 at ring bases bo/bi
+// and dT/dr.
+__device__ void integ_imp(const View& V, const PzInst& I, int mi, int bo, int bi, bool calc, bool from_us, MS& s) {
+  const int n = I.N, m = mi * I.minc;
+  const double dm = (double)m, dm2 = dm * dm;
+  const double* r = V.rad(RV_R);
+  const double* or1 = V.rad(RV_OR1);
+  const double* rgrav = V.rad(RV_RGRAV);
+  double2* T = V.fld(F_TEMP, mi);
+  double2* psi = V.fld(F_PSI, mi);
+  double2* up = V.fld(F_UP, mi);
+  const double2* us = V.fld(F_US, mi);
+  for (int i = threadIdx.x; i < n; i += blockDim.x) s.a[i] = T[i];
+  __syncthreads();
+  op_C(V, n, s.a, s.b, s.w);                                     // T_hat
+  __syncthreads();
+  op_D1c(V, n, s.b, s.c, s.w);
+  __syncthreads();
+  double2* dT = V.fld(F_DTEMP, mi);
+  for (int i = threadIdx.x; i < n; i += blockDim.x) dT[i] = s.c[i];
+  band_mv(band1(V, IM_I2R2), n, s.b, V.hist(0, 0, bo, mi));
+  if (calc) band_mv(band_tlap(V, dm2, I.TdiffFac), n, s.b, V.hist(0, 1, bi, mi));
+  __syncthreads();
+  double2* oP = V.hist(1, 0, bo, mi);
+  double2* iP = V.hist(1, 1, bi, mi);
+  if (m == 0) {
+    for (int i = threadIdx.x; i < n; i += blockDim.x) s.a[i] = make_double2(up[i].x, 0.0);
+    __syncthreads();
+    op_C(V, n, s.a, s.b, s.w);                                   // costf1(Re u_phi)
+    __syncthreads();
+    band_mv(band1(V, IM_I2R2), n, s.b, oP);
+    if (calc) band_mv(band1(V, IM_ULAP, I.ViscFac), n, s.b, iP);
+    __syncthreads();
+    return;
+  }
+  if (from_us) {
+    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+      const double h2 = (I.flags & PZF_NON_ROT) ? 1.0 : I.r_cmb * I.r_cmb - r[i] * r[i];
+      psi[i] = i == 0 ? make_double2(0.0, 0.0) : cscale(r[i] / (dm * h2), cim(-1.0, us[i]));
+    }
+    __syncthreads();
+  }
+  for (int i = threadIdx.x; i < n; i += blockDim.x) {
+    s.a[i] = psi[i];
+    s.e[i] = cscale(-I.BuoFac * rgrav[i] * or1[i], cim(dm, T[i]));
+  }
+  __syncthreads();
+  op_C(V, n, s.a, s.b, s.w);                                     // psi_hat
+  __syncthreads();
+  op_C(V, n, s.e, s.f, s.w);                                     // buoyancy, Chebyshev
+  __syncthreads();
+  band_mv(band_rot(V, dm2), n, s.b, oP);
+  if (calc) {
+    band_mv(band_rot2(V, dm2, I.ViscFac), n, s.b, s.c);
+    band_mv(band1(V, IM_I4R4, I.CorFac * dm), n, s.b, s.g);
+    band_mv(band1(V, IM_I4R4), n, s.f, s.h);
+    __syncthreads();
+    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+      double2 v = s.c[i];
+      if (I.flags & PZF_COR_IMP) v = cadd(v, cim(-1.0, s.g[i]));
+      if (I.flags & PZF_BUO_IMP) v = cadd(v, s.h[i]);
+      iP[i] = v;
+    }
+  }
+  __syncthreads();
+}
+
+// -- one stage for one m (mloop.f90:84-100 and :209-226) --------------------------
+// finish_exp_temp_int / finish_exp_psi_int_smat (update_temp_integ.f90:396-469,
+// update_psi_integ_smat.f90:793-958) on this stage's explicit slot, then
+// update_temp_int and update_psi_int_smat (update_temp_integ.f90:179-298,
+// update_psi_integ_smat.f90:247-573) with the implicit terms of the target
+// stage.  Returns true on a non-finite value (for the block's status vote).
+struct IntegStage {
+  int stage, eslot, oslot, islot;
+  bool dirk, do_finish, do_solve, wold, calc;
+};
+
+__device__ __forceinline__ void trunc_cheb(double2* x, int n, int n_max) {
+  for (int i = n_max + threadIdx.x; i < n; i += blockDim.x) x[i] = make_double2(0.0, 0.0);
+}
+
+__device__ bool integ_stage(const PzDev& d, const View& V, const PzInst& I, const PzState& S, int mi,
+                            const IntegStage& c, MS& s) {
+  const int n = I.N, m = mi * I.minc, n_max = I.n_max;
+  const double dm = (double)m, dm2 = dm * dm;
+  const double rc2 = I.r_cmb * I.r_cmb;
+  const bool rot = !(I.flags & PZF_NON_ROT);
+  const double* r = V.rad(RV_R);
+  const double* or1 = V.rad(RV_OR1);
+  const double* or2 = V.rad(RV_OR2);
+  const double* rgrav = V.rad(RV_RGRAV);
+  const double* tcond = V.rad(RV_TCOND);
+  const double* dtcond = V.rad(RV_DTCOND);
+  const double* ekpump = V.rad(RV_EKPUMP);
+  const double* ekp_up = V.rad(RV_EKP_UP);
+  const double* ekp_us = V.rad(RV_EKP_US);
+  const double* ekp_dusdp = V.rad(RV_EKP_DUSDP);
+  double2* us = V.fld(F_US, mi);
+  double2* up = V.fld(F_UP, mi);
+  double2* om = V.fld(F_OM, mi);
+  double2* psi = V.fld(F_PSI, mi);
+  double2* T = V.fld(F_TEMP, mi);
+  double2* dT = V.fld(F_DTEMP, mi);
+  const bool buo_imp = (I.flags & PZF_BUO_IMP) != 0;
+  const bool cor_imp = (I.flags & PZF_COR_IMP) != 0;
+  bool bad = false;
+
+  if (c.do_finish) {
+    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+      s.a[i] = V.fld(F_DVST, mi)[i];
+      s.e[i] = V.fld(F_DVSOM, mi)[i];
+    }
+    __syncthreads();
+    op_C(V, n, s.a, s.b, s.w);
+    __syncthreads();
+    op_C(V, n, s.e, s.f, s.w);
+    __syncthreads();
+    trunc_cheb(s.b, n, n_max);
+    trunc_cheb(s.f, n, n_max);
+    __syncthreads();
+    op_D1c(V, n, s.b, s.c, s.w);                                 // d(u_s r T)/dr (dealiased)
+    __syncthreads();
+    op_D1c(V, n, s.f, s.g, s.w);                                 // d(u_s r om)/dr
+    __syncthreads();
+    double2* eT = V.hist(0, 2, c.eslot, mi);
+    double2* eP = V.hist(1, 2, c.eslot, mi);
+    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+      const double h2 = rc2 - r[i] * r[i];
+      const double g = rot ? h2 * dtcond[i] + I.tadvz * r[i] * tcond[i] : dtcond[i];
+      s.a[i] = csub(csub(cscale(r[i], eT[i]), cim(dm * g, psi[i])), s.c[i]);
+      double2 p = eP[i];
+      if (m != 0) {
+        p = cscale(r[i], p);
+        if (!cor_imp) p = csub(p, cim(I.CorFac * dm * r[i], psi[i]));
+        if (!buo_imp) p = csub(p, cim(I.BuoFac * rgrav[i] * dm, T[i]));
+        if (I.flags & PZF_EK_PUMP) {
+          const double2 u = us[i];
+          const double2 q = make_double2(ekp_us[i] * u.x - ekp_dusdp[i] * dm * u.y,
+                                         ekp_us[i] * u.y + ekp_dusdp[i] * dm * u.x);
+          const double2 o = om[i], w = up[i];
+          const double ce = I.CorFac * ekpump[i] * r[i];
+          p.x -= ce * (o.x + ekp_up[i] * w.x + q.x);
+          p.y -= ce * (o.y + ekp_up[i] * w.y + q.y);
+        }
+        p = csub(p, s.g[i]);
+      } else if (I.flags & PZF_EK_PUMP) {
+        p = csub(p, cscale(I.CorFac * ekpump[i], up[i]));
+      }
+      s.e[i] = p;
+    }
+    __syncthreads();
+    op_C(V, n, s.a, s.b, s.w);
+    __syncthreads();
+    op_C(V, n, s.e, s.f, s.w);
+    __syncthreads();
+    trunc_cheb(s.b, n, n_max);
+    trunc_cheb(s.f, n, n_max);
+    __syncthreads();
+    band_mv(band1(V, IM_I2R1), n, s.b, eT);
+    band_mv(band1(V, m == 0 ? IM_I2R2 : IM_I4R3), n, s.f, eP);
+    __syncthreads();
+  }
+  if (!c.do_solve) return false;
+  if (S.bridge) integ_imp(V, I, mi, S.r_old, S.r_impl, true, false, s);
+
+  // -- temperature: T_hat = G_T rhs, rhs(1:2) = topt, bott = 0
+  for (int i = threadIdx.x; i < n; i += blockDim.x) {
+    const double2 v = c.dirk ? dirk_rhs(V, I, S, 0, mi, i, c.stage) : imex_rhs(V, I, S, 0, mi, i);
+    s.a[i] = i < 2 ? make_double2(0.0, 0.0) : v;
+  }
+  __syncthreads();
+  mv_lanes(d.pool + I.o_gt + (long long)mi * n * n, n, s.a, s.b);
+  __syncthreads();
+  op_C(V, n, s.b, s.f, s.w);                                     // T (physical), kept in s.f
+  __syncthreads();
+  op_D1c(V, n, s.b, s.c, s.w);                                   // dT/dr
+  __syncthreads();
+  for (int i = threadIdx.x; i < n; i += blockDim.x) {
+    const double2 t = s.f[i];
+    T[i] = t;
+    dT[i] = s.c[i];
+    bad |= !isfinite(t.x) || !isfinite(t.y);
+  }
+  if (c.wold) band_mv(band1(V, IM_I2R2), n, s.b, V.hist(0, 0, c.oslot, mi));
+  if (c.calc) band_mv(band_tlap(V, dm2, I.TdiffFac), n, s.b, V.hist(0, 1, c.islot, mi));
+  __syncthreads();
+
+  double2* oP = V.hist(1, 0, c.oslot, mi);
+  double2* iP = V.hist(1, 1, c.islot, mi);
+  if (m == 0) {
+    // u_phi: real solve, then om = du/dr + u/r
+    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+      const double2 v = c.dirk ? dirk_rhs(V, I, S, 1, mi, i, c.stage) : imex_rhs(V, I, S, 1, mi, i);
+      s.a[i] = make_double2(v.x, 0.0);
+    }
+    __syncthreads();
+    mv_lanes(d.pool + I.o_guphi, n, s.a, s.b);                   // u_phi, Chebyshev
+    __syncthreads();
+    op_C(V, n, s.b, s.g, s.w);
+    __syncthreads();
+    if (I.flags & PZF_RERR) {
+      dcheb_thr(s.b, s.c, n, I.rerr_thr);                        // get_dr_real_1d, l_dct=.false.
+      op_C(V, n, s.c, s.e, s.w);
+      __syncthreads();
+      const double drx = 2.0 / (I.r_cmb - I.r_icb);
+      for (int i = threadIdx.x; i < n; i += blockDim.x) s.e[i] = cscale(drx, s.e[i]);
+    } else {
+      op_D1c(V, n, s.b, s.e, s.w);
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+      const double u = s.g[i].x;
+      us[i] = make_double2(0.0, 0.0);
+      up[i] = make_double2(u, 0.0);
+      om[i] = make_double2(s.e[i].x + or1[i] * u, 0.0);
+      s.g[i] = make_double2(u, 0.0);
+      bad |= !isfinite(u);
+    }
+    __syncthreads();
+    op_C(V, n, s.g, s.a, s.w);                                   // costf1(Re u_phi)
+    __syncthreads();
+    if (c.wold) band_mv(band1(V, IM_I2R2), n, s.a, oP);
+    if (c.calc) band_mv(band1(V, IM_ULAP, I.ViscFac), n, s.a, iP);
+    return bad;
+  }
+  // -- streamfunction, m /= 0: buoyancy I4R4 C(-BuoFac rgrav/r i m T) with the new T
+  if (buo_imp) {
+    for (int i = threadIdx.x; i < n; i += blockDim.x) s.a[i] = cscale(-I.BuoFac * rgrav[i] * or1[i], cim(dm, s.f[i]));
+    __syncthreads();
+    op_C(V, n, s.a, s.c, s.w);
+    __syncthreads();
+    band_mv(band1(V, IM_I4R4), n, s.c, s.e);
+    __syncthreads();
+  }
+  for (int i = threadIdx.x; i < n; i += blockDim.x) {
+    double2 v = c.dirk ? dirk_rhs(V, I, S, 1, mi, i, c.stage) : imex_rhs(V, I, S, 1, mi, i);
+    if (buo_imp) v = cadd(v, cscale(S.wimp_lin[0], s.e[i]));
+    s.a[i] = v;
+  }
+  __syncthreads();
+  cmvn_lanes(reinterpret_cast<const double2*>(d.pool + I.o_gsm) + (long long)mi * n * n, n, s.a, s.b);
+  __syncthreads();
+  op_C(V, n, s.b, s.h, s.w);                                     // psi
+  __syncthreads();
+  op_Dc2(V, n, s.b, s.c, s.g, s.w);                              // dpsi/dr, d2psi/dr2
+  __syncthreads();
+  for (int i = threadIdx.x; i < n; i += blockDim.x) {
+    const double2 p = s.h[i], dp = s.c[i], d2p = s.g[i];
+    const double h2 = rc2 - r[i] * r[i];
+    psi[i] = p;
+    us[i] = cscale(or1[i] * h2, cim(dm, p));
+    up[i] = make_double2(-h2 * dp.x + 3.0 * r[i] * p.x, -h2 * dp.y + 3.0 * r[i] * p.y);
+    const double a1 = rc2 * or1[i] - 6.0 * r[i], a0 = 6.0 + dm2 * or2[i] * h2;
+    const double2 o = make_double2(-h2 * d2p.x - a1 * dp.x + a0 * p.x, -h2 * d2p.y - a1 * dp.y + a0 * p.y);
+    om[i] = o;
+    bad |= !isfinite(o.x) || !isfinite(o.y);
+  }
+  if (c.wold) band_mv(band_rot(V, dm2), n, s.b, oP);
+  if (c.calc) {
+    band_mv(band_rot2(V, dm2, I.ViscFac), n, s.b, s.k);
+    band_mv(band1(V, IM_I4R4, I.CorFac * dm), n, s.b, s.a);
+    __syncthreads();
+    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+      double2 v = s.k[i];
+      if (cor_imp) v = cadd(v, cim(-1.0, s.a[i]));
+      if (buo_imp) v = cadd(v, s.e[i]);
+      iP[i] = v;
+    }
+  }
+  return bad;
+}

@@ -43,6 +43,29 @@ enum {
   PZF_T_IS_OM  = 64,   // TdiffFac == ViscFac (Pr = 1, no hyperdiffusion): the
                        // temperature and vorticity operators of each m /= 0 are
                        // the same matrix; one inverse serves both solves
+  PZF_INTEG    = 128,  // Chebyshev integration method (cheb_method='integ'),
+                       // tau boundary rows, direct streamfunction solve
+  PZF_RERR     = 256,  // l_rerror_fix: round-off threshold in the real
+                       // Chebyshev derivative recursions of the m = 0 flow
+};
+
+// integration-method operators (N x N, column-major, times rnorm, tau rows
+// zero) at o_integ + IM_xxx*N*N, shared by instances of equal N and radratio;
+// each is I_k [sum_d P_d(r) f^(d)] on Chebyshev coefficients
+enum {
+  IM_I2R1 = 0,  // I2 [r f]                        (intcheb2rmult1)
+  IM_I2R2,      // I2 [r^2 f]                      (intcheb2rmult2)
+  IM_I2,        // I2 [f]
+  IM_LT0,       // I2 [r^2 f'' + r f']: intcheb2rmult2lapl(m) = LT0 - m^2 I2
+  IM_ULAP,      // I2 [r^2 f'' + r f' - f]         (rmult2 - 3 intcheb1rmult1, m = 0 u_phi)
+  IM_I4R3,      // I4 [r^3 f]                      (intcheb4rmult3)
+  IM_I4R4,      // I4 [r^4 f]                      (intcheb4rmult4)
+  IM_Q0,        // intcheb4rmult4laplrot(m)  = Q0 + m^2 Q1
+  IM_Q1,
+  IM_S0,        // intcheb4rmult4laplrot2(m) = S0 + m^2 S1 + m^4 S2
+  IM_S1,
+  IM_S2,
+  IM_COUNT
 };
 
 // radial vectors, each N doubles, at o_rad + RV_xxx*N
@@ -120,6 +143,9 @@ struct PzInst {
   long long o_hist;         // 2*(2*(nold+nimp+nexp))*M*N
   long long o_cfl;          // 2*N: dtr, dth
   long long o_series;       // PZ_SERIES_CAP*16
+  long long o_integ;        // integration method: IM_COUNT*N*N (shared by equal N, radratio)
+  int im_band[IM_COUNT];    // bandwidth of each IM_ operator (max |i-j| of a nonzero)
+  double rerr_thr;          // rerror_fac * epsilon with l_rerror_fix, else 0
 };
 
 struct PzState {
@@ -174,11 +200,16 @@ cudaError_t pz_launch_start(const PzDev& d, int only, cudaStream_t s);
 // kernel kinds of a step; a step launches, for stage s = 1..max_stages,
 // k_rloop(s) [k_cfl, k_build after stage 1] k_mloop(s), then k_assemble (if
 // any instance has an assembly stage) and k_obs
-enum { PZK_RLOOP = 0, PZK_CFL, PZK_BUILD, PZK_MLOOP, PZK_OBS, PZK_ASSEMBLE, PZK_KINDS };
+enum { PZK_RLOOP = 0, PZK_CFL, PZK_BUILD, PZK_MLOOP, PZK_OBS, PZK_ASSEMBLE, PZK_MLOOP_INTEG, PZK_KINDS };
 struct PzLaunch { int kind, stage; };
 cudaError_t pz_launch_step_kernel(const PzDev& d, int kind, int stage, cudaStream_t s);
 const char* pz_step_kernel_name(int kind);
 cudaError_t pz_launch_obs(const PzDev& d, int only, cudaStream_t s);
 cudaError_t pz_launch_gather_rows(const PzDev& d, double* out, cudaStream_t s);
 cudaError_t pz_setup_kernels();
-size_t pz_build_smem_bytes(int n, bool direct);   // k_build shared memory for one instance
+size_t pz_build_smem_bytes(int n, bool direct, bool integ);   // k_build shared memory for one instance
+
+// host: the integration-method operators of one (N, radratio), IM_COUNT
+// column-major N x N blocks, and their bandwidths (pz_integ_ops.cu)
+#include <vector>
+void pz_integ_operators(int N, double r_icb, double r_cmb, double rnorm, std::vector<double>& out, int* band);

@@ -623,12 +623,15 @@ __device__ void flag_status(PzState& S, int code) {
   if (threadIdx.x == 0) atomicCAS(&S.status, 0, code);
 }
 
+// integration method (pz_integ.cuh, included below)
+__device__ int integ_build(const PzDev& d, const PzInst& I, const View& V, int mi, double wlin);
+
 // dt independent streamfunction operators (update_psi_coll_dmat.f90:94-98)
 __global__ void __launch_bounds__(PZ_THREADS) k_build_static(PzDev d) {
   const PzItem it = d.mitems[blockIdx.x];
   const PzInst& I = d.inst[it.inst];
   PzState& S = d.state[it.inst];
-  if (it.idx == 0) return;
+  if (it.idx == 0 || (I.flags & PZF_INTEG)) return;
   const View V{&I, d.pool};
   const int n = I.N, m = it.idx * I.minc;
   BuildSmem s = build_smem(n);
@@ -672,6 +675,10 @@ __global__ void __launch_bounds__(PZ_THREADS) k_build(PzDev d) {
   const View V{&I, d.pool};
   const int n = I.N, mi = it.idx, m = mi * I.minc;
   const double wlin = S.wimp_lin[0];
+  if (I.flags & PZF_INTEG) {
+    if (integ_build(d, I, V, mi, wlin) != 0) flag_status(S, PZ_E_SINGULAR);
+    return;
+  }
   BuildSmem s = build_smem(n);
   BuildCtx B{&I, V.basis(BM_RMAT), V.basis(BM_DRMAT), V.basis(BM_D2RMAT), n};
   const bool shared = (I.flags & PZF_T_IS_OM) && m != 0;
@@ -833,6 +840,8 @@ __device__ void imp_from_physical(const View& V, const PzInst& I, int mi, int bo
   __syncthreads();
 }
 
+__device__ void integ_imp(const View& V, const PzInst& I, int mi, int bo, int bi, bool calc, bool from_us, MS& s);
+
 __device__ MS ms_smem(int n) {
   extern __shared__ double2 shm[];
   const int h2 = (n + 1) / 2;
@@ -880,7 +889,8 @@ __global__ void __launch_bounds__(PZ_THREADS) k_start(PzDev d, int only) {
     om[i] = make_double2(w.x + or1[i] * u.x - or1[i] * vs.x, w.y + or1[i] * u.y - or1[i] * vs.y);
   }
   __syncthreads();
-  imp_from_physical(V, I, mi, S.b_old, S.b_impl, true, s);
+  if (I.flags & PZF_INTEG) integ_imp(V, I, mi, S.b_old, S.b_impl, true, true, s);
+  else imp_from_physical(V, I, mi, S.b_old, S.b_impl, true, s);
 }
 
 // ---------------------------------------------------------------------------
@@ -928,11 +938,13 @@ __device__ __forceinline__ double2 dirk_rhs(const View& V, const PzInst& I, cons
   return acc;
 }
 
+#include "pz_integ.cuh"
+
 __global__ void __launch_bounds__(256) k_mloop(PzDev d, int stage) {
   const PzItem it = d.mitems[blockIdx.x];
   const PzInst& I = d.inst[it.inst];
   PzState& Sg = d.state[it.inst];
-  if (Sg.status != 0 || stage > I.nstages) return;
+  if (Sg.status != 0 || stage > I.nstages || (I.flags & PZF_INTEG)) return;
   const PzState S = Sg;
   // stage bookkeeping: the explicit slot of this stage, whether this stage
   // solves (not the last stage of an assembly scheme), and where the solution's
@@ -968,7 +980,6 @@ __global__ void __launch_bounds__(256) k_mloop(PzDev d, int stage) {
   double2* dT = V.fld(F_DTEMP, mi);
   const bool buo_imp = (I.flags & PZF_BUO_IMP) != 0;
   const bool direct = (I.flags & PZF_DIRECT) != 0;
-
   // -- finish_exp_temp_coll (update_temp_coll.f90:152-176)
   if (do_finish) {
   for (int i = threadIdx.x; i < n; i += blockDim.x) {
@@ -1163,6 +1174,34 @@ __global__ void __launch_bounds__(256) k_mloop(PzDev d, int stage) {
       }
     }
   }
+  if (__syncthreads_or(bad)) flag_status(Sg, PZ_E_NONFINITE);
+}
+
+// ---------------------------------------------------------------------------
+// k_mloop_integ: the stage body of the integration method for one m of one
+// instance (mloop.f90:84-100, :209-226); its own kernel so that the
+// collocation kernel keeps its register allocation.
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(256) k_mloop_integ(PzDev d, int stage) {
+  const PzItem it = d.mitems[blockIdx.x];
+  const PzInst& I = d.inst[it.inst];
+  PzState& Sg = d.state[it.inst];
+  if (Sg.status != 0 || stage > I.nstages || !(I.flags & PZF_INTEG)) return;
+  const PzState S = Sg;
+  IntegStage c;
+  c.stage = stage;
+  c.dirk = I.dirk != 0;
+  c.eslot = c.dirk ? stage - 1 : S.r_expl;
+  c.do_finish = !c.dirk || ((I.exp_mask >> (stage - 1)) & 1);
+  c.do_solve = !(c.dirk && I.assembly && stage == I.nstages);
+  const int tgt = (!c.dirk || stage == I.nstages) ? 1 : stage + 1;
+  c.oslot = c.dirk ? 0 : S.b_old;
+  c.islot = c.dirk ? tgt - 1 : S.b_impl;
+  c.wold = tgt == 1;
+  c.calc = c.dirk ? ((I.imp_mask >> (tgt - 1)) & 1) != 0 : S.l_calc_lin != 0;
+  const View V{&I, d.pool};
+  MS s = ms_smem(I.N);
+  const bool bad = integ_stage(d, V, I, S, it.idx, c, s);
   if (__syncthreads_or(bad)) flag_status(Sg, PZ_E_NONFINITE);
 }
 
@@ -1414,8 +1453,13 @@ cudaError_t pz_setup_kernels() {
   return cudaSuccess;
 }
 
-size_t pz_build_smem_bytes(int n, bool direct) {
+size_t pz_build_smem_bytes(int n, bool direct, bool integ) {
   const size_t a = build_smem_bytes(n);
+  if (integ) {
+    // integ_build: complex n x n, f1 (even), colk (2n), red, redi, piv
+    const size_t nd = 2 * (size_t)n * n + (((size_t)n + 1) & ~(size_t)1) + 2 * (size_t)n + 32 + 16 + ((size_t)n + 1) / 2;
+    return nd * sizeof(double);
+  }
   if (!direct) return a;
   const size_t b = build_smat_smem_bytes(n);
   return a > b ? a : b;
@@ -1453,6 +1497,9 @@ cudaError_t pz_launch_step_kernel(const PzDev& d, int kind, int stage, cudaStrea
     case PZK_CFL: k_cfl<<<d.n_inst, 32, 0, s>>>(d); break;
     case PZK_BUILD: k_build<<<d.n_mitems, PZ_THREADS, d.smem_build, s>>>(d); break;
     case PZK_MLOOP: k_mloop<<<d.n_mitems, mloop_threads(d.maxN), ms_smem_bytes(d.maxN), s>>>(d, stage); break;
+    case PZK_MLOOP_INTEG:
+      k_mloop_integ<<<d.n_mitems, mloop_threads(d.maxN), ms_smem_bytes(d.maxN), s>>>(d, stage);
+      break;
     case PZK_OBS: k_obs<<<d.n_inst, 256, 0, s>>>(d, -1); break;
     case PZK_ASSEMBLE: k_assemble<<<d.n_mitems, mloop_threads(d.maxN), ms_smem_bytes(d.maxN), s>>>(d); break;
     default: return cudaErrorInvalidValue;
@@ -1461,6 +1508,7 @@ cudaError_t pz_launch_step_kernel(const PzDev& d, int kind, int stage, cudaStrea
 }
 
 const char* pz_step_kernel_name(int kind) {
-  static const char* names[PZK_KINDS] = {"k_rloop", "k_cfl", "k_build", "k_mloop", "k_obs", "k_assemble"};
+  static const char* names[PZK_KINDS] = {"k_rloop", "k_cfl", "k_build", "k_mloop", "k_obs", "k_assemble",
+                                         "k_mloop_integ"};
   return (kind >= 0 && kind < PZK_KINDS) ? names[kind] : "";
 }

@@ -1,0 +1,123 @@
+"""The Chebyshev integration method (cheb_method='integ', tau rows, direct
+solve; update_temp_integ.f90, update_psi_integ_smat.f90) on the GPU against
+the oracle and the reference's RotInteg fixture (needs a GB300).
+
+The GPU applies per m the inverse of the preconditioned tau-banded operator,
+built by Gauss-Jordan on the device; the oracle solves the same system with
+LAPACK.  The integrated operators are well conditioned, so the fields agree
+to the 1e-10 of the collocation path.
+"""
+import json
+import os
+
+import numpy as np
+import pytest
+
+from tests.helpers import gpu_config, oracle, rel_err, seeded, series_from_oracle
+from tests.test_gpu_parity import check_fields, run_pair
+
+pytestmark = pytest.mark.gpu
+HERE = os.path.dirname(os.path.abspath(__file__))
+
+# the RotInteg first run's physics at a smaller grid and step
+CI = dict(n_r_max=33, n_cheb_max=24, m_max=24, ek=1e-3, ra=5e4, pr=1.0, radratio=0.35, time_scale="ROT",
+          cheb_method="INTEG", matrix_solve="DIRECT", time_scheme="CNAB2", dtMax=2e-2, courfac=4.0)
+
+
+@pytest.fixture(scope="module")
+def pz():
+    import torch
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    from pizza_gb300 import build as b
+    b.build()
+    import pizza_gb300
+    return pizza_gb300
+
+
+def test_integ_start_state(pz):
+    t0 = seeded(CI, 3, 1e-2)
+    sim = oracle(CI, temp0=t0)
+    ens = pz.Ensemble(gpu_config(CI))
+    ens.set_state(0, temp=t0)
+    g = ens.get_state(0)
+    check_fields(sim, g, 1e-13, "start")
+    assert rel_err(g["dtemp"], sim.dtemp) < 1e-12
+    for f in ("old", "impl"):
+        for k, ta in ((0, sim.dTdt), (1, sim.dpsidt)):
+            got = ens.get_history(0, k, {"old": 0, "impl": 1}[f], 1)
+            assert rel_err(got, getattr(ta, f)[0]) < 1e-12, (f, k)
+
+
+def test_integ_cnab2_steps(pz):
+    sim, ens, out = run_pair(pz, CI, 100, seed=5, amp=1e-2, checkpoints=(1, 10))
+    for k, s, g in out:
+        check_fields(s, g, 1e-10, f"integ step {k}")
+    ref = series_from_oracle(sim)
+    np.testing.assert_allclose(ens.series(0)[-1, :15], ref[:15], rtol=1e-10, atol=1e-20)
+
+
+@pytest.mark.parametrize("variant", [
+    dict(time_scheme="SBDF3"),
+    dict(time_scheme="CK232"),
+    dict(time_scheme="BPR353"),
+    dict(corio_term="EXPLICIT"),
+    dict(buo_term="EXPLICIT"),
+    dict(l_ek_pump=True),
+    dict(l_rerror_fix=True),
+    dict(pr=0.3, n_cheb_max=33),
+])
+def test_integ_variants(pz, variant):
+    spec = dict(CI, **variant)
+    sim, ens, out = run_pair(pz, spec, 30, seed=7, amp=1e-2)
+    check_fields(sim, out[-1][2], 1e-10, str(variant))
+
+
+def test_integ_larger_grid(pz):
+    """The grid of RotInteg's continuation run (n_r_max=97, n_cheb_max=64)."""
+    spec = dict(CI, n_r_max=97, n_cheb_max=64, m_max=64, ek=1e-4, ra=2e6, dtMax=2e-3)
+    sim, ens, out = run_pair(pz, spec, 10, seed=9, amp=1e-3)
+    check_fields(sim, out[-1][2], 1e-9, "N=97")
+
+
+def test_mixed_integ_and_collocation_batch(pz):
+    specs = [CI,
+             dict(CI, cheb_method="COLL", n_cheb_max=33),
+             dict(CI, n_r_max=49, n_cheb_max=32, m_max=32, ra=8e4),
+             dict(CI, cheb_method="COLL", matrix_solve="INFLUENCE", time_scale="VISC", dtMax=2e-5, n_cheb_max=33)]
+    temps = [seeded(s, 30 + i, 1e-2) for i, s in enumerate(specs)]
+    ens = pz.Ensemble([gpu_config(s) for s in specs])
+    ens.set_state_all(temps)
+    ens.step(20)
+    for i, s in enumerate(specs):
+        sim = oracle(s, temp0=temps[i])
+        for _ in range(20):
+            sim.advance()
+        check_fields(sim, ens.get_state(i), 1e-10, f"instance {i}")
+
+
+def test_rotinteg_fixture_on_gpu(pz):
+    """All 201 e_kin_3D rows of RotInteg's first run (4000 CNAB2 steps,
+    Courant-controlled dt) at the reference harness's tolerances."""
+    with open(os.path.join(HERE, "golden", "cases.json")) as f:
+        spec = json.load(f)["RotInteg"]
+    p = dict(spec["params"])
+    ref = np.loadtxt(os.path.join(HERE, "golden", "RotInteg.txt"))
+    sim = oracle(p)                          # init_t = -1 start field built by the oracle
+    ens = pz.Ensemble(gpu_config(p))
+    ens.set_state(0, temp=sim.temp.copy())
+    n, nlog = p["n_time_steps"], p["n_log_step"]
+    rows = [ens.series(0)[-1]]
+    for _ in range(n // nlog):
+        ens.step(nlog)
+        rows.append(ens.series(0)[-1])
+    got = np.array(rows)[:, [0, 4, 5, 6, 7]]
+    assert got.shape == ref.shape
+    np.testing.assert_allclose(got, ref, rtol=1e-8, atol=1e-20)
+
+
+def test_integ_rejections(pz):
+    bad = [dict(CI, matrix_solve="INFLUENCE"), dict(CI, time_scheme="ARS232"), dict(CI, l_non_rot=True)]
+    for s in bad:
+        with pytest.raises(RuntimeError):
+            pz.Ensemble(gpu_config(s))
