@@ -54,7 +54,12 @@ def test_integ_cnab2_steps(pz):
     for k, s, g in out:
         check_fields(s, g, 1e-10, f"integ step {k}")
     ref = series_from_oracle(sim)
-    np.testing.assert_allclose(ens.series(0)[-1, :15], ref[:15], rtol=1e-10, atol=1e-20)
+    row = ens.series(0)[-1]
+    keep = [k for k in range(15) if k not in (12, 13)]
+    np.testing.assert_allclose(row[keep], ref[keep], rtol=1e-10, atol=1e-20)
+    # tTop, tBot: the tau rows hold T = 0 on the walls in Chebyshev space, so
+    # the wall values are rounding residues (~1e-12 of the O(1) temperature)
+    np.testing.assert_allclose(row[12:14], ref[12:14], rtol=0, atol=1e-11)
 
 
 @pytest.mark.parametrize("variant", [
