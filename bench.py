@@ -1,7 +1,6 @@
 """Benchmark of the GB300 pizza time step.
 
-Workload (configs[2] shape, the configuration the headline metric is quoted
-on): a batched ensemble of B independent annulus instances of uneven size,
+Workload (the batched ensemble the headline metric is quoted on): a batched ensemble of B independent annulus instances of uneven size,
 n_r_max in {33, 49, 65}, n_phi_max in {96, 192, 288} (m_max = n_phi_max/3),
 log10 Ra ~ U[5, log10 Ra_max(n_r_max)] with Ra_max = 1e6, 3e6, 1e7 for
 n_r_max = 33, 49, 65 (the resolution that keeps a 500-step run stable; 1e7 at
@@ -11,7 +10,7 @@ courfac = 2: dt = dr / (courfac |u|)), dtMax = min(1e-4, 0.03/sqrt(Ra)),
 collocation with the influence-matrix solve, each instance started from its
 own seeded temperature perturbation of amplitude 1e-3 (synthetic data: the
 reference publishes no dataset).  One step advances every instance by one
-time step; the default timed region is configs[2]'s 500 steps.
+time step; the default timed region is the ensemble's 500 steps.
 
 Metric: aggregate instance-steps/s of the batched step (``value``), next to the
 plain one-instance-per-handle GPU step of the same instances
@@ -249,7 +248,7 @@ def reference_arm(args, specs):
     line = {"impl": "reference", "metric": METRIC, "value": rate, "unit": UNIT, "n_gpus": 0,
             "steps": steps, "warmup": 1, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "f64", "data": "synthetic",
-            "config": {"workload": f"batched ensemble of {len(specs)} instances (configs[2] shape)",
+            "config": {"workload": f"batched ensemble of {len(specs)} annulus instances",
                        "instances_sampled": len(sample)},
             "cpu_baseline": {"value": rate, "unit": UNIT, "cores": cores, "kind": "port",
                              "sample": f"{len(sample)} instances x {steps} steps of the oracle port, one process "
@@ -290,6 +289,27 @@ def plain_rate(specs, steps, warmup, torch):
         e.close()
     t_step_ms = sum(t_class[(s["n_r_max"], s["m_max"])] for s in specs)
     return len(specs) / (t_step_ms * 1e-3), {f"{k[0]}x{3 * k[1]}": v for k, v in t_class.items()}
+
+
+# the single large integration-method instance (sparse Chebyshev, tau rows):
+# n_r_max=97, n_phi_max=384, E=1e-5, Ra=3e7, SBDF3, dt=2e-6, amplitude 1e-4
+INTEG_SPEC = dict(n_r_max=97, n_cheb_max=97, m_max=128, ek=1e-5, ra=3e7, pr=1.0, radratio=0.35, l_ek_pump=True,
+                  time_scheme="SBDF3", dtMax=2e-6, cheb_method="INTEG", matrix_solve="DIRECT", seed=3)
+
+
+def integ_leg(torch, steps=200, warmup=5):
+    """Steps/s of the integration-method instance on its own handle (graph
+    replay) and its per-kernel times; parity with the oracle is in the tests."""
+    import pizza_gb300 as pz
+    ens = pz.Ensemble(gpu_cfg(INTEG_SPEC))
+    ens.set_state(0, temp=seeded_temp(INTEG_SPEC, amp=1e-4))
+    ens.step(warmup)
+    ms = time_steps(ens, steps, torch)
+    kms = ens.profile_steps(5)
+    ens.close()
+    return {"workload": "one integ instance: n_r_max=97, n_phi_max=384, E=1e-5, Ra=3e7, SBDF3, dt=2e-6",
+            "steps": steps, "steps_per_s": steps / (ms * 1e-3), "ms_per_step": ms / steps,
+            "kernel_ms_per_step": {k: v for k, v in kms.items() if v > 0.0}}
 
 
 ADJ_SPEC = dict(n_r_max=65, n_cheb_max=65, m_max=64, ek=1e-4, ra=2e6, pr=1.0, radratio=0.35, l_ek_pump=True,
@@ -344,6 +364,9 @@ def main():
     ap.add_argument("--no-plain", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-adjoint", action="store_true")
+    ap.add_argument("--no-integ", action="store_true")
+    ap.add_argument("--integ-only", action="store_true", help="print only the integration-method measurement")
+    ap.add_argument("--integ-steps", type=int, default=200)
     ap.add_argument("--adjoint-only", action="store_true", help="print only the adjoint/forward measurement")
     ap.add_argument("--adj-steps", type=int, default=ADJ_STEPS)
     ap.add_argument("--adj-reps", type=int, default=3)
@@ -369,6 +392,11 @@ def main():
     from __graft_entry__ import build
     build()
     import pizza_gb300 as pz
+
+    if args.integ_only:
+        if rank == 0:
+            print(json.dumps({"integ": integ_leg(torch, args.integ_steps, args.warmup)}))
+        return
 
     if args.adjoint_only:
         if rank == 0:
@@ -440,6 +468,7 @@ def main():
     adj = None
     if not args.no_adjoint:
         adj = {"checkpointed": adjoint_ratio(torch), "stored_trajectory": adjoint_ratio(torch, checkpoint_every=0)}
+    integ = None if args.no_integ else integ_leg(torch, args.integ_steps)
     cpu = None
     if not args.no_cpu:
         cpu = cpu_baseline(specs)
@@ -447,7 +476,7 @@ def main():
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": f"batched ensemble of {len(specs)} annulus instances per GPU (configs[2] shape): "
+        "config": {"workload": f"batched ensemble of {len(specs)} annulus instances per GPU: "
                                "n_r_max in {33,49,65}, n_phi_max in {96,192,288}, Ra log-uniform [1e5, Ra_max(N)] "
                                "with Ra_max = 1e6/3e6/1e7 for N = 33/49/65, E in {1e-3,1e-4}, CNAB2, CFL 0.5, "
                                "collocation + influence matrix",
@@ -469,6 +498,7 @@ def main():
         "dominant_kernel": dom,
         "operator_rebuilds_per_step": n_dt_changes / max(1, args.steps - 1),
         "adjoint": adj,
+        "integ": integ,
         "cpu_baseline": cpu,
         "e2e": e2e,
         "gpu_launches": ens.launches_per_step() * args.steps,

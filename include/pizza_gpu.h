@@ -240,7 +240,7 @@ int pz_explicit_terms_noalloc(pz_handle* h, int inst, const double* us, const do
                               double* dpsidt_expl, double* dtr, double* dth);
 
 /* Release all device memory of the handle. */
-/* ---- discrete adjoint (the gradient path of the benchmark spec) ----------
+/* ---- discrete adjoint (the gradient path) ----------------------------------
  * pizza itself has no adjoint; these entry points back the PyTorch
  * autograd.Function of the binding.  The objective of every instance is
  *   J = (1/n_window) * sum over the last n_window states k of

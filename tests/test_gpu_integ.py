@@ -126,3 +126,29 @@ def test_integ_rejections(pz):
     for s in bad:
         with pytest.raises(RuntimeError):
             pz.Ensemble(gpu_config(s))
+
+
+def test_c1_integ_sbdf3_full_size(pz):
+    """The integ workload at full size (n_r_max=97, n_phi_max=384, E=1e-5,
+    Ra=3e7, SBDF3, dt=2e-6, seeded amplitude 1e-4): 20 steps against the
+    oracle, then 500 more on the GPU alone, checked for finiteness and for
+    the tau rows, which hold in Chebyshev space: for T and psi (m > 0)
+    c_0/2 + sum_n c_n (+-1)^n = 0 at both walls (the physical wall value
+    differs from it by the DCT-I's half weight on c_{N-1})."""
+    spec = dict(n_r_max=97, n_cheb_max=97, m_max=128, ek=1e-5, ra=3e7, pr=1.0, radratio=0.35,
+                time_scheme="SBDF3", dtMax=2e-6, cheb_method="INTEG", matrix_solve="DIRECT", l_ek_pump=True)
+    sim, ens, out = run_pair(pz, spec, 20, seed=11, amp=1e-4, checkpoints=(3,))
+    for k, s, g in out:
+        check_fields(s, g, 1e-10, f"c1 step {k}")
+    ens.step(500)
+    g = ens.get_state(0)
+    for f in ("temp", "us", "up", "om"):
+        assert np.all(np.isfinite(g[f]))
+    N = spec["n_r_max"]
+    sg = np.where(np.arange(N) % 2 == 0, 1.0, -1.0)
+    for f in ("temp", "psi"):
+        c = sim.cheb.costf1(g[f])[1:]              # Chebyshev coefficients, m > 0
+        top = 0.5 * c[:, 0] + c[:, 1:].sum(axis=1)
+        bot = 0.5 * c[:, 0] + (c[:, 1:] * sg[1:]).sum(axis=1)
+        scale = np.max(np.abs(c))
+        assert np.max(np.abs(top)) < 1e-11 * scale and np.max(np.abs(bot)) < 1e-11 * scale, f

@@ -2,7 +2,7 @@
 
 Parity bar: fields and time series agree with the FP64 oracle to 1e-10
 relative (norm-wise: max |gpu - oracle| / max |oracle| per field), the
-tolerance pizza's spec sets for this FP64 path.  The GPU applies the
+tolerance set for this FP64 path.  The GPU applies the
 same linear operators as the reference (DCT-I, Chebyshev derivatives, LU
 solves) as dense inverse operators; rounding differs at ~1e-14 per step.
 """
@@ -74,7 +74,7 @@ def test_start_state_matches_oracle(pz):
 
 
 def test_c0_influence_cnab2_200_steps(pz):
-    """configs[0] shape (N=33, m_max=32, E=1e-3, Ra=1e5, Ekman pumping, CNAB2)."""
+    """The single-instance workload (N=33, m_max=32, E=1e-3, Ra=1e5, Ekman pumping, CNAB2)."""
     sim, ens, out = run_pair(pz, C0, 200, checkpoints=(1, 10))
     for k, s, g in out:
         check_fields(s, g, TOL, f"step {k}")
