@@ -200,7 +200,7 @@ void* pz_stream(pz_handle* h);
  * events between them on the handle's stream; kernel_ms[k] receives the mean
  * device time per step of kernel kind k (k < PZ_KERNEL_KINDS, summed over the
  * stages of a DIRK step), names in pz_kernel_name(k).  Synchronises. */
-#define PZ_KERNEL_KINDS 7
+#define PZ_KERNEL_KINDS 9
 int pz_step_profile(pz_handle* h, int n_steps, double* kernel_ms);
 const char* pz_kernel_name(int k);
 

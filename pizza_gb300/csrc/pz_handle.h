@@ -25,6 +25,7 @@ struct pz_handle {
   PzState* d_state = nullptr;
   PzItem* d_ritems = nullptr;
   PzItem* d_mitems = nullptr;
+  PzItem* d_order = nullptr;
   PzDev dev{};
   cudaStream_t stream = nullptr;
   cudaGraphExec_t graph = nullptr;

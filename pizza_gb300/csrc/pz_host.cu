@@ -719,6 +719,7 @@ extern "C" int pz_create(const pz_config* cfgs, int n, pz_handle** out) {
   if ((e = cudaMalloc(&h->d_inst, n * sizeof(PzInst))) || (e = cudaMalloc(&h->d_state, n * sizeof(PzState))) ||
       (e = cudaMalloc(&h->d_ritems, ritems.size() * sizeof(PzItem))) ||
       (e = cudaMalloc(&h->d_mitems, mitems.size() * sizeof(PzItem))) ||
+      (e = cudaMalloc(&h->d_order, mitems.size() * sizeof(PzItem))) ||
       (e = cudaMalloc(&h->d_rows, (size_t)n * PZ_SERIES_COLS * sizeof(double)))) {
     g_create_error = std::string("device allocation: ") + cudaGetErrorString(e);
     pz_destroy(h);
@@ -733,6 +734,7 @@ extern "C" int pz_create(const pz_config* cfgs, int n, pz_handle** out) {
   h->dev.pool = h->pool;
   h->dev.ritems = h->d_ritems; h->dev.n_ritems = (int)ritems.size();
   h->dev.mitems = h->d_mitems; h->dev.n_mitems = (int)mitems.size();
+  h->dev.order = h->d_order;
   h->dev.n_inst = n;
   h->dev.maxN = maxN; h->dev.maxP = maxP; h->dev.maxM = maxM;
   size_t sb = 0;
@@ -751,11 +753,19 @@ extern "C" int pz_create(const pz_config* cfgs, int n, pz_handle** out) {
     any_integ |= integ;
     any_coll |= !integ;
   }
+  // the rebuild fused with the first stage when it costs the stage no
+  // occupancy: collocation only, build staged in at most 48 KB of shared memory
+  const bool fused = !any_integ && sb <= 48 * 1024;
   h->plan.clear();
   for (int st = 1; st <= smax; ++st) {
     h->plan.push_back({PZK_RLOOP, st});
     if (st == 1) {
       h->plan.push_back({PZK_CFL, 1});
+      if (fused) {
+        h->plan.push_back({PZK_ORDER, 1});
+        h->plan.push_back({PZK_BUILD_MLOOP, 1});
+        continue;
+      }
       h->plan.push_back({PZK_BUILD, 1});
     }
     if (any_coll) h->plan.push_back({PZK_MLOOP, st});
@@ -1182,6 +1192,7 @@ extern "C" int pz_destroy(pz_handle* h) {
   cudaFree(h->d_state);
   cudaFree(h->d_ritems);
   cudaFree(h->d_mitems);
+  cudaFree(h->d_order);
   cudaFree(h->d_rows);
   if (h->stream) cudaStreamDestroy(h->stream);
   delete h;

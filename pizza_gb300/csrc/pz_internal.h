@@ -181,6 +181,7 @@ struct PzDev {
   double* pool;
   const PzItem* ritems; int n_ritems;     // (inst, r)
   const PzItem* mitems; int n_mitems;     // (inst, m index)
+  PzItem* order;                          // n_mitems: k_order's layout of the fused first stage
   int n_inst;
   int maxN, maxP, maxM;
   int smem_build;           // dynamic shared memory of k_build (bytes)
@@ -200,7 +201,10 @@ cudaError_t pz_launch_start(const PzDev& d, int only, cudaStream_t s);
 // kernel kinds of a step; a step launches, for stage s = 1..max_stages,
 // k_rloop(s) [k_cfl, k_build after stage 1] k_mloop(s), then k_assemble (if
 // any instance has an assembly stage) and k_obs
-enum { PZK_RLOOP = 0, PZK_CFL, PZK_BUILD, PZK_MLOOP, PZK_OBS, PZK_ASSEMBLE, PZK_MLOOP_INTEG, PZK_KINDS };
+// (k_order + k_build_mloop replace k_build + k_mloop(1) when every instance is
+// a collocation instance with a small build footprint)
+enum { PZK_RLOOP = 0, PZK_CFL, PZK_BUILD, PZK_MLOOP, PZK_OBS, PZK_ASSEMBLE, PZK_MLOOP_INTEG, PZK_ORDER,
+       PZK_BUILD_MLOOP, PZK_KINDS };
 struct PzLaunch { int kind, stage; };
 cudaError_t pz_launch_step_kernel(const PzDev& d, int kind, int stage, cudaStream_t s);
 const char* pz_step_kernel_name(int kind);

@@ -667,8 +667,7 @@ __global__ void __launch_bounds__(PZ_THREADS) k_build_static(PzDev d) {
 
 // dt dependent operators, rebuilt when lMat (step_time.f90:296-303):
 // temperature, omega and u_phi, plus the influence-matrix ingredients.
-__global__ void __launch_bounds__(PZ_THREADS) k_build(PzDev d) {
-  const PzItem it = d.mitems[blockIdx.x];
+__device__ __forceinline__ void build_item(const PzDev& d, const PzItem it) {
   const PzInst& I = d.inst[it.inst];
   PzState& S = d.state[it.inst];
   if (S.status != 0 || !S.lMat) return;
@@ -746,6 +745,8 @@ __global__ void __launch_bounds__(PZ_THREADS) k_build(PzDev d) {
     infl[0] = b3 / det; infl[1] = -t3 / det; infl[2] = -b2 / det; infl[3] = t2 / det;
   }
 }
+
+__global__ void __launch_bounds__(PZ_THREADS) k_build(PzDev d) { build_item(d, d.mitems[blockIdx.x]); }
 
 // ---------------------------------------------------------------------------
 // implicit terms from physical-space fields: get_temp_rhs_imp_coll and
@@ -940,8 +941,7 @@ __device__ __forceinline__ double2 dirk_rhs(const View& V, const PzInst& I, cons
 
 #include "pz_integ.cuh"
 
-__global__ void __launch_bounds__(256) k_mloop(PzDev d, int stage) {
-  const PzItem it = d.mitems[blockIdx.x];
+__device__ __forceinline__ void mloop_item(const PzDev& d, const PzItem it, int stage) {
   const PzInst& I = d.inst[it.inst];
   PzState& Sg = d.state[it.inst];
   if (Sg.status != 0 || stage > I.nstages || (I.flags & PZF_INTEG)) return;
@@ -1177,12 +1177,64 @@ __global__ void __launch_bounds__(256) k_mloop(PzDev d, int stage) {
   if (__syncthreads_or(bad)) flag_status(Sg, PZ_E_NONFINITE);
 }
 
+__global__ void __launch_bounds__(256) k_mloop(PzDev d, int stage) { mloop_item(d, d.mitems[blockIdx.x], stage); }
+
+// ---------------------------------------------------------------------------
+// k_order + k_build_mloop: the operator rebuild fused with the first stage.
+// Each (instance, m) only needs its own operators, so a block rebuilds them
+// (if its instance's dt changed) and then runs the stage.  k_order lays the
+// work items out so that the rebuilding ones -- long, latency-bound
+// Gauss-Jordan chains -- are spread one in four over the first waves instead
+// of running as a wave of their own: the other blocks keep the FP64 pipe busy
+// meanwhile.  Item k of the rebuild list goes to position k + min(3k, n_rest),
+// item j of the rest to j + min(j/3 + 1, n_rebuild); both lists keep the
+// largest-first order of the work list.
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(1024) k_order(PzDev d) {
+  __shared__ int sc[1024];
+  const int n = d.n_mitems, T = blockDim.x, t = threadIdx.x;
+  const int per = (n + T - 1) / T;
+  const int b0 = min(n, t * per), b1 = min(n, b0 + per);
+  auto rebuild = [&](const PzItem& it) {
+    const PzState& S = d.state[it.inst];
+    return S.status == 0 && S.lMat != 0;
+  };
+  int cnt = 0;
+  for (int b = b0; b < b1; ++b) cnt += rebuild(d.mitems[b]) ? 1 : 0;
+  sc[t] = cnt;
+  __syncthreads();
+  for (int off = 1; off < T; off <<= 1) {          // inclusive scan
+    const int v = t >= off ? sc[t - off] : 0;
+    __syncthreads();
+    sc[t] += v;
+    __syncthreads();
+  }
+  const int n_reb = sc[T - 1], n_rest = n - n_reb;
+  int k = sc[t] - cnt;                              // rebuild items before b0
+  int j = b0 - k;                                   // other items before b0
+  for (int b = b0; b < b1; ++b) {
+    const PzItem it = d.mitems[b];
+    int pos;
+    if (rebuild(it)) { pos = k + min(3 * k, n_rest); ++k; }
+    else { pos = j + min(j / 3 + 1, n_reb); ++j; }
+    d.order[pos] = it;
+  }
+}
+
+__global__ void __launch_bounds__(256) k_build_mloop(PzDev d) {
+  const PzItem it = d.order[blockIdx.x];
+  if (d.inst[it.inst].flags & PZF_INTEG) return;
+  build_item(d, it);
+  __syncthreads();
+  mloop_item(d, it, 1);
+}
+
 // ---------------------------------------------------------------------------
 // k_mloop_integ: the stage body of the integration method for one m of one
 // instance (mloop.f90:84-100, :209-226); its own kernel so that the
 // collocation kernel keeps its register allocation.
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(256) k_mloop_integ(PzDev d, int stage) {
+__global__ void __launch_bounds__(256, 3) k_mloop_integ(PzDev d, int stage) {
   const PzItem it = d.mitems[blockIdx.x];
   const PzInst& I = d.inst[it.inst];
   PzState& Sg = d.state[it.inst];
@@ -1448,6 +1500,7 @@ cudaError_t pz_setup_kernels() {
   cudaError_t e;
   const int big = 200 * 1024;
   if ((e = cudaFuncSetAttribute(k_build, cudaFuncAttributeMaxDynamicSharedMemorySize, PZ_SMEM_MAX))) return e;
+  if ((e = cudaFuncSetAttribute(k_build_mloop, cudaFuncAttributeMaxDynamicSharedMemorySize, PZ_SMEM_MAX))) return e;
   if ((e = cudaFuncSetAttribute(k_build_static, cudaFuncAttributeMaxDynamicSharedMemorySize, big))) return e;
   if ((e = cudaFuncSetAttribute(k_rloop, cudaFuncAttributeMaxDynamicSharedMemorySize, PZ_SMEM_MAX))) return e;
   return cudaSuccess;
@@ -1497,6 +1550,12 @@ cudaError_t pz_launch_step_kernel(const PzDev& d, int kind, int stage, cudaStrea
     case PZK_CFL: k_cfl<<<d.n_inst, 32, 0, s>>>(d); break;
     case PZK_BUILD: k_build<<<d.n_mitems, PZ_THREADS, d.smem_build, s>>>(d); break;
     case PZK_MLOOP: k_mloop<<<d.n_mitems, mloop_threads(d.maxN), ms_smem_bytes(d.maxN), s>>>(d, stage); break;
+    case PZK_ORDER: k_order<<<1, 1024, 0, s>>>(d); break;
+    case PZK_BUILD_MLOOP: {
+      const size_t sm = (size_t)d.smem_build > ms_smem_bytes(d.maxN) ? (size_t)d.smem_build : ms_smem_bytes(d.maxN);
+      k_build_mloop<<<d.n_mitems, mloop_threads(d.maxN), sm, s>>>(d);
+      break;
+    }
     case PZK_MLOOP_INTEG:
       k_mloop_integ<<<d.n_mitems, mloop_threads(d.maxN), ms_smem_bytes(d.maxN), s>>>(d, stage);
       break;
@@ -1509,6 +1568,6 @@ cudaError_t pz_launch_step_kernel(const PzDev& d, int kind, int stage, cudaStrea
 
 const char* pz_step_kernel_name(int kind) {
   static const char* names[PZK_KINDS] = {"k_rloop", "k_cfl", "k_build", "k_mloop", "k_obs", "k_assemble",
-                                         "k_mloop_integ"};
+                                         "k_mloop_integ", "k_order", "k_build_mloop"};
   return (kind >= 0 && kind < PZK_KINDS) ? names[kind] : "";
 }
