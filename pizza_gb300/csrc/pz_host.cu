@@ -382,6 +382,8 @@ int validate(const pz_config& c, std::string* why) {
   if (c.cheb_method != PZ_CHEB_COLL && c.cheb_method != PZ_CHEB_INTEG) return bad("unknown cheb_method");
   if (c.time_scale != PZ_TS_VISC && c.time_scale != PZ_TS_ROT) return bad("unknown time_scale");
   if (c.l_rerror_fix && !(c.rerror_fac > 0.0)) return bad("rerror_fac must be > 0");
+  if (c.l_rerror_fix && c.cheb_method != PZ_CHEB_INTEG)
+    return uns("l_rerror_fix is implemented for cheb_method 'integ' (the collocation m = 0 recursions take no threshold)");
   if (c.cheb_method == PZ_CHEB_INTEG) {
     if (c.matrix_solve != PZ_SOLVE_DIRECT)
       return uns("cheb_method 'integ' is implemented with matrix_solve 'DIRECT' (update_psi_integ_smat)");

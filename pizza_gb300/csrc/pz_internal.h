@@ -161,6 +161,7 @@ struct PzState {
   int status;               // 0 or a negative PZ_E_* code
   int series_count;
   int pad;
+  double w_lhs;             // implicit weight the current operators were built with
 };
 
 // history ring accessors: field f in {0: temperature, 1: psi/omega},

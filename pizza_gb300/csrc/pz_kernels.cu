@@ -235,6 +235,7 @@ __global__ void k_cfl(PzDev d) {
   if (set_weights(I, S)) S.lMatNext = 1;
   S.time = S.time + S.dt[0];
   S.lMat = (S.lMatNext || l_new_dt) ? 1 : 0;
+  if (S.lMat) S.w_lhs = S.wimp_lin[0];
   S.lMatNext = 0;
   S.n_step += 1;
   S.bridge = (!I.dirk && I.scheme != PZ_CNAB2 && S.n_step <= I.nold - 1) ? 1 : 0;
@@ -1035,6 +1036,20 @@ __device__ __forceinline__ void mloop_item(const PzDev& d, const PzItem it, int 
   // -- start_from_another_scheme (step_time.f90:417-516)
   if (S.bridge) imp_from_physical(V, I, mi, S.r_old, S.r_impl, true, s);
 
+  // Implicit terms from the solve.  At every interior row the solution x of
+  // (I - w L) x = rhs satisfies L x = (x - rhs) / w exactly, w being the weight
+  // the operators were built with; the boundary rows of an implicit term are
+  // never read (the next right-hand side replaces them by boundary values).
+  // So the multistep family takes L x from the residual instead of second
+  // derivatives (the rounding this adds to the next right-hand side is
+  // w * O(eps |x| / w)).  Needs the untruncated solution (n_cheb_max = n_r_max).
+  // The coupled (omega, psi) operator of the direct solve is too ill-conditioned
+  // for its residual at n_r_max ~ 100 (it adds ~1e-9 relative there), so its
+  // vorticity keeps the second derivatives.
+  const bool resid = calc && !dirk && !S.bridge && I.n_max == n && S.w_lhs > 0.0;
+  const bool resid_om = resid && !direct;
+  const double iw = resid ? 1.0 / S.w_lhs : 0.0;
+
   // -- update_temp_co (update_temp_coll.f90:66-150)
   for (int i = threadIdx.x; i < n; i += blockDim.x) {
     const double2 v = dirk ? dirk_rhs(V, I, S, 0, mi, i, stage) : imex_rhs(V, I, S, 0, mi, i);
@@ -1045,7 +1060,8 @@ __device__ __forceinline__ void mloop_item(const PzDev& d, const PzItem it, int 
                                                          : d.pool + I.o_gt + (long long)mi * n * n;
   mv_lanes(GT, n, s.a, s.b);                                              // Chebyshev T
   __syncthreads();
-  op_Dc2(V, n, s.b, s.c, s.e, s.w);                                       // dT/dr, d2T/dr2
+  if (resid) op_D1c(V, n, s.b, s.c, s.w);                                 // dT/dr
+  else op_Dc2(V, n, s.b, s.c, s.e, s.w);                                  // dT/dr, d2T/dr2
   __syncthreads();
   op_C(V, n, s.b, s.f, s.w);                                              // T (physical)
   __syncthreads();
@@ -1059,13 +1075,16 @@ __device__ __forceinline__ void mloop_item(const PzDev& d, const PzItem it, int 
       dT[i] = d1;
       if (wold) oT[i] = t;
       bad |= !isfinite(t.x) || !isfinite(t.y);
-      if (calc) {
+      if (resid) {
+        iT[i] = (i == 0 || i == n - 1) ? make_double2(0.0, 0.0) : cscale(iw, csub(t, s.a[i]));
+      } else if (calc) {
         const double f = I.TdiffFac;
         iT[i] = make_double2(f * (d2.x + or1[i] * d1.x - dm2 * or2[i] * t.x),
                              f * (d2.y + or1[i] * d1.y - dm2 * or2[i] * t.y));
       }
     }
   }
+  __syncthreads();
   // s.f keeps the new physical temperature
   // -- update_om_coll_dmat (update_psi_coll_dmat.f90:126-466)
   for (int i = threadIdx.x; i < n; i += blockDim.x) {
@@ -1084,20 +1103,23 @@ __device__ __forceinline__ void mloop_item(const PzDev& d, const PzItem it, int 
   if (m == 0) {
     mv_lanes(d.pool + I.o_guphi, n, s.a, s.b);           // uphi, Chebyshev
     __syncthreads();
-    op_Dc2(V, n, s.b, s.c, s.e, s.w);
+    if (resid) op_D1c(V, n, s.b, s.c, s.w);
+    else op_Dc2(V, n, s.b, s.c, s.e, s.w);
     __syncthreads();
     op_C(V, n, s.b, s.g, s.w);
     __syncthreads();
     const double* ekp = ekpump;
     for (int i = threadIdx.x; i < n; i += blockDim.x) {
-      const double u = s.g[i].x, du = s.c[i].x, d2u = s.e[i].x;
+      const double u = s.g[i].x, du = s.c[i].x, d2u = resid ? 0.0 : s.e[i].x;
       us[i] = make_double2(0.0, 0.0);
       up[i] = make_double2(u, 0.0);
       om[i] = make_double2(du + or1[i] * u, 0.0);
       psi[i] = make_double2(0.0, 0.0);
       if (wold) oP[i] = make_double2(u, 0.0);
       bad |= !isfinite(u);
-      if (calc)
+      if (resid)
+        iP[i] = make_double2((i == 0 || i == n - 1) ? 0.0 : iw * (u - s.a[i].x), 0.0);
+      else if (calc)
         iP[i] = make_double2(I.ViscFac * (d2u + or1[i] * du - or2[i] * u) - I.CorFac * ekp[i] * u, 0.0);
     }
   } else {
@@ -1152,19 +1174,28 @@ __device__ __forceinline__ void mloop_item(const PzDev& d, const PzItem it, int 
       us[i] = cscale(or1[i], cim(dm, p));
       up[i] = make_double2(-dp.x - beta[i] * p.x, -dp.y - beta[i] * p.y);
     }
-    op_Dc2(V, n, s.b, s.c, s.a, s.w);                                // dom, d2om
+    if (!resid_om) op_Dc2(V, n, s.b, s.c, s.a, s.w);                 // dom, d2om
     __syncthreads();
     op_C(V, n, s.b, s.k, s.w);                                       // om
     __syncthreads();
     for (int i = threadIdx.x; i < n; i += blockDim.x) {
-      const double2 o = s.k[i], d1 = s.c[i], d2 = s.a[i];
+      const double2 o = s.k[i];
       om[i] = o;
       if (wold) oP[i] = o;
       bad |= !isfinite(o.x) || !isfinite(o.y);
       if (calc) {
-        double2 v = make_double2(I.ViscFac * (d2.x + or1[i] * d1.x - dm2 * or2[i] * o.x),
-                                 I.ViscFac * (d2.y + or1[i] * d1.y - dm2 * or2[i] * o.y));
-        if (direct) v = cadd(v, smat_imp_extra(I, V, i, dm, o, up[i], us[i]));
+        double2 v;
+        if (resid_om) {
+          // s.a holds the right-hand side with the implicit buoyancy folded in,
+          // so (om - s.a)/w is every implicit term of the vorticity row but
+          // the buoyancy, which is added below
+          v = (i == 0 || i == n - 1) ? make_double2(0.0, 0.0) : cscale(iw, csub(o, s.a[i]));
+        } else {
+          const double2 d1 = s.c[i], d2 = s.a[i];
+          v = make_double2(I.ViscFac * (d2.x + or1[i] * d1.x - dm2 * or2[i] * o.x),
+                           I.ViscFac * (d2.y + or1[i] * d1.y - dm2 * or2[i] * o.y));
+          if (direct) v = cadd(v, smat_imp_extra(I, V, i, dm, o, up[i], us[i]));
+        }
         if (buo_imp) {
           const double2 b = cim(dm, s.f[i]);
           const double c = rgrav[i] * or1[i] * I.BuoFac;
