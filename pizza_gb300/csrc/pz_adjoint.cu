@@ -123,8 +123,10 @@ int adj_threads(int maxN) {
   const int t = 2 * maxN > 4 * h2 ? 2 * maxN : 4 * h2;
   return ((t + 31) / 32) * 32;
 }
-size_t adj_rloop_smem_bytes(int P) {
-  return 6 * (size_t)PZ_RLOOP_G * P * sizeof(double2) + PZ_RLOOP_G * sizeof(double);
+// G radii per block: the forward's k_rloop grouping (PzInst::rg), since both
+// walk the same (instance, radius) work list
+size_t adj_rloop_smem_bytes(int P, int G) {
+  return 6 * (size_t)G * P * sizeof(double2) + G * sizeof(double);
 }
 
 __device__ __forceinline__ double2 cz() { return make_double2(0.0, 0.0); }
@@ -372,7 +374,7 @@ __global__ void __launch_bounds__(256) k_adj_solve(PzAdjDev a, int n, int slot) 
   }
 }
 
-// NL^T for PZ_RLOOP_G radii: the adjoint of
+// NL^T for a group of PzInst::rg radii: the adjoint of
 //   A = fft(r us T), B = fft(up T), C = fft(r us om), D = fft(up om)
 //   ET = -(i m/r) B - tfac A,  EP = -(i m/r) D (m > 0),  EP(0) = -sum_m us_fluct om
 // with fft = rfft/P truncated to M and the grids from c2r of the spectra.
@@ -387,7 +389,7 @@ __global__ void __launch_bounds__(256) k_adj_rloop(PzAdjDev a, int slot) {
   const View V{&I, a.d.pool};
   const AdjView A = adj_view(a, inst);
   const int N = I.N, M = I.M, P = I.P;
-  const int G = min(PZ_RLOOP_G, N - r0);
+  const int G = min(I.rg, N - r0);
   const double2* tw = reinterpret_cast<const double2*>(V.pool + I.o_tw);
   double2* b0 = sh;
   double2* b1 = sh + 2 * G * P;
@@ -782,7 +784,7 @@ extern "C" int pz_adjoint_forward(pz_handle* h, int objective, int n_steps, int 
     const PzInst& I = h->inst[i];
     if (I.scheme != PZ_CNAB2 || (I.flags & PZF_DIRECT))
       return pz_fail(h, PZ_E_UNSUPPORTED, "pz_adjoint_forward: the adjoint covers CNAB2 with the influence-matrix solve");
-    if (adj_rloop_smem_bytes(I.P) > PZ_SMEM_MAX)
+    if (adj_rloop_smem_bytes(I.P, I.rg) > PZ_SMEM_MAX)
       return pz_fail(h, PZ_E_UNSUPPORTED, "pz_adjoint_forward: n_phi_max too large for the adjoint transform kernel");
   }
   cudaError_t e;
@@ -891,7 +893,9 @@ extern "C" int pz_adjoint_backward(pz_handle* h, double* dJ_dtemp, double* dJ_dr
   const int k0_last = (A->n_seg - 1) * K;
   const int threads = adj_threads(h->dev.maxN);
   const size_t smem = as_smem_bytes(h->dev.maxN);
-  const size_t rsmem = adj_rloop_smem_bytes(h->dev.maxP);
+  size_t rsmem = 0;
+  for (int i = 0; i < h->n_inst; ++i)
+    rsmem = std::max(rsmem, adj_rloop_smem_bytes(h->inst[i].P, h->inst[i].rg));
   if ((e = cudaFuncSetAttribute(k_adj_rloop, cudaFuncAttributeMaxDynamicSharedMemorySize, PZ_SMEM_MAX)))
     return acuda(h, e, "pz_adjoint_backward");
   k_adj_zero<<<h->dev.n_mitems, 64, 0, s>>>(a);

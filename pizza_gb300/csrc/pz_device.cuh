@@ -227,12 +227,12 @@ __device__ double2* fft_run(double2* a, double2* b, const PzInst& I, const doubl
 // the Courant steps of radius r).  The two real fields of each pair are packed
 // into one complex FFT (us + i up, om + i T on the way to the grid; the
 // products r us T + i up T and r us om + i up om on the way back).
-// Shared memory: 4*G*P complex (two ping-pong buffers of 2*G transforms) and
-// 3*G + G*M doubles.
+// G = min(gmax, N - r0) radii.  Shared memory: 4*G*P complex (two ping-pong
+// buffers of 2*G transforms) and 3*G + G*M doubles.
 template <class IO>
-__device__ void rloop_group(const PzInst& I, const View& V, int r0, IO& io, double2* sh, double* rsh) {
+__device__ void rloop_group(const PzInst& I, const View& V, int r0, int gmax, IO& io, double2* sh, double* rsh) {
   const int N = I.N, M = I.M, P = I.P;
-  const int G = min(PZ_RLOOP_G, N - r0);
+  const int G = min(gmax, N - r0);
   const double2* tw = reinterpret_cast<const double2*>(V.pool + I.o_tw);
   double2* za = sh;                  // [g][2][P]
   double2* zb = sh + 2 * G * P;

@@ -26,6 +26,7 @@ struct pz_handle {
   PzItem* d_ritems = nullptr;
   PzItem* d_mitems = nullptr;
   PzItem* d_order = nullptr;
+  int* d_iorder = nullptr;
   PzDev dev{};
   cudaStream_t stream = nullptr;
   cudaGraphExec_t graph = nullptr;

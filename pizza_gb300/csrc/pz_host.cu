@@ -457,6 +457,7 @@ extern "C" int pz_create(const pz_config* cfgs, int n, pz_handle** out) {
     I.N = c.n_r_max; I.n_max = c.n_cheb_max; I.mmax = c.m_max; I.minc = c.minc;
     I.M = c.m_max / c.minc + 1;                   // truncation.f90:28
     I.P = 3 * c.m_max / c.minc;                   // truncation.f90:30-31
+    I.rg = std::max(1, std::min(8, PZ_RLOOP_PG / I.P));
     factor_fft(I.P, I.radix, &I.nrad);
     double cf;
     int imp_calc;
@@ -715,13 +716,14 @@ extern "C" int pz_create(const pz_config* cfgs, int n, pz_handle** out) {
   });
   std::vector<PzItem> ritems, mitems;
   for (int i : order) {
-    for (int r = 0; r < h->inst[i].N; r += PZ_RLOOP_G) ritems.push_back({i, r});
+    for (int r = 0; r < h->inst[i].N; r += h->inst[i].rg) ritems.push_back({i, r});
     for (int m = 0; m < h->inst[i].M; ++m) mitems.push_back({i, m});
   }
   if ((e = cudaMalloc(&h->d_inst, n * sizeof(PzInst))) || (e = cudaMalloc(&h->d_state, n * sizeof(PzState))) ||
       (e = cudaMalloc(&h->d_ritems, ritems.size() * sizeof(PzItem))) ||
       (e = cudaMalloc(&h->d_mitems, mitems.size() * sizeof(PzItem))) ||
       (e = cudaMalloc(&h->d_order, mitems.size() * sizeof(PzItem))) ||
+      (e = cudaMalloc(&h->d_iorder, n * sizeof(int))) ||
       (e = cudaMalloc(&h->d_rows, (size_t)n * PZ_SERIES_COLS * sizeof(double)))) {
     g_create_error = std::string("device allocation: ") + cudaGetErrorString(e);
     pz_destroy(h);
@@ -730,6 +732,7 @@ extern "C" int pz_create(const pz_config* cfgs, int n, pz_handle** out) {
   cudaMemcpyAsync(h->d_inst, h->inst.data(), n * sizeof(PzInst), cudaMemcpyHostToDevice, h->stream);
   cudaMemcpyAsync(h->d_ritems, ritems.data(), ritems.size() * sizeof(PzItem), cudaMemcpyHostToDevice, h->stream);
   cudaMemcpyAsync(h->d_mitems, mitems.data(), mitems.size() * sizeof(PzItem), cudaMemcpyHostToDevice, h->stream);
+  cudaMemcpyAsync(h->d_iorder, order.data(), n * sizeof(int), cudaMemcpyHostToDevice, h->stream);
   cudaMemsetAsync(h->d_state, 0, n * sizeof(PzState), h->stream);
   h->dev.inst = h->d_inst;
   h->dev.state = h->d_state;
@@ -737,6 +740,7 @@ extern "C" int pz_create(const pz_config* cfgs, int n, pz_handle** out) {
   h->dev.ritems = h->d_ritems; h->dev.n_ritems = (int)ritems.size();
   h->dev.mitems = h->d_mitems; h->dev.n_mitems = (int)mitems.size();
   h->dev.order = h->d_order;
+  h->dev.iorder = h->d_iorder;
   h->dev.n_inst = n;
   h->dev.maxN = maxN; h->dev.maxP = maxP; h->dev.maxM = maxM;
   size_t sb = 0;
@@ -744,6 +748,10 @@ extern "C" int pz_create(const pz_config* cfgs, int n, pz_handle** out) {
     sb = std::max(sb, pz_build_smem_bytes(h->inst[i].N, (h->inst[i].flags & PZF_DIRECT) != 0,
                                           (h->inst[i].flags & PZF_INTEG) != 0));
   h->dev.smem_build = (int)sb;
+  size_t srl = 0;
+  for (int i = 0; i < n; ++i)
+    srl = std::max(srl, pz_rloop_smem_bytes(h->inst[i].P, h->inst[i].M, h->inst[i].rg));
+  h->dev.smem_rloop = (int)srl;
   // launch plan of one step: per stage k_rloop [k_cfl, k_build] k_mloop, then
   // the assembly stage and the time series (step_time.f90:139-406)
   int smax = 1;
@@ -1195,6 +1203,7 @@ extern "C" int pz_destroy(pz_handle* h) {
   cudaFree(h->d_ritems);
   cudaFree(h->d_mitems);
   cudaFree(h->d_order);
+  cudaFree(h->d_iorder);
   cudaFree(h->d_rows);
   if (h->stream) cudaStreamDestroy(h->stream);
   delete h;

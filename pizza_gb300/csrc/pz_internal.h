@@ -20,7 +20,9 @@
 
 #define PZ_MAX_RADIX 8
 #define PZ_SERIES_CAP 1024
-#define PZ_RLOOP_G 4        // radii per block of the phi-transform kernels
+#define PZ_RLOOP_G 4        // radii per block of the stage-level phi-transform kernels
+#define PZ_RLOOP_PG 576     // k_rloop: radii per block = clamp(PZ_RLOOP_PG / n_phi_max, 1, 8), so
+                            // that every block stages about the same 4*576 complex values
 #define PZ_SMEM_MAX (227 * 1024)
 #define PZ_MAX_STAGES 8     // DIRK stages
 #define PZ_BT_LD (PZ_MAX_STAGES + 1)
@@ -145,6 +147,7 @@ struct PzInst {
   long long o_series;       // PZ_SERIES_CAP*16
   long long o_integ;        // integration method: IM_COUNT*N*N (shared by equal N, radratio)
   int im_band[IM_COUNT];    // bandwidth of each IM_ operator (max |i-j| of a nonzero)
+  int rg;                   // radii per k_rloop block
   double rerr_thr;          // rerror_fac * epsilon with l_rerror_fix, else 0
 };
 
@@ -183,9 +186,12 @@ struct PzDev {
   const PzItem* ritems; int n_ritems;     // (inst, r)
   const PzItem* mitems; int n_mitems;     // (inst, m index)
   PzItem* order;                          // n_mitems: k_order's layout of the fused first stage
+  const int* iorder;                      // n_inst: instances in work-list order (their m items are
+                                          // contiguous in mitems, m ascending)
   int n_inst;
   int maxN, maxP, maxM;
   int smem_build;           // dynamic shared memory of k_build (bytes)
+  int smem_rloop;           // dynamic shared memory of k_rloop (bytes)
   // time-step schedule of the adjoint sweeps (null on the plain step):
   // sched_mode 1 takes dt of step k (0-based n_step) from dt_io[inst*sched_n + k]
   // instead of the Courant estimate, 2 records the chosen dt there; rec (if
@@ -213,6 +219,7 @@ cudaError_t pz_launch_obs(const PzDev& d, int only, cudaStream_t s);
 cudaError_t pz_launch_gather_rows(const PzDev& d, double* out, cudaStream_t s);
 cudaError_t pz_setup_kernels();
 size_t pz_build_smem_bytes(int n, bool direct, bool integ);   // k_build shared memory for one instance
+size_t pz_rloop_smem_bytes(int P, int M, int G);             // k_rloop shared memory, G radii per block
 
 // host: the integration-method operators of one (N, radratio), IM_COUNT
 // column-major N x N blocks, and their bandwidths (pz_integ_ops.cu)

@@ -190,8 +190,8 @@ __global__ void __launch_bounds__(256) k_rloop(PzDev d, int stage) {
   io.vsT = V.fld(F_DVST, 0);
   io.vsOm = V.fld(F_DVSOM, 0);
   io.cflv = d.pool + I.o_cfl;
-  double* rsh = reinterpret_cast<double*>(sh + 4 * PZ_RLOOP_G * I.P);
-  rloop_group(I, V, it.idx, io, sh, rsh);
+  double* rsh = reinterpret_cast<double*>(sh + 4 * I.rg * I.P);
+  rloop_group(I, V, it.idx, I.rg, io, sh, rsh);
 }
 
 // ---------------------------------------------------------------------------
@@ -1222,33 +1222,44 @@ __global__ void __launch_bounds__(256) k_mloop(PzDev d, int stage) { mloop_item(
 // largest-first order of the work list.
 // ---------------------------------------------------------------------------
 __global__ void __launch_bounds__(1024) k_order(PzDev d) {
-  __shared__ int sc[1024];
-  const int n = d.n_mitems, T = blockDim.x, t = threadIdx.x;
+  // one scan over the instances (in work-list order, where each instance's m
+  // items are contiguous): rebuilding items and all items before each one
+  __shared__ int sr[1024], sa[1024];
+  const int n = d.n_inst, T = blockDim.x, t = threadIdx.x;
   const int per = (n + T - 1) / T;
-  const int b0 = min(n, t * per), b1 = min(n, b0 + per);
-  auto rebuild = [&](const PzItem& it) {
-    const PzState& S = d.state[it.inst];
+  const int q0 = min(n, t * per), q1 = min(n, q0 + per);
+  auto rebuild = [&](int inst) {
+    const PzState& S = d.state[inst];
     return S.status == 0 && S.lMat != 0;
   };
-  int cnt = 0;
-  for (int b = b0; b < b1; ++b) cnt += rebuild(d.mitems[b]) ? 1 : 0;
-  sc[t] = cnt;
+  int reb = 0, all = 0;
+  for (int q = q0; q < q1; ++q) {
+    const int inst = d.iorder[q], M = d.inst[inst].M;
+    all += M;
+    if (rebuild(inst)) reb += M;
+  }
+  sr[t] = reb;
+  sa[t] = all;
   __syncthreads();
-  for (int off = 1; off < T; off <<= 1) {          // inclusive scan
-    const int v = t >= off ? sc[t - off] : 0;
+  for (int off = 1; off < T; off <<= 1) {          // inclusive scans
+    const int vr = t >= off ? sr[t - off] : 0, va = t >= off ? sa[t - off] : 0;
     __syncthreads();
-    sc[t] += v;
+    sr[t] += vr;
+    sa[t] += va;
     __syncthreads();
   }
-  const int n_reb = sc[T - 1], n_rest = n - n_reb;
-  int k = sc[t] - cnt;                              // rebuild items before b0
-  int j = b0 - k;                                   // other items before b0
-  for (int b = b0; b < b1; ++b) {
-    const PzItem it = d.mitems[b];
-    int pos;
-    if (rebuild(it)) { pos = k + min(3 * k, n_rest); ++k; }
-    else { pos = j + min(j / 3 + 1, n_reb); ++j; }
-    d.order[pos] = it;
+  const int n_reb = sr[T - 1], n_rest = d.n_mitems - n_reb;
+  int k = sr[t] - reb;                              // rebuilding items before this chunk
+  int j = (sa[t] - all) - k;                        // other items before this chunk
+  for (int q = q0; q < q1; ++q) {
+    const int inst = d.iorder[q], M = d.inst[inst].M;
+    const bool rb = rebuild(inst);
+    for (int m = 0; m < M; ++m) {
+      int pos;
+      if (rb) { pos = k + min(3 * k, n_rest); ++k; }
+      else { pos = j + min(j / 3 + 1, n_reb); ++j; }
+      d.order[pos] = PzItem{inst, m};
+    }
   }
 }
 
@@ -1518,9 +1529,13 @@ int mloop_threads(int maxN) {
   const int t = 2 * maxN > 4 * h2 ? 2 * maxN : 4 * h2;
   return ((t + 31) / 32) * 32;
 }
-size_t rloop_smem_bytes(int P, int M) {
-  return 4 * (size_t)PZ_RLOOP_G * P * sizeof(double2) + (3 + (size_t)M) * PZ_RLOOP_G * sizeof(double);
+}  // namespace
+
+size_t pz_rloop_smem_bytes(int P, int M, int G) {
+  return 4 * (size_t)G * P * sizeof(double2) + (3 + (size_t)M) * G * sizeof(double);
 }
+
+namespace {
 
 }  // namespace
 
@@ -1577,7 +1592,7 @@ cudaError_t pz_launch_gather_rows(const PzDev& d, double* out, cudaStream_t s) {
 
 cudaError_t pz_launch_step_kernel(const PzDev& d, int kind, int stage, cudaStream_t s) {
   switch (kind) {
-    case PZK_RLOOP: k_rloop<<<d.n_ritems, 256, rloop_smem_bytes(d.maxP, d.maxM), s>>>(d, stage); break;
+    case PZK_RLOOP: k_rloop<<<d.n_ritems, 256, d.smem_rloop, s>>>(d, stage); break;
     case PZK_CFL: k_cfl<<<d.n_inst, 32, 0, s>>>(d); break;
     case PZK_BUILD: k_build<<<d.n_mitems, PZ_THREADS, d.smem_build, s>>>(d); break;
     case PZK_MLOOP: k_mloop<<<d.n_mitems, mloop_threads(d.maxN), ms_smem_bytes(d.maxN), s>>>(d, stage); break;

@@ -45,7 +45,7 @@ __global__ void __launch_bounds__(256) k_expl_rloop(PzExplArgs a) {
   const View V{&I, a.pool};
   ExplIO io{&a, I.N, I.M};
   double* rsh = reinterpret_cast<double*>(sh + 4 * PZ_RLOOP_G * I.P);
-  rloop_group(I, V, blockIdx.x * PZ_RLOOP_G, io, sh, rsh);
+  rloop_group(I, V, blockIdx.x * PZ_RLOOP_G, PZ_RLOOP_G, io, sh, rsh);
 }
 
 // finish_exp_temp_coll and finish_exp_psi_coll_{dmat,smat} for one m
