@@ -282,11 +282,12 @@ int pz_set_ra(pz_handle* h, int inst, double ra);
  * as pz_create derives it for a grid (host only, no device needed):
  * `which` in 0..PZ_INTEG_OPS-1 selects I2[r f], I2[r^2 f], I2[f],
  * I2[r^2 f'' + r f'], I2[r^2 f'' + r f' - f], I4[r^3 f], I4[r^4 f], then
- * Q0, Q1 (intcheb4rmult4laplrot = Q0 + m^2 Q1) and S0, S1, S2
- * (intcheb4rmult4laplrot2 = S0 + m^2 S1 + m^4 S2); all times rnorm with the
+ * Q0, Q1 (intcheb4rmult4laplrot = Q0 + m^2 Q1), S0, S1, S2
+ * (intcheb4rmult4laplrot2 = S0 + m^2 S1 + m^4 S2) and P0, P1
+ * (intcheb2rmult2laplrot = -(P0 + m^2 P1)); all times rnorm with the
  * tau rows zero.  out: n_r_max^2 doubles, column-major; *bandwidth: max |i-j|
  * of a nonzero entry. */
-#define PZ_INTEG_OPS 12
+#define PZ_INTEG_OPS 14
 int pz_integ_operator(int n_r_max, double radratio, int which, double* out, int* bandwidth);
 
 int pz_destroy(pz_handle* h);

@@ -1,6 +1,7 @@
-"""pizza's Chebyshev-integration ("integ") method with the tau boundary rows
-and the direct (coupled) streamfunction solve: the oracle restatement of
-src/update_temp_integ.f90 and src/update_psi_integ_smat.f90 as called from
+"""pizza's Chebyshev-integration ("integ") method with the tau boundary rows:
+the oracle restatement of src/update_temp_integ.f90 with either the direct
+(coupled) streamfunction solve, src/update_psi_integ_smat.f90, or the
+influence-matrix solve, src/update_psi_integ_dmat.f90, as called from
 mloop.f90:84-100 and :209-226, step_time.f90:488-500 and
 init_fields.f90:54-258.
 
@@ -44,14 +45,41 @@ class IntegScheme:
         self.d2r_top = 4.0 / 3.0 * dn2 * (dn2 - 1.0)
         self.d2r_bot = self.d2r_top * sg
         self.d3top = 8.0 / 15.0 * dn2 * (dn2 - 1.0) * (dn2 - 4.0)    # update_psi_integ_smat.f90:1303-1306
+        # the influence-matrix top condition of the rotating rigid wall: the
+        # fourth x-derivative of T_n at x = 1 (update_psi_integ_dmat.f90:1381-1384)
+        self.d4top = 16.0 / 105.0 * dn2 * (dn2 - 1.0) * (dn2 - 4.0) * (dn2 - 9.0)
         mvec = pz.mvec
         rot = not d["l_non_rot"]
         vis = d["ViscFac"]
+        self.dmat = not pz.l_direct
         # d/dt operators (RHSI) and linear implicit operators (RHSIL) per m
-        # (update_temp_integ.f90:813-832; update_psi_integ_smat.f90:1631-1764)
+        # (update_temp_integ.f90:813-832; update_psi_integ_smat.f90:1631-1764;
+        # update_psi_integ_dmat.f90:1128-1210)
         self.t_rhsi = [ops.temp_lap(int(m)) for m in mvec]
         self.p_rhsi = [ops.i2r2.astype(complex)]
         self.p_rhsil = [vis * pz.hdif[0] * ops.uphi_lap + 0j]
+        self.tmats = None
+        self.pmats = None
+        if self.dmat:
+            # vorticity equation I2[r^2 .] (2 tau rows) and the dt-independent
+            # streamfunction operator from omega, psi_hat = -L_psi^-1 I2[r^2 om]
+            # with L_psi = intcheb2rmult2laplrot = -I2[r^2 omega(psi)]
+            # (update_psi_integ_dmat.f90:971-1089)
+            from .chebsparse import omega_rot_terms
+            self.psi_ops = [None]
+            for i in range(1, len(mvec)):
+                m = int(mvec[i])
+                self.p_rhsi.append(ops.i2r2 + 0j)
+                self.p_rhsil.append(vis * pz.hdif[i] * ops.temp_lap(m) + 0j)
+                if rot:
+                    L = -ops._rows(ops.c.integrated(omega_rot_terms(ops.ro, float(m)), 2), 2)
+                else:
+                    L = ops.temp_lap(m)
+                L = L.copy()
+                L[0] = self.rnorm * self.r_top
+                L[1] = self.rnorm * self.r_bot
+                self.psi_ops.append(self._finish_lhs(L, 2))
+            return
         for i in range(1, len(mvec)):
             m = int(mvec[i])
             if rot:
@@ -63,8 +91,6 @@ class IntegScheme:
                 self.p_rhsi.append(-ops.psi_nonrot(m) + 0j)
                 L = -vis * pz.hdif[i] * ops.psi_nonrot2(m) + 0j
             self.p_rhsil.append(L)
-        self.tmats = None
-        self.pmats = None
 
     # -- left-hand sides (get_lhs_mat_tau) ----------------------------------
     def _finish_lhs(self, A, ntau):
@@ -87,13 +113,20 @@ class IntegScheme:
 
     def _psi_lhs(self, i):
         """update_psi_integ_smat.f90:1286-1581: LHS = RHSI - wimp RHSIL with
-        the 2 (m = 0) or 4 tau rows."""
+        the 2 (m = 0) or 4 tau rows; influence-matrix variant
+        (update_psi_integ_dmat.f90:783-969): the vorticity operator with 2 tau
+        rows, omega(r_o) and omega(r_i) for m > 0."""
         pz, p, d = self.pz, self.pz.p, self.pz.d
         w = pz.ts.wimp_lin[0]
         or1 = pz.or1
         N = pz.N
         A = self.p_rhsi[i] - w * self.p_rhsil[i]
         rn = self.rnorm
+        if self.dmat and i > 0:
+            A = A.real.copy()
+            A[0] = rn * self.r_top
+            A[1] = rn * self.r_bot
+            return self._finish_lhs(A, 2)
         if i == 0:
             A = A.real.copy()
             A[0] = rn * ((self.dr_top - or1[0] * self.r_top) if p.ktopv == 1 else self.r_top)
@@ -117,6 +150,59 @@ class IntegScheme:
         M = self.pz.M
         self.tmats = [self._temp_lhs(i) for i in range(M)]
         self.pmats = [self._psi_lhs(i) for i in range(M)]
+        if self.dmat:
+            self._intermediate()
+
+    def _psi_from_om(self, i, om_hat):
+        """psi_hat from omega_hat (update_psi_integ_dmat.f90:310-327)."""
+        rhs = -(self.ops.i2r2 @ om_hat)
+        rhs[:2] = 0.0
+        return self._solve(self.psi_ops[i], rhs)
+
+    def _bc_sums(self, psi_hat):
+        """get_bc_influence_matrix (update_psi_integ_dmat.f90:1361-1530):
+        the two conditions left to the influence matrix, on Chebyshev
+        coefficients with the half weight at both ends."""
+        pz, p = self.pz, self.pz.p
+        N = pz.N
+        fac = np.ones(N)
+        fac[0] = fac[N - 1] = pz.cheb.boundary_fac
+        if p.ktopv == 1:
+            top = self.d2r_top - pz.or1[0] * self.dr_top
+        elif pz.d["l_non_rot"]:
+            top = self.dr_top
+        else:
+            top = self.d4top
+        if p.kbotv == 1:
+            bot = self.d2r_bot - pz.or1[N - 1] * self.dr_bot
+        else:
+            bot = self.dr_bot
+        t = b = 0.0
+        for n in range(N):            # sequential sums as in the reference
+            t = t + fac[n] * top[n] * psi_hat[..., n]
+            b = b + fac[n] * bot[n] * psi_hat[..., n]
+        return self.rnorm * t, self.rnorm * b
+
+    def _intermediate(self):
+        """get_intermediate_sol and get_influence_matrix
+        (update_psi_integ_dmat.f90:1212-1313): the homogeneous solutions with
+        omega = 1 on the inner (set 1) or outer (set 2) wall."""
+        pz = self.pz
+        M, N = pz.M, pz.N
+        self.om23 = np.zeros((M, 2, N))
+        self.psi23 = np.zeros((M, 2, N))
+        self.infl = np.zeros((M, 2, 2))
+        for i in range(1, M):
+            for k, row in enumerate((1, 0)):
+                rhs = np.zeros(N)
+                rhs[row] = 1.0
+                om = self._solve(self.pmats[i], rhs).real
+                self.om23[i, k] = om
+                self.psi23[i, k] = self._psi_from_om(i, om).real
+            t2, b2 = self._bc_sums(self.psi23[i, 0])
+            t3, b3 = self._bc_sums(self.psi23[i, 1])
+            det = t2 * b3 - t3 * b2
+            self.infl[i] = [[b3 / det, -t3 / det], [-b2 / det, t2 / det]]
 
     @staticmethod
     def _solve(lu_fac, rhs):
@@ -165,12 +251,28 @@ class IntegScheme:
         e = c.costf1(e - work)
         e[:, n_max:] = 0.0
         pz.dTdt.expl[ist] = e @ self.ops.i2r1.T
-        # finish_exp_psi_int_smat (update_psi_integ_smat.f90:793-958)
         w = c.costf1(dVsOm)
         w[:, n_max:] = 0.0
         work = c.get_dr(w, l_dct_in=False)
         e = pz.dpsidt.expl[ist].copy()
         nz = slice(1, None)
+        if self.dmat:
+            # finish_exp_psi_int_dmat (update_psi_integ_dmat.f90:486-623)
+            e[nz] = e[nz] - pz.or1 * work[nz]
+            if not d["l_non_rot"]:
+                e[nz] = e[nz] - d["CorFac"] * 1j * m[nz] * pz.psi[nz]
+            if not d["l_buo_imp"]:
+                e[nz] = e[nz] - d["BuoFac"] * pz.rgrav * pz.or1 * 1j * m[nz] * pz.temp[nz]
+            if pz.p.l_ek_pump:
+                ekp = d["CorFac"] * pz.ekpump
+                e[0] = e[0] - ekp * pz.up[0]
+                e[nz] = e[nz] - ekp * (pz.om[nz] + pz.ekp_up * pz.up[nz]
+                                       + (1j * m[nz] * pz.ekp_dusdp + pz.ekp_us) * pz.us[nz])
+            e = c.costf1(e)
+            e[:, n_max:] = 0.0
+            pz.dpsidt.expl[ist] = e @ self.ops.i2r2.T
+            return
+        # finish_exp_psi_int_smat (update_psi_integ_smat.f90:793-958)
         e[nz] = r * e[nz]
         if not d["l_coriolis_imp"]:
             e[nz] = e[nz] - d["CorFac"] * 1j * m[nz] * r * pz.psi[nz]
@@ -203,23 +305,32 @@ class IntegScheme:
             pz.dTdt.impl[istage - 1] = imp
 
     def _buo_coeffs(self):
-        """I4 r^4 of the buoyancy -BuoFac rgrav/r i m T, m > 0, in Chebyshev
-        space (update_psi_integ_smat.f90:266-330, :1075-1111)."""
+        """I4 r^4 (I2 r^2 with the influence-matrix variant) of the buoyancy
+        -BuoFac rgrav/r i m T, m > 0, in Chebyshev space
+        (update_psi_integ_smat.f90:266-330, :1075-1111;
+        update_psi_integ_dmat.f90:171-240, :748-779)."""
         pz, d = self.pz, self.pz.d
         m = pz.mvec[:, None].astype(float)
         buo = -d["BuoFac"] * pz.rgrav * pz.or1 * 1j * m * pz.temp
         buo[0] = 0.0
         buo = pz.cheb.costf1(buo)
-        out = buo @ self.ops.i4r4.T
+        out = buo @ (self.ops.i2r2 if self.dmat else self.ops.i4r4).T
         out[0] = 0.0
         return out
 
     def psi_rhs_imp(self, istage, l_calc_lin):
-        """get_psi_rhs_imp_int_smat (update_psi_integ_smat.f90:960-1115)."""
+        """get_psi_rhs_imp_int_smat (update_psi_integ_smat.f90:960-1115) or
+        get_psi_rhs_imp_int_dmat (update_psi_integ_dmat.f90:625-781), which
+        works on omega (u_phi for m = 0) instead of psi_hat."""
         pz, d = self.pz, self.pz.d
-        work_r = pz.cheb.costf1_real(pz.up[0].real)
-        src = pz.psi_hat.copy()
-        src[0] = work_r
+        if self.dmat:
+            work = pz.om.copy()
+            work[0] = pz.up[0]
+            src = pz.cheb.costf1(work)
+        else:
+            work_r = pz.cheb.costf1_real(pz.up[0].real)
+            src = pz.psi_hat.copy()
+            src[0] = work_r
         if istage == 1:
             old = np.empty_like(src)
             for i in range(pz.M):
@@ -256,6 +367,8 @@ class IntegScheme:
 
     def update_psi(self):
         """update_psi_int_smat (update_psi_integ_smat.f90:247-573)."""
+        if self.dmat:
+            return self._update_psi_dmat()
         pz, ts, c, d = self.pz, self.pz.ts, self.pz.cheb, self.pz.d
         N, M = pz.N, pz.M
         buo = self._buo_coeffs() if d["l_buo_imp"] else None
@@ -288,6 +401,55 @@ class IntegScheme:
         us[0] = 0.0
         up[0] = uphi0
         om[0] = om0 + or1 * uphi0
+        pz.psi, pz.us, pz.up, pz.om = psi, us, up, om
+        ts.rotate_imex(pz.dpsidt)
+        if ts.istage == ts.nstages:
+            self.psi_rhs_imp(1, pz._calc_rhs(1))
+        else:
+            self.psi_rhs_imp(ts.istage + 1, pz._calc_rhs(ts.istage + 1))
+
+    def _update_psi_dmat(self):
+        """update_psi_int_dmat (update_psi_integ_dmat.f90:150-484): omega from
+        its own solve with omega = 0 on the walls, psi from omega, then the
+        influence-matrix combination of the two homogeneous solutions that
+        imposes the remaining wall conditions on psi."""
+        pz, ts, c, d = self.pz, self.pz.ts, self.pz.cheb, self.pz.d
+        M = pz.M
+        buo = self._buo_coeffs() if d["l_buo_imp"] else None
+        work = ts.set_imex_rhs(pz.dpsidt)
+        if buo is not None:
+            work[1:] = work[1:] + ts.wimp_lin[0] * buo[1:]
+        uphi0 = self._solve(self.pmats[0], work[0]).real
+        om_hat = np.zeros_like(work)
+        psi_hat = np.zeros_like(work)
+        for i in range(1, M):
+            om_hat[i] = self._solve(self.pmats[i], work[i])
+            psi_hat[i] = self._psi_from_om(i, om_hat[i])
+            t1, b1 = self._bc_sums(psi_hat[i])
+            inf = self.infl[i]
+            c1 = -inf[0, 0] * t1 - inf[0, 1] * b1
+            c2 = -inf[1, 0] * t1 - inf[1, 1] * b1
+            psi_hat[i] = psi_hat[i] + c1 * self.psi23[i, 0] + c2 * self.psi23[i, 1]
+            om_hat[i] = om_hat[i] + c1 * self.om23[i, 0] + c2 * self.om23[i, 1]
+        om0 = c.get_dr_real(uphi0, l_dct=False)
+        uphi0 = c.costf1_real(uphi0)
+        dpsi = c.get_dr(psi_hat, l_dct_in=False)
+        psi = c.costf1(psi_hat)
+        om = c.costf1(om_hat)
+        r, or1 = pz.r, pz.or1
+        m = pz.mvec[:, None].astype(float)
+        if d["l_non_rot"]:
+            us = 1j * m * or1 * psi
+            up = -dpsi
+        else:
+            h2 = d["r_cmb"] ** 2 - r * r
+            us = 1j * m * or1 * h2 * psi
+            up = -h2 * dpsi + 3.0 * r * psi
+        psi[0] = 0.0
+        us[0] = 0.0
+        up[0] = uphi0
+        om[0] = om0 + or1 * uphi0
+        pz.psi_hat = psi_hat
         pz.psi, pz.us, pz.up, pz.om = psi, us, up, om
         ts.rotate_imex(pz.dpsidt)
         if ts.istage == ts.nstages:

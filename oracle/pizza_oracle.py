@@ -825,8 +825,6 @@ class Pizza:
         self.temp_hat = np.zeros(shp, complex)
         self.psi_hat = np.zeros(shp, complex)
         if self.l_integ:
-            if not self.l_direct:
-                raise NotImplementedError("integ with the influence-matrix solve is not restated")
             from .pizza_integ import IntegScheme
             self.integ = IntegScheme(self)
 

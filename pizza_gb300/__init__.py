@@ -186,7 +186,7 @@ def load_library(path: str | None = None):
     return lib
 
 
-INTEG_OPERATORS = ("I2R1", "I2R2", "I2", "LT0", "ULAP", "I4R3", "I4R4", "Q0", "Q1", "S0", "S1", "S2")
+INTEG_OPERATORS = ("I2R1", "I2R2", "I2", "LT0", "ULAP", "I4R3", "I4R4", "Q0", "Q1", "S0", "S1", "S2", "P0", "P1")
 
 
 def integ_operator(n_r_max: int, radratio: float, name: str):

@@ -385,9 +385,8 @@ int validate(const pz_config& c, std::string* why) {
   if (c.l_rerror_fix && c.cheb_method != PZ_CHEB_INTEG)
     return uns("l_rerror_fix is implemented for cheb_method 'integ' (the collocation m = 0 recursions take no threshold)");
   if (c.cheb_method == PZ_CHEB_INTEG) {
-    if (c.matrix_solve != PZ_SOLVE_DIRECT)
-      return uns("cheb_method 'integ' is implemented with matrix_solve 'DIRECT' (update_psi_integ_smat)");
-    if (c.l_non_rot || c.ek < 0.0) return uns("cheb_method 'integ' is implemented for rotating runs");
+    if (c.matrix_solve == PZ_SOLVE_DIRECT && (c.l_non_rot || c.ek < 0.0))
+      return uns("cheb_method 'integ' with matrix_solve 'DIRECT' is implemented for rotating runs");
     if (pz_build_smem_bytes(c.n_r_max, true, true) > PZ_SMEM_MAX)
       return uns("cheb_method 'integ' needs n_r_max <= 118 (the operator build is staged in shared memory)");
     DirkTab t;
@@ -499,7 +498,7 @@ extern "C" int pz_create(const pz_config* cfgs, int n, pz_handle** out) {
     // get_tempMat and get_omMat (update_temp_coll.f90:310-393,
     // update_psi_coll_dmat.f90:829-911) build the same rows when
     // TdiffFac*hdif_T == ViscFac*hdif_V and both use fixed/no-slip boundary rows
-    if (!direct && I.TdiffFac == I.ViscFac) I.flags |= PZF_T_IS_OM;
+    if (!direct && c.cheb_method != PZ_CHEB_INTEG && I.TdiffFac == I.ViscFac) I.flags |= PZF_T_IS_OM;
     if (c.cheb_method == PZ_CHEB_INTEG) I.flags |= PZF_INTEG;
     if (c.l_rerror_fix) {   // radial_derivatives.f90:51-66
       I.flags |= PZF_RERR;
@@ -622,7 +621,7 @@ extern "C" int pz_create(const pz_config* cfgs, int n, pz_handle** out) {
     const long long N = I.N, M = I.M;
     I.o_gt = take(M * N * N);
     I.o_guphi = take(N * N);
-    if (I.flags & PZF_INTEG) {
+    if ((I.flags & PZF_INTEG) && (I.flags & PZF_DIRECT)) {
       I.o_gsm = take(2 * M * N * N);      // complex N x N streamfunction inverse per m
       I.o_gom = I.o_gpsi = I.o_aux = 0;
     } else if (I.flags & PZF_DIRECT) {

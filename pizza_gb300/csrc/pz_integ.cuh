@@ -124,6 +124,69 @@ __device__ void ddcheb_thr(const double2* c, double2* df, double2* ddf, int n, d
   __syncthreads();
 }
 
+// -- influence-matrix variant (update_psi_integ_dmat.f90) -----------------------
+// The two wall conditions left to the influence matrix, as weights on the
+// Chebyshev coefficients of psi (get_bc_influence_matrix, :1361-1530): top
+// d4psi/dx4 (rotating, rigid) or dpsi/dr (non-rotating, rigid), bottom
+// dpsi/dr; half weight at both ends; times rnorm.
+__device__ __forceinline__ double dmat_bc_top(const PzInst& I, int j) {
+  const double dn2 = (double)j * (double)j;
+  const double f = (j == 0 || j == I.N - 1) ? 0.5 : 1.0;
+  const double v = (I.flags & PZF_NON_ROT) ? 2.0 * dn2
+                                           : 16.0 / 105.0 * dn2 * (dn2 - 1.0) * (dn2 - 4.0) * (dn2 - 9.0);
+  return I.rnorm * f * v;
+}
+__device__ __forceinline__ double dmat_bc_bot(const PzInst& I, int j) {
+  const double dn2 = (double)j * (double)j;
+  const double f = (j == 0 || j == I.N - 1) ? 0.5 : 1.0;
+  return I.rnorm * f * (-2.0 * dn2 * ((j & 1) ? -1.0 : 1.0));
+}
+
+// dt-independent streamfunction-from-vorticity inverse for one m > 0
+// (get_lhs_psi_mat, update_psi_integ_dmat.f90:971-1089): intcheb2rmult2laplrot
+// = -I2[r^2 omega(psi)] = -(P0 + m^2 P1) (I2[r^2 Lap_m] = LT0 - m^2 I2 without
+// rotation), tau rows psi(r_o) = psi(r_i) = 0, row preconditioning; stored as
+// G_psi = A_s^-1 diag(fac) at o_gpsi.  Shared memory: the BuildSmem layout.
+__device__ int integ_psi_static(const PzDev& d, const PzInst& I, const View& V, int mi) {
+  extern __shared__ double shb[];
+  const int n = I.N, m = mi * I.minc;
+  const double dm2 = (double)m * (double)m, rn = I.rnorm;
+  const bool rot = !(I.flags & PZF_NON_ROT);
+  double* A = shb;
+  double* f1 = A + (long long)n * n;
+  double* colk = f1 + n + n;
+  double* red = colk + n;
+  int* redi = reinterpret_cast<int*>(red + 32);
+  int* piv = redi + 32;
+  const double* L0 = im_op(V, rot ? IM_P0 : IM_LT0);
+  const double* L1 = im_op(V, rot ? IM_P1 : IM_I2);
+  const double s0 = rot ? -1.0 : 1.0, s1 = -dm2;
+  for (int idx = threadIdx.x; idx < n * n; idx += blockDim.x) {
+    const int i = idx / n, j = idx - i * n;
+    double v;
+    if (i < 2) {
+      v = rn * ((i == 1 && (j & 1)) ? -1.0 : 1.0);
+      if (j == 0) v *= 0.5;
+    } else {
+      const long long c = i + (long long)j * n;
+      v = s0 * L0[c] + s1 * L1[c];
+    }
+    A[idx] = v;
+  }
+  __syncthreads();
+  for (int i = threadIdx.x; i < n; i += blockDim.x) {
+    double mx = 0.0;
+    for (int j = 0; j < n; ++j) mx = fmax(mx, fabs(A[i * n + j]));
+    f1[i] = 1.0 / mx;
+  }
+  __syncthreads();
+  for (int idx = threadIdx.x; idx < n * n; idx += blockDim.x) A[idx] *= f1[idx / n];
+  __syncthreads();
+  if (gj_invert(A, n, piv, colk, red, redi) != 0) return -1;
+  store_op(d.pool + I.o_gpsi + (long long)mi * n * n, A, n, n, nullptr, f1);
+  return 0;
+}
+
 // -- dt dependent left-hand sides (get_lhs_mat_tau) ----------------------------
 // k_build for one m of an integ instance: the temperature operator
 // (update_temp_integ.f90:631-776), the m = 0 u_phi operator or the m /= 0
@@ -145,14 +208,16 @@ __device__ int integ_build(const PzDev& d, const PzInst& I, const View& V, int m
   int* redi = reinterpret_cast<int*>(red + 32);
   int* piv = redi + 32;
   const double* I2R2 = im_op(V, IM_I2R2);
+  const bool dmat = !(I.flags & PZF_DIRECT);
   for (int pass = 0; pass < 2; ++pass) {
-    // pass 0: temperature; pass 1: u_phi (m = 0) -- the m /= 0 streamfunction
-    // operator is complex and built below
-    if (pass == 1 && m != 0) break;
-    const double* L0 = im_op(V, pass == 0 ? IM_LT0 : IM_ULAP);
+    // pass 0: temperature; pass 1: u_phi (m = 0) or, with the influence
+    // matrix, the vorticity operator (m /= 0, tau rows omega(r_o), omega(r_i));
+    // the direct solve's m /= 0 streamfunction operator is complex and built below
+    if (pass == 1 && m != 0 && !dmat) break;
+    const double* L0 = im_op(V, (pass == 0 || m != 0) ? IM_LT0 : IM_ULAP);
     const double* L1 = im_op(V, IM_I2);
     const double c0 = wlin * (pass == 0 ? I.TdiffFac : I.ViscFac);
-    const double c1 = pass == 0 ? -dm2 * c0 : 0.0;
+    const double c1 = (pass == 0 || m != 0) ? -dm2 * c0 : 0.0;
     for (int idx = threadIdx.x; idx < n * n; idx += blockDim.x) {
       const int i = idx / n, j = idx - i * n;
       double v;
@@ -176,11 +241,48 @@ __device__ int integ_build(const PzDev& d, const PzInst& I, const View& V, int m
     for (int idx = threadIdx.x; idx < n * n; idx += blockDim.x) A[idx] *= f1[idx / n];
     __syncthreads();
     if (gj_invert(A, n, piv, colk, red, redi) != 0) return -1;
-    double* G = d.pool + (pass == 0 ? I.o_gt + (long long)mi * n * n : I.o_guphi);
+    double* G = d.pool + (pass == 0 ? I.o_gt + (long long)mi * n * n
+                                    : (m == 0 ? I.o_guphi : I.o_gom + (long long)mi * n * n));
     store_op(G, A, n, n, nullptr, f1);
     __syncthreads();
   }
   if (m == 0) return 0;
+  if (dmat) {
+    // get_intermediate_sol + get_influence_matrix (update_psi_integ_dmat.f90:1212-1313):
+    // omega = 1 on the inner (set 1: om2, psi2) or outer (set 2: om3, psi3)
+    // wall, packed as the real and imaginary parts of one complex vector
+    const double* Gom = d.pool + I.o_gom + (long long)mi * n * n;
+    double2* va = reinterpret_cast<double2*>(shb);
+    double2* vb = va + n;
+    double2* vc = vb + n;
+    for (int i = threadIdx.x; i < n; i += blockDim.x)
+      va[i] = make_double2(Gom[i + (long long)1 * n], Gom[i]);     // columns 1 and 0
+    __syncthreads();
+    band_mv(band1(V, IM_I2R2, -1.0), n, va, vb);
+    __syncthreads();
+    mv_lanes(d.pool + I.o_gpsi + (long long)mi * n * n, n, vb, vc);
+    __syncthreads();
+    double* aux = d.pool + I.o_aux;
+    const long long MN = (long long)I.M * n;
+    double t2 = 0.0, t3 = 0.0, b2 = 0.0, b3 = 0.0;
+    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+      aux[0 * MN + (long long)mi * n + i] = va[i].x;
+      aux[1 * MN + (long long)mi * n + i] = va[i].y;
+      aux[2 * MN + (long long)mi * n + i] = vc[i].x;
+      aux[3 * MN + (long long)mi * n + i] = vc[i].y;
+      const double ct = dmat_bc_top(I, i), cb = dmat_bc_bot(I, i);
+      t2 += ct * vc[i].x; t3 += ct * vc[i].y;
+      b2 += cb * vc[i].x; b3 += cb * vc[i].y;
+    }
+    t2 = block_sum(t2, red); t3 = block_sum(t3, red);
+    b2 = block_sum(b2, red); b3 = block_sum(b3, red);
+    if (threadIdx.x == 0) {
+      double* infl = aux + 4 * MN + 4LL * mi;
+      const double det = t2 * b3 - t3 * b2;
+      infl[0] = b3 / det; infl[1] = -t3 / det; infl[2] = -b2 / det; infl[3] = t2 / det;
+    }
+    return 0;
+  }
   // streamfunction, m /= 0: Q0 + m^2 Q1 - wlin ViscFac (S0 + m^2 S1 + m^4 S2)
   // + i wlin CorFac m I4R4 (implicit Coriolis), tau rows psi(r_o) = psi(r_i) = 0,
   // d3psi/dx3(r_o) = 0 (rigid, rotating) and dpsi/dr(r_i) = 0
@@ -276,15 +378,31 @@ __device__ void integ_imp(const View& V, const PzInst& I, int mi, int bo, int bi
     }
     __syncthreads();
   }
+  const bool dmat = !(I.flags & PZF_DIRECT);
+  const double2* om = V.fld(F_OM, mi);
   for (int i = threadIdx.x; i < n; i += blockDim.x) {
-    s.a[i] = psi[i];
+    // the influence-matrix variant works on omega (get_psi_rhs_imp_int_dmat,
+    // update_psi_integ_dmat.f90:625-781), the direct solve on psi
+    s.a[i] = dmat ? om[i] : psi[i];
     s.e[i] = cscale(-I.BuoFac * rgrav[i] * or1[i], cim(dm, T[i]));
   }
   __syncthreads();
-  op_C(V, n, s.a, s.b, s.w);                                     // psi_hat
+  op_C(V, n, s.a, s.b, s.w);                                     // omega_hat or psi_hat
   __syncthreads();
   op_C(V, n, s.e, s.f, s.w);                                     // buoyancy, Chebyshev
   __syncthreads();
+  if (dmat) {
+    band_mv(band1(V, IM_I2R2), n, s.b, oP);
+    if (calc) {
+      band_mv(band_tlap(V, dm2, I.ViscFac), n, s.b, s.c);
+      band_mv(band1(V, IM_I2R2), n, s.f, s.h);
+      __syncthreads();
+      for (int i = threadIdx.x; i < n; i += blockDim.x)
+        iP[i] = (I.flags & PZF_BUO_IMP) ? cadd(s.c[i], s.h[i]) : s.c[i];
+    }
+    __syncthreads();
+    return;
+  }
   band_mv(band_rot(V, dm2), n, s.b, oP);
   if (calc) {
     band_mv(band_rot2(V, dm2, I.ViscFac), n, s.b, s.c);
@@ -316,6 +434,95 @@ __device__ __forceinline__ void trunc_cheb(double2* x, int n, int n_max) {
   for (int i = n_max + threadIdx.x; i < n; i += blockDim.x) x[i] = make_double2(0.0, 0.0);
 }
 
+// update_psi_int_dmat, m /= 0 (update_psi_integ_dmat.f90:150-484), after the
+// temperature: s.e holds I2R2 C(buoyancy) when the buoyancy is implicit.
+// omega_hat = G_om rhs with omega = 0 on the walls, psi_hat = -G_psi I2R2
+// omega_hat, then the influence matrix adds c1 (om2, psi2) + c2 (om3, psi3)
+// so that the two remaining wall conditions on psi hold.
+__device__ bool integ_dmat_psi(const PzDev& d, const View& V, const PzInst& I, const PzState& S, int mi,
+                               const IntegStage& c, MS& s) {
+  const int n = I.N, m = mi * I.minc;
+  const double dm = (double)m, dm2 = dm * dm;
+  const double rc2 = I.r_cmb * I.r_cmb;
+  const bool rot = !(I.flags & PZF_NON_ROT);
+  const bool buo_imp = (I.flags & PZF_BUO_IMP) != 0;
+  const double* r = V.rad(RV_R);
+  const double* or1 = V.rad(RV_OR1);
+  double2* us = V.fld(F_US, mi);
+  double2* up = V.fld(F_UP, mi);
+  double2* om = V.fld(F_OM, mi);
+  double2* psi = V.fld(F_PSI, mi);
+  for (int i = threadIdx.x; i < n; i += blockDim.x) {
+    double2 v = c.dirk ? dirk_rhs(V, I, S, 1, mi, i, c.stage) : imex_rhs(V, I, S, 1, mi, i);
+    if (buo_imp) v = cadd(v, cscale(S.wimp_lin[0], s.e[i]));
+    s.a[i] = v;
+    s.k[i] = buo_imp ? s.e[i] : make_double2(0.0, 0.0);
+  }
+  __syncthreads();
+  mv_lanes(d.pool + I.o_gom + (long long)mi * n * n, n, s.a, s.b);      // omega_hat
+  __syncthreads();
+  band_mv(band1(V, IM_I2R2, -1.0), n, s.b, s.c);
+  __syncthreads();
+  mv_lanes(d.pool + I.o_gpsi + (long long)mi * n * n, n, s.c, s.e);     // psi_hat, particular
+  __syncthreads();
+  double tr = 0.0, ti = 0.0, br = 0.0, bi = 0.0;
+  for (int i = threadIdx.x; i < n; i += blockDim.x) {
+    const double ct = dmat_bc_top(I, i), cb = dmat_bc_bot(I, i);
+    tr += ct * s.e[i].x; ti += ct * s.e[i].y;
+    br += cb * s.e[i].x; bi += cb * s.e[i].y;
+  }
+  tr = block_sum(tr, s.red); ti = block_sum(ti, s.red);
+  br = block_sum(br, s.red); bi = block_sum(bi, s.red);
+  const long long MN = (long long)I.M * n;
+  const double* aux = d.pool + I.o_aux;
+  const double* infl = aux + 4 * MN + 4LL * mi;
+  const double c1r = -infl[0] * tr - infl[1] * br, c1i = -infl[0] * ti - infl[1] * bi;
+  const double c2r = -infl[2] * tr - infl[3] * br, c2i = -infl[2] * ti - infl[3] * bi;
+  const double* om2 = aux + 0 * MN + (long long)mi * n;
+  const double* om3 = aux + 1 * MN + (long long)mi * n;
+  const double* psi2 = aux + 2 * MN + (long long)mi * n;
+  const double* psi3 = aux + 3 * MN + (long long)mi * n;
+  for (int i = threadIdx.x; i < n; i += blockDim.x) {
+    double2 p = s.e[i], o = s.b[i];
+    p.x += c1r * psi2[i] + c2r * psi3[i]; p.y += c1i * psi2[i] + c2i * psi3[i];
+    o.x += c1r * om2[i] + c2r * om3[i];   o.y += c1i * om2[i] + c2i * om3[i];
+    s.e[i] = p;
+    s.b[i] = o;
+  }
+  __syncthreads();
+  op_C(V, n, s.e, s.h, s.w);                                     // psi
+  __syncthreads();
+  op_D1c(V, n, s.e, s.c, s.w);                                   // dpsi/dr
+  __syncthreads();
+  op_C(V, n, s.b, s.g, s.w);                                     // omega
+  __syncthreads();
+  bool bad = false;
+  for (int i = threadIdx.x; i < n; i += blockDim.x) {
+    const double2 p = s.h[i], dp = s.c[i], o = s.g[i];
+    psi[i] = p;
+    if (rot) {
+      const double h2 = rc2 - r[i] * r[i];
+      us[i] = cscale(or1[i] * h2, cim(dm, p));
+      up[i] = make_double2(-h2 * dp.x + 3.0 * r[i] * p.x, -h2 * dp.y + 3.0 * r[i] * p.y);
+    } else {
+      us[i] = cscale(or1[i], cim(dm, p));
+      up[i] = make_double2(-dp.x, -dp.y);
+    }
+    om[i] = o;
+    bad |= !isfinite(o.x) || !isfinite(o.y) || !isfinite(p.x) || !isfinite(p.y);
+  }
+  // next-stage terms from omega_hat: I2R2 and ViscFac I2[r^2 Lap_m], plus the
+  // implicit buoyancy (s.k)
+  if (c.wold) band_mv(band1(V, IM_I2R2), n, s.b, V.hist(1, 0, c.oslot, mi));
+  if (c.calc) {
+    band_mv(band_tlap(V, dm2, I.ViscFac), n, s.b, s.a);
+    __syncthreads();
+    double2* iP = V.hist(1, 1, c.islot, mi);
+    for (int i = threadIdx.x; i < n; i += blockDim.x) iP[i] = cadd(s.a[i], s.k[i]);
+  }
+  return bad;
+}
+
 __device__ bool integ_stage(const PzDev& d, const View& V, const PzInst& I, const PzState& S, int mi,
                             const IntegStage& c, MS& s) {
   const int n = I.N, m = mi * I.minc, n_max = I.n_max;
@@ -340,6 +547,7 @@ __device__ bool integ_stage(const PzDev& d, const View& V, const PzInst& I, cons
   double2* dT = V.fld(F_DTEMP, mi);
   const bool buo_imp = (I.flags & PZF_BUO_IMP) != 0;
   const bool cor_imp = (I.flags & PZF_COR_IMP) != 0;
+  const bool dmat = !(I.flags & PZF_DIRECT);
   bool bad = false;
 
   if (c.do_finish) {
@@ -366,7 +574,22 @@ __device__ bool integ_stage(const PzDev& d, const View& V, const PzInst& I, cons
       const double g = rot ? h2 * dtcond[i] + I.tadvz * r[i] * tcond[i] : dtcond[i];
       s.a[i] = csub(csub(cscale(r[i], eT[i]), cim(dm * g, psi[i])), s.c[i]);
       double2 p = eP[i];
-      if (m != 0) {
+      if (m != 0 && dmat) {
+        // finish_exp_psi_int_dmat (update_psi_integ_dmat.f90:486-623): the
+        // vorticity equation without the r weight, Coriolis always explicit
+        p = csub(p, cscale(or1[i], s.g[i]));
+        if (rot) p = csub(p, cim(I.CorFac * dm, psi[i]));
+        if (!buo_imp) p = csub(p, cim(I.BuoFac * rgrav[i] * or1[i] * dm, T[i]));
+        if (I.flags & PZF_EK_PUMP) {
+          const double2 u = us[i];
+          const double2 q = make_double2(ekp_us[i] * u.x - ekp_dusdp[i] * dm * u.y,
+                                         ekp_us[i] * u.y + ekp_dusdp[i] * dm * u.x);
+          const double2 o = om[i], w = up[i];
+          const double ce = I.CorFac * ekpump[i];
+          p.x -= ce * (o.x + ekp_up[i] * w.x + q.x);
+          p.y -= ce * (o.y + ekp_up[i] * w.y + q.y);
+        }
+      } else if (m != 0) {
         p = cscale(r[i], p);
         if (!cor_imp) p = csub(p, cim(I.CorFac * dm * r[i], psi[i]));
         if (!buo_imp) p = csub(p, cim(I.BuoFac * rgrav[i] * dm, T[i]));
@@ -394,7 +617,7 @@ __device__ bool integ_stage(const PzDev& d, const View& V, const PzInst& I, cons
     trunc_cheb(s.f, n, n_max);
     __syncthreads();
     band_mv(band1(V, IM_I2R1), n, s.b, eT);
-    band_mv(band1(V, m == 0 ? IM_I2R2 : IM_I4R3), n, s.f, eP);
+    band_mv(band1(V, (m == 0 || dmat) ? IM_I2R2 : IM_I4R3), n, s.f, eP);
     __syncthreads();
   }
   if (!c.do_solve) return false;
@@ -460,15 +683,17 @@ __device__ bool integ_stage(const PzDev& d, const View& V, const PzInst& I, cons
     if (c.calc) band_mv(band1(V, IM_ULAP, I.ViscFac), n, s.a, iP);
     return bad;
   }
-  // -- streamfunction, m /= 0: buoyancy I4R4 C(-BuoFac rgrav/r i m T) with the new T
+  // -- streamfunction, m /= 0: buoyancy I4R4 C(-BuoFac rgrav/r i m T) (I2R2 with
+  // the influence matrix) with the new T
   if (buo_imp) {
     for (int i = threadIdx.x; i < n; i += blockDim.x) s.a[i] = cscale(-I.BuoFac * rgrav[i] * or1[i], cim(dm, s.f[i]));
     __syncthreads();
     op_C(V, n, s.a, s.c, s.w);
     __syncthreads();
-    band_mv(band1(V, IM_I4R4), n, s.c, s.e);
+    band_mv(band1(V, dmat ? IM_I2R2 : IM_I4R4), n, s.c, s.e);
     __syncthreads();
   }
+  if (dmat) return integ_dmat_psi(d, V, I, S, mi, c, s) || bad;
   for (int i = threadIdx.x; i < n; i += blockDim.x) {
     double2 v = c.dirk ? dirk_rhs(V, I, S, 1, mi, i, c.stage) : imex_rhs(V, I, S, 1, mi, i);
     if (buo_imp) v = cadd(v, cscale(S.wimp_lin[0], s.e[i]));

@@ -204,6 +204,8 @@ void pz_integ_operators(int N, double r_icb, double r_cmb, double rnorm, std::ve
       {IM_S0, lapl4(Ta), 4},                        // intcheb4rmult4laplrot2 = S0 + m^2 S1 + m^4 S2
       {IM_S1, s1, 4},
       {IM_S2, s2, 4},
+      {IM_P0, Ta, 2},                               // I2 [r^2 omega] = P0 + m^2 P1
+      {IM_P1, Tb, 2},
   };
   out.assign((size_t)IM_COUNT * N * N, 0.0);
   for (const Def& df : defs) {

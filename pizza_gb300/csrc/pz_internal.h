@@ -67,6 +67,8 @@ enum {
   IM_S0,        // intcheb4rmult4laplrot2(m) = S0 + m^2 S1 + m^4 S2
   IM_S1,
   IM_S2,
+  IM_P0,        // I2 [r^2 omega(psi)] = P0 + m^2 P1 (rotating omega of the integ streamfunction);
+  IM_P1,        //   intcheb2rmult2laplrot(m) = -(P0 + m^2 P1), the influence-matrix psi operator
   IM_COUNT
 };
 

@@ -626,14 +626,20 @@ __device__ void flag_status(PzState& S, int code) {
 
 // integration method (pz_integ.cuh, included below)
 __device__ int integ_build(const PzDev& d, const PzInst& I, const View& V, int mi, double wlin);
+__device__ int integ_psi_static(const PzDev& d, const PzInst& I, const View& V, int mi);
 
 // dt independent streamfunction operators (update_psi_coll_dmat.f90:94-98)
 __global__ void __launch_bounds__(PZ_THREADS) k_build_static(PzDev d) {
   const PzItem it = d.mitems[blockIdx.x];
   const PzInst& I = d.inst[it.inst];
   PzState& S = d.state[it.inst];
-  if (it.idx == 0 || (I.flags & PZF_INTEG)) return;
+  if (it.idx == 0) return;
   const View V{&I, d.pool};
+  if (I.flags & PZF_INTEG) {
+    // the influence-matrix variant's dt-independent psi-from-omega inverse
+    if (!(I.flags & PZF_DIRECT) && integ_psi_static(d, I, V, it.idx) != 0) flag_status(S, PZ_E_SINGULAR);
+    return;
+  }
   const int n = I.N, m = it.idx * I.minc;
   BuildSmem s = build_smem(n);
   BuildCtx B{&I, V.basis(BM_RMAT), V.basis(BM_DRMAT), V.basis(BM_D2RMAT), n};

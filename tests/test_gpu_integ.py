@@ -121,8 +121,36 @@ def test_rotinteg_fixture_on_gpu(pz):
     np.testing.assert_allclose(got, ref, rtol=1e-8, atol=1e-20)
 
 
+@pytest.mark.parametrize("variant", [
+    dict(),
+    dict(time_scheme="SBDF3"),
+    dict(time_scheme="CK232"),
+    dict(l_ek_pump=True),
+    dict(buo_term="EXPLICIT"),
+    dict(l_rerror_fix=True),
+    dict(pr=0.3, n_cheb_max=33),
+    dict(l_non_rot=True, ra=2e4, time_scale="VISC", dtMax=1e-3),
+])
+def test_integ_influence_matrix(pz, variant):
+    """update_psi_int_dmat: vorticity solve, psi from vorticity, influence
+    matrix for the remaining wall conditions (Coriolis explicit)."""
+    spec = dict(CI, matrix_solve="INFLUENCE", **variant)
+    sim, ens, out = run_pair(pz, spec, 40, seed=13, amp=1e-2, checkpoints=(1,))
+    for k, s, g in out:
+        check_fields(s, g, 1e-10, f"dmat step {k} {variant}")
+
+
+def test_integ_influence_matrix_larger_grid(pz):
+    """RotInteg's continuation grid and physics (n_r_max=97, n_cheb_max=64,
+    E=1e-4, Ra=2e6, Ekman pumping, SBDF3) with the influence matrix."""
+    spec = dict(CI, n_r_max=97, n_cheb_max=64, m_max=64, ek=1e-4, ra=2e6, dtMax=2e-3, l_ek_pump=True,
+                time_scheme="SBDF3", matrix_solve="INFLUENCE")
+    sim, ens, out = run_pair(pz, spec, 10, seed=9, amp=1e-3)
+    check_fields(sim, out[-1][2], 1e-9, "dmat N=97")
+
+
 def test_integ_rejections(pz):
-    bad = [dict(CI, matrix_solve="INFLUENCE"), dict(CI, time_scheme="ARS232"), dict(CI, l_non_rot=True)]
+    bad = [dict(CI, time_scheme="ARS232"), dict(CI, l_non_rot=True)]
     for s in bad:
         with pytest.raises(RuntimeError):
             pz.Ensemble(gpu_config(s))

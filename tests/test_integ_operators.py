@@ -6,7 +6,7 @@ fixture."""
 import numpy as np
 import pytest
 
-from oracle.chebsparse import IntegOperators, lapl_terms
+from oracle.chebsparse import IntegOperators, lapl_terms, omega_rot_terms
 
 
 @pytest.fixture(scope="module")
@@ -46,6 +46,10 @@ def test_library_operators_match_oracle(pz, n, radratio):
         rot2 = got["S0"][0] + m2 * (got["S1"][0] + m2 * got["S2"][0])
         w = ops.psi_rot2(m)
         assert np.max(np.abs(rot2 - w)) <= 1e-12 * np.max(np.abs(w)), m
+        # intcheb2rmult2laplrot = -I2 [r^2 omega(psi)]
+        p2 = got["P0"][0] + m2 * got["P1"][0]
+        w = ops._rows(c.integrated(omega_rot_terms(r_cmb, float(m)), 2), 2)
+        assert np.max(np.abs(p2 - w)) <= 1e-12 * np.max(np.abs(w)), m
 
 
 def test_operator_bad_arguments(pz):
