@@ -168,9 +168,15 @@ int pz_set_history(pz_handle* h, int inst, int field, int kind, int slot, const 
  * step count of one instance.  pz_set_step_state restores them after
  * pz_set_state; n_step >= nold - 1 skips the CNAB2 bridge of the first steps
  * (a restart with a full history), and the operators are rebuilt at the next
- * step. */
+ * step.  The latest time-series row is recomputed with the restored time. */
 int pz_get_step_state(pz_handle* h, int inst, double* time, double* dt, int* n_step);
 int pz_set_step_state(pz_handle* h, int inst, double time, const double* dt, int n_step);
+
+/* l_AB1 of read_checkpoint (src/checkpoints.f90:398-425): when set, the
+ * first step after pz_set_step_state(..., n_step = 0) takes first-order
+ * explicit weights (src/step_time.f90:309-314).  pizza sets it when a run
+ * restarts with another Ekman number or radial method. */
+int pz_set_restart_ab1(pz_handle* h, int inst, int l_ab1);
 
 /* Time series of one instance: one row per completed step plus the start row,
  * most recent last, at most *n_rows rows (in: capacity, out: count).

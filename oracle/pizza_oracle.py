@@ -904,30 +904,63 @@ class Pizza:
         self._temp_rhs_imp(1, True, l_in_cheb=False)
         self._psi_rhs_imp(1, True, l_in_cheb=False)
 
+    def _map_field(self, f, n_old, phys, lbc):
+        """map_field / map_field_r (checkpoints.f90:709-860), Chebyshev to
+        Chebyshev: (n_m_old, n_old) -> (M, N).  New azimuthal modes are zero;
+        in r the Chebyshev coefficients (costf1 of the old grid first when
+        the field is stored in physical space) are zero-padded or cut and
+        brought back with this grid's costf1, times rnorm_old / rnorm."""
+        f = np.array(f, complex)
+        out = np.zeros((self.M, self.N), complex)
+        mm = min(self.M, f.shape[0])
+        if n_old == self.N:
+            out[:mm] = f[:mm]
+            return out
+        g = f[:mm].copy()
+        if lbc and phys:
+            g[:, 0] = 2.0 * g[:, 1] - g[:, 2]
+        if phys:
+            g = Cheb(n_old, n_old, self.d["r_icb"], self.d["r_cmb"]).costf1(g)
+        pad = np.zeros((mm, max(self.N, n_old)), complex)
+        pad[:, :n_old] = g
+        g = pad[:, :self.N]
+        if phys:
+            g = self.cheb.costf1(g)
+        out[:mm] = math.sqrt(2.0 / (n_old - 1)) / self.cheb.rnorm * g
+        return out
+
     def start_from_checkpoint(self, ck):
         """get_start_fields with l_start_file (init_fields.f90:54-258) for a
-        version-7 checkpoint of the same grid and scheme (read_checkpoint,
-        checkpoints.f90:185-860, without grid mapping): fields, the history
-        slots 2..n, dt and time; then om and the first old/implicit slots as
-        for a fresh start.  Same scheme and Ekman number: no bridge, no AB1
-        (checkpoints.f90:398-416).  ``ck`` is a dict with header, us, up,
-        temp, hist_P, hist_T (expl 2..nexp, impl 2..nimp, old 2..nold)."""
+        version-7 checkpoint (read_checkpoint, checkpoints.f90:185-860): the
+        fields and the multistep history slots 2..n mapped onto this grid
+        (map_field), dt filled with the oldest value where this scheme keeps
+        more (:388-396), time; then om and the first old/implicit slots as
+        for a fresh start.  AB1 on the first step when the Ekman number or
+        the radial method changed, and the CNAB2 bridge when this scheme
+        needs more old or implicit slots than the file holds (:398-425).
+        ``ck`` is a dict with header (time, family, nexp, nimp, nold, dt, ek,
+        n_r_max, l_cheb_coll), us, up, temp, hist_P, hist_T (expl 2..nexp,
+        impl 2..nimp, old 2..nold of the file's scheme)."""
         ts, h = self.ts, ck["header"]
         self.time = h["time"]
         nd = len(h["dt"])
-        ts.dt[:nd] = h["dt"]
+        ts.dt[:min(nd, len(ts.dt))] = h["dt"][:len(ts.dt)]
         if nd < len(ts.dt):
             ts.dt[nd:] = h["dt"][-1]
         ts.set_weights()
-        self.us = np.array(ck["us"], complex)
-        self.up = np.array(ck["up"], complex)
-        self.temp = np.array(ck["temp"], complex)
-        if ts.family == "MULTISTEP":
-            order = ([("expl", k) for k in range(2, ts.nexp + 1)] + [("impl", k) for k in range(2, ts.nimp + 1)]
-                     + [("old", k) for k in range(2, ts.nold + 1)])
-            for (kind, k), aP, aT in zip(order, ck["hist_P"], ck["hist_T"]):
-                getattr(self.dpsidt, kind)[k - 1] = np.array(aP, complex)
-                getattr(self.dTdt, kind)[k - 1] = np.array(aT, complex)
+        n_old = int(h.get("n_r_max", self.N))
+        coll_old = bool(h.get("l_cheb_coll", True))
+        self.us = self._map_field(ck["us"], n_old, True, False)
+        self.up = self._map_field(ck["up"], n_old, True, False)
+        self.temp = self._map_field(ck["temp"], n_old, True, False)
+        if h["family"] == "MULTISTEP":
+            order = ([("expl", k, True) for k in range(2, h["nexp"] + 1)]
+                     + [("impl", k, True) for k in range(2, h["nimp"] + 1)]
+                     + [("old", k, False) for k in range(2, h["nold"] + 1)])
+            for (kind, k, lbc), aP, aT in zip(order, ck["hist_P"], ck["hist_T"]):
+                if ts.family == "MULTISTEP" and k <= {"expl": ts.nexp, "impl": ts.nimp, "old": ts.nold}[kind]:
+                    getattr(self.dpsidt, kind)[k - 1] = self._map_field(aP, n_old, coll_old, lbc)
+                    getattr(self.dTdt, kind)[k - 1] = self._map_field(aT, n_old, coll_old, lbc)
         if self.l_integ:
             self.psi = self.integ.psi_from_us()
         c = self.cheb
@@ -940,8 +973,17 @@ class Pizza:
         else:
             self._temp_rhs_imp(1, True, l_in_cheb=False)
             self._psi_rhs_imp(1, True, l_in_cheb=False)
-        self.l_bridge_step = False
-        self.l_AB1 = False
+        self.l_AB1 = h.get("ek", self.d["ek"]) != self.d["ek"]
+        if ts.family == "MULTISTEP":
+            if h["family"] == "DIRK":
+                self.l_bridge_step = True
+            else:
+                self.l_bridge_step = ts.nold > h["nold"] or ts.nimp > h["nimp"]
+            if coll_old != self.d["l_cheb_coll"]:
+                self.l_AB1 = True
+                self.l_bridge_step = True
+        else:
+            self.l_bridge_step = False
 
     def _init_prop(self, init_t, amp):
         """initProp (init_fields.f90:260-376), modes init_t>0 and -1."""

@@ -1029,9 +1029,27 @@ extern "C" int pz_set_step_state(pz_handle* h, int inst, double time, const doub
   for (int k = 0; k < nd; ++k) st.dt[k] = dt[k];
   st.n_step = n_step;
   st.lMatNext = 1;   // operators for the restored dt at the next step
+  // the latest time-series row is rewritten with the restored time
+  if (st.series_count > 0) st.series_count -= 1;
   e = cudaMemcpyAsync(h->d_state + inst, &st, sizeof(PzState), cudaMemcpyHostToDevice, h->stream);
+  if (!e) e = pz_launch_obs(h->dev, inst, h->stream);
   if (!e) e = cudaStreamSynchronize(h->stream);
   if (e) return cuda_fail(h, e, "pz_set_step_state");
+  return PZ_OK;
+}
+
+extern "C" int pz_set_restart_ab1(pz_handle* h, int inst, int l_ab1) {
+  if (!h) return fail(nullptr, PZ_E_ARG, "pz_set_restart_ab1: null handle");
+  if (inst < 0 || inst >= h->n_inst) return fail(h, PZ_E_ARG, "pz_set_restart_ab1: bad arguments");
+  pz_adjoint_invalidate(h);
+  PzState st;
+  cudaError_t e = cudaMemcpyAsync(&st, h->d_state + inst, sizeof(PzState), cudaMemcpyDeviceToHost, h->stream);
+  if (!e) e = cudaStreamSynchronize(h->stream);
+  if (e) return cuda_fail(h, e, "pz_set_restart_ab1");
+  st.ab1 = l_ab1 ? 1 : 0;
+  e = cudaMemcpyAsync(h->d_state + inst, &st, sizeof(PzState), cudaMemcpyHostToDevice, h->stream);
+  if (!e) e = cudaStreamSynchronize(h->stream);
+  if (e) return cuda_fail(h, e, "pz_set_restart_ab1");
   return PZ_OK;
 }
 

@@ -165,7 +165,7 @@ struct PzState {
   int r_old, r_impl, r_expl;          // ring base used by this step's rhs
   int status;               // 0 or a negative PZ_E_* code
   int series_count;
-  int pad;
+  int ab1;                  // first step of a restart takes AB1 explicit weights (l_AB1)
   double w_lhs;             // implicit weight the current operators were built with
 };
 

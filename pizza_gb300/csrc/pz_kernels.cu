@@ -240,6 +240,15 @@ __global__ void k_cfl(PzDev d) {
   S.n_step += 1;
   S.bridge = (!I.dirk && I.scheme != PZ_CNAB2 && S.n_step <= I.nold - 1) ? 1 : 0;
   if (S.bridge) bridge_with_cnab2(I, S);
+  if (S.ab1) {
+    // l_AB1 after a restart (checkpoints.f90:398-425): first-order explicit
+    // weights on the run's first step (step_time.f90:309-314)
+    if (S.n_step == 1) {
+      S.wexp[0] = S.dt[0];
+      for (int k = 1; k < 4; ++k) S.wexp[k] = 0.0;
+    }
+    S.ab1 = 0;
+  }
   S.l_calc_lin = (I.flags & PZF_IMP_CALC) ? 1 : 0;
   if (!I.dirk) {
     // rotate_imex on rings: this step reads slots from r_*, writes logical slot 1 at b_*

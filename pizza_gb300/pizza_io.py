@@ -4,9 +4,10 @@ version-7 checkpoints (src/checkpoints.f90:33-183 write, :185-860 read).
 
 A run on the GPU can therefore leave the same text series a pizza.exe run
 leaves (python/pizza reads them), save a checkpoint pizza.exe can restart
-from, and restart from a checkpoint pizza.exe wrote -- for the same grid and
-time-scheme family (pizza's own reader also interpolates between grids and
-bridges between schemes; that mapping is not restated here).
+from, and restart from a checkpoint pizza.exe wrote, also onto another
+Chebyshev grid, m truncation or multistep scheme, as pizza's reader does
+(Chebyshev-to-Chebyshev mapping, the CNAB2 bridge and AB1; finite
+differences and polynomial interpolation are not restated).
 """
 from __future__ import annotations
 
@@ -88,7 +89,7 @@ def write_checkpoint(path: str, header: dict, fields: dict):
     with open(path, "wb") as f:
         f.write(np.array([7], _I4).tobytes())
         f.write(np.array([h["time"]], _F8).tobytes())
-        f.write(np.array([1], _I4).tobytes())                            # l_cheb_coll
+        f.write(np.array([int(h.get("l_cheb_coll", True))], _I4).tobytes())   # l_cheb_coll
         f.write(h["family"].ljust(10)[:10].encode())
         f.write(np.array([h["nexp"], h["nimp"], h["nold"]], _I4).tobytes())
         f.write(np.asarray(h["dt"], _F8).tobytes())
@@ -180,7 +181,8 @@ def save_checkpoint(ens, i: int, path: str):
     header = dict(time=time, family=family, nexp=nexp, nimp=nimp, nold=nold,
                   dt=dt[:nexp] if family == "MULTISTEP" else dt[:1], ra=c.ra, pr=c.pr, ek=c.ek,
                   radratio=c.radratio, n_r_max=n, m_max=c.m_max, minc=c.minc,
-                  n_max=c.n_cheb_max if c.n_cheb_max is not None else n, r=_grid_r(n, c.radratio))
+                  n_max=c.n_cheb_max if c.n_cheb_max is not None else n, r=_grid_r(n, c.radratio),
+                  l_cheb_coll="COLL" in c.cheb_method.upper())
     fields = dict(us=st["us"], up=st["up"], temp=st["temp"])
     if family == "MULTISTEP":
         order = _hist_order(nexp, nimp, nold)
@@ -189,27 +191,84 @@ def save_checkpoint(ens, i: int, path: str):
     write_checkpoint(path, header, fields)
 
 
+def _costf1(f):
+    """DCT-I along the last axis with pizza's normalisation sqrt(1/(2(N-1))),
+    self-inverse (costf1 of src/dct_fftw.f90)."""
+    f = np.asarray(f, complex)
+    n = f.shape[-1]
+    ext = np.concatenate([f, f[..., n - 2:0:-1]], axis=-1)
+    return np.sqrt(0.5 / (n - 1)) * np.fft.fft(ext, axis=-1)[..., :n]
+
+
+def map_field(f, n_m_max: int, n_r_max: int, phys: bool, lbc: bool = False):
+    """A checkpoint field (n_m_old, n_r_old) onto (n_m_max, n_r_max), as
+    map_field / map_field_r do for Chebyshev grids (src/checkpoints.f90:709-860):
+    azimuthal modes the file lacks are zero; in r the Chebyshev coefficients
+    (costf1 of the old grid first for a physical-space field) are zero-padded
+    or cut and brought back with the new grid's costf1, times
+    sqrt(2/(n_r_old-1)) / sqrt(2/(n_r_max-1)).  lbc: a physical-space history
+    slot whose boundary value is re-extrapolated first."""
+    f = np.asarray(f, complex)
+    n_old = f.shape[1]
+    out = np.zeros((n_m_max, n_r_max), complex)
+    mm = min(n_m_max, f.shape[0])
+    if n_old == n_r_max:
+        out[:mm] = f[:mm]
+        return out
+    g = f[:mm].copy()
+    if lbc and phys:
+        g[:, 0] = 2.0 * g[:, 1] - g[:, 2]
+    if phys:
+        g = _costf1(g)
+    pad = np.zeros((mm, max(n_old, n_r_max)), complex)
+    pad[:, :n_old] = g
+    g = pad[:, :n_r_max]
+    if phys:
+        g = _costf1(g)
+    out[:mm] = np.sqrt(2.0 / (n_old - 1)) / np.sqrt(2.0 / (n_r_max - 1)) * g
+    return out
+
+
 def restart_from_checkpoint(ens, i: int, path: str):
-    """Start instance i from a checkpoint of the same grid and scheme family:
-    the fields (getStartFields recomputes the first old/implicit slots from
-    them), the history slots 2..n, time and dt."""
+    """Start instance i from a checkpoint as read_checkpoint and
+    get_start_fields do (src/checkpoints.f90:185-860, src/init_fields.f90:54-258):
+    fields and multistep history slots 2..n mapped onto the instance's grid
+    (map_field), dt filled with the oldest value where the instance's scheme
+    keeps more, time; the first old/implicit slots are recomputed from the
+    fields on the device.  AB1 on the first step when the Ekman number or the
+    radial method changed, and the CNAB2 bridge when the scheme needs more
+    old or implicit slots than the file holds.  Returns the header."""
     ck = read_checkpoint(path)
     h = ck["header"]
-    n, m, _ = ens.dims[i]
+    n, mm, _ = ens.dims[i]
     c = ens.configs[i]
-    if (h["n_r_max"], h["m_max"], h["minc"]) != (n, c.m_max, c.minc):
-        raise ValueError("checkpoint grid differs from the instance's (grid mapping is not restated)")
+    if h["minc"] != c.minc:
+        raise ValueError("checkpoint minc differs from the instance's (not restated)")
+    if h["rscheme"] != "cheb" or not h["l_heat"]:
+        raise ValueError("only Chebyshev checkpoints with temperature are read")
     nexp, nimp, nold, family = _scheme_counts(ens, i)
-    if h["family"] != family or (family == "MULTISTEP" and (h["nexp"], h["nimp"], h["nold"]) != (nexp, nimp, nold)):
-        raise ValueError("checkpoint time scheme differs from the instance's (scheme bridging is not restated)")
-    if not h["l_heat"]:
-        raise ValueError("checkpoint without temperature")
-    ens.set_state(i, us=ck["us"], up=ck["up"], temp=ck["temp"])
+    coll = "COLL" in c.cheb_method.upper()
+    coll_old = bool(h["l_cheb_coll"])
+    ens.set_state(i, us=map_field(ck["us"], mm, n, True), up=map_field(ck["up"], mm, n, True),
+                  temp=map_field(ck["temp"], mm, n, True))
+    if h["family"] == "MULTISTEP" and family == "MULTISTEP":
+        counts = {2: nexp, 1: nimp, 0: nold}
+        for (k, slot), aP, aT in zip(_hist_order(h["nexp"], h["nimp"], h["nold"]), ck["hist_P"], ck["hist_T"]):
+            if slot <= counts[k]:
+                ens.set_history(i, 1, k, slot, map_field(aP, mm, n, coll_old, lbc=k != 0))
+                ens.set_history(i, 0, k, slot, map_field(aT, mm, n, coll_old, lbc=k != 0))
+    nd = nexp if family == "MULTISTEP" else 1
+    dt = np.array([h["dt"][min(k, len(h["dt"]) - 1)] for k in range(nd)])
+    ab1 = h["ek"] != c.ek
     if family == "MULTISTEP":
-        for (k, s), aP, aT in zip(_hist_order(nexp, nimp, nold), ck["hist_P"], ck["hist_T"]):
-            ens.set_history(i, 1, k, s, aP)
-            ens.set_history(i, 0, k, s, aT)
-    ens.set_step_state(i, h["time"], h["dt"], max(nold, 1))
+        bridge = h["family"] == "DIRK" or nold > h["nold"] or nimp > h["nimp"]
+        if coll_old != coll:
+            ab1 = bridge = True
+    else:
+        bridge = False
+    # n_step 0 runs the CNAB2 bridge over the first nold-1 steps; nold skips it
+    ens.set_step_state(i, h["time"], dt, 0 if bridge else max(nold, 1))
+    ens.set_restart_ab1(i, ab1)
     return h
 
 

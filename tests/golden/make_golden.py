@@ -13,6 +13,13 @@ first run starts from the namelist and needs no checkpoint):
   TimeStepChange    all 21 rows   (e_kin, coll dmat SBDF3, CFL dt changes)
   DIRKSchemes       rows 0-10     (e_kin_3D, coll smat ARS222, a DIRK scheme)
   RotInteg          rows 0-200    (e_kin_3D, integ smat CNAB2, tau boundary rows)
+  RotIntegContinue  rows 201-216  (e_kin_3D, RotInteg's second run: its first run's
+                                   final state read onto n_r_max=97, m_max=64, integ
+                                   dmat SBDF3 with the CNAB2 bridge and AB1)
+
+A case with "restart_from" starts from the final state of that case's run
+(written as a checkpoint and read back) instead of its own start fields;
+"skip" is the number of fixture lines before its rows.
 """
 import argparse
 import json
@@ -54,6 +61,13 @@ CASES = {
                     courfac=4.0, time_scale="ROT", ra=5.0e4, pr=1.0, ek=1.0e-3, radratio=0.35,
                     g0=0.0, g1=1.0, g2=0.0, ktopv=2, kbotv=2, l_ek_pump=False, init_t=-1,
                     amp_t=1.0e-2, n_log_step=20)),
+    "RotIntegContinue": dict(
+        rows=16, skip=201, series="e_kin_3D", restart_from="RotInteg",
+        params=dict(n_r_max=97, n_cheb_max=64, m_max=64, n_time_steps=300, dtMax=1e-1,
+                    cheb_method="INTEG", matrix_solve="INFLUENCE", corio_term="EXPLICIT",
+                    l_rerror_fix=True, rerror_fac=5e2, courfac=4.0, time_scale="ROT", time_scheme="SBDF3",
+                    ra=2.0e6, pr=1.0, ek=1.0e-4, radratio=0.35, g0=0.0, g1=1.0, g2=0.0, ktopv=2, kbotv=2,
+                    l_ek_pump=True, n_log_step=20)),
 }
 
 
@@ -64,14 +78,19 @@ def main():
     here = os.path.dirname(os.path.abspath(__file__))
     meta = {}
     for case, spec in CASES.items():
-        src = os.path.join(args.ref, "samples", case, "reference.out")
+        sample = spec.get("restart_from", case)
+        src = os.path.join(args.ref, "samples", sample, "reference.out")
         with open(src) as f:
             lines = [ln for ln in f.read().splitlines() if ln.strip()]
-        keep = lines[:spec["rows"]]
+        skip = spec.get("skip", 0)
+        keep = lines[skip:skip + spec["rows"]]
         with open(os.path.join(here, f"{case}.txt"), "w") as f:
             f.write("\n".join(keep) + "\n")
         meta[case] = dict(series=spec["series"], rows=spec["rows"], params=spec["params"],
-                          source=f"samples/{case}/reference.out")
+                          source=f"samples/{sample}/reference.out")
+        if "restart_from" in spec:
+            meta[case]["restart_from"] = spec["restart_from"]
+            meta[case]["skip"] = skip
     with open(os.path.join(here, "cases.json"), "w") as f:
         json.dump(meta, f, indent=1, sort_keys=True)
 

@@ -149,6 +149,35 @@ def test_integ_influence_matrix_larger_grid(pz):
     check_fields(sim, out[-1][2], 1e-9, "dmat N=97")
 
 
+def test_rotinteg_continuation_fixture_on_gpu(pz, tmp_path):
+    """RotInteg's second run: the first run's final state, saved as a
+    version-7 checkpoint and read back onto n_r_max=97, n_cheb_max=64,
+    m_max=64 (Chebyshev mapping), with the influence-matrix solve, SBDF3
+    behind the CNAB2 bridge, AB1 on the first step (E changed), Ekman pumping
+    and explicit Coriolis: its 16 e_kin_3D rows at the harness's tolerances."""
+    from pizza_gb300 import pizza_io
+    with open(os.path.join(HERE, "golden", "cases.json")) as f:
+        cases = json.load(f)
+    p1, p2 = dict(cases["RotInteg"]["params"]), dict(cases["RotIntegContinue"]["params"])
+    ref = np.loadtxt(os.path.join(HERE, "golden", "RotIntegContinue.txt"))
+    sim = oracle(p1)                         # init_t = -1 start field built by the oracle
+    ens = pz.Ensemble(gpu_config(p1))
+    ens.set_state(0, temp=sim.temp.copy())
+    ens.step(p1["n_time_steps"])
+    path = str(tmp_path / "checkpoint_end.start")
+    pizza_io.save_checkpoint(ens, 0, path)
+    ens2 = pz.Ensemble(gpu_config(p2))
+    pizza_io.restart_from_checkpoint(ens2, 0, path)
+    n, nlog = p2["n_time_steps"], p2["n_log_step"]
+    rows = [ens2.series(0)[-1]]
+    for _ in range(n // nlog):
+        ens2.step(nlog)
+        rows.append(ens2.series(0)[-1])
+    got = np.array(rows)[:, [0, 4, 5, 6, 7]]
+    assert got.shape == ref.shape
+    np.testing.assert_allclose(got, ref, rtol=1e-8, atol=1e-20)
+
+
 def test_integ_rejections(pz):
     bad = [dict(CI, time_scheme="ARS232"), dict(CI, l_non_rot=True)]
     for s in bad:
