@@ -172,6 +172,12 @@ int pz_set_history(pz_handle* h, int inst, int field, int kind, int slot, const 
 int pz_get_step_state(pz_handle* h, int inst, double* time, double* dt, int* n_step);
 int pz_set_step_state(pz_handle* h, int inst, double time, const double* dt, int n_step);
 
+/* Snapshot spectra of one instance's current state, computed on the device
+ * (calculate_spectra, src/spectra.f90:104-196): out receives n_m_max rows
+ * of 4 doubles, for each m the r-integral (rInt_R) of
+ * pi cc2real(f(m, r)) r height(r) for f = us, up, om, temp. */
+int pz_get_spectra(pz_handle* h, int inst, double* out);
+
 /* l_AB1 of read_checkpoint (src/checkpoints.f90:398-425): when set, the
  * first step after pz_set_step_state(..., n_step = 0) takes first-order
  * explicit weights (src/step_time.f90:309-314).  pizza sets it when a run

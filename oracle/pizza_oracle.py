@@ -1666,6 +1666,19 @@ class Pizza:
         return lMat
 
     # -- time series (src/outputs.f90:418-830) -------------------------------
+    def spectra(self):
+        """calculate_spectra (spectra.f90:104-196), the snapshot part: per m
+        the rInt_R of pi cc2real(f) r height for f = us, up, om, temp, and
+        xi (zero: no composition).  (M, 5) array."""
+        c = self.cheb
+        out = np.zeros((self.M, 5))
+        for i in range(self.M):
+            for k, f in enumerate((self.us, self.up, self.om, self.temp)):
+                z = f[i]
+                c2 = z.real ** 2 if i == 0 else 2.0 * (z.real ** 2 + z.imag ** 2)
+                out[i, k] = c.rInt_R(np.pi * c2 * self.r * self.height)
+        return out
+
     def time_series(self):
         """Rows of e_kin, e_kin_3D and heat at the current state."""
         d, c = self.d, self.cheb

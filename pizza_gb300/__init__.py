@@ -173,6 +173,7 @@ def load_library(path: str | None = None):
     lib.pz_get_step_state.argtypes = [vp, ctypes.c_int, dp, dp, ctypes.POINTER(ctypes.c_int)]
     lib.pz_set_step_state.argtypes = [vp, ctypes.c_int, ctypes.c_double, dp, ctypes.c_int]
     lib.pz_set_restart_ab1.argtypes = [vp, ctypes.c_int, ctypes.c_int]
+    lib.pz_get_spectra.argtypes = [vp, ctypes.c_int, dp]
     lib.pz_integ_operator.argtypes = [ctypes.c_int, ctypes.c_double, ctypes.c_int, dp, ctypes.POINTER(ctypes.c_int)]
     lib.pz_destroy.argtypes = [ctypes.c_void_p]
     lib.pz_last_error.argtypes = [ctypes.c_void_p]
@@ -181,7 +182,8 @@ def load_library(path: str | None = None):
               "pz_get_series", "pz_get_dims", "pz_launches_per_step", "pz_latest_rows",
               "pz_step_profile", "pz_explicit_terms", "pz_explicit_terms_noalloc", "pz_adjoint_forward",
               "pz_adjoint_backward", "pz_set_ra", "pz_get_history", "pz_set_history", "pz_get_step_state",
-              "pz_set_step_state", "pz_set_restart_ab1", "pz_integ_operator", "pz_destroy"):
+              "pz_set_step_state", "pz_set_restart_ab1", "pz_get_spectra", "pz_integ_operator",
+              "pz_destroy"):
         getattr(lib, f).restype = ctypes.c_int
     _lib = lib
     return lib
@@ -346,6 +348,13 @@ class Ensemble:
         dt = np.atleast_1d(np.asarray(dt, np.float64))
         d[:len(dt)] = dt
         self._check(self.lib.pz_set_step_state(self._h, i, float(time), _dptr(d), int(n_step)))
+
+    def spectra(self, i):
+        """Snapshot spectra of instance i on the device: (n_m_max, 4) array of
+        the r-integrated us^2, up^2, enstrophy and T^2 per m (spectra.f90)."""
+        out = np.zeros(4 * self.dims[i][1])
+        self._check(self.lib.pz_get_spectra(self._h, i, _dptr(out)))
+        return out.reshape(-1, 4)
 
     def set_restart_ab1(self, i, on=True):
         """First step after a restart with first-order explicit weights (pizza's l_AB1)."""

@@ -723,7 +723,8 @@ extern "C" int pz_create(const pz_config* cfgs, int n, pz_handle** out) {
       (e = cudaMalloc(&h->d_mitems, mitems.size() * sizeof(PzItem))) ||
       (e = cudaMalloc(&h->d_order, mitems.size() * sizeof(PzItem))) ||
       (e = cudaMalloc(&h->d_iorder, n * sizeof(int))) ||
-      (e = cudaMalloc(&h->d_rows, (size_t)n * PZ_SERIES_COLS * sizeof(double)))) {
+      (e = cudaMalloc(&h->d_rows, (size_t)n * PZ_SERIES_COLS * sizeof(double))) ||
+      (e = cudaMalloc(&h->d_spec, (size_t)4 * maxM * sizeof(double)))) {
     g_create_error = std::string("device allocation: ") + cudaGetErrorString(e);
     pz_destroy(h);
     return PZ_E_NOMEM;
@@ -1038,6 +1039,17 @@ extern "C" int pz_set_step_state(pz_handle* h, int inst, double time, const doub
   return PZ_OK;
 }
 
+extern "C" int pz_get_spectra(pz_handle* h, int inst, double* out) {
+  if (!h) return fail(nullptr, PZ_E_ARG, "pz_get_spectra: null handle");
+  if (inst < 0 || inst >= h->n_inst || !out) return fail(h, PZ_E_ARG, "pz_get_spectra: bad arguments");
+  const int M = h->inst[inst].M;
+  cudaError_t e = pz_launch_spectra(h->dev, inst, M, h->d_spec, h->stream);
+  if (!e) e = cudaMemcpyAsync(out, h->d_spec, (size_t)4 * M * sizeof(double), cudaMemcpyDeviceToHost, h->stream);
+  if (!e) e = cudaStreamSynchronize(h->stream);
+  if (e) return cuda_fail(h, e, "pz_get_spectra");
+  return PZ_OK;
+}
+
 extern "C" int pz_set_restart_ab1(pz_handle* h, int inst, int l_ab1) {
   if (!h) return fail(nullptr, PZ_E_ARG, "pz_set_restart_ab1: null handle");
   if (inst < 0 || inst >= h->n_inst) return fail(h, PZ_E_ARG, "pz_set_restart_ab1: bad arguments");
@@ -1222,6 +1234,7 @@ extern "C" int pz_destroy(pz_handle* h) {
   cudaFree(h->d_order);
   cudaFree(h->d_iorder);
   cudaFree(h->d_rows);
+  cudaFree(h->d_spec);
   if (h->stream) cudaStreamDestroy(h->stream);
   delete h;
   return PZ_OK;

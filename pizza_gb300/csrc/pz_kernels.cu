@@ -1413,6 +1413,34 @@ __global__ void __launch_bounds__(256) k_assemble(PzDev d) {
 // (src/constants.f90:21)
 __device__ __forceinline__ double round_off(double x) { return fabs(x) < 10.0 * 2.220446049250313e-16 ? 0.0 : x; }
 
+// ---------------------------------------------------------------------------
+// k_spectra: snapshot spectra of one instance (calculate_spectra,
+// src/spectra.f90:104-196): per m, rInt_R of pi cc2real(f) r height for
+// f = us, up, om, T; one block per m
+// ---------------------------------------------------------------------------
+__global__ void k_spectra(PzDev d, int inst, double* out) {
+  const PzInst& I = d.inst[inst];
+  const View V{&I, d.pool};
+  __shared__ double red[32];
+  const int n = I.N, mi = blockIdx.x;
+  const double* rr = V.rad(RV_R);
+  const double* h = V.rad(RV_HEIGHT);
+  const double* wint = V.rad(RV_WINT);
+  const int fl[4] = {F_US, F_UP, F_OM, F_TEMP};
+  const double pi = 3.14159265358979323846;
+  for (int k = 0; k < 4; ++k) {
+    const double2* f = V.fld(fl[k], mi);
+    double acc = 0.0;
+    for (int r = threadIdx.x; r < n; r += blockDim.x) {
+      const double2 z = f[r];
+      const double c2 = (mi == 0) ? z.x * z.x : 2.0 * (z.x * z.x + z.y * z.y);   // cc2real
+      acc += wint[r] * (pi * c2 * rr[r] * h[r]);
+    }
+    acc = block_sum(acc, red);
+    if (threadIdx.x == 0) out[4 * mi + k] = acc;
+  }
+}
+
 __global__ void k_obs(PzDev d, int only) {
   const int inst = blockIdx.x;
   if (only >= 0 && inst != only) return;
@@ -1591,6 +1619,11 @@ cudaError_t pz_launch_init_state(const PzDev& d, int only, cudaStream_t s) {
 
 cudaError_t pz_launch_start(const PzDev& d, int only, cudaStream_t s) {
   k_start<<<d.n_mitems, PZ_THREADS, ms_smem_bytes(d.maxN), s>>>(d, only);
+  return cudaGetLastError();
+}
+
+cudaError_t pz_launch_spectra(const PzDev& d, int inst, int n_m_max, double* out, cudaStream_t s) {
+  k_spectra<<<n_m_max, 64, 0, s>>>(d, inst, out);
   return cudaGetLastError();
 }
 

@@ -44,6 +44,31 @@ def format_series_line(values) -> str:
     return fortran_es(values[0], 20, 12) + "".join(fortran_es(v, 16, 8) for v in values[1:])
 
 
+def format_spectrum_lines(spec, minc: int = 1):
+    """spec_N.TAG lines of write_spectra (src/spectra.f90:306-369): for each
+    m, '(I5, 5ES16.8)' of m and the round_off'ed us2, up2, enstrophy, T^2 and
+    composition (zero) spectra.  spec: (n_m_max, 4) array."""
+    lines = []
+    for mi, row in enumerate(np.asarray(spec, float)):
+        vals = [_round_off(v) for v in row] + [0.0]
+        lines.append(f"{mi * minc:5d}" + "".join(fortran_es(v, 16, 8) for v in vals))
+    return lines
+
+
+def _round_off(x):
+    """round_off (src/useful.f90:222-233): |x| < 10 epsilon -> 0."""
+    return 0.0 if abs(x) < 10.0 * np.finfo(float).eps else float(x)
+
+
+def write_spectrum(ens, i: int, counter: int, tag: str, directory: str = "."):
+    """spec_<counter>.<tag> of instance i from its device spectra."""
+    p = os.path.join(directory, f"spec_{counter}.{tag}")
+    with open(p, "w") as f:
+        for ln in format_spectrum_lines(ens.spectra(i), ens.configs[i].minc):
+            f.write(ln + "\n")
+    return p
+
+
 def write_series(ens, i: int, tag: str, directory: str = ".", rows=None):
     """Write e_kin.TAG, heat.TAG and (rotating runs) e_kin_3D.TAG of instance i
     from its time-series rows (Ensemble.series: at most the last 1024).
@@ -189,6 +214,74 @@ def save_checkpoint(ens, i: int, path: str):
         fields["hist_P"] = [ens.get_history(i, 1, k, s) for k, s in order]
         fields["hist_T"] = [ens.get_history(i, 0, k, s) for k, s in order]
     write_checkpoint(path, header, fields)
+
+
+# ---------------------------------------------------------------------------
+# frames: 2-D snapshots of one field (src/output_frames.f90:105-145, read by
+# python/pizza/frame.py), stream-unformatted, native byte order
+# ---------------------------------------------------------------------------
+def write_frame(path: str, header: dict, field):
+    """Write a version-2 frame (write_snapshot_mloc): version, time, ra, ek,
+    pr, radratio, sc, raxi, n_r_max, n_m_max, m_max, minc, n_phi_max, r,
+    tcond, xicond, idx2m, then the (n_m_max, n_r_max) complex field with m
+    fastest.  header: time, ra, ek, pr, radratio, sc, raxi, m_max, minc, r,
+    tcond, xicond (the last may be None: written as zeros)."""
+    h = header
+    f = np.asarray(field, np.complex128)
+    n_m_max, n_r_max = f.shape
+    r = np.asarray(h["r"], _F8)
+    xicond = np.zeros(n_r_max) if h.get("xicond") is None else np.asarray(h["xicond"], _F8)
+    with open(path, "wb") as out:
+        out.write(np.array([2], _I4).tobytes())
+        out.write(np.array([h["time"], h["ra"], h["ek"], h["pr"], h["radratio"], h.get("sc", 0.0),
+                            h.get("raxi", 0.0)], _F8).tobytes())
+        out.write(np.array([n_r_max, n_m_max, h["m_max"], h["minc"], 3 * h["m_max"] // h["minc"]], _I4).tobytes())
+        out.write(r.tobytes())
+        out.write(np.asarray(h["tcond"], _F8).tobytes())
+        out.write(np.asarray(xicond, _F8).tobytes())
+        out.write((np.arange(n_m_max, dtype=np.int32) * h["minc"]).astype(_I4).tobytes())
+        out.write(np.asfortranarray(f).tobytes(order="F"))
+
+
+def read_frame(path: str) -> dict:
+    """Read a version-2 frame written by pizza.exe or write_frame."""
+    with open(path, "rb") as fh:
+        version = int(np.fromfile(fh, _I4, 1)[0])
+        if version != 2:
+            raise ValueError(f"frame version {version}: only version 2 is read")
+        vals = np.fromfile(fh, _F8, 7)
+        n_r_max, n_m_max, m_max, minc, n_phi_max = (int(v) for v in np.fromfile(fh, _I4, 5))
+        r = np.fromfile(fh, _F8, n_r_max)
+        tcond = np.fromfile(fh, _F8, n_r_max)
+        xicond = np.fromfile(fh, _F8, n_r_max)
+        idx2m = np.fromfile(fh, _I4, n_m_max)
+        field = np.fromfile(fh, np.dtype("<c16"), n_m_max * n_r_max).reshape((n_m_max, n_r_max), order="F")
+    keys = ("time", "ra", "ek", "pr", "radratio", "sc", "raxi")
+    out = {k: float(v) for k, v in zip(keys, vals)}
+    out.update(version=version, n_r_max=n_r_max, n_m_max=n_m_max, m_max=m_max, minc=minc, n_phi_max=n_phi_max,
+               r=r, tcond=tcond, xicond=xicond, idx2m=idx2m, field=field)
+    return out
+
+
+def save_frames(ens, i: int, counter: int, tag: str, directory: str = "."):
+    """frame_temp_<counter>.<tag>, frame_us_..., frame_up_..., frame_om_... of
+    instance i (outputs.f90:293-310: temperature, then the three flow
+    fields; temperature is the perturbation, tcond is in the header).
+    Returns the paths written."""
+    c = ens.configs[i]
+    n, _, _ = ens.dims[i]
+    st = ens.get_state(i)
+    time, _, _ = ens.get_step_state(i)
+    r = _grid_r(n, c.radratio)
+    r_cmb = 1.0 / (1.0 - c.radratio)
+    header = dict(time=time, ra=c.ra, ek=c.ek, pr=c.pr, radratio=c.radratio, sc=0.0, raxi=0.0, m_max=c.m_max,
+                  minc=c.minc, r=r, tcond=np.log(r / r_cmb) / np.log(c.radratio), xicond=None)
+    paths = []
+    for name, key in (("temp", "temp"), ("us", "us"), ("up", "up"), ("om", "om")):
+        p = os.path.join(directory, f"frame_{name}_{counter}.{tag}")
+        write_frame(p, header, st[key])
+        paths.append(p)
+    return paths
 
 
 def _costf1(f):

@@ -78,3 +78,44 @@ def test_checkpoint_restart_matches_pizza_restart(pz, tmp_path, scheme, solve):
     gb = b.get_state(0)
     check_fields(sim, gb, 1e-10, f"{scheme} restarted")
     assert abs(gb["time"] - sim.time) < 1e-15
+
+
+def test_frames_of_a_gpu_run(pz, tmp_path):
+    """frame_temp/us/up/om of a GPU run (pizza's snapshot files) read back:
+    the fields are the instance's state, the header its run."""
+    from pizza_gb300.pizza_io import read_frame, save_frames
+    spec = C0
+    ens = pz.Ensemble(gpu_config(spec))
+    ens.set_state(0, temp=seeded(spec, 60))
+    ens.step(5)
+    paths = save_frames(ens, 0, 3, "gpu", str(tmp_path))
+    assert [os.path.basename(p) for p in paths] == ["frame_temp_3.gpu", "frame_us_3.gpu", "frame_up_3.gpu",
+                                                     "frame_om_3.gpu"]
+    st = ens.get_state(0)
+    time, _, _ = ens.get_step_state(0)
+    for p, key in zip(paths, ("temp", "us", "up", "om")):
+        f = read_frame(p)
+        assert f["time"] == time and f["n_r_max"] == 33 and f["n_m_max"] == 33 and f["n_phi_max"] == 96
+        assert np.array_equal(f["field"], st[key])
+
+
+@pytest.mark.parametrize("spec_extra", [dict(), dict(cheb_method="INTEG", n_cheb_max=24, time_scale="ROT",
+                                                      dtMax=2e-2, ra=5e4)])
+def test_device_spectra_match_oracle(pz, tmp_path, spec_extra):
+    """Snapshot spectra computed on the device against the oracle's
+    calculate_spectra, after 20 steps, and the spec_N.TAG file."""
+    from pizza_gb300.pizza_io import write_spectrum
+    spec = dict(C0, **spec_extra)
+    t0 = seeded(spec, 61, 1e-2)
+    sim = oracle(spec, temp0=t0)
+    ens = pz.Ensemble(gpu_config(spec))
+    ens.set_state(0, temp=t0)
+    for _ in range(20):
+        sim.advance()
+    ens.step(20)
+    got, ref = ens.spectra(0), sim.spectra()[:, :4]
+    # per spectrum, relative to its largest mode (the 1e-10 field bar)
+    err = np.max(np.abs(got - ref), axis=0) / np.max(np.abs(ref), axis=0)
+    assert np.all(err < 1e-10), err
+    p = write_spectrum(ens, 0, 0, "gpu", str(tmp_path))
+    assert np.loadtxt(p).shape == (ens.dims[0][1], 6)

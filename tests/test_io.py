@@ -5,6 +5,7 @@ import os
 import numpy as np
 import pytest
 
+from pizza_gb300 import pizza_io
 from pizza_gb300.pizza_io import fortran_es, format_series_line, read_checkpoint, write_checkpoint, _grid_r
 
 HERE = os.path.dirname(os.path.abspath(__file__))
@@ -52,3 +53,38 @@ def test_checkpoint_roundtrip(tmp_path):
         assert np.array_equal(ck[k], fields[k])
     for k in ("hist_P", "hist_T"):
         assert all(np.array_equal(a, b) for a, b in zip(ck[k], fields[k]))
+
+
+def test_frame_matches_reference_reader_fixture(tmp_path):
+    """write_frame's bytes equal the committed golden frame, whose contents
+    the reference's own reader (python/pizza/frame.py) parsed back to the
+    sample header and field (tests/golden/make_frame_golden.py)."""
+    import json
+    import sys
+    sys.path.insert(0, os.path.join(os.path.dirname(__file__), "golden"))
+    from make_frame_golden import sample
+    header, field = sample()
+    p = tmp_path / "frame.bin"
+    pizza_io.write_frame(str(p), header, field)
+    golden = os.path.join(os.path.dirname(__file__), "golden")
+    with open(os.path.join(golden, "frame_sample.bin"), "rb") as f:
+        assert p.read_bytes() == f.read()
+    with open(os.path.join(golden, "frame_sample.json")) as f:
+        ref = json.load(f)
+    assert (ref["version"], ref["n_r_max"], ref["n_m_max"], ref["m_max"], ref["minc"], ref["n_phi_max"]) == \
+        (2, 9, 5, 4, 1, 12)
+    for k in ("time", "ra", "ek", "pr", "radratio", "sc", "raxi"):
+        assert ref[k] == header[k]
+    assert np.array_equal(np.array(ref["radius"]), header["r"])
+    assert np.array_equal(np.array(ref["field_re"]) + 1j * np.array(ref["field_im"]), field)
+    back = pizza_io.read_frame(str(p))
+    assert np.array_equal(back["field"], field) and back["time"] == header["time"]
+    assert np.array_equal(back["idx2m"], np.arange(5))
+
+
+def test_spectrum_line_format():
+    """'(I5, 5ES16.8)' lines with round_off (src/spectra.f90:351-360)."""
+    lines = pizza_io.format_spectrum_lines(np.array([[1.5e-3, 2.0, 1e-16, -3.25e-7], [0.0, 1.0, 2.0, 3.0]]), minc=1)
+    assert lines[0] == "    0  1.50000000E-03  2.00000000E+00  0.00000000E+00 -3.25000000E-07  0.00000000E+00"
+    assert lines[1].startswith("    1  0.00000000E+00  1.00000000E+00")
+    assert all(len(x) == 5 + 5 * 16 for x in lines)
