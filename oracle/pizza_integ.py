@@ -102,13 +102,15 @@ class IntegScheme:
             raise np.linalg.LinAlgError("Singular matrix in the integ solve")
         return (lu, piv), fac
 
-    def _temp_lhs(self, i):
-        """update_temp_integ.f90:631-776."""
-        pz, p, d = self.pz, self.pz.p, self.pz.d
+    def _temp_lhs(self, i, kind="temp"):
+        """update_temp_integ.f90:631-776 (update_xi_integ.f90 for the
+        composition: the same operator with XidiffFac)."""
+        pz = self.pz
+        _, _, _, diff, _, _, ktop, kbot = pz._sc(kind)
         w = pz.ts.wimp_lin[0]
-        A = self.ops.i2r2 - w * d["TdiffFac"] * pz.hdif[i] * self.t_rhsi[i]
-        A[0] = self.rnorm * (self.r_top if p.ktopt == 1 else self.dr_top)
-        A[1] = self.rnorm * (self.r_bot if p.kbott == 1 else self.dr_bot)
+        A = self.ops.i2r2 - w * diff * pz.hdif[i] * self.t_rhsi[i]
+        A[0] = self.rnorm * (self.r_top if ktop == 1 else self.dr_top)
+        A[1] = self.rnorm * (self.r_bot if kbot == 1 else self.dr_bot)
         return self._finish_lhs(A, 2)
 
     def _psi_lhs(self, i):
@@ -149,6 +151,8 @@ class IntegScheme:
     def build_matrices(self):
         M = self.pz.M
         self.tmats = [self._temp_lhs(i) for i in range(M)]
+        if self.pz.l_chem:
+            self.ximats = [self._temp_lhs(i, "xi") for i in range(M)]
         self.pmats = [self._psi_lhs(i) for i in range(M)]
         if self.dmat:
             self._intermediate()
@@ -229,6 +233,9 @@ class IntegScheme:
         pz.temp_hat = c.costf1(pz.temp)
         pz.psi_hat = c.costf1(pz.psi)
         self.temp_rhs_imp(1, True)
+        if pz.l_chem:
+            pz.xi_hat = c.costf1(pz.xi)
+            self.temp_rhs_imp(1, True, "xi")
         self.psi_rhs_imp(1, True)
 
     # -- explicit terms (mloop.f90:209-226) ----------------------------------
@@ -251,6 +258,19 @@ class IntegScheme:
         e = c.costf1(e - work)
         e[:, n_max:] = 0.0
         pz.dTdt.expl[ist] = e @ self.ops.i2r1.T
+        if pz.l_chem:
+            # finish_exp_xi_int (update_xi_integ.f90:280-357): no tadvz term
+            w = c.costf1(pz._dVsXi)
+            w[:, n_max:] = 0.0
+            work = c.get_dr(w, l_dct_in=False)
+            e = pz.dxidt.expl[ist]
+            if d["l_non_rot"]:
+                e = r * e - 1j * m * pz.dxicond * pz.psi
+            else:
+                e = r * e - 1j * m * (d["r_cmb"] ** 2 - r * r) * pz.dxicond * pz.psi
+            e = c.costf1(e - work)
+            e[:, n_max:] = 0.0
+            pz.dxidt.expl[ist] = e @ self.ops.i2r1.T
         w = c.costf1(dVsOm)
         w[:, n_max:] = 0.0
         work = c.get_dr(w, l_dct_in=False)
@@ -263,6 +283,8 @@ class IntegScheme:
                 e[nz] = e[nz] - d["CorFac"] * 1j * m[nz] * pz.psi[nz]
             if not d["l_buo_imp"]:
                 e[nz] = e[nz] - d["BuoFac"] * pz.rgrav * pz.or1 * 1j * m[nz] * pz.temp[nz]
+                if pz.l_chem:
+                    e[nz] = e[nz] - d["ChemFac"] * pz.rgrav * pz.or1 * 1j * m[nz] * pz.xi[nz]
             if pz.p.l_ek_pump:
                 ekp = d["CorFac"] * pz.ekpump
                 e[0] = e[0] - ekp * pz.up[0]
@@ -278,6 +300,8 @@ class IntegScheme:
             e[nz] = e[nz] - d["CorFac"] * 1j * m[nz] * r * pz.psi[nz]
         if not d["l_buo_imp"]:
             e[nz] = e[nz] - d["BuoFac"] * pz.rgrav * 1j * m[nz] * pz.temp[nz]
+            if pz.l_chem:
+                e[nz] = e[nz] - d["ChemFac"] * pz.rgrav * 1j * m[nz] * pz.xi[nz]
         if pz.p.l_ek_pump:
             ekp = d["CorFac"] * pz.ekpump
             e[0] = e[0] - ekp * pz.up[0]
@@ -292,33 +316,38 @@ class IntegScheme:
         pz.dpsidt.expl[ist] = out
 
     # -- implicit terms ------------------------------------------------------
-    def temp_rhs_imp(self, istage, l_calc_lin):
-        """get_temp_rhs_imp_int (update_temp_integ.f90:471-536)."""
-        pz, d = self.pz, self.pz.d
-        th = pz.temp_hat
+    def temp_rhs_imp(self, istage, l_calc_lin, kind="temp"):
+        """get_temp_rhs_imp_int (update_temp_integ.f90:471-536) or
+        get_xi_rhs_imp_int (update_xi_integ.f90:449-510)."""
+        pz = self.pz
+        _, _, ta, diff = pz._sc(kind)[:4]
+        th = pz.temp_hat if kind == "temp" else pz.xi_hat
         if istage == 1:
-            pz.dTdt.old[istage - 1] = th @ self.ops.i2r2.T
+            ta.old[istage - 1] = th @ self.ops.i2r2.T
         if l_calc_lin:
             imp = np.empty_like(th)
             for i in range(pz.M):
-                imp[i] = d["TdiffFac"] * pz.hdif[i] * (self.t_rhsi[i] @ th[i])
-            pz.dTdt.impl[istage - 1] = imp
+                imp[i] = diff * pz.hdif[i] * (self.t_rhsi[i] @ th[i])
+            ta.impl[istage - 1] = imp
 
-    def _buo_coeffs(self):
+    def _buo_coeffs(self, xi=None):
         """I4 r^4 (I2 r^2 with the influence-matrix variant) of the buoyancy
-        -BuoFac rgrav/r i m T, m > 0, in Chebyshev space
-        (update_psi_integ_smat.f90:266-330, :1075-1111;
-        update_psi_integ_dmat.f90:171-240, :748-779)."""
+        -BuoFac rgrav/r i m T - ChemFac rgrav/r i m xi, m > 0, in Chebyshev
+        space (update_psi_integ_smat.f90:266-330, :1075-1111;
+        update_psi_integ_dmat.f90:171-240, :748-779).  ``xi`` replaces the
+        composition field (the bridge step passes psi there)."""
         pz, d = self.pz, self.pz.d
         m = pz.mvec[:, None].astype(float)
         buo = -d["BuoFac"] * pz.rgrav * pz.or1 * 1j * m * pz.temp
+        if pz.l_chem:
+            buo = buo - d["ChemFac"] * pz.rgrav * pz.or1 * 1j * m * (pz.xi if xi is None else xi)
         buo[0] = 0.0
         buo = pz.cheb.costf1(buo)
         out = buo @ (self.ops.i2r2 if self.dmat else self.ops.i4r4).T
         out[0] = 0.0
         return out
 
-    def psi_rhs_imp(self, istage, l_calc_lin):
+    def psi_rhs_imp(self, istage, l_calc_lin, xi=None):
         """get_psi_rhs_imp_int_smat (update_psi_integ_smat.f90:960-1115) or
         get_psi_rhs_imp_int_dmat (update_psi_integ_dmat.f90:625-781), which
         works on omega (u_phi for m = 0) instead of psi_hat."""
@@ -341,29 +370,32 @@ class IntegScheme:
             for i in range(pz.M):
                 imp[i] = self.p_rhsil[i] @ src[i]
             if d["l_buo_imp"]:
-                imp = imp + self._buo_coeffs()
+                imp = imp + self._buo_coeffs(xi)
             pz.dpsidt.impl[istage - 1] = imp
 
     # -- solves (mloop.f90:84-100) -------------------------------------------
-    def update_temp(self, l_log_next):
-        """update_temp_int (update_temp_integ.f90:179-298)."""
+    def update_temp(self, l_log_next, kind="temp"):
+        """update_temp_int (update_temp_integ.f90:179-298) or update_xi_int
+        (update_xi_integ.f90:167-278)."""
         pz, ts, c = self.pz, self.pz.ts, self.pz.cheb
-        work = ts.set_imex_rhs(pz.dTdt)
+        f, df, ta, _, top, bot = pz._sc(kind)[:6]
+        mats = self.tmats if kind == "temp" else self.ximats
+        work = ts.set_imex_rhs(ta)
         th = np.empty_like(work)
         for i in range(pz.M):
             rhs = work[i].copy()
-            rhs[0] = pz.topt[i]
-            rhs[1] = pz.bott[i]
-            th[i] = self._solve(self.tmats[i], rhs)
-        pz.temp_hat = th
-        pz.temp = c.costf1(th)
-        ts.rotate_imex(pz.dTdt)
+            rhs[0] = top[i]
+            rhs[1] = bot[i]
+            th[i] = self._solve(mats[i], rhs)
+        setattr(pz, f + "_hat", th)
+        setattr(pz, f, c.costf1(th))
+        ts.rotate_imex(ta)
         if ts.istage == ts.nstages:
-            self.temp_rhs_imp(1, pz._calc_rhs(1))
+            self.temp_rhs_imp(1, pz._calc_rhs(1), kind)
         else:
-            self.temp_rhs_imp(ts.istage + 1, pz._calc_rhs(ts.istage + 1))
+            self.temp_rhs_imp(ts.istage + 1, pz._calc_rhs(ts.istage + 1), kind)
         if l_log_next:
-            pz.dtemp = c.get_dr(pz.temp)
+            setattr(pz, df, c.get_dr(getattr(pz, f)))
 
     def update_psi(self):
         """update_psi_int_smat (update_psi_integ_smat.f90:247-573)."""

@@ -83,9 +83,16 @@ class Params:
     l_ek_pump: bool = False
     l_temp_advz: bool = False
     tcond_fac: float = 1.0
+    raxi: float = 0.0                 # composition (raxi /= 0 switches it on)
+    sc: float = 0.0
+    ktopxi: int = 1
+    kbotxi: int = 1
+    xicond_fac: float = 1.0
     # start_field
     init_t: int = 0
     amp_t: float = 0.0
+    init_xi: int = 0
+    amp_xi: float = 0.0
     init_u: int = 0
     amp_u: float = 0.0
     # output_control
@@ -101,6 +108,7 @@ class Params:
         d["ek"] = ek
         d["l_non_rot"] = l_non_rot
         d["l_heat"] = self.ra != 0.0
+        d["l_chem"] = self.raxi != 0.0                             # namelists.f90:323-327
         d["tadvz_fac"] = 1.0 if self.l_temp_advz else 0.0
         d["r_cmb"] = 1.0 / (1.0 - self.radratio)
         d["r_icb"] = d["r_cmb"] - 1.0
@@ -111,20 +119,27 @@ class Params:
             l_cor_imp = False  # namelists.f90:448-457
         d["l_coriolis_imp"] = l_cor_imp
         d["l_buo_imp"] = "IMP" in self.buo_term.upper()
+        ch = d["l_chem"]
         if l_non_rot:
             d["CorFac"] = 0.0
             d["BuoFac"] = self.ra / self.pr if d["l_heat"] else 0.0
             d["TdiffFac"] = 1.0 / self.pr if d["l_heat"] else 0.0
+            d["ChemFac"] = self.raxi / self.sc if ch else 0.0
+            d["XidiffFac"] = 1.0 / self.sc if ch else 0.0
             d["ViscFac"] = 1.0
         elif "ROT" in self.time_scale.upper():
             d["CorFac"] = 2.0
             d["BuoFac"] = self.ra * ek * ek / self.pr if d["l_heat"] else 0.0
             d["TdiffFac"] = ek / self.pr if d["l_heat"] else 0.0
+            d["ChemFac"] = self.raxi * ek * ek / self.sc if ch else 0.0
+            d["XidiffFac"] = ek / self.sc if ch else 0.0
             d["ViscFac"] = ek
         else:
             d["CorFac"] = 2.0 / ek
             d["BuoFac"] = self.ra / self.pr if d["l_heat"] else 0.0
             d["TdiffFac"] = 1.0 / self.pr if d["l_heat"] else 0.0
+            d["ChemFac"] = self.raxi / self.sc if ch else 0.0
+            d["XidiffFac"] = 1.0 / self.sc if ch else 0.0
             d["ViscFac"] = 1.0
         return d
 
@@ -824,6 +839,16 @@ class Pizza:
         self.l_integ = not d["l_cheb_coll"]
         self.temp_hat = np.zeros(shp, complex)
         self.psi_hat = np.zeros(shp, complex)
+        # composition (update_xi_coll.f90, update_xi_integ.f90): the same
+        # containers as temperature; they stay zero when raxi = 0
+        self.l_chem = d["l_chem"]
+        self.dxidt = TArray(shp, ts.nold, ts.nimp, ts.nexp)
+        self.xi = np.zeros(shp, complex)
+        self.dxi = np.zeros(shp, complex)
+        self.xi_hat = np.zeros(shp, complex)
+        self.topxi = np.zeros(self.M, complex)
+        self.botxi = np.zeros(self.M, complex)
+        self._dVsXi = np.zeros(shp, complex)
         if self.l_integ:
             from .pizza_integ import IntegScheme
             self.integ = IntegScheme(self)
@@ -855,6 +880,15 @@ class Pizza:
             self.dtcond = p.tcond_fac * (self.or1 / math.log(p.radratio))
         else:
             raise NotImplementedError("only fixed-temperature boundaries are restated")
+        # conducting composition: the same 2D profile with xicond_fac (radial.f90:194-195)
+        if p.ktopxi == 1 and p.kbotxi == 1:
+            self.xicond = p.xicond_fac * (np.log(r / r_cmb) / math.log(p.radratio))
+            self.dxicond = p.xicond_fac * (self.or1 / math.log(p.radratio))
+        elif d["l_chem"]:
+            raise NotImplementedError("only fixed-composition boundaries are restated")
+        else:
+            self.xicond = np.zeros(N)
+            self.dxicond = np.zeros(N)
         ek_pump_fac = 1.0 if (p.l_ek_pump and not d["l_non_rot"]) else 0.0
         z = np.zeros(N)
         if d["l_non_rot"]:
@@ -891,10 +925,14 @@ class Pizza:
             self.temp = self.temp + np.asarray(temp0, complex)
         elif p.init_t != 0:
             self._init_prop(p.init_t, p.amp_t)
+        if self.l_chem and p.init_xi != 0:
+            self._init_prop(p.init_xi, p.amp_xi, "xi")        # init_fields.f90:123
         if p.init_u != 0:
             self._init_u()
         c = self.cheb
         self.dtemp = c.get_dr(self.temp)
+        if self.l_chem:
+            self.dxi = c.get_dr(self.xi)
         work = c.get_dr(self.up)
         m = self.mvec[:, None]
         self.om = work + self.or1 * self.up - self.or1 * 1j * m * self.us
@@ -902,6 +940,8 @@ class Pizza:
             self.integ.start()
             return
         self._temp_rhs_imp(1, True, l_in_cheb=False)
+        if self.l_chem:
+            self._xi_rhs_imp(1, True, l_in_cheb=False)
         self._psi_rhs_imp(1, True, l_in_cheb=False)
 
     def _map_field(self, f, n_old, phys, lbc):
@@ -940,7 +980,8 @@ class Pizza:
         needs more old or implicit slots than the file holds (:398-425).
         ``ck`` is a dict with header (time, family, nexp, nimp, nold, dt, ek,
         n_r_max, l_cheb_coll), us, up, temp, hist_P, hist_T (expl 2..nexp,
-        impl 2..nimp, old 2..nold of the file's scheme)."""
+        impl 2..nimp, old 2..nold of the file's scheme) and, when the file
+        holds composition, xi and hist_Xi."""
         ts, h = self.ts, ck["header"]
         self.time = h["time"]
         nd = len(h["dt"])
@@ -953,6 +994,9 @@ class Pizza:
         self.us = self._map_field(ck["us"], n_old, True, False)
         self.up = self._map_field(ck["up"], n_old, True, False)
         self.temp = self._map_field(ck["temp"], n_old, True, False)
+        has_xi = self.l_chem and ck.get("xi") is not None
+        if has_xi:
+            self.xi = self._map_field(ck["xi"], n_old, True, False)
         if h["family"] == "MULTISTEP":
             order = ([("expl", k, True) for k in range(2, h["nexp"] + 1)]
                      + [("impl", k, True) for k in range(2, h["nimp"] + 1)]
@@ -961,10 +1005,16 @@ class Pizza:
                 if ts.family == "MULTISTEP" and k <= {"expl": ts.nexp, "impl": ts.nimp, "old": ts.nold}[kind]:
                     getattr(self.dpsidt, kind)[k - 1] = self._map_field(aP, n_old, coll_old, lbc)
                     getattr(self.dTdt, kind)[k - 1] = self._map_field(aT, n_old, coll_old, lbc)
+            if has_xi:
+                for (kind, k, lbc), aX in zip(order, ck.get("hist_Xi", [])):
+                    if ts.family == "MULTISTEP" and k <= {"expl": ts.nexp, "impl": ts.nimp, "old": ts.nold}[kind]:
+                        getattr(self.dxidt, kind)[k - 1] = self._map_field(aX, n_old, coll_old, lbc)
         if self.l_integ:
             self.psi = self.integ.psi_from_us()
         c = self.cheb
         self.dtemp = c.get_dr(self.temp)
+        if self.l_chem:
+            self.dxi = c.get_dr(self.xi)
         work = c.get_dr(self.up)
         m = self.mvec[:, None]
         self.om = work + self.or1 * self.up - self.or1 * 1j * m * self.us
@@ -972,6 +1022,8 @@ class Pizza:
             self.integ.start()
         else:
             self._temp_rhs_imp(1, True, l_in_cheb=False)
+            if self.l_chem:
+                self._xi_rhs_imp(1, True, l_in_cheb=False)
             self._psi_rhs_imp(1, True, l_in_cheb=False)
         self.l_AB1 = h.get("ek", self.d["ek"]) != self.d["ek"]
         if ts.family == "MULTISTEP":
@@ -985,15 +1037,17 @@ class Pizza:
         else:
             self.l_bridge_step = False
 
-    def _init_prop(self, init_t, amp):
-        """initProp (init_fields.f90:260-376), modes init_t>0 and -1."""
+    def _init_prop(self, init_t, amp, field="temp"):
+        """initProp (init_fields.f90:260-376), modes init_t>0 and -1, on the
+        temperature or (field="xi") the composition."""
         N, M = self.N, self.M
+        tgt = getattr(self, field)
         r = self.r
         r_cmb, r_icb = self.d["r_cmb"], self.d["r_icb"]
         t1 = np.sin(np.pi * (r - r_icb))
         if init_t > 0:
             idx = init_t // self.p.minc
-            self.temp[idx, :] += t1 * amp
+            tgt[idx, :] += t1 * amp
         elif init_t == -1:
             sigma_r = 0.1 / math.sqrt(2.0)
             rc = 0.5 * (r_cmb + r_icb)
@@ -1025,7 +1079,7 @@ class Pizza:
             for i in range(N):
                 c_r = amp * gasp[i]
                 func = c_r * np.exp(-(phi - phi0) ** 2 / 0.2 ** 2)
-                self.temp[:, i] += self._fft(func)
+                tgt[:, i] += self._fft(func)
         else:
             raise NotImplementedError("random init_t uses Fortran random_number; not restated")
 
@@ -1087,6 +1141,13 @@ class Pizza:
         dtempdt = self._fft(upT)
         dVsT = self._fft(usT)
         dtempdt = -or1 * 1j * m * dtempdt - (1.0 - d["tadvz_fac"]) * self.beta[:, None] * or1 * dVsT
+        if self.l_chem:
+            # composition: r us xi and up xi, no beta term (radial_loop.f90:320-323, :356-374);
+            # dxi/dt goes to its explicit slot, r us xi to finish_explicit
+            X_g = self._ifft(self.xi.T)
+            dxidt = self._fft(up_g * X_g)
+            self._dVsXi = self._fft(r * us_g * X_g).T.copy()
+            self.dxidt.expl[self.ts.istage - 1] = (-or1 * 1j * m * dxidt).T.copy()
         dpsidt[:, 0] = -usom
         dpsidt[:, 1:] = -or1 * 1j * m[1:] * dpsidt[:, 1:]
         return dtempdt.T.copy(), dVsT.T.copy(), dpsidt.T.copy(), dVsOm.T.copy()
@@ -1104,6 +1165,10 @@ class Pizza:
         e = self.dTdt.expl[ist]
         e = e - self.or1 * work - self.us * (self.dtcond - d["tadvz_fac"] * self.beta * self.tcond)
         self.dTdt.expl[ist] = e
+        if self.l_chem:
+            # finish_exp_xi_coll (update_xi_coll.f90:142-166)
+            work = c.get_dr(self._dVsXi)
+            self.dxidt.expl[ist] = self.dxidt.expl[ist] - self.or1 * work - self.us * self.dxicond
         # finish_exp_psi_coll_{dmat,smat}
         work = c.get_dr(dVsOm)
         e = self.dpsidt.expl[ist].copy()
@@ -1119,6 +1184,8 @@ class Pizza:
                 e[nz] = e[nz] + d["CorFac"] * self.beta * self.us[nz]
         if not d["l_buo_imp"]:
             e[nz] = e[nz] - d["BuoFac"] * self.rgrav * self.or1 * 1j * m[nz] * self.temp[nz]
+            if self.l_chem:
+                e[nz] = e[nz] - d["ChemFac"] * self.rgrav * self.or1 * 1j * m[nz] * self.xi[nz]
         if (not self.l_direct) and self.p.l_ek_pump:
             e[nz] = e[nz] - d["CorFac"] * self.ekpump * (
                 self.om[nz] + self.ekp_up * self.up[nz]
@@ -1159,14 +1226,25 @@ class Pizza:
         for cidx in cols:
             A[:, cidx] = self.cheb.boundary_fac * A[:, cidx]
 
-    def _temp_mat(self, m):
-        """get_tempMat (update_temp_coll.f90:310-393) with WITH_PRECOND_S."""
-        c, d, p = self.cheb, self.d, self.p
+    def _sc(self, kind):
+        """(field, radial derivative, history, diffusivity, top and bottom
+        values, top and bottom kinds) of an advected scalar: "temp" or "xi"."""
+        d, p = self.d, self.p
+        if kind == "temp":
+            return "temp", "dtemp", self.dTdt, d["TdiffFac"], self.topt, self.bott, p.ktopt, p.kbott
+        return "xi", "dxi", self.dxidt, d["XidiffFac"], self.topxi, self.botxi, p.ktopxi, p.kbotxi
+
+    def _temp_mat(self, m, kind="temp"):
+        """get_tempMat (update_temp_coll.f90:310-393) or get_xiMat
+        (update_xi_coll.f90:321-393, the same with XidiffFac) with
+        WITH_PRECOND_S."""
+        c, p = self.cheb, self.p
         N, n_max = self.N, self.n_max
+        _, _, _, diff, _, _, ktop, kbot = self._sc(kind)
         A = np.zeros((N, N))
-        A[0, :n_max] = c.rnorm * (c.rMat[0, :n_max] if p.ktopt == 1 else c.drMat[0, :n_max])
-        A[N - 1, :n_max] = c.rnorm * (c.rMat[N - 1, :n_max] if p.kbott == 1 else c.drMat[N - 1, :n_max])
-        w = self.ts.wimp_lin[0] * d["TdiffFac"] * self.hdif[m // p.minc]
+        A[0, :n_max] = c.rnorm * (c.rMat[0, :n_max] if ktop == 1 else c.drMat[0, :n_max])
+        A[N - 1, :n_max] = c.rnorm * (c.rMat[N - 1, :n_max] if kbot == 1 else c.drMat[N - 1, :n_max])
+        w = self.ts.wimp_lin[0] * diff * self.hdif[m // p.minc]
         i = slice(1, N - 1)
         dm2 = float(m) * float(m)
         A[i, :] = c.rnorm * (c.rMat[i] - w * (c.d2rMat[i] + self.or1[i, None] * c.drMat[i]
@@ -1285,6 +1363,8 @@ class Pizza:
             self._mats_built = True
             return
         self.tmats = [self._temp_mat(int(self.mvec[i])) for i in range(M)]
+        if self.l_chem:
+            self.ximats = [self._temp_mat(int(self.mvec[i]), "xi") for i in range(M)]
         self.uphi = self._uphi_mat()
         if self.l_direct:
             self.psimats = [None] + [self._psi_mat_smat(int(self.mvec[i])) for i in range(1, M)]
@@ -1349,24 +1429,32 @@ class Pizza:
             self.infl[i] = [[bot3[i] / det, -top3[i] / det], [-bot2[i] / det, top2[i] / det]]
 
     # -- implicit terms ------------------------------------------------------
-    def _temp_rhs_imp(self, istage, l_calc_lin, l_in_cheb):
-        """get_temp_rhs_imp_coll (update_temp_coll.f90:178-236)."""
+    def _temp_rhs_imp(self, istage, l_calc_lin, l_in_cheb, kind="temp"):
+        """get_temp_rhs_imp_coll (update_temp_coll.f90:178-236) or
+        get_xi_rhs_imp_coll (update_xi_coll.f90:168-216)."""
         if self.l_integ:
-            return self.integ.temp_rhs_imp(istage, l_calc_lin)
-        c, d = self.cheb, self.d
+            return self.integ.temp_rhs_imp(istage, l_calc_lin, kind)
+        c = self.cheb
+        f, df, ta, diff = self._sc(kind)[:4]
+        fld = getattr(self, f)
         if l_calc_lin:
-            self.dtemp, work = c.get_ddr(self.temp, l_dct=not l_in_cheb)
+            dfld, work = c.get_ddr(fld, l_dct=not l_in_cheb)
+            setattr(self, df, dfld)
             if l_in_cheb:
-                self.temp = c.costf1(self.temp)
+                fld = c.costf1(fld)
         else:
             if l_in_cheb:
-                self.temp = c.costf1(self.temp)
+                fld = c.costf1(fld)
+        setattr(self, f, fld)
         if istage == 1:
-            self.dTdt.old[istage - 1] = self.temp.copy()
+            ta.old[istage - 1] = fld.copy()
         if l_calc_lin:
             dm2 = (self.mvec.astype(float) ** 2)[:, None]
-            self.dTdt.impl[istage - 1] = d["TdiffFac"] * self.hdif[:, None] * (
-                work + self.or1 * self.dtemp - dm2 * self.or2 * self.temp)
+            ta.impl[istage - 1] = diff * self.hdif[:, None] * (
+                work + self.or1 * getattr(self, df) - dm2 * self.or2 * fld)
+
+    def _xi_rhs_imp(self, istage, l_calc_lin, l_in_cheb):
+        return self._temp_rhs_imp(istage, l_calc_lin, l_in_cheb, kind="xi")
 
     def _psi_rhs_imp(self, istage, l_calc_lin, l_in_cheb):
         """get_psi_rhs_imp_coll_{dmat,smat} (update_psi_coll_dmat.f90:554-682,
@@ -1401,36 +1489,44 @@ class Pizza:
                     imp = imp + d["CorFac"] * self.beta * self.us
             if d["l_buo_imp"]:
                 imp = imp - self.rgrav * self.or1 * d["BuoFac"] * 1j * m * self.temp
+                if self.l_chem:
+                    imp = imp - self.rgrav * self.or1 * d["ChemFac"] * 1j * m * self.xi
             imp[0] = (d["ViscFac"] * self.hdif[0] * (d2uphi0 + self.or1 * duphi0 - self.or2 * uphi0)
                       - d["CorFac"] * self.ekpump * uphi0)
             self.dpsidt.impl[istage - 1] = imp
 
     # -- solves (mloop) ------------------------------------------------------
-    def update_temp(self, lMat, l_log_next):
-        """update_temp_co (update_temp_coll.f90:66-150)."""
+    def update_temp(self, lMat, l_log_next, kind="temp"):
+        """update_temp_co (update_temp_coll.f90:66-150) or update_xi_co
+        (update_xi_coll.f90:66-140)."""
         if self.l_integ:
-            return self.integ.update_temp(l_log_next)
+            return self.integ.update_temp(l_log_next, kind)
         N, M, n_max = self.N, self.M, self.n_max
         ts = self.ts
-        work = ts.set_imex_rhs(self.dTdt)
-        temp = np.zeros((M, N), complex)
+        f, df, ta, _, top, bot = self._sc(kind)[:6]
+        mats = self.tmats if kind == "temp" else self.ximats
+        work = ts.set_imex_rhs(ta)
+        fld = np.zeros((M, N), complex)
         for i in range(M):
-            (lu_piv, fac) = self.tmats[i]
+            (lu_piv, fac) = mats[i]
             rhs = np.empty(N, complex)
-            rhs[0] = self.topt[i]
-            rhs[N - 1] = self.bott[i]
+            rhs[0] = top[i]
+            rhs[N - 1] = bot[i]
             rhs[1:N - 1] = work[i, 1:N - 1]
             rhs = fac * rhs
             x = self._solve_real(lu_piv, rhs)
-            temp[i, :n_max] = x[:n_max]
-        self.temp = temp
-        ts.rotate_imex(self.dTdt)
+            fld[i, :n_max] = x[:n_max]
+        setattr(self, f, fld)
+        ts.rotate_imex(ta)
         if ts.istage == ts.nstages:
-            self._temp_rhs_imp(1, self._calc_rhs(1), l_in_cheb=True)
+            self._temp_rhs_imp(1, self._calc_rhs(1), l_in_cheb=True, kind=kind)
         else:
-            self._temp_rhs_imp(ts.istage + 1, self._calc_rhs(ts.istage + 1), l_in_cheb=True)
+            self._temp_rhs_imp(ts.istage + 1, self._calc_rhs(ts.istage + 1), l_in_cheb=True, kind=kind)
         if l_log_next:
-            self.dtemp = self.cheb.get_dr(self.temp)
+            setattr(self, df, self.cheb.get_dr(getattr(self, f)))
+
+    def update_xi(self, lMat, l_log_next):
+        return self.update_temp(lMat, l_log_next, kind="xi")
 
     def update_om(self):
         """update_om_coll_dmat (update_psi_coll_dmat.f90:126-466) or
@@ -1453,10 +1549,13 @@ class Pizza:
         buo = None
         if d["l_buo_imp"]:
             buo = ts.wimp_lin[0] * d["BuoFac"] * self.rgrav * self.or1
+            buo_xi = ts.wimp_lin[0] * d["ChemFac"] * self.rgrav * self.or1
         for i in range(1, M):
             rhs = np.zeros(N, complex)
             if buo is not None:
                 rhs[1:N - 1] = work[i, 1:N - 1] - buo[1:N - 1] * 1j * m[i] * self.temp[i, 1:N - 1]
+                if self.l_chem:
+                    rhs[1:N - 1] = rhs[1:N - 1] - buo_xi[1:N - 1] * 1j * m[i] * self.xi[i, 1:N - 1]
             else:
                 rhs[1:N - 1] = work[i, 1:N - 1]
             if self.l_direct:
@@ -1553,6 +1652,16 @@ class Pizza:
         self._temp_rhs_imp(1, self._calc_rhs(1), l_in_cheb=False)
         if l_log_next:
             self.dtemp = c.get_dr(self.temp)
+        if self.l_chem:
+            # assemble_xi_coll (update_xi_coll.f90:218-269): no dxi refresh
+            work = ts.assemble_imex(self.dxidt)
+            xi = self.xi.copy()
+            xi[:, 1:N - 1] = work[:, 1:N - 1]
+            xi[0, 1:N - 1] = work[0, 1:N - 1].real + 0j
+            xi[:, 0] = self.topxi
+            xi[:, N - 1] = self.botxi
+            self.xi = xi
+            self._xi_rhs_imp(1, self._calc_rhs(1), l_in_cheb=False)
         # streamfunction from the assembled vorticity
         work = ts.assemble_imex(self.dpsidt)
         up0 = np.zeros(N)
@@ -1613,6 +1722,8 @@ class Pizza:
                 if lMat or not self._mats_built:
                     self.build_matrices()
                 self.update_temp(lMat, l_log_next)
+                if self.l_chem:
+                    self.update_xi(lMat, l_log_next)
                 self.update_om()
                 ts.istage += 1
         if ts.l_assembly:
@@ -1652,7 +1763,15 @@ class Pizza:
         if (self.l_bridge_step and ts.time_scheme != "CNAB2"
                 and n_time_step <= ts.nold - 1 and ts.family == "MULTISTEP"):
             self._temp_rhs_imp(1, True, l_in_cheb=False)
-            self._psi_rhs_imp(1, True, l_in_cheb=False)
+            if self.l_chem:
+                self._xi_rhs_imp(1, True, l_in_cheb=False)
+            if self.l_integ and self.l_direct:
+                # step_time.f90:497-498 hands psi_Mloc to get_psi_rhs_imp_int_smat
+                # in the place of xi_Mloc: with composition on, the bridge's
+                # implicit buoyancy takes -ChemFac rgrav/r i m psi
+                self.integ.psi_rhs_imp(1, True, xi=self.psi)
+            else:
+                self._psi_rhs_imp(1, True, l_in_cheb=False)
             ts.bridge_with_cnab2()
         if self.l_AB1 and n_time_step == 1:
             ts.wexp[0] = ts.dt[0]
@@ -1661,6 +1780,8 @@ class Pizza:
         if lMat or not self._mats_built:
             self.build_matrices()
         self.update_temp(lMat, l_log_next)
+        if self.l_chem:
+            self.update_xi(lMat, l_log_next)
         self.update_om()
         ts.istage += 1
         return lMat
@@ -1669,11 +1790,11 @@ class Pizza:
     def spectra(self):
         """calculate_spectra (spectra.f90:104-196), the snapshot part: per m
         the rInt_R of pi cc2real(f) r height for f = us, up, om, temp, and
-        xi (zero: no composition).  (M, 5) array."""
+        xi (zero without composition).  (M, 5) array."""
         c = self.cheb
         out = np.zeros((self.M, 5))
         for i in range(self.M):
-            for k, f in enumerate((self.us, self.up, self.om, self.temp)):
+            for k, f in enumerate((self.us, self.up, self.om, self.temp, self.xi)):
                 z = f[i]
                 c2 = z.real ** 2 if i == 0 else 2.0 * (z.real ** 2 + z.imag ** 2)
                 out[i, k] = c.rInt_R(np.pi * c2 * self.r * self.height)

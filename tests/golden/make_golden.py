@@ -16,6 +16,11 @@ first run starts from the namelist and needs no checkpoint):
   RotIntegContinue  rows 201-216  (e_kin_3D, RotInteg's second run: its first run's
                                    final state read onto n_r_max=97, m_max=64, integ
                                    dmat SBDF3 with the CNAB2 bridge and AB1)
+  FingConv          rows 0-5      (e_kin, fingering convection: temperature and
+                                   composition, non-rotating integ smat SBDF3)
+  FingConvContinue  rows 6-11     (e_kin, FingConv's second run: its first run's final
+                                   state read onto the n_r_max=33 collocation grid,
+                                   DIRK BPR353)
 
 A case with "restart_from" starts from the final state of that case's run
 (written as a checkpoint and read back) instead of its own start fields;
@@ -68,6 +73,19 @@ CASES = {
                     l_rerror_fix=True, rerror_fac=5e2, courfac=4.0, time_scale="ROT", time_scheme="SBDF3",
                     ra=2.0e6, pr=1.0, ek=1.0e-4, radratio=0.35, g0=0.0, g1=1.0, g2=0.0, ktopv=2, kbotv=2,
                     l_ek_pump=True, n_log_step=20)),
+    "FingConv": dict(
+        rows=6, series="e_kin",
+        params=dict(n_r_max=49, n_cheb_max=32, m_max=32, n_time_steps=500, dtMax=1e-3, l_non_rot=True,
+                    cheb_method="INTEG", time_scheme="SBDF3", ra=-1.0e4, pr=0.3, raxi=2.0e4, sc=3.0,
+                    ek=1.0e-3, radratio=0.35, g0=1.0, g1=0.0, g2=0.0, ktopt=1, kbott=1, ktopxi=1,
+                    kbotxi=1, ktopv=2, kbotv=2, init_t=-1, amp_t=2.5e-4, init_xi=0, amp_xi=2.5e-4,
+                    n_log_step=100)),
+    "FingConvContinue": dict(
+        rows=6, skip=6, series="e_kin", restart_from="FingConv",
+        params=dict(n_r_max=33, n_cheb_max=33, m_max=32, n_time_steps=500, dtMax=1e-3, l_non_rot=True,
+                    cheb_method="COLL", time_scheme="BPR353", ra=-1.0e4, pr=0.3, raxi=2.0e4, sc=3.0,
+                    ek=1.0e-3, radratio=0.35, g0=1.0, g1=0.0, g2=0.0, ktopt=1, kbott=1, ktopxi=1,
+                    kbotxi=1, ktopv=2, kbotv=2, n_log_step=100)),
 }
 
 

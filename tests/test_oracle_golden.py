@@ -40,7 +40,8 @@ def oracle_run(case):
 
 def checkpoint_of(sim):
     """What write_checkpoint_mloc stores of a multistep run, as the oracle's
-    reader takes it: header, fields and history slots 2..n."""
+    reader takes it: header, fields (composition too when the run has it)
+    and history slots 2..n."""
     ts, d = sim.ts, sim.d
     order = ([("expl", k) for k in range(2, ts.nexp + 1)] + [("impl", k) for k in range(2, ts.nimp + 1)]
              + [("old", k) for k in range(2, ts.nold + 1)])
@@ -48,7 +49,9 @@ def checkpoint_of(sim):
                            dt=ts.dt.copy(), ek=d["ek"], n_r_max=sim.N, l_cheb_coll=d["l_cheb_coll"]),
             "us": sim.us.copy(), "up": sim.up.copy(), "temp": sim.temp.copy(),
             "hist_P": [getattr(sim.dpsidt, k)[s - 1].copy() for k, s in order],
-            "hist_T": [getattr(sim.dTdt, k)[s - 1].copy() for k, s in order]}
+            "hist_T": [getattr(sim.dTdt, k)[s - 1].copy() for k, s in order],
+            "xi": sim.xi.copy() if sim.l_chem else None,
+            "hist_Xi": [getattr(sim.dxidt, k)[s - 1].copy() for k, s in order] if sim.l_chem else []}
 
 
 @pytest.mark.parametrize("case", sorted(CASES))
