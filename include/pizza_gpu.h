@@ -109,6 +109,10 @@ typedef struct pz_config {
   int    l_rerror_fix; /* round-off threshold in the real m = 0 Chebyshev
                           derivative recursions (radial_derivatives.f90)   */
   double rerror_fac;   /* threshold = rerror_fac * epsilon (500)            */
+  double raxi, sc;     /* composition: raxi /= 0 switches on the xi equation
+                          (update_xi_coll.f90, update_xi_integ.f90), sc > 0 */
+  int    ktopxi, kbotxi; /* composition BCs: 1 = fixed composition          */
+  double xicond_fac;   /* rescaling of the conducting composition (1)       */
 } pz_config;
 
 typedef struct pz_handle pz_handle;
@@ -137,6 +141,16 @@ int pz_set_state(pz_handle* h, int inst, const double* us, const double* up,
 int pz_set_state_all(pz_handle* h, const double* us, const double* up,
                      const double* temp);
 
+/* pz_set_state with the composition perturbation xi (on top of the
+ * conducting profile; NULL = zero) of an instance with raxi /= 0
+ * (init_fields.f90:54-258 with l_chem).  pz_set_state leaves xi zero. */
+int pz_set_state_xi(pz_handle* h, int inst, const double* us, const double* up,
+                    const double* temp, const double* xi);
+
+/* Composition of one instance (complex (n_m, n_r) arrays, either may be
+ * NULL): xi and d xi/dr.  Zero without composition. */
+int pz_get_state_xi(pz_handle* h, int inst, double* xi, double* dxi);
+
 /* Advance every instance by n_steps time steps: for each step the stage body
  * of time_loop, with the CFL decision, weight update and matrix rebuild done
  * on the device.  The step is captured once in a CUDA graph and replayed.
@@ -155,7 +169,8 @@ int pz_get_state(pz_handle* h, int inst, double* us, double* up, double* om,
 
 /* History slots of the IMEX time arrays (type_tarray, src/time_array.f90:11-71)
  * at a step boundary, in the layout of pz_set_state: field 0 temperature,
- * 1 vorticity (u_phi for m = 0); kind 0 old, 1 impl, 2 expl; slot 1-based
+ * 1 vorticity (u_phi for m = 0), 2 composition (instances with raxi /= 0);
+ * kind 0 old, 1 impl, 2 expl; slot 1-based
  * as in dfdt%old(:,:,slot).  Slot 1 of old/impl is the current state's
  * (recomputed from the fields by pz_set_state); expl slot 1 is formed by the
  * next step.  These carry a multistep run across a checkpoint
@@ -174,8 +189,9 @@ int pz_set_step_state(pz_handle* h, int inst, double time, const double* dt, int
 
 /* Snapshot spectra of one instance's current state, computed on the device
  * (calculate_spectra, src/spectra.f90:104-196): out receives n_m_max rows
- * of 4 doubles, for each m the r-integral (rInt_R) of
- * pi cc2real(f(m, r)) r height(r) for f = us, up, om, temp. */
+ * of 5 doubles, for each m the r-integral (rInt_R) of
+ * pi cc2real(f(m, r)) r height(r) for f = us, up, om, temp, xi (zero
+ * without composition). */
 int pz_get_spectra(pz_handle* h, int inst, double* out);
 
 /* l_AB1 of read_checkpoint (src/checkpoints.f90:398-425): when set, the
@@ -190,8 +206,10 @@ int pz_set_restart_ab1(pz_handle* h, int inst, int l_ab1);
  *   time, us2_2D, up2_2D, up2_axi_2D,                 (e_kin, outputs.f90:677)
  *   us2_3D, up2_3D, uz2_3D, up2_axi_3D,               (e_kin_3D, outputs.f90:686)
  *   NuTop, NuBot, Nu_vol, Nu_int, tTop, tBot, beta_t, (heat, outputs.f90:791)
- *   dt                                                  (dt(1) of the step) */
-#define PZ_SERIES_COLS 16
+ *   dt,                                                 (dt(1) of the step)
+ *   ShTop, ShBot, Sh_vol, xiTop, xiBot, beta_xi        (composition, outputs.f90:825;
+ *                                                        zero without composition) */
+#define PZ_SERIES_COLS 22
 int pz_get_series(pz_handle* h, int inst, double* rows, int* n_rows);
 
 /* Sizes of one instance: n_r_max, n_m_max, n_phi_max. */
@@ -295,11 +313,12 @@ int pz_set_ra(pz_handle* h, int inst, double ra);
  * `which` in 0..PZ_INTEG_OPS-1 selects I2[r f], I2[r^2 f], I2[f],
  * I2[r^2 f'' + r f'], I2[r^2 f'' + r f' - f], I4[r^3 f], I4[r^4 f], then
  * Q0, Q1 (intcheb4rmult4laplrot = Q0 + m^2 Q1), S0, S1, S2
- * (intcheb4rmult4laplrot2 = S0 + m^2 S1 + m^4 S2) and P0, P1
- * (intcheb2rmult2laplrot = -(P0 + m^2 P1)); all times rnorm with the
- * tau rows zero.  out: n_r_max^2 doubles, column-major; *bandwidth: max |i-j|
- * of a nonzero entry. */
-#define PZ_INTEG_OPS 14
+ * (intcheb4rmult4laplrot2 = S0 + m^2 S1 + m^4 S2), P0, P1
+ * (intcheb2rmult2laplrot = -(P0 + m^2 P1)), N0, N1 (intcheb4rmult4lapl
+ * = N0 + m^2 N1) and L0, L1, L2 (intcheb4rmult4lapl2 = L0 + m^2 L1 +
+ * m^4 L2); all times rnorm with the tau rows zero.  out: n_r_max^2 doubles,
+ * column-major; *bandwidth: max |i-j| of a nonzero entry. */
+#define PZ_INTEG_OPS 19
 int pz_integ_operator(int n_r_max, double radratio, int which, double* out, int* bandwidth);
 
 int pz_destroy(pz_handle* h);

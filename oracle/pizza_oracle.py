@@ -833,7 +833,7 @@ class Pizza:
         self.lMatNext = True
         self.l_bridge_step = True
         self.l_AB1 = False
-        self.rows = {"e_kin": [], "e_kin_3D": [], "heat": []}
+        self.rows = {"e_kin": [], "e_kin_3D": [], "heat": [], "composition": []}
         if p.l_rerror_fix:
             self.cheb.thr = p.rerror_fac * np.finfo(float).eps
         self.l_integ = not d["l_cheb_coll"]
@@ -913,10 +913,11 @@ class Pizza:
         self.vol_otc = 4.0 / 3.0 * np.pi * (r_cmb ** 2 - r_icb ** 2) ** 1.5
 
     # -- start fields (src/init_fields.f90:54-258) ---------------------------
-    def start(self, temp0=None):
+    def start(self, temp0=None, xi0=None):
         """get_start_fields without a checkpoint: zero state, dt(:)=dtMax,
-        weights, perturbation (initProp/initU or an injected ``temp0``), then
-        the derived fields and the first implicit state."""
+        weights, perturbation (initProp/initU or an injected ``temp0`` and,
+        with composition, ``xi0``), then the derived fields and the first
+        implicit state."""
         p, ts = self.p, self.ts
         self.time = 0.0
         ts.dt[:] = p.dtMax
@@ -925,7 +926,9 @@ class Pizza:
             self.temp = self.temp + np.asarray(temp0, complex)
         elif p.init_t != 0:
             self._init_prop(p.init_t, p.amp_t)
-        if self.l_chem and p.init_xi != 0:
+        if self.l_chem and xi0 is not None:
+            self.xi = self.xi + np.asarray(xi0, complex)
+        elif self.l_chem and p.init_xi != 0:
             self._init_prop(p.init_xi, p.amp_xi, "xi")        # init_fields.f90:123
         if p.init_u != 0:
             self._init_u()
@@ -1863,6 +1866,22 @@ class Pizza:
             Nu_int = round_off(Nu_int)
             beta_t = round_off(self.dtcond[N // 2 - 1] + dT[0, N // 2 - 1].real)
             rows["heat"] = [self.time, NuTop, NuBot, Nu_vol, Nu_int, tTop, tBot, beta_t]
+        if self.l_chem:
+            # composition.TAG (outputs.f90:795-827)
+            N = self.N
+            X, dX = self.xi, self.dxi
+            a_x, a_dx = c2r(X), c2r(dX)
+            sh_r = np.zeros(N)
+            for i in range(self.M):
+                sh_r = sh_r + a_dx[i] + m2[i] * self.or2 * a_x[i]
+            sh_r = sh_r * r * self.height
+            xiTop = round_off(X[0, 0].real + self.xicond[0])
+            xiBot = round_off(X[0, N - 1].real + self.xicond[N - 1])
+            ShTop = round_off(1.0 + dX[0, 0].real / self.dxicond[0])
+            ShBot = round_off(1.0 + dX[0, N - 1].real / self.dxicond[N - 1])
+            Sh_vol = round_off(1.0 + c.rInt_R(sh_r) / c.rInt_R(self.dxicond * self.dxicond * self.height * r))
+            beta_xi = round_off(self.dxicond[N // 2 - 1] + dX[0, N // 2 - 1].real)
+            rows["composition"] = [self.time, ShTop, ShBot, Sh_vol, xiTop, xiBot, beta_xi]
         return rows
 
     # -- the outer loop (src/step_time.f90:69-415) ----------------------------

@@ -33,9 +33,10 @@ KERNEL_KINDS = 9
 SOLVE_INFLUENCE, SOLVE_DIRECT = 0, 1
 CHEB_COLL, CHEB_INTEG = 0, 1
 TS_VISC, TS_ROT = 0, 1
-SERIES_COLS = 16
+SERIES_COLS = 22
 SERIES_NAMES = ("time", "us2_2D", "up2_2D", "up2_axi_2D", "us2_3D", "up2_3D", "uz2_3D",
-                "up2_axi_3D", "NuTop", "NuBot", "Nu_vol", "Nu_int", "tTop", "tBot", "beta_t", "dt")
+                "up2_axi_3D", "NuTop", "NuBot", "Nu_vol", "Nu_int", "tTop", "tBot", "beta_t", "dt",
+                "ShTop", "ShBot", "Sh_vol", "xiTop", "xiBot", "beta_xi")
 
 PZ_ERRORS = {-1: "invalid argument", -2: "CUDA error", -3: "singular matrix",
              -4: "time step too small", -5: "non-finite state", -6: "unsupported option",
@@ -60,7 +61,9 @@ class _CConfig(ctypes.Structure):
                 ("time_scheme", ctypes.c_int), ("matrix_solve", ctypes.c_int), ("corio_imp", ctypes.c_int),
                 ("buo_imp", ctypes.c_int), ("dtMax", ctypes.c_double), ("courfac", ctypes.c_double),
                 ("alpha", ctypes.c_double), ("dt_fac", ctypes.c_double), ("cheb_method", ctypes.c_int),
-                ("time_scale", ctypes.c_int), ("l_rerror_fix", ctypes.c_int), ("rerror_fac", ctypes.c_double)]
+                ("time_scale", ctypes.c_int), ("l_rerror_fix", ctypes.c_int), ("rerror_fac", ctypes.c_double),
+                ("raxi", ctypes.c_double), ("sc", ctypes.c_double), ("ktopxi", ctypes.c_int),
+                ("kbotxi", ctypes.c_int), ("xicond_fac", ctypes.c_double)]
 
 
 @dataclasses.dataclass
@@ -69,7 +72,8 @@ class Config:
     matrix_solve 'DIRECT' is pizza's coupled smat solve, 'INFLUENCE' the dmat
     influence-matrix solve (the one the adjoint covers).  cheb_method 'COLL'
     is the collocation method, 'INTEG' the sparse Chebyshev integration
-    method with tau boundary rows (direct solve, rotating runs)."""
+    method with tau boundary rows.  raxi /= 0 adds the composition equation
+    (Schmidt number sc)."""
     n_r_max: int = 32
     n_cheb_max: int | None = None
     m_max: int = 32
@@ -100,11 +104,17 @@ class Config:
     time_scale: str = "VISC"
     l_rerror_fix: bool = False
     rerror_fac: float = 500.0
+    raxi: float = 0.0
+    sc: float = 0.0
+    ktopxi: int = 1
+    kbotxi: int = 1
+    xicond_fac: float = 1.0
 
     def to_c(self) -> _CConfig:
         c = _CConfig()
         for f in ("n_r_max", "m_max", "minc", "ra", "ek", "pr", "radratio", "g0", "g1", "g2",
-                  "ktopt", "kbott", "ktopv", "kbotv", "dtMax", "courfac", "alpha", "dt_fac"):
+                  "ktopt", "kbott", "ktopv", "kbotv", "dtMax", "courfac", "alpha", "dt_fac",
+                  "raxi", "sc", "ktopxi", "kbotxi", "xicond_fac"):
             setattr(c, f, getattr(self, f))
         c.n_cheb_max = self.n_r_max if self.n_cheb_max is None else self.n_cheb_max
         c.l_ek_pump = int(bool(self.l_ek_pump))
@@ -150,6 +160,8 @@ def load_library(path: str | None = None):
     lib.pz_create.argtypes = [ctypes.POINTER(_CConfig), ctypes.c_int, ctypes.POINTER(ctypes.c_void_p)]
     lib.pz_set_state.argtypes = [ctypes.c_void_p, ctypes.c_int, dp, dp, dp]
     lib.pz_set_state_all.argtypes = [ctypes.c_void_p, dp, dp, dp]
+    lib.pz_set_state_xi.argtypes = [ctypes.c_void_p, ctypes.c_int, dp, dp, dp, dp]
+    lib.pz_get_state_xi.argtypes = [ctypes.c_void_p, ctypes.c_int, dp, dp]
     lib.pz_step.argtypes = [ctypes.c_void_p, ctypes.c_int]
     lib.pz_sync.argtypes = [ctypes.c_void_p]
     lib.pz_get_state.argtypes = [ctypes.c_void_p, ctypes.c_int, dp, dp, dp, dp, dp, dp, dp, dp]
@@ -178,7 +190,8 @@ def load_library(path: str | None = None):
     lib.pz_destroy.argtypes = [ctypes.c_void_p]
     lib.pz_last_error.argtypes = [ctypes.c_void_p]
     lib.pz_last_error.restype = ctypes.c_char_p
-    for f in ("pz_create", "pz_set_state", "pz_set_state_all", "pz_step", "pz_sync", "pz_get_state",
+    for f in ("pz_create", "pz_set_state", "pz_set_state_all", "pz_set_state_xi", "pz_get_state_xi", "pz_step",
+              "pz_sync", "pz_get_state",
               "pz_get_series", "pz_get_dims", "pz_launches_per_step", "pz_latest_rows",
               "pz_step_profile", "pz_explicit_terms", "pz_explicit_terms_noalloc", "pz_adjoint_forward",
               "pz_adjoint_backward", "pz_set_ra", "pz_get_history", "pz_set_history", "pz_get_step_state",
@@ -189,7 +202,8 @@ def load_library(path: str | None = None):
     return lib
 
 
-INTEG_OPERATORS = ("I2R1", "I2R2", "I2", "LT0", "ULAP", "I4R3", "I4R4", "Q0", "Q1", "S0", "S1", "S2", "P0", "P1")
+INTEG_OPERATORS = ("I2R1", "I2R2", "I2", "LT0", "ULAP", "I4R3", "I4R4", "Q0", "Q1", "S0", "S1", "S2", "P0", "P1",
+                   "N0", "N1", "L0", "L1", "L2")
 
 
 def integ_operator(n_r_max: int, radratio: float, name: str):
@@ -252,11 +266,16 @@ class Ensemble:
         n, m, _ = self.dims[i]
         return (m, n)
 
-    def set_state(self, i, us=None, up=None, temp=None):
-        """pizza's start fields (src/init_fields.f90:54-258) from physical fields."""
+    def set_state(self, i, us=None, up=None, temp=None, xi=None):
+        """pizza's start fields (src/init_fields.f90:54-258) from physical
+        fields; ``xi`` is the composition perturbation (raxi /= 0)."""
         shp = self.shape(i)
         a, b, c = _carr(us, shp), _carr(up, shp), _carr(temp, shp)
-        self._check(self.lib.pz_set_state(self._h, i, _dptr(a), _dptr(b), _dptr(c)))
+        if xi is None:
+            self._check(self.lib.pz_set_state(self._h, i, _dptr(a), _dptr(b), _dptr(c)))
+        else:
+            x = _carr(xi, shp)
+            self._check(self.lib.pz_set_state_xi(self._h, i, _dptr(a), _dptr(b), _dptr(c), _dptr(x)))
 
     def set_state_all(self, temps, us=None, up=None):
         """Start fields of every instance; ``temps`` is a list of (n_m, n_r) arrays."""
@@ -285,6 +304,10 @@ class Ensemble:
         out = {k: v.T.copy() for k, v in bufs.items()}
         out["time"] = t.value
         out["dt"] = dt.value
+        if self.configs[i].raxi != 0.0:
+            xi, dxi = np.zeros((n, m), np.complex128), np.zeros((n, m), np.complex128)
+            self._check(self.lib.pz_get_state_xi(self._h, i, _dptr(xi), _dptr(dxi)))
+            out["xi"], out["dxi"] = xi.T.copy(), dxi.T.copy()
         return out
 
     def series(self, i, max_rows=1024):
@@ -325,7 +348,8 @@ class Ensemble:
     # -- history and step state (checkpoints) ------------------------------
     def get_history(self, i, field, kind, slot):
         """History slot (1-based) of the time arrays: field 0 temperature, 1
-        vorticity; kind 0 old, 1 impl, 2 expl.  (n_m, n_r) complex."""
+        vorticity, 2 composition; kind 0 old, 1 impl, 2 expl.  (n_m, n_r)
+        complex."""
         n, m, _ = self.dims[i]
         buf = np.zeros((n, m), np.complex128)
         self._check(self.lib.pz_get_history(self._h, i, int(field), int(kind), int(slot), _dptr(buf.view(np.float64))))
@@ -350,11 +374,12 @@ class Ensemble:
         self._check(self.lib.pz_set_step_state(self._h, i, float(time), _dptr(d), int(n_step)))
 
     def spectra(self, i):
-        """Snapshot spectra of instance i on the device: (n_m_max, 4) array of
-        the r-integrated us^2, up^2, enstrophy and T^2 per m (spectra.f90)."""
-        out = np.zeros(4 * self.dims[i][1])
+        """Snapshot spectra of instance i on the device: (n_m_max, 5) array of
+        the r-integrated us^2, up^2, enstrophy, T^2 and xi^2 per m
+        (spectra.f90)."""
+        out = np.zeros(5 * self.dims[i][1])
         self._check(self.lib.pz_get_spectra(self._h, i, _dptr(out)))
-        return out.reshape(-1, 4)
+        return out.reshape(-1, 5)
 
     def set_restart_ab1(self, i, on=True):
         """First step after a restart with first-order explicit weights (pizza's l_AB1)."""

@@ -163,9 +163,10 @@ __global__ void k_adj_ckpt(PzAdjDev a, int c, int dir) {
   const int n = I.N, mi = it.idx;
   const long long MN = (long long)I.M * n;
   const int nh = 2 * (I.nold + I.nimp + I.nexp);
-  for (int k = 0; k < F_COUNT + nh; ++k) {
-    double2* p = reinterpret_cast<double2*>(a.d.pool + (k < F_COUNT ? I.o_fld + 2LL * k * MN
-                                                                      : I.o_hist + 2LL * (k - F_COUNT) * MN)) +
+  // the flow and temperature planes (F_US .. F_DVSOM; the adjoint runs no composition)
+  for (int k = 0; k < F_XI + nh; ++k) {
+    double2* p = reinterpret_cast<double2*>(a.d.pool + (k < F_XI ? I.o_fld + 2LL * k * MN
+                                                                   : I.o_hist + 2LL * (k - F_XI) * MN)) +
                  (long long)mi * n;
     double2* q = A.ck(a.n_snap, a.ck_planes, c, k, mi);
     if (dir == 0)
@@ -782,8 +783,10 @@ extern "C" int pz_adjoint_forward(pz_handle* h, int objective, int n_steps, int 
   if (n_window < 0 || n_window > n_steps) return pz_fail(h, PZ_E_ARG, "pz_adjoint_forward: n_window outside [0, n_steps]");
   for (int i = 0; i < h->n_inst; ++i) {
     const PzInst& I = h->inst[i];
-    if (I.scheme != PZ_CNAB2 || (I.flags & PZF_DIRECT))
-      return pz_fail(h, PZ_E_UNSUPPORTED, "pz_adjoint_forward: the adjoint covers CNAB2 with the influence-matrix solve");
+    if (I.scheme != PZ_CNAB2 || (I.flags & (PZF_DIRECT | PZF_INTEG | PZF_CHEM)))
+      return pz_fail(h, PZ_E_UNSUPPORTED,
+                     "pz_adjoint_forward: the adjoint covers the collocation CNAB2 step with the influence-matrix "
+                     "solve, without composition");
     if (adj_rloop_smem_bytes(I.P, I.rg) > PZ_SMEM_MAX)
       return pz_fail(h, PZ_E_UNSUPPORTED, "pz_adjoint_forward: n_phi_max too large for the adjoint transform kernel");
   }
@@ -810,7 +813,7 @@ extern "C" int pz_adjoint_forward(pz_handle* h, int objective, int n_steps, int 
   A->n_seg = (n_steps + A->K - 1) / A->K;
   A->n_snap = A->K + 1;
   A->n_ck = A->n_seg + 1;             // one per segment start, plus the final state
-  A->ck_planes = F_COUNT + 2 * (1 + 1 + 2);
+  A->ck_planes = F_XI + 2 * (1 + 1 + 2);
   std::vector<long long> ows(h->n_inst), oout(h->n_inst);
   long long tot = 0, tout = 0;
   const long long planes = AP_SNAP + 4LL * A->n_snap + (long long)A->n_ck * A->ck_planes;

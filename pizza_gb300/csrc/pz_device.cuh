@@ -226,21 +226,28 @@ __device__ double2* fft_run(double2* a, double2* b, const PzInst& I, const doubl
 // at (m, r)) and takes the outputs (dT/dt, dVsT, dpsi/dt, dVsOm at (m, r), and
 // the Courant steps of radius r).  The two real fields of each pair are packed
 // into one complex FFT (us + i up, om + i T on the way to the grid; the
-// products r us T + i up T and r us om + i up om on the way back).
-// G = min(gmax, N - r0) radii.  Shared memory: 4*G*P complex (two ping-pong
-// buffers of 2*G transforms) and 3*G + G*M doubles.
-template <class IO>
+// products r us T + i up T and r us om + i up om on the way back).  With
+// composition (PZF_CHEM) a third transform per radius carries xi to the grid
+// and r us xi + i up xi back (radial_loop.f90:297, :320-323, :356-374); IO
+// then supplies in(4, m, r) and takes outx(m, r, dxi/dt, r us xi).
+// G = min(gmax, N - r0) radii, nt = 2 (3 with composition) transforms per
+// radius.  Shared memory: 2*nt*G*P complex (two ping-pong buffers of nt*G
+// transforms) and 3*G + G*M doubles.  CHEM = false compiles the composition
+// out (a handle without composition launches that instantiation).
+template <bool CHEM, class IO>
 __device__ void rloop_group(const PzInst& I, const View& V, int r0, int gmax, IO& io, double2* sh, double* rsh) {
   const int N = I.N, M = I.M, P = I.P;
   const int G = min(gmax, N - r0);
+  const bool chem = CHEM && (I.flags & PZF_CHEM) != 0;
+  const int nt = chem ? 3 : 2;
   const double2* tw = reinterpret_cast<const double2*>(V.pool + I.o_tw);
-  double2* za = sh;                  // [g][2][P]
-  double2* zb = sh + 2 * G * P;
+  double2* za = sh;                  // [g][nt][P]
+  double2* zb = sh + nt * G * P;
   double* usom = rsh;                // [G]
   double* vr = rsh + G;              // [G]
   double* vh = rsh + 2 * G;          // [G]
   double* prod = rsh + 3 * G;        // [G][M] Reynolds-stress terms
-  for (int k = threadIdx.x; k < 2 * G * P; k += blockDim.x) za[k] = make_double2(0.0, 0.0);
+  for (int k = threadIdx.x; k < nt * G * P; k += blockDim.x) za[k] = make_double2(0.0, 0.0);
   for (int k = threadIdx.x; k < 3 * G; k += blockDim.x) rsh[k] = 0.0;
   __syncthreads();
   // spectra at the G radii; Reynolds stress of the m=0 equation
@@ -256,13 +263,20 @@ __device__ void rloop_group(const PzInst& I, const View& V, int r0, int gmax, IO
       us_om = 2.0 * (a.x * c.x + a.y * c.y);
     }
     prod[g * M + m] = us_om;
-    double2* z1 = za + (2 * g) * P;
-    double2* z2 = za + (2 * g + 1) * P;
+    double2* z1 = za + (nt * g) * P;
+    double2* z2 = z1 + P;
     z1[m] = make_double2(a.x - b.y, a.y + b.x);
     z2[m] = make_double2(c.x - e.y, c.y + e.x);
     if (m > 0) {
       z1[P - m] = make_double2(a.x + b.y, -a.y + b.x);
       z2[P - m] = make_double2(c.x + e.y, -c.y + e.x);
+    }
+    if (chem) {
+      double2 x = io.in(4, m, r);
+      if (m == 0) x.y = 0.0;
+      double2* z3 = z2 + P;
+      z3[m] = x;
+      if (m > 0) z3[P - m] = make_double2(x.x, -x.y);
     }
   }
   __syncthreads();
@@ -276,19 +290,23 @@ __device__ void rloop_group(const PzInst& I, const View& V, int r0, int gmax, IO
       if (lane == 0) usom[g] = acc;
     }
   }
-  double2* g1 = fft_run(za, zb, I, tw, 2 * G, true);
+  double2* g1 = fft_run(za, zb, I, tw, nt * G, true);
   double2* h = (g1 == za) ? zb : za;
   // Courant velocities and the nonlinear products on the grid
   for (int t = threadIdx.x; t < G * P; t += blockDim.x) {
     const int g = t / P, j = t - g * P;
     const double rr = V.rad(RV_R)[r0 + g];
-    const double2 z1 = g1[(2 * g) * P + j], z2 = g1[(2 * g + 1) * P + j];
+    const double2 z1 = g1[(nt * g) * P + j], z2 = g1[(nt * g + 1) * P + j];
     const double usg = z1.x, upg = z1.y, omg = z2.x, Tg = z2.y;
     // squares are >= 0: their bit patterns order like unsigned integers
     atomicMax(reinterpret_cast<unsigned long long*>(&vr[g]), (unsigned long long)__double_as_longlong(usg * usg));
     atomicMax(reinterpret_cast<unsigned long long*>(&vh[g]), (unsigned long long)__double_as_longlong(upg * upg));
-    h[(2 * g) * P + j] = make_double2(rr * usg * Tg, upg * Tg);
-    h[(2 * g + 1) * P + j] = make_double2(rr * usg * omg, upg * omg);
+    h[(nt * g) * P + j] = make_double2(rr * usg * Tg, upg * Tg);
+    h[(nt * g + 1) * P + j] = make_double2(rr * usg * omg, upg * omg);
+    if (chem) {
+      const double xg = g1[(nt * g + 2) * P + j].x;
+      h[(nt * g + 2) * P + j] = make_double2(rr * usg * xg, upg * xg);
+    }
   }
   __syncthreads();
   for (int g = threadIdx.x; g < G; g += blockDim.x) {
@@ -300,14 +318,14 @@ __device__ void rloop_group(const PzInst& I, const View& V, int r0, int gmax, IO
     if (vh2 != 0.0) dth = fmin(dth, sqrt(V.rad(RV_DELXH2)[r] / vh2));
     io.cfl(r, dtr, dth);
   }
-  double2* f = fft_run(h, g1, I, tw, 2 * G, false);
+  double2* f = fft_run(h, g1, I, tw, nt * G, false);
   for (int t = threadIdx.x; t < G * M; t += blockDim.x) {
     const int g = t / M, m = t - g * M, r = r0 + g;
     const double or1 = V.rad(RV_OR1)[r];
     const double tfac = (1.0 - I.tadvz) * V.rad(RV_BETA)[r] * or1;
     const int mc = (P - m) % P;
-    const double2* f1 = f + (2 * g) * P;
-    const double2* f2 = f + (2 * g + 1) * P;
+    const double2* f1 = f + (nt * g) * P;
+    const double2* f2 = f1 + P;
     // split the two real transforms packed in one complex FFT
     const double2 Z = f1[m], Zc = f1[mc], Y = f2[m], Yc = f2[mc];
     const double2 vsT = make_double2(0.5 * (Z.x + Zc.x) / (double)P, 0.5 * (Z.y - Zc.y) / (double)P);
@@ -317,6 +335,14 @@ __device__ void rloop_group(const PzInst& I, const View& V, int r0, int gmax, IO
     const double tm = or1 * (double)(m * I.minc);
     io.out(m, r, make_double2(tm * upT.y - tfac * vsT.x, -tm * upT.x - tfac * vsT.y), vsT,
            (m == 0) ? make_double2(-usom[g], 0.0) : make_double2(tm * upOm.y, -tm * upOm.x), vsOm);
+    if (chem) {
+      // dxi/dt = -(i m / r) FFT(up xi), no beta term (radial_loop.f90:372-374)
+      const double2* f3 = f2 + P;
+      const double2 X = f3[m], Xc = f3[mc];
+      const double2 vsX = make_double2(0.5 * (X.x + Xc.x) / (double)P, 0.5 * (X.y - Xc.y) / (double)P);
+      const double2 upX = make_double2(0.5 * (X.y + Xc.y) / (double)P, -0.5 * (X.x - Xc.x) / (double)P);
+      io.outx(m, r, make_double2(tm * upX.y, -tm * upX.x), vsX);
+    }
   }
 }
 

@@ -384,9 +384,11 @@ int validate(const pz_config& c, std::string* why) {
   if (c.l_rerror_fix && !(c.rerror_fac > 0.0)) return bad("rerror_fac must be > 0");
   if (c.l_rerror_fix && c.cheb_method != PZ_CHEB_INTEG)
     return uns("l_rerror_fix is implemented for cheb_method 'integ' (the collocation m = 0 recursions take no threshold)");
+  if (c.raxi != 0.0) {
+    if (!(c.sc > 0.0)) return bad("sc must be > 0 when raxi /= 0");
+    if (c.ktopxi != 1 || c.kbotxi != 1) return uns("only fixed-composition boundaries (ktopxi = kbotxi = 1)");
+  }
   if (c.cheb_method == PZ_CHEB_INTEG) {
-    if (c.matrix_solve == PZ_SOLVE_DIRECT && (c.l_non_rot || c.ek < 0.0))
-      return uns("cheb_method 'integ' with matrix_solve 'DIRECT' is implemented for rotating runs");
     if (pz_build_smem_bytes(c.n_r_max, true, true) > PZ_SMEM_MAX)
       return uns("cheb_method 'integ' needs n_r_max <= 118 (the operator build is staged in shared memory)");
     DirkTab t;
@@ -424,6 +426,7 @@ extern "C" void pz_config_default(pz_config* c) {
   c->dtMax = 1.0e-5; c->courfac = 1.0e3; c->alpha = 0.5; c->dt_fac = 2.0;
   c->cheb_method = PZ_CHEB_COLL; c->time_scale = PZ_TS_VISC;
   c->l_rerror_fix = 0; c->rerror_fac = 500.0;
+  c->raxi = 0.0; c->sc = 0.0; c->ktopxi = 1; c->kbotxi = 1; c->xicond_fac = 1.0;
 }
 
 extern "C" int pz_create(const pz_config* cfgs, int n, pz_handle** out) {
@@ -482,11 +485,18 @@ extern "C" int pz_create(const pz_config* cfgs, int n, pz_handle** out) {
     I.alpha = c.alpha;
     I.dtMax = c.dtMax; I.dtMin = c.dtMax / 1.0e6;   // pre_calculations.f90:33
     I.dt_fac = c.dt_fac;
+    const bool chem = c.raxi != 0.0;   // namelists.f90:323-327
     if (non_rot) { I.CorFac = 0.0; I.BuoFac = c.ra / c.pr; I.TdiffFac = 1.0 / c.pr; I.ViscFac = 1.0; }
     else if (c.time_scale == PZ_TS_ROT) {   // namelists.f90:491-500
       I.CorFac = 2.0; I.BuoFac = c.ra * ek * ek / c.pr; I.TdiffFac = ek / c.pr; I.ViscFac = ek;
     } else { I.CorFac = 2.0 / ek; I.BuoFac = c.ra / c.pr; I.TdiffFac = 1.0 / c.pr; I.ViscFac = 1.0; }
+    if (chem) {   // namelists.f90:482-522: raxi and sc in place of ra and pr
+      if (non_rot || c.time_scale != PZ_TS_ROT) { I.ChemFac = c.raxi / c.sc; I.XidiffFac = 1.0 / c.sc; }
+      else { I.ChemFac = c.raxi * ek * ek / c.sc; I.XidiffFac = ek / c.sc; }
+    }
+    I.nhf = chem ? 3 : 2;
     I.flags = 0;
+    if (chem) I.flags |= PZF_CHEM;
     if (c.buo_imp) I.flags |= PZF_BUO_IMP;
     if (c.l_ek_pump) I.flags |= PZF_EK_PUMP;
     if (non_rot) I.flags |= PZF_NON_ROT;
@@ -545,6 +555,10 @@ extern "C" int pz_create(const pz_config* cfgs, int n, pz_handle** out) {
       rv(RV_RGRAV, k) = c.g0 + c.g1 * r[k] / rc + c.g2 * rc * rc * rv(RV_OR2, k);
       rv(RV_TCOND, k) = std::log(r[k] / rc) / std::log(c.radratio);
       rv(RV_DTCOND, k) = rv(RV_OR1, k) / std::log(c.radratio);
+      if (chem) {   // the same 2D profile with xicond_fac (radial.f90:377-379)
+        rv(RV_XICOND, k) = c.xicond_fac * (std::log(r[k] / rc) / std::log(c.radratio));
+        rv(RV_DXICOND, k) = c.xicond_fac * (rv(RV_OR1, k) / std::log(c.radratio));
+      }
       if (non_rot) {
         rv(RV_HEIGHT, k) = 1.0;
       } else if (k > 0) {
@@ -607,6 +621,9 @@ extern "C" int pz_create(const pz_config* cfgs, int n, pz_handle** out) {
     }
     sfs = simps(tmp, th);
     I.nu_vol_den = sv;
+    double sx = 0.0;
+    for (int k = 0; k < N; ++k) sx += rv(RV_WINT, k) * rv(RV_DXICOND, k) * rv(RV_DXICOND, k) * rv(RV_HEIGHT, k) * r[k];
+    I.sh_vol_den = sx;
     I.nu_int_fac = non_rot ? sf : sfs;
     I.o_rad = take((long long)RV_COUNT * N);
     h->hin[i].c = c;
@@ -620,6 +637,7 @@ extern "C" int pz_create(const pz_config* cfgs, int n, pz_handle** out) {
     PzInst& I = h->inst[i];
     const long long N = I.N, M = I.M;
     I.o_gt = take(M * N * N);
+    I.o_gx = (I.flags & PZF_CHEM) ? take(M * N * N) : 0;
     I.o_guphi = take(N * N);
     if ((I.flags & PZF_INTEG) && (I.flags & PZF_DIRECT)) {
       I.o_gsm = take(2 * M * N * N);      // complex N x N streamfunction inverse per m
@@ -636,7 +654,7 @@ extern "C" int pz_create(const pz_config* cfgs, int n, pz_handle** out) {
     I.o_bt = I.dirk ? take(PZ_BT_SIZE) : 0;
     I.o_gass = (I.dirk && I.assembly) ? take(M * N * N) : 0;
     I.o_fld = take(2LL * F_COUNT * M * N);
-    I.o_hist = take(2LL * 2 * (I.nold + I.nimp + I.nexp) * M * N);
+    I.o_hist = take(2LL * I.nhf * (I.nold + I.nimp + I.nexp) * M * N);
     I.o_cfl = take(2 * N);
     I.o_series = take((long long)PZ_SERIES_CAP * PZ_SERIES_COLS);
   }
@@ -724,7 +742,7 @@ extern "C" int pz_create(const pz_config* cfgs, int n, pz_handle** out) {
       (e = cudaMalloc(&h->d_order, mitems.size() * sizeof(PzItem))) ||
       (e = cudaMalloc(&h->d_iorder, n * sizeof(int))) ||
       (e = cudaMalloc(&h->d_rows, (size_t)n * PZ_SERIES_COLS * sizeof(double))) ||
-      (e = cudaMalloc(&h->d_spec, (size_t)4 * maxM * sizeof(double)))) {
+      (e = cudaMalloc(&h->d_spec, (size_t)5 * maxM * sizeof(double)))) {
     g_create_error = std::string("device allocation: ") + cudaGetErrorString(e);
     pz_destroy(h);
     return PZ_E_NOMEM;
@@ -742,6 +760,8 @@ extern "C" int pz_create(const pz_config* cfgs, int n, pz_handle** out) {
   h->dev.order = h->d_order;
   h->dev.iorder = h->d_iorder;
   h->dev.n_inst = n;
+  h->dev.any_chem = 0;
+  for (int i = 0; i < n; ++i) h->dev.any_chem |= (h->inst[i].flags & PZF_CHEM) ? 1 : 0;
   h->dev.maxN = maxN; h->dev.maxP = maxP; h->dev.maxM = maxM;
   size_t sb = 0;
   for (int i = 0; i < n; ++i)
@@ -750,7 +770,8 @@ extern "C" int pz_create(const pz_config* cfgs, int n, pz_handle** out) {
   h->dev.smem_build = (int)sb;
   size_t srl = 0;
   for (int i = 0; i < n; ++i)
-    srl = std::max(srl, pz_rloop_smem_bytes(h->inst[i].P, h->inst[i].M, h->inst[i].rg));
+    srl = std::max(srl, pz_rloop_smem_bytes(h->inst[i].P, h->inst[i].M, h->inst[i].rg,
+                                            (h->inst[i].flags & PZF_CHEM) ? 3 : 2));
   h->dev.smem_rloop = (int)srl;
   // launch plan of one step: per stage k_rloop [k_cfl, k_build] k_mloop, then
   // the assembly stage and the time series (step_time.f90:139-406)
@@ -841,19 +862,26 @@ int check_status(pz_handle* h) {
 
 int pz_check_status(pz_handle* h) { return check_status(h); }
 
-extern "C" int pz_set_state(pz_handle* h, int inst, const double* us, const double* up, const double* temp) {
+extern "C" int pz_set_state_xi(pz_handle* h, int inst, const double* us, const double* up, const double* temp,
+                               const double* xi) {
   if (!h) return fail(nullptr, PZ_E_ARG, "pz_set_state: null handle");
   pz_adjoint_invalidate(h);
   if (inst < 0 || inst >= h->n_inst) return fail(h, PZ_E_ARG, "pz_set_state: instance out of range");
+  const bool chem = (h->inst[inst].flags & PZF_CHEM) != 0;
+  if (xi && !chem) return fail(h, PZ_E_ARG, "pz_set_state_xi: the instance has no composition (raxi = 0)");
   int rc;
   if ((rc = upload_field(h, inst, F_US, us)) || (rc = upload_field(h, inst, F_UP, up)) ||
-      (rc = upload_field(h, inst, F_TEMP, temp)))
+      (rc = upload_field(h, inst, F_TEMP, temp)) || (chem && (rc = upload_field(h, inst, F_XI, xi))))
     return rc;
   cudaError_t e;
   if ((e = pz_launch_init_state(h->dev, inst, h->stream)) || (e = pz_launch_start(h->dev, inst, h->stream)) ||
       (e = pz_launch_obs(h->dev, inst, h->stream)))
     return cuda_fail(h, e, "pz_set_state");
   return check_status(h);
+}
+
+extern "C" int pz_set_state(pz_handle* h, int inst, const double* us, const double* up, const double* temp) {
+  return pz_set_state_xi(h, inst, us, up, temp, nullptr);
 }
 
 extern "C" int pz_set_state_all(pz_handle* h, const double* us, const double* up, const double* temp) {
@@ -864,7 +892,8 @@ extern "C" int pz_set_state_all(pz_handle* h, const double* us, const double* up
     const PzInst& I = h->inst[i];
     int rc;
     if ((rc = upload_field(h, i, F_US, us ? us + o : nullptr)) || (rc = upload_field(h, i, F_UP, up ? up + o : nullptr)) ||
-        (rc = upload_field(h, i, F_TEMP, temp ? temp + o : nullptr)))
+        (rc = upload_field(h, i, F_TEMP, temp ? temp + o : nullptr)) ||
+        ((I.flags & PZF_CHEM) && (rc = upload_field(h, i, F_XI, nullptr))))
       return rc;
     o += 2LL * I.M * I.N;
   }
@@ -932,6 +961,29 @@ extern "C" int pz_get_state(pz_handle* h, int inst, double* us, double* up, doub
   return st.status ? check_status(h) : PZ_OK;
 }
 
+extern "C" int pz_get_state_xi(pz_handle* h, int inst, double* xi, double* dxi) {
+  if (!h) return fail(nullptr, PZ_E_ARG, "pz_get_state_xi: null handle");
+  if (inst < 0 || inst >= h->n_inst) return fail(h, PZ_E_ARG, "pz_get_state_xi: instance out of range");
+  const PzInst& I = h->inst[inst];
+  const long long MN = (long long)I.M * I.N;
+  std::vector<double> buf(2 * MN * 2);
+  cudaError_t e = cudaMemcpyAsync(buf.data(), h->pool + I.o_fld + 2LL * F_XI * MN, buf.size() * sizeof(double),
+                                  cudaMemcpyDeviceToHost, h->stream);
+  if (!e) e = cudaStreamSynchronize(h->stream);
+  if (e) return cuda_fail(h, e, "pz_get_state_xi");
+  double* outs[2] = {xi, dxi};
+  for (int k = 0; k < 2; ++k) {
+    if (!outs[k]) continue;
+    const double* src = buf.data() + 2 * MN * k;
+    for (int r = 0; r < I.N; ++r)
+      for (int m = 0; m < I.M; ++m) {
+        outs[k][2 * (m + (long long)r * I.M)] = src[2 * ((long long)m * I.N + r)];
+        outs[k][2 * (m + (long long)r * I.M) + 1] = src[2 * ((long long)m * I.N + r) + 1];
+      }
+  }
+  return PZ_OK;
+}
+
 namespace {
 // physical ring slot of logical history slot `slot` (1-based) at a step boundary
 int hist_phys(const PzInst& I, const PzState& st, int kind, int slot) {
@@ -945,7 +997,7 @@ int hist_args(pz_handle* h, int inst, int field, int kind, int slot, const char*
   if (inst < 0 || inst >= h->n_inst) return fail(h, PZ_E_ARG, std::string(who) + ": instance out of range");
   const PzInst& I = h->inst[inst];
   const int n = kind == 0 ? I.nold : (kind == 1 ? I.nimp : (kind == 2 ? I.nexp : 0));
-  if (field < 0 || field > 1 || kind < 0 || kind > 2 || slot < 1 || slot > n)
+  if (field < 0 || field >= I.nhf || kind < 0 || kind > 2 || slot < 1 || slot > n)
     return fail(h, PZ_E_ARG, std::string(who) + ": field, kind or slot out of range");
   return PZ_OK;
 }
@@ -1044,7 +1096,7 @@ extern "C" int pz_get_spectra(pz_handle* h, int inst, double* out) {
   if (inst < 0 || inst >= h->n_inst || !out) return fail(h, PZ_E_ARG, "pz_get_spectra: bad arguments");
   const int M = h->inst[inst].M;
   cudaError_t e = pz_launch_spectra(h->dev, inst, M, h->d_spec, h->stream);
-  if (!e) e = cudaMemcpyAsync(out, h->d_spec, (size_t)4 * M * sizeof(double), cudaMemcpyDeviceToHost, h->stream);
+  if (!e) e = cudaMemcpyAsync(out, h->d_spec, (size_t)5 * M * sizeof(double), cudaMemcpyDeviceToHost, h->stream);
   if (!e) e = cudaStreamSynchronize(h->stream);
   if (e) return cuda_fail(h, e, "pz_get_spectra");
   return PZ_OK;
@@ -1200,6 +1252,8 @@ int pz_expl_args(pz_handle* h, int inst, const double* us, const double* up, con
   const PzInst& I = h->inst[inst];
   if (I.flags & PZF_INTEG)
     return fail(h, PZ_E_UNSUPPORTED, "explicit terms entry point: collocation instances only (cheb_method 'integ')");
+  if (I.flags & PZF_CHEM)
+    return fail(h, PZ_E_UNSUPPORTED, "explicit terms entry point: instances without composition only");
   a->inst = h->d_inst + inst;
   a->pool = h->pool;
   a->us = reinterpret_cast<const double2*>(us);

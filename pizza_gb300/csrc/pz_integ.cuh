@@ -1,6 +1,7 @@
 // Chebyshev integration method ("integ", tau boundary rows, direct solve):
-// the per-m device code of update_temp_int (src/update_temp_integ.f90) and
-// update_psi_int_smat (src/update_psi_integ_smat.f90).  Included by
+// the per-m device code of update_temp_int (src/update_temp_integ.f90),
+// update_xi_int (src/update_xi_integ.f90, the same operators with XidiffFac)
+// and update_psi_int_smat (src/update_psi_integ_smat.f90).  Included by
 // pz_kernels.cu after the collocation helpers it reuses (View, MS, op_*,
 // mv_lanes, imex_rhs, dirk_rhs, gj_invert, gj_invert_c, store_op).
 //
@@ -54,22 +55,31 @@ __device__ __forceinline__ Band3 band_tlap(const View& V, double dm2, double f) 
   b.na = 2; b.bw = max(V.I->im_band[IM_LT0], V.I->im_band[IM_I2]);
   return b;
 }
-// intcheb4rmult4laplrot(m) = Q0 + m^2 Q1
+// d/dt operator of the direct streamfunction solve, m /= 0: rotating
+// intcheb4rmult4laplrot(m) = Q0 + m^2 Q1, non-rotating -intcheb4rmult4lapl(m)
+// = -(N0 + m^2 N1) (update_psi_integ_smat.f90:1631-1764)
 __device__ __forceinline__ Band3 band_rot(const View& V, double dm2) {
+  const bool rot = !(V.I->flags & PZF_NON_ROT);
+  const int a0 = rot ? IM_Q0 : IM_N0, a1 = rot ? IM_Q1 : IM_N1;
+  const double sg = rot ? 1.0 : -1.0;
   Band3 b;
-  b.A[0] = im_op(V, IM_Q0); b.c[0] = 1.0;
-  b.A[1] = im_op(V, IM_Q1); b.c[1] = dm2;
+  b.A[0] = im_op(V, a0); b.c[0] = sg;
+  b.A[1] = im_op(V, a1); b.c[1] = sg * dm2;
   b.A[2] = nullptr; b.c[2] = 0.0;
-  b.na = 2; b.bw = max(V.I->im_band[IM_Q0], V.I->im_band[IM_Q1]);
+  b.na = 2; b.bw = max(V.I->im_band[a0], V.I->im_band[a1]);
   return b;
 }
-// f * intcheb4rmult4laplrot2(m) = f (S0 + m^2 S1 + m^4 S2)
+// f times the viscous operator: rotating intcheb4rmult4laplrot2(m) = S0 +
+// m^2 S1 + m^4 S2, non-rotating -intcheb4rmult4lapl2(m) = -(L0 + m^2 L1 + m^4 L2)
 __device__ __forceinline__ Band3 band_rot2(const View& V, double dm2, double f) {
+  const bool rot = !(V.I->flags & PZF_NON_ROT);
+  const int a0 = rot ? IM_S0 : IM_L0, a1 = rot ? IM_S1 : IM_L1, a2 = rot ? IM_S2 : IM_L2;
+  if (!rot) f = -f;
   Band3 b;
-  b.A[0] = im_op(V, IM_S0); b.c[0] = f;
-  b.A[1] = im_op(V, IM_S1); b.c[1] = f * dm2;
-  b.A[2] = im_op(V, IM_S2); b.c[2] = f * dm2 * dm2;
-  b.na = 3; b.bw = max(V.I->im_band[IM_S0], max(V.I->im_band[IM_S1], V.I->im_band[IM_S2]));
+  b.A[0] = im_op(V, a0); b.c[0] = f;
+  b.A[1] = im_op(V, a1); b.c[1] = f * dm2;
+  b.A[2] = im_op(V, a2); b.c[2] = f * dm2 * dm2;
+  b.na = 3; b.bw = max(V.I->im_band[a0], max(V.I->im_band[a1], V.I->im_band[a2]));
   return b;
 }
 
@@ -209,15 +219,19 @@ __device__ int integ_build(const PzDev& d, const PzInst& I, const View& V, int m
   int* piv = redi + 32;
   const double* I2R2 = im_op(V, IM_I2R2);
   const bool dmat = !(I.flags & PZF_DIRECT);
-  for (int pass = 0; pass < 2; ++pass) {
-    // pass 0: temperature; pass 1: u_phi (m = 0) or, with the influence
-    // matrix, the vorticity operator (m /= 0, tau rows omega(r_o), omega(r_i));
-    // the direct solve's m /= 0 streamfunction operator is complex and built below
-    if (pass == 1 && m != 0 && !dmat) break;
-    const double* L0 = im_op(V, (pass == 0 || m != 0) ? IM_LT0 : IM_ULAP);
+  for (int pass = 0; pass < 3; ++pass) {
+    // pass 0: temperature; pass 1: composition (update_xi_integ.f90, the
+    // temperature's operator with XidiffFac); pass 2: u_phi (m = 0) or, with
+    // the influence matrix, the vorticity operator (m /= 0, tau rows
+    // omega(r_o), omega(r_i)); the direct solve's m /= 0 streamfunction
+    // operator is complex and built below
+    if (pass == 1 && !(I.flags & PZF_CHEM)) continue;
+    if (pass == 2 && m != 0 && !dmat) break;
+    const bool scal = pass < 2;
+    const double* L0 = im_op(V, (scal || m != 0) ? IM_LT0 : IM_ULAP);
     const double* L1 = im_op(V, IM_I2);
-    const double c0 = wlin * (pass == 0 ? I.TdiffFac : I.ViscFac);
-    const double c1 = (pass == 0 || m != 0) ? -dm2 * c0 : 0.0;
+    const double c0 = wlin * (pass == 0 ? I.TdiffFac : pass == 1 ? I.XidiffFac : I.ViscFac);
+    const double c1 = (scal || m != 0) ? -dm2 * c0 : 0.0;
     for (int idx = threadIdx.x; idx < n * n; idx += blockDim.x) {
       const int i = idx / n, j = idx - i * n;
       double v;
@@ -241,8 +255,9 @@ __device__ int integ_build(const PzDev& d, const PzInst& I, const View& V, int m
     for (int idx = threadIdx.x; idx < n * n; idx += blockDim.x) A[idx] *= f1[idx / n];
     __syncthreads();
     if (gj_invert(A, n, piv, colk, red, redi) != 0) return -1;
-    double* G = d.pool + (pass == 0 ? I.o_gt + (long long)mi * n * n
-                                    : (m == 0 ? I.o_guphi : I.o_gom + (long long)mi * n * n));
+    double* G = d.pool + (pass == 0   ? I.o_gt + (long long)mi * n * n
+                          : pass == 1 ? I.o_gx + (long long)mi * n * n
+                                      : (m == 0 ? I.o_guphi : I.o_gom + (long long)mi * n * n));
     store_op(G, A, n, n, nullptr, f1);
     __syncthreads();
   }
@@ -285,12 +300,16 @@ __device__ int integ_build(const PzDev& d, const PzInst& I, const View& V, int m
   }
   // streamfunction, m /= 0: Q0 + m^2 Q1 - wlin ViscFac (S0 + m^2 S1 + m^4 S2)
   // + i wlin CorFac m I4R4 (implicit Coriolis), tau rows psi(r_o) = psi(r_i) = 0,
-  // d3psi/dx3(r_o) = 0 (rigid, rotating) and dpsi/dr(r_i) = 0
-  const double* Q0 = im_op(V, IM_Q0);
-  const double* Q1 = im_op(V, IM_Q1);
-  const double* S0 = im_op(V, IM_S0);
-  const double* S1 = im_op(V, IM_S1);
-  const double* S2 = im_op(V, IM_S2);
+  // d3psi/dx3(r_o) = 0 (rigid, rotating) and dpsi/dr(r_i) = 0; non-rotating
+  // -(N0 + m^2 N1) + wlin (L0 + m^2 L1 + m^4 L2) with dpsi/dr(r_o) = 0 in
+  // the third tau row (update_psi_integ_smat.f90:1286-1581)
+  const bool rot = !(I.flags & PZF_NON_ROT);
+  const double sg0 = rot ? 1.0 : -1.0;
+  const double* Q0 = im_op(V, rot ? IM_Q0 : IM_N0);
+  const double* Q1 = im_op(V, rot ? IM_Q1 : IM_N1);
+  const double* S0 = im_op(V, rot ? IM_S0 : IM_L0);
+  const double* S1 = im_op(V, rot ? IM_S1 : IM_L1);
+  const double* S2 = im_op(V, rot ? IM_S2 : IM_L2);
   const double* R4 = im_op(V, IM_I4R4);
   const double cv = wlin * I.ViscFac;
   const double cc = (I.flags & PZF_COR_IMP) ? wlin * I.CorFac * dm : 0.0;
@@ -301,13 +320,14 @@ __device__ int integ_build(const PzDev& d, const PzInst& I, const View& V, int m
       const double dj = (double)j, dn2 = dj * dj, sg = (j & 1) ? -1.0 : 1.0;
       if (i == 0) re = 1.0;
       else if (i == 1) re = sg;
-      else if (i == 2) re = 8.0 / 15.0 * dn2 * (dn2 - 1.0) * (dn2 - 4.0);   // update_psi_integ_smat.f90:1303-1306
+      else if (i == 2) re = rot ? 8.0 / 15.0 * dn2 * (dn2 - 1.0) * (dn2 - 4.0)   // update_psi_integ_smat.f90:1303-1306
+                                : 2.0 * dn2;                                  // drMat(1,:)
       else re = -2.0 * dn2 * sg;                                           // drMat(2,:), chebyshev.f90:363-379
       re *= rn;
       if (j == 0) re *= 0.5;                                               // boundary_fac
     } else {
       const long long c = i + (long long)j * n;
-      re = Q0[c] + dm2 * Q1[c] - cv * (S0[c] + dm2 * (S1[c] + dm2 * S2[c]));
+      re = sg0 * (Q0[c] + dm2 * Q1[c] - cv * (S0[c] + dm2 * (S1[c] + dm2 * S2[c])));
       im = cc * R4[c];
     }
     Ac[idx] = make_double2(re, im);
@@ -337,8 +357,12 @@ __device__ int integ_build(const PzDev& d, const PzInst& I, const View& V, int m
 // and start_from_another_scheme (step_time.f90:488-500).  With from_us the
 // streamfunction is first rebuilt from u_s, psi = -i r u_s / (m h^2)
 // (init_fields.f90:73-91).  Writes old/impl logical slot 1 at ring bases bo/bi
-// and dT/dr.
-__device__ void integ_imp(const View& V, const PzInst& I, int mi, int bo, int bi, bool calc, bool from_us, MS& s) {
+// and dT/dr (d xi/dr).  With psi_as_xi the buoyancy takes psi in the place of
+// the composition, as start_from_another_scheme does for the direct solve
+// (step_time.f90:497-498 passes psi_Mloc for xi_Mloc).
+template <bool CHEM>
+__device__ void integ_imp(const View& V, const PzInst& I, int mi, int bo, int bi, bool calc, bool from_us, MS& s,
+                          bool psi_as_xi) {
   const int n = I.N, m = mi * I.minc;
   const double dm = (double)m, dm2 = dm * dm;
   const double* r = V.rad(RV_R);
@@ -359,6 +383,22 @@ __device__ void integ_imp(const View& V, const PzInst& I, int mi, int bo, int bi
   band_mv(band1(V, IM_I2R2), n, s.b, V.hist(0, 0, bo, mi));
   if (calc) band_mv(band_tlap(V, dm2, I.TdiffFac), n, s.b, V.hist(0, 1, bi, mi));
   __syncthreads();
+  const bool chem = CHEM && (I.flags & PZF_CHEM) != 0;
+  const double2* X = V.fld(F_XI, mi);
+  if (chem) {
+    // get_xi_rhs_imp_int (update_xi_integ.f90:449-510)
+    for (int i = threadIdx.x; i < n; i += blockDim.x) s.a[i] = X[i];
+    __syncthreads();
+    op_C(V, n, s.a, s.b, s.w);                                   // xi_hat
+    __syncthreads();
+    op_D1c(V, n, s.b, s.c, s.w);
+    __syncthreads();
+    double2* dX = V.fld(F_DXI, mi);
+    for (int i = threadIdx.x; i < n; i += blockDim.x) dX[i] = s.c[i];
+    band_mv(band1(V, IM_I2R2), n, s.b, V.hist(2, 0, bo, mi));
+    if (calc) band_mv(band_tlap(V, dm2, I.XidiffFac), n, s.b, V.hist(2, 1, bi, mi));
+    __syncthreads();
+  }
   double2* oP = V.hist(1, 0, bo, mi);
   double2* iP = V.hist(1, 1, bi, mi);
   if (m == 0) {
@@ -380,11 +420,14 @@ __device__ void integ_imp(const View& V, const PzInst& I, int mi, int bo, int bi
   }
   const bool dmat = !(I.flags & PZF_DIRECT);
   const double2* om = V.fld(F_OM, mi);
+  const double2* xs = psi_as_xi ? psi : X;
   for (int i = threadIdx.x; i < n; i += blockDim.x) {
     // the influence-matrix variant works on omega (get_psi_rhs_imp_int_dmat,
     // update_psi_integ_dmat.f90:625-781), the direct solve on psi
     s.a[i] = dmat ? om[i] : psi[i];
-    s.e[i] = cscale(-I.BuoFac * rgrav[i] * or1[i], cim(dm, T[i]));
+    double2 b = cscale(-I.BuoFac * rgrav[i] * or1[i], cim(dm, T[i]));
+    if (chem) b = csub(b, cscale(I.ChemFac * rgrav[i] * or1[i], cim(dm, xs[i])));
+    s.e[i] = b;
   }
   __syncthreads();
   op_C(V, n, s.a, s.b, s.w);                                     // omega_hat or psi_hat
@@ -523,6 +566,7 @@ __device__ bool integ_dmat_psi(const PzDev& d, const View& V, const PzInst& I, c
   return bad;
 }
 
+template <bool CHEM>
 __device__ bool integ_stage(const PzDev& d, const View& V, const PzInst& I, const PzState& S, int mi,
                             const IntegStage& c, MS& s) {
   const int n = I.N, m = mi * I.minc, n_max = I.n_max;
@@ -545,9 +589,11 @@ __device__ bool integ_stage(const PzDev& d, const View& V, const PzInst& I, cons
   double2* psi = V.fld(F_PSI, mi);
   double2* T = V.fld(F_TEMP, mi);
   double2* dT = V.fld(F_DTEMP, mi);
+  double2* X = V.fld(F_XI, mi);
   const bool buo_imp = (I.flags & PZF_BUO_IMP) != 0;
   const bool cor_imp = (I.flags & PZF_COR_IMP) != 0;
   const bool dmat = !(I.flags & PZF_DIRECT);
+  const bool chem = CHEM && (I.flags & PZF_CHEM) != 0;
   bool bad = false;
 
   if (c.do_finish) {
@@ -579,7 +625,10 @@ __device__ bool integ_stage(const PzDev& d, const View& V, const PzInst& I, cons
         // vorticity equation without the r weight, Coriolis always explicit
         p = csub(p, cscale(or1[i], s.g[i]));
         if (rot) p = csub(p, cim(I.CorFac * dm, psi[i]));
-        if (!buo_imp) p = csub(p, cim(I.BuoFac * rgrav[i] * or1[i] * dm, T[i]));
+        if (!buo_imp) {
+          p = csub(p, cim(I.BuoFac * rgrav[i] * or1[i] * dm, T[i]));
+          if (chem) p = csub(p, cim(I.ChemFac * rgrav[i] * or1[i] * dm, X[i]));
+        }
         if (I.flags & PZF_EK_PUMP) {
           const double2 u = us[i];
           const double2 q = make_double2(ekp_us[i] * u.x - ekp_dusdp[i] * dm * u.y,
@@ -592,7 +641,10 @@ __device__ bool integ_stage(const PzDev& d, const View& V, const PzInst& I, cons
       } else if (m != 0) {
         p = cscale(r[i], p);
         if (!cor_imp) p = csub(p, cim(I.CorFac * dm * r[i], psi[i]));
-        if (!buo_imp) p = csub(p, cim(I.BuoFac * rgrav[i] * dm, T[i]));
+        if (!buo_imp) {
+          p = csub(p, cim(I.BuoFac * rgrav[i] * dm, T[i]));
+          if (chem) p = csub(p, cim(I.ChemFac * rgrav[i] * dm, X[i]));
+        }
         if (I.flags & PZF_EK_PUMP) {
           const double2 u = us[i];
           const double2 q = make_double2(ekp_us[i] * u.x - ekp_dusdp[i] * dm * u.y,
@@ -619,9 +671,34 @@ __device__ bool integ_stage(const PzDev& d, const View& V, const PzInst& I, cons
     band_mv(band1(V, IM_I2R1), n, s.b, eT);
     band_mv(band1(V, (m == 0 || dmat) ? IM_I2R2 : IM_I4R3), n, s.f, eP);
     __syncthreads();
+    if (chem) {
+      // finish_exp_xi_int (update_xi_integ.f90:280-357): the temperature's
+      // finish with dxicond and no tadvz term
+      for (int i = threadIdx.x; i < n; i += blockDim.x) s.a[i] = V.fld(F_DVSXI, mi)[i];
+      __syncthreads();
+      op_C(V, n, s.a, s.b, s.w);
+      __syncthreads();
+      trunc_cheb(s.b, n, n_max);
+      __syncthreads();
+      op_D1c(V, n, s.b, s.c, s.w);                               // d(u_s r xi)/dr (dealiased)
+      __syncthreads();
+      const double* dxicond = V.rad(RV_DXICOND);
+      double2* eX = V.hist(2, 2, c.eslot, mi);
+      for (int i = threadIdx.x; i < n; i += blockDim.x) {
+        const double g = rot ? (rc2 - r[i] * r[i]) * dxicond[i] : dxicond[i];
+        s.a[i] = csub(csub(cscale(r[i], eX[i]), cim(dm * g, psi[i])), s.c[i]);
+      }
+      __syncthreads();
+      op_C(V, n, s.a, s.b, s.w);
+      __syncthreads();
+      trunc_cheb(s.b, n, n_max);
+      __syncthreads();
+      band_mv(band1(V, IM_I2R1), n, s.b, eX);
+      __syncthreads();
+    }
   }
   if (!c.do_solve) return false;
-  if (S.bridge) integ_imp(V, I, mi, S.r_old, S.r_impl, true, false, s);
+  if (S.bridge) integ_imp<CHEM>(V, I, mi, S.r_old, S.r_impl, true, false, s, !dmat);
 
   // -- temperature: T_hat = G_T rhs, rhs(1:2) = topt, bott = 0
   for (int i = threadIdx.x; i < n; i += blockDim.x) {
@@ -644,6 +721,30 @@ __device__ bool integ_stage(const PzDev& d, const View& V, const PzInst& I, cons
   if (c.wold) band_mv(band1(V, IM_I2R2), n, s.b, V.hist(0, 0, c.oslot, mi));
   if (c.calc) band_mv(band_tlap(V, dm2, I.TdiffFac), n, s.b, V.hist(0, 1, c.islot, mi));
   __syncthreads();
+  if (chem) {
+    // -- composition (update_xi_int, update_xi_integ.f90:167-278): xi_hat = G_xi rhs
+    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+      const double2 v = c.dirk ? dirk_rhs(V, I, S, 2, mi, i, c.stage) : imex_rhs(V, I, S, 2, mi, i);
+      s.a[i] = i < 2 ? make_double2(0.0, 0.0) : v;               // topxi, botxi = 0
+    }
+    __syncthreads();
+    mv_lanes(d.pool + I.o_gx + (long long)mi * n * n, n, s.a, s.b);
+    __syncthreads();
+    op_C(V, n, s.b, s.g, s.w);                                   // xi (physical)
+    __syncthreads();
+    op_D1c(V, n, s.b, s.c, s.w);                                 // dxi/dr
+    __syncthreads();
+    double2* dX = V.fld(F_DXI, mi);
+    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+      const double2 t = s.g[i];
+      X[i] = t;
+      dX[i] = s.c[i];
+      bad |= !isfinite(t.x) || !isfinite(t.y);
+    }
+    if (c.wold) band_mv(band1(V, IM_I2R2), n, s.b, V.hist(2, 0, c.oslot, mi));
+    if (c.calc) band_mv(band_tlap(V, dm2, I.XidiffFac), n, s.b, V.hist(2, 1, c.islot, mi));
+    __syncthreads();
+  }
 
   double2* oP = V.hist(1, 0, c.oslot, mi);
   double2* iP = V.hist(1, 1, c.islot, mi);
@@ -686,7 +787,11 @@ __device__ bool integ_stage(const PzDev& d, const View& V, const PzInst& I, cons
   // -- streamfunction, m /= 0: buoyancy I4R4 C(-BuoFac rgrav/r i m T) (I2R2 with
   // the influence matrix) with the new T
   if (buo_imp) {
-    for (int i = threadIdx.x; i < n; i += blockDim.x) s.a[i] = cscale(-I.BuoFac * rgrav[i] * or1[i], cim(dm, s.f[i]));
+    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+      double2 b = cscale(-I.BuoFac * rgrav[i] * or1[i], cim(dm, s.f[i]));
+      if (chem) b = csub(b, cscale(I.ChemFac * rgrav[i] * or1[i], cim(dm, X[i])));
+      s.a[i] = b;
+    }
     __syncthreads();
     op_C(V, n, s.a, s.c, s.w);
     __syncthreads();
@@ -708,12 +813,22 @@ __device__ bool integ_stage(const PzDev& d, const View& V, const PzInst& I, cons
   __syncthreads();
   for (int i = threadIdx.x; i < n; i += blockDim.x) {
     const double2 p = s.h[i], dp = s.c[i], d2p = s.g[i];
-    const double h2 = rc2 - r[i] * r[i];
     psi[i] = p;
-    us[i] = cscale(or1[i] * h2, cim(dm, p));
-    up[i] = make_double2(-h2 * dp.x + 3.0 * r[i] * p.x, -h2 * dp.y + 3.0 * r[i] * p.y);
-    const double a1 = rc2 * or1[i] - 6.0 * r[i], a0 = 6.0 + dm2 * or2[i] * h2;
-    const double2 o = make_double2(-h2 * d2p.x - a1 * dp.x + a0 * p.x, -h2 * d2p.y - a1 * dp.y + a0 * p.y);
+    double2 o;
+    if (rot) {
+      const double h2 = rc2 - r[i] * r[i];
+      us[i] = cscale(or1[i] * h2, cim(dm, p));
+      up[i] = make_double2(-h2 * dp.x + 3.0 * r[i] * p.x, -h2 * dp.y + 3.0 * r[i] * p.y);
+      const double a1 = rc2 * or1[i] - 6.0 * r[i], a0 = 6.0 + dm2 * or2[i] * h2;
+      o = make_double2(-h2 * d2p.x - a1 * dp.x + a0 * p.x, -h2 * d2p.y - a1 * dp.y + a0 * p.y);
+    } else {
+      // update_psi_integ_smat.f90:474-499: us = i m psi / r, up = -dpsi/dr,
+      // om = -Lap_m psi
+      us[i] = cscale(or1[i], cim(dm, p));
+      up[i] = make_double2(-dp.x, -dp.y);
+      const double a0 = dm2 * or2[i];
+      o = make_double2(-d2p.x - or1[i] * dp.x + a0 * p.x, -d2p.y - or1[i] * dp.y + a0 * p.y);
+    }
     om[i] = o;
     bad |= !isfinite(o.x) || !isfinite(o.y);
   }

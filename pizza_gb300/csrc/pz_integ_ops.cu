@@ -1,6 +1,6 @@
 // Host-side derivation of the banded operators of pizza's Chebyshev
-// integration method (src/chebsparselib.f90, used by update_temp_integ.f90
-// and update_psi_integ_smat.f90).
+// integration method (src/chebsparselib.f90, used by update_temp_integ.f90,
+// update_xi_integ.f90 and update_psi_integ_smat.f90).
 //
 // Coefficients follow pizza's DCT-I convention f = c_0/2 + sum_{n>=1} c_n T_n
 // with x = (r - b)/a.  Every operator is I_k [sum_d P_d(r) f^(d)] -- an
@@ -190,6 +190,14 @@ void pz_integ_operators(int N, double r_icb, double r_cmb, double rnorm, std::ve
   Terms s1 = lapl4(Tb);
   for (const Term& x : Ta) add_term(s1, x.d, pscale(x.P, -1.0));
   Terms s2 = {{0, pscale(h2, -1.0)}};
+  // non-rotating streamfunction: r^2 Lap_m psi = A + m^2 B with A = r^2 psi'' + r psi',
+  // B = -psi; intcheb4rmult4lapl = I4[r^2 (A + m^2 B)] = N0 + m^2 N1 and
+  // intcheb4rmult4lapl2 = I4[r^4 Lap_m (r^-2 (A + m^2 B))]
+  //                     = I4[lapl4(A) + m^2 (lapl4(B) - A) - m^4 B] = L0 + m^2 L1 + m^4 L2
+  const Terms nA = {{2, r2}, {1, r1}};
+  const Terms nB = {{0, Poly{-1.0}}};
+  Terms l1 = lapl4(nB);
+  for (const Term& x : nA) add_term(l1, x.d, pscale(x.P, -1.0));
   struct Def { int id; Terms t; int k; };
   const Def defs[] = {
       {IM_I2R1, {{0, r1}}, 2},
@@ -206,6 +214,11 @@ void pz_integ_operators(int N, double r_icb, double r_cmb, double rnorm, std::ve
       {IM_S2, s2, 4},
       {IM_P0, Ta, 2},                               // I2 [r^2 omega] = P0 + m^2 P1
       {IM_P1, Tb, 2},
+      {IM_N0, times_r2(nA), 4},                     // intcheb4rmult4lapl = N0 + m^2 N1
+      {IM_N1, times_r2(nB), 4},
+      {IM_L0, lapl4(nA), 4},                        // intcheb4rmult4lapl2 = L0 + m^2 L1 + m^4 L2
+      {IM_L1, l1, 4},
+      {IM_L2, {{0, one}}, 4},
   };
   out.assign((size_t)IM_COUNT * N * N, 0.0);
   for (const Def& df : defs) {

@@ -49,6 +49,8 @@ enum {
                        // tau boundary rows, direct streamfunction solve
   PZF_RERR     = 256,  // l_rerror_fix: round-off threshold in the real
                        // Chebyshev derivative recursions of the m = 0 flow
+  PZF_CHEM     = 512,  // composition equation (raxi /= 0): update_xi_coll.f90,
+                       // update_xi_integ.f90, ChemFac buoyancy
 };
 
 // integration-method operators (N x N, column-major, times rnorm, tau rows
@@ -69,6 +71,11 @@ enum {
   IM_S2,
   IM_P0,        // I2 [r^2 omega(psi)] = P0 + m^2 P1 (rotating omega of the integ streamfunction);
   IM_P1,        //   intcheb2rmult2laplrot(m) = -(P0 + m^2 P1), the influence-matrix psi operator
+  IM_N0,        // intcheb4rmult4lapl(m)  = N0 + m^2 N1 (non-rotating streamfunction, I4 [r^4 Lap psi])
+  IM_N1,
+  IM_L0,        // intcheb4rmult4lapl2(m) = L0 + m^2 L1 + m^4 L2 (I4 [r^4 Lap^2 psi])
+  IM_L1,
+  IM_L2,
   IM_COUNT
 };
 
@@ -80,6 +87,8 @@ enum {
   RV_WSIMP,   // simps(f, theta) = sum_r WSIMP[r] f[r] (integration.f90:104-152)
   RV_BCTOP,   // influence-matrix boundary row at r_cmb (update_psi_coll_dmat.f90:1302-1376)
   RV_BCBOT,   // ... at r_icb
+  RV_XICOND,  // conducting composition and its radial derivative (radial.f90:194-195)
+  RV_DXICOND,
   RV_COUNT
 };
 
@@ -111,7 +120,9 @@ enum {
 
 // complex fields per instance, each M*N complex, at o_fld + 2*F_xxx*M*N
 enum {
-  F_US = 0, F_UP, F_OM, F_PSI, F_TEMP, F_DTEMP, F_DVST, F_DVSOM, F_COUNT
+  F_US = 0, F_UP, F_OM, F_PSI, F_TEMP, F_DTEMP, F_DVST, F_DVSOM,
+  F_XI, F_DXI, F_DVSXI,     // composition, d xi/dr, r u_s xi (zero without composition)
+  F_COUNT
 };
 
 struct PzInst {
@@ -126,14 +137,18 @@ struct PzInst {
   int nrad;                 // number of phi-FFT stages
   int radix[PZ_MAX_RADIX];
   double CorFac, BuoFac, TdiffFac, ViscFac, ek, tadvz, alpha;
+  double ChemFac, XidiffFac;  // composition (namelists.f90:476-522); 0 without it
+  int nhf;                    // history fields: 2 (temperature, psi) or 3 (+ composition)
   double dtMax, dtMin, courfac, dt_fac, rnorm;
   double r_cmb, r_icb;
   double nu_vol_den;        // rInt_R(dtcond^2 height r)
   double nu_int_fac;        // denominator of Nu_int
+  double sh_vol_den;        // rInt_R(dxicond^2 height r), denominator of Sh_vol
   long long o_rad;          // RV_COUNT*N
   long long o_basis;        // BM_COUNT*N*N (shared by instances of equal N)
   long long o_tw;           // 2*P: exp(-2 pi i k/P), shared by equal P
   long long o_gt;           // M*N*N   temperature operator per m
+  long long o_gx;           // M*N*N   composition operator per m (get_xiMat / integ xi lhs)
   long long o_gom;          // M*N*N   vorticity operator per m (influence)
   long long o_guphi;        // N*N     m=0 u_phi operator
   long long o_gpsi;         // M*N*N   K = G_psi P C per m: psi_cheb = -K om_cheb (dt independent)
@@ -144,7 +159,7 @@ struct PzInst {
   long long o_bt;           // DIRK tables, PZ_BT_SIZE doubles
   long long o_gass;         // DIRK assembly: M*N*N, psi_cheb = G_ass rhs (get_assMat, dt independent)
   long long o_fld;          // 2*F_COUNT*M*N
-  long long o_hist;         // 2*(2*(nold+nimp+nexp))*M*N
+  long long o_hist;         // 2*(nhf*(nold+nimp+nexp))*M*N
   long long o_cfl;          // 2*N: dtr, dth
   long long o_series;       // PZ_SERIES_CAP*16
   long long o_integ;        // integration method: IM_COUNT*N*N (shared by equal N, radratio)
@@ -169,8 +184,8 @@ struct PzState {
   double w_lhs;             // implicit weight the current operators were built with
 };
 
-// history ring accessors: field f in {0: temperature, 1: psi/omega},
-// kind in {0: old, 1: impl, 2: expl}
+// history ring accessors: field f in {0: temperature, 1: psi/omega,
+// 2: composition}, kind in {0: old, 1: impl, 2: expl}
 __host__ __device__ inline long long pz_hist_off(const PzInst& I, int f, int kind, int phys) {
   long long mn2 = 2LL * I.M * I.N;
   int per = I.nold + I.nimp + I.nexp;
@@ -191,6 +206,8 @@ struct PzDev {
   const int* iorder;                      // n_inst: instances in work-list order (their m items are
                                           // contiguous in mitems, m ascending)
   int n_inst;
+  int any_chem;             // some instance has composition: the step launches the
+                            // kernels' composition instantiations
   int maxN, maxP, maxM;
   int smem_build;           // dynamic shared memory of k_build (bytes)
   int smem_rloop;           // dynamic shared memory of k_rloop (bytes)
@@ -222,7 +239,8 @@ cudaError_t pz_launch_spectra(const PzDev& d, int inst, int n_m_max, double* out
 cudaError_t pz_launch_gather_rows(const PzDev& d, double* out, cudaStream_t s);
 cudaError_t pz_setup_kernels();
 size_t pz_build_smem_bytes(int n, bool direct, bool integ);   // k_build shared memory for one instance
-size_t pz_rloop_smem_bytes(int P, int M, int G);             // k_rloop shared memory, G radii per block
+size_t pz_rloop_smem_bytes(int P, int M, int G, int nt);     // k_rloop shared memory, G radii per block,
+                                                             // nt transforms per radius (2, or 3 with composition)
 
 // host: the integration-method operators of one (N, radratio), IM_COUNT
 // column-major N x N blocks, and their bandwidths (pz_integ_ops.cu)

@@ -154,10 +154,16 @@ struct StepIO {
   View V;
   int N;
   double2 *us, *up, *om, *T, *eT, *eP, *vsT, *vsOm;
+  double2 *X, *eX, *vsX;     // composition (null without it)
   double* cflv;
   __device__ double2 in(int f, int m, int r) const {
     const long long o = (long long)m * N + r;
-    return f == 0 ? us[o] : f == 1 ? up[o] : f == 2 ? om[o] : T[o];
+    return f == 0 ? us[o] : f == 1 ? up[o] : f == 2 ? om[o] : f == 3 ? T[o] : X[o];
+  }
+  __device__ void outx(int m, int r, double2 dxdt, double2 vsx) const {
+    const long long o = (long long)m * N + r;
+    eX[o] = dxdt;
+    vsX[o] = vsx;
   }
   __device__ void out(int m, int r, double2 dtdt, double2 vst, double2 dpdt, double2 vsom) const {
     const long long o = (long long)m * N + r;
@@ -172,6 +178,7 @@ struct StepIO {
   }
 };
 
+template <bool CHEM>
 __global__ void __launch_bounds__(256) k_rloop(PzDev d, int stage) {
   extern __shared__ double2 sh[];
   const PzItem it = d.ritems[blockIdx.x];
@@ -189,9 +196,13 @@ __global__ void __launch_bounds__(256) k_rloop(PzDev d, int stage) {
   io.eP = V.hist(1, 2, eslot, 0);
   io.vsT = V.fld(F_DVST, 0);
   io.vsOm = V.fld(F_DVSOM, 0);
+  const bool chem = CHEM && (I.flags & PZF_CHEM) != 0;
+  io.X = chem ? V.fld(F_XI, 0) : nullptr;
+  io.eX = chem ? V.hist(2, 2, eslot, 0) : nullptr;
+  io.vsX = chem ? V.fld(F_DVSXI, 0) : nullptr;
   io.cflv = d.pool + I.o_cfl;
-  double* rsh = reinterpret_cast<double*>(sh + 4 * I.rg * I.P);
-  rloop_group(I, V, it.idx, I.rg, io, sh, rsh);
+  double* rsh = reinterpret_cast<double*>(sh + (chem ? 6 : 4) * I.rg * I.P);
+  rloop_group<CHEM>(I, V, it.idx, I.rg, io, sh, rsh);
 }
 
 // ---------------------------------------------------------------------------
@@ -369,8 +380,8 @@ __device__ void equilibrate(double* A, int n, double* f1, double* f2, bool cols)
 }
 
 // kind: 0 temperature (get_tempMat), 1 omega (get_omMat), 2 psi (get_psiMat),
-// 3 uphi (get_uphiMat), 4 DIRK assembly psi (get_assMat).  Fills A
-// (row-major) before scaling.
+// 3 uphi (get_uphiMat), 4 DIRK assembly psi (get_assMat), 5 composition
+// (get_xiMat).  Fills A (row-major) before scaling.
 __device__ void fill_matrix(double* A, const BuildCtx& B, const View& V, int kind, int m, double wlin) {
   const PzInst& I = *B.I;
   const int n = B.N, n_max = I.n_max;
@@ -397,8 +408,9 @@ __device__ void fill_matrix(double* A, const BuildCtx& B, const View& V, int kin
       }
     } else {
       const double r0 = B.rm(i, k), r1 = B.drm(i, k), r2 = B.d2rm(i, k);
-      if (kind == 0) {
-        v = rn * (r0 - wlin * I.TdiffFac * (r2 + or1[i] * r1 - dm2 * or2[i] * r0));
+      if (kind == 0 || kind == 5) {
+        const double diff = kind == 0 ? I.TdiffFac : I.XidiffFac;
+        v = rn * (r0 - wlin * diff * (r2 + or1[i] * r1 - dm2 * or2[i] * r0));
       } else if (kind == 1) {
         v = rn * (r0 - wlin * I.ViscFac * (r2 + or1[i] * r1 - dm2 * or2[i] * r0));
       } else if (kind == 2) {
@@ -683,6 +695,7 @@ __global__ void __launch_bounds__(PZ_THREADS) k_build_static(PzDev d) {
 
 // dt dependent operators, rebuilt when lMat (step_time.f90:296-303):
 // temperature, omega and u_phi, plus the influence-matrix ingredients.
+template <bool CHEM>
 __device__ __forceinline__ void build_item(const PzDev& d, const PzItem it) {
   const PzInst& I = d.inst[it.inst];
   PzState& S = d.state[it.inst];
@@ -703,6 +716,14 @@ __device__ __forceinline__ void build_item(const PzDev& d, const PzItem it) {
     equilibrate(s.A, n, s.f1, s.f2, false);
     if (gj_invert(s.A, n, s.piv, s.colk, s.red, s.redi) != 0) { flag_status(S, PZ_E_SINGULAR); return; }
     store_op(d.pool + I.o_gt + (long long)mi * n * n, s.A, n, I.n_max, nullptr, s.f1);
+    __syncthreads();
+  }
+  if (CHEM && (I.flags & PZF_CHEM)) {
+    // composition (get_xiMat, update_xi_coll.f90:321-393: row scaling only)
+    fill_matrix(s.A, B, V, 5, m, wlin);
+    equilibrate(s.A, n, s.f1, s.f2, false);
+    if (gj_invert(s.A, n, s.piv, s.colk, s.red, s.redi) != 0) { flag_status(S, PZ_E_SINGULAR); return; }
+    store_op(d.pool + I.o_gx + (long long)mi * n * n, s.A, n, I.n_max, nullptr, s.f1);
     __syncthreads();
   }
   if (m == 0) {
@@ -762,7 +783,7 @@ __device__ __forceinline__ void build_item(const PzDev& d, const PzItem it) {
   }
 }
 
-__global__ void __launch_bounds__(PZ_THREADS) k_build(PzDev d) { build_item(d, d.mitems[blockIdx.x]); }
+__global__ void __launch_bounds__(PZ_THREADS) k_build(PzDev d) { build_item<true>(d, d.mitems[blockIdx.x]); }
 
 // ---------------------------------------------------------------------------
 // implicit terms from physical-space fields: get_temp_rhs_imp_coll and
@@ -792,6 +813,7 @@ struct MS {   // per-m vectors in shared memory
   double* red;
 };
 
+template <bool CHEM>
 __device__ void imp_from_physical(const View& V, const PzInst& I, int mi, int bo, int bi, bool calc, MS& s) {
   const int n = I.N;
   const int m = mi * I.minc;
@@ -821,6 +843,31 @@ __device__ void imp_from_physical(const View& V, const PzInst& I, int mi, int bo
     }
   }
   __syncthreads();
+  const bool chem = CHEM && (I.flags & PZF_CHEM) != 0;
+  double2* X = V.fld(F_XI, mi);
+  if (chem) {
+    // get_xi_rhs_imp_coll (update_xi_coll.f90:168-216)
+    for (int i = threadIdx.x; i < n; i += blockDim.x) s.a[i] = X[i];
+    __syncthreads();
+    op_Dp2(V, n, s.a, s.b, s.c, s.w);
+    __syncthreads();
+    double2* oX = V.hist(2, 0, bo, mi);
+    double2* iX = V.hist(2, 1, bi, mi);
+    double2* dX = V.fld(F_DXI, mi);
+    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+      const double2 t = s.a[i], d1 = s.b[i], d2 = s.c[i];
+      oX[i] = t;
+      if (calc) {
+        // assemble_xi_coll has no l_log_next refresh of dxi: it changes
+        // only with the implicit term (update_xi_coll.f90:188-195, :264-266)
+        dX[i] = d1;
+        const double f = I.XidiffFac;
+        iX[i] = make_double2(f * (d2.x + or1[i] * d1.x - dm2 * or2[i] * t.x),
+                             f * (d2.y + or1[i] * d1.y - dm2 * or2[i] * t.y));
+      }
+    }
+    __syncthreads();
+  }
   double2* oP = V.hist(1, 0, bo, mi);
   double2* iP = V.hist(1, 1, bi, mi);
   if (m == 0) {
@@ -849,6 +896,11 @@ __device__ void imp_from_physical(const View& V, const PzInst& I, int mi, int bo
           const double2 b = cim(dm, T[i]);
           const double c = rgrav[i] * or1[i] * I.BuoFac;
           v.x -= c * b.x; v.y -= c * b.y;
+          if (chem) {
+            const double2 bx = cim(dm, X[i]);
+            const double cx = rgrav[i] * or1[i] * I.ChemFac;
+            v.x -= cx * bx.x; v.y -= cx * bx.y;
+          }
         }
         iP[i] = v;
       }
@@ -857,7 +909,9 @@ __device__ void imp_from_physical(const View& V, const PzInst& I, int mi, int bo
   __syncthreads();
 }
 
-__device__ void integ_imp(const View& V, const PzInst& I, int mi, int bo, int bi, bool calc, bool from_us, MS& s);
+template <bool CHEM>
+__device__ void integ_imp(const View& V, const PzInst& I, int mi, int bo, int bi, bool calc, bool from_us, MS& s,
+                          bool psi_as_xi);
 
 __device__ MS ms_smem(int n) {
   extern __shared__ double2 shm[];
@@ -883,7 +937,7 @@ __global__ void __launch_bounds__(PZ_THREADS) k_start(PzDev d, int only) {
   const double dm = (double)m;
   MS s = ms_smem(n);
   // zero the history rings of this m
-  for (int f = 0; f < 2; ++f)
+  for (int f = 0; f < I.nhf; ++f)
     for (int kind = 0; kind < 3; ++kind) {
       const int ns = kind == 0 ? I.nold : (kind == 1 ? I.nimp : I.nexp);
       for (int ph = 0; ph < ns; ++ph) {
@@ -906,8 +960,8 @@ __global__ void __launch_bounds__(PZ_THREADS) k_start(PzDev d, int only) {
     om[i] = make_double2(w.x + or1[i] * u.x - or1[i] * vs.x, w.y + or1[i] * u.y - or1[i] * vs.y);
   }
   __syncthreads();
-  if (I.flags & PZF_INTEG) integ_imp(V, I, mi, S.b_old, S.b_impl, true, true, s);
-  else imp_from_physical(V, I, mi, S.b_old, S.b_impl, true, s);
+  if (I.flags & PZF_INTEG) integ_imp<true>(V, I, mi, S.b_old, S.b_impl, true, true, s, false);
+  else imp_from_physical<true>(V, I, mi, S.b_old, S.b_impl, true, s);
 }
 
 // ---------------------------------------------------------------------------
@@ -957,6 +1011,7 @@ __device__ __forceinline__ double2 dirk_rhs(const View& V, const PzInst& I, cons
 
 #include "pz_integ.cuh"
 
+template <bool CHEM>
 __device__ __forceinline__ void mloop_item(const PzDev& d, const PzItem it, int stage) {
   const PzInst& I = d.inst[it.inst];
   PzState& Sg = d.state[it.inst];
@@ -994,8 +1049,10 @@ __device__ __forceinline__ void mloop_item(const PzDev& d, const PzItem it, int 
   double2* psi = V.fld(F_PSI, mi);
   double2* T = V.fld(F_TEMP, mi);
   double2* dT = V.fld(F_DTEMP, mi);
+  double2* X = V.fld(F_XI, mi);
   const bool buo_imp = (I.flags & PZF_BUO_IMP) != 0;
   const bool direct = (I.flags & PZF_DIRECT) != 0;
+  const bool chem = CHEM && (I.flags & PZF_CHEM) != 0;
   // -- finish_exp_temp_coll (update_temp_coll.f90:152-176)
   if (do_finish) {
   for (int i = threadIdx.x; i < n; i += blockDim.x) {
@@ -1032,6 +1089,11 @@ __device__ __forceinline__ void mloop_item(const PzDev& d, const PzItem it, int 
           const double2 b = cim(dm, T[i]);
           const double cb = I.BuoFac * rgrav[i] * or1[i];
           p.x -= cb * b.x; p.y -= cb * b.y;
+          if (chem) {
+            const double2 bx = cim(dm, X[i]);
+            const double cx = I.ChemFac * rgrav[i] * or1[i];
+            p.x -= cx * bx.x; p.y -= cx * bx.y;
+          }
         }
         if (!direct && (I.flags & PZF_EK_PUMP)) {
           const double2 o = om[i], w = up[i];
@@ -1046,10 +1108,27 @@ __device__ __forceinline__ void mloop_item(const PzDev& d, const PzItem it, int 
     }
   }
   __syncthreads();
+  if (chem) {
+    // finish_exp_xi_coll (update_xi_coll.f90:142-166)
+    for (int i = threadIdx.x; i < n; i += blockDim.x) s.g[i] = V.fld(F_DVSXI, mi)[i];
+    __syncthreads();
+    op_D1p(V, n, s.g, s.h, s.w);
+    __syncthreads();
+    const double* dxicond = V.rad(RV_DXICOND);
+    double2* eX = V.hist(2, 2, eslot, mi);
+    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+      double2 e = eX[i];
+      const double2 u = us[i];
+      e.x = e.x - or1[i] * s.h[i].x - u.x * dxicond[i];
+      e.y = e.y - or1[i] * s.h[i].y - u.y * dxicond[i];
+      eX[i] = e;
+    }
+    __syncthreads();
+  }
   }
   if (!do_solve) return;   // assembly follows (k_assemble)
   // -- start_from_another_scheme (step_time.f90:417-516)
-  if (S.bridge) imp_from_physical(V, I, mi, S.r_old, S.r_impl, true, s);
+  if (S.bridge) imp_from_physical<CHEM>(V, I, mi, S.r_old, S.r_impl, true, s);
 
   // Implicit terms from the solve.  At every interior row the solution x of
   // (I - w L) x = rhs satisfies L x = (x - rhs) / w exactly, w being the weight
@@ -1100,13 +1179,51 @@ __device__ __forceinline__ void mloop_item(const PzDev& d, const PzItem it, int 
     }
   }
   __syncthreads();
-  // s.f keeps the new physical temperature
+  // s.f keeps the new physical temperature; with composition it becomes the
+  // buoyancy source BuoFac T + ChemFac xi, and bf (the factor of s.f in the
+  // buoyancy) is 1
+  double bf = I.BuoFac;
+  if (chem) {
+    // -- update_xi_co (update_xi_coll.f90:66-140): the temperature's solve with XidiffFac
+    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+      const double2 v = dirk ? dirk_rhs(V, I, S, 2, mi, i, stage) : imex_rhs(V, I, S, 2, mi, i);
+      s.a[i] = (i == 0 || i == n - 1) ? make_double2(0.0, 0.0) : v;   // topxi = botxi = 0
+    }
+    __syncthreads();
+    mv_lanes(d.pool + I.o_gx + (long long)mi * n * n, n, s.a, s.b);    // Chebyshev xi
+    __syncthreads();
+    if (resid) op_D1c(V, n, s.b, s.c, s.w);
+    else op_Dc2(V, n, s.b, s.c, s.e, s.w);
+    __syncthreads();
+    op_C(V, n, s.b, s.g, s.w);                                          // xi (physical)
+    __syncthreads();
+    double2* oX = V.hist(2, 0, oslot, mi);
+    double2* iX = V.hist(2, 1, islot, mi);
+    double2* dX = V.fld(F_DXI, mi);
+    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+      const double2 t = s.g[i], d1 = s.c[i], d2 = s.e[i];
+      X[i] = t;
+      dX[i] = d1;
+      if (wold) oX[i] = t;
+      bad |= !isfinite(t.x) || !isfinite(t.y);
+      if (resid) {
+        iX[i] = (i == 0 || i == n - 1) ? make_double2(0.0, 0.0) : cscale(iw, csub(t, s.a[i]));
+      } else if (calc) {
+        const double f = I.XidiffFac;
+        iX[i] = make_double2(f * (d2.x + or1[i] * d1.x - dm2 * or2[i] * t.x),
+                             f * (d2.y + or1[i] * d1.y - dm2 * or2[i] * t.y));
+      }
+      s.f[i] = cadd(cscale(I.BuoFac, s.f[i]), cscale(I.ChemFac, t));
+    }
+    bf = 1.0;
+    __syncthreads();
+  }
   // -- update_om_coll_dmat (update_psi_coll_dmat.f90:126-466)
   for (int i = threadIdx.x; i < n; i += blockDim.x) {
     double2 v = dirk ? dirk_rhs(V, I, S, 1, mi, i, stage) : imex_rhs(V, I, S, 1, mi, i);
     if (m != 0 && buo_imp) {
       const double2 b = cim(dm, s.f[i]);
-      const double c = S.wimp_lin[0] * I.BuoFac * rgrav[i] * or1[i];
+      const double c = S.wimp_lin[0] * bf * rgrav[i] * or1[i];
       v.x -= c * b.x; v.y -= c * b.y;
     }
     if (m == 0) v.y = 0.0;
@@ -1213,7 +1330,7 @@ __device__ __forceinline__ void mloop_item(const PzDev& d, const PzItem it, int 
         }
         if (buo_imp) {
           const double2 b = cim(dm, s.f[i]);
-          const double c = rgrav[i] * or1[i] * I.BuoFac;
+          const double c = rgrav[i] * or1[i] * bf;
           v.x -= c * b.x; v.y -= c * b.y;
         }
         iP[i] = v;
@@ -1223,7 +1340,7 @@ __device__ __forceinline__ void mloop_item(const PzDev& d, const PzItem it, int 
   if (__syncthreads_or(bad)) flag_status(Sg, PZ_E_NONFINITE);
 }
 
-__global__ void __launch_bounds__(256) k_mloop(PzDev d, int stage) { mloop_item(d, d.mitems[blockIdx.x], stage); }
+__global__ void __launch_bounds__(256) k_mloop(PzDev d, int stage) { mloop_item<true>(d, d.mitems[blockIdx.x], stage); }
 
 // ---------------------------------------------------------------------------
 // k_order + k_build_mloop: the operator rebuild fused with the first stage.
@@ -1278,12 +1395,13 @@ __global__ void __launch_bounds__(1024) k_order(PzDev d) {
   }
 }
 
+template <bool CHEM>
 __global__ void __launch_bounds__(256) k_build_mloop(PzDev d) {
   const PzItem it = d.order[blockIdx.x];
   if (d.inst[it.inst].flags & PZF_INTEG) return;
-  build_item(d, it);
+  build_item<CHEM>(d, it);
   __syncthreads();
-  mloop_item(d, it, 1);
+  mloop_item<CHEM>(d, it, 1);
 }
 
 // ---------------------------------------------------------------------------
@@ -1310,7 +1428,7 @@ __global__ void __launch_bounds__(256, 3) k_mloop_integ(PzDev d, int stage) {
   c.calc = c.dirk ? ((I.imp_mask >> (tgt - 1)) & 1) != 0 : S.l_calc_lin != 0;
   const View V{&I, d.pool};
   MS s = ms_smem(I.N);
-  const bool bad = integ_stage(d, V, I, S, it.idx, c, s);
+  const bool bad = integ_stage<true>(d, V, I, S, it.idx, c, s);
   if (__syncthreads_or(bad)) flag_status(Sg, PZ_E_NONFINITE);
 }
 
@@ -1368,6 +1486,14 @@ __global__ void __launch_bounds__(256) k_assemble(PzDev d) {
     if (i == 0 || i == n - 1) t = make_double2(0.0, 0.0);   // robin_bc, Dirichlet: topt = bott = 0
     T[i] = t;
     bad |= !isfinite(t.x) || !isfinite(t.y);
+    if (I.flags & PZF_CHEM) {
+      // assemble_xi_coll (update_xi_coll.f90:218-269)
+      double2 x = assemble_imex(V, I, S, 2, mi, i);
+      if (m == 0) x.y = 0.0;
+      if (i == 0 || i == n - 1) x = make_double2(0.0, 0.0);
+      V.fld(F_XI, mi)[i] = x;
+      bad |= !isfinite(x.x) || !isfinite(x.y);
+    }
     const double2 w = assemble_imex(V, I, S, 1, mi, i);
     if (m == 0) s.a[i] = (i == 0 || i == n - 1) ? make_double2(0.0, 0.0) : make_double2(w.x, 0.0);
     else s.a[i] = (i < 2 || i > n - 3) ? make_double2(0.0, 0.0) : w;
@@ -1402,7 +1528,7 @@ __global__ void __launch_bounds__(256) k_assemble(PzDev d) {
     }
   }
   __syncthreads();
-  imp_from_physical(V, I, mi, 0, 0, (I.imp_mask & 1) != 0, s);
+  imp_from_physical<true>(V, I, mi, 0, 0, (I.imp_mask & 1) != 0, s);
   if (__syncthreads_or(bad)) flag_status(Sg, PZ_E_NONFINITE);
 }
 
@@ -1416,7 +1542,7 @@ __device__ __forceinline__ double round_off(double x) { return fabs(x) < 10.0 * 
 // ---------------------------------------------------------------------------
 // k_spectra: snapshot spectra of one instance (calculate_spectra,
 // src/spectra.f90:104-196): per m, rInt_R of pi cc2real(f) r height for
-// f = us, up, om, T; one block per m
+// f = us, up, om, T, xi (zero without composition); one block per m
 // ---------------------------------------------------------------------------
 __global__ void k_spectra(PzDev d, int inst, double* out) {
   const PzInst& I = d.inst[inst];
@@ -1426,9 +1552,9 @@ __global__ void k_spectra(PzDev d, int inst, double* out) {
   const double* rr = V.rad(RV_R);
   const double* h = V.rad(RV_HEIGHT);
   const double* wint = V.rad(RV_WINT);
-  const int fl[4] = {F_US, F_UP, F_OM, F_TEMP};
+  const int fl[5] = {F_US, F_UP, F_OM, F_TEMP, F_XI};
   const double pi = 3.14159265358979323846;
-  for (int k = 0; k < 4; ++k) {
+  for (int k = 0; k < 5; ++k) {
     const double2* f = V.fld(fl[k], mi);
     double acc = 0.0;
     for (int r = threadIdx.x; r < n; r += blockDim.x) {
@@ -1437,7 +1563,7 @@ __global__ void k_spectra(PzDev d, int inst, double* out) {
       acc += wint[r] * (pi * c2 * rr[r] * h[r]);
     }
     acc = block_sum(acc, red);
-    if (threadIdx.x == 0) out[4 * mi + k] = acc;
+    if (threadIdx.x == 0) out[5 * mi + k] = acc;
   }
 }
 
@@ -1460,19 +1586,28 @@ __global__ void k_obs(PzDev d, int only) {
   const double2* up = V.fld(F_UP, 0);
   const double2* T = V.fld(F_TEMP, 0);
   const double2* dT = V.fld(F_DTEMP, 0);
+  const double2* X = V.fld(F_XI, 0);
+  const double2* dX = V.fld(F_DXI, 0);
   const bool rot = !(I.flags & PZF_NON_ROT);
-  double s_us = 0, s_up = 0, s_ax = 0, s_us3 = 0, s_up3 = 0, s_uz3 = 0, s_ax3 = 0, s_nu = 0, s_fl = 0;
+  const bool chem = (I.flags & PZF_CHEM) != 0;
+  double s_us = 0, s_up = 0, s_ax = 0, s_us3 = 0, s_up3 = 0, s_uz3 = 0, s_ax3 = 0, s_nu = 0, s_fl = 0, s_sh = 0;
   // thread (r, c) sums the m = c, c + nc, ... terms of radius r; the radial
   // weights are applied to those partial sums (their sum over c is the sum
   // over m of outputs.f90:418-830)
   const int nc = max(1, (int)blockDim.x / n);
   for (int t = threadIdx.x; t < nc * n; t += blockDim.x) {
     const int r = t % n, c = t / n;
-    double us2 = 0, up2 = 0, nu = 0, fl = 0, ax = 0;
+    double us2 = 0, up2 = 0, nu = 0, fl = 0, ax = 0, sh = 0;
     for (int mi = c; mi < M; mi += nc) {
       const long long o = (long long)mi * n + r;
       const double2 a = us[o], b = up[o], tt = T[o], dt = dT[o];
       const double mm = (double)(mi * I.minc);
+      if (chem) {
+        // sh_vol_r (outputs.f90:488-490)
+        const double2 x = X[o], dx = dX[o];
+        sh += mi == 0 ? dx.x * dx.x + mm * mm * or2[r] * (x.x * x.x)
+                      : 2.0 * (dx.x * dx.x + dx.y * dx.y) + mm * mm * or2[r] * 2.0 * (x.x * x.x + x.y * x.y);
+      }
       if (mi == 0) {
         us2 += a.x * a.x;
         up2 += b.x * b.x;
@@ -1501,10 +1636,12 @@ __global__ void k_obs(PzDev d, int only) {
       s_fl += wint[r] * fl * rr[r];
     }
     s_nu += wint[r] * nu;
+    s_sh += wint[r] * (sh * rr[r] * h[r]);
   }
   s_us = block_sum(s_us, red); s_up = block_sum(s_up, red); s_ax = block_sum(s_ax, red);
   s_us3 = block_sum(s_us3, red); s_up3 = block_sum(s_up3, red); s_uz3 = block_sum(s_uz3, red);
   s_ax3 = block_sum(s_ax3, red); s_nu = block_sum(s_nu, red); s_fl = block_sum(s_fl, red);
+  if (chem) s_sh = block_sum(s_sh, red);
   if (threadIdx.x != 0) return;
   const double pi = 3.14159265358979323846;
   double* row = d.pool + I.o_series + (long long)(S.series_count % PZ_SERIES_CAP) * PZ_SERIES_COLS;
@@ -1525,6 +1662,19 @@ __global__ void k_obs(PzDev d, int only) {
   row[13] = round_off(T[n - 1].x + tcond[n - 1]);
   row[14] = round_off(dtcond[n / 2 - 1] + dT[n / 2 - 1].x);
   row[15] = S.dt[0];
+  if (chem) {
+    // composition.TAG (outputs.f90:795-827)
+    const double* xicond = V.rad(RV_XICOND);
+    const double* dxicond = V.rad(RV_DXICOND);
+    row[16] = round_off(1.0 + dX[0].x / dxicond[0]);
+    row[17] = round_off(1.0 + dX[n - 1].x / dxicond[n - 1]);
+    row[18] = round_off(1.0 + s_sh / I.sh_vol_den);
+    row[19] = round_off(X[0].x + xicond[0]);
+    row[20] = round_off(X[n - 1].x + xicond[n - 1]);
+    row[21] = round_off(dxicond[n / 2 - 1] + dX[n / 2 - 1].x);
+  } else {
+    for (int k = 16; k < PZ_SERIES_COLS; ++k) row[k] = 0.0;
+  }
   S.series_count += 1;
 }
 
@@ -1574,8 +1724,8 @@ int mloop_threads(int maxN) {
 }
 }  // namespace
 
-size_t pz_rloop_smem_bytes(int P, int M, int G) {
-  return 4 * (size_t)G * P * sizeof(double2) + (3 + (size_t)M) * G * sizeof(double);
+size_t pz_rloop_smem_bytes(int P, int M, int G, int nt) {
+  return 2 * (size_t)nt * G * P * sizeof(double2) + (3 + (size_t)M) * G * sizeof(double);
 }
 
 namespace {
@@ -1589,9 +1739,11 @@ cudaError_t pz_setup_kernels() {
   cudaError_t e;
   const int big = 200 * 1024;
   if ((e = cudaFuncSetAttribute(k_build, cudaFuncAttributeMaxDynamicSharedMemorySize, PZ_SMEM_MAX))) return e;
-  if ((e = cudaFuncSetAttribute(k_build_mloop, cudaFuncAttributeMaxDynamicSharedMemorySize, PZ_SMEM_MAX))) return e;
+  if ((e = cudaFuncSetAttribute(k_build_mloop<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, PZ_SMEM_MAX))) return e;
+  if ((e = cudaFuncSetAttribute(k_build_mloop<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, PZ_SMEM_MAX))) return e;
   if ((e = cudaFuncSetAttribute(k_build_static, cudaFuncAttributeMaxDynamicSharedMemorySize, big))) return e;
-  if ((e = cudaFuncSetAttribute(k_rloop, cudaFuncAttributeMaxDynamicSharedMemorySize, PZ_SMEM_MAX))) return e;
+  if ((e = cudaFuncSetAttribute(k_rloop<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, PZ_SMEM_MAX))) return e;
+  if ((e = cudaFuncSetAttribute(k_rloop<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, PZ_SMEM_MAX))) return e;
   return cudaSuccess;
 }
 
@@ -1640,14 +1792,18 @@ cudaError_t pz_launch_gather_rows(const PzDev& d, double* out, cudaStream_t s) {
 
 cudaError_t pz_launch_step_kernel(const PzDev& d, int kind, int stage, cudaStream_t s) {
   switch (kind) {
-    case PZK_RLOOP: k_rloop<<<d.n_ritems, 256, d.smem_rloop, s>>>(d, stage); break;
+    case PZK_RLOOP:
+      if (d.any_chem) k_rloop<true><<<d.n_ritems, 256, d.smem_rloop, s>>>(d, stage);
+      else k_rloop<false><<<d.n_ritems, 256, d.smem_rloop, s>>>(d, stage);
+      break;
     case PZK_CFL: k_cfl<<<d.n_inst, 32, 0, s>>>(d); break;
     case PZK_BUILD: k_build<<<d.n_mitems, PZ_THREADS, d.smem_build, s>>>(d); break;
     case PZK_MLOOP: k_mloop<<<d.n_mitems, mloop_threads(d.maxN), ms_smem_bytes(d.maxN), s>>>(d, stage); break;
     case PZK_ORDER: k_order<<<1, 1024, 0, s>>>(d); break;
     case PZK_BUILD_MLOOP: {
       const size_t sm = (size_t)d.smem_build > ms_smem_bytes(d.maxN) ? (size_t)d.smem_build : ms_smem_bytes(d.maxN);
-      k_build_mloop<<<d.n_mitems, mloop_threads(d.maxN), sm, s>>>(d);
+      if (d.any_chem) k_build_mloop<true><<<d.n_mitems, mloop_threads(d.maxN), sm, s>>>(d);
+      else k_build_mloop<false><<<d.n_mitems, mloop_threads(d.maxN), sm, s>>>(d);
       break;
     }
     case PZK_MLOOP_INTEG:

@@ -26,6 +26,8 @@ struct ExplIO {
     const long long o = (long long)r * M + m;
     return f == 0 ? a->us[o] : f == 1 ? a->up[o] : f == 2 ? a->om[o] : a->temp[o];
   }
+  // composition: never asked for (the stage-level entry points reject it)
+  __device__ void outx(int, int, double2, double2) const {}
   __device__ void out(int m, int r, double2 dtdt, double2 vst, double2 dpdt, double2 vsom) const {
     const long long o = (long long)r * M + m;
     a->dTdt[o] = dtdt;
@@ -45,7 +47,7 @@ __global__ void __launch_bounds__(256) k_expl_rloop(PzExplArgs a) {
   const View V{&I, a.pool};
   ExplIO io{&a, I.N, I.M};
   double* rsh = reinterpret_cast<double*>(sh + 4 * PZ_RLOOP_G * I.P);
-  rloop_group(I, V, blockIdx.x * PZ_RLOOP_G, PZ_RLOOP_G, io, sh, rsh);
+  rloop_group<false>(I, V, blockIdx.x * PZ_RLOOP_G, PZ_RLOOP_G, io, sh, rsh);
 }
 
 // finish_exp_temp_coll and finish_exp_psi_coll_{dmat,smat} for one m

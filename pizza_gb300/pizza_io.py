@@ -20,6 +20,7 @@ SERIES_FILES = {
     "e_kin": (0, 1, 2, 3),                    # time, us2_2D, up2_2D, up2_axi_2D
     "e_kin_3D": (0, 4, 5, 6, 7),              # time, us2_3D, up2_3D, uz2_3D, up2_axi_3D
     "heat": (0, 8, 9, 10, 11, 12, 13, 14),    # time, NuTop, NuBot, Nu_vol, Nu_int, tTop, tBot, beta_t
+    "composition": (0, 16, 17, 18, 19, 20, 21),   # time, ShTop, ShBot, Sh_vol, xiTop, xiBot, beta_xi
 }
 
 
@@ -47,10 +48,11 @@ def format_series_line(values) -> str:
 def format_spectrum_lines(spec, minc: int = 1):
     """spec_N.TAG lines of write_spectra (src/spectra.f90:306-369): for each
     m, '(I5, 5ES16.8)' of m and the round_off'ed us2, up2, enstrophy, T^2 and
-    composition (zero) spectra.  spec: (n_m_max, 4) array."""
+    composition spectra.  spec: (n_m_max, 5) array, or (n_m_max, 4) without
+    the composition column (written as zero)."""
     lines = []
     for mi, row in enumerate(np.asarray(spec, float)):
-        vals = [_round_off(v) for v in row] + [0.0]
+        vals = [_round_off(v) for v in row] + [0.0] * (5 - len(row))
         lines.append(f"{mi * minc:5d}" + "".join(fortran_es(v, 16, 8) for v in vals))
     return lines
 
@@ -70,15 +72,15 @@ def write_spectrum(ens, i: int, counter: int, tag: str, directory: str = "."):
 
 
 def write_series(ens, i: int, tag: str, directory: str = ".", rows=None):
-    """Write e_kin.TAG, heat.TAG and (rotating runs) e_kin_3D.TAG of instance i
-    from its time-series rows (Ensemble.series: at most the last 1024).
-    Returns the paths written."""
+    """Write e_kin.TAG, heat.TAG, (rotating runs) e_kin_3D.TAG and (with
+    composition) composition.TAG of instance i from its time-series rows
+    (Ensemble.series: at most the last 1024).  Returns the paths written."""
     if rows is None:
         rows = ens.series(i)
     rot = not ens.configs[i].l_non_rot and ens.configs[i].ek >= 0.0
     paths = []
     for name, cols in SERIES_FILES.items():
-        if name == "e_kin_3D" and not rot:
+        if (name == "e_kin_3D" and not rot) or (name == "composition" and ens.configs[i].raxi == 0.0):
             continue
         p = os.path.join(directory, f"{name}.{tag}")
         with open(p, "w") as f:
@@ -106,10 +108,13 @@ def write_checkpoint(path: str, header: dict, fields: dict):
     """Write a version-7 checkpoint (write_checkpoint_mloc).
 
     header: time, family ('MULTISTEP' or 'DIRK'), nexp, nimp, nold, dt (array),
-    ra, pr, ek, radratio, n_r_max, m_max, minc, n_max, r (n_r_max radii).
+    ra, pr, ek, radratio, n_r_max, m_max, minc, n_max, r (n_r_max radii) and,
+    with composition, raxi and sc.
     fields: us, up, temp ((n_m_max, n_r_max) complex) and, for MULTISTEP,
     lists hist_P and hist_T of the slots written after up and temp: expl
-    2..nexp, impl 2..nimp, old 2..nold, in that order."""
+    2..nexp, impl 2..nimp, old 2..nold, in that order; with composition xi
+    and hist_Xi after them (write_one_field_mpi of xi_Mloc, checkpoints.f90:158)."""
+    chem = fields.get("xi") is not None
     h = header
     with open(path, "wb") as f:
         f.write(np.array([7], _I4).tobytes())
@@ -118,13 +123,14 @@ def write_checkpoint(path: str, header: dict, fields: dict):
         f.write(h["family"].ljust(10)[:10].encode())
         f.write(np.array([h["nexp"], h["nimp"], h["nold"]], _I4).tobytes())
         f.write(np.asarray(h["dt"], _F8).tobytes())
-        f.write(np.array([h["ra"], h["pr"], 0.0, 0.0, h["ek"], 0.0, h["radratio"]], _F8).tobytes())
+        f.write(np.array([h["ra"], h["pr"], h.get("raxi", 0.0), h.get("sc", 0.0), h["ek"], 0.0, h["radratio"]],
+                         _F8).tobytes())
         f.write(np.array([h["n_r_max"], h["m_max"], h["minc"]], _I4).tobytes())
         f.write("cheb".ljust(72).encode())
         f.write(np.array([h["n_max"], h.get("order_boundary", 0)], _I4).tobytes())
         f.write(np.array([0.0, 0.0], _F8).tobytes())                     # alph1, alph2 (no mapping)
         f.write(np.asarray(h["r"], _F8).tobytes())
-        f.write(np.array([1, 0, 0], _I4).tobytes())                      # l_heat, l_chem, l_phase_field
+        f.write(np.array([1, int(chem), 0], _I4).tobytes())              # l_heat, l_chem, l_phase_field
 
         def put(a):
             # (n_m_max, n_r_max) Fortran order: m fastest
@@ -137,6 +143,10 @@ def write_checkpoint(path: str, header: dict, fields: dict):
         put(fields["temp"])
         for a in fields.get("hist_T", []):
             put(a)
+        if chem:
+            put(fields["xi"])
+            for a in fields.get("hist_Xi", []):
+                put(a)
 
 
 def read_checkpoint(path: str) -> dict:
@@ -185,8 +195,11 @@ def read_checkpoint(path: str) -> dict:
     if h["l_heat"]:
         out["temp"] = field()
         out["hist_T"] = [field() for _ in range(nh)]
+    if h["l_chem"]:
+        out["xi"] = field()
+        out["hist_Xi"] = [field() for _ in range(nh)]
     if pos != len(buf):
-        raise ValueError(f"checkpoint {path}: {len(buf) - pos} trailing bytes (chemistry or phase field?)")
+        raise ValueError(f"checkpoint {path}: {len(buf) - pos} trailing bytes (phase field?)")
     return out
 
 
@@ -207,12 +220,15 @@ def save_checkpoint(ens, i: int, path: str):
                   dt=dt[:nexp] if family == "MULTISTEP" else dt[:1], ra=c.ra, pr=c.pr, ek=c.ek,
                   radratio=c.radratio, n_r_max=n, m_max=c.m_max, minc=c.minc,
                   n_max=c.n_cheb_max if c.n_cheb_max is not None else n, r=_grid_r(n, c.radratio),
-                  l_cheb_coll="COLL" in c.cheb_method.upper())
-    fields = dict(us=st["us"], up=st["up"], temp=st["temp"])
+                  l_cheb_coll="COLL" in c.cheb_method.upper(), raxi=c.raxi, sc=c.sc)
+    chem = c.raxi != 0.0
+    fields = dict(us=st["us"], up=st["up"], temp=st["temp"], xi=st["xi"] if chem else None)
     if family == "MULTISTEP":
         order = _hist_order(nexp, nimp, nold)
         fields["hist_P"] = [ens.get_history(i, 1, k, s) for k, s in order]
         fields["hist_T"] = [ens.get_history(i, 0, k, s) for k, s in order]
+        if chem:
+            fields["hist_Xi"] = [ens.get_history(i, 2, k, s) for k, s in order]
     write_checkpoint(path, header, fields)
 
 
@@ -264,20 +280,23 @@ def read_frame(path: str) -> dict:
 
 
 def save_frames(ens, i: int, counter: int, tag: str, directory: str = "."):
-    """frame_temp_<counter>.<tag>, frame_us_..., frame_up_..., frame_om_... of
-    instance i (outputs.f90:293-310: temperature, then the three flow
-    fields; temperature is the perturbation, tcond is in the header).
-    Returns the paths written."""
+    """frame_temp_<counter>.<tag>, (with composition) frame_xi_..., then
+    frame_us_..., frame_up_..., frame_om_... of instance i (outputs.f90:293-310;
+    temperature and composition are the perturbations, tcond and xicond are in
+    the header).  Returns the paths written."""
     c = ens.configs[i]
     n, _, _ = ens.dims[i]
     st = ens.get_state(i)
     time, _, _ = ens.get_step_state(i)
     r = _grid_r(n, c.radratio)
     r_cmb = 1.0 / (1.0 - c.radratio)
-    header = dict(time=time, ra=c.ra, ek=c.ek, pr=c.pr, radratio=c.radratio, sc=0.0, raxi=0.0, m_max=c.m_max,
-                  minc=c.minc, r=r, tcond=np.log(r / r_cmb) / np.log(c.radratio), xicond=None)
+    chem = c.raxi != 0.0
+    header = dict(time=time, ra=c.ra, ek=c.ek, pr=c.pr, radratio=c.radratio, sc=c.sc, raxi=c.raxi, m_max=c.m_max,
+                  minc=c.minc, r=r, tcond=np.log(r / r_cmb) / np.log(c.radratio),
+                  xicond=c.xicond_fac * np.log(r / r_cmb) / np.log(c.radratio) if chem else None)
     paths = []
-    for name, key in (("temp", "temp"), ("us", "us"), ("up", "up"), ("om", "om")):
+    names = (("temp", "temp"),) + ((("xi", "xi"),) if chem else ()) + (("us", "us"), ("up", "up"), ("om", "om"))
+    for name, key in names:
         p = os.path.join(directory, f"frame_{name}_{counter}.{tag}")
         write_frame(p, header, st[key])
         paths.append(p)
@@ -342,14 +361,21 @@ def restart_from_checkpoint(ens, i: int, path: str):
     nexp, nimp, nold, family = _scheme_counts(ens, i)
     coll = "COLL" in c.cheb_method.upper()
     coll_old = bool(h["l_cheb_coll"])
+    chem = c.raxi != 0.0 and h["l_chem"]
     ens.set_state(i, us=map_field(ck["us"], mm, n, True), up=map_field(ck["up"], mm, n, True),
-                  temp=map_field(ck["temp"], mm, n, True))
+                  temp=map_field(ck["temp"], mm, n, True),
+                  xi=map_field(ck["xi"], mm, n, True) if chem else None)
     if h["family"] == "MULTISTEP" and family == "MULTISTEP":
         counts = {2: nexp, 1: nimp, 0: nold}
-        for (k, slot), aP, aT in zip(_hist_order(h["nexp"], h["nimp"], h["nold"]), ck["hist_P"], ck["hist_T"]):
+        order = _hist_order(h["nexp"], h["nimp"], h["nold"])
+        for (k, slot), aP, aT in zip(order, ck["hist_P"], ck["hist_T"]):
             if slot <= counts[k]:
                 ens.set_history(i, 1, k, slot, map_field(aP, mm, n, coll_old, lbc=k != 0))
                 ens.set_history(i, 0, k, slot, map_field(aT, mm, n, coll_old, lbc=k != 0))
+        if chem:
+            for (k, slot), aX in zip(order, ck["hist_Xi"]):
+                if slot <= counts[k]:
+                    ens.set_history(i, 2, k, slot, map_field(aX, mm, n, coll_old, lbc=k != 0))
     nd = nexp if family == "MULTISTEP" else 1
     dt = np.array([h["dt"][min(k, len(h["dt"]) - 1)] for k in range(nd)])
     ab1 = h["ek"] != c.ek

@@ -5,7 +5,7 @@ import numpy as np
 
 from oracle.pizza_oracle import Params, Pizza, seeded_temperature
 
-ORACLE_ONLY = {"n_time_steps", "n_log_step", "init_t", "amp_t", "init_u", "amp_u"}
+ORACLE_ONLY = {"n_time_steps", "n_log_step", "init_t", "amp_t", "init_u", "amp_u", "init_xi", "amp_xi"}
 
 
 def gpu_config(spec):
@@ -14,9 +14,9 @@ def gpu_config(spec):
     return pz.Config(**kw)
 
 
-def oracle(spec, temp0=None):
+def oracle(spec, temp0=None, xi0=None):
     sim = Pizza(Params(**spec))
-    sim.start(temp0=temp0)
+    sim.start(temp0=temp0, xi0=xi0)
     return sim
 
 
@@ -39,5 +39,6 @@ def series_from_oracle(sim):
     ek = rows["e_kin"]
     e3 = rows.get("e_kin_3D", [ek[0], 0.0, 0.0, 0.0, 0.0])
     ht = rows["heat"]
+    ch = rows.get("composition", [0.0] * 7)
     return np.array([ek[0], ek[1], ek[2], ek[3], e3[1], e3[2], e3[3], e3[4],
-                     ht[1], ht[2], ht[3], ht[4], ht[5], ht[6], ht[7], sim.ts.dt[0]])
+                     ht[1], ht[2], ht[3], ht[4], ht[5], ht[6], ht[7], sim.ts.dt[0]] + list(ch[1:]))

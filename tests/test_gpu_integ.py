@@ -179,7 +179,7 @@ def test_rotinteg_continuation_fixture_on_gpu(pz, tmp_path):
 
 
 def test_integ_rejections(pz):
-    bad = [dict(CI, time_scheme="ARS232"), dict(CI, l_non_rot=True)]
+    bad = [dict(CI, time_scheme="ARS232"), dict(CI, ktopv=1)]
     for s in bad:
         with pytest.raises(RuntimeError):
             pz.Ensemble(gpu_config(s))

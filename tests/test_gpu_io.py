@@ -113,7 +113,8 @@ def test_device_spectra_match_oracle(pz, tmp_path, spec_extra):
     for _ in range(20):
         sim.advance()
     ens.step(20)
-    got, ref = ens.spectra(0), sim.spectra()[:, :4]
+    got, ref = ens.spectra(0)[:, :4], sim.spectra()[:, :4]
+    assert np.all(ens.spectra(0)[:, 4] == 0.0)                  # no composition
     # per spectrum, relative to its largest mode (the 1e-10 field bar)
     err = np.max(np.abs(got - ref), axis=0) / np.max(np.abs(ref), axis=0)
     assert np.all(err < 1e-10), err

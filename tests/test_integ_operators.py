@@ -50,6 +50,13 @@ def test_library_operators_match_oracle(pz, n, radratio):
         p2 = got["P0"][0] + m2 * got["P1"][0]
         w = ops._rows(c.integrated(omega_rot_terms(r_cmb, float(m)), 2), 2)
         assert np.max(np.abs(p2 - w)) <= 1e-12 * np.max(np.abs(w)), m
+        # non-rotating: intcheb4rmult4lapl and intcheb4rmult4lapl2
+        nl = got["N0"][0] + m2 * got["N1"][0]
+        w = ops.psi_nonrot(m)
+        assert np.max(np.abs(nl - w)) <= 1e-12 * np.max(np.abs(w)), m
+        nl2 = got["L0"][0] + m2 * (got["L1"][0] + m2 * got["L2"][0])
+        w = ops.psi_nonrot2(m)
+        assert np.max(np.abs(nl2 - w)) <= 1e-12 * np.max(np.abs(w)), m
 
 
 def test_operator_bad_arguments(pz):
