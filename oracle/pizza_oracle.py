@@ -9,9 +9,10 @@ streamfunction/vorticity system, both the coupled direct solve
 (src/update_psi_coll_dmat.f90), with the multistep IMEX schemes of
 src/multistep_schemes.f90 and the DIRK schemes of src/dirk_schemes.f90.
 With ``cheb_method="INTEG"`` the stage routines are those of the sparse
-Chebyshev-integration method with tau boundary rows and the direct
-streamfunction solve (src/update_temp_integ.f90,
-src/update_psi_integ_smat.f90), restated in oracle/pizza_integ.py.
+Chebyshev-integration method with tau boundary rows (src/update_temp_integ.f90,
+src/update_psi_integ_smat.f90, src/update_psi_integ_dmat.f90), restated in
+oracle/pizza_integ.py.  ``raxi /= 0`` adds the composition equation
+(src/update_xi_coll.f90, src/update_xi_integ.f90).
 
 It is the checker for the CUDA library and nothing else: only ``tests/``,
 ``__graft_entry__.smoke()`` and the ``cpu_baseline`` / ``--impl reference``
@@ -20,8 +21,8 @@ legs of ``bench.py`` import it.  The product path never calls it.
 Parity pin: the oracle reproduces the reference's own regression fixtures
 (``samples/*/reference.out``: NonRotRa2e3, RotE1e3EkPump first run,
 MultistepSchemes first run, TimeStepChange, DIRKSchemes first run, RotInteg
-first run) at the fixtures' rtol=1e-8, atol=1e-20, see
-``tests/test_oracle_golden.py``.  Third-party arithmetic the reference calls
+first run and continuation, FingConv first run and continuation) at the
+fixtures' rtol=1e-8, atol=1e-20, see ``tests/test_oracle_golden.py``.  Third-party arithmetic the reference calls
 (FFTW3 r2c/c2r/dft, LAPACK dgetrf/dgetrs/zgetrf/zgetrs; not vendored, versions
 unpinned in src/CMakeLists.txt) is restated with numpy.fft (pocketfft) and
 scipy.linalg (LAPACK getrf/getrs), which compute the same transforms and the
