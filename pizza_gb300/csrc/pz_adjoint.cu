@@ -248,7 +248,7 @@ __global__ void k_adj_bstate(PzAdjDev a, int n) {
 }
 
 // SOLVE^T and the local part of FIN^T for step n (snapshot `slot` = state n)
-__global__ void __launch_bounds__(256) k_adj_solve(PzAdjDev a, int n, int slot) {
+__global__ void __launch_bounds__(256, 3) k_adj_solve(PzAdjDev a, int n, int slot) {
   const PzItem it = a.d.mitems[blockIdx.x];
   const int inst = it.inst;
   const PzInst& I = a.d.inst[inst];

@@ -31,7 +31,10 @@ struct pz_handle {
   cudaStream_t stream = nullptr;
   cudaGraphExec_t graph = nullptr;
   double* d_rows = nullptr;    // n_inst x PZ_SERIES_COLS gather buffer
-  double* d_spec = nullptr;    // 4 x max n_m_max: spectra of one instance
+  double* d_spec = nullptr;    // 5 x max n_m_max: spectra of one instance
+  PzItem* d_oitems = nullptr;  // k_obs blocks
+  double* d_obs_part = nullptr;
+  int* d_obs_cnt = nullptr;
   std::string err = "no error";
   PzAdjoint* adj = nullptr;   // allocated by the first adjoint call
   std::vector<PzLaunch> plan;  // kernel launches of one step, in order

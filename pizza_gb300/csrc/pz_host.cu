@@ -731,10 +731,11 @@ extern "C" int pz_create(const pz_config* cfgs, int n, pz_handle** out) {
   std::stable_sort(order.begin(), order.end(), [&](int a, int b) {
     return (long long)h->inst[a].N * h->inst[a].M > (long long)h->inst[b].N * h->inst[b].M;
   });
-  std::vector<PzItem> ritems, mitems;
+  std::vector<PzItem> ritems, mitems, oitems;
   for (int i : order) {
     for (int r = 0; r < h->inst[i].N; r += h->inst[i].rg) ritems.push_back({i, r});
     for (int m = 0; m < h->inst[i].M; ++m) mitems.push_back({i, m});
+    for (int r = 0; r < h->inst[i].N; r += PZ_OBS_RC) oitems.push_back({i, r});
   }
   if ((e = cudaMalloc(&h->d_inst, n * sizeof(PzInst))) || (e = cudaMalloc(&h->d_state, n * sizeof(PzState))) ||
       (e = cudaMalloc(&h->d_ritems, ritems.size() * sizeof(PzItem))) ||
@@ -742,7 +743,10 @@ extern "C" int pz_create(const pz_config* cfgs, int n, pz_handle** out) {
       (e = cudaMalloc(&h->d_order, mitems.size() * sizeof(PzItem))) ||
       (e = cudaMalloc(&h->d_iorder, n * sizeof(int))) ||
       (e = cudaMalloc(&h->d_rows, (size_t)n * PZ_SERIES_COLS * sizeof(double))) ||
-      (e = cudaMalloc(&h->d_spec, (size_t)5 * maxM * sizeof(double)))) {
+      (e = cudaMalloc(&h->d_spec, (size_t)5 * maxM * sizeof(double))) ||
+      (e = cudaMalloc(&h->d_oitems, oitems.size() * sizeof(PzItem))) ||
+      (e = cudaMalloc(&h->d_obs_part, oitems.size() * PZ_OBS_NP * sizeof(double))) ||
+      (e = cudaMalloc(&h->d_obs_cnt, n * sizeof(int)))) {
     g_create_error = std::string("device allocation: ") + cudaGetErrorString(e);
     pz_destroy(h);
     return PZ_E_NOMEM;
@@ -751,6 +755,8 @@ extern "C" int pz_create(const pz_config* cfgs, int n, pz_handle** out) {
   cudaMemcpyAsync(h->d_ritems, ritems.data(), ritems.size() * sizeof(PzItem), cudaMemcpyHostToDevice, h->stream);
   cudaMemcpyAsync(h->d_mitems, mitems.data(), mitems.size() * sizeof(PzItem), cudaMemcpyHostToDevice, h->stream);
   cudaMemcpyAsync(h->d_iorder, order.data(), n * sizeof(int), cudaMemcpyHostToDevice, h->stream);
+  cudaMemcpyAsync(h->d_oitems, oitems.data(), oitems.size() * sizeof(PzItem), cudaMemcpyHostToDevice, h->stream);
+  cudaMemsetAsync(h->d_obs_cnt, 0, n * sizeof(int), h->stream);
   cudaMemsetAsync(h->d_state, 0, n * sizeof(PzState), h->stream);
   h->dev.inst = h->d_inst;
   h->dev.state = h->d_state;
@@ -758,6 +764,9 @@ extern "C" int pz_create(const pz_config* cfgs, int n, pz_handle** out) {
   h->dev.ritems = h->d_ritems; h->dev.n_ritems = (int)ritems.size();
   h->dev.mitems = h->d_mitems; h->dev.n_mitems = (int)mitems.size();
   h->dev.order = h->d_order;
+  h->dev.oitems = h->d_oitems; h->dev.n_oitems = (int)oitems.size();
+  h->dev.obs_part = h->d_obs_part;
+  h->dev.obs_cnt = h->d_obs_cnt;
   h->dev.iorder = h->d_iorder;
   h->dev.n_inst = n;
   h->dev.any_chem = 0;
@@ -1289,6 +1298,9 @@ extern "C" int pz_destroy(pz_handle* h) {
   cudaFree(h->d_iorder);
   cudaFree(h->d_rows);
   cudaFree(h->d_spec);
+  cudaFree(h->d_oitems);
+  cudaFree(h->d_obs_part);
+  cudaFree(h->d_obs_cnt);
   if (h->stream) cudaStreamDestroy(h->stream);
   delete h;
   return PZ_OK;

@@ -24,6 +24,8 @@
 #define PZ_RLOOP_PG 576     // k_rloop: radii per block = clamp(PZ_RLOOP_PG / n_phi_max, 1, 8), so
                             // that every block stages about the same 4*576 complex values
 #define PZ_SMEM_MAX (227 * 1024)
+#define PZ_OBS_RC 16        // k_obs: radii per block
+#define PZ_OBS_NP 10        // k_obs: partial sums per block
 #define PZ_MAX_STAGES 8     // DIRK stages
 #define PZ_BT_LD (PZ_MAX_STAGES + 1)
 // DIRK tables at o_bt (unscaled, row-major with leading dimension PZ_BT_LD):
@@ -202,6 +204,10 @@ struct PzDev {
   double* pool;
   const PzItem* ritems; int n_ritems;     // (inst, r)
   const PzItem* mitems; int n_mitems;     // (inst, m index)
+  const PzItem* oitems; int n_oitems;     // (inst, first radius) of the k_obs blocks, PZ_OBS_RC radii
+                                          // each, an instance's blocks consecutive
+  double* obs_part;                       // n_oitems x PZ_OBS_NP partial sums of k_obs
+  int* obs_cnt;                           // n_inst: k_obs blocks done this launch (reset by the last)
   PzItem* order;                          // n_mitems: k_order's layout of the fused first stage
   const int* iorder;                      // n_inst: instances in work-list order (their m items are
                                           // contiguous in mitems, m ascending)

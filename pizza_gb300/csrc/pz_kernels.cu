@@ -274,61 +274,132 @@ __global__ void k_cfl(PzDev d) {
 // ---------------------------------------------------------------------------
 // Gauss-Jordan inversion with partial pivoting of a row-major n x n matrix in
 // shared memory (in place).  Returns 0, or -1 on a zero pivot.
+//
+// Three phases and three barriers per pivot: (1) each warp proposes the
+// largest |A(i,k)|, i >= k (first index on ties, idamax semantics) with its
+// signed value; (2) every thread reduces the warps' proposals itself (the
+// same result everywhere), then the pivot row is swapped in, scaled by one
+// reciprocal of the pivot, and the pivot column of the other rows is saved;
+// (3) elimination.  The column swaps that undo the row pivoting are composed
+// into one permutation and applied per row, cycle by cycle, at the end.
+// T is double or double2 (izamax's |re| + |im| for the complex pivot).
 // ---------------------------------------------------------------------------
-__device__ int gj_invert(double* A, int n, int* piv, double* colk, double* red, int* redi) {
+__device__ __forceinline__ double gj_abs(double a) { return fabs(a); }
+__device__ __forceinline__ double gj_abs(double2 a) { return fabs(a.x) + fabs(a.y); }
+__device__ __forceinline__ bool gj_zero(double a) { return a == 0.0; }
+__device__ __forceinline__ bool gj_zero(double2 a) { return a.x == 0.0 && a.y == 0.0; }
+__device__ __forceinline__ double gj_inv(double a) { return 1.0 / a; }
+__device__ __forceinline__ double2 gj_inv(double2 a) {
+  const double den = a.x * a.x + a.y * a.y;
+  return make_double2(a.x / den, -a.y / den);
+}
+__device__ __forceinline__ double gj_mul(double a, double b) { return a * b; }
+__device__ __forceinline__ double2 gj_mul(double2 a, double2 b) { return cmul(a, b); }
+__device__ __forceinline__ double gj_axpy(double a, double c, double b) { return fma(-c, b, a); }   // a - c b
+__device__ __forceinline__ double2 gj_axpy(double2 a, double2 c, double2 b) { return csub(a, cmul(c, b)); }
+__device__ __forceinline__ double gj_one(double) { return 1.0; }
+__device__ __forceinline__ double2 gj_one(double2) { return make_double2(1.0, 0.0); }
+__device__ __forceinline__ double gj_nil(double) { return 0.0; }
+__device__ __forceinline__ double2 gj_nil(double2) { return make_double2(0.0, 0.0); }
+__device__ __forceinline__ double gj_shfl(double v, int o) { return __shfl_xor_sync(0xffffffffu, v, o); }
+__device__ __forceinline__ double2 gj_shfl(double2 v, int o) {
+  return make_double2(__shfl_xor_sync(0xffffffffu, v.x, o), __shfl_xor_sync(0xffffffffu, v.y, o));
+}
+// a warp's signed pivot candidate in red[8 + w] (and its imaginary part in red[16 + w])
+__device__ __forceinline__ void gj_put(double* red, int w, double a) { red[8 + w] = a; }
+__device__ __forceinline__ void gj_put(double* red, int w, double2 a) { red[8 + w] = a.x; red[16 + w] = a.y; }
+__device__ __forceinline__ void gj_get(const double* red, int w, double& a) { a = red[8 + w]; }
+__device__ __forceinline__ void gj_get(const double* red, int w, double2& a) { a = make_double2(red[8 + w], red[16 + w]); }
+
+// blockDim <= 256 (at most 8 warps); red: 32 doubles (per warp |pivot| at
+// [0, 8), the signed pivot at [8, 24)); colk: n values of T (also the
+// permutation scratch, 2n ints, at the end)
+template <class T>
+__device__ int gj_core(T* A, int n, int* piv, T* colk, double* red, int* redi) {
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
   for (int k = 0; k < n; ++k) {
-    // pivot: first index of max |A(i,k)|, i >= k (idamax semantics)
+    // (1) per-warp pivot proposals
     double best = -1.0;
     int bi = n;
+    T bv = gj_nil(T());
     for (int i = k + threadIdx.x; i < n; i += blockDim.x) {
-      const double v = fabs(A[i * n + k]);
-      if (v > best) { best = v; bi = i; }
+      const T a = A[i * n + k];
+      const double v = gj_abs(a);
+      if (v > best) { best = v; bi = i; bv = a; }
     }
     for (int o = 16; o > 0; o >>= 1) {
       const double ov = __shfl_xor_sync(0xffffffffu, best, o);
       const int oi = __shfl_xor_sync(0xffffffffu, bi, o);
-      if (ov > best || (ov == best && oi < bi)) { best = ov; bi = oi; }
+      const T oa = gj_shfl(bv, o);
+      if (ov > best || (ov == best && oi < bi)) { best = ov; bi = oi; bv = oa; }
     }
-    if (lane == 0) { red[wid] = best; redi[wid] = bi; }
-    __syncthreads();
-    if (threadIdx.x == 0) {
-      double b = red[0];
-      int ib = redi[0];
-      for (int w = 1; w < nw; ++w)
-        if (red[w] > b || (red[w] == b && redi[w] < ib)) { b = red[w]; ib = redi[w]; }
-      piv[k] = ib;
+    if (lane == 0) {
+      red[wid] = best;
+      redi[wid] = bi;
+      gj_put(red, wid, bv);
     }
     __syncthreads();
-    const int p = piv[k];
-    if (p >= n || A[p * n + k] == 0.0) return -1;
-    if (p != k) {
-      for (int j = threadIdx.x; j < n; j += blockDim.x) {
-        const double t = A[k * n + j]; A[k * n + j] = A[p * n + j]; A[p * n + j] = t;
-      }
-      __syncthreads();
+    // (2) every thread picks the pivot; swap, scale, save the pivot column
+    double b = red[0];
+    int p = redi[0];
+    int pw = 0;
+    for (int w = 1; w < nw; ++w)
+      if (red[w] > b || (red[w] == b && redi[w] < p)) { b = red[w]; p = redi[w]; pw = w; }
+    T pv;
+    gj_get(red, pw, pv);
+    if (p >= n || gj_zero(pv)) return -1;
+    if (threadIdx.x == 0) piv[k] = p;
+    const T rinv = gj_inv(pv);
+    for (int j = threadIdx.x; j < n; j += blockDim.x) {
+      const T ak = A[k * n + j], ap = A[p * n + j];
+      if (p != k) A[p * n + j] = ak;
+      A[k * n + j] = gj_mul(j == k ? gj_one(T()) : ap, rinv);
+      if (j == k && p != k) colk[p] = ak;     // the old A(k,k) is row p's pivot-column entry now
     }
-    const double pv = A[k * n + k];
-    for (int i = threadIdx.x; i < n; i += blockDim.x) colk[i] = A[i * n + k];
+    for (int i = threadIdx.x; i < n; i += blockDim.x)
+      if (i != k && i != p) colk[i] = A[i * n + k];
     __syncthreads();
-    for (int j = threadIdx.x; j < n; j += blockDim.x) A[k * n + j] = (j == k ? 1.0 : A[k * n + j]) / pv;
-    __syncthreads();
+    // (3) elimination
     for (int idx = threadIdx.x; idx < n * n; idx += blockDim.x) {
       const int i = idx / n, j = idx - i * n;
-      if (i != k) A[idx] = (j == k ? 0.0 : A[idx]) - colk[i] * A[k * n + j];
+      if (i != k) A[idx] = gj_axpy(j == k ? gj_nil(T()) : A[idx], colk[i], A[k * n + j]);
     }
     __syncthreads();
   }
-  for (int k = n - 1; k >= 0; --k) {
-    const int p = piv[k];
-    if (p != k) {
-      for (int i = threadIdx.x; i < n; i += blockDim.x) {
-        const double t = A[i * n + k]; A[i * n + k] = A[i * n + p]; A[i * n + p] = t;
-      }
+  // undo the row pivoting: the column swaps (k, piv[k]), k = n-1 .. 0, as
+  // one map src (final column j = current column src[j]) applied cycle by
+  // cycle in each row; lead marks the smallest index of each cycle
+  int* src = reinterpret_cast<int*>(colk);
+  int* lead = src + n;
+  if (threadIdx.x == 0) {
+    for (int j = 0; j < n; ++j) { src[j] = j; lead[j] = 0; }
+    for (int k = n - 1; k >= 0; --k) {
+      const int p = piv[k];
+      const int t = src[k]; src[k] = src[p]; src[p] = t;
     }
-    __syncthreads();
+    for (int j = 0; j < n; ++j) {
+      if (lead[j] != 0) continue;
+      lead[j] = 1;
+      for (int q = src[j]; q != j; q = src[q]) lead[q] = 2;
+    }
   }
+  __syncthreads();
+  for (int i = threadIdx.x; i < n; i += blockDim.x) {
+    T* row = A + (long long)i * n;
+    for (int l = 0; l < n; ++l) {
+      if (lead[l] != 1 || src[l] == l) continue;
+      const T t = row[l];
+      int j = l;
+      while (src[j] != l) { row[j] = row[src[j]]; j = src[j]; }
+      row[j] = t;
+    }
+  }
+  __syncthreads();
   return 0;
+}
+
+__device__ int gj_invert(double* A, int n, int* piv, double* colk, double* red, int* redi) {
+  return gj_core<double>(A, n, piv, colk, red, redi);
 }
 
 // Boundary rows and the Chebyshev boundary factor of the collocation builders.
@@ -468,61 +539,7 @@ __device__ double2 smat_entry(const BuildCtx& B, const View& V, int m, double wl
 // Gauss-Jordan inversion with partial pivoting (pivot: max |re| + |im|, the
 // cabs1 of izamax) of a complex row-major n x n matrix in shared memory.
 __device__ int gj_invert_c(double2* A, int n, int* piv, double2* colk, double* red, int* redi) {
-  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
-  for (int k = 0; k < n; ++k) {
-    double best = -1.0;
-    int bi = n;
-    for (int i = k + threadIdx.x; i < n; i += blockDim.x) {
-      const double v = fabs(A[i * n + k].x) + fabs(A[i * n + k].y);
-      if (v > best) { best = v; bi = i; }
-    }
-    for (int o = 16; o > 0; o >>= 1) {
-      const double ov = __shfl_xor_sync(0xffffffffu, best, o);
-      const int oi = __shfl_xor_sync(0xffffffffu, bi, o);
-      if (ov > best || (ov == best && oi < bi)) { best = ov; bi = oi; }
-    }
-    if (lane == 0) { red[wid] = best; redi[wid] = bi; }
-    __syncthreads();
-    if (threadIdx.x == 0) {
-      double b = red[0];
-      int ib = redi[0];
-      for (int w = 1; w < nw; ++w)
-        if (red[w] > b || (red[w] == b && redi[w] < ib)) { b = red[w]; ib = redi[w]; }
-      piv[k] = ib;
-    }
-    __syncthreads();
-    const int p = piv[k];
-    if (p >= n || (A[p * n + k].x == 0.0 && A[p * n + k].y == 0.0)) return -1;
-    if (p != k) {
-      for (int j = threadIdx.x; j < n; j += blockDim.x) {
-        const double2 t = A[k * n + j]; A[k * n + j] = A[p * n + j]; A[p * n + j] = t;
-      }
-      __syncthreads();
-    }
-    const double2 pv = A[k * n + k];
-    const double den = pv.x * pv.x + pv.y * pv.y;
-    const double2 inv = make_double2(pv.x / den, -pv.y / den);
-    for (int i = threadIdx.x; i < n; i += blockDim.x) colk[i] = A[i * n + k];
-    __syncthreads();
-    for (int j = threadIdx.x; j < n; j += blockDim.x)
-      A[k * n + j] = cmul(j == k ? make_double2(1.0, 0.0) : A[k * n + j], inv);
-    __syncthreads();
-    for (int idx = threadIdx.x; idx < n * n; idx += blockDim.x) {
-      const int i = idx / n, j = idx - i * n;
-      if (i != k) A[idx] = csub(j == k ? make_double2(0.0, 0.0) : A[idx], cmul(colk[i], A[k * n + j]));
-    }
-    __syncthreads();
-  }
-  for (int k = n - 1; k >= 0; --k) {
-    const int p = piv[k];
-    if (p != k) {
-      for (int i = threadIdx.x; i < n; i += blockDim.x) {
-        const double2 t = A[i * n + k]; A[i * n + k] = A[i * n + p]; A[i * n + p] = t;
-      }
-    }
-    __syncthreads();
-  }
-  return 0;
+  return gj_core<double2>(A, n, piv, colk, red, redi);
 }
 
 // smat operator of one m /= 0 by block elimination of the equilibrated
@@ -1340,7 +1357,7 @@ __device__ __forceinline__ void mloop_item(const PzDev& d, const PzItem it, int 
   if (__syncthreads_or(bad)) flag_status(Sg, PZ_E_NONFINITE);
 }
 
-__global__ void __launch_bounds__(256) k_mloop(PzDev d, int stage) { mloop_item<true>(d, d.mitems[blockIdx.x], stage); }
+__global__ void __launch_bounds__(256, 3) k_mloop(PzDev d, int stage) { mloop_item<true>(d, d.mitems[blockIdx.x], stage); }
 
 // ---------------------------------------------------------------------------
 // k_order + k_build_mloop: the operator rebuild fused with the first stage.
@@ -1396,7 +1413,7 @@ __global__ void __launch_bounds__(1024) k_order(PzDev d) {
 }
 
 template <bool CHEM>
-__global__ void __launch_bounds__(256) k_build_mloop(PzDev d) {
+__global__ void __launch_bounds__(256, 3) k_build_mloop(PzDev d) {
   const PzItem it = d.order[blockIdx.x];
   if (d.inst[it.inst].flags & PZF_INTEG) return;
   build_item<CHEM>(d, it);
@@ -1567,14 +1584,22 @@ __global__ void k_spectra(PzDev d, int inst, double* out) {
   }
 }
 
-__global__ void k_obs(PzDev d, int only) {
-  const int inst = blockIdx.x;
+// One block per PZ_OBS_RC radii of one instance (PzDev::oitems).  Thread
+// (r, c) sums the m = c, c + 16, ... terms of its radius; the block applies
+// the radial weights and writes its partial sums, and the last block of the
+// instance to finish (a counter per instance) adds the partials in radius
+// order and writes the row, so the result does not depend on block timing.
+__global__ void __launch_bounds__(256) k_obs(PzDev d, int only) {
+  const PzItem it = d.oitems[blockIdx.x];
+  const int inst = it.inst;
   if (only >= 0 && inst != only) return;
   const PzInst& I = d.inst[inst];
   PzState& S = d.state[inst];
   const View V{&I, d.pool};
-  __shared__ double red[32];
-  const int n = I.N, M = I.M;
+  constexpr int RC = PZ_OBS_RC, NC = 256 / PZ_OBS_RC;
+  __shared__ double q[6][NC][RC];
+  __shared__ int last;
+  const int n = I.N, M = I.M, r0 = it.idx;
   const double* rr = V.rad(RV_R);
   const double* or2 = V.rad(RV_OR2);
   const double* h = V.rad(RV_HEIGHT);
@@ -1590,59 +1615,88 @@ __global__ void k_obs(PzDev d, int only) {
   const double2* dX = V.fld(F_DXI, 0);
   const bool rot = !(I.flags & PZF_NON_ROT);
   const bool chem = (I.flags & PZF_CHEM) != 0;
-  double s_us = 0, s_up = 0, s_ax = 0, s_us3 = 0, s_up3 = 0, s_uz3 = 0, s_ax3 = 0, s_nu = 0, s_fl = 0, s_sh = 0;
-  // thread (r, c) sums the m = c, c + nc, ... terms of radius r; the radial
-  // weights are applied to those partial sums (their sum over c is the sum
-  // over m of outputs.f90:418-830)
-  const int nc = max(1, (int)blockDim.x / n);
-  for (int t = threadIdx.x; t < nc * n; t += blockDim.x) {
-    const int r = t % n, c = t / n;
+  {
+    const int rl = threadIdx.x % RC, c = threadIdx.x / RC, r = r0 + rl;
     double us2 = 0, up2 = 0, nu = 0, fl = 0, ax = 0, sh = 0;
-    for (int mi = c; mi < M; mi += nc) {
-      const long long o = (long long)mi * n + r;
-      const double2 a = us[o], b = up[o], tt = T[o], dt = dT[o];
-      const double mm = (double)(mi * I.minc);
-      if (chem) {
-        // sh_vol_r (outputs.f90:488-490)
-        const double2 x = X[o], dx = dX[o];
-        sh += mi == 0 ? dx.x * dx.x + mm * mm * or2[r] * (x.x * x.x)
-                      : 2.0 * (dx.x * dx.x + dx.y * dx.y) + mm * mm * or2[r] * 2.0 * (x.x * x.x + x.y * x.y);
-      }
-      if (mi == 0) {
-        us2 += a.x * a.x;
-        up2 += b.x * b.x;
-        ax = b.x * b.x;
-        nu += dt.x * dt.x + mm * mm * or2[r] * (tt.x * tt.x);
-        fl += a.x * tt.x - I.TdiffFac * dt.x - I.TdiffFac * dtcond[r];
-      } else {
-        us2 += 2.0 * (a.x * a.x + a.y * a.y);
-        up2 += 2.0 * (b.x * b.x + b.y * b.y);
-        nu += 2.0 * (dt.x * dt.x + dt.y * dt.y) + mm * mm * or2[r] * 2.0 * (tt.x * tt.x + tt.y * tt.y);
-        fl += 2.0 * (a.x * tt.x + a.y * tt.y);
+    if (r < n) {
+      for (int mi = c; mi < M; mi += NC) {
+        const long long o = (long long)mi * n + r;
+        const double2 a = us[o], b = up[o], tt = T[o], dt = dT[o];
+        const double mm = (double)(mi * I.minc);
+        if (chem) {
+          // sh_vol_r (outputs.f90:488-490)
+          const double2 x = X[o], dx = dX[o];
+          sh += mi == 0 ? dx.x * dx.x + mm * mm * or2[r] * (x.x * x.x)
+                        : 2.0 * (dx.x * dx.x + dx.y * dx.y) + mm * mm * or2[r] * 2.0 * (x.x * x.x + x.y * x.y);
+        }
+        if (mi == 0) {
+          us2 += a.x * a.x;
+          up2 += b.x * b.x;
+          ax = b.x * b.x;
+          nu += dt.x * dt.x + mm * mm * or2[r] * (tt.x * tt.x);
+          fl += a.x * tt.x - I.TdiffFac * dt.x - I.TdiffFac * dtcond[r];
+        } else {
+          us2 += 2.0 * (a.x * a.x + a.y * a.y);
+          up2 += 2.0 * (b.x * b.x + b.y * b.y);
+          nu += 2.0 * (dt.x * dt.x + dt.y * dt.y) + mm * mm * or2[r] * 2.0 * (tt.x * tt.x + tt.y * tt.y);
+          fl += 2.0 * (a.x * tt.x + a.y * tt.y);
+        }
       }
     }
-    nu = nu * rr[r] * h[r];
-    s_us += wint[r] * us2 * rr[r];
-    s_up += wint[r] * up2 * rr[r];
-    s_ax += wint[r] * ax * rr[r];
-    if (rot) {
-      s_us3 += wint[r] * us2 * rr[r] * h[r];
-      s_up3 += wint[r] * up2 * rr[r] * h[r];
-      s_uz3 += wint[r] * us2 * beta[r] * beta[r] * rr[r] * h[r] * h[r] * h[r] / 12.0;
-      s_ax3 += wint[r] * ax * rr[r] * h[r];
-      const double x = rr[r] / I.r_cmb;
-      s_fl += wsimp[r] * fl * x * x;
-    } else {
-      s_fl += wint[r] * fl * rr[r];
-    }
-    s_nu += wint[r] * nu;
-    s_sh += wint[r] * (sh * rr[r] * h[r]);
+    q[0][c][rl] = us2; q[1][c][rl] = up2; q[2][c][rl] = nu; q[3][c][rl] = fl; q[4][c][rl] = ax; q[5][c][rl] = sh;
   }
-  s_us = block_sum(s_us, red); s_up = block_sum(s_up, red); s_ax = block_sum(s_ax, red);
-  s_us3 = block_sum(s_us3, red); s_up3 = block_sum(s_up3, red); s_uz3 = block_sum(s_uz3, red);
-  s_ax3 = block_sum(s_ax3, red); s_nu = block_sum(s_nu, red); s_fl = block_sum(s_fl, red);
-  if (chem) s_sh = block_sum(s_sh, red);
-  if (threadIdx.x != 0) return;
+  __syncthreads();
+  // per radius: the sum over m (c in order), then the radial weights
+  double v[PZ_OBS_NP] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
+  if (threadIdx.x < 32) {
+    const int rl = threadIdx.x, r = r0 + rl;
+    if (rl < RC && r < n) {
+      double us2 = 0, up2 = 0, nu = 0, fl = 0, ax = 0, sh = 0;
+      for (int c = 0; c < NC; ++c) {
+        us2 += q[0][c][rl]; up2 += q[1][c][rl]; nu += q[2][c][rl];
+        fl += q[3][c][rl]; ax += q[4][c][rl]; sh += q[5][c][rl];
+      }
+      nu = nu * rr[r] * h[r];
+      v[0] = wint[r] * us2 * rr[r];
+      v[1] = wint[r] * up2 * rr[r];
+      v[2] = wint[r] * ax * rr[r];
+      if (rot) {
+        v[3] = wint[r] * us2 * rr[r] * h[r];
+        v[4] = wint[r] * up2 * rr[r] * h[r];
+        v[5] = wint[r] * us2 * beta[r] * beta[r] * rr[r] * h[r] * h[r] * h[r] / 12.0;
+        v[6] = wint[r] * ax * rr[r] * h[r];
+        const double x = rr[r] / I.r_cmb;
+        v[8] = wsimp[r] * fl * x * x;
+      } else {
+        v[8] = wint[r] * fl * rr[r];
+      }
+      v[7] = wint[r] * nu;
+      v[9] = wint[r] * (sh * rr[r] * h[r]);
+    }
+    for (int k = 0; k < PZ_OBS_NP; ++k) v[k] = warp_sum(v[k]);
+    if (threadIdx.x == 0) {
+      double* part = d.obs_part + (long long)blockIdx.x * PZ_OBS_NP;
+      for (int k = 0; k < PZ_OBS_NP; ++k) part[k] = v[k];
+      __threadfence();
+      const int nchunk = (n + RC - 1) / RC;
+      last = atomicAdd(d.obs_cnt + inst, 1) == nchunk - 1;
+    }
+  }
+  __syncthreads();
+  if (!last || threadIdx.x != 0) return;
+  __threadfence();
+  double s_us = 0, s_up = 0, s_ax = 0, s_us3 = 0, s_up3 = 0, s_uz3 = 0, s_ax3 = 0, s_nu = 0, s_fl = 0, s_sh = 0;
+  {
+    const int nchunk = (n + RC - 1) / RC;
+    const double* part = d.obs_part + (long long)(blockIdx.x - r0 / RC) * PZ_OBS_NP;
+    for (int k = 0; k < nchunk; ++k) {
+      const double* p = part + (long long)k * PZ_OBS_NP;
+      s_us += __ldcg(p + 0); s_up += __ldcg(p + 1); s_ax += __ldcg(p + 2);
+      s_us3 += __ldcg(p + 3); s_up3 += __ldcg(p + 4); s_uz3 += __ldcg(p + 5); s_ax3 += __ldcg(p + 6);
+      s_nu += __ldcg(p + 7); s_fl += __ldcg(p + 8); s_sh += __ldcg(p + 9);
+    }
+    d.obs_cnt[inst] = 0;
+  }
   const double pi = 3.14159265358979323846;
   double* row = d.pool + I.o_series + (long long)(S.series_count % PZ_SERIES_CAP) * PZ_SERIES_COLS;
   row[0] = S.time;
@@ -1780,7 +1834,7 @@ cudaError_t pz_launch_spectra(const PzDev& d, int inst, int n_m_max, double* out
 }
 
 cudaError_t pz_launch_obs(const PzDev& d, int only, cudaStream_t s) {
-  k_obs<<<d.n_inst, 256, 0, s>>>(d, only);
+  k_obs<<<d.n_oitems, 256, 0, s>>>(d, only);
   return cudaGetLastError();
 }
 
@@ -1809,7 +1863,7 @@ cudaError_t pz_launch_step_kernel(const PzDev& d, int kind, int stage, cudaStrea
     case PZK_MLOOP_INTEG:
       k_mloop_integ<<<d.n_mitems, mloop_threads(d.maxN), ms_smem_bytes(d.maxN), s>>>(d, stage);
       break;
-    case PZK_OBS: k_obs<<<d.n_inst, 256, 0, s>>>(d, -1); break;
+    case PZK_OBS: k_obs<<<d.n_oitems, 256, 0, s>>>(d, -1); break;
     case PZK_ASSEMBLE: k_assemble<<<d.n_mitems, mloop_threads(d.maxN), ms_smem_bytes(d.maxN), s>>>(d); break;
     default: return cudaErrorInvalidValue;
   }
