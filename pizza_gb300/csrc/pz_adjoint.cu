@@ -58,8 +58,12 @@ enum {
   AP_VTB, AP_VOB,                        // adjoint of dVsT, dVsOm
   AP_AUS, AP_AUP, AP_AOM, AP_AT,         // adjoint of us, up, om, T through the nonlinear terms
   AP_DB,                                 // dJ/dBuoFac partial sums per m (first M doubles)
-  AP_SNAP                                // snapshots, 4 planes each (T, us, up, om)
+  AP_SNAP                                // CNAB2: snapshots, 4 planes each (T, us, up, om)
 };
+// DIRK sweep: after AP_DB, the adjoint of the physical fields of the state
+// (lambda), of the old slot, and of the explicit and implicit terms of each
+// stage (2 planes each: temperature, vorticity); the snapshots follow
+enum { DP_LT = AP_SNAP, DP_LUS, DP_LUP, DP_LOM, DP_OT, DP_OP, DP_E };
 enum { SN_T = 0, SN_US, SN_UP, SN_OM };
 
 struct PzAdjDev {
@@ -76,23 +80,31 @@ struct PzAdjDev {
   int win0;                 // first state index of the averaging window
   double inv_window;
   int objective;            // PZ_OBJ_EKIN3D or PZ_OBJ_NUTOP
+  int snap0;                // plane of snapshot 0 (AP_SNAP, or after the DIRK planes)
+  // DIRK sweep (one tableau for all instances): stages, solved stages + 1
+  // (stage states per step), assembly stage, l_exp_calc / l_imp_calc_rhs bits
+  int dirk, ns, s1, assembly, exp_mask, imp_mask;
 };
 
 struct AdjView {
   const PzInst* I;
   double* base;
+  int snap0;
   __device__ double2* plane(long long k, int mi) const {
     return reinterpret_cast<double2*>(base) + (k * I->M + mi) * I->N;
   }
-  __device__ double2* snap(int slot, int f, int mi) const { return plane(AP_SNAP + 4LL * slot + f, mi); }
+  __device__ double2* snap(int slot, int f, int mi) const { return plane(snap0 + 4LL * slot + f, mi); }
   __device__ double2* ck(int n_snap, int ck_planes, int c, int k, int mi) const {
-    return plane(AP_SNAP + 4LL * n_snap + (long long)c * ck_planes + k, mi);
+    return plane(snap0 + 4LL * n_snap + (long long)c * ck_planes + k, mi);
   }
   __device__ double* db() const { return reinterpret_cast<double*>(plane(AP_DB, 0)); }
+  // DIRK: adjoint of the explicit (e) or implicit (i) term of stage slot k, field f (0 T, 1 vorticity)
+  __device__ double2* dE(int k, int f, int mi) const { return plane(DP_E + 2LL * k + f, mi); }
+  __device__ double2* dI(int ns, int k, int f, int mi) const { return plane(DP_E + 2LL * ns + 2LL * k + f, mi); }
 };
 
 __device__ __forceinline__ AdjView adj_view(const PzAdjDev& a, int inst) {
-  return AdjView{&a.d.inst[inst], a.ws + a.o_ws[inst]};
+  return AdjView{&a.d.inst[inst], a.ws + a.o_ws[inst], a.snap0};
 }
 
 // per-m scratch: 12 vectors of n complex, the parity-product scratch and a
@@ -635,6 +647,489 @@ __global__ void __launch_bounds__(256) k_adj_lin(PzAdjDev a, int n, int slot, in
   }
 }
 
+// ---------------------------------------------------------------------------
+// DIRK sweep (the stage loop of time_loop, step_time.f90:210-384, with the
+// tableaux of dirk_schemes.f90).  A step has the stage states z_0 = S_n and
+// z_s (s = 1..S', the solutions of the solved stages) with
+//   E_k   = FIN(NL(z_k))                        explicit term of stage k+1
+//   I_k   = L(z_k)                              implicit term (l_imp_calc_rhs)
+//   rhs_s = old + dt sum_{k<s} (bex[s][k] E_k + bim[s][k] I_k),   z_s = SOLVE(rhs_s)
+//   S_{n+1} = ASSEMBLE(old + dt sum_k (bae[k] E_k + bai[k] I_k))  (assembly
+//   schemes, update_temp_coll.f90:238-307, update_psi_coll_dmat.f90:684-827),
+//   else S_{n+1} = z_S
+// where old = (T, om) of z_0 (u_phi for m = 0).  Between steps the sweep
+// carries lambda, the adjoint of the physical fields (T, us, up, om) of the
+// state; the adjoints of old, E_k and I_k of the current step live in the
+// DP_ planes.  The stage-state fields are snapshots (s1 per step).
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ double dirk_w(const PzInst& I, const double* pool, int table, int row, int k) {
+  return pool[I.o_bt + table + row * PZ_BT_LD + k];
+}
+
+// objective source of state `slot`: d J / d (T, us, up) of the physical fields
+__device__ __forceinline__ void dadj_source(const PzAdjDev& a, const AdjView& A, const View& V, int mi, int slot,
+                                            int i, double2& Tb, double2& usb, double2& upb) {
+  const PzInst& I = *V.I;
+  if (a.objective == PZ_OBJ_NUTOP) {
+    // NuTop = 1 + dT/dr(m=0, r_cmb) / dtcond(r_cmb), dT/dr = D1p T (imp_from_physical)
+    if (mi == 0) Tb.x += a.inv_window / V.rad(RV_DTCOND)[0] * V.basis(BM_D1P)[(long long)i * I.N];
+    return;
+  }
+  const double pi = 3.14159265358979323846;
+  const double* rr = V.rad(RV_R);
+  const double* h = V.rad(RV_HEIGHT);
+  const double* beta = V.rad(RV_BETA);
+  const double* wint = V.rad(RV_WINT);
+  if (I.flags & PZF_NON_ROT) return;
+  const double W1 = pi * wint[i] * (rr[i] * h[i] + beta[i] * beta[i] * rr[i] * h[i] * h[i] * h[i] / 12.0);
+  const double W2 = pi * wint[i] * rr[i] * h[i];
+  const double2 us = A.snap(slot, SN_US, mi)[i], up = A.snap(slot, SN_UP, mi)[i];
+  if (mi != 0) {
+    usb = caxpy(4.0 * W1 * a.inv_window, us, usb);
+    upb = caxpy(4.0 * W2 * a.inv_window, up, upb);
+  } else {
+    usb.x += 2.0 * W1 * a.inv_window * us.x;
+    upb.x += 2.0 * W2 * a.inv_window * up.x;
+  }
+}
+
+// FIN^T, pointwise part (update_temp_coll.f90:152-176, update_psi_coll_dmat.f90:468-552):
+// adds the adjoint of the explicit term (eT, eP) to the field adjoints
+__device__ __forceinline__ void dadj_fin_pointwise(const PzInst& I, const View& V, int i, int m, double2 eT,
+                                                   double2 eP, double2& Tb, double2& usb, double2& upb,
+                                                   double2& omb) {
+  const double dm = (double)m;
+  const double* beta = V.rad(RV_BETA);
+  const double gT = V.rad(RV_DTCOND)[i] - I.tadvz * beta[i] * V.rad(RV_TCOND)[i];
+  usb = caxpy(-gT, eT, usb);
+  if (m != 0) {
+    if (!(I.flags & PZF_NON_ROT)) usb = caxpy(I.CorFac * beta[i], eP, usb);
+    if (I.flags & PZF_EK_PUMP) {
+      const double ce = I.CorFac * V.rad(RV_EKPUMP)[i];
+      usb = csub(usb, cscale(ce, csub(cscale(V.rad(RV_EKP_US)[i], eP), cscale(V.rad(RV_EKP_DUSDP)[i], cim(dm, eP)))));
+      upb = caxpy(-ce * V.rad(RV_EKP_UP)[i], eP, upb);
+      omb = caxpy(-ce, eP, omb);
+    }
+    if (!(I.flags & PZF_BUO_IMP)) Tb = cadd(Tb, cscale(I.BuoFac * V.rad(RV_RGRAV)[i] * V.rad(RV_OR1)[i], cim(dm, eP)));
+  }
+}
+
+// lambda at the final state: the objective source (zero outside the window)
+__global__ void k_dadj_term(PzAdjDev a, int slot, int src) {
+  const PzItem it = a.d.mitems[blockIdx.x];
+  const PzInst& I = a.d.inst[it.inst];
+  const View V{&I, a.d.pool};
+  const AdjView A = adj_view(a, it.inst);
+  const int mi = it.idx;
+  for (int i = threadIdx.x; i < I.N; i += blockDim.x) {
+    double2 Tb = cz(), usb = cz(), upb = cz();
+    if (src) dadj_source(a, A, V, mi, slot, i, Tb, usb, upb);
+    A.plane(DP_LT, mi)[i] = Tb;
+    A.plane(DP_LUS, mi)[i] = usb;
+    A.plane(DP_LUP, mi)[i] = upb;
+    A.plane(DP_LOM, mi)[i] = cz();
+  }
+}
+
+// ASSEMBLE^T (assembly schemes), or zero (the others): lambda of S_{n+1} ->
+// adjoints of old, E_k, I_k.  The assembly sets T = assembled values at the
+// interior radii (robin_bc: zero on the walls), psi = G_ass w (interior rows
+// 2..N-3) and us, up, om from psi; for m = 0 u_phi = Re w at the interior
+// radii and om = du/dr + u/r.
+__global__ void __launch_bounds__(256) k_dadj_ass(PzAdjDev a, int n) {
+  const PzItem it = a.d.mitems[blockIdx.x];
+  const int inst = it.inst;
+  const PzInst& I = a.d.inst[inst];
+  const View V{&I, a.d.pool};
+  const AdjView A = adj_view(a, inst);
+  const int N = I.N, mi = it.idx, m = mi * I.minc, ns = a.ns;
+  const double dm = (double)m, dm2 = dm * dm;
+  AS s = as_smem(N);
+  double2 *wT = s.v[0], *wP = s.v[1], *v0 = s.v[2], *v1 = s.v[3], *v2 = s.v[4], *t0 = s.v[5], *t1 = s.v[6],
+          *t2 = s.v[7], *pc = s.v[8];
+  if (!a.assembly) {
+    for (int i = threadIdx.x; i < N; i += blockDim.x) {
+      A.plane(DP_OT, mi)[i] = cz();
+      A.plane(DP_OP, mi)[i] = cz();
+      for (int k = 0; k < ns; ++k)
+        for (int f = 0; f < 2; ++f) { A.dE(k, f, mi)[i] = cz(); A.dI(ns, k, f, mi)[i] = cz(); }
+    }
+    return;
+  }
+  const double* or1 = V.rad(RV_OR1);
+  const double* or2 = V.rad(RV_OR2);
+  const double* beta = V.rad(RV_BETA);
+  const double* dbeta = V.rad(RV_DBETA);
+  for (int i = threadIdx.x; i < N; i += blockDim.x) {
+    double2 tb = A.plane(DP_LT, mi)[i];
+    if (mi == 0) tb.y = 0.0;
+    wT[i] = (i == 0 || i == N - 1) ? cz() : tb;
+    const double2 usb = A.plane(DP_LUS, mi)[i], upb = A.plane(DP_LUP, mi)[i], omb = A.plane(DP_LOM, mi)[i];
+    if (m != 0) {
+      // us = (i m / r) psi, up = -dpsi - beta psi, om = -(d2psi + c1 dpsi + c0 psi)
+      const double c1 = or1[i] + beta[i], c0 = or1[i] * beta[i] + dbeta[i] - dm2 * or2[i];
+      v0[i] = csub(csub(cscale(-or1[i], cim(dm, usb)), cscale(beta[i], upb)), cscale(c0, omb));
+      v1[i] = cscale(-1.0, caxpy(c1, omb, upb));
+      v2[i] = cscale(-1.0, omb);
+    } else {
+      v0[i] = omb;      // om = D1p u + u/r: D1p^T below
+      v1[i] = make_double2(upb.x + or1[i] * omb.x, 0.0);
+    }
+  }
+  __syncthreads();
+  if (m != 0) {
+    op_CT(V, N, v0, t0, s.w);
+    __syncthreads();
+    op_D1cT(V, N, v1, t1, s.w);
+    __syncthreads();
+    op_D2cT(V, N, v2, t2, s.w);
+    __syncthreads();
+    for (int i = threadIdx.x; i < N; i += blockDim.x) pc[i] = cadd(t0[i], cadd(t1[i], t2[i]));
+    __syncthreads();
+    mvT_lanes(a.d.pool + I.o_gass + (long long)mi * N * N, N, pc, wP);
+    __syncthreads();
+    for (int i = threadIdx.x; i < N; i += blockDim.x)
+      if (i < 2 || i > N - 3) wP[i] = cz();
+  } else {
+    op_D1pT(V, N, v0, t0, s.w);
+    __syncthreads();
+    for (int i = threadIdx.x; i < N; i += blockDim.x)
+      wP[i] = (i == 0 || i == N - 1) ? cz() : make_double2(v1[i].x + t0[i].x, 0.0);
+  }
+  __syncthreads();
+  const PzState& S = a.rec[(long long)inst * a.n_steps + n];
+  const double dt = S.dt[0];
+  for (int i = threadIdx.x; i < N; i += blockDim.x) {
+    const double2 rt = wT[i], rp = wP[i];
+    A.plane(DP_OT, mi)[i] = rt;
+    A.plane(DP_OP, mi)[i] = rp;
+    for (int k = 0; k < ns; ++k) {
+      const double we = dt * dirk_w(I, a.d.pool, PZ_BT_AEXP, 0, k), wi = dt * dirk_w(I, a.d.pool, PZ_BT_AIMP, 0, k);
+      A.dE(k, 0, mi)[i] = cscale(we, rt);
+      A.dE(k, 1, mi)[i] = cscale(we, rp);
+      A.dI(ns, k, 0, mi)[i] = cscale(wi, rt);
+      A.dI(ns, k, 1, mi)[i] = cscale(wi, rp);
+    }
+  }
+}
+
+// FIN^T, the D1p part, for the explicit term of stage state k (snapshot
+// `slot`): the inputs of k_adj_rloop (adjoints of E, dVsT, dVsOm), and the
+// explicit buoyancy's share of dJ/dBuoFac
+__global__ void __launch_bounds__(256) k_dadj_fin(PzAdjDev a, int k, int slot) {
+  const PzItem it = a.d.mitems[blockIdx.x];
+  const int inst = it.inst;
+  const PzInst& I = a.d.inst[inst];
+  const View V{&I, a.d.pool};
+  const AdjView A = adj_view(a, inst);
+  const int N = I.N, mi = it.idx, m = mi * I.minc;
+  const double dm = (double)m;
+  AS s = as_smem(N);
+  const double* or1 = V.rad(RV_OR1);
+  const double* rgrav = V.rad(RV_RGRAV);
+  double2 *x = s.v[0], *y = s.v[1], *t = s.v[2];
+  for (int i = threadIdx.x; i < N; i += blockDim.x) {
+    const double2 et = A.dE(k, 0, mi)[i], ep = A.dE(k, 1, mi)[i];
+    A.plane(AP_ETB, mi)[i] = et;
+    A.plane(AP_EPB, mi)[i] = ep;
+    x[i] = cscale(-or1[i], et);
+    y[i] = cscale(-or1[i], ep);
+  }
+  __syncthreads();
+  op_D1pT(V, N, x, t, s.w);
+  __syncthreads();
+  for (int i = threadIdx.x; i < N; i += blockDim.x) A.plane(AP_VTB, mi)[i] = t[i];
+  __syncthreads();
+  if (m != 0) {
+    op_D1pT(V, N, y, t, s.w);
+    __syncthreads();
+    for (int i = threadIdx.x; i < N; i += blockDim.x) A.plane(AP_VOB, mi)[i] = t[i];
+    if (!(I.flags & PZF_BUO_IMP)) {
+      const double2* Tk = A.snap(slot, SN_T, mi);
+      double acc = 0.0;
+      for (int i = threadIdx.x; i < N; i += blockDim.x)
+        acc += cdotr(A.dE(k, 1, mi)[i], cscale(-rgrav[i] * or1[i], cim(dm, Tk[i])));
+      acc = block_sum(acc, s.red);
+      if (threadIdx.x == 0) A.db()[mi] += acc;
+    }
+  } else {
+    for (int i = threadIdx.x; i < N; i += blockDim.x) A.plane(AP_VOB, mi)[i] = cz();
+  }
+}
+
+// Stage s (solved, snapshot `slot` holds z_s): the field adjoint of z_s
+// (lambda when z_s is S_{n+1}, the explicit term E_s through FIN^T and NL^T
+// when it is used), the implicit term I_s -> adjoint of the Chebyshev
+// solution (L^T, as k_adj_lin) -> SOLVE^T (as k_adj_solve) -> adjoint of
+// the right-hand side, added to old, E_k and I_k (k < s) with the stage's
+// Butcher weights.
+__global__ void __launch_bounds__(256, 2) k_dadj_stage(PzAdjDev a, int n, int st, int slot, int e_used) {
+  const PzItem it = a.d.mitems[blockIdx.x];
+  const int inst = it.inst;
+  const PzInst& I = a.d.inst[inst];
+  const PzState& S = a.rec[(long long)inst * a.n_steps + n];
+  const View V{&I, a.d.pool};
+  const AdjView A = adj_view(a, inst);
+  const int N = I.N, mi = it.idx, m = mi * I.minc, ns = a.ns;
+  const double dm = (double)m, dm2 = dm * dm;
+  AS s = as_smem(N);
+  const bool buo_imp = (I.flags & PZF_BUO_IMP) != 0;
+  const bool last = !a.assembly && st == ns;            // z_s is S_{n+1}
+  const bool has_imp = !last && ((a.imp_mask >> st) & 1);  // I_s in impl slot s
+  const double TdF = I.TdiffFac, Vis = I.ViscFac;
+  const double* or1 = V.rad(RV_OR1);
+  const double* or2 = V.rad(RV_OR2);
+  const double* beta = V.rad(RV_BETA);
+  const double* rgrav = V.rad(RV_RGRAV);
+  const double* ekpump = V.rad(RV_EKPUMP);
+  double2** v = s.v;
+  for (int i = threadIdx.x; i < N; i += blockDim.x) {
+    double2 Tb = cz(), usb = cz(), upb = cz(), omb = cz();
+    if (last) {
+      Tb = A.plane(DP_LT, mi)[i]; usb = A.plane(DP_LUS, mi)[i];
+      upb = A.plane(DP_LUP, mi)[i]; omb = A.plane(DP_LOM, mi)[i];
+    }
+    if (e_used) {
+      Tb = cadd(Tb, A.plane(AP_AT, mi)[i]); usb = cadd(usb, A.plane(AP_AUS, mi)[i]);
+      upb = cadd(upb, A.plane(AP_AUP, mi)[i]); omb = cadd(omb, A.plane(AP_AOM, mi)[i]);
+      dadj_fin_pointwise(I, V, i, m, A.dE(st, 0, mi)[i], A.dE(st, 1, mi)[i], Tb, usb, upb, omb);
+    }
+    const double2 iTb = has_imp ? A.dI(ns, st, 0, mi)[i] : cz();
+    const double2 iPb = has_imp ? A.dI(ns, st, 1, mi)[i] : cz();
+    v[1][i] = cscale(TdF, iTb);
+    v[2][i] = cscale(TdF * or1[i], iTb);
+    if (m != 0) {
+      double2 Tt = caxpy(-TdF * dm2 * or2[i], iTb, Tb);
+      if (buo_imp) Tt = cadd(Tt, cscale(I.BuoFac * rgrav[i] * or1[i], cim(dm, iPb)));
+      v[0][i] = Tt;
+      v[3][i] = caxpy(-Vis * dm2 * or2[i], iPb, omb);
+      v[4][i] = cscale(Vis, iPb);
+      v[5][i] = cscale(Vis * or1[i], iPb);
+      v[6][i] = csub(cscale(-or1[i], cim(dm, usb)), cscale(beta[i], upb));
+      v[7][i] = upb;
+    } else {
+      v[0][i] = Tb;
+      const double u0b = upb.x + or1[i] * omb.x + (-Vis * or2[i] - I.CorFac * ekpump[i]) * iPb.x;
+      v[3][i] = make_double2(u0b, 0.0);
+      v[4][i] = make_double2(Vis * iPb.x, 0.0);
+      v[5][i] = make_double2(omb.x + Vis * or1[i] * iPb.x, 0.0);
+    }
+  }
+  __syncthreads();
+  // L^T: Tc (v11), om_c or u_c (v0), psi_c (v1)
+  double2 *t0 = v[8], *t1 = v[9], *t2 = v[10], *Tc = v[11];
+  op_CT(V, N, v[0], t0, s.w);
+  __syncthreads();
+  op_D2cT(V, N, v[1], t1, s.w);
+  __syncthreads();
+  op_D1cT(V, N, v[2], t2, s.w);
+  __syncthreads();
+  for (int i = threadIdx.x; i < N; i += blockDim.x) Tc[i] = cadd(t0[i], cadd(t1[i], t2[i]));
+  __syncthreads();
+  op_CT(V, N, v[3], t0, s.w);
+  __syncthreads();
+  op_D2cT(V, N, v[4], t1, s.w);
+  __syncthreads();
+  op_D1cT(V, N, v[5], t2, s.w);
+  __syncthreads();
+  double2 *oc = v[0], *pc = v[1];
+  for (int i = threadIdx.x; i < N; i += blockDim.x) {
+    const double2 o = cadd(t0[i], cadd(t1[i], t2[i]));
+    oc[i] = (m == 0) ? make_double2(o.x, 0.0) : o;
+  }
+  __syncthreads();
+  if (m != 0) {
+    op_CT(V, N, v[6], t0, s.w);
+    __syncthreads();
+    op_D1cT(V, N, v[7], t1, s.w);
+    __syncthreads();
+    for (int i = threadIdx.x; i < N; i += blockDim.x) pc[i] = csub(t0[i], t1[i]);
+    __syncthreads();
+  }
+  // SOLVE^T (update_temp_co, update_om_coll_dmat), transposed as in k_adj_solve
+  const double wl0 = S.wimp_lin[0];
+  double2 *x = v[2], *y = v[3], *rT = v[4], *rP = v[5];
+  if (m != 0) {
+    const long long MN = (long long)I.M * N;
+    const double* aux = a.d.pool + I.o_aux;
+    const double* om2 = aux + 0 * MN + (long long)mi * N;
+    const double* om3 = aux + 1 * MN + (long long)mi * N;
+    const double* psi2 = aux + 2 * MN + (long long)mi * N;
+    const double* psi3 = aux + 3 * MN + (long long)mi * N;
+    const double* infl = aux + 4 * MN + 4LL * mi;
+    const double* bct = V.rad(RV_BCTOP);
+    const double* bcb = V.rad(RV_BCBOT);
+    double c1r = 0.0, c1i = 0.0, c2r = 0.0, c2i = 0.0;
+    for (int i = threadIdx.x; i < N; i += blockDim.x) {
+      c1r += psi2[i] * pc[i].x + om2[i] * oc[i].x;
+      c1i += psi2[i] * pc[i].y + om2[i] * oc[i].y;
+      c2r += psi3[i] * pc[i].x + om3[i] * oc[i].x;
+      c2i += psi3[i] * pc[i].y + om3[i] * oc[i].y;
+    }
+    c1r = block_sum(c1r, s.red); c1i = block_sum(c1i, s.red);
+    c2r = block_sum(c2r, s.red); c2i = block_sum(c2i, s.red);
+    const double ttr = -infl[0] * c1r - infl[2] * c2r, tti = -infl[0] * c1i - infl[2] * c2i;
+    const double tbr = -infl[1] * c1r - infl[3] * c2r, tbi = -infl[1] * c1i - infl[3] * c2i;
+    for (int i = threadIdx.x; i < N; i += blockDim.x)
+      x[i] = make_double2(pc[i].x + ttr * bct[i] + tbr * bcb[i], pc[i].y + tti * bct[i] + tbi * bcb[i]);
+    __syncthreads();
+    mvT_lanes(a.d.pool + I.o_gpsi + (long long)mi * N * N, N, x, y);
+    __syncthreads();
+    for (int i = threadIdx.x; i < N; i += blockDim.x) x[i] = csub(oc[i], y[i]);
+    __syncthreads();
+    mvT_lanes(a.d.pool + I.o_gom + (long long)mi * N * N, N, x, rP);
+    __syncthreads();
+    for (int i = threadIdx.x; i < N; i += blockDim.x) {
+      if (i == 0 || i == N - 1) rP[i] = cz();
+      x[i] = buo_imp ? cscale(wl0 * I.BuoFac * rgrav[i] * or1[i], cim(dm, rP[i])) : cz();
+    }
+    __syncthreads();
+    if (buo_imp) {
+      op_CT(V, N, x, y, s.w);
+      __syncthreads();
+      for (int i = threadIdx.x; i < N; i += blockDim.x) Tc[i] = cadd(Tc[i], y[i]);
+      __syncthreads();
+    }
+  } else {
+    mvT_lanes(a.d.pool + I.o_guphi, N, oc, rP);
+    __syncthreads();
+    for (int i = threadIdx.x; i < N; i += blockDim.x)
+      if (i == 0 || i == N - 1) rP[i] = cz(); else rP[i].y = 0.0;
+    __syncthreads();
+  }
+  const double* GT = ((I.flags & PZF_T_IS_OM) && m != 0) ? a.d.pool + I.o_gom + (long long)mi * N * N
+                                                         : a.d.pool + I.o_gt + (long long)mi * N * N;
+  mvT_lanes(GT, N, Tc, rT);
+  __syncthreads();
+  // distribute the right-hand side's adjoint (dirk_rhs)
+  const double dt = S.dt[0];
+  const double2* Ts = A.snap(slot, SN_T, mi);
+  double acc = 0.0;
+  for (int i = threadIdx.x; i < N; i += blockDim.x) {
+    const double2 rt = (i == 0 || i == N - 1) ? cz() : rT[i];
+    const double2 rp = rP[i];
+    A.plane(DP_OT, mi)[i] = cadd(A.plane(DP_OT, mi)[i], rt);
+    A.plane(DP_OP, mi)[i] = cadd(A.plane(DP_OP, mi)[i], rp);
+    for (int k = 0; k < st; ++k) {
+      const double we = dt * dirk_w(I, a.d.pool, PZ_BT_EXP, st, k), wi = dt * dirk_w(I, a.d.pool, PZ_BT_IMP, st, k);
+      if (we != 0.0) {
+        A.dE(k, 0, mi)[i] = caxpy(we, rt, A.dE(k, 0, mi)[i]);
+        A.dE(k, 1, mi)[i] = caxpy(we, rp, A.dE(k, 1, mi)[i]);
+      }
+      if (wi != 0.0) {
+        A.dI(ns, k, 0, mi)[i] = caxpy(wi, rt, A.dI(ns, k, 0, mi)[i]);
+        A.dI(ns, k, 1, mi)[i] = caxpy(wi, rp, A.dI(ns, k, 1, mi)[i]);
+      }
+    }
+    if (m != 0 && buo_imp) {
+      // buoyancy of the new temperature in this solve, and in I_s
+      const double c = rgrav[i] * or1[i];
+      acc += cdotr(rp, cscale(-wl0 * c, cim(dm, Ts[i])));
+      if (has_imp) acc += cdotr(A.dI(ns, st, 1, mi)[i], cscale(-c, cim(dm, Ts[i])));
+    }
+  }
+  acc = block_sum(acc, s.red);
+  if (threadIdx.x == 0) A.db()[mi] += acc;
+}
+
+// z_0 = S_n (snapshot `slot`): lambda_n from old, I_0 (imp_from_physical,
+// D2p = D2c C), E_0 (FIN^T after k_adj_rloop) and the objective source
+__global__ void __launch_bounds__(256) k_dadj_z0(PzAdjDev a, int slot, int src) {
+  const PzItem it = a.d.mitems[blockIdx.x];
+  const int inst = it.inst;
+  const PzInst& I = a.d.inst[inst];
+  const View V{&I, a.d.pool};
+  const AdjView A = adj_view(a, inst);
+  const int N = I.N, mi = it.idx, m = mi * I.minc, ns = a.ns;
+  const double dm = (double)m, dm2 = dm * dm;
+  AS s = as_smem(N);
+  const bool buo_imp = (I.flags & PZF_BUO_IMP) != 0;
+  const bool has_imp = (a.imp_mask & 1) != 0;
+  const double TdF = I.TdiffFac, Vis = I.ViscFac;
+  const double* or1 = V.rad(RV_OR1);
+  const double* or2 = V.rad(RV_OR2);
+  const double* rgrav = V.rad(RV_RGRAV);
+  const double* ekpump = V.rad(RV_EKPUMP);
+  double2 *Tb = s.v[0], *usb = s.v[1], *upb = s.v[2], *omb = s.v[3];
+  double2 *aT = s.v[4], *bT = s.v[5], *aP = s.v[6], *bP = s.v[7], *t0 = s.v[8], *t1 = s.v[9];
+  const double2* T0 = A.snap(slot, SN_T, mi);
+  double acc = 0.0;
+  for (int i = threadIdx.x; i < N; i += blockDim.x) {
+    double2 tb = cadd(A.plane(DP_OT, mi)[i], A.plane(AP_AT, mi)[i]);
+    double2 ub = A.plane(AP_AUS, mi)[i], pb = A.plane(AP_AUP, mi)[i], ob = A.plane(AP_AOM, mi)[i];
+    const double2 op = A.plane(DP_OP, mi)[i];
+    if (m != 0) ob = cadd(ob, op);
+    else pb.x += op.x;
+    dadj_fin_pointwise(I, V, i, m, A.dE(0, 0, mi)[i], A.dE(0, 1, mi)[i], tb, ub, pb, ob);
+    if (src) dadj_source(a, A, V, mi, slot, i, tb, ub, pb);
+    const double2 iTb = has_imp ? A.dI(ns, 0, 0, mi)[i] : cz();
+    const double2 iPb = has_imp ? A.dI(ns, 0, 1, mi)[i] : cz();
+    tb = caxpy(-TdF * dm2 * or2[i], iTb, tb);
+    aT[i] = cscale(TdF, iTb);
+    bT[i] = cscale(TdF * or1[i], iTb);
+    if (m != 0) {
+      ob = caxpy(-Vis * dm2 * or2[i], iPb, ob);
+      if (buo_imp) {
+        const double c = rgrav[i] * or1[i];
+        tb = cadd(tb, cscale(I.BuoFac * c, cim(dm, iPb)));
+        acc += cdotr(iPb, cscale(-c, cim(dm, T0[i])));
+      }
+      aP[i] = cscale(Vis, iPb);
+      bP[i] = cscale(Vis * or1[i], iPb);
+    } else {
+      pb.x += (-Vis * or2[i] - I.CorFac * ekpump[i]) * iPb.x;
+      aP[i] = make_double2(Vis * iPb.x, 0.0);
+      bP[i] = make_double2(Vis * or1[i] * iPb.x, 0.0);
+    }
+    Tb[i] = tb; usb[i] = ub; upb[i] = pb; omb[i] = ob;
+  }
+  acc = block_sum(acc, s.red);
+  if (threadIdx.x == 0) A.db()[mi] += acc;
+  __syncthreads();
+  if (has_imp) {
+    // T: D2p^T (TdF iT) + D1p^T (TdF/r iT)
+    op_D2cT(V, N, aT, t0, s.w);
+    __syncthreads();
+    op_CT(V, N, t0, t1, s.w);
+    __syncthreads();
+    op_D1pT(V, N, bT, t0, s.w);
+    __syncthreads();
+    for (int i = threadIdx.x; i < N; i += blockDim.x) Tb[i] = cadd(Tb[i], cadd(t0[i], t1[i]));
+    __syncthreads();
+    op_D2cT(V, N, aP, t0, s.w);
+    __syncthreads();
+    op_CT(V, N, t0, t1, s.w);
+    __syncthreads();
+    op_D1pT(V, N, bP, t0, s.w);
+    __syncthreads();
+    for (int i = threadIdx.x; i < N; i += blockDim.x) {
+      const double2 d = cadd(t0[i], t1[i]);
+      if (m != 0) omb[i] = cadd(omb[i], d);
+      else upb[i].x += d.x;
+    }
+    __syncthreads();
+  }
+  for (int i = threadIdx.x; i < N; i += blockDim.x) {
+    double2 tb = Tb[i];
+    if (m == 0) tb.y = 0.0;
+    A.plane(DP_LT, mi)[i] = tb;
+    A.plane(DP_LUS, mi)[i] = (m == 0) ? cz() : usb[i];
+    A.plane(DP_LUP, mi)[i] = (m == 0) ? make_double2(upb[i].x, 0.0) : upb[i];
+    A.plane(DP_LOM, mi)[i] = (m == 0) ? make_double2(omb[i].x, 0.0) : omb[i];
+  }
+}
+
+// dJ/dT0 of the DIRK sweep: lambda_0's temperature (the start state is physical)
+__global__ void k_dadj_out(PzAdjDev a) {
+  const PzItem it = a.d.mitems[blockIdx.x];
+  const int inst = it.inst;
+  const PzInst& I = a.d.inst[inst];
+  const AdjView A = adj_view(a, inst);
+  const int mi = it.idx;
+  double2* out = reinterpret_cast<double2*>(a.out + a.o_out[inst]);
+  for (int i = threadIdx.x; i < I.N; i += blockDim.x) out[mi + (long long)i * I.M] = A.plane(DP_LT, mi)[i];
+}
+
 // dJ/dT0 = C^T Tc_bar(0), in the ABI layout (m fastest)
 __global__ void __launch_bounds__(256) k_adj_out(PzAdjDev a) {
   const PzItem it = a.d.mitems[blockIdx.x];
@@ -670,6 +1165,8 @@ __global__ void k_adj_db(PzAdjDev a, double* out) {
 // ---------------------------------------------------------------------------
 struct PzAdjoint {
   int n_steps = 0, K = 0, n_seg = 0, n_window = 0, n_snap = 0, n_ck = 0, ck_planes = 0, objective = 0;
+  int snap0 = AP_SNAP;       // first snapshot plane
+  int dirk = 0, ns = 1, s1 = 1, assembly = 0, exp_mask = 1, imp_mask = 1;   // DIRK sweep
   bool ready = false;        // a forward sweep is stored
   bool last_valid = false;   // snapshots of the last segment are those of the forward sweep
   double* ws = nullptr;
@@ -724,6 +1221,13 @@ PzAdjDev adj_dev(pz_handle* h) {
   a.win0 = A->n_steps - A->n_window + 1;
   a.inv_window = A->n_window > 0 ? 1.0 / A->n_window : 0.0;
   a.objective = A->objective;
+  a.snap0 = A->snap0;
+  a.dirk = A->dirk;
+  a.ns = A->ns;
+  a.s1 = A->s1;
+  a.assembly = A->assembly;
+  a.exp_mask = A->exp_mask;
+  a.imp_mask = A->imp_mask;
   return a;
 }
 
@@ -741,6 +1245,24 @@ cudaError_t launch_fwd(const PzDev& d, cudaStream_t s) {
     const cudaError_t e = pz_launch_step_kernel(d, k, 1, s);
     if (e) return e;
   }
+  return cudaSuccess;
+}
+
+// one forward DIRK step without the time series (the stage loop of the plan:
+// per stage k_rloop, [k_cfl, k_build after stage 1], k_mloop, then
+// k_assemble), with the stage states saved to snapshots base .. base + s1 - 1
+// when base >= 0
+cudaError_t launch_fwd_dirk(const PzDev& d, const PzAdjDev& a, int base, cudaStream_t s) {
+  cudaError_t e;
+  if (base >= 0 && (e = launch_snap(a, base, s))) return e;
+  for (int st = 1; st <= a.ns; ++st) {
+    if ((e = pz_launch_step_kernel(d, PZK_RLOOP, st, s))) return e;
+    if (st == 1 && ((e = pz_launch_step_kernel(d, PZK_CFL, 1, s)) || (e = pz_launch_step_kernel(d, PZK_BUILD, 1, s))))
+      return e;
+    if ((e = pz_launch_step_kernel(d, PZK_MLOOP, st, s))) return e;
+    if (base >= 0 && st < a.s1 && (e = launch_snap(a, base + st, s))) return e;
+  }
+  if (a.assembly && (e = pz_launch_step_kernel(d, PZK_ASSEMBLE, 0, s))) return e;
   return cudaSuccess;
 }
 
@@ -783,10 +1305,12 @@ extern "C" int pz_adjoint_forward(pz_handle* h, int objective, int n_steps, int 
   if (n_window < 0 || n_window > n_steps) return pz_fail(h, PZ_E_ARG, "pz_adjoint_forward: n_window outside [0, n_steps]");
   for (int i = 0; i < h->n_inst; ++i) {
     const PzInst& I = h->inst[i];
-    if (I.scheme != PZ_CNAB2 || (I.flags & (PZF_DIRECT | PZF_INTEG | PZF_CHEM)))
+    if ((I.scheme != PZ_CNAB2 && !I.dirk) || (I.flags & (PZF_DIRECT | PZF_INTEG | PZF_CHEM)))
       return pz_fail(h, PZ_E_UNSUPPORTED,
-                     "pz_adjoint_forward: the adjoint covers the collocation CNAB2 step with the influence-matrix "
-                     "solve, without composition");
+                     "pz_adjoint_forward: the adjoint covers the collocation step with the influence-matrix solve "
+                     "(CNAB2 or a DIRK scheme), without composition");
+    if (I.scheme != h->inst[0].scheme)
+      return pz_fail(h, PZ_E_UNSUPPORTED, "pz_adjoint_forward: all instances must use the same time scheme");
     if (adj_rloop_smem_bytes(I.P, I.rg) > PZ_SMEM_MAX)
       return pz_fail(h, PZ_E_UNSUPPORTED, "pz_adjoint_forward: n_phi_max too large for the adjoint transform kernel");
   }
@@ -811,12 +1335,22 @@ extern "C" int pz_adjoint_forward(pz_handle* h, int objective, int n_steps, int 
   A->n_window = n_window;
   A->K = (checkpoint_every <= 0 || checkpoint_every > n_steps) ? n_steps : checkpoint_every;
   A->n_seg = (n_steps + A->K - 1) / A->K;
-  A->n_snap = A->K + 1;
+  {
+    const PzInst& I0 = h->inst[0];
+    A->dirk = I0.dirk;
+    A->ns = I0.nstages;
+    A->assembly = I0.dirk ? I0.assembly : 0;
+    A->s1 = I0.dirk ? I0.nstages - A->assembly + 1 : 1;
+    A->exp_mask = I0.exp_mask;
+    A->imp_mask = I0.imp_mask;
+    A->snap0 = I0.dirk ? DP_E + 4 * I0.nstages : AP_SNAP;
+    A->ck_planes = F_XI + 2 * (I0.nold + I0.nimp + I0.nexp);
+  }
+  A->n_snap = A->K * A->s1 + 1;       // stage states of every step of a segment, plus the final state
   A->n_ck = A->n_seg + 1;             // one per segment start, plus the final state
-  A->ck_planes = F_XI + 2 * (1 + 1 + 2);
   std::vector<long long> ows(h->n_inst), oout(h->n_inst);
   long long tot = 0, tout = 0;
-  const long long planes = AP_SNAP + 4LL * A->n_snap + (long long)A->n_ck * A->ck_planes;
+  const long long planes = A->snap0 + 4LL * A->n_snap + (long long)A->n_ck * A->ck_planes;
   for (int i = 0; i < h->n_inst; ++i) {
     const long long MN = (long long)h->inst[i].M * h->inst[i].N;
     ows[i] = tot;
@@ -853,14 +1387,18 @@ extern "C" int pz_adjoint_forward(pz_handle* h, int objective, int n_steps, int 
   const int k0_last = (A->n_seg - 1) * A->K;
   for (int n = 0; n < n_steps; ++n) {
     if (n % A->K == 0 && (e = launch_ckpt(a, n / A->K, 0, s))) return acuda(h, e, "checkpoint");
-    if (n >= k0_last && (e = launch_snap(a, n - k0_last, s))) return acuda(h, e, "snapshot");
-    if ((e = launch_fwd(dF, s))) return acuda(h, e, "forward step");
+    if (A->dirk) {
+      if ((e = launch_fwd_dirk(dF, a, n >= k0_last ? (n - k0_last) * A->s1 : -1, s))) return acuda(h, e, "forward step");
+    } else {
+      if (n >= k0_last && (e = launch_snap(a, n - k0_last, s))) return acuda(h, e, "snapshot");
+      if ((e = launch_fwd(dF, s))) return acuda(h, e, "forward step");
+    }
     if (n_window > 0 && n + 1 >= a.win0) {
       k_adj_ke<<<h->n_inst, PZ_THREADS, 0, s>>>(a);
       if ((e = cudaGetLastError())) return acuda(h, e, "objective");
     }
   }
-  if ((e = launch_snap(a, n_steps - k0_last, s)) || (e = launch_ckpt(a, A->n_seg, 0, s)))
+  if ((e = launch_snap(a, (n_steps - k0_last) * A->s1, s)) || (e = launch_ckpt(a, A->n_seg, 0, s)))
     return acuda(h, e, "final state");
   int rc = pz_check_status(h);
   if (rc) return rc;
@@ -876,6 +1414,83 @@ extern "C" int pz_adjoint_forward(pz_handle* h, int objective, int n_steps, int 
   A->last_valid = true;
   return PZ_OK;
 }
+
+namespace {
+// the backward sweep of a DIRK scheme (see the DIRK kernels above)
+int dirk_backward(pz_handle* h, const PzAdjDev& a, const PzDev& dR, const PzDev& dB, int threads, size_t smem,
+                  size_t rsmem, double* dJ_dtemp, double* dJ_dra) {
+  PzAdjoint* A = h->adj;
+  cudaStream_t s = h->stream;
+  cudaError_t e;
+  const int n_steps = A->n_steps, K = A->K, s1 = A->s1;
+  const int k0_last = (A->n_seg - 1) * K;
+  const int mb = h->dev.n_mitems;
+  if (!A->last_valid) {
+    if ((e = launch_ckpt(a, A->n_seg - 1, 1, s))) return acuda(h, e, "restore");
+    for (int n = k0_last; n < n_steps; ++n)
+      if ((e = launch_fwd_dirk(dR, a, (n - k0_last) * s1, s))) return acuda(h, e, "recompute");
+    if ((e = launch_snap(a, (n_steps - k0_last) * s1, s))) return acuda(h, e, "recompute");
+  }
+  k_dadj_term<<<mb, 64, 0, s>>>(a, (n_steps - k0_last) * s1, A->n_window > 0 ? 1 : 0);
+  if ((e = cudaGetLastError())) return acuda(h, e, "adjoint terminal");
+  for (int sg = A->n_seg - 1; sg >= 0; --sg) {
+    const int k0 = sg * K, k1 = std::min(k0 + K, n_steps);
+    if (sg != A->n_seg - 1) {
+      if ((e = launch_ckpt(a, sg, 1, s))) return acuda(h, e, "restore");
+      for (int n = k0; n < k1; ++n)
+        if ((e = launch_fwd_dirk(dR, a, (n - k0) * s1, s))) return acuda(h, e, "recompute");
+      if ((e = launch_snap(a, (k1 - k0) * s1, s))) return acuda(h, e, "recompute");
+    }
+    for (int n = k1 - 1; n >= k0; --n) {
+      bool rebuild = false;
+      if (n < k1 - 1)
+        for (int i = 0; i < h->n_inst && !rebuild; ++i) {
+          const PzState* r = &A->h_rec[(size_t)i * n_steps];
+          rebuild = r[n].wimp_lin[0] != r[n + 1].wimp_lin[0];
+        }
+      if (rebuild) {
+        k_adj_bstate<<<(h->n_inst + 63) / 64, 64, 0, s>>>(a, n);
+        if ((e = cudaGetLastError()) || (e = pz_launch_step_kernel(dB, PZK_BUILD, 1, s))) return acuda(h, e, "rebuild");
+      }
+      const int b = (n - k0) * s1;
+      k_dadj_ass<<<mb, threads, smem, s>>>(a, n);
+      for (int st = s1 - 1; st >= 1; --st) {
+        const int e_used = (st < A->ns && ((A->exp_mask >> st) & 1)) ? 1 : 0;
+        if (e_used) {
+          k_dadj_fin<<<mb, threads, smem, s>>>(a, st, b + st);
+          k_adj_rloop<<<h->dev.n_ritems, 256, rsmem, s>>>(a, b + st);
+        }
+        k_dadj_stage<<<mb, threads, smem, s>>>(a, n, st, b + st, e_used);
+      }
+      k_dadj_fin<<<mb, threads, smem, s>>>(a, 0, b);
+      k_adj_rloop<<<h->dev.n_ritems, 256, rsmem, s>>>(a, b);
+      k_dadj_z0<<<mb, threads, smem, s>>>(a, b, n >= a.win0 ? 1 : 0);
+      if ((e = cudaGetLastError())) return acuda(h, e, "adjoint step");
+    }
+  }
+  A->last_valid = false;
+  k_dadj_out<<<mb, 64, 0, s>>>(a);
+  k_adj_db<<<(h->n_inst + 63) / 64, 64, 0, s>>>(a, A->d_J);
+  if ((e = cudaGetLastError())) return acuda(h, e, "adjoint output");
+  if ((e = launch_ckpt(a, A->n_seg, 1, s))) return acuda(h, e, "restore final state");
+  std::vector<double> db(h->n_inst);
+  std::vector<PzState> bst(h->n_inst);
+  if ((e = cudaMemcpyAsync(db.data(), A->d_J, h->n_inst * sizeof(double), cudaMemcpyDeviceToHost, s)) ||
+      (e = cudaMemcpyAsync(bst.data(), A->d_bstate, h->n_inst * sizeof(PzState), cudaMemcpyDeviceToHost, s)))
+    return acuda(h, e, "pz_adjoint_backward");
+  if (dJ_dtemp &&
+      (e = cudaMemcpyAsync(dJ_dtemp, A->d_out, A->out_doubles * sizeof(double), cudaMemcpyDeviceToHost, s)))
+    return acuda(h, e, "pz_adjoint_backward");
+  if ((e = cudaStreamSynchronize(s))) return acuda(h, e, "pz_adjoint_backward");
+  for (int i = 0; i < h->n_inst; ++i)
+    if (bst[i].status != 0) return pz_fail(h, bst[i].status, "pz_adjoint_backward: operator rebuild failed");
+  int rc = pz_check_status(h);
+  if (rc) return rc;
+  if (dJ_dra)
+    for (int i = 0; i < h->n_inst; ++i) dJ_dra[i] = db[i] / h->hin[i].c.pr;   // dBuoFac/dRa = 1/Pr
+  return PZ_OK;
+}
+}  // namespace
 
 extern "C" int pz_adjoint_backward(pz_handle* h, double* dJ_dtemp, double* dJ_dra) {
   if (!h) return pz_fail(nullptr, PZ_E_ARG, "pz_adjoint_backward: null handle");
@@ -904,6 +1519,7 @@ extern "C" int pz_adjoint_backward(pz_handle* h, double* dJ_dtemp, double* dJ_dr
   k_adj_zero<<<h->dev.n_mitems, 64, 0, s>>>(a);
   if ((e = cudaGetLastError()) || (e = cudaMemsetAsync(A->d_bstate, 0, h->n_inst * sizeof(PzState), s)))
     return acuda(h, e, "adjoint init");
+  if (A->dirk) return dirk_backward(h, a, dR, dB, threads, smem, rsmem, dJ_dtemp, dJ_dra);
   if (!A->last_valid) {
     // snapshots and operators of the last segment were overwritten: recompute
     if ((e = launch_ckpt(a, A->n_seg - 1, 1, s))) return acuda(h, e, "restore");
