@@ -354,6 +354,91 @@ def adjoint_ratio(torch, reps=3, checkpoint_every=ADJ_CK, n_steps=ADJ_STEPS, n_w
             "J": float(J[0]), "dJ_dra": float(dra[0]), "distinct_dt": int(len(np.unique(dt)))}
 
 
+# dt: 5e-5 is unstable for ARS233 with the influence-matrix solve at E = 1e-4
+# (explicit Coriolis; the oracle's run of the same step blows up near step
+# 50), 1e-5 is the largest power-of-ten step stable for all 300 steps
+BADJ_STEPS, BADJ_CK, BADJ_DT = 300, 30, 1e-5
+
+
+def batched_adjoint_specs(n_inst=64, seed=4321):
+    """The batched adjoint ensemble: n_r_max in {49, 65}, n_phi_max in {126, 192}
+    (m_max 42 or 64: n_phi_max = 3 m_max, so 128 is taken as 126), Ra
+    log-uniform in [1e6, 1e7], E = 1e-4, Pr = 1, ARS233, influence matrix."""
+    rng = np.random.default_rng(seed)
+    specs = []
+    for i in range(n_inst):
+        n = int(rng.choice([49, 65]))
+        mm = int(rng.choice([42, 64]))
+        ra = float(10.0 ** rng.uniform(6.0, 7.0))
+        specs.append(dict(n_r_max=n, n_cheb_max=n, m_max=mm, ek=1e-4, ra=ra, pr=1.0, radratio=0.35,
+                          l_ek_pump=True, time_scheme="ARS233", dtMax=BADJ_DT, matrix_solve="INFLUENCE",
+                          seed=seed + i))
+    return specs
+
+
+def batched_adjoint_leg(torch, reps=2, n_fd=4, checkpoint_every=BADJ_CK, fd=True):
+    """Batched adjoint ensemble (64 instances, ARS233 with its assembly stage,
+    dt = 1e-5, 300 steps, checkpoint every 30): cost of every instance's
+    gradient of its time-averaged NuTop over the whole run with respect to
+    its initial temperature perturbation, over a plain forward run of the
+    same ensemble; and central finite differences of the forward sweep along
+    one seeded direction on n_fd instances, eps = 1e-4 relative to the
+    perturbation (J = mean NuTop is 1 + O(1e-2): below 1e-5 the difference
+    quotient is dominated by the rounding of J, above it agrees with the
+    adjoint to better than 1e-6)."""
+    import pizza_gb300 as pz
+    specs = batched_adjoint_specs()
+    temps = [seeded_temp(s) for s in specs]
+    ens = pz.Ensemble([gpu_cfg(s) for s in specs])
+    sched = np.full((len(specs), BADJ_STEPS), BADJ_DT)
+    fw, gr, sw, bw = [], [], [], []
+    for rep in range(reps + 1):
+        torch.cuda.synchronize()
+        a = time.perf_counter()
+        ens.set_state_all(temps)
+        ens.step(BADJ_STEPS)
+        b = time.perf_counter()
+        ens.set_state_all(temps)
+        J, dt = ens.adjoint_forward(BADJ_STEPS, BADJ_STEPS, checkpoint_every, sched, objective="nutop")
+        c = time.perf_counter()
+        g, _ = ens.adjoint_backward()
+        d = time.perf_counter()
+        if rep == 0:
+            continue
+        fw.append(b - a)
+        gr.append(d - b)
+        sw.append(c - b)
+        bw.append(d - c)
+    # finite differences on n_fd instances
+    rng = np.random.default_rng(77)
+    errs = []
+    for inst in range(n_fd if fd else 0):
+        d = rng.standard_normal(temps[inst].shape) + 1j * rng.standard_normal(temps[inst].shape)
+        d[0] = d[0].real
+        eps = 1e-4 * np.max(np.abs(temps[inst])) / np.max(np.abs(d))
+        jj = []
+        for sgn in (1.0, -1.0):
+            tp = list(temps)
+            tp[inst] = temps[inst] + sgn * eps * d
+            ens.set_state_all(tp)
+            Jp, _ = ens.adjoint_forward(BADJ_STEPS, BADJ_STEPS, checkpoint_every, sched, objective="nutop")
+            jj.append(Jp[inst])
+        fd = (jj[0] - jj[1]) / (2 * eps)
+        ad = float(np.sum((np.conj(g[inst]) * d).real))
+        errs.append(abs(fd - ad) / abs(fd))
+    ens.close()
+    med = lambda x: float(np.median(x))
+    return {"workload": f"batched adjoint ensemble: {len(specs)} instances, n_r_max in {{49,65}}, n_phi_max in "
+                        "{126,192}, Ra log-uniform [1e6,1e7], E=1e-4, ARS233 (assembly stage), dt=1e-5, "
+                        f"{BADJ_STEPS} steps, checkpoint every "
+                        f"{checkpoint_every if checkpoint_every > 0 else BADJ_STEPS}, J_i = mean NuTop over the run, "
+                        "gradient w.r.t. each instance's initial temperature perturbation",
+            "forward_ms": 1e3 * med(fw), "gradient_ms": 1e3 * med(gr), "sweep_ms": 1e3 * med(sw),
+            "backward_ms": 1e3 * med(bw), "adjoint_over_forward": med(gr) / med(fw),
+            "fd_instances": len(errs), "fd_eps_rel": 1e-4, "fd_max_rel_err": max(errs) if errs else None,
+            "fd_rel_errs": errs}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -371,6 +456,8 @@ def main():
     ap.add_argument("--adjoint-only", action="store_true", help="print only the adjoint/forward measurement")
     ap.add_argument("--adj-steps", type=int, default=ADJ_STEPS)
     ap.add_argument("--adj-reps", type=int, default=3)
+    ap.add_argument("--batched-adjoint-only", action="store_true",
+                    help="print only the batched DIRK adjoint measurement")
     args = ap.parse_args()
     args.warmup = max(3, args.warmup)
 
@@ -397,6 +484,12 @@ def main():
     if args.integ_only:
         if rank == 0:
             print(json.dumps({"integ": integ_leg(torch, args.integ_steps, args.warmup)}))
+        return
+
+    if args.batched_adjoint_only:
+        if rank == 0:
+            print(json.dumps({"batched_adjoint": batched_adjoint_leg(torch),
+                              "batched_adjoint_stored": batched_adjoint_leg(torch, checkpoint_every=0, fd=False)}))
         return
 
     if args.adjoint_only:
@@ -471,7 +564,9 @@ def main():
         return
     adj = None
     if not args.no_adjoint:
-        adj = {"checkpointed": adjoint_ratio(torch), "stored_trajectory": adjoint_ratio(torch, checkpoint_every=0)}
+        adj = {"checkpointed": adjoint_ratio(torch), "stored_trajectory": adjoint_ratio(torch, checkpoint_every=0),
+               "batched_dirk": batched_adjoint_leg(torch),
+               "batched_dirk_stored_trajectory": batched_adjoint_leg(torch, checkpoint_every=0, fd=False)}
     integ = None if args.no_integ else integ_leg(torch, args.integ_steps)
     cpu = None
     if not args.no_cpu:

@@ -508,7 +508,7 @@ __global__ void __launch_bounds__(256) k_adj_rloop(PzAdjDev a, int slot) {
 // L^T for step n: field adjoints of state n -> adjoint of S_n.  `terminal`
 // handles the final state (only the kinetic-energy source), `ke` adds the
 // source of the averaging window.
-__global__ void __launch_bounds__(256) k_adj_lin(PzAdjDev a, int n, int slot, int terminal, int src) {
+__global__ void __launch_bounds__(256, 3) k_adj_lin(PzAdjDev a, int n, int slot, int terminal, int src) {
   const PzItem it = a.d.mitems[blockIdx.x];
   const int inst = it.inst;
   const PzInst& I = a.d.inst[inst];
@@ -714,6 +714,8 @@ __device__ __forceinline__ void dadj_fin_pointwise(const PzInst& I, const View& 
   }
 }
 
+__device__ void dadj_fin_body(const PzAdjDev& a, const AdjView& A, const View& V, int mi, int k, int slot, AS& s);
+
 // lambda at the final state: the objective source (zero outside the window)
 __global__ void k_dadj_term(PzAdjDev a, int slot, int src) {
   const PzItem it = a.d.mitems[blockIdx.x];
@@ -736,7 +738,7 @@ __global__ void k_dadj_term(PzAdjDev a, int slot, int src) {
 // interior radii (robin_bc: zero on the walls), psi = G_ass w (interior rows
 // 2..N-3) and us, up, om from psi; for m = 0 u_phi = Re w at the interior
 // radii and om = du/dr + u/r.
-__global__ void __launch_bounds__(256) k_dadj_ass(PzAdjDev a, int n) {
+__global__ void __launch_bounds__(256) k_dadj_ass(PzAdjDev a, int n, int fin_k, int fin_slot) {
   const PzItem it = a.d.mitems[blockIdx.x];
   const int inst = it.inst;
   const PzInst& I = a.d.inst[inst];
@@ -754,6 +756,7 @@ __global__ void __launch_bounds__(256) k_dadj_ass(PzAdjDev a, int n) {
       for (int k = 0; k < ns; ++k)
         for (int f = 0; f < 2; ++f) { A.dE(k, f, mi)[i] = cz(); A.dI(ns, k, f, mi)[i] = cz(); }
     }
+    if (fin_k >= 0) dadj_fin_body(a, A, V, mi, fin_k, fin_slot, s);
     return;
   }
   const double* or1 = V.rad(RV_OR1);
@@ -811,23 +814,21 @@ __global__ void __launch_bounds__(256) k_dadj_ass(PzAdjDev a, int n) {
       A.dI(ns, k, 1, mi)[i] = cscale(wi, rp);
     }
   }
+  if (fin_k >= 0) dadj_fin_body(a, A, V, mi, fin_k, fin_slot, s);
 }
 
 // FIN^T, the D1p part, for the explicit term of stage state k (snapshot
 // `slot`): the inputs of k_adj_rloop (adjoints of E, dVsT, dVsOm), and the
-// explicit buoyancy's share of dJ/dBuoFac
-__global__ void __launch_bounds__(256) k_dadj_fin(PzAdjDev a, int k, int slot) {
-  const PzItem it = a.d.mitems[blockIdx.x];
-  const int inst = it.inst;
-  const PzInst& I = a.d.inst[inst];
-  const View V{&I, a.d.pool};
-  const AdjView A = adj_view(a, inst);
-  const int N = I.N, mi = it.idx, m = mi * I.minc;
+// explicit buoyancy's share of dJ/dBuoFac.  Runs in the block of (instance,
+// m) after the last contribution to E_k's adjoint (stages > k, assembly).
+__device__ void dadj_fin_body(const PzAdjDev& a, const AdjView& A, const View& V, int mi, int k, int slot, AS& s) {
+  const PzInst& I = *V.I;
+  const int N = I.N, m = mi * I.minc;
   const double dm = (double)m;
-  AS s = as_smem(N);
   const double* or1 = V.rad(RV_OR1);
   const double* rgrav = V.rad(RV_RGRAV);
   double2 *x = s.v[0], *y = s.v[1], *t = s.v[2];
+  __syncthreads();
   for (int i = threadIdx.x; i < N; i += blockDim.x) {
     const double2 et = A.dE(k, 0, mi)[i], ep = A.dE(k, 1, mi)[i];
     A.plane(AP_ETB, mi)[i] = et;
@@ -863,7 +864,8 @@ __global__ void __launch_bounds__(256) k_dadj_fin(PzAdjDev a, int k, int slot) {
 // solution (L^T, as k_adj_lin) -> SOLVE^T (as k_adj_solve) -> adjoint of
 // the right-hand side, added to old, E_k and I_k (k < s) with the stage's
 // Butcher weights.
-__global__ void __launch_bounds__(256, 2) k_dadj_stage(PzAdjDev a, int n, int st, int slot, int e_used) {
+__global__ void __launch_bounds__(256, 3) k_dadj_stage(PzAdjDev a, int n, int st, int slot, int e_used,
+                                                        int fin_prev) {
   const PzItem it = a.d.mitems[blockIdx.x];
   const int inst = it.inst;
   const PzInst& I = a.d.inst[inst];
@@ -1030,11 +1032,13 @@ __global__ void __launch_bounds__(256, 2) k_dadj_stage(PzAdjDev a, int n, int st
   }
   acc = block_sum(acc, s.red);
   if (threadIdx.x == 0) A.db()[mi] += acc;
+  // E_{st-1} is complete now (its consumers are the stages >= st and the assembly)
+  if (fin_prev) dadj_fin_body(a, A, V, mi, st - 1, slot - 1, s);
 }
 
 // z_0 = S_n (snapshot `slot`): lambda_n from old, I_0 (imp_from_physical,
 // D2p = D2c C), E_0 (FIN^T after k_adj_rloop) and the objective source
-__global__ void __launch_bounds__(256) k_dadj_z0(PzAdjDev a, int slot, int src) {
+__global__ void __launch_bounds__(256, 3) k_dadj_z0(PzAdjDev a, int slot, int src) {
   const PzItem it = a.d.mitems[blockIdx.x];
   const int inst = it.inst;
   const PzInst& I = a.d.inst[inst];
@@ -1239,31 +1243,31 @@ cudaError_t launch_ckpt(const PzAdjDev& a, int c, int dir, cudaStream_t s) {
   k_adj_ckpt<<<a.d.n_mitems, 64, 0, s>>>(a, c, dir);
   return cudaGetLastError();
 }
-// one forward step without the time series: k_rloop, k_cfl, k_build, k_mloop
-cudaError_t launch_fwd(const PzDev& d, cudaStream_t s) {
-  for (int k = 0; k < 4; ++k) {
-    const cudaError_t e = pz_launch_step_kernel(d, k, 1, s);
+// one forward step without the time series: the handle's step plan (the
+// kernels of pz_step, with the rebuild fused into the first stage where the
+// plan fuses it) without k_obs; for a DIRK scheme the stage states are saved
+// to snapshots base + 1 .. base + s1 - 1 after their stages (base >= 0)
+cudaError_t launch_fwd_plan(const pz_handle* h, const PzDev& d, const PzAdjDev& a, int base, cudaStream_t s) {
+  for (const PzLaunch& L : h->plan) {
+    if (L.kind == PZK_OBS) continue;
+    cudaError_t e = pz_launch_step_kernel(d, L.kind, L.stage, s);
     if (e) return e;
+    if (base >= 0 && (L.kind == PZK_MLOOP || L.kind == PZK_BUILD_MLOOP) && L.stage < a.s1 &&
+        (e = launch_snap(a, base + L.stage, s)))
+      return e;
   }
   return cudaSuccess;
 }
+cudaError_t launch_fwd(const pz_handle* h, const PzDev& d, const PzAdjDev& a, cudaStream_t s) {
+  return launch_fwd_plan(h, d, a, -1, s);
+}
 
-// one forward DIRK step without the time series (the stage loop of the plan:
-// per stage k_rloop, [k_cfl, k_build after stage 1], k_mloop, then
-// k_assemble), with the stage states saved to snapshots base .. base + s1 - 1
-// when base >= 0
-cudaError_t launch_fwd_dirk(const PzDev& d, const PzAdjDev& a, int base, cudaStream_t s) {
+// one forward DIRK step without the time series, with the stage states
+// saved to snapshots base .. base + s1 - 1 when base >= 0
+cudaError_t launch_fwd_dirk(const pz_handle* h, const PzDev& d, const PzAdjDev& a, int base, cudaStream_t s) {
   cudaError_t e;
   if (base >= 0 && (e = launch_snap(a, base, s))) return e;
-  for (int st = 1; st <= a.ns; ++st) {
-    if ((e = pz_launch_step_kernel(d, PZK_RLOOP, st, s))) return e;
-    if (st == 1 && ((e = pz_launch_step_kernel(d, PZK_CFL, 1, s)) || (e = pz_launch_step_kernel(d, PZK_BUILD, 1, s))))
-      return e;
-    if ((e = pz_launch_step_kernel(d, PZK_MLOOP, st, s))) return e;
-    if (base >= 0 && st < a.s1 && (e = launch_snap(a, base + st, s))) return e;
-  }
-  if (a.assembly && (e = pz_launch_step_kernel(d, PZK_ASSEMBLE, 0, s))) return e;
-  return cudaSuccess;
+  return launch_fwd_plan(h, d, a, base, s);
 }
 
 template <class T>
@@ -1388,10 +1392,10 @@ extern "C" int pz_adjoint_forward(pz_handle* h, int objective, int n_steps, int 
   for (int n = 0; n < n_steps; ++n) {
     if (n % A->K == 0 && (e = launch_ckpt(a, n / A->K, 0, s))) return acuda(h, e, "checkpoint");
     if (A->dirk) {
-      if ((e = launch_fwd_dirk(dF, a, n >= k0_last ? (n - k0_last) * A->s1 : -1, s))) return acuda(h, e, "forward step");
+      if ((e = launch_fwd_dirk(h, dF, a, n >= k0_last ? (n - k0_last) * A->s1 : -1, s))) return acuda(h, e, "forward step");
     } else {
       if (n >= k0_last && (e = launch_snap(a, n - k0_last, s))) return acuda(h, e, "snapshot");
-      if ((e = launch_fwd(dF, s))) return acuda(h, e, "forward step");
+      if ((e = launch_fwd(h, dF, a, s))) return acuda(h, e, "forward step");
     }
     if (n_window > 0 && n + 1 >= a.win0) {
       k_adj_ke<<<h->n_inst, PZ_THREADS, 0, s>>>(a);
@@ -1428,7 +1432,7 @@ int dirk_backward(pz_handle* h, const PzAdjDev& a, const PzDev& dR, const PzDev&
   if (!A->last_valid) {
     if ((e = launch_ckpt(a, A->n_seg - 1, 1, s))) return acuda(h, e, "restore");
     for (int n = k0_last; n < n_steps; ++n)
-      if ((e = launch_fwd_dirk(dR, a, (n - k0_last) * s1, s))) return acuda(h, e, "recompute");
+      if ((e = launch_fwd_dirk(h, dR, a, (n - k0_last) * s1, s))) return acuda(h, e, "recompute");
     if ((e = launch_snap(a, (n_steps - k0_last) * s1, s))) return acuda(h, e, "recompute");
   }
   k_dadj_term<<<mb, 64, 0, s>>>(a, (n_steps - k0_last) * s1, A->n_window > 0 ? 1 : 0);
@@ -1438,7 +1442,7 @@ int dirk_backward(pz_handle* h, const PzAdjDev& a, const PzDev& dR, const PzDev&
     if (sg != A->n_seg - 1) {
       if ((e = launch_ckpt(a, sg, 1, s))) return acuda(h, e, "restore");
       for (int n = k0; n < k1; ++n)
-        if ((e = launch_fwd_dirk(dR, a, (n - k0) * s1, s))) return acuda(h, e, "recompute");
+        if ((e = launch_fwd_dirk(h, dR, a, (n - k0) * s1, s))) return acuda(h, e, "recompute");
       if ((e = launch_snap(a, (k1 - k0) * s1, s))) return acuda(h, e, "recompute");
     }
     for (int n = k1 - 1; n >= k0; --n) {
@@ -1452,17 +1456,18 @@ int dirk_backward(pz_handle* h, const PzAdjDev& a, const PzDev& dR, const PzDev&
         k_adj_bstate<<<(h->n_inst + 63) / 64, 64, 0, s>>>(a, n);
         if ((e = cudaGetLastError()) || (e = pz_launch_step_kernel(dB, PZK_BUILD, 1, s))) return acuda(h, e, "rebuild");
       }
+      // E_k (k = 0..s1-2 are the explicit terms of the stage states; E_k
+      // is used when stage k+1 computes it) runs through FIN^T at the end of
+      // the kernel that completes its adjoint, then NL^T (k_adj_rloop)
       const int b = (n - k0) * s1;
-      k_dadj_ass<<<mb, threads, smem, s>>>(a, n);
-      for (int st = s1 - 1; st >= 1; --st) {
-        const int e_used = (st < A->ns && ((A->exp_mask >> st) & 1)) ? 1 : 0;
-        if (e_used) {
-          k_dadj_fin<<<mb, threads, smem, s>>>(a, st, b + st);
-          k_adj_rloop<<<h->dev.n_ritems, 256, rsmem, s>>>(a, b + st);
-        }
-        k_dadj_stage<<<mb, threads, smem, s>>>(a, n, st, b + st, e_used);
+      auto e_used = [&](int k) { return (k < A->ns && ((A->exp_mask >> k) & 1)) ? 1 : 0; };
+      const int top = s1 - 1;   // the last solved stage
+      k_dadj_ass<<<mb, threads, smem, s>>>(a, n, (A->assembly && e_used(top)) ? top : -1, b + top);
+      for (int st = top; st >= 1; --st) {
+        const int eu = (A->assembly || st < top) ? e_used(st) : 0;
+        if (eu) k_adj_rloop<<<h->dev.n_ritems, 256, rsmem, s>>>(a, b + st);
+        k_dadj_stage<<<mb, threads, smem, s>>>(a, n, st, b + st, eu, e_used(st - 1));
       }
-      k_dadj_fin<<<mb, threads, smem, s>>>(a, 0, b);
       k_adj_rloop<<<h->dev.n_ritems, 256, rsmem, s>>>(a, b);
       k_dadj_z0<<<mb, threads, smem, s>>>(a, b, n >= a.win0 ? 1 : 0);
       if ((e = cudaGetLastError())) return acuda(h, e, "adjoint step");
@@ -1524,7 +1529,7 @@ extern "C" int pz_adjoint_backward(pz_handle* h, double* dJ_dtemp, double* dJ_dr
     // snapshots and operators of the last segment were overwritten: recompute
     if ((e = launch_ckpt(a, A->n_seg - 1, 1, s))) return acuda(h, e, "restore");
     for (int n = k0_last; n < n_steps; ++n)
-      if ((e = launch_snap(a, n - k0_last, s)) || (e = launch_fwd(dR, s))) return acuda(h, e, "recompute");
+      if ((e = launch_snap(a, n - k0_last, s)) || (e = launch_fwd(h, dR, a, s))) return acuda(h, e, "recompute");
     if ((e = launch_snap(a, n_steps - k0_last, s))) return acuda(h, e, "recompute");
   }
   if (A->n_window > 0) {
@@ -1536,7 +1541,7 @@ extern "C" int pz_adjoint_backward(pz_handle* h, double* dJ_dtemp, double* dJ_dr
     if (sg != A->n_seg - 1) {
       if ((e = launch_ckpt(a, sg, 1, s))) return acuda(h, e, "restore");
       for (int n = k0; n < k1; ++n)
-        if ((e = launch_snap(a, n - k0, s)) || (e = launch_fwd(dR, s))) return acuda(h, e, "recompute");
+        if ((e = launch_snap(a, n - k0, s)) || (e = launch_fwd(h, dR, a, s))) return acuda(h, e, "recompute");
       if ((e = launch_snap(a, k1 - k0, s))) return acuda(h, e, "recompute");
     }
     for (int n = k1 - 1; n >= k0; --n) {
