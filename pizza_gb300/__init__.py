@@ -423,7 +423,7 @@ class Ensemble:
         return out, dra
 
     def latest_rows(self, out=None):
-        """Latest time-series row of every instance, shape (n_instances, 16)."""
+        """Latest time-series row of every instance, shape (n_instances, SERIES_COLS)."""
         if out is None:
             out = np.zeros((len(self), SERIES_COLS))
         self._check(self.lib.pz_latest_rows(self._h, _dptr(out)))
