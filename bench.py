@@ -376,7 +376,7 @@ def batched_adjoint_specs(n_inst=64, seed=4321):
     return specs
 
 
-def batched_adjoint_leg(torch, reps=2, n_fd=4, checkpoint_every=BADJ_CK, fd=True):
+def batched_adjoint_leg(torch, reps=2, n_fd=4, checkpoint_every=BADJ_CK, fd=True, n_steps=BADJ_STEPS):
     """Batched adjoint ensemble (64 instances, ARS233 with its assembly stage,
     dt = 1e-5, 300 steps, checkpoint every 30): cost of every instance's
     gradient of its time-averaged NuTop over the whole run with respect to
@@ -390,16 +390,16 @@ def batched_adjoint_leg(torch, reps=2, n_fd=4, checkpoint_every=BADJ_CK, fd=True
     specs = batched_adjoint_specs()
     temps = [seeded_temp(s) for s in specs]
     ens = pz.Ensemble([gpu_cfg(s) for s in specs])
-    sched = np.full((len(specs), BADJ_STEPS), BADJ_DT)
+    sched = np.full((len(specs), n_steps), BADJ_DT)
     fw, gr, sw, bw = [], [], [], []
     for rep in range(reps + 1):
         torch.cuda.synchronize()
         a = time.perf_counter()
         ens.set_state_all(temps)
-        ens.step(BADJ_STEPS)
+        ens.step(n_steps)
         b = time.perf_counter()
         ens.set_state_all(temps)
-        J, dt = ens.adjoint_forward(BADJ_STEPS, BADJ_STEPS, checkpoint_every, sched, objective="nutop")
+        J, dt = ens.adjoint_forward(n_steps, n_steps, checkpoint_every, sched, objective="nutop")
         c = time.perf_counter()
         g, _ = ens.adjoint_backward()
         d = time.perf_counter()
@@ -421,7 +421,7 @@ def batched_adjoint_leg(torch, reps=2, n_fd=4, checkpoint_every=BADJ_CK, fd=True
             tp = list(temps)
             tp[inst] = temps[inst] + sgn * eps * d
             ens.set_state_all(tp)
-            Jp, _ = ens.adjoint_forward(BADJ_STEPS, BADJ_STEPS, checkpoint_every, sched, objective="nutop")
+            Jp, _ = ens.adjoint_forward(n_steps, n_steps, checkpoint_every, sched, objective="nutop")
             jj.append(Jp[inst])
         fd = (jj[0] - jj[1]) / (2 * eps)
         ad = float(np.sum((np.conj(g[inst]) * d).real))
@@ -430,8 +430,8 @@ def batched_adjoint_leg(torch, reps=2, n_fd=4, checkpoint_every=BADJ_CK, fd=True
     med = lambda x: float(np.median(x))
     return {"workload": f"batched adjoint ensemble: {len(specs)} instances, n_r_max in {{49,65}}, n_phi_max in "
                         "{126,192}, Ra log-uniform [1e6,1e7], E=1e-4, ARS233 (assembly stage), dt=1e-5, "
-                        f"{BADJ_STEPS} steps, checkpoint every "
-                        f"{checkpoint_every if checkpoint_every > 0 else BADJ_STEPS}, J_i = mean NuTop over the run, "
+                        f"{n_steps} steps, checkpoint every "
+                        f"{checkpoint_every if checkpoint_every > 0 else n_steps}, J_i = mean NuTop over the run, "
                         "gradient w.r.t. each instance's initial temperature perturbation",
             "forward_ms": 1e3 * med(fw), "gradient_ms": 1e3 * med(gr), "sweep_ms": 1e3 * med(sw),
             "backward_ms": 1e3 * med(bw), "adjoint_over_forward": med(gr) / med(fw),
@@ -458,6 +458,10 @@ def main():
     ap.add_argument("--adj-reps", type=int, default=3)
     ap.add_argument("--batched-adjoint-only", action="store_true",
                     help="print only the batched DIRK adjoint measurement")
+    ap.add_argument("--badj-steps", type=int, default=BADJ_STEPS)
+    ap.add_argument("--badj-ck", type=int, default=BADJ_CK)
+    ap.add_argument("--badj-reps", type=int, default=2)
+    ap.add_argument("--badj-fd", type=int, default=4)
     args = ap.parse_args()
     args.warmup = max(3, args.warmup)
 
@@ -488,8 +492,11 @@ def main():
 
     if args.batched_adjoint_only:
         if rank == 0:
-            print(json.dumps({"batched_adjoint": batched_adjoint_leg(torch),
-                              "batched_adjoint_stored": batched_adjoint_leg(torch, checkpoint_every=0, fd=False)}))
+            out = {"batched_adjoint": batched_adjoint_leg(torch, args.badj_reps, args.badj_fd, args.badj_ck,
+                                                          args.badj_fd > 0, args.badj_steps)}
+            if args.badj_steps == BADJ_STEPS:
+                out["batched_adjoint_stored"] = batched_adjoint_leg(torch, checkpoint_every=0, fd=False)
+            print(json.dumps(out))
         return
 
     if args.adjoint_only:

@@ -260,7 +260,7 @@ __global__ void k_adj_bstate(PzAdjDev a, int n) {
 }
 
 // SOLVE^T and the local part of FIN^T for step n (snapshot `slot` = state n)
-__global__ void __launch_bounds__(256, 3) k_adj_solve(PzAdjDev a, int n, int slot) {
+__global__ void __launch_bounds__(256, 4) k_adj_solve(PzAdjDev a, int n, int slot) {
   const PzItem it = a.d.mitems[blockIdx.x];
   const int inst = it.inst;
   const PzInst& I = a.d.inst[inst];
@@ -864,7 +864,7 @@ __device__ void dadj_fin_body(const PzAdjDev& a, const AdjView& A, const View& V
 // solution (L^T, as k_adj_lin) -> SOLVE^T (as k_adj_solve) -> adjoint of
 // the right-hand side, added to old, E_k and I_k (k < s) with the stage's
 // Butcher weights.
-__global__ void __launch_bounds__(256, 3) k_dadj_stage(PzAdjDev a, int n, int st, int slot, int e_used,
+__global__ void __launch_bounds__(256, 4) k_dadj_stage(PzAdjDev a, int n, int st, int slot, int e_used,
                                                         int fin_prev) {
   const PzItem it = a.d.mitems[blockIdx.x];
   const int inst = it.inst;

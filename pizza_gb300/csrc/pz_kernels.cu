@@ -1357,7 +1357,7 @@ __device__ __forceinline__ void mloop_item(const PzDev& d, const PzItem it, int 
   if (__syncthreads_or(bad)) flag_status(Sg, PZ_E_NONFINITE);
 }
 
-__global__ void __launch_bounds__(256, 3) k_mloop(PzDev d, int stage) { mloop_item<true>(d, d.mitems[blockIdx.x], stage); }
+__global__ void __launch_bounds__(256, 4) k_mloop(PzDev d, int stage) { mloop_item<true>(d, d.mitems[blockIdx.x], stage); }
 
 // ---------------------------------------------------------------------------
 // k_order + k_build_mloop: the operator rebuild fused with the first stage.
@@ -1413,7 +1413,7 @@ __global__ void __launch_bounds__(1024) k_order(PzDev d) {
 }
 
 template <bool CHEM>
-__global__ void __launch_bounds__(256, 3) k_build_mloop(PzDev d) {
+__global__ void __launch_bounds__(256, 4) k_build_mloop(PzDev d) {
   const PzItem it = d.order[blockIdx.x];
   if (d.inst[it.inst].flags & PZF_INTEG) return;
   build_item<CHEM>(d, it);
