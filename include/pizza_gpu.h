@@ -277,7 +277,8 @@ int pz_explicit_terms_noalloc(pz_handle* h, int inst, const double* us, const do
  *       (us2_3D + up2_3D + uz2_3D)(k)          (e_kin_3D, outputs.f90:553-570)
  * and the gradient is taken with respect to the initial temperature
  * perturbation (the temp argument of pz_set_state) and Ra, for a fixed
- * time-step sequence.  Only CNAB2 with the influence-matrix solve is covered.
+ * time-step sequence.  The collocation step with the influence-matrix solve
+ * is covered, with CNAB2 or a DIRK scheme (one scheme for all instances).
  *
  * The objective is selected per sweep: PZ_OBJ_EKIN3D (above) or
  * PZ_OBJ_NUTOP, the mean of NuTop = 1 + dT/dr(m=0, r_cmb)/dtcond(r_cmb).
@@ -302,6 +303,14 @@ int pz_adjoint_forward(pz_handle* h, int objective, int n_steps, int n_window, i
  * state of the forward sweep.  Any pz_step, pz_set_state* or pz_set_ra call
  * in between discards the stored sweep. */
 int pz_adjoint_backward(pz_handle* h, double* dJ_dtemp, double* dJ_dra);
+
+/* pz_adjoint_grid_snapshots: keep (enable != 0, the default) or drop the
+ * phi-grids of the stored stage states.  Kept, they cost 32*n_r_max*n_phi_max
+ * bytes per stored state and the backward sweep skips their inverse
+ * transforms; a sweep whose grid buffer cannot be allocated runs without them.
+ * Enabling takes effect at the next pz_adjoint_forward; disabling frees the
+ * grids at once.  The gradient is the same either way. */
+int pz_adjoint_grid_snapshots(pz_handle* h, int enable);
 
 /* Change Ra of one instance (BuoFac = Ra/Pr); the operators do not depend on
  * it.  Used for finite-difference checks of dJ/dRa. */

@@ -180,6 +180,7 @@ def load_library(path: str | None = None):
     lib.pz_adjoint_forward.argtypes = [vp, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, dp, dp, dp]
     lib.pz_adjoint_backward.argtypes = [vp, dp, dp]
     lib.pz_set_ra.argtypes = [vp, ctypes.c_int, ctypes.c_double]
+    lib.pz_adjoint_grid_snapshots.argtypes = [vp, ctypes.c_int]
     lib.pz_get_history.argtypes = [vp, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, dp]
     lib.pz_set_history.argtypes = [vp, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, dp]
     lib.pz_get_step_state.argtypes = [vp, ctypes.c_int, dp, dp, ctypes.POINTER(ctypes.c_int)]
@@ -194,7 +195,7 @@ def load_library(path: str | None = None):
               "pz_sync", "pz_get_state",
               "pz_get_series", "pz_get_dims", "pz_launches_per_step", "pz_latest_rows",
               "pz_step_profile", "pz_explicit_terms", "pz_explicit_terms_noalloc", "pz_adjoint_forward",
-              "pz_adjoint_backward", "pz_set_ra", "pz_get_history", "pz_set_history", "pz_get_step_state",
+              "pz_adjoint_backward", "pz_adjoint_grid_snapshots", "pz_set_ra", "pz_get_history", "pz_set_history", "pz_get_step_state",
               "pz_set_step_state", "pz_set_restart_ab1", "pz_get_spectra", "pz_integ_operator",
               "pz_destroy"):
         getattr(lib, f).restype = ctypes.c_int
@@ -407,6 +408,12 @@ class Ensemble:
         self._check(self.lib.pz_adjoint_forward(self._h, obj, int(n_steps), int(n_window), int(checkpoint_every),
                                                 _dptr(sched), _dptr(J), _dptr(dt_used)))
         return J, dt_used
+
+    def adjoint_grid_snapshots(self, enable=True):
+        """Keep (default) or drop the phi-grids of the stored stage states
+        (32 n_r_max n_phi_max bytes each); kept, the backward sweep skips
+        their inverse transforms (pz_adjoint_grid_snapshots)."""
+        self._check(self.lib.pz_adjoint_grid_snapshots(self._h, int(bool(enable))))
 
     def adjoint_backward(self):
         """Gradient of the last forward sweep's objective: a list of

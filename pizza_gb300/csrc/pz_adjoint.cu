@@ -84,6 +84,11 @@ struct PzAdjDev {
   // DIRK sweep (one tableau for all instances): stages, solved stages + 1
   // (stage states per step), assembly stage, l_exp_calc / l_imp_calc_rhs bits
   int dirk, ns, s1, assembly, exp_mask, imp_mask;
+  // grid snapshots (null: k_adj_rloop transforms the spectral snapshots):
+  // slot k of instance i at gs + o_gs[i] + k * N * 2P, written by the
+  // forward k_rloop that transforms stage state k
+  double2* gs;
+  const long long* o_gs;
 };
 
 struct AdjView {
@@ -137,8 +142,8 @@ int adj_threads(int maxN) {
 }
 // G radii per block: the forward's k_rloop grouping (PzInst::rg), since both
 // walk the same (instance, radius) work list
-size_t adj_rloop_smem_bytes(int P, int G) {
-  return 6 * (size_t)G * P * sizeof(double2) + G * sizeof(double);
+size_t adj_rloop_smem_bytes(int P, int G, bool grid) {
+  return (grid ? 4 : 6) * (size_t)G * P * sizeof(double2) + G * sizeof(double);
 }
 
 __device__ __forceinline__ double2 cz() { return make_double2(0.0, 0.0); }
@@ -393,7 +398,10 @@ __global__ void __launch_bounds__(256, 4) k_adj_solve(PzAdjDev a, int n, int slo
 // with fft = rfft/P truncated to M and the grids from c2r of the spectra.
 // The adjoint of fft is a c2r of the spectrum scaled by 1/(2P) (1/P and the
 // real part at m = 0); the adjoint of the c2r is an r2c scaled by 2 (1 and
-// the real part at m = 0).  Shared memory: three buffers of 2*G transforms.
+// the real part at m = 0).  The state's grids are the forward k_rloop's
+// (GRID: read from the grid snapshot) or a c2r of the spectral snapshot.
+// Shared memory: three buffers of 2*G transforms, two with GRID.
+template <bool GRID>
 __global__ void __launch_bounds__(256) k_adj_rloop(PzAdjDev a, int slot) {
   extern __shared__ double2 sh[];
   const PzItem it = a.d.ritems[blockIdx.x];
@@ -404,20 +412,34 @@ __global__ void __launch_bounds__(256) k_adj_rloop(PzAdjDev a, int slot) {
   const int N = I.N, M = I.M, P = I.P;
   const int G = min(I.rg, N - r0);
   const double2* tw = reinterpret_cast<const double2*>(V.pool + I.o_tw);
-  double2* b0 = sh;
-  double2* b1 = sh + 2 * G * P;
-  double2* b2 = sh + 4 * G * P;
-  double* ep0 = reinterpret_cast<double*>(sh + 6 * G * P);
-  for (int k = threadIdx.x; k < 2 * G * P; k += blockDim.x) { b0[k] = cz(); b2[k] = cz(); }
+  double2* b0 = sh;                                // state spectra (without GRID)
+  double2* b1 = GRID ? sh : sh + 2 * G * P;
+  double2* b2 = b1 + 2 * G * P;                    // spectra of the adjoint products
+  double* ep0 = reinterpret_cast<double*>(b2 + 2 * G * P);
+  for (int k = threadIdx.x; k < 2 * G * P; k += blockDim.x) {
+    if (!GRID) b0[k] = cz();
+    b2[k] = cz();
+  }
   __syncthreads();
   const double inv2P = 0.5 / (double)P, invP = 1.0 / (double)P;
   for (int t = threadIdx.x; t < G * M; t += blockDim.x) {
     const int g = t / M, mi = t - g * M, r = r0 + g;
     const double dm = (double)(mi * I.minc);
     const long long o = (long long)mi * N + r;
-    // grids of the state (as k_rloop)
-    double2 us = A.snap(slot, SN_US, 0)[o], up = A.snap(slot, SN_UP, 0)[o];
-    double2 om = A.snap(slot, SN_OM, 0)[o], T = A.snap(slot, SN_T, 0)[o];
+    if (!GRID) {
+      // grids of the state (as k_rloop)
+      double2 us = A.snap(slot, SN_US, 0)[o], up = A.snap(slot, SN_UP, 0)[o];
+      double2 om = A.snap(slot, SN_OM, 0)[o], T = A.snap(slot, SN_T, 0)[o];
+      if (mi == 0) { us.y = 0.0; up.y = 0.0; om.y = 0.0; T.y = 0.0; }
+      double2* z1 = b0 + (2 * g) * P;
+      double2* z2 = b0 + (2 * g + 1) * P;
+      z1[mi] = make_double2(us.x - up.y, us.y + up.x);
+      z2[mi] = make_double2(om.x - T.y, om.y + T.x);
+      if (mi > 0) {
+        z1[P - mi] = make_double2(us.x + up.y, -us.y + up.x);
+        z2[P - mi] = make_double2(om.x + T.y, -om.y + T.x);
+      }
+    }
     // spectra of the adjoint products
     const double or1 = V.rad(RV_OR1)[r];
     const double tfac = (1.0 - I.tadvz) * V.rad(RV_BETA)[r] * or1;
@@ -427,33 +449,35 @@ __global__ void __launch_bounds__(256) k_adj_rloop(PzAdjDev a, int slot) {
     double2 hC = A.plane(AP_VOB, 0)[o];
     double2 hD = (mi == 0) ? cz() : cscale(or1, cim(dm, ep));
     if (mi == 0) {
-      us.y = 0.0; up.y = 0.0; om.y = 0.0; T.y = 0.0;
       hA = make_double2(hA.x * invP, 0.0); hB = make_double2(hB.x * invP, 0.0);
       hC = make_double2(hC.x * invP, 0.0); hD = cz();
       ep0[g] = ep.x;
     } else {
       hA = cscale(inv2P, hA); hB = cscale(inv2P, hB); hC = cscale(inv2P, hC); hD = cscale(inv2P, hD);
     }
-    double2* z1 = b0 + (2 * g) * P;
-    double2* z2 = b0 + (2 * g + 1) * P;
     double2* z3 = b2 + (2 * g) * P;
     double2* z4 = b2 + (2 * g + 1) * P;
-    z1[mi] = make_double2(us.x - up.y, us.y + up.x);
-    z2[mi] = make_double2(om.x - T.y, om.y + T.x);
     z3[mi] = make_double2(hA.x - hB.y, hA.y + hB.x);
     z4[mi] = make_double2(hC.x - hD.y, hC.y + hD.x);
     if (mi > 0) {
-      z1[P - mi] = make_double2(us.x + up.y, -us.y + up.x);
-      z2[P - mi] = make_double2(om.x + T.y, -om.y + T.x);
       z3[P - mi] = make_double2(hA.x + hB.y, -hA.y + hB.x);
       z4[P - mi] = make_double2(hC.x + hD.y, -hC.y + hD.x);
     }
   }
   __syncthreads();
-  double2* X = fft_run(b0, b1, I, tw, 2 * G, true);
-  double2* fr = (X == b0) ? b1 : b0;
-  double2* Y = fft_run(b2, fr, I, tw, 2 * G, true);
-  double2* W = (Y == b2) ? fr : b2;
+  const double2* X;
+  double2 *Y, *W;
+  if (GRID) {
+    X = a.gs + a.o_gs[inst] + ((long long)slot * N + r0) * 2 * P;
+    Y = fft_run(b2, b1, I, tw, 2 * G, true);
+    W = (Y == b2) ? b1 : b2;
+  } else {
+    double2* Xs = fft_run(b0, b1, I, tw, 2 * G, true);
+    double2* fr = (Xs == b0) ? b1 : b0;
+    Y = fft_run(b2, fr, I, tw, 2 * G, true);
+    W = (Y == b2) ? fr : b2;
+    X = Xs;
+  }
   // product rule on the grid
   for (int t = threadIdx.x; t < G * P; t += blockDim.x) {
     const int g = t / P, j = t - g * P;
@@ -1182,7 +1206,12 @@ struct PzAdjoint {
   double* d_dt = nullptr;
   double* d_J = nullptr;
   double* d_out = nullptr;
+  double2* gs = nullptr;     // grid snapshots (PzAdjDev::gs)
+  long long* d_ogs = nullptr;
+  bool grids = false;        // the current sweep keeps grid snapshots
   size_t cap_ws = 0, cap_out = 0, cap_ows = 0, cap_oout = 0, cap_rec = 0, cap_ck = 0, cap_b = 0, cap_dt = 0, cap_J = 0;
+  size_t cap_gs = 0, cap_ogs = 0;
+  size_t rsmem = 0, rsmem_g = 0;   // dynamic shared memory of k_adj_rloop without / with grids
   size_t out_doubles = 0;    // gradient output of the current layout
   std::vector<PzState> h_rec;
 };
@@ -1192,6 +1221,7 @@ void pz_adjoint_free(pz_handle* h) {
   PzAdjoint* A = h->adj;
   cudaFree(A->ws); cudaFree(A->d_ows); cudaFree(A->d_oout); cudaFree(A->d_rec); cudaFree(A->d_ck);
   cudaFree(A->d_bstate); cudaFree(A->d_dt); cudaFree(A->d_J); cudaFree(A->d_out);
+  cudaFree(A->gs); cudaFree(A->d_ogs);
   delete A;
   h->adj = nullptr;
 }
@@ -1232,6 +1262,8 @@ PzAdjDev adj_dev(pz_handle* h) {
   a.assembly = A->assembly;
   a.exp_mask = A->exp_mask;
   a.imp_mask = A->imp_mask;
+  a.gs = A->grids ? A->gs : nullptr;
+  a.o_gs = A->grids ? A->d_ogs : nullptr;
   return a;
 }
 
@@ -1246,11 +1278,23 @@ cudaError_t launch_ckpt(const PzAdjDev& a, int c, int dir, cudaStream_t s) {
 // one forward step without the time series: the handle's step plan (the
 // kernels of pz_step, with the rebuild fused into the first stage where the
 // plan fuses it) without k_obs; for a DIRK scheme the stage states are saved
-// to snapshots base + 1 .. base + s1 - 1 after their stages (base >= 0)
-cudaError_t launch_fwd_plan(const pz_handle* h, const PzDev& d, const PzAdjDev& a, int base, cudaStream_t s) {
+// to snapshots base + 1 .. base + s1 - 1 after their stages (base >= 0).
+// With grid snapshots (a.gs) and gbase >= 0, k_rloop of stage s stores the
+// grids of the state it transforms at grid slot gbase + s - 1.
+cudaError_t launch_fwd_plan(const pz_handle* h, const PzDev& d, const PzAdjDev& a, int base, int gbase,
+                            cudaStream_t s) {
   for (const PzLaunch& L : h->plan) {
     if (L.kind == PZK_OBS) continue;
-    cudaError_t e = pz_launch_step_kernel(d, L.kind, L.stage, s);
+    cudaError_t e;
+    if (L.kind == PZK_RLOOP && gbase >= 0 && a.gs) {
+      PzDev dg = d;
+      dg.gsnap = a.gs;
+      dg.o_gsnap = a.o_gs;
+      dg.gsnap_slot0 = gbase;
+      e = pz_launch_step_kernel(dg, L.kind, L.stage, s);
+    } else {
+      e = pz_launch_step_kernel(d, L.kind, L.stage, s);
+    }
     if (e) return e;
     if (base >= 0 && (L.kind == PZK_MLOOP || L.kind == PZK_BUILD_MLOOP) && L.stage < a.s1 &&
         (e = launch_snap(a, base + L.stage, s)))
@@ -1258,8 +1302,9 @@ cudaError_t launch_fwd_plan(const pz_handle* h, const PzDev& d, const PzAdjDev& 
   }
   return cudaSuccess;
 }
-cudaError_t launch_fwd(const pz_handle* h, const PzDev& d, const PzAdjDev& a, cudaStream_t s) {
-  return launch_fwd_plan(h, d, a, -1, s);
+// a CNAB2 step; its state's grids go to grid slot gslot (>= 0)
+cudaError_t launch_fwd(const pz_handle* h, const PzDev& d, const PzAdjDev& a, int gslot, cudaStream_t s) {
+  return launch_fwd_plan(h, d, a, -1, gslot, s);
 }
 
 // one forward DIRK step without the time series, with the stage states
@@ -1267,7 +1312,16 @@ cudaError_t launch_fwd(const pz_handle* h, const PzDev& d, const PzAdjDev& a, cu
 cudaError_t launch_fwd_dirk(const pz_handle* h, const PzDev& d, const PzAdjDev& a, int base, cudaStream_t s) {
   cudaError_t e;
   if (base >= 0 && (e = launch_snap(a, base, s))) return e;
-  return launch_fwd_plan(h, d, a, base, s);
+  return launch_fwd_plan(h, d, a, base, base, s);
+}
+
+// NL^T of snapshot `slot`; `grid`: the forward stored the slot's grids
+cudaError_t launch_adj_rloop(const pz_handle* h, const PzAdjDev& a, int slot, bool grid, cudaStream_t s) {
+  if (grid && a.gs)
+    k_adj_rloop<true><<<h->dev.n_ritems, 256, h->adj->rsmem_g, s>>>(a, slot);
+  else
+    k_adj_rloop<false><<<h->dev.n_ritems, 256, h->adj->rsmem, s>>>(a, slot);
+  return cudaGetLastError();
 }
 
 template <class T>
@@ -1282,6 +1336,19 @@ cudaError_t grow(T** p, size_t* cap, size_t n) {
 }
 
 }  // namespace
+
+extern "C" int pz_adjoint_grid_snapshots(pz_handle* h, int enable) {
+  if (!h) return pz_fail(nullptr, PZ_E_ARG, "pz_adjoint_grid_snapshots: null handle");
+  h->adj_grids = enable ? 1 : 0;
+  if (!enable && h->adj) {
+    PzAdjoint* A = h->adj;
+    cudaFree(A->gs);
+    A->gs = nullptr;
+    A->cap_gs = 0;
+    A->grids = false;   // a stored sweep's backward transforms its spectral snapshots
+  }
+  return PZ_OK;
+}
 
 extern "C" int pz_set_ra(pz_handle* h, int inst, double ra) {
   if (!h) return pz_fail(nullptr, PZ_E_ARG, "pz_set_ra: null handle");
@@ -1315,7 +1382,7 @@ extern "C" int pz_adjoint_forward(pz_handle* h, int objective, int n_steps, int 
                      "(CNAB2 or a DIRK scheme), without composition");
     if (I.scheme != h->inst[0].scheme)
       return pz_fail(h, PZ_E_UNSUPPORTED, "pz_adjoint_forward: all instances must use the same time scheme");
-    if (adj_rloop_smem_bytes(I.P, I.rg) > PZ_SMEM_MAX)
+    if (adj_rloop_smem_bytes(I.P, I.rg, false) > PZ_SMEM_MAX)
       return pz_fail(h, PZ_E_UNSUPPORTED, "pz_adjoint_forward: n_phi_max too large for the adjoint transform kernel");
   }
   cudaError_t e;
@@ -1374,6 +1441,28 @@ extern "C" int pz_adjoint_forward(pz_handle* h, int objective, int n_steps, int 
   }
   A->out_doubles = (size_t)tout;
   cudaStream_t s = h->stream;
+  // grid snapshots: n_snap slots of N x 2P values per instance; a sweep whose
+  // grid buffer does not fit runs without them
+  A->grids = false;
+  if (h->adj_grids) {
+    std::vector<long long> ogs(h->n_inst);
+    long long tg = 0;
+    for (int i = 0; i < h->n_inst; ++i) {
+      ogs[i] = tg;
+      tg += (long long)A->n_snap * h->inst[i].N * 2 * h->inst[i].P;
+    }
+    cudaError_t eg = grow(&A->gs, &A->cap_gs, (size_t)tg);
+    if (!eg) eg = grow(&A->d_ogs, &A->cap_ogs, (size_t)h->n_inst);
+    if (eg == cudaErrorMemoryAllocation) {
+      cudaGetLastError();
+    } else if (eg) {
+      return acuda(h, eg, "pz_adjoint_forward");
+    } else {
+      if ((e = cudaMemcpyAsync(A->d_ogs, ogs.data(), ogs.size() * sizeof(long long), cudaMemcpyHostToDevice, s)))
+        return acuda(h, e, "pz_adjoint_forward");
+      A->grids = true;
+    }
+  }
   if ((e = cudaMemcpyAsync(A->d_ows, ows.data(), ows.size() * sizeof(long long), cudaMemcpyHostToDevice, s)) ||
       (e = cudaMemcpyAsync(A->d_oout, oout.data(), oout.size() * sizeof(long long), cudaMemcpyHostToDevice, s)) ||
       (e = cudaMemsetAsync(A->d_J, 0, h->n_inst * sizeof(double), s)))
@@ -1395,7 +1484,7 @@ extern "C" int pz_adjoint_forward(pz_handle* h, int objective, int n_steps, int 
       if ((e = launch_fwd_dirk(h, dF, a, n >= k0_last ? (n - k0_last) * A->s1 : -1, s))) return acuda(h, e, "forward step");
     } else {
       if (n >= k0_last && (e = launch_snap(a, n - k0_last, s))) return acuda(h, e, "snapshot");
-      if ((e = launch_fwd(h, dF, a, s))) return acuda(h, e, "forward step");
+      if ((e = launch_fwd(h, dF, a, n >= k0_last ? n - k0_last : -1, s))) return acuda(h, e, "forward step");
     }
     if (n_window > 0 && n + 1 >= a.win0) {
       k_adj_ke<<<h->n_inst, PZ_THREADS, 0, s>>>(a);
@@ -1422,7 +1511,7 @@ extern "C" int pz_adjoint_forward(pz_handle* h, int objective, int n_steps, int 
 namespace {
 // the backward sweep of a DIRK scheme (see the DIRK kernels above)
 int dirk_backward(pz_handle* h, const PzAdjDev& a, const PzDev& dR, const PzDev& dB, int threads, size_t smem,
-                  size_t rsmem, double* dJ_dtemp, double* dJ_dra) {
+                  double* dJ_dtemp, double* dJ_dra) {
   PzAdjoint* A = h->adj;
   cudaStream_t s = h->stream;
   cudaError_t e;
@@ -1465,10 +1554,12 @@ int dirk_backward(pz_handle* h, const PzAdjDev& a, const PzDev& dR, const PzDev&
       k_dadj_ass<<<mb, threads, smem, s>>>(a, n, (A->assembly && e_used(top)) ? top : -1, b + top);
       for (int st = top; st >= 1; --st) {
         const int eu = (A->assembly || st < top) ? e_used(st) : 0;
-        if (eu) k_adj_rloop<<<h->dev.n_ritems, 256, rsmem, s>>>(a, b + st);
+        // the grids of stage state st come from k_rloop of stage st + 1,
+        // which runs when E_st is used
+        if (eu && (e = launch_adj_rloop(h, a, b + st, true, s))) return acuda(h, e, "adjoint step");
         k_dadj_stage<<<mb, threads, smem, s>>>(a, n, st, b + st, eu, e_used(st - 1));
       }
-      k_adj_rloop<<<h->dev.n_ritems, 256, rsmem, s>>>(a, b);
+      if ((e = launch_adj_rloop(h, a, b, e_used(0) != 0, s))) return acuda(h, e, "adjoint step");
       k_dadj_z0<<<mb, threads, smem, s>>>(a, b, n >= a.win0 ? 1 : 0);
       if ((e = cudaGetLastError())) return acuda(h, e, "adjoint step");
     }
@@ -1516,20 +1607,24 @@ extern "C" int pz_adjoint_backward(pz_handle* h, double* dJ_dtemp, double* dJ_dr
   const int k0_last = (A->n_seg - 1) * K;
   const int threads = adj_threads(h->dev.maxN);
   const size_t smem = as_smem_bytes(h->dev.maxN);
-  size_t rsmem = 0;
-  for (int i = 0; i < h->n_inst; ++i)
-    rsmem = std::max(rsmem, adj_rloop_smem_bytes(h->inst[i].P, h->inst[i].rg));
-  if ((e = cudaFuncSetAttribute(k_adj_rloop, cudaFuncAttributeMaxDynamicSharedMemorySize, PZ_SMEM_MAX)))
+  A->rsmem = A->rsmem_g = 0;
+  for (int i = 0; i < h->n_inst; ++i) {
+    A->rsmem = std::max(A->rsmem, adj_rloop_smem_bytes(h->inst[i].P, h->inst[i].rg, false));
+    A->rsmem_g = std::max(A->rsmem_g, adj_rloop_smem_bytes(h->inst[i].P, h->inst[i].rg, true));
+  }
+  if ((e = cudaFuncSetAttribute(k_adj_rloop<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, PZ_SMEM_MAX)) ||
+      (e = cudaFuncSetAttribute(k_adj_rloop<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, PZ_SMEM_MAX)))
     return acuda(h, e, "pz_adjoint_backward");
   k_adj_zero<<<h->dev.n_mitems, 64, 0, s>>>(a);
   if ((e = cudaGetLastError()) || (e = cudaMemsetAsync(A->d_bstate, 0, h->n_inst * sizeof(PzState), s)))
     return acuda(h, e, "adjoint init");
-  if (A->dirk) return dirk_backward(h, a, dR, dB, threads, smem, rsmem, dJ_dtemp, dJ_dra);
+  if (A->dirk) return dirk_backward(h, a, dR, dB, threads, smem, dJ_dtemp, dJ_dra);
   if (!A->last_valid) {
     // snapshots and operators of the last segment were overwritten: recompute
     if ((e = launch_ckpt(a, A->n_seg - 1, 1, s))) return acuda(h, e, "restore");
     for (int n = k0_last; n < n_steps; ++n)
-      if ((e = launch_snap(a, n - k0_last, s)) || (e = launch_fwd(h, dR, a, s))) return acuda(h, e, "recompute");
+      if ((e = launch_snap(a, n - k0_last, s)) || (e = launch_fwd(h, dR, a, n - k0_last, s)))
+        return acuda(h, e, "recompute");
     if ((e = launch_snap(a, n_steps - k0_last, s))) return acuda(h, e, "recompute");
   }
   if (A->n_window > 0) {
@@ -1541,7 +1636,7 @@ extern "C" int pz_adjoint_backward(pz_handle* h, double* dJ_dtemp, double* dJ_dr
     if (sg != A->n_seg - 1) {
       if ((e = launch_ckpt(a, sg, 1, s))) return acuda(h, e, "restore");
       for (int n = k0; n < k1; ++n)
-        if ((e = launch_snap(a, n - k0, s)) || (e = launch_fwd(h, dR, a, s))) return acuda(h, e, "recompute");
+        if ((e = launch_snap(a, n - k0, s)) || (e = launch_fwd(h, dR, a, n - k0, s))) return acuda(h, e, "recompute");
       if ((e = launch_snap(a, k1 - k0, s))) return acuda(h, e, "recompute");
     }
     for (int n = k1 - 1; n >= k0; --n) {
@@ -1557,7 +1652,7 @@ extern "C" int pz_adjoint_backward(pz_handle* h, double* dJ_dtemp, double* dJ_dr
       }
       const int slot = n - k0;
       k_adj_solve<<<h->dev.n_mitems, threads, smem, s>>>(a, n, slot);
-      k_adj_rloop<<<h->dev.n_ritems, 256, rsmem, s>>>(a, slot);
+      if ((e = launch_adj_rloop(h, a, slot, true, s))) return acuda(h, e, "adjoint step");
       k_adj_lin<<<h->dev.n_mitems, threads, smem, s>>>(a, n, slot, 0, n >= a.win0 ? 1 : 0);
       if ((e = cudaGetLastError())) return acuda(h, e, "adjoint step");
     }

@@ -292,6 +292,7 @@ __device__ void rloop_group(const PzInst& I, const View& V, int r0, int gmax, IO
   }
   double2* g1 = fft_run(za, zb, I, tw, nt * G, true);
   double2* h = (g1 == za) ? zb : za;
+  io.grid(g1, r0 * nt * P, nt * G * P);   // read-only use of g1, like the loop below
   // Courant velocities and the nonlinear products on the grid
   for (int t = threadIdx.x; t < G * P; t += blockDim.x) {
     const int g = t / P, j = t - g * P;

@@ -37,6 +37,7 @@ struct pz_handle {
   int* d_obs_cnt = nullptr;
   std::string err = "no error";
   PzAdjoint* adj = nullptr;   // allocated by the first adjoint call
+  int adj_grids = 1;           // adjoint sweeps keep the phi-grids of the stage states
   std::vector<PzLaunch> plan;  // kernel launches of one step, in order
 };
 

@@ -224,6 +224,13 @@ struct PzDev {
   double* dt_io;
   PzState* rec;
   int sched_n, sched_mode;
+  // grid snapshots of the adjoint sweeps (null on the plain step): k_rloop of
+  // stage s stores the c2r grids of a collocation instance's state, rows
+  // [r][us + i up, om + i T][P], at slot gsnap_slot0 + s - 1 of
+  // gsnap + o_gsnap[inst] (N * 2P values per slot)
+  double2* gsnap;
+  const long long* o_gsnap;
+  int gsnap_slot0;
 };
 
 // `only` selects one instance (>= 0) or all of them (-1).

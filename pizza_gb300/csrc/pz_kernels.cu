@@ -156,6 +156,10 @@ struct StepIO {
   double2 *us, *up, *om, *T, *eT, *eP, *vsT, *vsOm;
   double2 *X, *eX, *vsX;     // composition (null without it)
   double* cflv;
+  // grid snapshot of this stage's state (gsnap null: none), PzDev::gsnap
+  double2* gsnap;
+  const long long* o_gsnap;
+  int gslot, inst;
   __device__ double2 in(int f, int m, int r) const {
     const long long o = (long long)m * N + r;
     return f == 0 ? us[o] : f == 1 ? up[o] : f == 2 ? om[o] : f == 3 ? T[o] : X[o];
@@ -176,10 +180,16 @@ struct StepIO {
     cflv[r] = dtr;
     cflv[N + r] = dth;
   }
+  // the c2r grids of a radius group, [g][field pair][P] from offset `off`
+  __device__ void grid(const double2* g, long long off, int n) const {
+    if (!gsnap) return;
+    double2* gs = gsnap + o_gsnap[inst] + (long long)gslot * N * 2 * V.I->P + off;
+    for (int k = threadIdx.x; k < n; k += blockDim.x) gs[k] = g[k];
+  }
 };
 
 template <bool CHEM>
-__global__ void __launch_bounds__(256) k_rloop(PzDev d, int stage) {
+__global__ void __launch_bounds__(256, CHEM ? 3 : 4) k_rloop(PzDev d, int stage) {
   extern __shared__ double2 sh[];
   const PzItem it = d.ritems[blockIdx.x];
   const PzInst& I = d.inst[it.inst];
@@ -201,6 +211,10 @@ __global__ void __launch_bounds__(256) k_rloop(PzDev d, int stage) {
   io.eX = chem ? V.hist(2, 2, eslot, 0) : nullptr;
   io.vsX = chem ? V.fld(F_DVSXI, 0) : nullptr;
   io.cflv = d.pool + I.o_cfl;
+  io.gsnap = chem ? nullptr : d.gsnap;
+  io.o_gsnap = d.o_gsnap;
+  io.gslot = d.gsnap_slot0 + stage - 1;
+  io.inst = it.inst;
   double* rsh = reinterpret_cast<double*>(sh + (chem ? 6 : 4) * I.rg * I.P);
   rloop_group<CHEM>(I, V, it.idx, I.rg, io, sh, rsh);
 }

@@ -28,6 +28,7 @@ struct ExplIO {
   }
   // composition: never asked for (the stage-level entry points reject it)
   __device__ void outx(int, int, double2, double2) const {}
+  __device__ void grid(const double2*, long long, int) const {}
   __device__ void out(int m, int r, double2 dtdt, double2 vst, double2 dpdt, double2 vsom) const {
     const long long o = (long long)r * M + m;
     a->dTdt[o] = dtdt;

@@ -124,6 +124,24 @@ def test_checkpoint_interval_does_not_change_gradient(pz):
         assert abs(r - r0) <= 1e-13 * abs(r0)
 
 
+def test_grid_snapshots_do_not_change_gradient(pz):
+    """The backward sweep with the forward's phi-grids (default) and with
+    grids recomputed from the spectral snapshots give the same gradient;
+    disabling the grids of a stored sweep falls back to the transforms."""
+    t0 = seeded(SMALL, 5, 1e-2)
+    ens = pz.Ensemble(gpu_config(SMALL))
+    fwd(ens, t0, 12, 7, SCHED, ck=5)
+    g1, r1 = ens.adjoint_backward()
+    ens.adjoint_grid_snapshots(False)
+    g2, r2 = ens.adjoint_backward()           # same stored sweep, no grids
+    fwd(ens, t0, 12, 7, SCHED, ck=5)
+    g3, r3 = ens.adjoint_backward()
+    ens.adjoint_grid_snapshots(True)
+    for g, r in ((g2, r2), (g3, r3)):
+        assert np.max(np.abs(g[0] - g1[0])) <= 1e-13 * np.max(np.abs(g1[0]))
+        assert abs(r[0] - r1[0]) <= 1e-13 * abs(r1[0])
+
+
 def test_backward_twice_and_state_left_at_final(pz):
     t0 = seeded(SMALL, 4, 1e-2)
     ens = pz.Ensemble(gpu_config(SMALL))

@@ -114,6 +114,23 @@ def test_dirk_checkpoint_interval_does_not_change_gradient(pz):
         assert abs(dra - grads[0][1]) <= 1e-12 * abs(grads[0][1])
 
 
+@pytest.mark.parametrize("scheme", ["ARS233", "ARS222", "BPR353"])
+def test_dirk_grid_snapshots_do_not_change_gradient(pz, scheme):
+    """Stage-state grids from the forward's k_rloop (default) against grids
+    recomputed from the spectral snapshots."""
+    spec = dict(SMALL, time_scheme=scheme)
+    t0 = seeded(spec, 4, 1e-2)
+    ens = pz.Ensemble(gpu_config(spec))
+    fwd(ens, [t0], 10, 6, SCHED, ck=4)
+    g1, r1 = ens.adjoint_backward()
+    ens.adjoint_grid_snapshots(False)
+    fwd(ens, [t0], 10, 6, SCHED, ck=4)
+    g2, r2 = ens.adjoint_backward()
+    ens.adjoint_grid_snapshots(True)
+    assert np.max(np.abs(g2[0] - g1[0])) <= 1e-13 * np.max(np.abs(g1[0]))
+    assert abs(r2[0] - r1[0]) <= 1e-13 * abs(r1[0])
+
+
 def test_dirk_batched_instances(pz):
     """Three instances of different grids and Ra in one ARS233 sweep; the
     gradient of each instance's NuTop against finite differences."""
