@@ -435,6 +435,21 @@ struct SymDot2 {
   __device__ __forceinline__ void store2(int t, double a, double b) const { oa[t] = a; ob[t] = b; }
 };
 
+// one parity-compact operator applied to two inputs (v0a, v1a) and (v0b, v1b)
+struct SymDotX2 {
+  const double* __restrict__ A; int nrow;
+  const double* __restrict__ v0a; const double* __restrict__ v1a;
+  const double* __restrict__ v0b; const double* __restrict__ v1b;
+  double* __restrict__ oa; double* __restrict__ ob;
+  __device__ __forceinline__ void fma2(int t, int j, double& a, double& b) const {
+    const int row = t >> 1, c = 2 * j + (t & 1);
+    const double m = __ldg(A + row + (long long)j * nrow);
+    a = ::fma(m, ((row & 1) ? v1a : v0a)[c], a);
+    b = ::fma(m, ((row & 1) ? v1b : v0b)[c], b);
+  }
+  __device__ __forceinline__ void store2(int t, double a, double b) const { oa[t] = a; ob[t] = b; }
+};
+
 // y = A x, A column-major n x n real, x complex
 __device__ __forceinline__ void mv_lanes(const double* __restrict__ A, int n, const double2* __restrict__ x,
                                          double2* __restrict__ y) {
@@ -542,6 +557,34 @@ __device__ void op_D1p(const View& V, int n, const double2* x, double2* y1, SymS
   sym_dot(V.basis(BM_D1PS), 2 * h2, h2, w.s, w.a, w.t1);
   __syncthreads();
   sym_combine(w.t1, n, -1.0, 1.0, y1);
+}
+// (ya, yb) = (D1p xa, D1p xb): the operator read once for both inputs; sb, ab
+// (h2 complex each) hold the second input's sums and differences.  The
+// products are those of op_D1p, bit for bit.
+__device__ void op_D1p2(const View& V, int n, const double2* xa, const double2* xb, double2* ya, double2* yb,
+                        SymScratch& w, double2* sb, double2* ab) {
+  const int h2 = (n + 1) / 2;
+  prep_sa(xa, n, w.s, w.a);
+  prep_sa(xb, n, sb, ab);
+  __syncthreads();
+  lane_dots2(SymDotX2{V.basis(BM_D1PS), 2 * h2, reinterpret_cast<const double*>(w.s),
+                      reinterpret_cast<const double*>(w.a), reinterpret_cast<const double*>(sb),
+                      reinterpret_cast<const double*>(ab), w.t1, w.t2},
+             4 * h2, h2);
+  __syncthreads();
+  sym_combine(w.t1, n, -1.0, 1.0, ya);
+  sym_combine(w.t2, n, -1.0, 1.0, yb);
+}
+// (yc, yd) = (C x, D1c x): Chebyshev coefficients -> physical values and
+// d/dr, one even/odd split of x for both
+__device__ void op_CD1c(const View& V, int n, const double2* x, double2* yc, double2* yd, SymScratch& w) {
+  const int h2 = (n + 1) / 2;
+  prep_eo(x, n, w.s, w.a);
+  __syncthreads();
+  sym_dot2(V.basis(BM_COS), V.basis(BM_D1CS), 2 * h2, h2, w.s, w.a, w.t1, w.t2);
+  __syncthreads();
+  sym_combine(w.t1, n, 1.0, -1.0, yc);
+  sym_combine(w.t2, n, -1.0, 1.0, yd);
 }
 
 // ---- transposes (discrete adjoint) -----------------------------------------

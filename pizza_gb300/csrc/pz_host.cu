@@ -56,6 +56,7 @@ struct Basis {
   std::vector<double> x, C, D1c, D2c, D1p, D2p, rMat, drMat, d2rMat;
   std::vector<double> Cs, D1cs, D2cs, D1ps, D2ps;   // parity-compact forms
   std::vector<double> CTs, D1cTs, D2cTs, D1pTs;     // ... of the transposes
+  std::vector<double> Cos;                          // C in the out-sym layout
 };
 
 // Parity-compact operators (see BM_CS..BM_D2PS in pz_internal.h).  The
@@ -113,6 +114,7 @@ void make_compact(Basis& b) {
   b.D1cTs = compact_in(transpose(b.D1c, N), N);
   b.D2cTs = compact_in(transpose(b.D2c, N), N);
   b.D1pTs = compact_centro(transpose(b.D1p, N), N);
+  b.Cos = compact_out(b.C, N);   // C(N-1-i, k) = (-1)^k C(i, k)
 }
 
 Basis make_basis(int N, double r_icb, double r_cmb) {
@@ -700,7 +702,7 @@ extern "C" int pz_create(const pz_config* cfgs, int n, pz_handle** out) {
       double* dst = img.data() + basis_off[kv.first];
       const std::vector<double>* mats[BM_COUNT] = {&B.C,    &B.D1c,  &B.D2c,  &B.D1p,   &B.D2p,   &B.rMat,
                                                    &B.drMat, &B.d2rMat, &B.Cs, &B.D1cs, &B.D2cs, &B.D1ps,
-                                                   &B.D2ps, &B.CTs, &B.D1cTs, &B.D2cTs, &B.D1pTs};
+                                                   &B.D2ps, &B.CTs, &B.D1cTs, &B.D2cTs, &B.D1pTs, &B.Cos};
       for (int k = 0; k < BM_COUNT; ++k) std::memcpy(dst + k * NN, mats[k]->data(), mats[k]->size() * sizeof(double));
     }
     const long double pi = 3.141592653589793238462643383279502884L;

@@ -117,6 +117,8 @@ enum {
   BM_D1CTS,   // D1c^T, N x h2 (layout of BM_CS; even rows pair with a, odd with s)
   BM_D2CTS,   // D2c^T, N x h2 (layout of BM_CS)
   BM_D1PTS,   // D1p^T, 2*h2 x h2 (layout of BM_D1PS)
+  BM_COS,     // C in the layout of BM_D1CS (mirror row = E - O), so that C and D1c
+              // share one even/odd split of their input
   BM_COUNT
 };
 

@@ -1091,9 +1091,7 @@ __device__ __forceinline__ void mloop_item(const PzDev& d, const PzItem it, int 
     s.e[i] = V.fld(F_DVSOM, mi)[i];
   }
   __syncthreads();
-  op_D1p(V, n, s.a, s.b, s.w);
-  __syncthreads();
-  op_D1p(V, n, s.e, s.f, s.w);
+  op_D1p2(V, n, s.a, s.e, s.b, s.f, s.w, s.g, s.h);
   __syncthreads();
   {
     double2* eT = V.hist(0, 2, eslot, mi);
@@ -1185,10 +1183,13 @@ __device__ __forceinline__ void mloop_item(const PzDev& d, const PzItem it, int 
                                                          : d.pool + I.o_gt + (long long)mi * n * n;
   mv_lanes(GT, n, s.a, s.b);                                              // Chebyshev T
   __syncthreads();
-  if (resid) op_D1c(V, n, s.b, s.c, s.w);                                 // dT/dr
-  else op_Dc2(V, n, s.b, s.c, s.e, s.w);                                  // dT/dr, d2T/dr2
-  __syncthreads();
-  op_C(V, n, s.b, s.f, s.w);                                              // T (physical)
+  if (resid) {
+    op_CD1c(V, n, s.b, s.f, s.c, s.w);                                    // T (physical), dT/dr
+  } else {
+    op_Dc2(V, n, s.b, s.c, s.e, s.w);                                     // dT/dr, d2T/dr2
+    __syncthreads();
+    op_C(V, n, s.b, s.f, s.w);                                            // T (physical)
+  }
   __syncthreads();
   bool bad = false;
   {
@@ -1223,10 +1224,13 @@ __device__ __forceinline__ void mloop_item(const PzDev& d, const PzItem it, int 
     __syncthreads();
     mv_lanes(d.pool + I.o_gx + (long long)mi * n * n, n, s.a, s.b);    // Chebyshev xi
     __syncthreads();
-    if (resid) op_D1c(V, n, s.b, s.c, s.w);
-    else op_Dc2(V, n, s.b, s.c, s.e, s.w);
-    __syncthreads();
-    op_C(V, n, s.b, s.g, s.w);                                          // xi (physical)
+    if (resid) {
+      op_CD1c(V, n, s.b, s.g, s.c, s.w);                                // xi (physical), dxi/dr
+    } else {
+      op_Dc2(V, n, s.b, s.c, s.e, s.w);
+      __syncthreads();
+      op_C(V, n, s.b, s.g, s.w);                                        // xi (physical)
+    }
     __syncthreads();
     double2* oX = V.hist(2, 0, oslot, mi);
     double2* iX = V.hist(2, 1, islot, mi);
@@ -1266,10 +1270,13 @@ __device__ __forceinline__ void mloop_item(const PzDev& d, const PzItem it, int 
   if (m == 0) {
     mv_lanes(d.pool + I.o_guphi, n, s.a, s.b);           // uphi, Chebyshev
     __syncthreads();
-    if (resid) op_D1c(V, n, s.b, s.c, s.w);
-    else op_Dc2(V, n, s.b, s.c, s.e, s.w);
-    __syncthreads();
-    op_C(V, n, s.b, s.g, s.w);
+    if (resid) {
+      op_CD1c(V, n, s.b, s.g, s.c, s.w);
+    } else {
+      op_Dc2(V, n, s.b, s.c, s.e, s.w);
+      __syncthreads();
+      op_C(V, n, s.b, s.g, s.w);
+    }
     __syncthreads();
     const double* ekp = ekpump;
     for (int i = threadIdx.x; i < n; i += blockDim.x) {
@@ -1327,9 +1334,7 @@ __device__ __forceinline__ void mloop_item(const PzDev& d, const PzItem it, int 
     }
     __syncthreads();
     }
-    op_D1c(V, n, s.e, s.g, s.w);                                     // dpsi/dr
-    __syncthreads();
-    op_C(V, n, s.e, s.h, s.w);                                       // psi
+    op_CD1c(V, n, s.e, s.h, s.g, s.w);                               // psi, dpsi/dr
     __syncthreads();
     for (int i = threadIdx.x; i < n; i += blockDim.x) {
       const double2 p = s.h[i], dp = s.g[i];
