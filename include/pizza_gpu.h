@@ -190,8 +190,9 @@ int pz_set_step_state(pz_handle* h, int inst, double time, const double* dt, int
 /* Snapshot spectra of one instance's current state, computed on the device
  * (calculate_spectra, src/spectra.f90:104-196): out receives n_m_max rows
  * of 5 doubles, for each m the r-integral (rInt_R) of
- * pi cc2real(f(m, r)) r height(r) for f = us, up, om, temp, xi (zero
- * without composition). */
+ * pi cc2real(f(m, r)) r height(r) for f = us, up, om, temp, and the
+ * reference's composition column xi2_m, which spectra.f90:183 fills with the
+ * temperature's integral when composition is on (zero without it). */
 int pz_get_spectra(pz_handle* h, int inst, double* out);
 
 /* l_AB1 of read_checkpoint (src/checkpoints.f90:398-425): when set, the

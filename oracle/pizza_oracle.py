@@ -1793,15 +1793,19 @@ class Pizza:
     # -- time series (src/outputs.f90:418-830) -------------------------------
     def spectra(self):
         """calculate_spectra (spectra.f90:104-196), the snapshot part: per m
-        the rInt_R of pi cc2real(f) r height for f = us, up, om, temp, and
-        xi (zero without composition).  (M, 5) array."""
+        the rInt_R of pi cc2real(f) r height for f = us, up, om, temp.  The
+        fifth column is the reference's xi2_m, which spectra.f90:183 fills
+        with the temperature's integral (rInt_R(temp2R)) when composition is
+        on; zero without composition.  (M, 5) array."""
         c = self.cheb
         out = np.zeros((self.M, 5))
         for i in range(self.M):
-            for k, f in enumerate((self.us, self.up, self.om, self.temp, self.xi)):
+            for k, f in enumerate((self.us, self.up, self.om, self.temp)):
                 z = f[i]
                 c2 = z.real ** 2 if i == 0 else 2.0 * (z.real ** 2 + z.imag ** 2)
                 out[i, k] = c.rInt_R(np.pi * c2 * self.r * self.height)
+            if self.l_chem:
+                out[i, 4] = out[i, 3]
         return out
 
     def time_series(self):

@@ -1578,7 +1578,10 @@ __device__ __forceinline__ double round_off(double x) { return fabs(x) < 10.0 * 
 // ---------------------------------------------------------------------------
 // k_spectra: snapshot spectra of one instance (calculate_spectra,
 // src/spectra.f90:104-196): per m, rInt_R of pi cc2real(f) r height for
-// f = us, up, om, T, xi (zero without composition); one block per m
+// f = us, up, om, T, and the composition column, one block per m.  The
+// reference fills that column with the temperature's integral (xi2_m =
+// rInt_R(temp2R), spectra.f90:183) when composition is on, and leaves it zero
+// otherwise; the column here is the same, so spec files match.
 // ---------------------------------------------------------------------------
 __global__ void k_spectra(PzDev d, int inst, double* out) {
   const PzInst& I = d.inst[inst];
@@ -1588,9 +1591,9 @@ __global__ void k_spectra(PzDev d, int inst, double* out) {
   const double* rr = V.rad(RV_R);
   const double* h = V.rad(RV_HEIGHT);
   const double* wint = V.rad(RV_WINT);
-  const int fl[5] = {F_US, F_UP, F_OM, F_TEMP, F_XI};
+  const int fl[4] = {F_US, F_UP, F_OM, F_TEMP};
   const double pi = 3.14159265358979323846;
-  for (int k = 0; k < 5; ++k) {
+  for (int k = 0; k < 4; ++k) {
     const double2* f = V.fld(fl[k], mi);
     double acc = 0.0;
     for (int r = threadIdx.x; r < n; r += blockDim.x) {
@@ -1599,7 +1602,10 @@ __global__ void k_spectra(PzDev d, int inst, double* out) {
       acc += wint[r] * (pi * c2 * rr[r] * h[r]);
     }
     acc = block_sum(acc, red);
-    if (threadIdx.x == 0) out[5 * mi + k] = acc;
+    if (threadIdx.x == 0) {
+      out[5 * mi + k] = acc;
+      if (k == 3) out[5 * mi + 4] = (I.flags & PZF_CHEM) ? acc : 0.0;
+    }
   }
 }
 

@@ -71,6 +71,59 @@ def write_spectrum(ens, i: int, counter: int, tag: str, directory: str = "."):
     return p
 
 
+class SpectraAverage:
+    """Time-averaged m-spectra (calculate_spectra and write_spectra_avg,
+    src/spectra.f90:104-196, :198-304): a running mean and standard deviation
+    of the five m-spectra, updated by getMSD2 (src/useful.f90:263-293), the
+    recursion for a variable averaging step.  After calls at averaging times
+    T_1 < ... < T_n, mean = sum_k dt_k x_k / T_n and SD = sqrt(sum_k dt_k
+    (x_k - mean)^2 / T_n), with dt_k = T_k - T_(k-1) and T_0 = 0."""
+
+    def __init__(self, n_m_max: int, minc: int = 1):
+        self.mean = np.zeros((n_m_max, 5))
+        self.sd = np.zeros((n_m_max, 5))
+        self.minc = minc
+        self.n_calls = 0
+        self.time_last = 0.0
+
+    def update(self, spec, time_avg: float):
+        """spec: (n_m_max, 5) snapshot spectra (Ensemble.spectra);
+        time_avg: the caller's running sum of dt over its output calls
+        (timeAvg_spec, outputs.f90:271-272)."""
+        x = np.asarray(spec, float)
+        self.n_calls += 1
+        dt = time_avg - self.time_last
+        if self.n_calls == 1:
+            self.mean = x.copy()
+            self.sd = np.zeros_like(x)
+        else:
+            delta = x - self.mean
+            self.mean = self.mean + delta * dt / time_avg
+            self.sd = self.sd + dt * delta * (x - self.mean)
+        self.time_last = time_avg
+
+    def result(self):
+        """(mean, SD) arrays, SD normalised as write_spectra_avg does."""
+        return self.mean.copy(), np.sqrt(self.sd / self.time_last)
+
+    def lines(self):
+        """spec_avg.TAG lines: '(I5, 10es16.8)' of m and the round_off'ed
+        mean and SD of us2, up2, enstrophy, T^2 and the composition column."""
+        mean, sd = self.result()
+        out = []
+        for mi in range(mean.shape[0]):
+            vals = [_round_off(v) for k in range(5) for v in (mean[mi, k], sd[mi, k])]
+            out.append(f"{mi * self.minc:5d}" + "".join(fortran_es(v, 16, 8) for v in vals))
+        return out
+
+    def write(self, tag: str, directory: str = "."):
+        p = os.path.join(directory, f"spec_avg.{tag}")
+        with open(p, "w") as f:
+            for ln in self.lines():
+                f.write(ln + "\n")
+        return p
+
+
 def write_series(ens, i: int, tag: str, directory: str = ".", rows=None):
     """Write e_kin.TAG, heat.TAG, (rotating runs) e_kin_3D.TAG and (with
     composition) composition.TAG of instance i from its time-series rows

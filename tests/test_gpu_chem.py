@@ -175,6 +175,8 @@ def test_chem_spectra_frames_and_series_files(pz, tmp_path):
     got, ref = ens.spectra(0), sim.spectra()
     err = np.max(np.abs(got - ref), axis=0) / np.max(np.abs(ref), axis=0)
     assert np.all(err < 1e-10), err
+    # the reference's xi2_m column holds the temperature's integral (spectra.f90:183)
+    assert np.array_equal(got[:, 4], got[:, 3])
     paths = save_frames(ens, 0, 1, "chem", str(tmp_path))
     assert [os.path.basename(p) for p in paths] == ["frame_temp_1.chem", "frame_xi_1.chem", "frame_us_1.chem",
                                                      "frame_up_1.chem", "frame_om_1.chem"]

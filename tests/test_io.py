@@ -88,3 +88,49 @@ def test_spectrum_line_format():
     assert lines[0] == "    0  1.50000000E-03  2.00000000E+00  0.00000000E+00 -3.25000000E-07  0.00000000E+00"
     assert lines[1].startswith("    1  0.00000000E+00  1.00000000E+00")
     assert all(len(x) == 5 + 5 * 16 for x in lines)
+
+
+def test_spectra_average_closed_form(tmp_path):
+    """The getMSD2 recursion (useful.f90:263-293) against its closed form: the
+    dt-weighted mean and standard deviation over the averaging time, dt_1 = T_1."""
+    rng = np.random.default_rng(5)
+    n_m, n = 7, 9
+    T = np.cumsum(rng.uniform(1e-4, 3e-4, n))
+    X = rng.uniform(0.0, 2.0, (n, n_m, 5))
+    avg = pizza_io.SpectraAverage(n_m, minc=2)
+    for t, x in zip(T, X):
+        avg.update(x, t)
+    dt = np.diff(np.concatenate([[0.0], T]))
+    mean = np.tensordot(dt, X, axes=1) / T[-1]
+    sd = np.sqrt(np.tensordot(dt, (X - mean) ** 2, axes=1) / T[-1])
+    got_mean, got_sd = avg.result()
+    assert np.max(np.abs(got_mean - mean)) <= 1e-13 * np.max(np.abs(mean))
+    assert np.max(np.abs(got_sd - sd)) <= 1e-10 * np.max(np.abs(sd))
+    p = avg.write("t", str(tmp_path))
+    rows = np.loadtxt(p)
+    assert rows.shape == (n_m, 11)
+    assert np.array_equal(rows[:, 0], 2 * np.arange(n_m))
+    assert np.allclose(rows[:, 1:11:2], mean, rtol=1e-7) and np.allclose(rows[:, 2:11:2], sd, rtol=1e-7)
+
+
+def test_spectra_average_of_oracle_run():
+    """Snapshot spectra of an oracle run averaged over its log steps; the first
+    call sets the mean (n_calls = 1) and the SD starts at zero."""
+    from tests.helpers import oracle, seeded
+    spec = dict(n_r_max=17, n_cheb_max=17, m_max=8, ek=1e-3, ra=1e5, pr=1.0, radratio=0.35, l_ek_pump=True,
+                time_scheme="CNAB2", dtMax=1e-4, matrix_solve="INFLUENCE")
+    sim = oracle(spec, temp0=seeded(spec, 1, 1e-2))
+    avg = pizza_io.SpectraAverage(sim.M)
+    t_avg, snaps, dts = 0.0, [], []
+    for k in range(6):
+        t_avg += sim.tscheme.dt[0] if hasattr(sim, "tscheme") else 1e-4
+        sp = sim.spectra()
+        avg.update(sp, t_avg)
+        snaps.append(sp)
+        dts.append(t_avg - (sum(dts) if dts else 0.0))
+        sim.advance()
+    mean, sd = avg.result()
+    w = np.array(dts)
+    ref = np.tensordot(w, np.array(snaps), axes=1) / t_avg
+    assert np.max(np.abs(mean - ref)) <= 1e-13 * np.max(np.abs(ref))
+    assert np.all(sd >= 0.0) and np.all(np.isfinite(sd))
