@@ -96,9 +96,10 @@ def mloop_work(specs, nold=1, nimp=1, nexp=2):
     N-vectors).  The Chebyshev operators shared by all m of one size are
     counted once per size.  Flops: per m, 3 dense real-operator x complex-vector
     products (4N^2 flops each: temperature/vorticity operator twice, the
-    streamfunction operator K once) and 10 products with the parity-compact
-    Chebyshev operators (2N^2 flops each); m = 0: 2 dense and 8 compact.
-    Elementwise work is neglected.
+    streamfunction operator K once) and 7 products with the parity-compact
+    Chebyshev operators (2N^2 flops each: D1p of dVsT and dVsOm, C and D1c of
+    T and of psi, C of omega); m = 0: 2 dense (temperature, u_phi) and 6
+    compact.  Elementwise work is neglected.
     """
     byts = 0.0
     flops = 0.0
@@ -109,7 +110,7 @@ def mloop_work(specs, nold=1, nimp=1, nexp=2):
         per_m = 8.0 * 2 * N * N + 8.0 * (4 * N + 4) + 16.0 * N * (6 + 2 * (nold + nimp + nexp) + 12)
         m0 = 8.0 * 2 * N * N + 16.0 * N * (6 + 2 * (nold + nimp + nexp) + 12)
         byts += (M - 1) * per_m + m0
-        flops += (M - 1) * (3 * 4.0 + 10 * 2.0) * N * N + (2 * 4.0 + 8 * 2.0) * N * N
+        flops += (M - 1) * (3 * 4.0 + 7 * 2.0) * N * N + (2 * 4.0 + 6 * 2.0) * N * N
     for N in sizes:
         byts += 8.0 * 4 * N * N
     return byts, flops
