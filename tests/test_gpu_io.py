@@ -120,3 +120,36 @@ def test_device_spectra_match_oracle(pz, tmp_path, spec_extra):
     assert np.all(err < 1e-10), err
     p = write_spectrum(ens, 0, 0, "gpu", str(tmp_path))
     assert np.loadtxt(p).shape == (ens.dims[0][1], 6)
+
+
+def test_input_nml_driver_matches_oracle(pz, tmp_path):
+    """python -m pizza_gb300.run on an input.nml: the e_kin.TAG and heat.TAG
+    rows it writes at step 0 and every n_log_step steps against the oracle's
+    rows at the same steps (8 significant digits, the file format)."""
+    from tests.helpers import series_from_oracle
+    from pizza_gb300 import namelist, run as drv
+    nml = tmp_path / "input.nml"
+    nml.write_text("&grid\n n_r_max=33, n_cheb_max=33, m_max=32,\n/\n"
+                   "&control\n tag='drv', n_time_steps=20, dtMax=1.0d-4, time_scheme='CNAB2',\n"
+                   " l_ek_pump=.true., matrix_solve='INFLUENCE',\n/\n"
+                   "&phys_param\n ra=1.0d5, ek=1.0d-3, pr=1.0d0, radratio=0.35d0,\n/\n"
+                   "&start_field\n init_t=2, amp_t=1.0d-2,\n/\n&output_control\n n_log_step=5,\n/\n")
+    out = tmp_path / "out"
+    paths = drv.run(str(nml), str(out))
+    names = sorted(os.path.basename(p) for p in paths)
+    assert names == ["checkpoint_end.drv", "e_kin.drv", "e_kin_3D.drv", "heat.drv", "spec_1.drv"]
+    cfg, ctl, _ = namelist.read(str(nml))
+    spec = dict(n_r_max=33, n_cheb_max=33, m_max=32, ek=1e-3, ra=1e5, pr=1.0, radratio=0.35, l_ek_pump=True,
+                dtMax=1e-4, time_scheme="CNAB2", matrix_solve="INFLUENCE")
+    sim = oracle(spec, temp0=drv.start_temperature(cfg, ctl))
+    ref = [series_from_oracle(sim)]
+    for k in range(20):
+        sim.advance()
+        if (k + 1) % 5 == 0:
+            ref.append(series_from_oracle(sim))
+    ref = np.array(ref)
+    ek = np.loadtxt(out / "e_kin.drv")
+    assert ek.shape[0] == 5
+    scale = np.max(np.abs(ref[:, 1:4]), axis=0)
+    assert np.all(np.abs(ek[:, 1:4] - ref[:, 1:4]) <= 1e-7 * scale + 1e-20), (ek[:, 1:4], ref[:, 1:4])
+    assert np.allclose(ek[:, 0], ref[:, 0], rtol=1e-9)
