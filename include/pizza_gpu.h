@@ -63,6 +63,14 @@ extern "C" {
 #define PZ_MARS343   21   /* (A) */
 #define PZ_SSP322    22   /* (A) */
 #define PZ_SSP332    23   /* (A) */
+#define PZ_SSP433    24   /* (A) */
+#define PZ_DP1_242   25   /* 'DP1-242' */
+#define PZ_DP2_242   26   /* 'DP2-242' */
+#define PZ_LZ453     27
+#define PZ_KC343     28   /* (A) */
+#define PZ_KC564     29   /* (A) */
+#define PZ_KC785     30   /* (A) */
+#define PZ_DBM453    31   /* (A) */
 
 /* matrix_solve values (src/namelists.f90:416-421) */
 #define PZ_SOLVE_INFLUENCE 0   /* update_psi_coll_dmat: real om/psi solves + 2x2 influence matrix */
@@ -245,7 +253,8 @@ const char* pz_kernel_name(int k);
  * n_r_max doubles each (the per-radius Courant steps of src/courant.f90:41-76,
  * evaluated with the instance's courfac).  Ordered on the handle's stream,
  * asynchronous; device memory for 2*n_m_max*n_r_max complex intermediates is
- * taken with cudaMallocAsync on that stream and released after the call. */
+ * taken with cudaMallocAsync on that stream and released after the call.
+ * Collocation instances without composition only (PZ_E_UNSUPPORTED else). */
 int pz_explicit_terms(pz_handle* h, int inst, const double* us, const double* up,
                       const double* om, const double* temp, double* dTdt_expl,
                       double* dpsidt_expl, double* dtr, double* dth);
@@ -261,7 +270,8 @@ int pz_explicit_terms(pz_handle* h, int inst, const double* us, const double* up
  *    PZ_E_ARG with a message;
  *  - call it with the handle's device current; the first call on a device
  *    looks up the array's device address (cudaGetSymbolAddress), so make that
- *    first call before any stream capture;
+ *    first call before any stream capture.  The address is kept for the life
+ *    of the process: do not call it again on a device after cudaDeviceReset;
  *  - all calls on a device share the array: calls that overlap on the GPU
  *    race, so order them (one stream, or events).  Nothing needs clearing
  *    between calls. */
@@ -270,7 +280,6 @@ int pz_explicit_terms_noalloc(pz_handle* h, int inst, const double* us, const do
                               const double* om, const double* temp, double* dTdt_expl,
                               double* dpsidt_expl, double* dtr, double* dth);
 
-/* Release all device memory of the handle. */
 /* ---- discrete adjoint (the gradient path) ----------------------------------
  * pizza itself has no adjoint; these entry points back the PyTorch
  * autograd.Function of the binding.  The objective of every instance is
@@ -331,6 +340,7 @@ int pz_set_ra(pz_handle* h, int inst, double ra);
 #define PZ_INTEG_OPS 19
 int pz_integ_operator(int n_r_max, double radratio, int which, double* out, int* bandwidth);
 
+/* Release all device memory of the handle. */
 int pz_destroy(pz_handle* h);
 
 /* Last error message of the handle (or of the last failed pz_create when h

@@ -436,6 +436,118 @@ def dirk_tableau(name: str):
         bi = [[0, 0, 0, 0], [0, g, 0, 0], [0, 1 - 2 * g, g, 0], [0, 0.5 - g, 0, g]]
         be = [[0, 0, 0, 0], [0, 0, 0, 0], [0, 1, 0, 0], [0, 0.25, 0.25, 0]]
         bai = bae = [0, 1.0 / 6.0, 1.0 / 6.0, 2.0 / 3.0]
+    elif n == "SSP433":
+        # dirk_schemes.f90:373-392; alpha, beta, eta are default-kind (single
+        # precision) literals there, so their float rounding is part of the tableau
+        a = float(np.float32(0.24169426078821))
+        b = float(np.float32(0.06042356519705))
+        e = float(np.float32(0.12915286960590))
+        g = a
+        ns, ass, cf = 5, True, 1.35
+        bi = [[0, 0, 0, 0, 0], [0, a, 0, 0, 0], [0, -a, a, 0, 0], [0, 0, 1 - a, a, 0], [0, b, e, 0.5 - b - e - a, a]]
+        be = [[0, 0, 0, 0, 0], [0, 0, 0, 0, 0], [0, 0, 0, 0, 0], [0, 0, 1, 0, 0], [0, 0, 0.25, 0.25, 0]]
+        bai = bae = [0, 0, 1.0 / 6.0, 1.0 / 6.0, 2.0 / 3.0]
+    elif n == "DP1-242":
+        # dirk_schemes.f90:393-409
+        g = 0.5
+        ns, ass, cf = 4, False, 1.35
+        bi = [[0, 0, 0, 0, 0], [0, 0.5, 0, 0, 0], [0, 1.0 / 6.0, 0.5, 0, 0], [0, -0.5, 0.5, 0.5, 0],
+              [0, 1.5, -1.5, 0.5, 0.5]]
+        be = [[0, 0, 0, 0, 0], [0, 0, 0, 0, 0], [0, 1.0 / 3.0, 0, 0, 0], [0, 1, 0, 0, 0], [0, 0.5, 0, 0.5, 0]]
+        exp_calc = [False, True, False, True]
+    elif n == "DP2-242":
+        # dirk_schemes.f90:410-425
+        g = 1.0 / 3.0
+        ns, ass, cf = 4, False, 1.35
+        bi = [[0, 0, 0, 0, 0], [0, g, 0, 0, 0], [0, -g, g, 0, 0], [0, 0, 1 - g, g, 0], [0, 0, 0.5, 0.5 - g, g]]
+        be = [[0, 0, 0, 0, 0], [0, 0, 0, 0, 0], [0, 0, 0, 0, 0], [0, 0, 1, 0, 0], [0, 0, 0.5, 0.5, 0]]
+        exp_calc = [False, True, True, True]
+    elif n == "LZ453":
+        # dirk_schemes.f90:498-513
+        g = 1.2
+        ns, ass, cf, imp1 = 4, False, 1.15, True
+        bi = [[0, 0, 0, 0, 0], [-44.0 / 45.0, 1.2, 0, 0, 0], [-47.0 / 300.0, -0.71, 1.2, 0, 0],
+              [3.375, -3.25, -59.0 / 120.0, 1.2, 0], [89.0 / 50.0, -486.0 / 55.0, 8.9, -562.0 / 275.0, 1.2]]
+        be = [[0, 0, 0, 0, 0], [2.0 / 9.0, 0, 0, 0, 0], [71.0 / 420.0, 23.0 / 140.0, 0, 0, 0],
+              [-281.0 / 336.0, 187.0 / 112.0, 0, 0, 0], [0.1, 0, 0.5, 0.4, 0]]
+    elif n == "KC343":
+        # dirk_schemes.f90:547-572 (Kennedy-Carpenter ARK3(2)4L[2]SA)
+        g = 1767732205903.0 / 4055673282236.0
+        ns, ass, cf, imp1 = 4, True, 0.5, True
+        last = [1471266399579.0 / 7840856788654.0, -4482444167858.0 / 7529755066697.0,
+                11266239266428.0 / 11593286722821.0, g]
+        bi = [[0, 0, 0, 0], [g, g, 0, 0],
+              [2746238789719.0 / 10658868560708.0, -640167445237.0 / 6845629431997.0, g, 0], last]
+        be = [[0, 0, 0, 0], [1767732205903.0 / 2027836641118.0, 0, 0, 0],
+              [5535828885825.0 / 10492691773637.0, 788022342437.0 / 10882634858940.0, 0, 0],
+              [6485989280629.0 / 16251701735622.0, -4246266847089.0 / 9704473918619.0,
+               10755448449292.0 / 10357097424841.0, 0]]
+        bai = bae = last
+    elif n == "KC564":
+        # dirk_schemes.f90:591-624 (Kennedy-Carpenter ARK4(3)6L[2]SA)
+        g = 0.25
+        ns, ass, cf, imp1 = 6, True, 0.5, True
+        last = [82889.0 / 524892.0, 0, 15625.0 / 83664.0, 69875.0 / 102672.0, -2260.0 / 8211.0, 0.25]
+        bi = [[0, 0, 0, 0, 0, 0], [0.25, 0.25, 0, 0, 0, 0], [8611.0 / 62500.0, -1743.0 / 31250.0, 0.25, 0, 0, 0],
+              [5012029.0 / 34652500.0, -654441.0 / 2922500.0, 174375.0 / 388108.0, 0.25, 0, 0],
+              [15267082809.0 / 155376265600.0, -71443401.0 / 120774400.0, 730878875.0 / 902184768.0,
+               2285395.0 / 8070912.0, 0.25, 0], last]
+        be = [[0, 0, 0, 0, 0, 0], [0.5, 0, 0, 0, 0, 0], [13861.0 / 62500.0, 6889.0 / 62500.0, 0, 0, 0, 0],
+              [-116923316275.0 / 2393684061468.0, -2731218467317.0 / 15368042101831.0,
+               9408046702089.0 / 11113171139209.0, 0, 0, 0],
+              [-451086348788.0 / 2902428689909.0, -2682348792572.0 / 7519795681897.0,
+               12662868775082.0 / 11960479115383.0, 3355817975965.0 / 11060851509271.0, 0, 0],
+              [647845179188.0 / 3216320057751.0, 73281519250.0 / 8382639484533.0,
+               552539513391.0 / 3454668386233.0, 3354512671639.0 / 8306763924573.0, 4040.0 / 17871.0, 0]]
+        bai = bae = last
+    elif n == "DBM453":
+        # dirk_schemes.f90:625-648; the assembly weights carry their own printed digits
+        g = 0.32591194130117247
+        ns, ass, cf, imp1 = 5, True, 0.5, True
+        bi = [[0, 0, 0, 0, 0], [-0.22284985318525410, g, 0, 0, 0], [-0.46801347074080545, 0.86349284225716961, g, 0, 0],
+              [-0.46509906651927421, 0.81063103116959553, 0.61036726756832357, g, 0],
+              [0.87795339639076675, -0.72692641526151547, 0.75204137157372720, -0.22898029400415088, g]]
+        be = [[0, 0, 0, 0, 0], [0.10306208811591838, 0, 0, 0, 0], [-0.94124866143519894, 1.6626399742527356, 0, 0, 0],
+              [-1.3670975201437765, 1.3815852911016873, 1.2673234025619065, 0, 0],
+              [-0.81287582068772448, 0.81223739060505738, 0.90644429603699305, 0.094194134045674111, 0]]
+        bai = bae = [0.87795339639076672, -0.72692641526151549, 0.7520413715737272, -0.22898029400415090,
+                     0.32591194130117247]
+    elif n == "KC785":
+        # dirk_schemes.f90:649-706 (Kennedy-Carpenter ARK5(4)8L[2]SA)
+        g = 2.0 / 9.0
+        ns, ass, cf, imp1 = 8, True, 0.5, True
+        a3 = 2366667076620.0 / 8822750406821.0
+        a4 = -257962897183.0 / 4451812247028.0
+        a5 = -486229321650.0 / 11227943450093.0
+        a6 = 621307788657.0 / 4714163060173.0
+        a7 = 2036305566805.0 / 6583108094622.0
+        last = [0, 0, 3517720773327.0 / 20256071687669.0, 4569610470461.0 / 17934693873752.0,
+                2819471173109.0 / 11655438449929.0, 3296210113763.0 / 10722700128969.0,
+                -1142099968913.0 / 5710983926999.0, g]
+        bi = [[0] * 8, [g, g, 0, 0, 0, 0, 0, 0], [a3, a3, g, 0, 0, 0, 0, 0],
+              [a4, a4, 128530224461.0 / 14379561246022.0, g, 0, 0, 0, 0],
+              [a5, a5, -225633144460.0 / 6633558740617.0, 1741320951451.0 / 6824444397158.0, g, 0, 0, 0],
+              [a6, a6, -125196015625.0 / 3866852212004.0, 940440206406.0 / 7593089888465.0,
+               961109811699.0 / 6734810228204.0, g, 0, 0],
+              [a7, a7, -3039402635899.0 / 4450598839912.0, -1829510709469.0 / 31102090912115.0,
+               -286320471013.0 / 6931253422520.0, 8651533662697.0 / 9642993110008.0, g, 0], last]
+        be = [[0] * 8, [4.0 / 9.0, 0, 0, 0, 0, 0, 0, 0],
+              [1.0 / 9.0, 1183333538310.0 / 1827251437969.0, 0, 0, 0, 0, 0, 0],
+              [895379019517.0 / 9750411845327.0, 477606656805.0 / 13473228687314.0,
+               -112564739183.0 / 9373365219272.0, 0, 0, 0, 0, 0],
+              [-4458043123994.0 / 13015289567637.0, -2500665203865.0 / 9342069639922.0,
+               983347055801.0 / 8893519644487.0, 2185051477207.0 / 2551468980502.0, 0, 0, 0, 0],
+              [-167316361917.0 / 17121522574472.0, 1605541814917.0 / 7619724128744.0,
+               991021770328.0 / 13052792161721.0, 2342280609577.0 / 11279663441611.0,
+               3012424348531.0 / 12792462456678.0, 0, 0, 0],
+              [6680998715867.0 / 14310383562358.0, 5029118570809.0 / 3897454228471.0,
+               2415062538259.0 / 6382199904604.0, -3924368632305.0 / 6964820224454.0,
+               -4331110370267.0 / 15021686902756.0, -3944303808049.0 / 11994238218192.0, 0, 0],
+              [2193717860234.0 / 3570523412979.0, 2193717860234.0 / 3570523412979.0,
+               5952760925747.0 / 18750164281544.0, -4412967128996.0 / 6196664114337.0,
+               4151782504231.0 / 36106512998704.0, 572599549169.0 / 6265429158920.0,
+               -457874356192.0 / 11306498036315.0, 0]]
+        bai = bae = last
     else:
         return None
     bi = np.array(bi, float)
@@ -450,6 +562,7 @@ def dirk_tableau(name: str):
 
 
 DIRK_SCHEMES = ("ARS222", "ARS232", "ARS233", "SSP222", "LSDIRK222", "LZ232", "CK232", "ARS443",
+                "SSP433", "DP1-242", "DP2-242", "LZ453", "KC343", "KC564", "KC785", "DBM453",
                 "BPR353", "PC2", "ARS343", "MARS343", "SSP322", "SSP332")
 
 

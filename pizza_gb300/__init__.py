@@ -28,7 +28,8 @@ SCHEMES = {"CNAB2": 0, "SBDF2": 1, "BDF2AB2": 1, "SBDF3": 2, "BDF3AB3": 2, "SBDF
            # DIRK IMEX Runge-Kutta (src/dirk_schemes.f90)
            "ARS222": 10, "ARS232": 11, "ARS233": 12, "SSP222": 13, "LSDIRK222": 14, "LZ232": 15,
            "CK232": 16, "ARS443": 17, "BPR353": 18, "PC2": 19, "ARS343": 20, "MARS343": 21,
-           "SSP322": 22, "SSP332": 23}
+           "SSP322": 22, "SSP332": 23, "SSP433": 24, "DP1-242": 25, "DP2-242": 26, "LZ453": 27,
+           "KC343": 28, "KC564": 29, "KC785": 30, "DBM453": 31}
 KERNEL_KINDS = 9
 SOLVE_INFLUENCE, SOLVE_DIRECT = 0, 1
 CHEB_COLL, CHEB_INTEG = 0, 1

@@ -316,6 +316,125 @@ bool dirk_tableau(int scheme, DirkTab* t) {
            {{0, 0, 0, 0}, {0, 0, 0, 0}, {0, 1, 0, 0}, {0, 0.25, 0.25, 0}});
       ass({0, 1.0 / 6.0, 1.0 / 6.0, 2.0 / 3.0});
       break;
+    case PZ_SSP433: {
+      // the reference writes alpha, beta and eta as default-kind (single
+      // precision) literals, so they carry float rounding into the double
+      // tableau; (double)<float literal> reproduces that
+      const double a = (double)0.24169426078821f, b = (double)0.06042356519705f;
+      const double e = (double)0.12915286960590f;
+      g = a;
+      t->nstages = 5; t->assembly = 1; t->courfac = 1.35;
+      rows({{0, 0, 0, 0, 0}, {0, a, 0, 0, 0}, {0, -a, a, 0, 0}, {0, 0, 1 - a, a, 0}, {0, b, e, 0.5 - b - e - a, a}},
+           {{0, 0, 0, 0, 0}, {0, 0, 0, 0, 0}, {0, 0, 0, 0, 0}, {0, 0, 1, 0, 0}, {0, 0, 0.25, 0.25, 0}});
+      ass({0, 0, 1.0 / 6.0, 1.0 / 6.0, 2.0 / 3.0});
+    } break;
+    case PZ_DP1_242:
+      g = 0.5;
+      t->nstages = 4; t->assembly = 0; t->courfac = 1.35;
+      rows({{0, 0, 0, 0, 0}, {0, 0.5, 0, 0, 0}, {0, 1.0 / 6.0, 0.5, 0, 0}, {0, -0.5, 0.5, 0.5, 0},
+            {0, 1.5, -1.5, 0.5, 0.5}},
+           {{0, 0, 0, 0, 0}, {0, 0, 0, 0, 0}, {0, 1.0 / 3.0, 0, 0, 0}, {0, 1, 0, 0, 0}, {0, 0.5, 0, 0.5, 0}});
+      t->exp_mask = 0xA;   // explicit terms at stages 2 and 4 only
+      break;
+    case PZ_DP2_242:
+      g = 1.0 / 3.0;
+      t->nstages = 4; t->assembly = 0; t->courfac = 1.35;
+      rows({{0, 0, 0, 0, 0}, {0, g, 0, 0, 0}, {0, -g, g, 0, 0}, {0, 0, 1 - g, g, 0}, {0, 0, 0.5, 0.5 - g, g}},
+           {{0, 0, 0, 0, 0}, {0, 0, 0, 0, 0}, {0, 0, 0, 0, 0}, {0, 0, 1, 0, 0}, {0, 0, 0.5, 0.5, 0}});
+      t->exp_mask = 0xE;   // no explicit terms at stage 1
+      break;
+    case PZ_LZ453:
+      g = 1.2; imp1 = true;
+      t->nstages = 4; t->assembly = 0; t->courfac = 1.15;
+      rows({{0, 0, 0, 0, 0}, {-44.0 / 45.0, 1.2, 0, 0, 0}, {-47.0 / 300.0, -0.71, 1.2, 0, 0},
+            {3.375, -3.25, -59.0 / 120.0, 1.2, 0}, {89.0 / 50.0, -486.0 / 55.0, 8.9, -562.0 / 275.0, 1.2}},
+           {{0, 0, 0, 0, 0}, {2.0 / 9.0, 0, 0, 0, 0}, {71.0 / 420.0, 23.0 / 140.0, 0, 0, 0},
+            {-281.0 / 336.0, 187.0 / 112.0, 0, 0, 0}, {0.1, 0, 0.5, 0.4, 0}});
+      break;
+    case PZ_KC343: {
+      g = 1767732205903.0 / 4055673282236.0; imp1 = true;
+      t->nstages = 4; t->assembly = 1; t->courfac = 0.5;
+      const double i41 = 1471266399579.0 / 7840856788654.0, i42 = -4482444167858.0 / 7529755066697.0;
+      const double i43 = 11266239266428.0 / 11593286722821.0;
+      rows({{0, 0, 0, 0}, {g, g, 0, 0},
+            {2746238789719.0 / 10658868560708.0, -640167445237.0 / 6845629431997.0, g, 0}, {i41, i42, i43, g}},
+           {{0, 0, 0, 0}, {1767732205903.0 / 2027836641118.0, 0, 0, 0},
+            {5535828885825.0 / 10492691773637.0, 788022342437.0 / 10882634858940.0, 0, 0},
+            {6485989280629.0 / 16251701735622.0, -4246266847089.0 / 9704473918619.0,
+             10755448449292.0 / 10357097424841.0, 0}});
+      ass({i41, i42, i43, g});
+    } break;
+    case PZ_KC564: {
+      g = 0.25; imp1 = true;
+      t->nstages = 6; t->assembly = 1; t->courfac = 0.5;
+      const double i61 = 82889.0 / 524892.0, i63 = 15625.0 / 83664.0, i64 = 69875.0 / 102672.0;
+      const double i65 = -2260.0 / 8211.0;
+      rows({{0, 0, 0, 0, 0, 0}, {0.25, 0.25, 0, 0, 0, 0}, {8611.0 / 62500.0, -1743.0 / 31250.0, 0.25, 0, 0, 0},
+            {5012029.0 / 34652500.0, -654441.0 / 2922500.0, 174375.0 / 388108.0, 0.25, 0, 0},
+            {15267082809.0 / 155376265600.0, -71443401.0 / 120774400.0, 730878875.0 / 902184768.0,
+             2285395.0 / 8070912.0, 0.25, 0},
+            {i61, 0, i63, i64, i65, 0.25}},
+           {{0, 0, 0, 0, 0, 0}, {0.5, 0, 0, 0, 0, 0}, {13861.0 / 62500.0, 6889.0 / 62500.0, 0, 0, 0, 0},
+            {-116923316275.0 / 2393684061468.0, -2731218467317.0 / 15368042101831.0,
+             9408046702089.0 / 11113171139209.0, 0, 0, 0},
+            {-451086348788.0 / 2902428689909.0, -2682348792572.0 / 7519795681897.0,
+             12662868775082.0 / 11960479115383.0, 3355817975965.0 / 11060851509271.0, 0, 0},
+            {647845179188.0 / 3216320057751.0, 73281519250.0 / 8382639484533.0, 552539513391.0 / 3454668386233.0,
+             3354512671639.0 / 8306763924573.0, 4040.0 / 17871.0, 0}});
+      ass({i61, 0, i63, i64, i65, 0.25});
+    } break;
+    case PZ_DBM453: {
+      g = 0.32591194130117247; imp1 = true;
+      t->nstages = 5; t->assembly = 1; t->courfac = 0.5;
+      rows({{0, 0, 0, 0, 0}, {-0.22284985318525410, g, 0, 0, 0},
+            {-0.46801347074080545, 0.86349284225716961, g, 0, 0},
+            {-0.46509906651927421, 0.81063103116959553, 0.61036726756832357, g, 0},
+            {0.87795339639076675, -0.72692641526151547, 0.75204137157372720, -0.22898029400415088, g}},
+           {{0, 0, 0, 0, 0}, {0.10306208811591838, 0, 0, 0, 0}, {-0.94124866143519894, 1.6626399742527356, 0, 0, 0},
+            {-1.3670975201437765, 1.3815852911016873, 1.2673234025619065, 0, 0},
+            {-0.81287582068772448, 0.81223739060505738, 0.90644429603699305, 0.094194134045674111, 0}});
+      // the assembly weights are printed with their own last digits
+      ass({0.87795339639076672, -0.72692641526151549, 0.7520413715737272, -0.22898029400415090,
+           0.32591194130117247});
+    } break;
+    case PZ_KC785: {
+      g = 2.0 / 9.0; imp1 = true;
+      t->nstages = 8; t->assembly = 1; t->courfac = 0.5;
+      const double a3 = 2366667076620.0 / 8822750406821.0, a4 = -257962897183.0 / 4451812247028.0;
+      const double a5 = -486229321650.0 / 11227943450093.0, a6 = 621307788657.0 / 4714163060173.0;
+      const double a7 = 2036305566805.0 / 6583108094622.0;
+      const double b83 = 3517720773327.0 / 20256071687669.0, b84 = 4569610470461.0 / 17934693873752.0;
+      const double b85 = 2819471173109.0 / 11655438449929.0, b86 = 3296210113763.0 / 10722700128969.0;
+      const double b87 = -1142099968913.0 / 5710983926999.0;
+      rows({{0, 0, 0, 0, 0, 0, 0, 0},
+            {g, g, 0, 0, 0, 0, 0, 0},
+            {a3, a3, g, 0, 0, 0, 0, 0},
+            {a4, a4, 128530224461.0 / 14379561246022.0, g, 0, 0, 0, 0},
+            {a5, a5, -225633144460.0 / 6633558740617.0, 1741320951451.0 / 6824444397158.0, g, 0, 0, 0},
+            {a6, a6, -125196015625.0 / 3866852212004.0, 940440206406.0 / 7593089888465.0,
+             961109811699.0 / 6734810228204.0, g, 0, 0},
+            {a7, a7, -3039402635899.0 / 4450598839912.0, -1829510709469.0 / 31102090912115.0,
+             -286320471013.0 / 6931253422520.0, 8651533662697.0 / 9642993110008.0, g, 0},
+            {0, 0, b83, b84, b85, b86, b87, g}},
+           {{0, 0, 0, 0, 0, 0, 0, 0},
+            {4.0 / 9.0, 0, 0, 0, 0, 0, 0, 0},
+            {1.0 / 9.0, 1183333538310.0 / 1827251437969.0, 0, 0, 0, 0, 0, 0},
+            {895379019517.0 / 9750411845327.0, 477606656805.0 / 13473228687314.0,
+             -112564739183.0 / 9373365219272.0, 0, 0, 0, 0, 0},
+            {-4458043123994.0 / 13015289567637.0, -2500665203865.0 / 9342069639922.0,
+             983347055801.0 / 8893519644487.0, 2185051477207.0 / 2551468980502.0, 0, 0, 0, 0},
+            {-167316361917.0 / 17121522574472.0, 1605541814917.0 / 7619724128744.0,
+             991021770328.0 / 13052792161721.0, 2342280609577.0 / 11279663441611.0,
+             3012424348531.0 / 12792462456678.0, 0, 0, 0},
+            {6680998715867.0 / 14310383562358.0, 5029118570809.0 / 3897454228471.0,
+             2415062538259.0 / 6382199904604.0, -3924368632305.0 / 6964820224454.0,
+             -4331110370267.0 / 15021686902756.0, -3944303808049.0 / 11994238218192.0, 0, 0},
+            {2193717860234.0 / 3570523412979.0, 2193717860234.0 / 3570523412979.0,
+             5952760925747.0 / 18750164281544.0, -4412967128996.0 / 6196664114337.0,
+             4151782504231.0 / 36106512998704.0, 572599549169.0 / 6265429158920.0,
+             -457874356192.0 / 11306498036315.0, 0}});
+      ass({0, 0, b83, b84, b85, b86, b87, g});
+    } break;
     default:
       return false;
   }
@@ -1224,30 +1343,20 @@ extern "C" int pz_integ_operator(int n_r_max, double radratio, int which, double
 extern "C" int pz_explicit_terms(pz_handle* h, int inst, const double* us, const double* up, const double* om,
                                  const double* temp, double* dTdt_expl, double* dpsidt_expl, double* dtr,
                                  double* dth) {
-  if (!h) return fail(nullptr, PZ_E_ARG, "pz_explicit_terms: null handle");
-  if (inst < 0 || inst >= h->n_inst) return fail(h, PZ_E_ARG, "pz_explicit_terms: instance out of range");
-  if (!us || !up || !om || !temp || !dTdt_expl || !dpsidt_expl || !dtr || !dth)
-    return fail(h, PZ_E_ARG, "pz_explicit_terms: null array");
-  const PzInst& I = h->inst[inst];
-  void* scratch = nullptr;
-  const size_t bytes = pz_expl_scratch_bytes(I.N, I.M);
-  cudaError_t e = cudaMallocAsync(&scratch, bytes, h->stream);
-  if (e) return cuda_fail(h, e, "pz_explicit_terms scratch");
+  // the same argument checks as pz_explicit_terms_noalloc (collocation
+  // instances without composition), then scratch from the handle's stream
   PzExplArgs a;
-  a.inst = h->d_inst + inst;
-  a.pool = h->pool;
-  a.us = reinterpret_cast<const double2*>(us);
-  a.up = reinterpret_cast<const double2*>(up);
-  a.om = reinterpret_cast<const double2*>(om);
-  a.temp = reinterpret_cast<const double2*>(temp);
-  a.dTdt = reinterpret_cast<double2*>(dTdt_expl);
-  a.dpsidt = reinterpret_cast<double2*>(dpsidt_expl);
-  a.dtr = dtr;
-  a.dth = dth;
+  int N = 0, M = 0, P = 0;
+  cudaStream_t s = nullptr;
+  const int rc = pz_expl_args(h, inst, us, up, om, temp, dTdt_expl, dpsidt_expl, dtr, dth, &a, &N, &M, &P, &s);
+  if (rc != PZ_OK) return rc;
+  void* scratch = nullptr;
+  cudaError_t e = cudaMallocAsync(&scratch, pz_expl_scratch_bytes(N, M), s);
+  if (e) return cuda_fail(h, e, "pz_explicit_terms scratch");
   a.s_dVsT = reinterpret_cast<double2*>(scratch);
-  a.s_dVsOm = a.s_dVsT + (size_t)I.N * I.M;
-  e = pz_launch_explicit_terms(a, I.N, I.M, I.P, h->stream);
-  const cudaError_t e2 = cudaFreeAsync(scratch, h->stream);
+  a.s_dVsOm = a.s_dVsT + (size_t)N * M;
+  e = pz_launch_explicit_terms(a, N, M, P, s);
+  const cudaError_t e2 = cudaFreeAsync(scratch, s);
   if (e) return cuda_fail(h, e, "pz_explicit_terms");
   if (e2) return cuda_fail(h, e2, "pz_explicit_terms scratch release");
   return PZ_OK;
@@ -1256,10 +1365,10 @@ extern "C" int pz_explicit_terms(pz_handle* h, int inst, const double* us, const
 int pz_expl_args(pz_handle* h, int inst, const double* us, const double* up, const double* om, const double* temp,
                  double* dTdt_expl, double* dpsidt_expl, double* dtr, double* dth, PzExplArgs* a, int* N, int* M,
                  int* P, cudaStream_t* s) {
-  if (!h) return fail(nullptr, PZ_E_ARG, "null handle");
-  if (inst < 0 || inst >= h->n_inst) return fail(h, PZ_E_ARG, "instance out of range");
+  if (!h) return fail(nullptr, PZ_E_ARG, "explicit terms entry point: null handle");
+  if (inst < 0 || inst >= h->n_inst) return fail(h, PZ_E_ARG, "explicit terms entry point: instance out of range");
   if (!us || !up || !om || !temp || !dTdt_expl || !dpsidt_expl || !dtr || !dth)
-    return fail(h, PZ_E_ARG, "null array");
+    return fail(h, PZ_E_ARG, "explicit terms entry point: null array");
   const PzInst& I = h->inst[inst];
   if (I.flags & PZF_INTEG)
     return fail(h, PZ_E_UNSUPPORTED, "explicit terms entry point: collocation instances only (cheb_method 'integ')");

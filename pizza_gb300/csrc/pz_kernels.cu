@@ -1768,6 +1768,11 @@ __global__ void k_init_state(PzDev d, int only) {
   S.lMatNext = 1;
   S.l_calc_lin = 1;
   d.state[inst] = S;
+  // dummy Courant steps of the time loop's start (step_time.f90:124-125): a
+  // scheme whose first stage skips the radial loop (l_exp_calc(1) false)
+  // takes its first dt_courant from these
+  double* cfl = d.pool + I.o_cfl;
+  for (int r = 0; r < 2 * I.N; ++r) cfl[r] = 1.0e10;
 }
 
 // latest time-series row of every instance into a contiguous buffer

@@ -394,9 +394,13 @@ def map_field(f, n_m_max: int, n_r_max: int, phys: bool, lbc: bool = False):
     return out
 
 
-def restart_from_checkpoint(ens, i: int, path: str):
+def restart_from_checkpoint(ens, i: int, path: str, temp_add=None, xi_add=None):
     """Start instance i from a checkpoint as read_checkpoint and
     get_start_fields do (src/checkpoints.f90:185-860, src/init_fields.f90:54-258):
+    temp_add / xi_add (complex (n_m_max, n_r_max), or None) are added to the
+    mapped temperature / composition before the state is set, as
+    get_start_fields applies initProp after reading a checkpoint
+    (init_fields.f90:121-123);
     fields and multistep history slots 2..n mapped onto the instance's grid
     (map_field), dt filled with the oldest value where the instance's scheme
     keeps more, time; the first old/implicit slots are recomputed from the
@@ -415,9 +419,14 @@ def restart_from_checkpoint(ens, i: int, path: str):
     coll = "COLL" in c.cheb_method.upper()
     coll_old = bool(h["l_cheb_coll"])
     chem = c.raxi != 0.0 and h["l_chem"]
+    temp = map_field(ck["temp"], mm, n, True)
+    if temp_add is not None:
+        temp = temp + temp_add
+    xi = map_field(ck["xi"], mm, n, True) if chem else None
+    if xi_add is not None and c.raxi != 0.0:
+        xi = xi_add if xi is None else xi + xi_add
     ens.set_state(i, us=map_field(ck["us"], mm, n, True), up=map_field(ck["up"], mm, n, True),
-                  temp=map_field(ck["temp"], mm, n, True),
-                  xi=map_field(ck["xi"], mm, n, True) if chem else None)
+                  temp=temp, xi=xi)
     if h["family"] == "MULTISTEP" and family == "MULTISTEP":
         counts = {2: nexp, 1: nimp, 0: nold}
         order = _hist_order(h["nexp"], h["nimp"], h["nold"])
@@ -455,6 +464,8 @@ def _scheme_counts(ens, i):
         nexp, nimp, nold = multistep[ts]
         return nexp, nimp, nold, "MULTISTEP"
     stages = {"ARS222": 2, "ARS232": 3, "ARS233": 3, "SSP222": 3, "LSDIRK222": 3, "LZ232": 2, "CK232": 2,
-              "ARS443": 4, "BPR353": 4, "PC2": 3, "ARS343": 4, "MARS343": 4, "SSP322": 4, "SSP332": 4}
+              "ARS443": 4, "BPR353": 4, "PC2": 3, "ARS343": 4, "MARS343": 4, "SSP322": 4, "SSP332": 4,
+              "SSP433": 5, "DP1-242": 4, "DP2-242": 4, "LZ453": 4, "KC343": 4, "KC564": 6, "KC785": 8,
+              "DBM453": 5}
     ns = stages[ts]
     return ns, ns, 1, "DIRK"

@@ -1,7 +1,7 @@
 """Golden frame for pizza_gb300.pizza_io.write_frame: a small deterministic
 field written by the library's writer and read back by the reference's own
-reader (python/pizza/frame.py of a magic-sph/pizza checkout, default: the
-read-only mount given by --ref), whose parsed values are stored next to the
+reader (python/pizza/frame.py of the magic-sph/pizza tree given by --ref,
+read only), whose parsed values are stored next to the
 file.  The reader imports matplotlib for plotting helpers that reading does
 not use; a stand-in module is installed for the import only.
 
@@ -33,7 +33,7 @@ def sample():
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--ref", default="/root/reference")
+    ap.add_argument("--ref", required=True, help="root of the pizza source tree (read only)")
     args = ap.parse_args()
     from pizza_gb300.pizza_io import write_frame
     header, field = sample()

@@ -1,7 +1,7 @@
 """Extract the reference's regression fixtures used to pin the oracle.
 
 Reads ``samples/<Case>/reference.out`` from a checkout of magic-sph/pizza
-(default: the read-only mount given by --ref) and writes the rows that come
+(the tree given by --ref, read only) and writes the rows that come
 from the collocation runs into ``tests/golden/<Case>.txt``, together with the
 namelist values of the run that produced them (``tests/golden/cases.json``).
 
@@ -91,7 +91,7 @@ CASES = {
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--ref", default="/root/reference")
+    ap.add_argument("--ref", required=True, help="root of the pizza source tree (read only)")
     args = ap.parse_args()
     here = os.path.dirname(os.path.abspath(__file__))
     meta = {}

@@ -191,6 +191,23 @@ def test_explicit_terms_entry_point_matches_oracle(pz):
         np.testing.assert_allclose(out[3].cpu().numpy(), sim.dth, rtol=1e-12)
 
 
+@pytest.mark.parametrize("noalloc", [False, True])
+def test_explicit_terms_entry_points_refuse_integ_and_composition(pz, noalloc):
+    """Both stage-level entry points serve collocation instances without
+    composition; an integration-method or composition instance is refused the
+    same way by each (PZ_E_UNSUPPORTED), not run on collocation kernels."""
+    import torch
+    specs = [dict(n_r_max=33, m_max=32, ek=1e-3, ra=1e5, dtMax=1e-4, cheb_method="INTEG", matrix_solve="DIRECT"),
+             dict(n_r_max=33, m_max=32, l_non_rot=True, ra=-1e4, pr=0.3, raxi=2e4, sc=3.0, g0=1.0, g1=0.0,
+                  time_scheme="BPR353", dtMax=1e-3)]
+    ens = pz.Ensemble([gpu_config(s) for s in specs])
+    z = torch.zeros((33, 33), dtype=torch.complex128, device="cuda")
+    for i in range(2):
+        with pytest.raises(pz.PizzaError) as e:
+            ens.explicit_terms(i, z, z, z, z, noalloc=noalloc)
+        assert e.value.code == -6, (i, str(e.value))
+
+
 def test_prandtl_not_one_uses_separate_temperature_operator(pz):
     """Pr != 1: the temperature and vorticity operators differ (TdiffFac != ViscFac)."""
     spec = dict(C0, pr=0.7)
@@ -205,3 +222,38 @@ def test_odd_and_even_grids_and_phi_sizes(pz):
                  dict(C0, n_r_max=33, n_cheb_max=30, m_max=32)):    # dealiased n_cheb_max < n_r_max
         sim, ens, out = run_pair(pz, spec, 15, seed=9)
         check_fields(sim, out[-1][2], TOL, str(spec["n_r_max"]))
+
+
+TSC_NML = """&grid
+ n_r_max = 48, n_cheb_max = 48, m_max = 64, minc = 1,
+/
+&control
+ tag = "tsc", l_newmap = .false., time_scheme = "SBDF3", n_time_steps = 2000,
+ dtMax = 5d-4, courfac = 2.5d0, l_non_rot = .true., matrix_solve = 'influence', n_fft_optim_lev = 2,
+/
+&phys_param
+ ra = 1.0E+04, pr = 1.0E+00, ek = 1.00E-03, radratio = 3.50E-01, g0 = 1.00E+00, g1 = 0.00E+00,
+ g2 = 0.00E+00, ktopt = 1, kbott = 1, ktopv = 2, kbotv = 2,
+/
+&start_field
+ l_start_file = .false., start_file = "checkpoint_end.testB", init_t = -1, amp_t = 1.0e-2,
+ init_u = 0, amp_u = 3.0e-4,
+/
+&output_control
+ n_log_step = 100, n_frames = 1,
+/
+"""
+
+
+def test_driver_runs_timestepchange_namelist(pz, tmp_path):
+    """python -m pizza_gb300.run on the TimeStepChange input (the bubble start,
+    init_t = -1, built by the library's own initProp): its e_kin file
+    reproduces the reference fixture rows."""
+    from pizza_gb300.run import run
+    nml = tmp_path / "input.nml"
+    nml.write_text(TSC_NML)
+    run(str(nml), str(tmp_path))
+    got = np.loadtxt(tmp_path / "e_kin.tsc")[:, :4]
+    ref = np.loadtxt(os.path.join(HERE, "golden", "TimeStepChange.txt"))
+    assert got.shape == ref.shape
+    np.testing.assert_allclose(got, ref, rtol=1e-8, atol=1e-14)

@@ -45,15 +45,25 @@ def reference():
     return _run("ARS443", 256)
 
 
-@pytest.mark.parametrize("name,order", [("ARS222", 2), ("LZ232", 2), ("ARS443", 3), ("BPR353", 3)])
+@pytest.mark.parametrize("name,order", [("ARS222", 2), ("LZ232", 2), ("ARS443", 3), ("BPR353", 3),
+                                        ("DP2-242", 2), ("LZ453", 3)])
 def test_convergence_order(reference, name, order):
     e = [np.abs(_run(name, n).temp - reference.temp).max() for n in (16, 32)]
     assert np.log2(e[0] / e[1]) > order - 0.3, e
 
 
-def test_assembly_scheme_temperature_converges(reference):
-    """ARS233 ends with pizza's assembly stage; its temperature converges at
-    better than second order (the velocity has the assembly's vorticity
-    projection at the walls)."""
-    e = [np.abs(_run("ARS233", n).temp - reference.temp).max() for n in (16, 32)]
+@pytest.mark.parametrize("name", ["ARS233", "KC343", "KC564"])
+def test_assembly_scheme_temperature_converges(reference, name):
+    """ARS233 and the Kennedy-Carpenter schemes end with pizza's assembly
+    stage; their temperature converges at better than second order (the
+    velocity has the assembly's vorticity projection at the walls)."""
+    e = [np.abs(_run(name, n).temp - reference.temp).max() for n in (16, 32)]
     assert np.log2(e[0] / e[1]) > 2.0, e
+
+
+def test_ssp433_literals_are_single_precision():
+    """dirk_schemes.f90 writes SSP433's alpha, beta and eta without a kind:
+    they are single-precision literals widened to double."""
+    t = dirk_tableau("SSP433")
+    assert t["gamma"] == float(np.float32(0.24169426078821))
+    assert t["gamma"] != 0.24169426078821
