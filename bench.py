@@ -81,10 +81,15 @@ def gpu_cfg(spec):
 
 
 # ---------------------------------------------------------------------------
-# algorithmic work per launch of the per-m solve kernel (k_mloop)
+# algorithmic work of the step's kernels
 # ---------------------------------------------------------------------------
+OZ_S = 7            # bf16 slices per FP64 operand in the tensor-core stage (pz_fast.h)
+FAST_G = 8          # instances per k_fast block
+
+
 def mloop_work(specs, nold=1, nimp=1, nexp=2):
-    """Algorithmic HBM bytes and FP64 flops of one k_mloop launch over the batch.
+    """Algorithmic HBM bytes and FP64 flops of one dense stage launch
+    (k_mloop / k_build_mloop) over the batch.
 
     Per (instance, m): the per-m operators (the vorticity operator, which at
     Pr = 1 is also the temperature operator, and the streamfunction operator;
@@ -99,7 +104,7 @@ def mloop_work(specs, nold=1, nimp=1, nexp=2):
     streamfunction operator K once) and 7 products with the parity-compact
     Chebyshev operators (2N^2 flops each: D1p of dVsT and dVsOm, C and D1c of
     T and of psi, C of omega); m = 0: 2 dense (temperature, u_phi) and 6
-    compact.  Elementwise work is neglected.
+    compact.  Elementwise work and operator rebuilds are neglected.
     """
     byts = 0.0
     flops = 0.0
@@ -114,6 +119,58 @@ def mloop_work(specs, nold=1, nimp=1, nexp=2):
     for N in sizes:
         byts += 8.0 * 4 * N * N
     return byts, flops
+
+
+def fast_work(specs, G=FAST_G, S=OZ_S):
+    """Work of one k_fast launch over the batch (every instance on the fast
+    path): (FP64-equivalent flops, bf16 mma flops issued, HBM bytes).
+
+    Per (instance, m), with n = N - 2 interior points, the stage applies
+    D1p (N x N) to 4 real columns (dVsT, dVsOm), U^-1 (n x n) to 2 + 2
+    (temperature, vorticity right-hand sides), [U; D1p U] ((n+N) x n) to 2 and
+    [U; K U; D1p K U] ((2n+N) x n; m = 0: [U; D1p U]) to 2: 2 R K flops per
+    real column is the FP64-equivalent work.  A block serves G instances of
+    one (N, m); its mma.sync m16n8k16 count per product is
+    ceil(R/16) ceil(K/16) * S(S+1)/2 slice pairs * ceil(C/8) column tiles
+    (C = 4g or 2g real columns for g instances), 4096 flops each.  HBM bytes
+    are the state the stage reads and writes (the operators, shared per
+    (N, m), come from L2): per (instance, m) 28 complex N-vectors.
+    """
+    def t16(x):
+        return (x + 15) // 16
+    pairs = S * (S + 1) // 2
+    f64 = mma = byts = 0.0
+    groups = {}
+    for s in specs:
+        N, M = s["n_r_max"], s["m_max"] + 1
+        n = N - 2
+        for m in range(M):
+            f64 += 2.0 * (4 * N * N + 4 * n * n + 2 * (n + N) * n + 2 * ((2 * n + N) if m else (n + N)) * n)
+            byts += 16.0 * N * 28
+            key = (N, m, s["ek"] if m == 0 else None)      # m = 0 groups share their u_phi operator
+            groups[key] = groups.get(key, 0) + 1
+    for (N, m, _), cnt in groups.items():
+        n = N - 2
+        r3 = (2 * n + N) if m else (n + N)
+        for a in range(0, cnt, G):
+            g = min(G, cnt - a)
+            tiles = (t16(N) * t16(N) * ((4 * g + 7) // 8) + 2 * t16(n) * t16(n) * ((2 * g + 7) // 8) +
+                     (t16(n + N) + t16(r3)) * t16(n) * ((2 * g + 7) // 8))
+            mma += 4096.0 * pairs * tiles
+    return f64, mma, byts
+
+
+def rloop_work(specs):
+    """FP64 flops of one k_rloop launch: per (instance, radius) four complex
+    FFTs of length P (two to the grid, two back), counted as 5 P log2 P each,
+    the grid products and Courant squares (8 P) and the spectral packing and
+    -i m / r post-multiply (20 M)."""
+    f = 0.0
+    for s in specs:
+        N, M = s["n_r_max"], s["m_max"] + 1
+        P = 3 * s["m_max"]
+        f += N * (4 * 5.0 * P * math.log2(P) + 8.0 * P + 20.0 * M)
+    return f
 
 
 # ---------------------------------------------------------------------------
@@ -187,23 +244,12 @@ def measured_peaks():
         return 6800.0, "fallback"
 
 
-def fp64_gemm_peak():
-    """FP64 throughput of cuBLAS DGEMM on this GPU (TFLOP/s), the FP64 ceiling."""
-    import torch
-    n = 4096
-    a = torch.randn(n, n, dtype=torch.float64, device="cuda")
-    b = torch.randn(n, n, dtype=torch.float64, device="cuda")
-    torch.matmul(a, b)
-    torch.cuda.synchronize()
-    best = 1e30
-    for _ in range(3):
-        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        e0.record()
-        torch.matmul(a, b)
-        e1.record()
-        e1.synchronize()
-        best = min(best, e0.elapsed_time(e1))
-    return 2.0 * n ** 3 / (best * 1e-3) / 1e12
+def measured_bf16_peak():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return float(json.load(f)["bf16_tflops"])
+    except Exception:
+        return 1900.0
 
 
 # ---------------------------------------------------------------------------
@@ -526,42 +572,77 @@ def main():
         ms = float(t.item())
     value = world * len(specs) * args.steps / (ms * 1e-3)
 
-    # ---- per-kernel device times (launched one by one, CUDA events)
-    kms = ens.profile_steps(max(3, min(10, args.steps)))
+    # ---- per-kernel device times over the same steps as the timed window:
+    # the same start state and warm-up, then the timed window's steps with
+    # the kernels launched one by one between CUDA events
+    ens.set_state_all(temps)
+    ens.step(args.warmup)
+    kms = ens.profile_steps(args.steps)
     dom = max(kms, key=kms.get)
-    byts, flops = mloop_work(specs)
-    peak, peak_kind = measured_peaks()
-    # the per-m stage kernel: k_build_mloop (operator rebuild of the instances
-    # whose dt changed, fused with the first stage) when the plan fuses them
-    stage_kernel = "k_build_mloop" if kms.get("k_build_mloop", 0.0) > 0.0 else "k_mloop"
-    mloop_ms = kms[stage_kernel]
-    achieved = byts / (mloop_ms * 1e-3) / 1e9
+    hbm_peak, peak_kind = measured_peaks()
     try:
-        fp64_peak = fp64_gemm_peak()
+        dfma_peak, mma_peak = pz.probe_peaks()
     except Exception:
-        fp64_peak = None
+        dfma_peak, mma_peak = None, None
+    bf16_peak = measured_bf16_peak()
+    kernels = {}
+    if kms.get("k_rloop", 0.0) > 0.0:
+        f = rloop_work(specs)
+        a_t = f / (kms["k_rloop"] * 1e-3) / 1e12
+        kernels["k_rloop"] = {"bound": "fp64", "achieved": a_t, "peak": dfma_peak, "unit": "TFLOP/s",
+                              "frac": a_t / dfma_peak if dfma_peak else None,
+                              "work": f, "work_note": "4 complex FFTs of length n_phi_max per (instance, radius) "
+                                                      "at 5 P log2 P flops, plus 8 P + 20 M elementwise",
+                              "peak_kind": "DFMA issue rate measured in this run (pz_probe_peaks)"}
+    if kms.get("k_fast", 0.0) > 0.0:
+        f64, mma, fb = fast_work(specs)
+        t = kms["k_fast"] * 1e-3
+        kernels["k_fast"] = {"bound": "tensor", "achieved": mma / t / 1e12, "peak": mma_peak, "unit": "TFLOP/s",
+                             "frac": (mma / t / 1e12 / mma_peak) if mma_peak else None,
+                             "frac_of_tcgen05_bf16": mma / t / 1e12 / bf16_peak,
+                             "mma_flops": mma, "fp64_equivalent_tflops": f64 / t / 1e12,
+                             "fp64_equivalent_flops": f64,
+                             "hbm": {"achieved": fb / t / 1e9, "peak": hbm_peak, "unit": "GB/s",
+                                     "frac": fb / t / 1e9 / hbm_peak, "bytes": fb},
+                             "peak_kind": "bf16 mma.sync issue rate measured in this run (pz_probe_peaks); "
+                                          "frac_of_tcgen05_bf16 against MEASURED_PEAKS bf16_tflops"}
+    for name in ("k_build_mloop", "k_mloop"):
+        if kms.get(name, 0.0) > 0.0:
+            byts, flops = mloop_work(specs)
+            t = kms[name] * 1e-3
+            kernels[name] = {"bound": "fp64", "achieved": flops / t / 1e12, "peak": dfma_peak, "unit": "TFLOP/s",
+                             "frac": flops / t / 1e12 / dfma_peak if dfma_peak else None,
+                             "hbm": {"achieved": byts / t / 1e9, "peak": hbm_peak, "unit": "GB/s",
+                                     "frac": byts / t / 1e9 / hbm_peak,
+                                     "traffic": MLOOP_TRAFFIC_PER_ALGO_BYTE * byts}}
+    roof = dict(kernels.get(dom, {}))
+    roof["kernel"] = dom
+    roof["traffic"] = None
+    roof["traffic_note"] = ("DRAM bytes of the dominant kernel per launch: profiles/ holds the ncu summaries; "
+                            "this line does not re-derive them")
+    roof["peaks"] = {"dfma_tflops": dfma_peak, "mma_bf16_tflops": mma_peak, "hbm_gbs": hbm_peak,
+                     "hbm_kind": peak_kind, "tcgen05_bf16_tflops": bf16_peak}
 
-    # ---- e2e through the C ABI with host buffers
+    # ---- e2e through the C ABI with host buffers; the rows of every step land
+    # in a preallocated array (one D2H per step), counted after the window
     ens2 = pz.Ensemble([gpu_cfg(s) for s in specs])
-    rows = np.zeros((len(specs), pz.SERIES_COLS))
+    rows_all = np.zeros((args.steps, len(specs), pz.SERIES_COLS))
     state_bytes = sum(t.size * 16 for t in temps)
     t0 = time.perf_counter()
     ens2.set_state_all(temps)
-    n_dt_changes, prev_dt = 0, None
-    for _ in range(args.steps):
+    for k in range(args.steps):
         ens2.step(1, sync=False)
-        ens2.latest_rows(rows)
-        if prev_dt is not None:
-            n_dt_changes += int(np.count_nonzero(rows[:, 15] != prev_dt))
-        prev_dt = rows[:, 15].copy()
+        ens2.latest_rows(rows_all[k])
     ens2.sync()
     e2e_wall = time.perf_counter() - t0
     ens2.close()
+    n_dt_changes = int(np.count_nonzero(rows_all[1:, :, 15] != rows_all[:-1, :, 15]))
     e2e = {"value": world * len(specs) * args.steps / e2e_wall, "unit": UNIT,
            "h2d_bytes_per_step": int(state_bytes // args.steps),
-           "d2h_bytes_per_step": int(rows.nbytes),
-           "note": "set_state_all from host arrays, then per step pz_step + pz_latest_rows (one D2H of every "
-                   "instance's e_kin/heat row); wall clock"}
+           "d2h_bytes_per_step": int(rows_all[0].nbytes),
+           "note": "timed on the host clock: set_state_all from host arrays (the one-time upload, amortised over "
+                   "the steps in h2d_bytes_per_step), then per step pz_step + pz_latest_rows (one D2H of every "
+                   "instance's e_kin/heat row into a preallocated host array), then pz_sync"}
 
     plain = None
     if not args.no_plain:
@@ -593,16 +674,10 @@ def main():
         "batched_over_plain": (value / world / plain["value"]) if plain else None,
         "plain_detail": plain,
         "kernel_ms_per_step": kms,
-        "roofline": {"bound": "hbm", "kernel": stage_kernel, "achieved": achieved, "peak": peak, "unit": "GB/s",
-                     "frac": achieved / peak, "peak_kind": peak_kind,
-                     "traffic": MLOOP_TRAFFIC_PER_ALGO_BYTE * byts,
-                     "traffic_note": "DRAM bytes per launch, ncu capture of the 16-instance ensemble scaled by "
-                                     "algorithmic bytes; achieved counts the stage's bytes only, not the "
-                                     "rebuilt operators' writes",
-                     "algorithmic_bytes": byts,
-                     "fp64": {"achieved_tflops": flops / (mloop_ms * 1e-3) / 1e12, "peak_tflops": fp64_peak,
-                              "peak_kind": "cuBLAS DGEMM 4096^3 measured in this run",
-                              "frac": (flops / (mloop_ms * 1e-3) / 1e12 / fp64_peak) if fp64_peak else None}},
+        "kernel_ms_note": "device ms per step of each kernel over the timed window's steps (same start state "
+                          "and warm-up), launched one by one between CUDA events",
+        "roofline": roof,
+        "kernel_rooflines": kernels,
         "dominant_kernel": dom,
         "operator_rebuilds_per_step": n_dt_changes / max(1, args.steps - 1),
         "adjoint": adj,

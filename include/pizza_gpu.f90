@@ -41,10 +41,11 @@ module pizza_gpu
    integer(c_int), parameter :: PZ_CHEB_COLL = 0, PZ_CHEB_INTEG = 1
    integer(c_int), parameter :: PZ_TS_VISC = 0, PZ_TS_ROT = 1
    integer(c_int), parameter :: PZ_SERIES_COLS = 22
-   integer(c_int), parameter :: PZ_KERNEL_KINDS = 9
+   integer(c_int), parameter :: PZ_KERNEL_KINDS = 10
    integer(c_int), parameter :: PZ_NOALLOC_MAX_MN = 32768
    integer(c_int), parameter :: PZ_OBJ_EKIN3D = 0, PZ_OBJ_NUTOP = 1
    integer(c_int), parameter :: PZ_INTEG_OPS = 19
+   integer(c_int), parameter :: PZ_TUNE_FAST_G = 0, PZ_TUNE_RLOOP_RG = 1
 
    ! One instance's namelist values, the C struct pz_config field by field.
    type, bind(c) :: pz_config
@@ -280,6 +281,29 @@ module pizza_gpu
          real(c_double), intent(out) :: out(*)
          integer(c_int), intent(out) :: bandwidth
       end function pz_integ_operator
+
+      integer(c_int) function pz_fast_path(enable) bind(c, name='pz_fast_path')
+         import :: c_int
+         integer(c_int), value :: enable
+      end function pz_fast_path
+
+      integer(c_int) function pz_tune_set(what, key, value) bind(c, name='pz_tune_set')
+         import :: c_int
+         integer(c_int), value :: what, key, value
+      end function pz_tune_set
+
+      integer(c_int) function pz_fast_eigen(n_r_max, radratio, m, lam, U) bind(c, name='pz_fast_eigen')
+         import :: c_int, c_double
+         integer(c_int), value :: n_r_max
+         real(c_double), value :: radratio
+         integer(c_int), value :: m
+         real(c_double), intent(out) :: lam(*), U(*)
+      end function pz_fast_eigen
+
+      integer(c_int) function pz_probe_peaks(dfma_tflops, mma_bf16_tflops) bind(c, name='pz_probe_peaks')
+         import :: c_int, c_double
+         real(c_double), intent(out), optional :: dfma_tflops, mma_bf16_tflops
+      end function pz_probe_peaks
 
       integer(c_int) function pz_destroy(h) bind(c, name='pz_destroy')
          import :: c_ptr, c_int

@@ -239,7 +239,7 @@ void* pz_stream(pz_handle* h);
  * events between them on the handle's stream; kernel_ms[k] receives the mean
  * device time per step of kernel kind k (k < PZ_KERNEL_KINDS, summed over the
  * stages of a DIRK step), names in pz_kernel_name(k).  Synchronises. */
-#define PZ_KERNEL_KINDS 9
+#define PZ_KERNEL_KINDS 10
 int pz_step_profile(pz_handle* h, int n_steps, double* kernel_ms);
 const char* pz_kernel_name(int k);
 
@@ -339,6 +339,49 @@ int pz_set_ra(pz_handle* h, int inst, double ra);
  * column-major; *bandwidth: max |i-j| of a nonzero entry. */
 #define PZ_INTEG_OPS 19
 int pz_integ_operator(int n_r_max, double radratio, int which, double* out, int* bandwidth);
+
+/* No counterpart in the reference.  Process-wide choice, for handles created
+ * afterwards, of the tensor-core stage: with enable = 1 (the default) every
+ * instance that runs the collocation step with the influence-matrix solve
+ * and CNAB2 (fixed-temperature, no-slip walls, no composition,
+ * n_cheb_max = n_r_max <= 97) solves its per-m systems in the eigenbasis of
+ * its dt-independent operator, with all operator products on bf16 tensor
+ * cores as an exact FP64 emulation; enable = 0 keeps every instance on the
+ * dense FP64 kernels.  Both give the reference's step to FP64 rounding.
+ * enable < 0 only queries.  Returns the previous setting.  The adjoint
+ * entry points always run the dense kernels. */
+int pz_fast_path(int enable);
+
+/* No counterpart in the reference (pizza chooses its MPI transpose variant
+ * by timing, src/communications.f90:407-516; this is the same idea for the
+ * kernels' launch shapes).  Process-wide tuning table read by pz_create for
+ * handles created afterwards:
+ *  - PZ_TUNE_FAST_G: instances of one (n_r_max, m) per block of the
+ *    tensor-core stage (key ignored; value 1..16, <= 0 restores the default 8);
+ *  - PZ_TUNE_RLOOP_RG: radii per block of the phi-transform kernel for
+ *    n_phi_max = key (value 1..16 within its shared memory; <= 0 restores the
+ *    default clamp(576 / n_phi_max, 1, 8)).
+ * pizza_gb300.autotune times the candidates on the device and applies the
+ * winners.  PZ_E_ARG for an unknown parameter or a value out of range. */
+#define PZ_TUNE_FAST_G   0
+#define PZ_TUNE_RLOOP_RG 1
+int pz_tune_set(int what, int key, int value);
+
+/* No counterpart in the reference.  Eigen-decomposition the tensor-core
+ * stage uses for mode m of an n_r_max grid (host only, no device needed):
+ * the Laplacian D2 + r^-1 D - m^2 r^-2 on the n = n_r_max - 2 interior
+ * collocation points with Dirichlet walls, P = U diag(lam) U^-1.  lam: n
+ * doubles, U: n x n row-major (columns of max-norm 1).  PZ_E_SINGULAR when
+ * the decomposition fails (then the instance would use the dense kernels). */
+int pz_fast_eigen(int n_r_max, double radratio, int m, double* lam, double* U);
+
+/* No counterpart in the reference.  Measured peak issue rates of the current
+ * device for the pipes the step runs on, for rooflines: FP64 fused
+ * multiply-add (the phi-FFTs and the dense FP64 kernels) and bf16
+ * mma.sync m16n8k16 with fp32 accumulation (the tensor-core stage), in
+ * TFLOP/s (2 flops per FMA).  Runs two probe kernels of some tens of ms on
+ * the default stream; either pointer may be NULL. */
+int pz_probe_peaks(double* dfma_tflops, double* mma_bf16_tflops);
 
 /* Release all device memory of the handle. */
 int pz_destroy(pz_handle* h);

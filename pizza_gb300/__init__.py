@@ -30,7 +30,7 @@ SCHEMES = {"CNAB2": 0, "SBDF2": 1, "BDF2AB2": 1, "SBDF3": 2, "BDF3AB3": 2, "SBDF
            "CK232": 16, "ARS443": 17, "BPR353": 18, "PC2": 19, "ARS343": 20, "MARS343": 21,
            "SSP322": 22, "SSP332": 23, "SSP433": 24, "DP1-242": 25, "DP2-242": 26, "LZ453": 27,
            "KC343": 28, "KC564": 29, "KC785": 30, "DBM453": 31}
-KERNEL_KINDS = 9
+KERNEL_KINDS = 10
 SOLVE_INFLUENCE, SOLVE_DIRECT = 0, 1
 CHEB_COLL, CHEB_INTEG = 0, 1
 TS_VISC, TS_ROT = 0, 1
@@ -189,6 +189,10 @@ def load_library(path: str | None = None):
     lib.pz_set_restart_ab1.argtypes = [vp, ctypes.c_int, ctypes.c_int]
     lib.pz_get_spectra.argtypes = [vp, ctypes.c_int, dp]
     lib.pz_integ_operator.argtypes = [ctypes.c_int, ctypes.c_double, ctypes.c_int, dp, ctypes.POINTER(ctypes.c_int)]
+    lib.pz_fast_path.argtypes = [ctypes.c_int]
+    lib.pz_probe_peaks.argtypes = [dp, dp]
+    lib.pz_tune_set.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int]
+    lib.pz_fast_eigen.argtypes = [ctypes.c_int, ctypes.c_double, ctypes.c_int, dp, dp]
     lib.pz_destroy.argtypes = [ctypes.c_void_p]
     lib.pz_last_error.argtypes = [ctypes.c_void_p]
     lib.pz_last_error.restype = ctypes.c_char_p
@@ -198,7 +202,7 @@ def load_library(path: str | None = None):
               "pz_step_profile", "pz_explicit_terms", "pz_explicit_terms_noalloc", "pz_adjoint_forward",
               "pz_adjoint_backward", "pz_adjoint_grid_snapshots", "pz_set_ra", "pz_get_history", "pz_set_history", "pz_get_step_state",
               "pz_set_step_state", "pz_set_restart_ab1", "pz_get_spectra", "pz_integ_operator",
-              "pz_destroy"):
+              "pz_fast_path", "pz_fast_eigen", "pz_probe_peaks", "pz_tune_set", "pz_destroy"):
         getattr(lib, f).restype = ctypes.c_int
     _lib = lib
     return lib
@@ -218,6 +222,53 @@ def integ_operator(n_r_max: int, radratio: float, name: str):
     if rc != 0:
         raise RuntimeError(lib.pz_last_error(None).decode())
     return out.reshape(n_r_max, n_r_max, order="F"), bw.value
+
+
+def fast_path(enable=None) -> bool:
+    """The tensor-core stage for handles created afterwards (pz_fast_path):
+    ``enable`` True/False sets it, None only queries; returns the previous
+    setting."""
+    lib = load_library()
+    return bool(lib.pz_fast_path(-1 if enable is None else int(bool(enable))))
+
+
+TUNE_FAST_G, TUNE_RLOOP_RG = 0, 1
+
+
+def tune_set(what: int, key: int, value: int):
+    """Process-wide launch-shape table for handles created afterwards
+    (pz_tune_set): TUNE_FAST_G (instances per tensor-core block) or
+    TUNE_RLOOP_RG (radii per transform block for n_phi_max = key); value <= 0
+    restores the default."""
+    lib = load_library()
+    rc = lib.pz_tune_set(int(what), int(key), int(value))
+    if rc != 0:
+        raise PizzaError(rc, lib.pz_last_error(None).decode())
+
+
+def probe_peaks():
+    """(DFMA, bf16 mma.sync) peak issue rates of the current GPU in TFLOP/s,
+    measured by the library's probe kernels (pz_probe_peaks)."""
+    lib = load_library()
+    a, b = np.zeros(1), np.zeros(1)
+    rc = lib.pz_probe_peaks(_dptr(a), _dptr(b))
+    if rc != 0:
+        raise PizzaError(rc, "pz_probe_peaks failed")
+    return float(a[0]), float(b[0])
+
+
+def fast_eigen(n_r_max: int, radratio: float, m: int):
+    """The eigen-decomposition the tensor-core stage uses for mode m (host
+    code, no GPU needed): lam (n,) and U (n, n), n = n_r_max - 2, with
+    (D2 + D/r - m^2/r^2) on the interior points = U diag(lam) U^-1."""
+    lib = load_library()
+    n = n_r_max - 2
+    lam = np.zeros(n)
+    U = np.zeros(n * n)
+    rc = lib.pz_fast_eigen(n_r_max, float(radratio), int(m), _dptr(lam), _dptr(U))
+    if rc != 0:
+        raise PizzaError(rc, lib.pz_last_error(None).decode())
+    return lam, U.reshape(n, n)
 
 
 def _dptr(a):

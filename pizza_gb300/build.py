@@ -17,7 +17,8 @@ CSRC = os.path.join(HERE, "csrc")
 LIBDIR = os.path.join(HERE, "_lib")
 OBJDIR = os.path.join(ROOT, "_build")
 LIB = os.path.join(LIBDIR, "libpizza_gb300.so")
-SOURCES = ["pz_kernels.cu", "pz_stage.cu", "pz_host.cu", "pz_noalloc.cu", "pz_adjoint.cu", "pz_integ_ops.cu"]
+SOURCES = ["pz_kernels.cu", "pz_stage.cu", "pz_host.cu", "pz_noalloc.cu", "pz_adjoint.cu", "pz_integ_ops.cu",
+           "pz_fast.cu", "pz_fast_setup.cu", "pz_probe.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC,-O2", "--expt-relaxed-constexpr",
          "-I" + os.path.join(ROOT, "include"), "-I" + CSRC]

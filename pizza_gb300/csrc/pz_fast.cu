@@ -1,0 +1,540 @@
+// k_fast: the stage of the collocation influence-matrix step on the tensor
+// cores (pz_fast.h explains the method).  One block runs one m for a group of
+// instances of the same (n_r_max, radratio) class: finish_explicit_assembly
+// (src/mloop.f90:169-229 with update_temp_coll.f90:152-176 and
+// update_psi_coll_dmat.f90:468-552), the IMEX right-hand sides
+// (multistep_schemes.f90:308-316), update_temp_co (update_temp_coll.f90:66-150)
+// and update_om_coll_dmat with its influence-matrix correction
+// (update_psi_coll_dmat.f90:126-466), the implicit terms from the solve
+// residual and the new fields.  Every operator product runs as bf16
+// mma.sync on integer slices of the FP64 operands (exact products, FP64 sums).
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+
+#include "pizza_gpu.h"
+#include "pz_device.cuh"
+#include "pz_fast.h"
+#include "pz_internal.h"
+
+namespace {
+
+// ---------------------------------------------------------------------------
+// operand slices in shared memory
+// ---------------------------------------------------------------------------
+// A block of columns for the tensor cores: for each slice s and column j,
+// sw 32-bit words, each holding two consecutive k (bf16, low half = even k).
+// sw = Kpad/2 + 4 keeps the B-fragment loads of a warp on 32 distinct banks.
+struct BOp {
+  uint32_t* w;
+  int* ce;       // per-column power of two: x = sum_s d_s 2^(ce - 8 (s + 1))
+  int C;         // allocated columns (multiple of 16)
+  int sw;        // words per (slice, column)
+};
+
+__device__ __forceinline__ unsigned long long umax64(unsigned long long a, unsigned long long b) {
+  return a > b ? a : b;
+}
+__device__ __forceinline__ unsigned long long warp_umax64(unsigned long long v) {
+  for (int o = 16; o > 0; o >>= 1) {
+    const unsigned lo = __shfl_xor_sync(0xffffffffu, (unsigned)v, o);
+    const unsigned hi = __shfl_xor_sync(0xffffffffu, (unsigned)(v >> 32), o);
+    v = umax64(v, ((unsigned long long)hi << 32) | lo);
+  }
+  return v;
+}
+#define PZ_CE_NONFINITE 0x40000000
+
+__device__ __forceinline__ uint16_t bf16_bits(int d) {
+  return (uint16_t)(__float_as_uint((float)d) >> 16);   // |d| <= 256: exact
+}
+
+// Slice column j (K values x[k * step], k < K; zero past K up to 2 sw) with
+// one warp: the column's power of two from the largest |x| (integer compare
+// of the bit patterns), then x * 2^(56 - ce) rounded to a 56-bit integer and
+// cut into balanced base-256 digits, all in integer arithmetic.
+__device__ void split_col(const BOp& B, int j, const double* x, int step, int K) {
+  const int lane = threadIdx.x & 31;
+  unsigned long long mb = 0;
+  for (int k = lane; k < K; k += 32)
+    mb = umax64(mb, (unsigned long long)__double_as_longlong(x[(long long)k * step]) & 0x7fffffffffffffffULL);
+  mb = warp_umax64(mb);
+  const int ce = mb == 0 ? 0 : (int)((mb >> 52) & 0x7ff) - 1022;
+  // a column holding Inf or NaN is marked so that its products come out NaN
+  // (its digits would otherwise be finite) and the status check sees it
+  if (lane == 0) B.ce[j] = ((mb >> 52) & 0x7ff) == 0x7ff ? PZ_CE_NONFINITE : ce;
+  uint16_t* h = reinterpret_cast<uint16_t*>(B.w);
+  const int kp = 2 * B.sw;
+  for (int k = lane; k < kp; k += 32) {
+    long long X = 0;
+    if (k < K) {
+      const unsigned long long u = (unsigned long long)__double_as_longlong(x[(long long)k * step]);
+      const int E = (int)((u >> 52) & 0x7ff);
+      const long long mant = (long long)(u & 0xfffffffffffffULL) | (E ? (1LL << 52) : 0LL);
+      const int sh = (E ? E : 1) - 1075 + 8 * PZ_OZ_S - ce;
+      if (sh >= 0) X = mant << sh;                                   // sh <= 3
+      else if (sh > -62) X = (mant + (1LL << (-sh - 1))) >> (-sh);
+      if (u >> 63) X = -X;
+    }
+#pragma unroll
+    for (int s = PZ_OZ_S - 1; s > 0; --s) {
+      const long long d = ((X + 128) & 255) - 128;
+      X = (X - d) >> 8;
+      h[((long long)s * B.C + j) * kp + k] = bf16_bits((int)d);
+    }
+    h[(long long)j * kp + k] = bf16_bits((int)X);
+  }
+}
+
+// zero the slices of columns [j0, C)
+__device__ void zero_cols(const BOp& B, int j0) {
+  for (int s = 0; s < PZ_OZ_S; ++s)
+    for (long long q = (long long)j0 * B.sw + threadIdx.x; q < (long long)B.C * B.sw; q += blockDim.x)
+      B.w[(long long)s * B.C * B.sw + q] = 0u;
+  for (int j = j0 + threadIdx.x; j < B.C; j += blockDim.x) B.ce[j] = 0;
+}
+
+__device__ __forceinline__ void mma16816(float* c, const uint4& a, uint32_t b0, uint32_t b1) {
+  asm("mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
+      "{%0,%1,%2,%3};\n"
+      : "+f"(c[0]), "+f"(c[1]), "+f"(c[2]), "+f"(c[3])
+      : "r"(a.x), "r"(a.y), "r"(a.z), "r"(a.w), "r"(b0), "r"(b1));
+}
+
+__device__ __forceinline__ double pow2(int e) {
+  if (e < -1022) return 0.0;
+  if (e > 1023) e = 1023;
+  return __longlong_as_double((long long)(e + 1023) << 52);
+}
+
+// Y[col * ldy + row] = (A X)(row, col), row < op.R, col < C (X = the slices in
+// B).  A warp takes a (16-row tile, NC 8-column tiles) task; for each k tile
+// it loads the NC x PZ_OZ_S B fragments once and every A slice once, and runs
+// the slice pairs kA + kx <= PZ_OZ_S - 1, accumulating the pair sums of equal
+// kA + kx in one fp32 register set (integers below 2^24: exact).
+template <int NC>
+__device__ void oz_mma_t(const PzFastDev& F, const PzOzOp& op, const BOp& B, int C, double* Y, int ldy) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  const int gid = lane >> 2, t = lane & 3;
+  const int CT = (C + 8 * NC - 1) / (8 * NC);
+  const uint4* Af = F.frag + op.frag;
+  const int* ea = F.ex + op.ex;
+  for (int task = warp; task < op.RT * CT; task += nw) {
+    const int rt = task / CT, ct = task - rt * CT;
+    float acc[NC][PZ_OZ_S][4];
+#pragma unroll
+    for (int c = 0; c < NC; ++c)
+#pragma unroll
+      for (int g = 0; g < PZ_OZ_S; ++g)
+#pragma unroll
+        for (int q = 0; q < 4; ++q) acc[c][g][q] = 0.0f;
+    for (int kt = 0; kt < op.KT; ++kt) {
+      uint32_t b[NC][PZ_OZ_S][2];
+#pragma unroll
+      for (int c = 0; c < NC; ++c) {
+        const int col = (ct * NC + c) * 8 + gid;
+#pragma unroll
+        for (int s = 0; s < PZ_OZ_S; ++s) {
+          const uint32_t* p = B.w + ((long long)s * B.C + col) * B.sw + kt * 8 + t;
+          b[c][s][0] = p[0];
+          b[c][s][1] = p[4];
+        }
+      }
+      const uint4* ap = Af + ((long long)(rt * op.KT + kt) * PZ_OZ_S) * 32 + lane;
+#pragma unroll
+      for (int ka = 0; ka < PZ_OZ_S; ++ka) {
+        const uint4 a = __ldg(ap + ka * 32);
+#pragma unroll
+        for (int g = ka; g < PZ_OZ_S; ++g)
+#pragma unroll
+          for (int c = 0; c < NC; ++c) mma16816(acc[c][g], a, b[c][g - ka][0], b[c][g - ka][1]);
+      }
+    }
+#pragma unroll
+    for (int c = 0; c < NC; ++c)
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        const int row = rt * 16 + gid + ((q & 2) ? 8 : 0);
+        const int col = (ct * NC + c) * 8 + 2 * t + (q & 1);
+        if (row < op.R && col < C) {
+          double v = (double)acc[c][PZ_OZ_S - 1][q];
+#pragma unroll
+          for (int g = PZ_OZ_S - 2; g >= 0; --g) v = fma(v, 0.00390625, (double)acc[c][g][q]);
+          const int ce = B.ce[col];
+          Y[(long long)col * ldy + row] =
+              ce == PZ_CE_NONFINITE ? __longlong_as_double(0x7ff8000000000000LL) : v * pow2(ea[row] + ce - 16);
+        }
+      }
+  }
+}
+// two column tiles per task when there are enough tasks for every warp
+__device__ __forceinline__ void oz_mma(const PzFastDev& F, const PzOzOp& op, const BOp& B, int C, double* Y,
+                                       int ldy) {
+  const int nw = blockDim.x >> 5;
+  if (op.RT * ((C + 15) >> 4) >= 2 * nw) oz_mma_t<2>(F, op, B, C, Y, ldy);
+  else oz_mma_t<1>(F, op, B, C, Y, ldy);
+}
+
+__device__ __forceinline__ double2 imex_rhs_f(const View& V, const PzInst& I, const PzState& S, int f, int mi,
+                                               int i) {
+  double2 acc;
+  {
+    const double2 v = V.hist(f, 0, S.r_old, mi)[i];
+    acc = make_double2(S.wimp[0] * v.x, S.wimp[0] * v.y);
+  }
+  for (int k = 1; k < I.nold; ++k) {
+    const double2 v = V.hist(f, 0, (S.r_old + k) % I.nold, mi)[i];
+    acc.x += S.wimp[k] * v.x; acc.y += S.wimp[k] * v.y;
+  }
+  for (int k = 0; k < I.nimp; ++k) {
+    const double2 v = V.hist(f, 1, (S.r_impl + k) % I.nimp, mi)[i];
+    acc.x += S.wimp_lin[k + 1] * v.x; acc.y += S.wimp_lin[k + 1] * v.y;
+  }
+  for (int k = 0; k < I.nexp; ++k) {
+    const double2 v = V.hist(f, 2, (S.r_expl + k) % I.nexp, mi)[i];
+    acc.x += S.wexp[k] * v.x; acc.y += S.wexp[k] * v.y;
+  }
+  return acc;
+}
+
+// shared-memory layout of k_fast for G instances and grids up to N
+struct FastSmem {
+  BOp B;
+  double* R;     // product outputs, column-major
+  double* RT;    // temperature right-hand sides (interior), then the new temperature (interior)
+  double* RW;    // vorticity / u_phi right-hand sides (interior)
+  double* sc;    // per instance: c1 (re, im), c2 (re, im)
+  int* st;       // per instance: active, bad
+};
+__host__ __device__ inline size_t fast_smem_layout(int G, int N, size_t* oR, size_t* oRT, size_t* oRW, size_t* osc,
+                                                   size_t* ost, size_t* oce, int* C, int* sw) {
+  const int n = N - 2;
+  *C = ((4 * G + 15) / 16) * 16;
+  *sw = ((N + 15) / 16) * 8 + 4;
+  size_t o = (size_t)PZ_OZ_S * (*C) * (*sw) * 4;
+  o = (o + 15) & ~(size_t)15;
+  *oce = o; o += (size_t)(*C) * 4;
+  o = (o + 15) & ~(size_t)15;
+  *oR = o;
+  const int rmax = (2 * N > 3 * N - 4) ? 2 * N : 3 * N - 4;
+  o += (size_t)2 * G * rmax * 8;
+  *oRT = o; o += (size_t)2 * G * n * 8;
+  *oRW = o; o += (size_t)2 * G * n * 8;
+  *osc = o; o += (size_t)G * 4 * 8;
+  *ost = o; o += (size_t)G * 2 * 4;
+  return (o + 15) & ~(size_t)15;
+}
+
+__global__ void __launch_bounds__(256, 2) k_fast(PzDev d) {
+  extern __shared__ __align__(16) unsigned char fsm[];
+  const PzFastDev& F = d.fast;
+  const PzFastItem it = F.items[blockIdx.x];
+  const PzFastCls cls = F.cls[it.cls];
+  const int N = cls.N, n = cls.n, mi = it.m, G = F.G, ni = it.ni;
+  FastSmem s;
+  {
+    size_t oR, oRT, oRW, osc, ost, oce;
+    int C, sw;
+    fast_smem_layout(G, d.fast_maxN, &oR, &oRT, &oRW, &osc, &ost, &oce, &C, &sw);
+    s.B.w = reinterpret_cast<uint32_t*>(fsm);
+    s.B.ce = reinterpret_cast<int*>(fsm + oce);
+    s.B.C = C;
+    s.B.sw = ((N + 15) / 16) * 8 + 4;
+    s.R = reinterpret_cast<double*>(fsm + oR);
+    s.RT = reinterpret_cast<double*>(fsm + oRT);
+    s.RW = reinterpret_cast<double*>(fsm + oRW);
+    s.sc = reinterpret_cast<double*>(fsm + osc);
+    s.st = reinterpret_cast<int*>(fsm + ost);
+  }
+  const int* fi = F.fi + it.i0;
+  const PzFastM& FM = F.ms[cls.m0 + mi];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+  for (int g = threadIdx.x; g < G; g += blockDim.x) {
+    s.st[2 * g] = (g < ni && d.state[fi[g]].status == 0) ? 1 : 0;
+    s.st[2 * g + 1] = 0;
+  }
+  __syncthreads();
+
+  // ---- explicit terms: D1p of dVsT and dVsOm (4 columns per instance)
+  zero_cols(s.B, 0);
+  __syncthreads();
+  for (int j = warp; j < 4 * ni; j += nw) {
+    const int g = j >> 2, f = (j >> 1) & 1, part = j & 1;
+    if (!s.st[2 * g]) continue;
+    const PzInst& I = d.inst[fi[g]];
+    const View V{&I, d.pool};
+    const double* x = reinterpret_cast<const double*>(V.fld(f ? F_DVSOM : F_DVST, mi)) + part;
+    split_col(s.B, j, x, 2, N);
+  }
+  __syncthreads();
+  oz_mma(F, cls.d1p, s.B, 4 * ni, s.R, N);
+  __syncthreads();
+
+  // ---- finish the explicit terms; IMEX right-hand sides (interior rows)
+  const double dm = (double)(mi * d.inst[fi[0]].minc), dm2 = dm * dm;
+  for (int t = threadIdx.x; t < ni * N; t += blockDim.x) {
+    const int g = t / N, i = t - g * N;
+    if (!s.st[2 * g]) continue;
+    const int inst = fi[g];
+    const PzInst& I = d.inst[inst];
+    const PzState& S = d.state[inst];
+    const View V{&I, d.pool};
+    const double* or1 = V.rad(RV_OR1);
+    const double* beta = V.rad(RV_BETA);
+    const double2 u = V.fld(F_US, mi)[i];
+    const double2 dT = make_double2(s.R[(4 * g + 0) * N + i], s.R[(4 * g + 1) * N + i]);
+    const double2 dO = make_double2(s.R[(4 * g + 2) * N + i], s.R[(4 * g + 3) * N + i]);
+    double2* eT = V.hist(0, 2, S.r_expl, mi);
+    double2 e = eT[i];
+    const double c = V.rad(RV_DTCOND)[i] - I.tadvz * beta[i] * V.rad(RV_TCOND)[i];
+    e.x = e.x - or1[i] * dT.x - u.x * c;
+    e.y = e.y - or1[i] * dT.y - u.y * c;
+    eT[i] = e;
+    if (mi != 0) {
+      double2* eP = V.hist(1, 2, S.r_expl, mi);
+      double2 p = eP[i];
+      p.x -= or1[i] * dO.x;
+      p.y -= or1[i] * dO.y;
+      if (!(I.flags & PZF_NON_ROT)) {
+        p.x += I.CorFac * beta[i] * u.x;
+        p.y += I.CorFac * beta[i] * u.y;
+      }
+      if (!(I.flags & PZF_BUO_IMP)) {
+        const double2 b = cim(dm, V.fld(F_TEMP, mi)[i]);
+        const double cb = I.BuoFac * V.rad(RV_RGRAV)[i] * or1[i];
+        p.x -= cb * b.x; p.y -= cb * b.y;
+      }
+      if (I.flags & PZF_EK_PUMP) {
+        const double2 o = V.fld(F_OM, mi)[i], w = V.fld(F_UP, mi)[i];
+        const double eus = V.rad(RV_EKP_US)[i], edp = V.rad(RV_EKP_DUSDP)[i];
+        const double2 q = make_double2(eus * u.x - edp * dm * u.y, eus * u.y + edp * dm * u.x);
+        const double ce = I.CorFac * V.rad(RV_EKPUMP)[i];
+        const double eup = V.rad(RV_EKP_UP)[i];
+        p.x -= ce * (o.x + eup * w.x + q.x);
+        p.y -= ce * (o.y + eup * w.y + q.y);
+      }
+      eP[i] = p;
+    }
+    if (i == 0 || i == N - 1) continue;
+    const double2 rt = imex_rhs_f(V, I, S, 0, mi, i);
+    double2 rw = imex_rhs_f(V, I, S, 1, mi, i);
+    if (mi == 0) rw.y = 0.0;
+    s.RT[(2 * g) * n + i - 1] = rt.x;
+    s.RT[(2 * g + 1) * n + i - 1] = rt.y;
+    s.RW[(2 * g) * n + i - 1] = rw.x;
+    s.RW[(2 * g + 1) * n + i - 1] = rw.y;
+  }
+  __syncthreads();
+
+  // ---- temperature: y = U^-1 rhs, z = y / (1 - w TdiffFac lam), [T; dT/dr] = [U; D1p U] z
+  zero_cols(s.B, 0);
+  __syncthreads();
+  for (int j = warp; j < 2 * ni; j += nw)
+    if (s.st[2 * (j >> 1)]) split_col(s.B, j, s.RT + (long long)j * n, 1, n);
+  __syncthreads();
+  oz_mma(F, FM.uinv, s.B, 2 * ni, s.R, n);
+  __syncthreads();
+  {
+    const double* lam = F.vec + FM.vec;
+    for (int t = threadIdx.x; t < 2 * ni * n; t += blockDim.x) {
+      const int j = t / n, k = t - j * n;
+      const int inst = fi[j >> 1];
+      const double w = d.state[inst].wimp_lin[0] * d.inst[inst].TdiffFac;
+      s.R[(long long)j * n + k] = s.R[(long long)j * n + k] / (1.0 - w * lam[k]);
+    }
+  }
+  __syncthreads();
+  zero_cols(s.B, 0);
+  __syncthreads();
+  for (int j = warp; j < 2 * ni; j += nw)
+    if (s.st[2 * (j >> 1)]) split_col(s.B, j, s.R + (long long)j * n, 1, n);
+  __syncthreads();
+  oz_mma(F, FM.s3t, s.B, 2 * ni, s.R, n + N);
+  __syncthreads();
+  // new temperature, dT/dr, history; the vorticity rhs gets the implicit buoyancy
+  for (int t = threadIdx.x; t < ni * N; t += blockDim.x) {
+    const int g = t / N, i = t - g * N;
+    if (!s.st[2 * g]) continue;
+    const int inst = fi[g];
+    const PzInst& I = d.inst[inst];
+    const PzState& S = d.state[inst];
+    const View V{&I, d.pool};
+    const int ld = n + N;
+    const bool edge = (i == 0 || i == N - 1);
+    const double2 T = edge ? make_double2(0.0, 0.0)
+                           : make_double2(s.R[(2 * g) * ld + i - 1], s.R[(2 * g + 1) * ld + i - 1]);
+    const double2 d1 = make_double2(s.R[(2 * g) * ld + n + i], s.R[(2 * g + 1) * ld + n + i]);
+    V.fld(F_TEMP, mi)[i] = T;
+    V.fld(F_DTEMP, mi)[i] = d1;
+    V.hist(0, 0, S.b_old, mi)[i] = T;
+    if (!isfinite(T.x) || !isfinite(T.y)) s.st[2 * g + 1] = 1;
+    const double w = S.wimp_lin[0];
+    if (S.l_calc_lin) {
+      double2 it = make_double2(0.0, 0.0);
+      if (!edge) {
+        const double iw = 1.0 / w;
+        it = make_double2(iw * (T.x - s.RT[(2 * g) * n + i - 1]), iw * (T.y - s.RT[(2 * g + 1) * n + i - 1]));
+      }
+      V.hist(0, 1, S.b_impl, mi)[i] = it;
+    }
+    if (edge) continue;
+    s.RT[(2 * g) * n + i - 1] = T.x;       // the new temperature for the buoyancy below
+    s.RT[(2 * g + 1) * n + i - 1] = T.y;
+    if (mi != 0 && (I.flags & PZF_BUO_IMP)) {
+      const double2 b = cim(dm, T);
+      const double c = w * I.BuoFac * V.rad(RV_RGRAV)[i] * V.rad(RV_OR1)[i];
+      s.RW[(2 * g) * n + i - 1] -= c * b.x;
+      s.RW[(2 * g + 1) * n + i - 1] -= c * b.y;
+    }
+  }
+  __syncthreads();
+
+  // ---- vorticity (m > 0) or u_phi (m = 0): y = U^-1 rhs
+  const PzOzOp& wuinv = (mi == 0) ? F.us[it.ucls].uinv : FM.uinv;
+  zero_cols(s.B, 0);
+  __syncthreads();
+  for (int j = warp; j < 2 * ni; j += nw)
+    if (s.st[2 * (j >> 1)]) split_col(s.B, j, s.RW + (long long)j * n, 1, n);
+  __syncthreads();
+  oz_mma(F, wuinv, s.B, 2 * ni, s.R, n);
+  __syncthreads();
+  if (mi == 0) {
+    const double* lam = F.vec + F.us[it.ucls].vec;
+    for (int t = threadIdx.x; t < 2 * ni * n; t += blockDim.x) {
+      const int j = t / n, k = t - j * n;
+      const double w = d.state[fi[j >> 1]].wimp_lin[0];
+      s.R[(long long)j * n + k] = s.R[(long long)j * n + k] / (1.0 - w * lam[k]);
+    }
+  } else {
+    // z = y / (1 - w nu lam); influence correction in eigen space: the two
+    // homogeneous solutions are h = w nu D U^-1 P_Ib e_wall, their dpsi/dr at
+    // the walls give the 2 x 2 influence matrix, and z + c1 h_bot + c2 h_top
+    // has the no-slip walls (update_psi_coll_dmat.f90:1136-1300)
+    const double* lam = F.vec + FM.vec;
+    const double* gtop = lam + n;
+    const double* gbot = lam + 2 * n;
+    const double* qt = lam + 3 * n;
+    const double* qb = lam + 4 * n;
+    for (int g = warp; g < ni; g += nw) {
+      if (!s.st[2 * g]) continue;
+      const int inst = fi[g];
+      const double wn = d.state[inst].wimp_lin[0] * d.inst[inst].ViscFac;
+      double* zr = s.R + (long long)(2 * g) * n;
+      double* zi = zr + n;
+      double t1r = 0.0, t1i = 0.0, b1r = 0.0, b1i = 0.0, t2 = 0.0, b2 = 0.0, t3 = 0.0, b3 = 0.0;
+      for (int k = lane; k < n; k += 32) {
+        const double D = 1.0 / (1.0 - wn * lam[k]);
+        const double yr = zr[k] * D, yi = zi[k] * D;
+        zr[k] = yr; zi[k] = yi;
+        const double h2 = wn * D * gbot[k], h3 = wn * D * gtop[k];
+        t1r += qt[k] * yr; t1i += qt[k] * yi; b1r += qb[k] * yr; b1i += qb[k] * yi;
+        t2 += qt[k] * h2; b2 += qb[k] * h2; t3 += qt[k] * h3; b3 += qb[k] * h3;
+      }
+      t1r = warp_sum(t1r); t1i = warp_sum(t1i); b1r = warp_sum(b1r); b1i = warp_sum(b1i);
+      t2 = warp_sum(t2); b2 = warp_sum(b2); t3 = warp_sum(t3); b3 = warp_sum(b3);
+      const double det = t2 * b3 - t3 * b2;
+      const double i00 = b3 / det, i01 = -t3 / det, i10 = -b2 / det, i11 = t2 / det;
+      const double c1r = -i00 * t1r - i01 * b1r, c1i = -i00 * t1i - i01 * b1i;
+      const double c2r = -i10 * t1r - i11 * b1r, c2i = -i10 * t1i - i11 * b1i;
+      for (int k = lane; k < n; k += 32) {
+        const double D = 1.0 / (1.0 - wn * lam[k]);
+        const double h2 = wn * D * gbot[k], h3 = wn * D * gtop[k];
+        zr[k] += c1r * h2 + c2r * h3;
+        zi[k] += c1i * h2 + c2i * h3;
+      }
+      if (lane == 0) {
+        s.sc[4 * g + 0] = c1r; s.sc[4 * g + 1] = c1i; s.sc[4 * g + 2] = c2r; s.sc[4 * g + 3] = c2i;
+      }
+    }
+  }
+  __syncthreads();
+  zero_cols(s.B, 0);
+  __syncthreads();
+  for (int j = warp; j < 2 * ni; j += nw)
+    if (s.st[2 * (j >> 1)]) split_col(s.B, j, s.R + (long long)j * n, 1, n);
+  __syncthreads();
+  const PzOzOp& w3 = (mi == 0) ? F.us[it.ucls].s3u : FM.s3w;
+  const int ld3 = w3.R;
+  oz_mma(F, w3, s.B, 2 * ni, s.R, ld3);
+  __syncthreads();
+
+  // ---- new velocity, vorticity and streamfunction; history
+  for (int t = threadIdx.x; t < ni * N; t += blockDim.x) {
+    const int g = t / N, i = t - g * N;
+    if (!s.st[2 * g]) continue;
+    const int inst = fi[g];
+    const PzInst& I = d.inst[inst];
+    const PzState& S = d.state[inst];
+    const View V{&I, d.pool};
+    const double* or1 = V.rad(RV_OR1);
+    const bool edge = (i == 0 || i == N - 1);
+    const double w = S.wimp_lin[0], iw = 1.0 / w;
+    const double* Rr = s.R + (long long)(2 * g) * ld3;
+    const double* Ri = s.R + (long long)(2 * g + 1) * ld3;
+    bool bad;
+    if (mi == 0) {
+      const double u = edge ? 0.0 : Rr[i - 1];
+      const double du = Rr[n + i];
+      V.fld(F_US, 0)[i] = make_double2(0.0, 0.0);
+      V.fld(F_UP, 0)[i] = make_double2(u, 0.0);
+      V.fld(F_OM, 0)[i] = make_double2(du + or1[i] * u, 0.0);
+      V.fld(F_PSI, 0)[i] = make_double2(0.0, 0.0);
+      V.hist(1, 0, S.b_old, 0)[i] = make_double2(u, 0.0);
+      if (S.l_calc_lin)
+        V.hist(1, 1, S.b_impl, 0)[i] = make_double2(edge ? 0.0 : iw * (u - s.RW[(2 * g) * n + i - 1]), 0.0);
+      bad = !isfinite(u);
+    } else {
+      double2 om, ps;
+      if (i == 0) om = make_double2(s.sc[4 * g + 2], s.sc[4 * g + 3]);
+      else if (i == N - 1) om = make_double2(s.sc[4 * g + 0], s.sc[4 * g + 1]);
+      else om = make_double2(Rr[i - 1], Ri[i - 1]);
+      ps = edge ? make_double2(0.0, 0.0) : make_double2(Rr[n + i - 1], Ri[n + i - 1]);
+      const double2 dp = make_double2(Rr[2 * n + i], Ri[2 * n + i]);
+      const double be = V.rad(RV_BETA)[i];
+      V.fld(F_PSI, mi)[i] = ps;
+      V.fld(F_US, mi)[i] = cscale(or1[i], cim(dm, ps));
+      V.fld(F_UP, mi)[i] = make_double2(-dp.x - be * ps.x, -dp.y - be * ps.y);
+      V.fld(F_OM, mi)[i] = om;
+      V.hist(1, 0, S.b_old, mi)[i] = om;
+      if (S.l_calc_lin) {
+        double2 v = make_double2(0.0, 0.0);
+        if (!edge) {
+          v = cscale(iw, csub(om, make_double2(s.RW[(2 * g) * n + i - 1], s.RW[(2 * g + 1) * n + i - 1])));
+          if (I.flags & PZF_BUO_IMP) {
+            const double2 b = cim(dm, make_double2(s.RT[(2 * g) * n + i - 1], s.RT[(2 * g + 1) * n + i - 1]));
+            const double c = V.rad(RV_RGRAV)[i] * or1[i] * I.BuoFac;
+            v.x -= c * b.x; v.y -= c * b.y;
+          }
+        }
+        V.hist(1, 1, S.b_impl, mi)[i] = v;
+      }
+      bad = !isfinite(om.x) || !isfinite(om.y);
+    }
+    if (bad) s.st[2 * g + 1] = 1;
+  }
+  __syncthreads();
+  for (int g = threadIdx.x; g < ni; g += blockDim.x)
+    if (s.st[2 * g] && s.st[2 * g + 1]) {
+      PzState& Sg = d.state[fi[g]];
+      if (Sg.status == 0) Sg.status = PZ_E_NONFINITE;
+    }
+}
+
+}  // namespace
+
+size_t pz_fast_smem_bytes(int G, int maxN) {
+  size_t oR, oRT, oRW, osc, ost, oce;
+  int C, sw;
+  return fast_smem_layout(G, maxN, &oR, &oRT, &oRW, &osc, &ost, &oce, &C, &sw);
+}
+
+cudaError_t pz_launch_fast(const PzDev& d, cudaStream_t s) {
+  if (d.fast.n_items == 0) return cudaSuccess;
+  static bool attr = false;
+  if (!attr) {
+    cudaError_t e = cudaFuncSetAttribute(k_fast, cudaFuncAttributeMaxDynamicSharedMemorySize, PZ_SMEM_MAX);
+    if (e) return e;
+    attr = true;
+  }
+  k_fast<<<d.fast.n_items, 256, d.fast.smem, s>>>(d);
+  return cudaGetLastError();
+}

@@ -39,6 +39,15 @@ struct pz_handle {
   PzAdjoint* adj = nullptr;   // allocated by the first adjoint call
   int adj_grids = 1;           // adjoint sweeps keep the phi-grids of the stage states
   std::vector<PzLaunch> plan;  // kernel launches of one step, in order
+  // the plain step with the tensor-core stage: fast instances leave the
+  // per-m work lists of fdev and run in k_fast; plan/dev (all instances on
+  // the standard kernels) stay for the adjoint sweeps
+  std::vector<PzLaunch> fplan;
+  PzDev fdev{};
+  int n_fast = 0;              // instances on the fast path
+  PzItem* d_mitems_std = nullptr;
+  int* d_iorder_std = nullptr;
+  void* d_fast = nullptr;      // one allocation: fragments, exponents, vectors, descriptors, items
 };
 
 // host helpers of pz_host.cu

@@ -14,10 +14,12 @@
 #include <cstring>
 #include <initializer_list>
 #include <map>
+#include <tuple>
 #include <string>
 #include <vector>
 
 #include "pizza_gpu.h"
+#include "pz_fast_setup.h"
 #include "pz_handle.h"
 #include "pz_internal.h"
 #include "pz_stage.h"
@@ -533,6 +535,188 @@ int validate(const pz_config& c, std::string* why) {
 // ===========================================================================
 // C ABI
 // ===========================================================================
+// process-wide default of the tensor-core stage for handles created afterwards
+int g_fast_default = 1;
+// process-wide tuning table (pz_tune_set): k_fast instances per block, and
+// k_rloop radii per block by n_phi_max; 0 = the built-in choice
+int g_tune_fast_g = 0;
+std::map<int, int> g_tune_rloop_rg;
+
+namespace {
+
+// Whether instance i can run its stage in k_fast: the collocation step with
+// the influence-matrix solve and CNAB2 (no start-up bridge), fixed
+// temperature and no-slip walls, no composition, no Chebyshev truncation,
+// and n_r_max within the exact fp32 accumulation bound of the products.
+bool fast_eligible(const pz_config& c, const PzInst& I) {
+  return g_fast_default && c.cheb_method == PZ_CHEB_COLL && c.matrix_solve == PZ_SOLVE_INFLUENCE &&
+         !(I.flags & (PZF_CHEM | PZF_DIRECT | PZF_INTEG)) && (I.flags & PZF_IMP_CALC) && !I.dirk &&
+         I.scheme == PZ_CNAB2 && I.n_max == I.N && c.ktopt == 1 && c.kbott == 1 && c.ktopv == 2 &&
+         c.kbotv == 2 && I.N >= 5 && I.N <= PZ_FAST_MAXN;
+}
+
+// Operators, work items and device descriptors of the fast instances;
+// instances whose class set-up fails stay on the standard kernels.  Returns
+// the device descriptor (n_items 0 when no instance takes the fast path).
+// radial functions: rad[i] (RV_COUNT x N) of each instance.
+struct FastBuild {
+  PzFastHost H;
+  std::vector<PzFastItem> items;
+  std::vector<int> fi;
+  int maxN = 0;
+  int G = PZ_FAST_G;        // instances per block, within the shared-memory budget
+};
+
+void fast_classes(pz_handle* h, const std::map<int, Basis>& bases, const std::vector<std::vector<double>>& rad,
+                  int G, FastBuild& fb) {
+  const int n = h->n_inst;
+  std::vector<int> cls_of(n, -1), ucls_of(n, -1);
+  std::map<std::tuple<int, double, int>, std::vector<int>> classes;
+  for (int i = 0; i < n; ++i)
+    if (fast_eligible(h->hin[i].c, h->inst[i]))
+      classes[std::make_tuple(h->inst[i].N, h->hin[i].c.radratio, h->inst[i].minc)].push_back(i);
+  std::map<std::tuple<int, double, double, double, double>, int> ukeys;
+  for (auto& kv : classes) {
+    const int N = std::get<0>(kv.first), minc = std::get<2>(kv.first);
+    const std::vector<double>& R = rad[kv.second[0]];
+    const Basis& B = bases.at(N);
+    PzFastGrid g{N, B.D1p.data(), B.D2p.data(), R.data() + (size_t)RV_OR1 * N, R.data() + (size_t)RV_OR2 * N,
+                 R.data() + (size_t)RV_BETA * N, R.data() + (size_t)RV_DBETA * N};
+    int Mc = 0;
+    for (int i : kv.second) Mc = std::max(Mc, h->inst[i].M);
+    int ci = -1;
+    if (!pz_fast_add_class(fb.H, g, Mc, minc, &ci)) continue;
+    for (int i : kv.second) {
+      const PzInst& I = h->inst[i];
+      const double* ekp = rad[i].data() + (size_t)RV_EKPUMP * N;
+      const auto uk = std::make_tuple(N, h->hin[i].c.radratio, I.ViscFac, I.CorFac, ekp[N / 2]);
+      int ui;
+      if (ukeys.count(uk)) ui = ukeys[uk];
+      else if (pz_fast_add_uclass(fb.H, g, I.ViscFac, I.CorFac, ekp, &ui)) ukeys[uk] = ui;
+      else continue;
+      cls_of[i] = ci;
+      ucls_of[i] = ui;
+    }
+  }
+  // work items: per class (largest grids first), per m, the instances that
+  // have that m in groups of G; m = 0 groups also share their u_phi class
+  std::vector<int> cl;
+  for (int c = 0; c < (int)fb.H.cls.size(); ++c) cl.push_back(c);
+  std::stable_sort(cl.begin(), cl.end(), [&](int a, int b) { return fb.H.cls[a].N > fb.H.cls[b].N; });
+  for (int c : cl) fb.maxN = std::max(fb.maxN, fb.H.cls[c].N);
+  while (G > 1 && pz_fast_smem_bytes(G, fb.maxN) > PZ_SMEM_MAX) --G;
+  fb.G = G;
+  for (int c : cl) {
+    for (int m = 0; m < fb.H.cls[c].Mc; ++m) {
+      std::map<int, std::vector<int>> groups;    // by u_phi class (m = 0), else one group
+      for (int i = 0; i < n; ++i)
+        if (cls_of[i] == c && h->inst[i].M > m) groups[m == 0 ? ucls_of[i] : 0].push_back(i);
+      for (auto& gv : groups)
+        for (size_t a = 0; a < gv.second.size(); a += G) {
+          PzFastItem it;
+          it.cls = c; it.m = m; it.ucls = m == 0 ? gv.first : 0;
+          it.i0 = (int)fb.fi.size();
+          it.ni = (int)std::min<size_t>(G, gv.second.size() - a);
+          for (int q = 0; q < it.ni; ++q) fb.fi.push_back(gv.second[a + q]);
+          fb.items.push_back(it);
+        }
+    }
+  }
+  for (int i = 0; i < n; ++i)
+    if (cls_of[i] >= 0) h->inst[i].flags |= PZF_FAST;
+}
+
+// one device allocation for the fast path: fragments, exponents, vectors,
+// class/m/u descriptors, items and instance lists
+cudaError_t fast_upload(pz_handle* h, const FastBuild& fb, int G, PzFastDev* F) {
+  auto al = [](size_t x) { return (x + 255) & ~(size_t)255; };
+  const PzFastHost& H = fb.H;
+  size_t o = 0;
+  const size_t o_frag = o; o = al(o + H.frag.size() * sizeof(uint4));
+  const size_t o_ex = o; o = al(o + H.ex.size() * sizeof(int));
+  const size_t o_vec = o; o = al(o + H.vec.size() * sizeof(double));
+  const size_t o_cls = o; o = al(o + H.cls.size() * sizeof(PzFastCls));
+  const size_t o_ms = o; o = al(o + H.ms.size() * sizeof(PzFastM));
+  const size_t o_us = o; o = al(o + H.us.size() * sizeof(PzFastU));
+  const size_t o_it = o; o = al(o + fb.items.size() * sizeof(PzFastItem));
+  const size_t o_fi = o; o = al(o + fb.fi.size() * sizeof(int));
+  cudaError_t e = cudaMalloc(&h->d_fast, o);
+  if (e) return e;
+  std::vector<unsigned char> img(o, 0);
+  auto put = [&](size_t off, const void* src, size_t bytes) { if (bytes) std::memcpy(img.data() + off, src, bytes); };
+  put(o_frag, H.frag.data(), H.frag.size() * sizeof(uint4));
+  put(o_ex, H.ex.data(), H.ex.size() * sizeof(int));
+  put(o_vec, H.vec.data(), H.vec.size() * sizeof(double));
+  put(o_cls, H.cls.data(), H.cls.size() * sizeof(PzFastCls));
+  put(o_ms, H.ms.data(), H.ms.size() * sizeof(PzFastM));
+  put(o_us, H.us.data(), H.us.size() * sizeof(PzFastU));
+  put(o_it, fb.items.data(), fb.items.size() * sizeof(PzFastItem));
+  put(o_fi, fb.fi.data(), fb.fi.size() * sizeof(int));
+  if ((e = cudaMemcpyAsync(h->d_fast, img.data(), o, cudaMemcpyHostToDevice, h->stream)) ||
+      (e = cudaStreamSynchronize(h->stream)))
+    return e;
+  unsigned char* b = static_cast<unsigned char*>(h->d_fast);
+  F->frag = reinterpret_cast<const uint4*>(b + o_frag);
+  F->ex = reinterpret_cast<const int*>(b + o_ex);
+  F->vec = reinterpret_cast<const double*>(b + o_vec);
+  F->cls = reinterpret_cast<const PzFastCls*>(b + o_cls);
+  F->ms = reinterpret_cast<const PzFastM*>(b + o_ms);
+  F->us = reinterpret_cast<const PzFastU*>(b + o_us);
+  F->items = reinterpret_cast<const PzFastItem*>(b + o_it);
+  F->n_items = (int)fb.items.size();
+  F->fi = reinterpret_cast<const int*>(b + o_fi);
+  F->G = G;
+  F->smem = (int)pz_fast_smem_bytes(G, fb.maxN);
+  return cudaSuccess;
+}
+
+}  // namespace
+
+extern "C" int pz_fast_path(int enable) {
+  const int prev = g_fast_default;
+  if (enable >= 0) g_fast_default = enable ? 1 : 0;
+  return prev;
+}
+
+extern "C" int pz_tune_set(int what, int key, int value) {
+  if (what == PZ_TUNE_FAST_G) {
+    if (value > PZ_FAST_GMAX) return fail(nullptr, PZ_E_ARG, "pz_tune_set: k_fast takes at most 16 instances per block");
+    g_tune_fast_g = value > 0 ? value : 0;
+    return PZ_OK;
+  }
+  if (what == PZ_TUNE_RLOOP_RG) {
+    if (key < 6 || key % 3 != 0) return fail(nullptr, PZ_E_ARG, "pz_tune_set: key must be an n_phi_max");
+    if (value <= 0) { g_tune_rloop_rg.erase(key); return PZ_OK; }
+    const int M = key / 3 + 1;
+    if (value > 16 || pz_rloop_smem_bytes(key, M, value, 3) > PZ_SMEM_MAX)
+      return fail(nullptr, PZ_E_ARG, "pz_tune_set: k_rloop radii per block exceed its shared memory");
+    g_tune_rloop_rg[key] = value;
+    return PZ_OK;
+  }
+  return fail(nullptr, PZ_E_ARG, "pz_tune_set: unknown parameter");
+}
+
+extern "C" int pz_fast_eigen(int n_r_max, double radratio, int m, double* lam, double* U) {
+  if (n_r_max < 5 || n_r_max > 1024 || m < 0 || !(radratio > 0.0 && radratio < 1.0) || !lam || !U)
+    return fail(nullptr, PZ_E_ARG, "pz_fast_eigen: bad arguments");
+  const int N = n_r_max, n = N - 2;
+  const double r_cmb = 1.0 / (1.0 - radratio), r_icb = r_cmb - 1.0;
+  const Basis B = make_basis(N, r_icb, r_cmb);
+  std::vector<double> or1(N), or2(N), zero(N, 0.0);
+  for (int k = 0; k < N; ++k) {
+    const double r = 0.5 * (r_cmb - r_icb) * B.x[k] + 0.5 * (r_icb + r_cmb);
+    or1[k] = 1.0 / r;
+    or2[k] = or1[k] * or1[k];
+  }
+  const PzFastGrid g{N, B.D1p.data(), B.D2p.data(), or1.data(), or2.data(), zero.data(), zero.data()};
+  std::vector<double> P, Pb, l, u, ui;
+  pz_fast_laplacian(g, (double)m * (double)m, P, Pb);
+  if (!pz_eig_real(n, P, l, u, ui)) return fail(nullptr, PZ_E_SINGULAR, "pz_fast_eigen: decomposition failed");
+  std::memcpy(lam, l.data(), n * sizeof(double));
+  std::memcpy(U, u.data(), (size_t)n * n * sizeof(double));
+  return PZ_OK;
+}
+
 extern "C" void pz_config_default(pz_config* c) {
   if (!c) return;
   std::memset(c, 0, sizeof(*c));
@@ -581,6 +765,7 @@ extern "C" int pz_create(const pz_config* cfgs, int n, pz_handle** out) {
     I.M = c.m_max / c.minc + 1;                   // truncation.f90:28
     I.P = 3 * c.m_max / c.minc;                   // truncation.f90:30-31
     I.rg = std::max(1, std::min(8, PZ_RLOOP_PG / I.P));
+    if (g_tune_rloop_rg.count(I.P)) I.rg = g_tune_rloop_rg[I.P];
     factor_fft(I.P, I.radix, &I.nrad);
     double cf;
     int imp_calc;
@@ -753,6 +938,10 @@ extern "C" int pz_create(const pz_config* cfgs, int n, pz_handle** out) {
     maxP = std::max(maxP, I.P);
     maxM = std::max(maxM, I.M);
   }
+  // tensor-core stage: classes, eigen-bases and work items of the eligible instances
+  FastBuild fb;
+  const int fast_g = g_tune_fast_g > 0 ? g_tune_fast_g : PZ_FAST_G;
+  fast_classes(h, bases, rad, fast_g, fb);
   // per-instance operators and state
   for (int i = 0; i < n; ++i) {
     PzInst& I = h->inst[i];
@@ -889,6 +1078,7 @@ extern "C" int pz_create(const pz_config* cfgs, int n, pz_handle** out) {
   h->dev.obs_part = h->d_obs_part;
   h->dev.obs_cnt = h->d_obs_cnt;
   h->dev.iorder = h->d_iorder;
+  h->dev.n_iorder = n;
   h->dev.n_inst = n;
   h->dev.any_chem = 0;
   for (int i = 0; i < n; ++i) h->dev.any_chem |= (h->inst[i].flags & PZF_CHEM) ? 1 : 0;
@@ -934,6 +1124,60 @@ extern "C" int pz_create(const pz_config* cfgs, int n, pz_handle** out) {
   }
   if (any_assembly) h->plan.push_back({PZK_ASSEMBLE, 0});
   h->plan.push_back({PZK_OBS, 0});
+  // the plain step's plan: fast instances leave the per-m work lists and run
+  // in k_fast after k_cfl; the standard stage kernels run for the others
+  if (!fb.items.empty()) {
+    std::vector<PzItem> mstd;
+    std::vector<int> ostd;
+    for (int i : order) {
+      if (h->inst[i].flags & PZF_FAST) { ++h->n_fast; continue; }
+      ostd.push_back(i);
+      for (int m = 0; m < h->inst[i].M; ++m) mstd.push_back({i, m});
+    }
+    h->fdev = h->dev;
+    if ((e = fast_upload(h, fb, fb.G, &h->fdev.fast)) ||
+        (!mstd.empty() && ((e = cudaMalloc(&h->d_mitems_std, mstd.size() * sizeof(PzItem))) ||
+                           (e = cudaMalloc(&h->d_iorder_std, ostd.size() * sizeof(int))) ||
+                           (e = cudaMemcpyAsync(h->d_mitems_std, mstd.data(), mstd.size() * sizeof(PzItem),
+                                                cudaMemcpyHostToDevice, h->stream)) ||
+                           (e = cudaMemcpyAsync(h->d_iorder_std, ostd.data(), ostd.size() * sizeof(int),
+                                                cudaMemcpyHostToDevice, h->stream))))) {
+      g_create_error = std::string("fast-path set-up: ") + cudaGetErrorString(e);
+      pz_destroy(h);
+      return PZ_E_NOMEM;
+    }
+    h->fdev.fast_maxN = fb.maxN;
+    h->fdev.mitems = h->d_mitems_std;
+    h->fdev.n_mitems = (int)mstd.size();
+    h->fdev.iorder = h->d_iorder_std;
+    h->fdev.n_iorder = (int)ostd.size();
+    int fsmax = 1;
+    bool f_integ = false, f_coll = false;
+    for (int i : ostd) {
+      fsmax = std::max(fsmax, h->inst[i].nstages);
+      f_integ |= (h->inst[i].flags & PZF_INTEG) != 0;
+      f_coll |= !(h->inst[i].flags & PZF_INTEG);
+    }
+    const bool ffused = !f_integ && sb <= 48 * 1024;
+    for (int st = 1; st <= fsmax; ++st) {
+      h->fplan.push_back({PZK_RLOOP, st});
+      if (st == 1) {
+        h->fplan.push_back({PZK_CFL, 1});
+        h->fplan.push_back({PZK_FAST, 1});
+        if (ostd.empty()) continue;
+        if (ffused) {
+          h->fplan.push_back({PZK_ORDER, 1});
+          h->fplan.push_back({PZK_BUILD_MLOOP, 1});
+          continue;
+        }
+        h->fplan.push_back({PZK_BUILD, 1});
+      }
+      if (f_coll) h->fplan.push_back({PZK_MLOOP, st});
+      if (f_integ) h->fplan.push_back({PZK_MLOOP_INTEG, st});
+    }
+    if (any_assembly) h->fplan.push_back({PZK_ASSEMBLE, 0});
+    h->fplan.push_back({PZK_OBS, 0});
+  }
   if ((e = pz_launch_init_state(h->dev, -1, h->stream)) || (e = pz_launch_build_static(h->dev, h->stream)) ||
       (e = cudaStreamSynchronize(h->stream))) {
     g_create_error = std::string("static operators: ") + cudaGetErrorString(e);
@@ -1042,8 +1286,9 @@ extern "C" int pz_step(pz_handle* h, int n_steps) {
   if (!h->graph) {
     cudaGraph_t g;
     if ((e = cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal))) return cuda_fail(h, e, "capture");
-    for (const PzLaunch& L : h->plan)
-      if (!e) e = pz_launch_step_kernel(h->dev, L.kind, L.stage, h->stream);
+    const bool fast = h->n_fast > 0;
+    for (const PzLaunch& L : fast ? h->fplan : h->plan)
+      if (!e) e = pz_launch_step_kernel(fast ? h->fdev : h->dev, L.kind, L.stage, h->stream);
     cudaError_t e2 = cudaStreamEndCapture(h->stream, &g);
     if (e || e2) return cuda_fail(h, e ? e : e2, "capture");
     e = cudaGraphInstantiate(&h->graph, g, 0);
@@ -1279,8 +1524,8 @@ extern "C" int pz_get_dims(pz_handle* h, int inst, int* n_r_max, int* n_m_max, i
 }
 
 extern "C" int pz_launches_per_step(pz_handle* h) {
-  (void)h;
-  return (int)h->plan.size();
+  if (!h) return 0;
+  return (int)(h->n_fast > 0 ? h->fplan.size() : h->plan.size());
 }
 
 extern "C" int pz_latest_rows(pz_handle* h, double* rows) {
@@ -1298,7 +1543,10 @@ extern "C" void* pz_stream(pz_handle* h) { return h ? (void*)h->stream : nullptr
 extern "C" int pz_step_profile(pz_handle* h, int n_steps, double* kernel_ms) {
   if (!h || n_steps <= 0 || !kernel_ms) return fail(h, PZ_E_ARG, "pz_step_profile: bad arguments");
   pz_adjoint_invalidate(h);
-  const int nk = (int)h->plan.size();
+  // the launches of pz_step (the fast plan when the handle has fast instances)
+  const std::vector<PzLaunch>& plan = h->n_fast > 0 ? h->fplan : h->plan;
+  const PzDev& dv = h->n_fast > 0 ? h->fdev : h->dev;
+  const int nk = (int)plan.size();
   std::vector<cudaEvent_t> ev((size_t)n_steps * (nk + 1));
   cudaError_t e = cudaSuccess;
   for (auto& x : ev) if (!e) e = cudaEventCreate(&x);
@@ -1306,7 +1554,7 @@ extern "C" int pz_step_profile(pz_handle* h, int n_steps, double* kernel_ms) {
   for (int s = 0; s < n_steps && !e; ++s) {
     e = cudaEventRecord(ev[(size_t)s * (nk + 1)], h->stream);
     for (int k = 0; k < nk && !e; ++k) {
-      e = pz_launch_step_kernel(h->dev, h->plan[k].kind, h->plan[k].stage, h->stream);
+      e = pz_launch_step_kernel(dv, plan[k].kind, plan[k].stage, h->stream);
       if (!e) e = cudaEventRecord(ev[(size_t)s * (nk + 1) + k + 1], h->stream);
     }
   }
@@ -1316,7 +1564,7 @@ extern "C" int pz_step_profile(pz_handle* h, int n_steps, double* kernel_ms) {
     for (int k = 0; k < nk && !e; ++k) {
       float ms = 0.f;
       e = cudaEventElapsedTime(&ms, ev[(size_t)s * (nk + 1) + k], ev[(size_t)s * (nk + 1) + k + 1]);
-      kernel_ms[h->plan[k].kind] += ms / n_steps;
+      kernel_ms[plan[k].kind] += ms / n_steps;
     }
   for (auto& x : ev) cudaEventDestroy(x);
   if (e) return cuda_fail(h, e, "pz_step_profile");
@@ -1412,6 +1660,9 @@ extern "C" int pz_destroy(pz_handle* h) {
   cudaFree(h->d_oitems);
   cudaFree(h->d_obs_part);
   cudaFree(h->d_obs_cnt);
+  cudaFree(h->d_fast);
+  cudaFree(h->d_mitems_std);
+  cudaFree(h->d_iorder_std);
   if (h->stream) cudaStreamDestroy(h->stream);
   delete h;
   return PZ_OK;

@@ -53,6 +53,8 @@ enum {
                        // Chebyshev derivative recursions of the m = 0 flow
   PZF_CHEM     = 512,  // composition equation (raxi /= 0): update_xi_coll.f90,
                        // update_xi_integ.f90, ChemFac buoyancy
+  PZF_FAST     = 1024, // collocation influence-matrix CNAB2 instance whose stage runs in
+                       // k_fast (tensor cores, eigen-basis solves) on the plain step
 };
 
 // integration-method operators (N x N, column-major, times rnorm, tau rows
@@ -199,6 +201,8 @@ __host__ __device__ inline long long pz_hist_off(const PzInst& I, int f, int kin
 
 struct PzItem { int inst; int idx; };   // (instance, r) or (instance, m index)
 
+#include "pz_fast.h"
+
 // launchers (pz_kernels.cu)
 struct PzDev {
   const PzInst* inst;       // device array
@@ -211,8 +215,9 @@ struct PzDev {
   double* obs_part;                       // n_oitems x PZ_OBS_NP partial sums of k_obs
   int* obs_cnt;                           // n_inst: k_obs blocks done this launch (reset by the last)
   PzItem* order;                          // n_mitems: k_order's layout of the fused first stage
-  const int* iorder;                      // n_inst: instances in work-list order (their m items are
+  const int* iorder;                      // n_iorder: instances in work-list order (their m items are
                                           // contiguous in mitems, m ascending)
+  int n_iorder;                           // instances of the per-m work list (mitems)
   int n_inst;
   int any_chem;             // some instance has composition: the step launches the
                             // kernels' composition instantiations
@@ -233,6 +238,9 @@ struct PzDev {
   double2* gsnap;
   const long long* o_gsnap;
   int gsnap_slot0;
+  // tensor-core stage of the plain step (n_items 0: none)
+  PzFastDev fast;
+  int fast_maxN;            // largest n_r_max of the fast classes
 };
 
 // `only` selects one instance (>= 0) or all of them (-1).
@@ -245,7 +253,7 @@ cudaError_t pz_launch_start(const PzDev& d, int only, cudaStream_t s);
 // (k_order + k_build_mloop replace k_build + k_mloop(1) when every instance is
 // a collocation instance with a small build footprint)
 enum { PZK_RLOOP = 0, PZK_CFL, PZK_BUILD, PZK_MLOOP, PZK_OBS, PZK_ASSEMBLE, PZK_MLOOP_INTEG, PZK_ORDER,
-       PZK_BUILD_MLOOP, PZK_KINDS };
+       PZK_BUILD_MLOOP, PZK_FAST, PZK_KINDS };
 struct PzLaunch { int kind, stage; };
 cudaError_t pz_launch_step_kernel(const PzDev& d, int kind, int stage, cudaStream_t s);
 const char* pz_step_kernel_name(int kind);
@@ -253,6 +261,10 @@ cudaError_t pz_launch_obs(const PzDev& d, int only, cudaStream_t s);
 cudaError_t pz_launch_spectra(const PzDev& d, int inst, int n_m_max, double* out, cudaStream_t s);
 cudaError_t pz_launch_gather_rows(const PzDev& d, double* out, cudaStream_t s);
 cudaError_t pz_setup_kernels();
+// k_fast (pz_fast.cu): the tensor-core stage of the fast instances, and its
+// dynamic shared memory for G instances per block and grids up to maxN
+cudaError_t pz_launch_fast(const PzDev& d, cudaStream_t s);
+size_t pz_fast_smem_bytes(int G, int maxN);
 size_t pz_build_smem_bytes(int n, bool direct, bool integ);   // k_build shared memory for one instance
 size_t pz_rloop_smem_bytes(int P, int M, int G, int nt);     // k_rloop shared memory, G radii per block,
                                                              // nt transforms per radius (2, or 3 with composition)

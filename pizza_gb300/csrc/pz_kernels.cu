@@ -1393,7 +1393,7 @@ __global__ void __launch_bounds__(1024) k_order(PzDev d) {
   // one scan over the instances (in work-list order, where each instance's m
   // items are contiguous): rebuilding items and all items before each one
   __shared__ int sr[1024], sa[1024];
-  const int n = d.n_inst, T = blockDim.x, t = threadIdx.x;
+  const int n = d.n_iorder, T = blockDim.x, t = threadIdx.x;
   const int per = (n + T - 1) / T;
   const int q0 = min(n, t * per), q1 = min(n, q0 + per);
   auto rebuild = [&](int inst) {
@@ -1895,6 +1895,7 @@ cudaError_t pz_launch_step_kernel(const PzDev& d, int kind, int stage, cudaStrea
       break;
     case PZK_OBS: k_obs<<<d.n_oitems, 256, 0, s>>>(d, -1); break;
     case PZK_ASSEMBLE: k_assemble<<<d.n_mitems, mloop_threads(d.maxN), ms_smem_bytes(d.maxN), s>>>(d); break;
+    case PZK_FAST: return pz_launch_fast(d, s);
     default: return cudaErrorInvalidValue;
   }
   return cudaGetLastError();
@@ -1902,6 +1903,6 @@ cudaError_t pz_launch_step_kernel(const PzDev& d, int kind, int stage, cudaStrea
 
 const char* pz_step_kernel_name(int kind) {
   static const char* names[PZK_KINDS] = {"k_rloop", "k_cfl", "k_build", "k_mloop", "k_obs", "k_assemble",
-                                         "k_mloop_integ", "k_order", "k_build_mloop"};
+                                         "k_mloop_integ", "k_order", "k_build_mloop", "k_fast"};
   return (kind >= 0 && kind < PZK_KINDS) ? names[kind] : "";
 }
