@@ -26,6 +26,16 @@ __device__ __forceinline__ double warp_sum(double v) {
   for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
   return v;
 }
+// largest 64-bit unsigned value over the warp (all 32 lanes active)
+__device__ __forceinline__ unsigned long long warp_umax64(unsigned long long v) {
+  for (int o = 16; o > 0; o >>= 1) {
+    const unsigned lo = __shfl_xor_sync(0xffffffffu, (unsigned)v, o);
+    const unsigned hi = __shfl_xor_sync(0xffffffffu, (unsigned)(v >> 32), o);
+    const unsigned long long w = ((unsigned long long)hi << 32) | lo;
+    v = w > v ? w : v;
+  }
+  return v;
+}
 __device__ __forceinline__ double warp_max(double v) {
   for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
   return v;
@@ -293,15 +303,26 @@ __device__ void rloop_group(const PzInst& I, const View& V, int r0, int gmax, IO
   double2* g1 = fft_run(za, zb, I, tw, nt * G, true);
   double2* h = (g1 == za) ? zb : za;
   io.grid(g1, r0 * nt * P, nt * G * P);   // read-only use of g1, like the loop below
-  // Courant velocities and the nonlinear products on the grid
+  // Courant velocities and the nonlinear products on the grid.  When P is a
+  // multiple of 32 the 32 points of a warp lie on one radius and every lane
+  // runs every pass: one atomic per warp after a warp maximum.
+  const bool warp_red = (P & 31) == 0 && (blockDim.x & 31) == 0;
   for (int t = threadIdx.x; t < G * P; t += blockDim.x) {
     const int g = t / P, j = t - g * P;
     const double rr = V.rad(RV_R)[r0 + g];
     const double2 z1 = g1[(nt * g) * P + j], z2 = g1[(nt * g + 1) * P + j];
     const double usg = z1.x, upg = z1.y, omg = z2.x, Tg = z2.y;
     // squares are >= 0: their bit patterns order like unsigned integers
-    atomicMax(reinterpret_cast<unsigned long long*>(&vr[g]), (unsigned long long)__double_as_longlong(usg * usg));
-    atomicMax(reinterpret_cast<unsigned long long*>(&vh[g]), (unsigned long long)__double_as_longlong(upg * upg));
+    unsigned long long br = (unsigned long long)__double_as_longlong(usg * usg);
+    unsigned long long bh = (unsigned long long)__double_as_longlong(upg * upg);
+    if (warp_red) {
+      br = warp_umax64(br);
+      bh = warp_umax64(bh);
+    }
+    if (!warp_red || (threadIdx.x & 31) == 0) {
+      atomicMax(reinterpret_cast<unsigned long long*>(&vr[g]), br);
+      atomicMax(reinterpret_cast<unsigned long long*>(&vh[g]), bh);
+    }
     h[(nt * g) * P + j] = make_double2(rr * usg * Tg, upg * Tg);
     h[(nt * g + 1) * P + j] = make_double2(rr * usg * omg, upg * omg);
     if (chem) {

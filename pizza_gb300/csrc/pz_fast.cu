@@ -34,14 +34,6 @@ struct BOp {
 __device__ __forceinline__ unsigned long long umax64(unsigned long long a, unsigned long long b) {
   return a > b ? a : b;
 }
-__device__ __forceinline__ unsigned long long warp_umax64(unsigned long long v) {
-  for (int o = 16; o > 0; o >>= 1) {
-    const unsigned lo = __shfl_xor_sync(0xffffffffu, (unsigned)v, o);
-    const unsigned hi = __shfl_xor_sync(0xffffffffu, (unsigned)(v >> 32), o);
-    v = umax64(v, ((unsigned long long)hi << 32) | lo);
-  }
-  return v;
-}
 #define PZ_CE_NONFINITE 0x40000000
 
 __device__ __forceinline__ uint16_t bf16_bits(int d) {
@@ -106,6 +98,33 @@ __device__ __forceinline__ double pow2(int e) {
   return __longlong_as_double((long long)(e + 1023) << 52);
 }
 
+// The diagonal sums of one output, acc[g][q] = sum over kA + kx = g of the
+// slice products (integers: |acc[0]| <= 97 * 2^16, |acc[g]| <= 97 * 2^14 (g + 3)),
+// combined as sum_g acc[g] 2^(8 (6 - g)) in integer arithmetic: the top four
+// diagonals exactly (below 2^47), the bottom three exactly (below 2^40), then
+// the bottom part without its 11 lowest bits (2^-37 of the top diagonal's unit,
+// far below the diagonals kA + kx >= 7 that the splitting leaves out) so the
+// sum fits an int64 (below 2^60).  Returns that sum / 2^11 as a double, rounded
+// once: the product is the result times 2^(ex_row + ex_col - 53).  Only the
+// final conversion and scaling use the FP64 pipe.
+static_assert(PZ_OZ_S == 7, "oz_combine is written for 7 slices");
+__device__ __forceinline__ double oz_combine(const float (&acc)[PZ_OZ_S][4], int q) {
+  long long hi = __float2int_rn(acc[0][q]);
+  hi = hi * 256 + __float2int_rn(acc[1][q]);
+  hi = hi * 256 + __float2int_rn(acc[2][q]);
+  hi = hi * 256 + __float2int_rn(acc[3][q]);
+  long long lo = __float2int_rn(acc[4][q]);
+  lo = lo * 256 + __float2int_rn(acc[5][q]);
+  lo = lo * 256 + __float2int_rn(acc[6][q]);
+  return __ll2double_rn(hi * 8192 + (lo >> 11));    // >> of a negative lo: floor
+}
+
+// v 2^e; scales below the normal range in two steps so a small e does not
+// flush a large v to zero
+__device__ __forceinline__ double scale2(double v, int e) {
+  return e >= -1022 ? v * pow2(e) : (v * pow2(e + 512)) * pow2(-512);
+}
+
 // Y[col * ldy + row] = (A X)(row, col), row < op.R, col < C (X = the slices in
 // B).  A warp takes a (16-row tile, NC 8-column tiles) task; for each k tile
 // it loads the NC x PZ_OZ_S B fragments once and every A slice once, and runs
@@ -156,12 +175,9 @@ __device__ void oz_mma_t(const PzFastDev& F, const PzOzOp& op, const BOp& B, int
         const int row = rt * 16 + gid + ((q & 2) ? 8 : 0);
         const int col = (ct * NC + c) * 8 + 2 * t + (q & 1);
         if (row < op.R && col < C) {
-          double v = (double)acc[c][PZ_OZ_S - 1][q];
-#pragma unroll
-          for (int g = PZ_OZ_S - 2; g >= 0; --g) v = fma(v, 0.00390625, (double)acc[c][g][q]);
           const int ce = B.ce[col];
-          Y[(long long)col * ldy + row] =
-              ce == PZ_CE_NONFINITE ? __longlong_as_double(0x7ff8000000000000LL) : v * pow2(ea[row] + ce - 16);
+          Y[(long long)col * ldy + row] = ce == PZ_CE_NONFINITE ? __longlong_as_double(0x7ff8000000000000LL)
+                                                                : scale2(oz_combine(acc[c], q), ea[row] + ce - 53);
         }
       }
   }
@@ -335,11 +351,13 @@ __global__ void __launch_bounds__(256, 2) k_fast(PzDev d) {
   __syncthreads();
   {
     const double* lam = F.vec + FM.vec;
-    for (int t = threadIdx.x; t < 2 * ni * n; t += blockDim.x) {
-      const int j = t / n, k = t - j * n;
-      const int inst = fi[j >> 1];
+    for (int t = threadIdx.x; t < ni * n; t += blockDim.x) {
+      const int g = t / n, k = t - g * n;
+      const int inst = fi[g];
       const double w = d.state[inst].wimp_lin[0] * d.inst[inst].TdiffFac;
-      s.R[(long long)j * n + k] = s.R[(long long)j * n + k] / (1.0 - w * lam[k]);
+      const double D = 1.0 / (1.0 - w * lam[k]);
+      s.R[(long long)(2 * g) * n + k] *= D;
+      s.R[(long long)(2 * g + 1) * n + k] *= D;
     }
   }
   __syncthreads();
@@ -399,10 +417,12 @@ __global__ void __launch_bounds__(256, 2) k_fast(PzDev d) {
   __syncthreads();
   if (mi == 0) {
     const double* lam = F.vec + F.us[it.ucls].vec;
-    for (int t = threadIdx.x; t < 2 * ni * n; t += blockDim.x) {
-      const int j = t / n, k = t - j * n;
-      const double w = d.state[fi[j >> 1]].wimp_lin[0];
-      s.R[(long long)j * n + k] = s.R[(long long)j * n + k] / (1.0 - w * lam[k]);
+    for (int t = threadIdx.x; t < ni * n; t += blockDim.x) {
+      const int g = t / n, k = t - g * n;
+      const double w = d.state[fi[g]].wimp_lin[0];
+      const double D = 1.0 / (1.0 - w * lam[k]);
+      s.R[(long long)(2 * g) * n + k] *= D;
+      s.R[(long long)(2 * g + 1) * n + k] *= D;
     }
   } else {
     // z = y / (1 - w nu lam); influence correction in eigen space: the two
@@ -421,11 +441,17 @@ __global__ void __launch_bounds__(256, 2) k_fast(PzDev d) {
       double* zr = s.R + (long long)(2 * g) * n;
       double* zi = zr + n;
       double t1r = 0.0, t1i = 0.0, b1r = 0.0, b1i = 0.0, t2 = 0.0, b2 = 0.0, t3 = 0.0, b3 = 0.0;
-      for (int k = lane; k < n; k += 32) {
+      double wD[PZ_FAST_KPL];            // w nu / (1 - w nu lam) of this lane's k
+#pragma unroll
+      for (int u = 0; u < PZ_FAST_KPL; ++u) {
+        const int k = lane + 32 * u;
+        wD[u] = 0.0;
+        if (k >= n) continue;
         const double D = 1.0 / (1.0 - wn * lam[k]);
+        wD[u] = wn * D;
         const double yr = zr[k] * D, yi = zi[k] * D;
         zr[k] = yr; zi[k] = yi;
-        const double h2 = wn * D * gbot[k], h3 = wn * D * gtop[k];
+        const double h2 = wD[u] * gbot[k], h3 = wD[u] * gtop[k];
         t1r += qt[k] * yr; t1i += qt[k] * yi; b1r += qb[k] * yr; b1i += qb[k] * yi;
         t2 += qt[k] * h2; b2 += qb[k] * h2; t3 += qt[k] * h3; b3 += qb[k] * h3;
       }
@@ -435,9 +461,11 @@ __global__ void __launch_bounds__(256, 2) k_fast(PzDev d) {
       const double i00 = b3 / det, i01 = -t3 / det, i10 = -b2 / det, i11 = t2 / det;
       const double c1r = -i00 * t1r - i01 * b1r, c1i = -i00 * t1i - i01 * b1i;
       const double c2r = -i10 * t1r - i11 * b1r, c2i = -i10 * t1i - i11 * b1i;
-      for (int k = lane; k < n; k += 32) {
-        const double D = 1.0 / (1.0 - wn * lam[k]);
-        const double h2 = wn * D * gbot[k], h3 = wn * D * gtop[k];
+#pragma unroll
+      for (int u = 0; u < PZ_FAST_KPL; ++u) {
+        const int k = lane + 32 * u;
+        if (k >= n) continue;
+        const double h2 = wD[u] * gbot[k], h3 = wD[u] * gtop[k];
         zr[k] += c1r * h2 + c2r * h3;
         zi[k] += c1i * h2 + c2i * h3;
       }

@@ -31,6 +31,7 @@
 #define PZ_FAST_MAXN 97      // exact fp32 accumulation bound on the product length
 #define PZ_FAST_G 8          // default instances per k_fast block
 #define PZ_FAST_GMAX 16      // largest instances per k_fast block
+#define PZ_FAST_KPL ((PZ_FAST_MAXN - 2 + 31) / 32)   // interior points per lane of a warp
 
 // One operator stored for the tensor cores: R x K, RT = ceil(R/16) row tiles,
 // KT = ceil(K/16) k tiles.  frag holds, for each (row tile, k tile, slice),

@@ -42,3 +42,18 @@ def series_from_oracle(sim):
     ch = rows.get("composition", [0.0] * 7)
     return np.array([ek[0], ek[1], ek[2], ek[3], e3[1], e3[2], e3[3], e3[4],
                      ht[1], ht[2], ht[3], ht[4], ht[5], ht[6], ht[7], sim.ts.dt[0]] + list(ch[1:]))
+
+
+def fp64_noise(sim, rng, level=1e-13):
+    """Add to the oracle's temperature and vorticity complex normal deviates
+    of `level` times each field's largest modulus: the size of the rounding
+    differences that another FP64 implementation (another summation order of
+    the transforms and products) makes per step.  The m = 0 modes stay real.
+    Run after every step, it measures how far the oracle drifts from itself
+    under rounding alone."""
+    for f in ("temp", "om"):
+        a = getattr(sim, f)
+        s = level * np.max(np.abs(a))
+        a = a + s * (rng.standard_normal(a.shape) + 1j * rng.standard_normal(a.shape))
+        a[0] = a[0].real
+        setattr(sim, f, a)

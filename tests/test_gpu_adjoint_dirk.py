@@ -142,3 +142,50 @@ def test_dirk_batched_instances(pz):
     for inst in (0, 1):
         errs = fd_dirs(ens, temps, g[inst], inst, 10, 6, SCHED, 2, 20 + inst, "nutop")
         assert max(errs) < GRAD_TOL, f"instance {inst}: {errs}"
+
+
+def test_batched_adjoint_workload_ars233_fd(pz):
+    """The batched adjoint workload itself (bench.batched_adjoint_specs(64):
+    64 instances, n_r_max in {49, 65}, n_phi_max in {126, 192}, Ra in
+    [1e6, 1e7], ARS233 with its assembly stage, dt = 1e-5, 300 steps,
+    checkpoint every 30) in one handle: each instance's gradient of its
+    time-averaged NuTop with respect to its initial temperature, against
+    central finite differences of the GPU forward along one seeded direction
+    on 4 instances of different grids, eps = 1e-4 relative to the
+    perturbation (J = mean NuTop is 1 + O(1e-2); below 1e-5 the difference
+    quotient is dominated by the rounding of J)."""
+    import os
+    import sys
+    sys.path.insert(0, os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
+    import bench
+    specs = bench.batched_adjoint_specs(64)
+    temps = [bench.seeded_temp(s) for s in specs]
+    n_steps, ck = bench.BADJ_STEPS, bench.BADJ_CK
+    sched = np.full((len(specs), n_steps), bench.BADJ_DT)
+    ens = pz.Ensemble([bench.gpu_cfg(s) for s in specs])
+    ens.set_state_all(temps)
+    J, _ = ens.adjoint_forward(n_steps, n_steps, ck, sched, objective="nutop")
+    assert np.all(np.isfinite(J))
+    g, _ = ens.adjoint_backward()
+    # one instance of each (n_r_max, m_max) class
+    picks = []
+    for cls in sorted({(s["n_r_max"], s["m_max"]) for s in specs}):
+        picks.append(next(i for i, s in enumerate(specs) if (s["n_r_max"], s["m_max"]) == cls))
+    rng = np.random.default_rng(77)
+    errs = {}
+    for inst in picks:
+        d = rng.standard_normal(temps[inst].shape) + 1j * rng.standard_normal(temps[inst].shape)
+        d[0] = d[0].real
+        eps = 1e-4 * np.max(np.abs(temps[inst])) / np.max(np.abs(d))
+        jj = []
+        for sgn in (1.0, -1.0):
+            tp = list(temps)
+            tp[inst] = temps[inst] + sgn * eps * d
+            ens.set_state_all(tp)
+            Jp, _ = ens.adjoint_forward(n_steps, n_steps, ck, sched, objective="nutop")
+            jj.append(Jp[inst])
+        fd = (jj[0] - jj[1]) / (2 * eps)
+        errs[inst] = abs(fd - directional(g[inst], d)) / abs(fd)
+    ens.close()
+    assert len(picks) == 4
+    assert max(errs.values()) < 1e-6, errs

@@ -7,13 +7,22 @@ Ekman numbers, the highest and lowest Rayleigh numbers -- are compared with
 the oracle at steps 50, 100, 200, 300 and 500 on the fields and on the
 time-series row, and on the sequence of Courant time steps.
 
-The workload is chaotic at its higher Rayleigh numbers: the oracle itself,
-started from its own initial field perturbed by 1e-13 relative (the size of
-the GPU's rounding differences per step), drifts away from its unperturbed
-run at a rate set by the flow, to O(1) within a few hundred steps for
-Ra ~ 1e7.  So the bar at each checkpoint is 1e-10 relative while the
-oracle's own 1e-13 spread is below 1e-12, and 100x that spread beyond (the
-GPU must stay as close to the oracle as the oracle stays to itself).
+The workload is chaotic at its higher Rayleigh numbers, and at E = 1e-4 the
+vorticity equation amplifies small disturbances strongly even at low Ra:
+the oracle itself, with complex normal deviates of 1e-13 times each field's
+largest modulus added to its temperature and vorticity after every step (the
+size of the rounding differences another FP64 implementation makes per
+step), drifts away from its unperturbed run at a rate set by the flow, to
+O(1) within a few hundred steps for Ra ~ 1e7.  So the bar at each checkpoint
+is 1e-10 relative while that spread of the oracle is below 1e-12, and 100x
+the spread beyond (the GPU must stay as close to the oracle as the oracle
+stays to itself), on the fields and on the time-series row (against the
+larger of the field and series spreads).  Past the predictability horizon,
+where the oracle's spread exceeds 1e-6, no pointwise comparison means
+anything; there the GPU state must be finite and of the oracle's magnitude
+(the largest modulus of each field within a factor of 10).  The dense FP64
+kernels (pz_fast_path(0)) run the same workload beside the tensor-core stage
+and are reported with it.
 
 The Courant controller (src/courant.f90:78-167) keeps or changes dt by
 comparing dt with the Courant step at a hysteresis factor.  When that
@@ -59,23 +68,24 @@ def pick(specs):
 
 def _oracle_run(args):
     """Oracle trajectory of one bench instance: (T, om, series row) at CK,
-    from the seeded start, optionally perturbed by `pert` relative."""
+    from the seeded start; with `pert`, fp64_noise of that level after every
+    step."""
     i, pert = args
     sys.path.insert(0, ROOT)
     import bench
     from oracle.pizza_oracle import Params, Pizza
-    from tests.helpers import series_from_oracle
+    from tests.helpers import fp64_noise, series_from_oracle
     spec = bench.ensemble_specs(256)[i]
     kw = {k: v for k, v in spec.items() if k != "seed"}
     sim = Pizza(Params(**kw))
-    t0 = bench.seeded_temp(spec)
-    if pert:
-        t0 = t0 * (1.0 + pert * np.random.default_rng(1000 + i).standard_normal(t0.shape))
-    sim.start(temp0=t0)
+    sim.start(temp0=bench.seeded_temp(spec))
+    rng = np.random.default_rng(1000 + i)
     out, done, dts = {}, 0, []
     for k in CK:
         for _ in range(k - done):
             sim.advance()
+            if pert:
+                fp64_noise(sim, rng, pert)
             dts.append(sim.ts.dt[0])
         done = k
         out[k] = (sim.temp.copy(), sim.om.copy(), series_from_oracle(sim))
@@ -86,6 +96,10 @@ def _oracle_run(args):
 def _err(a, b):
     return max(float(np.max(np.abs(a[0] - b[0])) / np.max(np.abs(b[0]))),
                float(np.max(np.abs(a[1] - b[1])) / np.max(np.abs(b[1]))))
+
+
+def _serr(a, b):
+    return max(abs(a[c] - b[c]) / max(abs(b[c]), 1e-300) for c in SERIES)
 
 
 @pytest.fixture(scope="module")
@@ -112,20 +126,32 @@ def test_batched_ensemble_matches_oracle_over_500_steps(pz):
         res = pool.map(_oracle_run, jobs)
     ref = {i: o for i, p, o in res if p == 0.0}
     spread = {i: o for i, p, o in res if p != 0.0}
-    ens = pz.Ensemble([bench.gpu_cfg(s) for s in specs])
-    ens.set_state_all([bench.seeded_temp(s) for s in specs])
-    got = {i: {} for i in sel}
-    done = 0
-    for k in CK:
-        ens.step(k - done)
-        done = k
-        rows = ens.latest_rows()
-        for i in sel:
-            g = ens.get_state(i)
-            got[i][k] = (g["temp"], g["om"], rows[i])
-    report, strict_until, split = [], {}, {}
+
+    def gpu_run(fast):
+        prev = pz.fast_path(fast)
+        try:
+            e = pz.Ensemble([bench.gpu_cfg(s) for s in specs])
+        finally:
+            pz.fast_path(prev)
+        e.set_state_all([bench.seeded_temp(s) for s in specs])
+        out = {i: {} for i in sel}
+        done = 0
+        for k in CK:
+            e.step(k - done)
+            done = k
+            rows = e.latest_rows()
+            for i in sel:
+                g = e.get_state(i)
+                out[i][k] = (g["temp"], g["om"], rows[i])
+        return e, out
+
+    dense_ens, dense = gpu_run(False)
+    dense_ens.close()
+    ens, got = gpu_run(True)
+    assert ens.profile_steps(1)["k_fast"] > 0.0
+    report, strict_until, split, fails = [], {}, {}, []
     for i in sel:
-        dt_gpu = ens.series(i, CK[-1] + 1)[1:, 15]
+        dt_gpu = ens.series(i, CK[-1] + 2)[1:CK[-1] + 1, 15]
         dev = np.abs(dt_gpu - ref[i]["dt"]) / ref[i]["dt"]
         first = np.nonzero(dev > 1e-9)[0]
         # a branch of the Courant hysteresis taken differently: the first
@@ -134,26 +160,40 @@ def test_batched_ensemble_matches_oracle_over_500_steps(pz):
         strict_until[i] = 0
         for k in CK:
             e = _err(got[i][k], ref[i][k])
+            ed = _err(dense[i][k], ref[i][k])
             fl = _err(spread[i][k], ref[i][k])
-            rs = [abs(got[i][k][2][c] - ref[i][k][2][c]) / max(abs(ref[i][k][2][c]), 1e-300) for c in SERIES]
-            report.append((i, k, e, fl, max(rs), split[i]))
-            assert np.all(np.isfinite(got[i][k][0])) and np.all(np.isfinite(got[i][k][1]))
+            rs = _serr(got[i][k][2], ref[i][k][2])
+            rfl = _serr(spread[i][k][2], ref[i][k][2])
+            report.append((i, k, e, ed, fl, rs, rfl, split[i]))
+            if not (np.all(np.isfinite(got[i][k][0])) and np.all(np.isfinite(got[i][k][1]))):
+                fails.append(f"instance {i} step {k}: non-finite state")
+                continue
             if split[i] is not None and k >= split[i]:
                 continue
+            if fl > 1e-6:
+                # past the predictability horizon: magnitudes only
+                for a, b, name in ((got[i][k][0], ref[i][k][0], "temp"), (got[i][k][1], ref[i][k][1], "om")):
+                    q = np.max(np.abs(a)) / np.max(np.abs(b))
+                    if not 0.1 < q < 10.0:
+                        fails.append(f"instance {i} step {k}: {name} magnitude ratio {q:.2e}")
+                continue
             tol = 1e-10 if fl < 1e-12 else max(1e-10, 100.0 * fl)
-            assert e <= tol, f"instance {i} step {k}: field rel err {e:.2e}, oracle 1e-13 spread {fl:.2e}"
-            assert max(rs) <= max(tol, 1e-9), f"instance {i} step {k}: series rel err {max(rs):.2e}"
+            if e > tol:
+                fails.append(f"instance {i} step {k}: field rel err {e:.2e} (dense {ed:.2e}), oracle spread {fl:.2e}")
+            if rs > max(tol, 1e-9, 100.0 * rfl):
+                fails.append(f"instance {i} step {k}: series rel err {rs:.2e}, oracle spread {rfl:.2e}")
             if e <= 1e-10 and strict_until[i] == (CK[CK.index(k) - 1] if k != CK[0] else 0):
                 strict_until[i] = k
+    out_dir = os.path.join(ROOT, "gpurun_out")
+    with open(os.path.join(out_dir, "bench_parity.txt") if os.path.isdir(out_dir) else os.devnull, "w") as f:
+        for i, k, e, ed, fl, rs, rfl, sp in report:
+            f.write(f"inst {i} N={specs[i]['n_r_max']} P={3 * specs[i]['m_max']} ek={specs[i]['ek']} "
+                    f"Ra={specs[i]['ra']:.3g} step {k}: fast {e:.2e} dense {ed:.2e} series {rs:.2e} "
+                    f"oracle-spread {fl:.2e} series-spread {rfl:.2e} dt-split {sp}\n")
+    assert not fails, "\n".join(fails)
     assert sum(v is not None for v in split.values()) <= 2, split
     # the strict bar holds over all 500 steps wherever the flow is predictable
     # at that level (the oracle's own spread stays below 1e-12) and dt did not split
     for i in sel:
         if split[i] is None and all(_err(spread[i][k], ref[i][k]) < 1e-12 for k in CK):
             assert strict_until[i] == CK[-1], (i, strict_until[i])
-    with open(os.path.join(ROOT, "gpurun_out", "bench_parity.txt") if os.path.isdir(
-            os.path.join(ROOT, "gpurun_out")) else os.devnull, "w") as f:
-        for i, k, e, fl, rs, sp in report:
-            f.write(f"inst {i} N={specs[i]['n_r_max']} P={3 * specs[i]['m_max']} ek={specs[i]['ek']} "
-                    f"Ra={specs[i]['ra']:.3g} step {k}: gpu {e:.2e} series {rs:.2e} oracle-spread {fl:.2e} "
-                    f"dt-split {sp}\n")
