@@ -287,6 +287,11 @@ module pizza_gpu
          integer(c_int), value :: enable
       end function pz_fast_path
 
+      integer(c_int) function pz_integ_banded(enable) bind(c, name='pz_integ_banded')
+         import :: c_int
+         integer(c_int), value :: enable
+      end function pz_integ_banded
+
       integer(c_int) function pz_tune_set(what, key, value) bind(c, name='pz_tune_set')
          import :: c_int
          integer(c_int), value :: what, key, value

@@ -352,6 +352,17 @@ int pz_integ_operator(int n_r_max, double radratio, int which, double* out, int*
  * entry points always run the dense kernels. */
 int pz_fast_path(int enable);
 
+/* Process-wide choice, for handles created afterwards, of how the
+ * integration method (cheb_method='integ') solves its per-m tau-bordered
+ * systems.  enable = 1 (the default): bordered banded LU factors, as the
+ * reference's type_bordmat (src/bordered_matrix.f90:137-183 over
+ * src/band_matrix.f90:212-261): the banded block is factorised with partial
+ * pivoting inside the band when dt changes, the tau rows through a Schur
+ * complement, and every stage runs banded sweeps.  enable = 0: dense per-m
+ * inverses applied as dense products.  Both give the reference's step to
+ * FP64 rounding.  enable < 0 only queries.  Returns the previous setting. */
+int pz_integ_banded(int enable);
+
 /* No counterpart in the reference (pizza chooses its MPI transpose variant
  * by timing, src/communications.f90:407-516; this is the same idea for the
  * kernels' launch shapes).  Process-wide tuning table read by pz_create for

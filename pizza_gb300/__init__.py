@@ -190,6 +190,7 @@ def load_library(path: str | None = None):
     lib.pz_get_spectra.argtypes = [vp, ctypes.c_int, dp]
     lib.pz_integ_operator.argtypes = [ctypes.c_int, ctypes.c_double, ctypes.c_int, dp, ctypes.POINTER(ctypes.c_int)]
     lib.pz_fast_path.argtypes = [ctypes.c_int]
+    lib.pz_integ_banded.argtypes = [ctypes.c_int]
     lib.pz_probe_peaks.argtypes = [dp, dp]
     lib.pz_tune_set.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int]
     lib.pz_fast_eigen.argtypes = [ctypes.c_int, ctypes.c_double, ctypes.c_int, dp, dp]
@@ -202,7 +203,7 @@ def load_library(path: str | None = None):
               "pz_step_profile", "pz_explicit_terms", "pz_explicit_terms_noalloc", "pz_adjoint_forward",
               "pz_adjoint_backward", "pz_adjoint_grid_snapshots", "pz_set_ra", "pz_get_history", "pz_set_history", "pz_get_step_state",
               "pz_set_step_state", "pz_set_restart_ab1", "pz_get_spectra", "pz_integ_operator",
-              "pz_fast_path", "pz_fast_eigen", "pz_probe_peaks", "pz_tune_set", "pz_destroy"):
+              "pz_fast_path", "pz_integ_banded", "pz_fast_eigen", "pz_probe_peaks", "pz_tune_set", "pz_destroy"):
         getattr(lib, f).restype = ctypes.c_int
     _lib = lib
     return lib
@@ -222,6 +223,15 @@ def integ_operator(n_r_max: int, radratio: float, name: str):
     if rc != 0:
         raise RuntimeError(lib.pz_last_error(None).decode())
     return out.reshape(n_r_max, n_r_max, order="F"), bw.value
+
+
+def integ_banded(enable=None) -> bool:
+    """Bordered banded factors (True, the default) or dense per-m inverses
+    (False) for the integration method's solves, for handles created
+    afterwards (pz_integ_banded); None only queries.  Returns the previous
+    setting."""
+    lib = load_library()
+    return bool(lib.pz_integ_banded(-1 if enable is None else int(bool(enable))))
 
 
 def fast_path(enable=None) -> bool:

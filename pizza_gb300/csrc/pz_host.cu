@@ -537,6 +537,7 @@ int validate(const pz_config& c, std::string* why) {
 // ===========================================================================
 // process-wide default of the tensor-core stage for handles created afterwards
 int g_fast_default = 1;
+int g_integ_banded = 1;   // integration method: bordered banded factors (else dense inverses)
 // process-wide tuning table (pz_tune_set): k_fast instances per block, and
 // k_rloop radii per block by n_phi_max; 0 = the built-in choice
 int g_tune_fast_g = 0;
@@ -671,6 +672,12 @@ cudaError_t fast_upload(pz_handle* h, const FastBuild& fb, int G, PzFastDev* F) 
 }
 
 }  // namespace
+
+extern "C" int pz_integ_banded(int enable) {
+  const int prev = g_integ_banded;
+  if (enable >= 0) g_integ_banded = enable ? 1 : 0;
+  return prev;
+}
 
 extern "C" int pz_fast_path(int enable) {
   const int prev = g_fast_default;
@@ -839,6 +846,28 @@ extern "C" int pz_create(const pz_config* cfgs, int n, pz_handle** out) {
       }
       I.o_integ = integ_off[key];
       std::memcpy(I.im_band, integ_blocks[key].band, sizeof(I.im_band));
+      if (!g_integ_banded) I.flags |= PZF_INTEG_DENSE;
+      const int* bd = I.im_band;
+      const bool rot = !(I.flags & PZF_NON_ROT);
+      I.bkw_t = std::max(std::max(bd[IM_I2R2], bd[IM_LT0]), std::max(bd[IM_I2], bd[IM_ULAP]));
+      I.bkl_t = bord_kl(I.bkw_t);
+      I.bstr_t = bord_size(N, 2, I.bkl_t);
+      if (I.flags & PZF_DIRECT) {
+        I.bkw_p = rot ? std::max(std::max(std::max(bd[IM_Q0], bd[IM_Q1]), std::max(bd[IM_S0], bd[IM_S1])),
+                                 std::max(bd[IM_S2], bd[IM_I4R4]))
+                      : std::max(std::max(std::max(bd[IM_N0], bd[IM_N1]), std::max(bd[IM_L0], bd[IM_L1])),
+                                 std::max(bd[IM_L2], bd[IM_I4R4]));
+        I.bkl_p = bord_kl(I.bkw_p);
+        I.bstr_p = 2 * bord_size(N, 4, I.bkl_p);
+      } else {
+        I.bkw_p = rot ? std::max(bd[IM_P0], bd[IM_P1]) : std::max(bd[IM_LT0], bd[IM_I2]);
+        I.bkl_p = bord_kl(I.bkw_p);
+        I.bstr_p = bord_size(N, 2, I.bkl_p);
+      }
+      if (I.bkw_t > 8 || I.bkw_p > 8) {
+        delete h;
+        return fail(nullptr, PZ_E_UNSUPPORTED, "integration-method operator with a half band width above 8");
+      }
     }
     if (!tw_off.count(I.P)) tw_off[I.P] = take(2LL * I.P);
     I.o_tw = tw_off[I.P];
@@ -946,6 +975,21 @@ extern "C" int pz_create(const pz_config* cfgs, int n, pz_handle** out) {
   for (int i = 0; i < n; ++i) {
     PzInst& I = h->inst[i];
     const long long N = I.N, M = I.M;
+    if ((I.flags & PZF_INTEG) && !(I.flags & PZF_INTEG_DENSE)) {
+      // bordered banded factors per m (pz_bord.cuh)
+      I.o_gt = take(M * I.bstr_t);
+      I.o_gx = (I.flags & PZF_CHEM) ? take(M * I.bstr_t) : 0;
+      I.o_guphi = take(I.bstr_t);
+      if (I.flags & PZF_DIRECT) {
+        I.o_gsm = take(M * I.bstr_p);
+        I.o_gom = I.o_gpsi = I.o_aux = 0;
+      } else {
+        I.o_gom = take(M * I.bstr_t);
+        I.o_gpsi = take(M * I.bstr_p);
+        I.o_aux = take(4 * M * N + 4 * M);
+        I.o_gsm = 0;
+      }
+    } else {
     I.o_gt = take(M * N * N);
     I.o_gx = (I.flags & PZF_CHEM) ? take(M * N * N) : 0;
     I.o_guphi = take(N * N);
@@ -960,6 +1004,7 @@ extern "C" int pz_create(const pz_config* cfgs, int n, pz_handle** out) {
       I.o_gpsi = take(M * N * N);
       I.o_aux = take(4 * M * N + 4 * M);
       I.o_gsm = 0;
+    }
     }
     I.o_bt = I.dirk ? take(PZ_BT_SIZE) : 0;
     I.o_gass = (I.dirk && I.assembly) ? take(M * N * N) : 0;

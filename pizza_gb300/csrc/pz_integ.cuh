@@ -10,9 +10,14 @@
 // by r^2 (temperature, u_phi) or r^4 (streamfunction) and integrated twice
 // (four times) in r, which makes every operator except the tau rows banded:
 // the banded operators (IM_*) are applied with band_mv over their band
-// only, the dt dependent left-hand sides are inverted per m in k_build and
-// applied as dense products, like the collocation path.
+// only.  The dt dependent left-hand sides (and the influence matrix's
+// dt-independent streamfunction operator) are bordered banded systems: their
+// tau rows are dense, every other row banded.  k_build factorises them per m
+// into bordered banded LU records (pz_bord.cuh) and every stage applies those
+// with banded sweeps; pz_integ_banded(0) switches a handle created afterwards
+// to dense per-m inverses applied as dense products instead.
 #pragma once
+#include "pz_bord.cuh"
 
 // -- banded products ---------------------------------------------------------
 // y_i = sum_{|j-i|<=bw} (sum_k c_k A_k(i,j)) x_j, A_k column-major n x n;
@@ -98,6 +103,34 @@ __device__ __forceinline__ void cmvn_lanes(const double2* __restrict__ G, int n,
   lane_dots(CDenseDotN{G, n, reinterpret_cast<const double*>(x), reinterpret_cast<double*>(y)}, 2 * n, n);
 }
 
+// -- applying the per-m left-hand-side inverses ---------------------------------
+// y = A^-1 x for the temperature-like operators (temperature, composition,
+// u_phi, vorticity) at base (o_gt, o_gx, o_guphi with mi = 0, o_gom) and for
+// the influence matrix's streamfunction operator (psi: base o_gpsi): the
+// bordered banded record of m, or the dense inverse with PZF_INTEG_DENSE.
+// st: shared staging space (integ_stage_bytes), red: 8 doubles of shared memory.
+__device__ __forceinline__ void integ_apply(const PzDev& d, const PzInst& I, long long base, int mi, bool psi,
+                                            const double2* x, double2* y, double* st, double* red) {
+  const int n = I.N;
+  if (I.flags & PZF_INTEG_DENSE) {
+    mv_lanes(d.pool + base + (long long)mi * n * n, n, x, y);
+    return;
+  }
+  const long long str = psi ? I.bstr_p : I.bstr_t;
+  bord_solve<double>(d.pool + base + mi * str, n, 2, psi ? I.bkl_p : I.bkl_t, x, y, st, red);
+}
+// the direct solve's complex streamfunction operator
+__device__ __forceinline__ void integ_apply_sm(const PzDev& d, const PzInst& I, int mi, const double2* x, double2* y,
+                                               double* st, double* red) {
+  const int n = I.N;
+  if (I.flags & PZF_INTEG_DENSE) {
+    cmvn_lanes(reinterpret_cast<const double2*>(d.pool + I.o_gsm) + (long long)mi * n * n, n, x, y);
+    return;
+  }
+  bord_solve<double2>(reinterpret_cast<const double2*>(d.pool + I.o_gsm + mi * I.bstr_p), n, 4, I.bkl_p, x, y,
+                      reinterpret_cast<double2*>(st), red);
+}
+
 // -- m = 0 derivative with the round-off threshold ---------------------------
 // get_dcheb_real_1d (src/radial_derivatives.f90:143-185) on the real parts of
 // the Chebyshev coefficients c: with thr > 0, a coefficient below
@@ -157,11 +190,41 @@ __device__ __forceinline__ double dmat_bc_bot(const PzInst& I, int j) {
 // = -I2[r^2 omega(psi)] = -(P0 + m^2 P1) (I2[r^2 Lap_m] = LT0 - m^2 I2 without
 // rotation), tau rows psi(r_o) = psi(r_i) = 0, row preconditioning; stored as
 // G_psi = A_s^-1 diag(fac) at o_gpsi.  Shared memory: the BuildSmem layout.
+// Tau rows T_j(+-1) (rows 0 and 1: value 1, (-1)^j; boundary_fac on column
+// 0), times rnorm, then the rows of c0 A0 + c1 A1 + c2 A2 (A_k integration
+// operators, a null A2 skipped): the real operators of the integration method
+struct IntegGet {
+  const double *A0, *A1, *A2;
+  double c0, c1, c2, rn;
+  int n;
+  __device__ double operator()(int i, int j) const {
+    if (i < 2) {
+      const double v = rn * ((i == 1 && (j & 1)) ? -1.0 : 1.0);
+      return j == 0 ? 0.5 * v : v;
+    }
+    const long long c = i + (long long)j * n;
+    double v = c0 * A0[c] + c1 * A1[c];
+    if (A2) v += c2 * A2[c];
+    return v;
+  }
+};
+// shared memory of the banded factorisations: workspace for the largest
+// record (complex, 4 tau rows, kl = 8), its pivots and a flag
+__host__ __device__ inline long long integ_bord_ws_doubles(int n) {
+  return 2 * bord_ws_size(n, 4, 8) + (n + 1) / 2 + 2;
+}
+
 __device__ int integ_psi_static(const PzDev& d, const PzInst& I, const View& V, int mi) {
   extern __shared__ double shb[];
   const int n = I.N, m = mi * I.minc;
   const double dm2 = (double)m * (double)m, rn = I.rnorm;
   const bool rot = !(I.flags & PZF_NON_ROT);
+  if (!(I.flags & PZF_INTEG_DENSE)) {
+    const IntegGet g{im_op(V, rot ? IM_P0 : IM_LT0), im_op(V, rot ? IM_P1 : IM_I2), nullptr,
+                     rot ? -1.0 : 1.0, -dm2, 0.0, rn, n};
+    int* flag = reinterpret_cast<int*>(shb + integ_bord_ws_doubles(n) - 1);
+    return bord_factor<double>(g, n, 2, I.bkl_p, I.bkw_p, shb, flag, d.pool + I.o_gpsi + mi * I.bstr_p);
+  }
   double* A = shb;
   double* f1 = A + (long long)n * n;
   double* colk = f1 + n + n;
@@ -206,8 +269,105 @@ __device__ int integ_psi_static(const PzDev& d, const PzInst& I, const View& V, 
 // that x = G rhs.  Unlike the collocation builders nothing is truncated: the
 // integration method keeps all n_r_max coefficients of the solution.
 // Shared memory: see pz_build_smem_bytes (integ).
+// The complex streamfunction operator of the direct solve, m /= 0 (the
+// dense builder below spells out its rows)
+struct IntegGetSm {
+  const double *Q0, *Q1, *S0, *S1, *S2, *R4;
+  double sg0, dm2, cv, cc, rn;
+  int n;
+  bool rot;
+  __device__ double2 operator()(int i, int j) const {
+    if (i < 4) {
+      const double dj = (double)j, dn2 = dj * dj, sg = (j & 1) ? -1.0 : 1.0;
+      double re;
+      if (i == 0) re = 1.0;
+      else if (i == 1) re = sg;
+      else if (i == 2) re = rot ? 8.0 / 15.0 * dn2 * (dn2 - 1.0) * (dn2 - 4.0) : 2.0 * dn2;
+      else re = -2.0 * dn2 * sg;
+      re *= rn;
+      if (j == 0) re *= 0.5;
+      return make_double2(re, 0.0);
+    }
+    const long long c = i + (long long)j * n;
+    return make_double2(sg0 * (Q0[c] + dm2 * Q1[c] - cv * (S0[c] + dm2 * (S1[c] + dm2 * S2[c]))), cc * R4[c]);
+  }
+};
+
+// integ_build with bordered banded factors (the same operators as the dense
+// builder below)
+__device__ int integ_build_banded(const PzDev& d, const PzInst& I, const View& V, int mi, double wlin) {
+  extern __shared__ double shb[];
+  const int n = I.N, m = mi * I.minc;
+  const double dm = (double)m, dm2 = dm * dm, rn = I.rnorm;
+  const bool dmat = !(I.flags & PZF_DIRECT);
+  int* flag = reinterpret_cast<int*>(shb + integ_bord_ws_doubles(n) - 1);
+  for (int pass = 0; pass < 3; ++pass) {
+    if (pass == 1 && !(I.flags & PZF_CHEM)) continue;
+    if (pass == 2 && m != 0 && !dmat) break;
+    const bool scal = pass < 2;
+    const double c0 = wlin * (pass == 0 ? I.TdiffFac : pass == 1 ? I.XidiffFac : I.ViscFac);
+    const double c1 = (scal || m != 0) ? -dm2 * c0 : 0.0;
+    // I2R2 - c0 L0 - c1 I2
+    const IntegGet g{im_op(V, IM_I2R2), im_op(V, (scal || m != 0) ? IM_LT0 : IM_ULAP), im_op(V, IM_I2),
+                     1.0, -c0, -c1, rn, n};
+    double* out = d.pool + (pass == 0   ? I.o_gt + mi * I.bstr_t
+                            : pass == 1 ? I.o_gx + mi * I.bstr_t
+                                        : (m == 0 ? I.o_guphi : I.o_gom + mi * I.bstr_t));
+    if (bord_factor<double>(g, n, 2, I.bkl_t, I.bkw_t, shb, flag, out)) return -1;
+  }
+  if (m == 0) return 0;
+  if (dmat) {
+    // get_intermediate_sol + get_influence_matrix (update_psi_integ_dmat.f90:1212-1313):
+    // omega = 1 on the inner (set 1: om2, psi2) or outer (set 2: om3, psi3)
+    // wall, packed as the real and imaginary parts of one complex vector
+    double2* x = reinterpret_cast<double2*>(shb);
+    double2* va = x + n;
+    double2* vb = va + n;
+    double2* vc = vb + n;
+    double* st = reinterpret_cast<double*>(vc + n);
+    double* red = st + (long long)(n - 2) * (3 * 8 + 2);
+    for (int i = threadIdx.x; i < n; i += blockDim.x)
+      x[i] = make_double2(i == 1 ? 1.0 : 0.0, i == 0 ? 1.0 : 0.0);
+    __syncthreads();
+    integ_apply(d, I, I.o_gom, mi, false, x, va, st, red);
+    band_mv(band1(V, IM_I2R2, -1.0), n, va, vb);
+    __syncthreads();
+    integ_apply(d, I, I.o_gpsi, mi, true, vb, vc, st, red);
+    double* aux = d.pool + I.o_aux;
+    const long long MN = (long long)I.M * n;
+    double t2 = 0.0, t3 = 0.0, b2 = 0.0, b3 = 0.0;
+    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+      aux[0 * MN + (long long)mi * n + i] = va[i].x;
+      aux[1 * MN + (long long)mi * n + i] = va[i].y;
+      aux[2 * MN + (long long)mi * n + i] = vc[i].x;
+      aux[3 * MN + (long long)mi * n + i] = vc[i].y;
+      const double ct = dmat_bc_top(I, i), cb = dmat_bc_bot(I, i);
+      t2 += ct * vc[i].x; t3 += ct * vc[i].y;
+      b2 += cb * vc[i].x; b3 += cb * vc[i].y;
+    }
+    t2 = block_sum(t2, red); t3 = block_sum(t3, red);
+    b2 = block_sum(b2, red); b3 = block_sum(b3, red);
+    if (threadIdx.x == 0) {
+      double* infl = aux + 4 * MN + 4LL * mi;
+      const double det = t2 * b3 - t3 * b2;
+      infl[0] = b3 / det; infl[1] = -t3 / det; infl[2] = -b2 / det; infl[3] = t2 / det;
+    }
+    return 0;
+  }
+  const bool rot = !(I.flags & PZF_NON_ROT);
+  const IntegGetSm g{im_op(V, rot ? IM_Q0 : IM_N0), im_op(V, rot ? IM_Q1 : IM_N1), im_op(V, rot ? IM_S0 : IM_L0),
+                     im_op(V, rot ? IM_S1 : IM_L1), im_op(V, rot ? IM_S2 : IM_L2), im_op(V, IM_I4R4),
+                     rot ? 1.0 : -1.0, dm2, wlin * I.ViscFac,
+                     (I.flags & PZF_COR_IMP) ? wlin * I.CorFac * dm : 0.0, rn, n, rot};
+  return bord_factor<double2>(g, n, 4, I.bkl_p, I.bkw_p, reinterpret_cast<double2*>(shb), flag,
+                              reinterpret_cast<double2*>(d.pool + I.o_gsm + mi * I.bstr_p))
+             ? -1
+             : 0;
+}
+
 __device__ int integ_build(const PzDev& d, const PzInst& I, const View& V, int mi, double wlin) {
   extern __shared__ double shb[];
+  if (!(I.flags & PZF_INTEG_DENSE)) return integ_build_banded(d, I, V, mi, wlin);
   const int n = I.N, m = mi * I.minc;
   const double dm = (double)m, dm2 = dm * dm, rn = I.rnorm;
   double* A = shb;
@@ -502,11 +662,11 @@ __device__ bool integ_dmat_psi(const PzDev& d, const View& V, const PzInst& I, c
     s.k[i] = buo_imp ? s.e[i] : make_double2(0.0, 0.0);
   }
   __syncthreads();
-  mv_lanes(d.pool + I.o_gom + (long long)mi * n * n, n, s.a, s.b);      // omega_hat
+  integ_apply(d, I, I.o_gom, mi, false, s.a, s.b, s.st, s.red);         // omega_hat
   __syncthreads();
   band_mv(band1(V, IM_I2R2, -1.0), n, s.b, s.c);
   __syncthreads();
-  mv_lanes(d.pool + I.o_gpsi + (long long)mi * n * n, n, s.c, s.e);     // psi_hat, particular
+  integ_apply(d, I, I.o_gpsi, mi, true, s.c, s.e, s.st, s.red);         // psi_hat, particular
   __syncthreads();
   double tr = 0.0, ti = 0.0, br = 0.0, bi = 0.0;
   for (int i = threadIdx.x; i < n; i += blockDim.x) {
@@ -706,7 +866,7 @@ __device__ bool integ_stage(const PzDev& d, const View& V, const PzInst& I, cons
     s.a[i] = i < 2 ? make_double2(0.0, 0.0) : v;
   }
   __syncthreads();
-  mv_lanes(d.pool + I.o_gt + (long long)mi * n * n, n, s.a, s.b);
+  integ_apply(d, I, I.o_gt, mi, false, s.a, s.b, s.st, s.red);
   __syncthreads();
   op_C(V, n, s.b, s.f, s.w);                                     // T (physical), kept in s.f
   __syncthreads();
@@ -728,7 +888,7 @@ __device__ bool integ_stage(const PzDev& d, const View& V, const PzInst& I, cons
       s.a[i] = i < 2 ? make_double2(0.0, 0.0) : v;               // topxi, botxi = 0
     }
     __syncthreads();
-    mv_lanes(d.pool + I.o_gx + (long long)mi * n * n, n, s.a, s.b);
+    integ_apply(d, I, I.o_gx, mi, false, s.a, s.b, s.st, s.red);
     __syncthreads();
     op_C(V, n, s.b, s.g, s.w);                                   // xi (physical)
     __syncthreads();
@@ -755,7 +915,7 @@ __device__ bool integ_stage(const PzDev& d, const View& V, const PzInst& I, cons
       s.a[i] = make_double2(v.x, 0.0);
     }
     __syncthreads();
-    mv_lanes(d.pool + I.o_guphi, n, s.a, s.b);                   // u_phi, Chebyshev
+    integ_apply(d, I, I.o_guphi, 0, false, s.a, s.b, s.st, s.red);  // u_phi, Chebyshev
     __syncthreads();
     op_C(V, n, s.b, s.g, s.w);
     __syncthreads();
@@ -805,7 +965,7 @@ __device__ bool integ_stage(const PzDev& d, const View& V, const PzInst& I, cons
     s.a[i] = v;
   }
   __syncthreads();
-  cmvn_lanes(reinterpret_cast<const double2*>(d.pool + I.o_gsm) + (long long)mi * n * n, n, s.a, s.b);
+  integ_apply_sm(d, I, mi, s.a, s.b, s.st, s.red);
   __syncthreads();
   op_C(V, n, s.b, s.h, s.w);                                     // psi
   __syncthreads();

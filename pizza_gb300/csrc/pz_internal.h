@@ -55,6 +55,8 @@ enum {
                        // update_xi_integ.f90, ChemFac buoyancy
   PZF_FAST     = 1024, // collocation influence-matrix CNAB2 instance whose stage runs in
                        // k_fast (tensor cores, eigen-basis solves) on the plain step
+  PZF_INTEG_DENSE = 2048, // integration method with dense per-m inverses in place of the
+                          // bordered banded factors (pz_integ_banded(0))
 };
 
 // integration-method operators (N x N, column-major, times rnorm, tau rows
@@ -170,9 +172,27 @@ struct PzInst {
   long long o_series;       // PZ_SERIES_CAP*16
   long long o_integ;        // integration method: IM_COUNT*N*N (shared by equal N, radratio)
   int im_band[IM_COUNT];    // bandwidth of each IM_ operator (max |i-j| of a nonzero)
+  // integration method, bordered banded factors (pz_bord.cuh): half band
+  // widths (bkw: of the operator, bkl: of the record) and record strides per
+  // m in doubles, of the temperature-like operators (temperature,
+  // composition, u_phi, vorticity; 2 tau rows, real) and of the
+  // streamfunction operator (influence matrix: 2 tau rows, real; direct
+  // solve: 4 tau rows, complex)
+  int bkw_t, bkl_t, bkw_p, bkl_p;
+  long long bstr_t, bstr_p;
   int rg;                   // radii per k_rloop block
   double rerr_thr;          // rerror_fac * epsilon with l_rerror_fix, else 0
 };
+
+// bordered banded factors of the integration method (pz_bord.cuh): kl of a
+// record (the operator's half band width rounded up to 2, 4 or 8) and the
+// record's size in entries (doubles, or double2 for a complex operator) for
+// order n with nt tau rows
+__host__ __device__ inline int bord_kl(int bw) { return bw <= 2 ? 2 : bw <= 4 ? 4 : 8; }
+__host__ __device__ inline long long bord_size(int n, int nt, int kl) {
+  const long long nb = n - nt;
+  return nb * (3 * kl + 2) + 2LL * nt * nb + (long long)nt * nt + n;
+}
 
 struct PzState {
   double time;

@@ -842,7 +842,18 @@ struct MS {   // per-m vectors in shared memory
   double2 *a, *b, *c, *e, *f, *g, *h, *k;
   SymScratch w;
   double* red;
+  double* st;   // k_mloop_integ: staging space of the bordered banded sweeps
 };
+__host__ __device__ inline size_t ms_smem_bytes(int n) {
+  const size_t h2 = (size_t)(n + 1) / 2;
+  return 8 * (size_t)n * sizeof(double2) + 2 * h2 * sizeof(double2) + 8 * h2 * sizeof(double) + 64 * sizeof(double);
+}
+// k_mloop_integ: the MS vectors of the largest grid, then the staging space
+// of the largest record rows (complex, kl = 8)
+__host__ __device__ inline size_t integ_st_offset(int maxN) { return (ms_smem_bytes(maxN) + 15) & ~(size_t)15; }
+__host__ __device__ inline size_t integ_mloop_smem_bytes(int maxN) {
+  return integ_st_offset(maxN) + (size_t)maxN * (3 * 8 + 2) * sizeof(double2);
+}
 
 template <bool CHEM>
 __device__ void imp_from_physical(const View& V, const PzInst& I, int mi, int bo, int bi, bool calc, MS& s) {
@@ -954,6 +965,7 @@ __device__ MS ms_smem(int n) {
   s.w.t1 = reinterpret_cast<double*>(s.w.a + h2);
   s.w.t2 = s.w.t1 + 4 * h2;
   s.red = s.w.t2 + 4 * h2;
+  s.st = nullptr;
   return s;
 }
 
@@ -1464,6 +1476,10 @@ __global__ void __launch_bounds__(256, 3) k_mloop_integ(PzDev d, int stage) {
   c.calc = c.dirk ? ((I.imp_mask >> (tgt - 1)) & 1) != 0 : S.l_calc_lin != 0;
   const View V{&I, d.pool};
   MS s = ms_smem(I.N);
+  {
+    extern __shared__ double2 shm[];
+    s.st = reinterpret_cast<double*>(reinterpret_cast<unsigned char*>(shm) + integ_st_offset(d.maxN));
+  }
   const bool bad = integ_stage<true>(d, V, I, S, it.idx, c, s);
   if (__syncthreads_or(bad)) flag_status(Sg, PZ_E_NONFINITE);
 }
@@ -1795,10 +1811,6 @@ size_t build_smem_bytes(int n) {
   off += 4LL * n;
   return (size_t)off * sizeof(double);
 }
-size_t ms_smem_bytes(int n) {
-  const size_t h2 = (size_t)(n + 1) / 2;
-  return 8 * (size_t)n * sizeof(double2) + 2 * h2 * sizeof(double2) + 8 * h2 * sizeof(double) + 64 * sizeof(double);
-}
 // threads of the per-m kernels: one lane per (row, re/im) task of the
 // widest product, rounded up to whole warps
 int mloop_threads(int maxN) {
@@ -1826,6 +1838,7 @@ cudaError_t pz_setup_kernels() {
   if ((e = cudaFuncSetAttribute(k_build_mloop<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, PZ_SMEM_MAX))) return e;
   if ((e = cudaFuncSetAttribute(k_build_mloop<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, PZ_SMEM_MAX))) return e;
   if ((e = cudaFuncSetAttribute(k_build_static, cudaFuncAttributeMaxDynamicSharedMemorySize, big))) return e;
+  if ((e = cudaFuncSetAttribute(k_mloop_integ, cudaFuncAttributeMaxDynamicSharedMemorySize, PZ_SMEM_MAX))) return e;
   if ((e = cudaFuncSetAttribute(k_rloop<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, PZ_SMEM_MAX))) return e;
   if ((e = cudaFuncSetAttribute(k_rloop<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, PZ_SMEM_MAX))) return e;
   return cudaSuccess;
@@ -1834,9 +1847,11 @@ cudaError_t pz_setup_kernels() {
 size_t pz_build_smem_bytes(int n, bool direct, bool integ) {
   const size_t a = build_smem_bytes(n);
   if (integ) {
-    // integ_build: complex n x n, f1 (even), colk (2n), red, redi, piv
+    // integ_build: complex n x n, f1 (even), colk (2n), red, redi, piv;
+    // the banded factorisations: integ_bord_ws_doubles
     const size_t nd = 2 * (size_t)n * n + (((size_t)n + 1) & ~(size_t)1) + 2 * (size_t)n + 32 + 16 + ((size_t)n + 1) / 2;
-    return nd * sizeof(double);
+    const size_t nb = (size_t)integ_bord_ws_doubles(n);
+    return (nd > nb ? nd : nb) * sizeof(double);
   }
   if (!direct) return a;
   const size_t b = build_smat_smem_bytes(n);
@@ -1844,7 +1859,8 @@ size_t pz_build_smem_bytes(int n, bool direct, bool integ) {
 }
 
 cudaError_t pz_launch_build_static(const PzDev& d, cudaStream_t s) {
-  k_build_static<<<d.n_mitems, PZ_THREADS, build_smem_bytes(d.maxN), s>>>(d);
+  const size_t a = build_smem_bytes(d.maxN), b = (size_t)integ_bord_ws_doubles(d.maxN) * sizeof(double);
+  k_build_static<<<d.n_mitems, PZ_THREADS, a > b ? a : b, s>>>(d);
   return cudaGetLastError();
 }
 
@@ -1891,7 +1907,7 @@ cudaError_t pz_launch_step_kernel(const PzDev& d, int kind, int stage, cudaStrea
       break;
     }
     case PZK_MLOOP_INTEG:
-      k_mloop_integ<<<d.n_mitems, mloop_threads(d.maxN), ms_smem_bytes(d.maxN), s>>>(d, stage);
+      k_mloop_integ<<<d.n_mitems, mloop_threads(d.maxN), integ_mloop_smem_bytes(d.maxN), s>>>(d, stage);
       break;
     case PZK_OBS: k_obs<<<d.n_oitems, 256, 0, s>>>(d, -1); break;
     case PZK_ASSEMBLE: k_assemble<<<d.n_mitems, mloop_threads(d.maxN), ms_smem_bytes(d.maxN), s>>>(d); break;
