@@ -203,6 +203,15 @@ int pz_set_step_state(pz_handle* h, int inst, double time, const double* dt, int
  * temperature's integral when composition is on (zero without it). */
 int pz_get_spectra(pz_handle* h, int inst, double* out);
 
+/* The (r, m) spectra of one instance's current state, computed on the
+ * device: the integrands us2R, up2R and enstR of calculate_spectra
+ * (src/spectra.f90:134-142), pi cc2real(f(m, r)) r height(r) for f = us, up,
+ * om, before the r-integration.  out receives 3 * n_r_max * n_m_max doubles:
+ * for each of the three fields an (n_m_max, n_r_max) array with m varying
+ * fastest, the layout of 2D_spec_avg.TAG (write_2D_spectra,
+ * spectra.f90:371-457), whose time averages the caller accumulates. */
+int pz_get_spectra_2d(pz_handle* h, int inst, double* out);
+
 /* l_AB1 of read_checkpoint (src/checkpoints.f90:398-425): when set, the
  * first step after pz_set_step_state(..., n_step = 0) takes first-order
  * explicit weights (src/step_time.f90:309-314).  pizza sets it when a run

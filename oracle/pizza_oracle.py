@@ -1921,6 +1921,17 @@ class Pizza:
                 out[i, 4] = out[i, 3]
         return out
 
+    def spectra_2d(self):
+        """The (r, m) spectra of calculate_spectra (spectra.f90:134-142):
+        pi cc2real(f) r height for f = us, up, om at every (r, m), before
+        the r-integration.  (3, N, M) array."""
+        out = np.zeros((3, self.N, self.M))
+        for k, f in enumerate((self.us, self.up, self.om)):
+            c2 = 2.0 * (f.real ** 2 + f.imag ** 2)
+            c2[0] = f[0].real ** 2
+            out[k] = (np.pi * c2 * self.r * self.height).T
+        return out
+
     def time_series(self):
         """Rows of e_kin, e_kin_3D and heat at the current state."""
         d, c = self.d, self.cheb

@@ -188,6 +188,7 @@ def load_library(path: str | None = None):
     lib.pz_set_step_state.argtypes = [vp, ctypes.c_int, ctypes.c_double, dp, ctypes.c_int]
     lib.pz_set_restart_ab1.argtypes = [vp, ctypes.c_int, ctypes.c_int]
     lib.pz_get_spectra.argtypes = [vp, ctypes.c_int, dp]
+    lib.pz_get_spectra_2d.argtypes = [vp, ctypes.c_int, dp]
     lib.pz_integ_operator.argtypes = [ctypes.c_int, ctypes.c_double, ctypes.c_int, dp, ctypes.POINTER(ctypes.c_int)]
     lib.pz_fast_path.argtypes = [ctypes.c_int]
     lib.pz_integ_banded.argtypes = [ctypes.c_int]
@@ -202,7 +203,7 @@ def load_library(path: str | None = None):
               "pz_get_series", "pz_get_dims", "pz_launches_per_step", "pz_latest_rows",
               "pz_step_profile", "pz_explicit_terms", "pz_explicit_terms_noalloc", "pz_adjoint_forward",
               "pz_adjoint_backward", "pz_adjoint_grid_snapshots", "pz_set_ra", "pz_get_history", "pz_set_history", "pz_get_step_state",
-              "pz_set_step_state", "pz_set_restart_ab1", "pz_get_spectra", "pz_integ_operator",
+              "pz_set_step_state", "pz_set_restart_ab1", "pz_get_spectra", "pz_get_spectra_2d", "pz_integ_operator",
               "pz_fast_path", "pz_integ_banded", "pz_fast_eigen", "pz_probe_peaks", "pz_tune_set", "pz_destroy"):
         getattr(lib, f).restype = ctypes.c_int
     _lib = lib
@@ -443,6 +444,15 @@ class Ensemble:
         out = np.zeros(5 * self.dims[i][1])
         self._check(self.lib.pz_get_spectra(self._h, i, _dptr(out)))
         return out.reshape(-1, 5)
+
+    def spectra_2d(self, i):
+        """(r, m) spectra of instance i on the device: (3, n_r_max, n_m_max)
+        array of pi cc2real(f) r height for f = us, up, om (the integrands of
+        spectra, before the r-integration)."""
+        N, M = self.dims[i][0], self.dims[i][1]
+        out = np.zeros(3 * N * M)
+        self._check(self.lib.pz_get_spectra_2d(self._h, i, _dptr(out)))
+        return out.reshape(3, N, M)
 
     def set_restart_ab1(self, i, on=True):
         """First step after a restart with first-order explicit weights (pizza's l_AB1)."""

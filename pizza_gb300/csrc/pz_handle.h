@@ -32,6 +32,7 @@ struct pz_handle {
   cudaGraphExec_t graph = nullptr;
   double* d_rows = nullptr;    // n_inst x PZ_SERIES_COLS gather buffer
   double* d_spec = nullptr;    // 5 x max n_m_max: spectra of one instance
+  double* d_spec2d = nullptr;  // 3 x max n_r_max x max n_m_max: (r, m) spectra of one instance
   PzItem* d_oitems = nullptr;  // k_obs blocks
   double* d_obs_part = nullptr;
   int* d_obs_cnt = nullptr;

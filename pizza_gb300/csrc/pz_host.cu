@@ -1099,6 +1099,7 @@ extern "C" int pz_create(const pz_config* cfgs, int n, pz_handle** out) {
       (e = cudaMalloc(&h->d_iorder, n * sizeof(int))) ||
       (e = cudaMalloc(&h->d_rows, (size_t)n * PZ_SERIES_COLS * sizeof(double))) ||
       (e = cudaMalloc(&h->d_spec, (size_t)5 * maxM * sizeof(double))) ||
+      (e = cudaMalloc(&h->d_spec2d, (size_t)3 * maxN * maxM * sizeof(double))) ||
       (e = cudaMalloc(&h->d_oitems, oitems.size() * sizeof(PzItem))) ||
       (e = cudaMalloc(&h->d_obs_part, oitems.size() * PZ_OBS_NP * sizeof(double))) ||
       (e = cudaMalloc(&h->d_obs_cnt, n * sizeof(int)))) {
@@ -1515,10 +1516,22 @@ extern "C" int pz_get_spectra(pz_handle* h, int inst, double* out) {
   if (!h) return fail(nullptr, PZ_E_ARG, "pz_get_spectra: null handle");
   if (inst < 0 || inst >= h->n_inst || !out) return fail(h, PZ_E_ARG, "pz_get_spectra: bad arguments");
   const int M = h->inst[inst].M;
-  cudaError_t e = pz_launch_spectra(h->dev, inst, M, h->d_spec, h->stream);
+  cudaError_t e = pz_launch_spectra(h->dev, inst, M, h->d_spec, nullptr, h->stream);
   if (!e) e = cudaMemcpyAsync(out, h->d_spec, (size_t)5 * M * sizeof(double), cudaMemcpyDeviceToHost, h->stream);
   if (!e) e = cudaStreamSynchronize(h->stream);
   if (e) return cuda_fail(h, e, "pz_get_spectra");
+  return PZ_OK;
+}
+
+extern "C" int pz_get_spectra_2d(pz_handle* h, int inst, double* out) {
+  if (!h) return fail(nullptr, PZ_E_ARG, "pz_get_spectra_2d: null handle");
+  if (inst < 0 || inst >= h->n_inst || !out) return fail(h, PZ_E_ARG, "pz_get_spectra_2d: bad arguments");
+  const PzInst& I = h->inst[inst];
+  cudaError_t e = pz_launch_spectra(h->dev, inst, I.M, h->d_spec, h->d_spec2d, h->stream);
+  if (!e)
+    e = cudaMemcpyAsync(out, h->d_spec2d, (size_t)3 * I.N * I.M * sizeof(double), cudaMemcpyDeviceToHost, h->stream);
+  if (!e) e = cudaStreamSynchronize(h->stream);
+  if (e) return cuda_fail(h, e, "pz_get_spectra_2d");
   return PZ_OK;
 }
 
@@ -1702,6 +1715,7 @@ extern "C" int pz_destroy(pz_handle* h) {
   cudaFree(h->d_iorder);
   cudaFree(h->d_rows);
   cudaFree(h->d_spec);
+  cudaFree(h->d_spec2d);
   cudaFree(h->d_oitems);
   cudaFree(h->d_obs_part);
   cudaFree(h->d_obs_cnt);

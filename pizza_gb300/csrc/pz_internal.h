@@ -278,7 +278,7 @@ struct PzLaunch { int kind, stage; };
 cudaError_t pz_launch_step_kernel(const PzDev& d, int kind, int stage, cudaStream_t s);
 const char* pz_step_kernel_name(int kind);
 cudaError_t pz_launch_obs(const PzDev& d, int only, cudaStream_t s);
-cudaError_t pz_launch_spectra(const PzDev& d, int inst, int n_m_max, double* out, cudaStream_t s);
+cudaError_t pz_launch_spectra(const PzDev& d, int inst, int n_m_max, double* out, double* out2d, cudaStream_t s);
 cudaError_t pz_launch_gather_rows(const PzDev& d, double* out, cudaStream_t s);
 cudaError_t pz_setup_kernels();
 // k_fast (pz_fast.cu): the tensor-core stage of the fast instances, and its

@@ -1597,9 +1597,12 @@ __device__ __forceinline__ double round_off(double x) { return fabs(x) < 10.0 * 
 // f = us, up, om, T, and the composition column, one block per m.  The
 // reference fills that column with the temperature's integral (xi2_m =
 // rInt_R(temp2R), spectra.f90:183) when composition is on, and leaves it zero
-// otherwise; the column here is the same, so spec files match.
+// otherwise; the column here is the same, so spec files match.  With out2d,
+// the integrands of us2, up2 and the enstrophy at every (r, m) as well (the
+// 2-D spectra us2R, up2R, enstR of calculate_spectra), at
+// out2d[(k N + r) M + m], k = 0, 1, 2.
 // ---------------------------------------------------------------------------
-__global__ void k_spectra(PzDev d, int inst, double* out) {
+__global__ void k_spectra(PzDev d, int inst, double* out, double* out2d) {
   const PzInst& I = d.inst[inst];
   const View V{&I, d.pool};
   __shared__ double red[32];
@@ -1615,7 +1618,9 @@ __global__ void k_spectra(PzDev d, int inst, double* out) {
     for (int r = threadIdx.x; r < n; r += blockDim.x) {
       const double2 z = f[r];
       const double c2 = (mi == 0) ? z.x * z.x : 2.0 * (z.x * z.x + z.y * z.y);   // cc2real
-      acc += wint[r] * (pi * c2 * rr[r] * h[r]);
+      const double v = pi * c2 * rr[r] * h[r];
+      acc += wint[r] * v;
+      if (out2d && k < 3) out2d[((long long)k * n + r) * I.M + mi] = v;
     }
     acc = block_sum(acc, red);
     if (threadIdx.x == 0) {
@@ -1874,8 +1879,8 @@ cudaError_t pz_launch_start(const PzDev& d, int only, cudaStream_t s) {
   return cudaGetLastError();
 }
 
-cudaError_t pz_launch_spectra(const PzDev& d, int inst, int n_m_max, double* out, cudaStream_t s) {
-  k_spectra<<<n_m_max, 64, 0, s>>>(d, inst, out);
+cudaError_t pz_launch_spectra(const PzDev& d, int inst, int n_m_max, double* out, double* out2d, cudaStream_t s) {
+  k_spectra<<<n_m_max, 64, 0, s>>>(d, inst, out, out2d);
   return cudaGetLastError();
 }
 

@@ -124,6 +124,75 @@ class SpectraAverage:
         return p
 
 
+class Spectra2DAverage:
+    """Time-averaged (r, m) spectra (the l_2D_spectra part of
+    calculate_spectra, src/spectra.f90:134-164, and write_2D_spectra,
+    :371-457): running means (and with l_2D_SD standard deviations, getMSD2
+    of src/useful.f90:263-293 per point) of us2R, up2R and enstR, the device
+    snapshots of Ensemble.spectra_2d."""
+
+    def __init__(self, n_r_max: int, n_m_max: int, l_sd: bool = False):
+        self.mean = np.zeros((3, n_r_max, n_m_max))
+        self.sd = np.zeros((3, n_r_max, n_m_max))
+        self.l_sd = l_sd
+        self.n_calls = 0
+        self.time_last = 0.0
+
+    def update(self, spec2d, time_avg: float):
+        """spec2d: (3, n_r_max, n_m_max) snapshot (Ensemble.spectra_2d);
+        time_avg: the caller's running sum of dt over its output calls."""
+        x = np.asarray(spec2d, float)
+        self.n_calls += 1
+        dt = time_avg - self.time_last
+        if self.n_calls == 1:
+            self.mean = x.copy()
+            self.sd = np.zeros_like(x)
+        else:
+            delta = x - self.mean
+            self.mean = self.mean + delta * dt / time_avg
+            self.sd = self.sd + dt * delta * (x - self.mean)
+        self.time_last = time_avg
+
+    def result(self):
+        """(mean, SD): SD normalised as write_spectra_avg does (spectra.f90:290-299)."""
+        return self.mean.copy(), np.sqrt(self.sd / self.time_last)
+
+    def write(self, path: str, cfg, r):
+        """2D_spec_avg.TAG: version (1, or 2 with SD), ra, pr, raxi, sc, ek,
+        radratio, n_r_max, n_m_max, m_max, minc, r, then per field its mean
+        (and SD) as (n_m_max, n_r_max) with m varying fastest, stream
+        unformatted."""
+        mean, sd = self.result()
+        _, n_r, n_m = mean.shape
+        with open(path, "wb") as f:
+            np.array([2 if self.l_sd else 1], _I4).tofile(f)
+            np.array([cfg.ra, cfg.pr, cfg.raxi, cfg.sc, cfg.ek, cfg.radratio], _F8).tofile(f)
+            np.array([n_r, n_m, cfg.m_max, cfg.minc], _I4).tofile(f)
+            np.asarray(r, _F8).tofile(f)
+            for k in range(3):
+                np.ascontiguousarray(mean[k], _F8).tofile(f)
+                if self.l_sd:
+                    np.ascontiguousarray(sd[k], _F8).tofile(f)
+        return path
+
+
+def read_2d_spectra(path: str):
+    """Read a 2D_spec_avg.TAG file: header fields, r and the (mean, SD)
+    arrays of us2, up2, enst as (n_m_max, n_r_max) arrays (SD None for
+    version 1)."""
+    with open(path, "rb") as f:
+        version = int(np.fromfile(f, _I4, 1)[0])
+        ra, pr, raxi, sc, ek, radratio = (float(v) for v in np.fromfile(f, _F8, 6))
+        n_r, n_m, m_max, minc = (int(v) for v in np.fromfile(f, _I4, 4))
+        r = np.fromfile(f, _F8, n_r)
+        out = dict(version=version, ra=ra, pr=pr, raxi=raxi, sc=sc, ek=ek, radratio=radratio, n_r_max=n_r,
+                   n_m_max=n_m, m_max=m_max, minc=minc, r=r)
+        for name in ("us2", "up2", "enst"):
+            out[name] = np.fromfile(f, _F8, n_r * n_m).reshape(n_r, n_m).T
+            out[name + "_SD"] = np.fromfile(f, _F8, n_r * n_m).reshape(n_r, n_m).T if version == 2 else None
+    return out
+
+
 def write_series(ens, i: int, tag: str, directory: str = ".", rows=None):
     """Write e_kin.TAG, heat.TAG, (rotating runs) e_kin_3D.TAG and (with
     composition) composition.TAG of instance i from its time-series rows

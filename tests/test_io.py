@@ -134,3 +134,33 @@ def test_spectra_average_of_oracle_run():
     ref = np.tensordot(w, np.array(snaps), axes=1) / t_avg
     assert np.max(np.abs(mean - ref)) <= 1e-13 * np.max(np.abs(ref))
     assert np.all(sd >= 0.0) and np.all(np.isfinite(sd))
+
+
+def test_2d_spectra_match_reference_reader_fixture(tmp_path):
+    """The 2D_spec_avg writer against the golden file that the reference's
+    own reader parsed (tests/golden/make_2d_spectra_golden.py): the same
+    bytes, the same parsed values; and the averages against their closed
+    form (getMSD2's recursion)."""
+    import json
+    import sys
+    sys.path.insert(0, os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden"))
+    from make_2d_spectra_golden import sample, write_sample
+    here = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+    p = write_sample(str(tmp_path / "spec2d.bin"))
+    with open(p, "rb") as a, open(os.path.join(here, "spec2d_sample.bin"), "rb") as b:
+        assert a.read() == b.read()
+    with open(os.path.join(here, "spec2d_sample.json")) as f:
+        ref = json.load(f)
+    got = pizza_io.read_2d_spectra(p)
+    for k in ("version", "n_r_max", "n_m_max", "m_max", "minc"):
+        assert got[k] == ref[k]
+    assert np.array_equal(got["r"], np.array(ref["radius"]))
+    for name, key in (("us2", "us2_m"), ("us2_SD", "us2_m_SD"), ("up2", "up2_m"), ("up2_SD", "up2_m_SD"),
+                      ("enst", "enst_m")):
+        assert np.array_equal(got[name], np.array(ref[key])), name
+    cfg, r, snaps, times = sample()
+    dts = np.diff((0.0,) + tuple(times))
+    mean = sum(d * x for d, x in zip(dts, snaps)) / times[-1]
+    var = sum(d * (x - mean) ** 2 for d, x in zip(dts, snaps)) / times[-1]
+    np.testing.assert_allclose(got["us2"], mean[0].T, rtol=1e-13)
+    np.testing.assert_allclose(got["up2_SD"], np.sqrt(var[1]).T, rtol=1e-10)
