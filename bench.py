@@ -509,6 +509,11 @@ def main():
     ap.add_argument("--badj-ck", type=int, default=BADJ_CK)
     ap.add_argument("--badj-reps", type=int, default=2)
     ap.add_argument("--badj-fd", type=int, default=4)
+    ap.add_argument("--tune", default="auto", choices=["auto", "run", "off"],
+                    help="launch shapes: auto = the committed table if present, else tune now; run = tune now; "
+                         "off = built-in defaults")
+    ap.add_argument("--tune-table", default=os.path.join(os.path.dirname(os.path.abspath(__file__)), "pizza_gb300",
+                                                          "tuning_gb300.json"))
     args = ap.parse_args()
     args.warmup = max(3, args.warmup)
 
@@ -553,8 +558,25 @@ def main():
                               "adjoint_no_recompute": adjoint_ratio(torch, args.adj_reps, 0, n, w)}))
         return
 
-    ens = pz.Ensemble([gpu_cfg(s) for s in specs])
     temps = [seeded_temp(s) for s in specs]
+    tuning = None
+    if args.tune != "off":
+        from pizza_gb300 import autotune
+        t0 = time.perf_counter()
+        if args.tune == "auto" and os.path.exists(args.tune_table):
+            table = autotune.load(args.tune_table)
+            source = "table " + os.path.relpath(args.tune_table, os.path.dirname(os.path.abspath(__file__)))
+        else:
+            table = autotune.tune([gpu_cfg(s) for s in specs], temps)
+            source = "tuned in this run on this workload"
+            out_dir = os.path.join(os.path.dirname(os.path.abspath(__file__)), "gpurun_out")
+            if os.path.isdir(out_dir):
+                autotune.save(table, os.path.join(out_dir, "tuning_gb300.json"))
+        autotune.apply(table)
+        tuning = {"source": source, "k_fast_G": table.get("k_fast_G"), "k_rloop_rg": table.get("k_rloop_rg"),
+                  "gain_over_defaults": autotune.gain(table), "candidates_ms_per_step": table.get("ms"),
+                  "seconds": time.perf_counter() - t0}
+    ens = pz.Ensemble([gpu_cfg(s) for s in specs])
     ens.set_state_all(temps)
     ens.step(args.warmup)
 
@@ -680,6 +702,7 @@ def main():
         "kernel_rooflines": kernels,
         "dominant_kernel": dom,
         "operator_rebuilds_per_step": n_dt_changes / max(1, args.steps - 1),
+        "tuning": tuning,
         "adjoint": adj,
         "integ": integ,
         "cpu_baseline": cpu,

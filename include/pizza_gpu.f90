@@ -180,6 +180,13 @@ module pizza_gpu
          real(c_double), intent(out) :: out(*)
       end function pz_get_spectra_2d
 
+      integer(c_int) function pz_balance_step(h, inst, vort, vp) bind(c, name='pz_balance_step')
+         import :: c_ptr, c_int, c_double
+         type(c_ptr), value :: h
+         integer(c_int), value :: inst
+         real(c_double), intent(out) :: vort(*), vp(*)
+      end function pz_balance_step
+
       integer(c_int) function pz_set_restart_ab1(h, inst, l_ab1) bind(c, name='pz_set_restart_ab1')
          import :: c_ptr, c_int
          type(c_ptr), value :: h

@@ -212,6 +212,24 @@ int pz_get_spectra(pz_handle* h, int inst, double* out);
  * spectra.f90:371-457), whose time averages the caller accumulates. */
 int pz_get_spectra_2d(pz_handle* h, int inst, double* out);
 
+/* One step of every instance of the handle, as pz_step(h, 1) followed by
+ * pz_sync, that also returns the force balances of instance inst over that
+ * step: the terms vort_balance.f90 and vp_balance.f90 collect when
+ * l_vort_balance / l_vphi_balance are set and the next step is a log step
+ * (src/step_time.f90:156-157), with the hooks of update_om_coll_dmat
+ * (src/update_psi_coll_dmat.f90:154-230, :444-556, :590-682).
+ * vort: 6 * n_r_max * n_m_max complex (interleaved doubles), the terms buo,
+ *   cor, adv, dwdt, visc, pump, each (n_m_max, n_r_max) with m varying fastest;
+ *   as in the reference, dwdt of m /= 0 is the new vorticity in Chebyshev
+ *   space minus the old one in physical space, over dt, and visc carries no
+ *   ViscFac factor.
+ * vp: 4 * n_r_max doubles: rey_stress, dvpdt, visc, pump of u_phi(m = 0).
+ * The host accumulates them (vort_balance's calc_avg, vp_balance's
+ * write_outputs).  Collocation instances with the influence-matrix solve and
+ * a multistep scheme (PZ_E_UNSUPPORTED otherwise).  The first call allocates
+ * the handle's balance buffers. */
+int pz_balance_step(pz_handle* h, int inst, double* vort, double* vp);
+
 /* l_AB1 of read_checkpoint (src/checkpoints.f90:398-425): when set, the
  * first step after pz_set_step_state(..., n_step = 0) takes first-order
  * explicit weights (src/step_time.f90:309-314).  pizza sets it when a run

@@ -1291,6 +1291,20 @@ class Pizza:
         e = self.dpsidt.expl[ist].copy()
         nz = slice(1, None)
         e[nz] = e[nz] - self.or1 * work[nz]
+        bal = getattr(self, "_bal", None)
+        if bal is not None:
+            # vort_balance's adv and cor (update_psi_coll_dmat.f90:500-505) and
+            # pump (:540-546); zero where the reference leaves them unset
+            bal["adv"] = np.zeros_like(e)
+            bal["adv"][nz] = e[nz]
+            bal["cor"] = np.zeros_like(e)
+            if not d["l_non_rot"]:
+                bal["cor"][nz] = d["CorFac"] * self.beta * self.us[nz]
+            bal["pump"] = np.zeros_like(e)
+            if self.p.l_ek_pump:
+                bal["pump"][nz] = -d["CorFac"] * self.ekpump * (
+                    self.om[nz] + self.ekp_up * self.up[nz]
+                    + (self.ekp_dusdp * 1j * m[nz] + self.ekp_us) * self.us[nz])
         if self.l_direct:
             # update_psi_coll_smat.f90:323-378
             if not d["l_coriolis_imp"]:
@@ -1611,6 +1625,19 @@ class Pizza:
             imp[0] = (d["ViscFac"] * self.hdif[0] * (d2uphi0 + self.or1 * duphi0 - self.or2 * uphi0)
                       - d["CorFac"] * self.ekpump * uphi0)
             self.dpsidt.impl[istage - 1] = imp
+        bal = getattr(self, "_bal", None)
+        if bal is not None and not self.l_direct:
+            # update_psi_coll_dmat.f90:642-676 (computed whatever l_calc_lin)
+            if not l_calc_lin:
+                self.dom, work = c.get_ddr(self.om, l_dct=True)
+            dm2 = (self.mvec.astype(float) ** 2)[:, None]
+            visc = work + self.or1 * self.dom - dm2 * self.or2 * self.om
+            visc[0] = 0.0
+            bal["visc"] = visc
+            uphi0 = self.up[0].real.copy()
+            duphi0, d2uphi0 = c.get_ddr_real(uphi0)
+            bal["vp_visc"] = d["ViscFac"] * self.hdif[0] * (d2uphi0 + self.or1 * duphi0 - self.or2 * uphi0)
+            bal["vp_pump"] = -d["CorFac"] * self.ekpump * uphi0 if self.p.l_ek_pump else np.zeros(self.N)
 
     # -- solves (mloop) ------------------------------------------------------
     def update_temp(self, lMat, l_log_next, kind="temp"):
@@ -1653,6 +1680,18 @@ class Pizza:
         c, d = self.cheb, self.d
         N, M, n_max = self.N, self.M, self.n_max
         ts = self.ts
+        bal = getattr(self, "_bal", None)
+        if bal is not None:
+            # initialize_domdt / initialize_dvpdt (vort_balance.f90, vp_balance.f90)
+            bal["dwdt"] = self.om / ts.dt[0]
+            bal["dvpdt"] = self.up[0].real / ts.dt[0]
+            bal["rey_stress"] = self.dpsidt.expl[ts.istage - 1][0].real.copy()
+            m_ = self.mvec[:, None]
+            buo = np.zeros((M, N), complex)
+            buo[1:] = -d["BuoFac"] * self.rgrav * self.or1 * 1j * m_[1:] * self.temp[1:]
+            if self.l_chem:
+                buo[1:] = buo[1:] - d["ChemFac"] * self.rgrav * self.or1 * 1j * m_[1:] * self.xi[1:]
+            bal["buo"] = buo
         work = ts.set_imex_rhs(self.dpsidt)
         m = self.mvec
         # m = 0: uphi solve
@@ -1717,6 +1756,11 @@ class Pizza:
         om[0] = om0 + self.or1 * uphi0
         self.psi, self.us, self.up, self.om = psi, us, up, om
         ts.rotate_imex(self.dpsidt)
+        if bal is not None:
+            # finalize_domdt before get_psi_rhs_imp: om of m /= 0 is still in
+            # Chebyshev space there (update_psi_coll_dmat.f90:444-451)
+            bal["dwdt"] = om / ts.dt[0] - bal["dwdt"]
+            bal["dvpdt"] = up[0].real / ts.dt[0] - bal["dvpdt"]
         if ts.istage == ts.nstages:
             self._psi_rhs_imp(1, self._calc_rhs(1), l_in_cheb=True)
         else:
@@ -1902,6 +1946,22 @@ class Pizza:
         self.update_om()
         ts.istage += 1
         return lMat
+
+    def balance_step(self):
+        """One step that also records the vorticity and u_phi force balances
+        (vort_balance.f90, vp_balance.f90 with l_calc set: the hooks of
+        update_psi_coll_dmat.f90).  Returns {"vort": {buo, cor, adv, dwdt,
+        visc, pump: (M, N) complex}, "vp": {rey_stress, dvpdt, visc, pump:
+        (N,) real}}.  Collocation, influence matrix, multistep schemes."""
+        self._bal = {}
+        try:
+            self.advance()
+            b = self._bal
+        finally:
+            self._bal = None
+        vort = {k: b[k] for k in ("buo", "cor", "adv", "dwdt", "visc", "pump")}
+        vp = {"rey_stress": b["rey_stress"], "dvpdt": b["dvpdt"], "visc": b["vp_visc"], "pump": b["vp_pump"]}
+        return {"vort": vort, "vp": vp}
 
     # -- time series (src/outputs.f90:418-830) -------------------------------
     def spectra(self):

@@ -189,6 +189,7 @@ def load_library(path: str | None = None):
     lib.pz_set_restart_ab1.argtypes = [vp, ctypes.c_int, ctypes.c_int]
     lib.pz_get_spectra.argtypes = [vp, ctypes.c_int, dp]
     lib.pz_get_spectra_2d.argtypes = [vp, ctypes.c_int, dp]
+    lib.pz_balance_step.argtypes = [vp, ctypes.c_int, dp, dp]
     lib.pz_integ_operator.argtypes = [ctypes.c_int, ctypes.c_double, ctypes.c_int, dp, ctypes.POINTER(ctypes.c_int)]
     lib.pz_fast_path.argtypes = [ctypes.c_int]
     lib.pz_integ_banded.argtypes = [ctypes.c_int]
@@ -203,7 +204,7 @@ def load_library(path: str | None = None):
               "pz_get_series", "pz_get_dims", "pz_launches_per_step", "pz_latest_rows",
               "pz_step_profile", "pz_explicit_terms", "pz_explicit_terms_noalloc", "pz_adjoint_forward",
               "pz_adjoint_backward", "pz_adjoint_grid_snapshots", "pz_set_ra", "pz_get_history", "pz_set_history", "pz_get_step_state",
-              "pz_set_step_state", "pz_set_restart_ab1", "pz_get_spectra", "pz_get_spectra_2d", "pz_integ_operator",
+              "pz_set_step_state", "pz_set_restart_ab1", "pz_get_spectra", "pz_get_spectra_2d", "pz_balance_step", "pz_integ_operator",
               "pz_fast_path", "pz_integ_banded", "pz_fast_eigen", "pz_probe_peaks", "pz_tune_set", "pz_destroy"):
         getattr(lib, f).restype = ctypes.c_int
     _lib = lib
@@ -453,6 +454,21 @@ class Ensemble:
         out = np.zeros(3 * N * M)
         self._check(self.lib.pz_get_spectra_2d(self._h, i, _dptr(out)))
         return out.reshape(3, N, M)
+
+    BALANCE_TERMS = ("buo", "cor", "adv", "dwdt", "visc", "pump")
+    VP_TERMS = ("rey_stress", "dvpdt", "visc", "pump")
+
+    def balance_step(self, i):
+        """One step of the handle (every instance) that also returns the force
+        balances of instance i over it (pz_balance_step): {"vort": {term:
+        (n_m_max, n_r_max) complex}, "vp": {term: (n_r_max,) real}}."""
+        N, M = self.dims[i][0], self.dims[i][1]
+        vort = np.zeros(12 * N * M)
+        vpo = np.zeros(4 * N)
+        self._check(self.lib.pz_balance_step(self._h, i, _dptr(vort), _dptr(vpo)))
+        z = vort.view(np.complex128).reshape(6, N, M)
+        return {"vort": {t: z[k].T.copy() for k, t in enumerate(self.BALANCE_TERMS)},
+                "vp": {t: vpo[k * N:(k + 1) * N].copy() for k, t in enumerate(self.VP_TERMS)}}
 
     def set_restart_ab1(self, i, on=True):
         """First step after a restart with first-order explicit weights (pizza's l_AB1)."""

@@ -24,7 +24,7 @@ import numpy as np
 
 from . import Ensemble, TUNE_FAST_G, TUNE_RLOOP_RG, tune_set
 
-FAST_G = (2, 4, 8, 12, 16)
+FAST_G = (4, 8, 12, 16)
 RLOOP_RG = (1, 2, 3, 4, 6, 8)
 
 
@@ -122,3 +122,4 @@ def gain(table):
     if tot_t > 0:
         out["k_rloop"] = tot_d / tot_t
     return {k: float(np.round(v, 4)) for k, v in out.items()}
+

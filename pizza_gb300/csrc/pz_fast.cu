@@ -182,12 +182,10 @@ __device__ void oz_mma_t(const PzFastDev& F, const PzOzOp& op, const BOp& B, int
       }
   }
 }
-// two column tiles per task when there are enough tasks for every warp
+// one 8-column tile per task: the register budget of three blocks per SM
 __device__ __forceinline__ void oz_mma(const PzFastDev& F, const PzOzOp& op, const BOp& B, int C, double* Y,
                                        int ldy) {
-  const int nw = blockDim.x >> 5;
-  if (op.RT * ((C + 15) >> 4) >= 2 * nw) oz_mma_t<2>(F, op, B, C, Y, ldy);
-  else oz_mma_t<1>(F, op, B, C, Y, ldy);
+  oz_mma_t<1>(F, op, B, C, Y, ldy);
 }
 
 __device__ __forceinline__ double2 imex_rhs_f(const View& V, const PzInst& I, const PzState& S, int f, int mi,
@@ -224,7 +222,7 @@ struct FastSmem {
 __host__ __device__ inline size_t fast_smem_layout(int G, int N, size_t* oR, size_t* oRT, size_t* oRW, size_t* osc,
                                                    size_t* ost, size_t* oce, int* C, int* sw) {
   const int n = N - 2;
-  *C = ((4 * G + 15) / 16) * 16;
+  *C = ((2 * G + 15) / 16) * 16;
   *sw = ((N + 15) / 16) * 8 + 4;
   size_t o = (size_t)PZ_OZ_S * (*C) * (*sw) * 4;
   o = (o + 15) & ~(size_t)15;
@@ -235,12 +233,12 @@ __host__ __device__ inline size_t fast_smem_layout(int G, int N, size_t* oR, siz
   o += (size_t)2 * G * rmax * 8;
   *oRT = o; o += (size_t)2 * G * n * 8;
   *oRW = o; o += (size_t)2 * G * n * 8;
-  *osc = o; o += (size_t)G * 4 * 8;
+  *osc = o; o += (size_t)G * 8 * 8;
   *ost = o; o += (size_t)G * 2 * 4;
   return (o + 15) & ~(size_t)15;
 }
 
-__global__ void __launch_bounds__(256, 2) k_fast(PzDev d) {
+__global__ void __launch_bounds__(256, 3) k_fast(PzDev d) {
   extern __shared__ __align__(16) unsigned char fsm[];
   const PzFastDev& F = d.fast;
   const PzFastItem it = F.items[blockIdx.x];
@@ -267,23 +265,34 @@ __global__ void __launch_bounds__(256, 2) k_fast(PzDev d) {
   for (int g = threadIdx.x; g < G; g += blockDim.x) {
     s.st[2 * g] = (g < ni && d.state[fi[g]].status == 0) ? 1 : 0;
     s.st[2 * g + 1] = 0;
+    if (g < ni) {
+      // per instance: w = wimp_lin(1), 1/w, w TdiffFac, w ViscFac
+      const double w = d.state[fi[g]].wimp_lin[0];
+      s.sc[8 * g + 4] = w;
+      s.sc[8 * g + 5] = 1.0 / w;
+      s.sc[8 * g + 6] = w * d.inst[fi[g]].TdiffFac;
+      s.sc[8 * g + 7] = w * d.inst[fi[g]].ViscFac;
+    }
   }
   __syncthreads();
 
-  // ---- explicit terms: D1p of dVsT and dVsOm (4 columns per instance)
-  zero_cols(s.B, 0);
-  __syncthreads();
-  for (int j = warp; j < 4 * ni; j += nw) {
-    const int g = j >> 2, f = (j >> 1) & 1, part = j & 1;
-    if (!s.st[2 * g]) continue;
-    const PzInst& I = d.inst[fi[g]];
-    const View V{&I, d.pool};
-    const double* x = reinterpret_cast<const double*>(V.fld(f ? F_DVSOM : F_DVST, mi)) + part;
-    split_col(s.B, j, x, 2, N);
+  // ---- explicit terms: D1p of dVsT, then of dVsOm (2 columns per instance
+  // each), into s.R and s.R + 2 G N
+  for (int f = 0; f < 2; ++f) {
+    zero_cols(s.B, 0);
+    __syncthreads();
+    for (int j = warp; j < 2 * ni; j += nw) {
+      const int g = j >> 1, part = j & 1;
+      if (!s.st[2 * g]) continue;
+      const PzInst& I = d.inst[fi[g]];
+      const View V{&I, d.pool};
+      const double* x = reinterpret_cast<const double*>(V.fld(f ? F_DVSOM : F_DVST, mi)) + part;
+      split_col(s.B, j, x, 2, N);
+    }
+    __syncthreads();
+    oz_mma(F, cls.d1p, s.B, 2 * ni, s.R + (long long)f * 2 * G * N, N);
+    __syncthreads();
   }
-  __syncthreads();
-  oz_mma(F, cls.d1p, s.B, 4 * ni, s.R, N);
-  __syncthreads();
 
   // ---- finish the explicit terms; IMEX right-hand sides (interior rows)
   const double dm = (double)(mi * d.inst[fi[0]].minc), dm2 = dm * dm;
@@ -297,8 +306,8 @@ __global__ void __launch_bounds__(256, 2) k_fast(PzDev d) {
     const double* or1 = V.rad(RV_OR1);
     const double* beta = V.rad(RV_BETA);
     const double2 u = V.fld(F_US, mi)[i];
-    const double2 dT = make_double2(s.R[(4 * g + 0) * N + i], s.R[(4 * g + 1) * N + i]);
-    const double2 dO = make_double2(s.R[(4 * g + 2) * N + i], s.R[(4 * g + 3) * N + i]);
+    const double2 dT = make_double2(s.R[(2 * g + 0) * N + i], s.R[(2 * g + 1) * N + i]);
+    const double2 dO = make_double2(s.R[(long long)(2 * G + 2 * g) * N + i], s.R[(long long)(2 * G + 2 * g + 1) * N + i]);
     double2* eT = V.hist(0, 2, S.r_expl, mi);
     double2 e = eT[i];
     const double c = V.rad(RV_DTCOND)[i] - I.tadvz * beta[i] * V.rad(RV_TCOND)[i];
@@ -354,8 +363,7 @@ __global__ void __launch_bounds__(256, 2) k_fast(PzDev d) {
     for (int t = threadIdx.x; t < ni * n; t += blockDim.x) {
       const int g = t / n, k = t - g * n;
       const int inst = fi[g];
-      const double w = d.state[inst].wimp_lin[0] * d.inst[inst].TdiffFac;
-      const double D = 1.0 / (1.0 - w * lam[k]);
+      const double D = 1.0 / (1.0 - s.sc[8 * g + 6] * lam[k]);
       s.R[(long long)(2 * g) * n + k] *= D;
       s.R[(long long)(2 * g + 1) * n + k] *= D;
     }
@@ -389,7 +397,7 @@ __global__ void __launch_bounds__(256, 2) k_fast(PzDev d) {
     if (S.l_calc_lin) {
       double2 it = make_double2(0.0, 0.0);
       if (!edge) {
-        const double iw = 1.0 / w;
+        const double iw = s.sc[8 * g + 5];
         it = make_double2(iw * (T.x - s.RT[(2 * g) * n + i - 1]), iw * (T.y - s.RT[(2 * g + 1) * n + i - 1]));
       }
       V.hist(0, 1, S.b_impl, mi)[i] = it;
@@ -419,8 +427,7 @@ __global__ void __launch_bounds__(256, 2) k_fast(PzDev d) {
     const double* lam = F.vec + F.us[it.ucls].vec;
     for (int t = threadIdx.x; t < ni * n; t += blockDim.x) {
       const int g = t / n, k = t - g * n;
-      const double w = d.state[fi[g]].wimp_lin[0];
-      const double D = 1.0 / (1.0 - w * lam[k]);
+      const double D = 1.0 / (1.0 - s.sc[8 * g + 4] * lam[k]);
       s.R[(long long)(2 * g) * n + k] *= D;
       s.R[(long long)(2 * g + 1) * n + k] *= D;
     }
@@ -437,7 +444,7 @@ __global__ void __launch_bounds__(256, 2) k_fast(PzDev d) {
     for (int g = warp; g < ni; g += nw) {
       if (!s.st[2 * g]) continue;
       const int inst = fi[g];
-      const double wn = d.state[inst].wimp_lin[0] * d.inst[inst].ViscFac;
+      const double wn = s.sc[8 * g + 7];
       double* zr = s.R + (long long)(2 * g) * n;
       double* zi = zr + n;
       double t1r = 0.0, t1i = 0.0, b1r = 0.0, b1i = 0.0, t2 = 0.0, b2 = 0.0, t3 = 0.0, b3 = 0.0;
@@ -470,7 +477,7 @@ __global__ void __launch_bounds__(256, 2) k_fast(PzDev d) {
         zi[k] += c1i * h2 + c2i * h3;
       }
       if (lane == 0) {
-        s.sc[4 * g + 0] = c1r; s.sc[4 * g + 1] = c1i; s.sc[4 * g + 2] = c2r; s.sc[4 * g + 3] = c2i;
+        s.sc[8 * g + 0] = c1r; s.sc[8 * g + 1] = c1i; s.sc[8 * g + 2] = c2r; s.sc[8 * g + 3] = c2i;
       }
     }
   }
@@ -495,7 +502,7 @@ __global__ void __launch_bounds__(256, 2) k_fast(PzDev d) {
     const View V{&I, d.pool};
     const double* or1 = V.rad(RV_OR1);
     const bool edge = (i == 0 || i == N - 1);
-    const double w = S.wimp_lin[0], iw = 1.0 / w;
+    const double iw = s.sc[8 * g + 5];
     const double* Rr = s.R + (long long)(2 * g) * ld3;
     const double* Ri = s.R + (long long)(2 * g + 1) * ld3;
     bool bad;
@@ -512,8 +519,8 @@ __global__ void __launch_bounds__(256, 2) k_fast(PzDev d) {
       bad = !isfinite(u);
     } else {
       double2 om, ps;
-      if (i == 0) om = make_double2(s.sc[4 * g + 2], s.sc[4 * g + 3]);
-      else if (i == N - 1) om = make_double2(s.sc[4 * g + 0], s.sc[4 * g + 1]);
+      if (i == 0) om = make_double2(s.sc[8 * g + 2], s.sc[8 * g + 3]);
+      else if (i == N - 1) om = make_double2(s.sc[8 * g + 0], s.sc[8 * g + 1]);
       else om = make_double2(Rr[i - 1], Ri[i - 1]);
       ps = edge ? make_double2(0.0, 0.0) : make_double2(Rr[n + i - 1], Ri[n + i - 1]);
       const double2 dp = make_double2(Rr[2 * n + i], Ri[2 * n + i]);

@@ -33,6 +33,8 @@ struct pz_handle {
   double* d_rows = nullptr;    // n_inst x PZ_SERIES_COLS gather buffer
   double* d_spec = nullptr;    // 5 x max n_m_max: spectra of one instance
   double* d_spec2d = nullptr;  // 3 x max n_r_max x max n_m_max: (r, m) spectra of one instance
+  double* d_bal = nullptr;     // force balances (pz_balance_step, allocated at its first call): the
+                               // field block of one instance, 6 complex and 4 real (r, m) planes
   PzItem* d_oitems = nullptr;  // k_obs blocks
   double* d_obs_part = nullptr;
   int* d_obs_cnt = nullptr;

@@ -1523,6 +1523,38 @@ extern "C" int pz_get_spectra(pz_handle* h, int inst, double* out) {
   return PZ_OK;
 }
 
+extern "C" int pz_balance_step(pz_handle* h, int inst, double* vort, double* vp) {
+  if (!h) return fail(nullptr, PZ_E_ARG, "pz_balance_step: null handle");
+  if (inst < 0 || inst >= h->n_inst || !vort || !vp) return fail(h, PZ_E_ARG, "pz_balance_step: bad arguments");
+  const PzInst& I = h->inst[inst];
+  if ((I.flags & (PZF_INTEG | PZF_DIRECT)) || I.dirk)
+    return fail(h, PZ_E_UNSUPPORTED,
+                "pz_balance_step: the force balances are computed for the collocation method with the "
+                "influence-matrix solve and a multistep scheme");
+  const long long MN = (long long)I.M * I.N, fld = 2LL * F_COUNT * MN;
+  size_t need = 0;
+  for (int i = 0; i < h->n_inst; ++i) {
+    const long long mn = (long long)h->inst[i].M * h->inst[i].N;
+    need = std::max(need, (size_t)(2LL * F_COUNT * mn + 12 * mn + 4LL * h->inst[i].N));
+  }
+  cudaError_t e = cudaSuccess;
+  if (!h->d_bal) e = cudaMalloc(&h->d_bal, need * sizeof(double));
+  if (e) { h->d_bal = nullptr; return cuda_fail(h, e, "pz_balance_step"); }
+  double* snap = h->d_bal;
+  double* dv = snap + fld;
+  double* dp = dv + 12 * MN;
+  e = cudaMemcpyAsync(snap, h->pool + I.o_fld, fld * sizeof(double), cudaMemcpyDeviceToDevice, h->stream);
+  if (e) return cuda_fail(h, e, "pz_balance_step");
+  int rc = pz_step(h, 1);
+  if (rc) return rc;
+  e = pz_launch_balance(h->dev, inst, I.M, snap, dv, dp, h->stream);
+  if (!e) e = cudaMemcpyAsync(vort, dv, 12 * MN * sizeof(double), cudaMemcpyDeviceToHost, h->stream);
+  if (!e) e = cudaMemcpyAsync(vp, dp, 4LL * I.N * sizeof(double), cudaMemcpyDeviceToHost, h->stream);
+  if (!e) e = cudaStreamSynchronize(h->stream);
+  if (e) return cuda_fail(h, e, "pz_balance_step");
+  return check_status(h);
+}
+
 extern "C" int pz_get_spectra_2d(pz_handle* h, int inst, double* out) {
   if (!h) return fail(nullptr, PZ_E_ARG, "pz_get_spectra_2d: null handle");
   if (inst < 0 || inst >= h->n_inst || !out) return fail(h, PZ_E_ARG, "pz_get_spectra_2d: bad arguments");
@@ -1716,6 +1748,7 @@ extern "C" int pz_destroy(pz_handle* h) {
   cudaFree(h->d_rows);
   cudaFree(h->d_spec);
   cudaFree(h->d_spec2d);
+  cudaFree(h->d_bal);
   cudaFree(h->d_oitems);
   cudaFree(h->d_obs_part);
   cudaFree(h->d_obs_cnt);

@@ -278,6 +278,8 @@ struct PzLaunch { int kind, stage; };
 cudaError_t pz_launch_step_kernel(const PzDev& d, int kind, int stage, cudaStream_t s);
 const char* pz_step_kernel_name(int kind);
 cudaError_t pz_launch_obs(const PzDev& d, int only, cudaStream_t s);
+cudaError_t pz_launch_balance(const PzDev& d, int inst, int n_m_max, const double* snap, double* vort, double* vp,
+                              cudaStream_t s);
 cudaError_t pz_launch_spectra(const PzDev& d, int inst, int n_m_max, double* out, double* out2d, cudaStream_t s);
 cudaError_t pz_launch_gather_rows(const PzDev& d, double* out, cudaStream_t s);
 cudaError_t pz_setup_kernels();

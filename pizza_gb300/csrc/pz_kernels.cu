@@ -1630,6 +1630,96 @@ __global__ void k_spectra(PzDev d, int inst, double* out, double* out2d) {
   }
 }
 
+// ---------------------------------------------------------------------------
+// k_balance: the vorticity and u_phi force balances of one instance over the
+// step just taken (vort_balance.f90 and vp_balance.f90 with their hooks in
+// update_psi_coll_dmat.f90: initialize/finalize_domdt :154-156, :449-451,
+// buo :214-230, adv/cor :500-505, pump :540-546, visc :643-676; the u_phi
+// terms :183-187, :444-446, :642-647), from the fields at the start of the
+// step (snap: the instance's field block copied before it) and after it.
+// One block per m.  vort: 6 terms (buo, cor, adv, dwdt, visc, pump) at
+// vort[((t N + r) M + m)] complex; vp (m = 0 block): rey_stress, dvpdt, visc,
+// pump at vp[t N + r].  As in the reference, dwdt of m /= 0 takes the new
+// vorticity in Chebyshev space (finalize_domdt runs before the transform back)
+// minus the old one in physical space, and visc has no ViscFac factor.
+// ---------------------------------------------------------------------------
+__global__ void k_balance(PzDev d, int inst, const double2* __restrict__ snap, double2* vort, double* vp) {
+  const PzInst& I = d.inst[inst];
+  const PzState& S = d.state[inst];
+  const View V{&I, d.pool};
+  const int n = I.N, M = I.M, mi = blockIdx.x, m = mi * I.minc;
+  const double dm = (double)m, dt = S.dt[0];
+  MS s = ms_smem(n);
+  auto sfld = [&](int f) { return snap + ((long long)f * M + mi) * n; };
+  const double2* us0 = sfld(F_US);
+  const double2* up0 = sfld(F_UP);
+  const double2* om0 = sfld(F_OM);
+  const double2* T0 = sfld(F_TEMP);
+  const double* or1 = V.rad(RV_OR1);
+  const double* or2 = V.rad(RV_OR2);
+  const double* beta = V.rad(RV_BETA);
+  const double* rgrav = V.rad(RV_RGRAV);
+  const double* ekpump = V.rad(RV_EKPUMP);
+  const bool chem = (I.flags & PZF_CHEM) != 0;
+  auto out = [&](int t, int r) -> double2& { return vort[((long long)t * n + r) * M + mi]; };
+  // new vorticity and its derivatives (physical), its Chebyshev coefficients
+  for (int i = threadIdx.x; i < n; i += blockDim.x) s.a[i] = V.fld(F_OM, mi)[i];
+  __syncthreads();
+  op_Dp2(V, n, s.a, s.b, s.c, s.w);
+  __syncthreads();
+  op_C(V, n, s.a, s.e, s.w);
+  __syncthreads();
+  const double2* ex = V.hist(1, 2, S.r_expl, mi);
+  for (int i = threadIdx.x; i < n; i += blockDim.x) {
+    const double2 z = make_double2(0.0, 0.0);
+    if (m == 0) {
+      for (int t = 0; t < 6; ++t) out(t, i) = z;
+      out(3, i) = cscale(1.0 / dt, csub(s.a[i], om0[i]));
+      continue;
+    }
+    double2 buo = cscale(-I.BuoFac * rgrav[i] * or1[i], cim(dm, V.fld(F_TEMP, mi)[i]));
+    if (chem) buo = csub(buo, cscale(I.ChemFac * rgrav[i] * or1[i], cim(dm, V.fld(F_XI, mi)[i])));
+    const double2 cor = (I.flags & PZF_NON_ROT) ? z : cscale(I.CorFac * beta[i], us0[i]);
+    double2 pump = z;
+    if (I.flags & PZF_EK_PUMP) {
+      const double2 u = us0[i];
+      const double2 q = make_double2(V.rad(RV_EKP_US)[i] * u.x - V.rad(RV_EKP_DUSDP)[i] * dm * u.y,
+                                     V.rad(RV_EKP_US)[i] * u.y + V.rad(RV_EKP_DUSDP)[i] * dm * u.x);
+      const double2 w = cadd(cadd(om0[i], cscale(V.rad(RV_EKP_UP)[i], up0[i])), q);
+      pump = cscale(-I.CorFac * ekpump[i], w);
+    }
+    // the explicit term of the step is adv + cor - buoyancy (explicit) + pump
+    double2 adv = csub(csub(ex[i], cor), pump);
+    if (!(I.flags & PZF_BUO_IMP)) {
+      double2 b = cscale(-I.BuoFac * rgrav[i] * or1[i], cim(dm, T0[i]));
+      if (chem) b = csub(b, cscale(I.ChemFac * rgrav[i] * or1[i], cim(dm, sfld(F_XI)[i])));
+      adv = csub(adv, b);
+    }
+    const double2 lap = make_double2(s.c[i].x + or1[i] * s.b[i].x - dm * dm * or2[i] * s.a[i].x,
+                                     s.c[i].y + or1[i] * s.b[i].y - dm * dm * or2[i] * s.a[i].y);
+    out(0, i) = buo;
+    out(1, i) = cor;
+    out(2, i) = adv;
+    out(3, i) = cscale(1.0 / dt, csub(s.e[i], om0[i]));
+    out(4, i) = lap;
+    out(5, i) = pump;
+  }
+  if (m != 0) return;
+  __syncthreads();
+  // u_phi: derivatives of the new u_phi(m = 0)
+  for (int i = threadIdx.x; i < n; i += blockDim.x) s.f[i] = make_double2(V.fld(F_UP, 0)[i].x, 0.0);
+  __syncthreads();
+  op_Dp2(V, n, s.f, s.g, s.h, s.w);
+  __syncthreads();
+  for (int i = threadIdx.x; i < n; i += blockDim.x) {
+    const double u = s.f[i].x;
+    vp[i] = ex[i].x;
+    vp[n + i] = (u - up0[i].x) / dt;
+    vp[2 * n + i] = I.ViscFac * (s.h[i].x + or1[i] * s.g[i].x - or2[i] * u);
+    vp[3 * n + i] = (I.flags & PZF_EK_PUMP) ? -I.CorFac * ekpump[i] * u : 0.0;
+  }
+}
+
 // One block per PZ_OBS_RC radii of one instance (PzDev::oitems).  Thread
 // (r, c) sums the m = c, c + 16, ... terms of its radius; the block applies
 // the radial weights and writes its partial sums, and the last block of the
@@ -1881,6 +1971,13 @@ cudaError_t pz_launch_start(const PzDev& d, int only, cudaStream_t s) {
 
 cudaError_t pz_launch_spectra(const PzDev& d, int inst, int n_m_max, double* out, double* out2d, cudaStream_t s) {
   k_spectra<<<n_m_max, 64, 0, s>>>(d, inst, out, out2d);
+  return cudaGetLastError();
+}
+
+cudaError_t pz_launch_balance(const PzDev& d, int inst, int n_m_max, const double* snap, double* vort, double* vp,
+                              cudaStream_t s) {
+  k_balance<<<n_m_max, 128, ms_smem_bytes(d.maxN), s>>>(d, inst, reinterpret_cast<const double2*>(snap),
+                                                        reinterpret_cast<double2*>(vort), vp);
   return cudaGetLastError();
 }
 

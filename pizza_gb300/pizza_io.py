@@ -193,6 +193,187 @@ def read_2d_spectra(path: str):
     return out
 
 
+# ---------------------------------------------------------------------------
+# force balances (vort_balance.f90, vp_balance.f90), accumulated on the host
+# from the device terms of Ensemble.balance_step
+# ---------------------------------------------------------------------------
+def _cc2real(z, m):
+    """cc2real (src/useful.f90): Re(z)^2 for m = 0, 2 |z|^2 otherwise; m (M,) broadcast over r."""
+    z = np.asarray(z)
+    out = 2.0 * (z.real ** 2 + z.imag ** 2)
+    out[np.asarray(m) == 0] = (z.real ** 2)[np.asarray(m) == 0]
+    return out
+
+
+def simps(f, r):
+    """simps (src/integration.f90:102-152): Simpson's rule on the (non-uniform)
+    radial grid, r(1) = r_cmb first; twice Simpson plus trapezoids for an even
+    number of points."""
+    n = len(f)
+
+    def panel(i):
+        h2 = r[i + 1] - r[i]
+        h1 = r[i] - r[i - 1]
+        return (h1 + h2) / 6.0 * (f[i - 1] * (2 * h1 - h2) / h1 + f[i] * (h1 + h2) ** 2 / (h1 * h2)
+                                  + f[i + 1] * (2 * h2 - h1) / h2)
+    if n % 2 == 1:
+        return -sum(panel(i) for i in range(1, n - 1, 2))
+    rint = 0.5 * (r[1] - r[0]) * (f[1] + f[0])
+    for i in range(2, n, 2):
+        rint += panel(i)
+    rint += 0.5 * (r[n - 1] - r[n - 2]) * (f[n - 1] + f[n - 2])
+    for i in range(1, n - 1, 2):
+        rint += panel(i)
+    return -0.5 * rint
+
+
+def rint_weights(n_r_max: int, radratio: float):
+    """Weights w of rInt_R (src/integration.f90:18-55, Chebyshev grid):
+    rInt_R(f) = sum_k w_k f_k (the DCT-I of f / drx, the integrals of the
+    Chebyshev polynomials)."""
+    N = n_r_max
+    drx = 2.0                                   # 2 / (r_cmb - r_icb), unit gap
+    k = np.arange(N)
+    C = 2.0 * np.cos(np.pi * np.outer(k, k) / (N - 1))
+    C[:, 0] = 1.0
+    C[:, N - 1] = (-1.0) ** k
+    C *= np.sqrt(0.5 / (N - 1))                 # costf_real_1d
+    a = np.zeros(N)
+    a[0] = 0.5
+    for nc in range(3, N + 1, 2):
+        a[nc - 1] = -1.0 / float(nc * (nc - 2))
+    a[N - 1] *= 0.5 if (N - 1) % 2 == 0 else 1.0
+    w = 2.0 * np.sqrt(2.0 / (N - 1)) * (a @ C) / drx
+    return w
+
+
+class VortBalance:
+    """The vorticity force balance averaged over time (vort_balance.f90:
+    calc_avg and mean_sd_loc :188-262, write_outputs :264-520): per call the
+    six terms of Ensemble.balance_step and three sums (thwind = buo + cor,
+    iner = adv - dwdt, cia = adv - dwdt + buo + cor) give cc2real(term) r
+    height, averaged at every (m, r) (with SD if l_sd) and, with the points
+    within bl_cut of the walls left out, integrated over r by simps and
+    averaged per m.  Writes vort_terms_avg.TAG and vort_bal.TAG."""
+
+    QUANT = ("buo", "cor", "adv", "dwdt", "visc", "pump", "thwind", "iner", "cia")
+
+    def __init__(self, cfg, r, height, l_sd: bool = False, bl_cut: float = 1.0e-3):
+        self.cfg, self.r, self.h = cfg, np.asarray(r, float), np.asarray(height, float)
+        self.l_sd, self.bl_cut = l_sd, bl_cut
+        M, N = cfg.m_max // cfg.minc + 1, len(self.r)
+        self.m = np.arange(M) * cfg.minc
+        self.mean2 = {q: np.zeros((M, N)) for q in self.QUANT}
+        self.sd2 = {q: np.zeros((M, N)) for q in self.QUANT}
+        self.meanM = {q: np.zeros(M) for q in self.QUANT}
+        self.sdM = {q: np.zeros(M) for q in self.QUANT}
+        self.n_calls = 0
+        self.time_last = 0.0
+        r_cmb = 1.0 / (1.0 - cfg.radratio)
+        self.mask = (self.r >= r_cmb - bl_cut) | (self.r <= r_cmb - 1.0 + bl_cut)
+
+    @staticmethod
+    def _msd(mean, sd, x, n, dt, total):
+        if n == 1:
+            return x.copy(), np.zeros_like(x)
+        delta = x - mean
+        mean = mean + delta * dt / total
+        return mean, sd + dt * delta * (x - mean)
+
+    def calc_avg(self, vort, time_avg: float):
+        """vort: the "vort" dict of Ensemble.balance_step; time_avg: the running
+        sum of dt over the balance steps (timeAvg_vortbal, outputs.f90:335-338)."""
+        self.n_calls += 1
+        dt = time_avg - self.time_last
+        t = vort
+        terms = {"buo": t["buo"], "cor": t["cor"], "adv": t["adv"], "dwdt": t["dwdt"], "visc": t["visc"],
+                 "pump": t["pump"], "thwind": t["buo"] + t["cor"], "iner": -t["dwdt"] + t["adv"],
+                 "cia": -t["dwdt"] + t["adv"] + t["buo"] + t["cor"]}
+        mcol = self.m[:, None] * np.ones_like(self.r)[None, :]
+        for q in self.QUANT:
+            dat = _cc2real(terms[q], mcol) * self.r * self.h
+            self.mean2[q], self.sd2[q] = self._msd(self.mean2[q], self.sd2[q], dat, self.n_calls, dt, time_avg)
+            dat = np.where(self.mask, 0.0, dat)
+            val = np.array([simps(dat[k], self.r) for k in range(dat.shape[0])])
+            self.meanM[q], self.sdM[q] = self._msd(self.meanM[q], self.sdM[q], val, self.n_calls, dt, time_avg)
+        self.time_last = time_avg
+
+    def terms_lines(self):
+        """vort_terms_avg.TAG: '(I5, 18es16.8)' of m >= 1 and the mean and SD
+        of buo, cor, adv, dwdt, visc, pump, thwind, iner, cia."""
+        out = []
+        order = ("buo", "cor", "adv", "dwdt", "visc", "pump", "thwind", "iner", "cia")
+        for k, m in enumerate(self.m):
+            if m < 1:
+                continue
+            vals = []
+            for q in order:
+                vals += [self.meanM[q][k], np.sqrt(self.sdM[q][k] / self.time_last)]
+            out.append(f"{m:5d}" + "".join(fortran_es(v, 16, 8) for v in vals))
+        return out
+
+    def write(self, tag: str, directory: str = "."):
+        """vort_terms_avg.TAG and vort_bal.TAG (version 1, or 2 with SD; the
+        header of 2D_spec_avg, then per quantity its (n_m_max, n_r_max) mean
+        (and SD) with m varying fastest)."""
+        p1 = os.path.join(directory, f"vort_terms_avg.{tag}")
+        with open(p1, "w") as f:
+            for ln in self.terms_lines():
+                f.write(ln + "\n")
+        cfg = self.cfg
+        M, N = len(self.m), len(self.r)
+        p2 = os.path.join(directory, f"vort_bal.{tag}")
+        with open(p2, "wb") as f:
+            np.array([2 if self.l_sd else 1], _I4).tofile(f)
+            np.array([cfg.ra, cfg.pr, cfg.raxi, cfg.sc, cfg.ek, cfg.radratio], _F8).tofile(f)
+            np.array([N, M, cfg.m_max, cfg.minc], _I4).tofile(f)
+            self.r.astype(_F8).tofile(f)
+            for q in ("buo", "cor", "adv", "dwdt", "visc", "pump", "thwind", "iner", "cia"):
+                np.ascontiguousarray(self.mean2[q].T, _F8).tofile(f)
+                if self.l_sd:
+                    np.ascontiguousarray(np.sqrt(self.sd2[q] / self.time_last).T, _F8).tofile(f)
+        return p1, p2
+
+
+class VpBalance:
+    """The u_phi (m = 0) force balance (vp_balance.f90:write_outputs
+    :140-210): per call, vphi_bal.TAG (stream unformatted: ra, ek, pr,
+    radratio, raxi, sc and r once, then time, u_phi(m = 0), dvpdt,
+    rey_stress, pump, visc) and one vphi_power.TAG line '(1P,es20.12,5es16.8)'
+    of time, Ez and the powers 2 pi rInt_R(term u_phi height r)."""
+
+    def __init__(self, cfg, r, height, tag: str, directory: str = "."):
+        self.cfg, self.r, self.h = cfg, np.asarray(r, float), np.asarray(height, float)
+        self.w = rint_weights(len(self.r), cfg.radratio)
+        self.bal = os.path.join(directory, f"vphi_bal.{tag}")
+        self.power = os.path.join(directory, f"vphi_power.{tag}")
+        self.n_calls = 0
+        for p in (self.bal, self.power):
+            if os.path.exists(p):
+                os.remove(p)
+
+    def write(self, time: float, up_m0, vp):
+        """up_m0: the real part of u_phi(m = 0) after the balance step; vp: the
+        "vp" dict of Ensemble.balance_step."""
+        self.n_calls += 1
+        cfg = self.cfg
+        vz = np.asarray(up_m0, float).real
+        with open(self.bal, "ab") as f:
+            if self.n_calls == 1:
+                np.array([cfg.ra, cfg.ek, cfg.pr, cfg.radratio, cfg.raxi, cfg.sc], _F8).tofile(f)
+                self.r.astype(_F8).tofile(f)
+            np.array([time], _F8).tofile(f)
+            for a in (vz, vp["dvpdt"], vp["rey_stress"], vp["pump"], vp["visc"]):
+                np.asarray(a, _F8).tofile(f)
+        hr = self.h * self.r
+        ez = np.pi * self.w @ (vz * vz * hr)
+        vals = [2.0 * np.pi * self.w @ (vp[k] * vz * hr) for k in ("dvpdt", "rey_stress", "pump", "visc")]
+        with open(self.power, "a") as f:
+            f.write(fortran_es(time, 20, 12) + fortran_es(ez, 16, 8) + "".join(fortran_es(v, 16, 8) for v in vals)
+                    + "\n")
+        return ez, vals
+
+
 def write_series(ens, i: int, tag: str, directory: str = ".", rows=None):
     """Write e_kin.TAG, heat.TAG, (rotating runs) e_kin_3D.TAG and (with
     composition) composition.TAG of instance i from its time-series rows

@@ -49,6 +49,7 @@ def main():
     for name in ("matplotlib", "matplotlib.pyplot", "matplotlib.colors", "matplotlib.cm", "matplotlib.ticker"):
         mod = sys.modules.setdefault(name, types.ModuleType(name))
         mod.__version__ = "3.0.0"
+    sys.dont_write_bytecode = True             # the reference tree stays untouched
     sys.path.insert(0, os.path.join(args.ref, "python"))
     from pizza.spectrum import Pizza2DSpectrum
     sp = object.__new__(Pizza2DSpectrum)

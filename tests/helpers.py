@@ -44,14 +44,15 @@ def series_from_oracle(sim):
                      ht[1], ht[2], ht[3], ht[4], ht[5], ht[6], ht[7], sim.ts.dt[0]] + list(ch[1:]))
 
 
-def fp64_noise(sim, rng, level=1e-13):
+def fp64_noise(sim, rng, level=1e-13, fields=("temp", "om")):
     """Add to the oracle's temperature and vorticity complex normal deviates
     of `level` times each field's largest modulus: the size of the rounding
     differences that another FP64 implementation (another summation order of
     the transforms and products) makes per step.  The m = 0 modes stay real.
     Run after every step, it measures how far the oracle drifts from itself
-    under rounding alone."""
-    for f in ("temp", "om"):
+    under rounding alone.  (The integration method's prognostic variables
+    are the temperature and the streamfunction: perturb its temperature only.)"""
+    for f in fields:
         a = getattr(sim, f)
         s = level * np.max(np.abs(a))
         a = a + s * (rng.standard_normal(a.shape) + 1j * rng.standard_normal(a.shape))

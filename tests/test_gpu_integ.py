@@ -241,7 +241,7 @@ def _c1_oracle(pert):
         for _ in range(k - done):
             sim.advance()
             if pert:
-                fp64_noise(sim, rng, pert)
+                fp64_noise(sim, rng, pert, fields=("temp",))
         done = k
         out[k] = {f: getattr(sim, f).copy() for f in ("us", "up", "om", "temp", "psi")}
     return out
@@ -252,7 +252,8 @@ def test_c1_integ_sbdf3_full_size(pz):
     Ra=3e7, SBDF3, dt=2e-6, seeded amplitude 1e-4) over its 2000 steps
     against the oracle at steps 20, 500, 1000 and 2000.  The bar is 1e-10
     relative while the oracle's own spread (its run with fp64_noise of 1e-13
-    after every step) stays below 1e-12, and 100x that spread beyond.  The tau rows, which hold in Chebyshev space, are checked
+    on the temperature after every step) stays below 1e-12, and 100x that
+    spread beyond.  The tau rows, which hold in Chebyshev space, are checked
     on the final GPU state: for T and psi (m > 0) c_0/2 + sum_n c_n (+-1)^n = 0
     at both walls (the physical wall value differs from it by the DCT-I's
     half weight on c_{N-1})."""

@@ -187,3 +187,49 @@ def test_device_2d_spectra_match_oracle(pz, tmp_path):
     mean, sd = av.result()
     assert back["version"] == 2 and back["n_r_max"] == spec["n_r_max"]
     assert np.array_equal(back["us2"], mean[0].T) and np.array_equal(back["enst_SD"], sd[2].T)
+
+
+@pytest.mark.parametrize("variant,fast", [(dict(), True), (dict(), False),
+                                          (dict(buo_term="EXPLICIT", pr=0.7), False),
+                                          (dict(l_non_rot=True, l_ek_pump=False, ra=2e4, dtMax=1e-4), True)])
+def test_force_balances_match_oracle(pz, tmp_path, variant, fast):
+    """The vorticity and u_phi force balances (pz_balance_step) against the
+    oracle's record of the same step, per term relative to its largest
+    value, at the 6th and 9th step, on the tensor-core stage and on the dense
+    kernels; then the time-averaged files written from the device terms."""
+    from pizza_gb300.pizza_io import VortBalance, VpBalance
+    spec = dict(C0, matrix_solve="INFLUENCE", time_scheme="CNAB2", **variant)
+    t0 = seeded(spec, 71, 1e-2)
+    sim = oracle(spec, temp0=t0)
+    prev = pz.fast_path(fast)
+    try:
+        ens = pz.Ensemble(gpu_config(spec))
+    finally:
+        pz.fast_path(prev)
+    ens.set_state(0, temp=t0)
+    cfg = gpu_config(spec)
+    vb = VortBalance(cfg, sim.r, sim.height, l_sd=True)
+    vpb = VpBalance(cfg, sim.r, sim.height, "gpu", str(tmp_path))
+    t_avg, done = 0.0, 0
+    for k in (6, 9):
+        for _ in range(k - 1 - done):
+            sim.advance()
+        ens.step(k - 1 - done)
+        ref = sim.balance_step()
+        got = ens.balance_step(0)
+        done = k
+        for part in ("vort", "vp"):
+            for name, a in ref[part].items():
+                b = got[part][name]
+                scale = np.max(np.abs(a))
+                if scale == 0.0:
+                    assert np.max(np.abs(b)) == 0.0, (k, part, name)
+                    continue
+                e = np.max(np.abs(b - a)) / scale
+                assert e < 1e-10, (k, part, name, e)
+        t_avg += sim.ts.dt[0]
+        vb.calc_avg(got["vort"], t_avg)
+        vpb.write(sim.time, ens.get_state(0)["up"][0].real, got["vp"])
+    p1, p2 = vb.write("gpu", str(tmp_path))
+    assert len(open(p1).read().splitlines()) == spec["m_max"]
+    assert os.path.getsize(vpb.bal) == 8 * (6 + spec["n_r_max"] + 2 * (1 + 5 * spec["n_r_max"]))

@@ -164,3 +164,45 @@ def test_2d_spectra_match_reference_reader_fixture(tmp_path):
     var = sum(d * (x - mean) ** 2 for d, x in zip(dts, snaps)) / times[-1]
     np.testing.assert_allclose(got["us2"], mean[0].T, rtol=1e-13)
     np.testing.assert_allclose(got["up2_SD"], np.sqrt(var[1]).T, rtol=1e-10)
+
+
+def test_force_balance_files_match_reference_reader_fixture(tmp_path):
+    """The vort_bal / vort_terms_avg / vphi_bal / vphi_power writers against
+    the golden files that the reference's own readers parsed
+    (tests/golden/make_balance_golden.py): the same bytes; the parsed
+    averages against their closed form (getMSD2's recursion, cc2real r
+    height), and the u_phi records as written."""
+    import json
+    import sys
+    here = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+    sys.path.insert(0, here)
+    from make_balance_golden import TERMS, sample, write_sample
+    paths = write_sample(str(tmp_path))
+    for p in paths:
+        with open(p, "rb") as a, open(os.path.join(here, os.path.basename(p)), "rb") as b:
+            assert a.read() == b.read(), os.path.basename(p)
+    with open(os.path.join(here, "balance_golden.json")) as f:
+        ref = json.load(f)
+    cfg, r, height, calls = sample()
+    assert ref["version"] == 2 and ref["n_r_max"] == len(r) and ref["n_m_max"] == cfg.m_max + 1
+    m = np.arange(cfg.m_max + 1)[:, None]
+
+    def cc2(z):
+        out = 2.0 * np.abs(z) ** 2
+        out[0] = z[0].real ** 2
+        return out * r * height
+    # equal averaging steps: the mean is the plain mean over the calls
+    for key, q in (("buo_mean", "buo"), ("cor_mean", "cor"), ("adv_mean", "adv"), ("domdt_mean", "dwdt"),
+                   ("visc_mean", "visc"), ("pump_mean", "pump")):
+        want = sum(cc2(c[1][q]) for c in calls) / len(calls)
+        np.testing.assert_allclose(np.array(ref[key]), want, rtol=1e-12, err_msg=key)
+    want = sum(cc2(c[1]["buo"] + c[1]["cor"]) for c in calls) / len(calls)
+    np.testing.assert_allclose(np.array(ref["thwind_mean"]), want, rtol=1e-12)
+    v = ref["vphi"]
+    assert v["time"] == [c[0] for c in calls]
+    np.testing.assert_array_equal(np.array(v["vp"]), np.array([c[2] for c in calls]))
+    np.testing.assert_array_equal(np.array(v["rey_stress"]), np.array([c[3]["rey_stress"] for c in calls]))
+    np.testing.assert_array_equal(np.array(v["visc"]), np.array([c[3]["visc"] for c in calls]))
+    lines = open(paths[3]).read().splitlines()
+    assert len(lines) == 3 and all(len(ln) == 20 + 5 * 16 for ln in lines)
+    assert TERMS == ("buo", "cor", "adv", "dwdt", "visc", "pump")
