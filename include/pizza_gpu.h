@@ -315,7 +315,10 @@ int pz_explicit_terms_noalloc(pz_handle* h, int inst, const double* us, const do
  * and the gradient is taken with respect to the initial temperature
  * perturbation (the temp argument of pz_set_state) and Ra, for a fixed
  * time-step sequence.  The collocation step with the influence-matrix solve
- * is covered, with CNAB2 or a DIRK scheme (one scheme for all instances).
+ * is covered, with CNAB2 or a DIRK scheme (one scheme for all instances), and
+ * with pizza's default direct solve (update_om_coll_smat, the coupled
+ * vorticity-streamfunction system with implicit Ekman pumping and, with
+ * corio_term='IMPLICIT', implicit Coriolis) with CNAB2.
  *
  * The objective is selected per sweep: PZ_OBJ_EKIN3D (above) or
  * PZ_OBJ_NUTOP, the mean of NuTop = 1 + dT/dr(m=0, r_cmb)/dtcond(r_cmb).
@@ -381,13 +384,14 @@ int pz_fast_path(int enable);
 
 /* Process-wide choice, for handles created afterwards, of how the
  * integration method (cheb_method='integ') solves its per-m tau-bordered
- * systems.  enable = 1 (the default): bordered banded LU factors, as the
- * reference's type_bordmat (src/bordered_matrix.f90:137-183 over
+ * systems.  enable = 1: bordered banded LU factors, as the reference's
+ * type_bordmat (src/bordered_matrix.f90:137-183 over
  * src/band_matrix.f90:212-261): the banded block is factorised with partial
  * pivoting inside the band when dt changes, the tau rows through a Schur
- * complement, and every stage runs banded sweeps.  enable = 0: dense per-m
- * inverses applied as dense products.  Both give the reference's step to
- * FP64 rounding.  enable < 0 only queries.  Returns the previous setting. */
+ * complement, and every stage runs banded sweeps.  enable = 0 (the default,
+ * the faster on this GPU): dense per-m inverses applied as dense products
+ * with every lane busy.  Both give the reference's step to FP64 rounding.
+ * enable < 0 only queries.  Returns the previous setting. */
 int pz_integ_banded(int enable);
 
 /* No counterpart in the reference (pizza chooses its MPI transpose variant

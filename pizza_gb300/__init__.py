@@ -228,8 +228,8 @@ def integ_operator(n_r_max: int, radratio: float, name: str):
 
 
 def integ_banded(enable=None) -> bool:
-    """Bordered banded factors (True, the default) or dense per-m inverses
-    (False) for the integration method's solves, for handles created
+    """Bordered banded factors (True) or dense per-m inverses (False, the
+    default) for the integration method's solves, for handles created
     afterwards (pz_integ_banded); None only queries.  Returns the previous
     setting."""
     lib = load_library()

@@ -1,4 +1,6 @@
-// Discrete adjoint of the CNAB2 collocation step (influence-matrix solve):
+// Discrete adjoint of the CNAB2 collocation step (influence-matrix solve, or
+// the direct solve of update_om_coll_smat, whose coupled solve transposes to
+// G^H and whose implicit Ekman pumping and Coriolis terms join L^T):
 // gradient of a time-averaged 3-D kinetic energy or outer-boundary Nusselt
 // number with respect to the initial temperature perturbation and to BuoFac
 // (hence Ra).
@@ -153,6 +155,23 @@ __device__ __forceinline__ double2 caxpy(double s, double2 x, double2 y) {
 // Re(conj(x) y)
 __device__ __forceinline__ double cdotr(double2 x, double2 y) { return x.x * y.x + x.y * y.y; }
 
+// y = G^H (x0; x1), G complex 2n x n column-major with leading dimension 2n
+// (the smat solve's inverse columns): the adjoint of (x0, x1) = G y
+struct CDenseDotH {
+  const double2* __restrict__ G; int n; const double2* __restrict__ x0; const double2* __restrict__ x1;
+  double* __restrict__ y;
+  __device__ __forceinline__ double fma(int t, int i, double acc) const {
+    const double2 g = __ldg(G + i + (long long)(t >> 1) * 2 * n);
+    const double2 v = i < n ? x0[i] : x1[i - n];
+    return (t & 1) ? ::fma(g.x, v.y, ::fma(-g.y, v.x, acc)) : ::fma(g.x, v.x, ::fma(g.y, v.y, acc));
+  }
+  __device__ __forceinline__ void store(int t, double v) const { y[t] = v; }
+};
+__device__ __forceinline__ void cmvH_lanes(const double2* __restrict__ G, int n, const double2* __restrict__ x0,
+                                           const double2* __restrict__ x1, double2* __restrict__ y) {
+  lane_dots(CDenseDotH{G, n, x0, x1, reinterpret_cast<double*>(y)}, 2 * n, 2 * n);
+}
+
 // ---------------------------------------------------------------------------
 // forward-sweep helpers
 // ---------------------------------------------------------------------------
@@ -289,7 +308,14 @@ __global__ void __launch_bounds__(256, 4) k_adj_solve(PzAdjDev a, int n, int slo
     pc[i] = (m == 0) ? cz() : A.plane(AP_PCB, mi)[i];
   }
   __syncthreads();
+  if (m != 0 && (I.flags & PZF_DIRECT)) {
+    // update_om_coll_smat's coupled solve (update_psi_coll_smat.f90:88-321):
+    // (oc, pc) = G rhs  ->  rhs_bar = G^H (oc_bar, pc_bar)
+    cmvH_lanes(reinterpret_cast<const double2*>(a.d.pool + I.o_gsm) + 2LL * mi * N * N, N, oc, pc, rP);
+    __syncthreads();
+  }
   if (m != 0) {
+    if (!(I.flags & PZF_DIRECT)) {
     // influence correction (update_psi_coll_dmat.f90:1256-1300), transposed
     const long long MN = (long long)I.M * N;
     const double* aux = a.d.pool + I.o_aux;
@@ -321,6 +347,7 @@ __global__ void __launch_bounds__(256, 4) k_adj_solve(PzAdjDev a, int n, int slo
     __syncthreads();
     mvT_lanes(a.d.pool + I.o_gom + (long long)mi * N * N, N, x, rP);
     __syncthreads();
+    }
     // implicit buoyancy of the new temperature in the vorticity rhs
     for (int i = threadIdx.x; i < N; i += blockDim.x) {
       if (i == 0 || i == N - 1) rP[i] = cz();
@@ -550,6 +577,7 @@ __global__ void __launch_bounds__(256, 3) k_adj_lin(PzAdjDev a, int n, int slot,
   const bool buo_imp = (I.flags & PZF_BUO_IMP) != 0;
   const bool rot = !(I.flags & PZF_NON_ROT);
   const bool ek = (I.flags & PZF_EK_PUMP) != 0;
+  const bool direct = (I.flags & PZF_DIRECT) != 0;
   const double TdF = I.TdiffFac, Vis = I.ViscFac;
   const double* rr = V.rad(RV_R);
   const double* or1 = V.rad(RV_OR1);
@@ -580,8 +608,10 @@ __global__ void __launch_bounds__(256, 3) k_adj_lin(PzAdjDev a, int n, int slot,
     const double gT = dtcond[i] - I.tadvz * beta[i] * tcond[i];
     double2 usb = caxpy(-gT, eT, aus), upb = aup, omb = aom;
     if (m != 0) {
-      if (rot) usb = caxpy(I.CorFac * beta[i], eP, usb);
-      if (ek) {
+      // explicit Coriolis: dmat when rotating, smat unless it is implicit;
+      // Ekman pumping is explicit with dmat, implicit (below) with smat
+      if (direct ? !(I.flags & PZF_COR_IMP) : rot) usb = caxpy(I.CorFac * beta[i], eP, usb);
+      if (ek && !direct) {
         const double ce = I.CorFac * ekpump[i];
         // (i m ekp_dusdp + ekp_us) us  ->  conj(.) eP
         usb = csub(usb, cscale(ce, csub(cscale(ekp_us[i], eP), cscale(ekp_dusdp[i], cim(dm, eP)))));
@@ -589,6 +619,14 @@ __global__ void __launch_bounds__(256, 3) k_adj_lin(PzAdjDev a, int n, int slot,
         omb = caxpy(-ce, eP, omb);
       }
       if (!buo_imp) Tb = cadd(Tb, cscale(I.BuoFac * rgrav[i] * or1[i], cim(dm, eP)));
+      if (direct) {
+        // smat's implicit Ekman pumping and Coriolis in iP (smat_imp_extra), transposed
+        const double ce = I.CorFac * ekpump[i];
+        usb = csub(usb, cscale(ce, csub(cscale(ekp_us[i], iPb), cscale(ekp_dusdp[i], cim(dm, iPb)))));
+        upb = caxpy(-ce * ekp_up[i], iPb, upb);
+        omb = caxpy(-ce, iPb, omb);
+        if (I.flags & PZF_COR_IMP) usb = caxpy(I.CorFac * beta[i], iPb, usb);
+      }
     }
     if (src && a.objective == PZ_OBJ_EKIN3D) {
       // d(us2_3D + up2_3D + uz2_3D)/d(us, up) of the state, averaged
@@ -1376,10 +1414,11 @@ extern "C" int pz_adjoint_forward(pz_handle* h, int objective, int n_steps, int 
   if (n_window < 0 || n_window > n_steps) return pz_fail(h, PZ_E_ARG, "pz_adjoint_forward: n_window outside [0, n_steps]");
   for (int i = 0; i < h->n_inst; ++i) {
     const PzInst& I = h->inst[i];
-    if ((I.scheme != PZ_CNAB2 && !I.dirk) || (I.flags & (PZF_DIRECT | PZF_INTEG | PZF_CHEM)))
+    if ((I.scheme != PZ_CNAB2 && !I.dirk) || (I.flags & (PZF_INTEG | PZF_CHEM)) ||
+        (I.dirk && (I.flags & PZF_DIRECT)))
       return pz_fail(h, PZ_E_UNSUPPORTED,
                      "pz_adjoint_forward: the adjoint covers the collocation step with the influence-matrix solve "
-                     "(CNAB2 or a DIRK scheme), without composition");
+                     "(CNAB2 or a DIRK scheme) or with the direct solve (CNAB2), without composition");
     if (I.scheme != h->inst[0].scheme)
       return pz_fail(h, PZ_E_UNSUPPORTED, "pz_adjoint_forward: all instances must use the same time scheme");
     if (adj_rloop_smem_bytes(I.P, I.rg, false) > PZ_SMEM_MAX)

@@ -24,7 +24,8 @@
 // changes (k_build); every stage applies the record with one thread per
 // real column walking the rows with its band window in registers (the
 // sweeps are sequential in the rows, 2-3 dependent operations per row),
-// the rest of the block doing the border products.
+// the rest of the block doing the border products.  The solve needs no
+// minimum block size.
 #pragma once
 
 // factorisation workspace in T units (plus nb ints of pivots after it)
@@ -233,7 +234,7 @@ template <> struct BordCol<double2> {
 // in shared memory): forward elimination with the pivots, then back
 // substitution; a window of the band in registers
 template <class T, int KL>
-__device__ void bord_sweep(const T* __restrict__ rec, int nb, const BordCol<T>& b) {
+__device__ __forceinline__ void bord_sweep(const T* __restrict__ rec, int nb, const BordCol<T>& b) {
   constexpr int R = 3 * KL + 2;
   const T zero = bz(T());
   T w[KL + 1];
@@ -253,25 +254,23 @@ __device__ void bord_sweep(const T* __restrict__ rec, int nb, const BordCol<T>& 
     for (int i = 0; i < KL; ++i) w[i] = w[i + 1];
     w[KL] = j + KL + 1 < nb ? b.ld(j + KL + 1) : zero;
   }
-  T u[2 * KL];              // y(j + 1 .. j + 2 KL)
-#pragma unroll
-  for (int c = 0; c < 2 * KL; ++c) u[c] = zero;
+  // back substitution: the older solution values y(j + 2 .. j + 2 KL) are
+  // read back from shared memory (stored at least two rows earlier), only the
+  // newest y(j + 1) is carried in a register; two chains, the newest term last
+  T u0 = zero;
   for (int j = nb - 1; j >= 0; --j) {
     const T* r = rec + (long long)j * R;
-    // the terms of the older solution values first, in two chains; the newest last
     T sa = b.ld(j), sb = zero;
 #pragma unroll
     for (int c = 2 * KL; c >= 2; c -= 2) {
-      sa = bfms(sa, r[c], u[c - 1]);
-      if (c - 1 >= 2) sb = bfms(sb, r[c - 1], u[c - 2]);
+      if (j + c < nb) sa = bfms(sa, r[c], b.ld(j + c));
+      if (c - 1 >= 2 && j + c - 1 < nb) sb = bfms(sb, r[c - 1], b.ld(j + c - 1));
     }
     T s = badd(sa, sb);            // sb holds minus its terms
-    s = bfms(s, r[1], u[0]);
+    s = bfms(s, r[1], u0);
     s = bmul(s, r[0]);
     b.st(j, s);
-#pragma unroll
-    for (int c = 2 * KL - 1; c > 0; --c) u[c] = u[c - 1];
-    u[0] = s;
+    u0 = s;
   }
 }
 
@@ -290,16 +289,17 @@ __device__ void bord_solve_k(const T* __restrict__ gr, int n, int nt, const doub
   constexpr bool real_op = sizeof(T) == sizeof(double);
   if (threadIdx.x < (real_op ? 2 : 1)) bord_sweep<T, KL>(st, nb, BordCol<T>(y + nt, threadIdx.x));
   __syncthreads();
-  // border: r_t = b1_t - A2_t y2, one warp per tau row
-  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-  if (wid < nt) {
+  // border: r_t = b1_t - A2_t y2, one warp per tau row (the block may have
+  // fewer warps than tau rows)
+  const int lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+  for (int t = threadIdx.x >> 5; t < nt; t += nw) {
     double ar = 0.0, ai = 0.0;
     for (int j = lane; j < nb; j += 32) {
-      const double2 v = bmul(A2[(long long)wid * nb + j], y[nt + j]);
+      const double2 v = bmul(A2[(long long)t * nb + j], y[nt + j]);
       ar += v.x; ai += v.y;
     }
     ar = warp_sum(ar); ai = warp_sum(ai);
-    if (lane == 0) { red[2 * wid] = y[wid].x - ar; red[2 * wid + 1] = y[wid].y - ai; }
+    if (lane == 0) { red[2 * t] = y[t].x - ar; red[2 * t + 1] = y[t].y - ai; }
   }
   __syncthreads();
   if (threadIdx.x < nt) {

@@ -537,7 +537,7 @@ int validate(const pz_config& c, std::string* why) {
 // ===========================================================================
 // process-wide default of the tensor-core stage for handles created afterwards
 int g_fast_default = 1;
-int g_integ_banded = 1;   // integration method: bordered banded factors (else dense inverses)
+int g_integ_banded = 0;   // integration method: bordered banded factors (else dense inverses)
 // process-wide tuning table (pz_tune_set): k_fast instances per block, and
 // k_rloop radii per block by n_phi_max; 0 = the built-in choice
 int g_tune_fast_g = 0;

@@ -12,10 +12,12 @@
 // the banded operators (IM_*) are applied with band_mv over their band
 // only.  The dt dependent left-hand sides (and the influence matrix's
 // dt-independent streamfunction operator) are bordered banded systems: their
-// tau rows are dense, every other row banded.  k_build factorises them per m
-// into bordered banded LU records (pz_bord.cuh) and every stage applies those
-// with banded sweeps; pz_integ_banded(0) switches a handle created afterwards
-// to dense per-m inverses applied as dense products instead.
+// tau rows are dense, every other row banded.  By default k_build inverts them
+// per m (Gauss-Jordan) and every stage applies the inverses as dense products
+// with every lane busy; pz_integ_banded(1) switches a handle created
+// afterwards to bordered banded LU records (pz_bord.cuh) applied by banded
+// sweeps, with a quarter of the flops but one or two active lanes per
+// sequential sweep, which the FP64 issue rate of this GPU makes the slower.
 #pragma once
 #include "pz_bord.cuh"
 

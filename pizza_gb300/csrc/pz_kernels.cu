@@ -1755,28 +1755,36 @@ __global__ void __launch_bounds__(256) k_obs(PzDev d, int only) {
     const int rl = threadIdx.x % RC, c = threadIdx.x / RC, r = r0 + rl;
     double us2 = 0, up2 = 0, nu = 0, fl = 0, ax = 0, sh = 0;
     if (r < n) {
-      for (int mi = c; mi < M; mi += NC) {
+      const double o2 = or2[r];
+      int mi = c;
+      if (mi == 0) {
+        const double2 a = us[r], b = up[r], tt = T[r], dt = dT[r];
+        if (chem) {
+          // sh_vol_r (outputs.f90:488-490)
+          const double2 dx = dX[r];
+          sh += dx.x * dx.x;
+        }
+        us2 += a.x * a.x;
+        up2 += b.x * b.x;
+        ax = b.x * b.x;
+        nu += dt.x * dt.x;
+        fl += a.x * tt.x - I.TdiffFac * dt.x - I.TdiffFac * dtcond[r];
+        mi += NC;
+      }
+      // m > 0: the loads of several m in flight at once
+#pragma unroll 4
+      for (; mi < M; mi += NC) {
         const long long o = (long long)mi * n + r;
         const double2 a = us[o], b = up[o], tt = T[o], dt = dT[o];
         const double mm = (double)(mi * I.minc);
         if (chem) {
-          // sh_vol_r (outputs.f90:488-490)
           const double2 x = X[o], dx = dX[o];
-          sh += mi == 0 ? dx.x * dx.x + mm * mm * or2[r] * (x.x * x.x)
-                        : 2.0 * (dx.x * dx.x + dx.y * dx.y) + mm * mm * or2[r] * 2.0 * (x.x * x.x + x.y * x.y);
+          sh += 2.0 * (dx.x * dx.x + dx.y * dx.y) + mm * mm * o2 * 2.0 * (x.x * x.x + x.y * x.y);
         }
-        if (mi == 0) {
-          us2 += a.x * a.x;
-          up2 += b.x * b.x;
-          ax = b.x * b.x;
-          nu += dt.x * dt.x + mm * mm * or2[r] * (tt.x * tt.x);
-          fl += a.x * tt.x - I.TdiffFac * dt.x - I.TdiffFac * dtcond[r];
-        } else {
-          us2 += 2.0 * (a.x * a.x + a.y * a.y);
-          up2 += 2.0 * (b.x * b.x + b.y * b.y);
-          nu += 2.0 * (dt.x * dt.x + dt.y * dt.y) + mm * mm * or2[r] * 2.0 * (tt.x * tt.x + tt.y * tt.y);
-          fl += 2.0 * (a.x * tt.x + a.y * tt.y);
-        }
+        us2 += 2.0 * (a.x * a.x + a.y * a.y);
+        up2 += 2.0 * (b.x * b.x + b.y * b.y);
+        nu += 2.0 * (dt.x * dt.x + dt.y * dt.y) + mm * mm * o2 * 2.0 * (tt.x * tt.x + tt.y * tt.y);
+        fl += 2.0 * (a.x * tt.x + a.y * tt.y);
       }
     }
     q[0][c][rl] = us2; q[1][c][rl] = up2; q[2][c][rl] = nu; q[3][c][rl] = fl; q[4][c][rl] = ax; q[5][c][rl] = sh;

@@ -306,3 +306,30 @@ def test_batched_nutop_gradient_ensemble(pz):
     print("batched NuTop FD rel errors (eps 1e-6, 1e-5):", errs)
     for i in check:
         assert min(errs[i]) <= GRAD_TOL, (i, errs[i])
+
+
+@pytest.mark.parametrize("variant", [dict(), dict(corio_term="IMPLICIT"), dict(l_ek_pump=False, ra=3e5)])
+def test_direct_solve_adjoint(pz, variant):
+    """The adjoint of pizza's default direct solve (update_om_coll_smat: the
+    coupled vorticity-streamfunction system, implicit Ekman pumping, and
+    implicit Coriolis with corio_term='IMPLICIT'), CNAB2, with a dt change in
+    the middle: J against the oracle (1e-10), the temperature gradient
+    against FD along 3 directions and dJ/dRa against FD (1e-6)."""
+    spec = dict(SMALL, matrix_solve="DIRECT", **variant)
+    t0 = seeded(spec, 3, 1e-2)
+    ens = pz.Ensemble(gpu_config(spec))
+    J, dt = fwd(ens, t0, 12, 7, SCHED, ck=4)
+    assert np.array_equal(dt, SCHED)
+    Jo = oracle_objective(spec, t0, SCHED, 7)
+    assert abs(J - Jo) <= 1e-10 * abs(Jo), (J, Jo)
+    g, dra = ens.adjoint_backward()
+    fd_check(ens, t0, g[0], 12, 7, SCHED, n_dir=3, seed=11)
+    ra = spec["ra"]
+    h = 1e-6 * ra
+    ens.set_ra(0, ra + h)
+    jp, _ = fwd(ens, t0, 12, 7, SCHED)
+    ens.set_ra(0, ra - h)
+    jm, _ = fwd(ens, t0, 12, 7, SCHED)
+    ens.set_ra(0, ra)
+    fd = (jp - jm) / (2 * h)
+    assert abs(fd - dra[0]) <= GRAD_TOL * abs(fd), (fd, dra[0])

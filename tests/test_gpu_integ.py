@@ -149,19 +149,19 @@ def test_integ_influence_matrix(pz, variant):
     dict(n_r_max=97, n_cheb_max=97, m_max=32, ek=1e-5, ra=3e7, dtMax=2e-6, time_scheme="SBDF3", l_ek_pump=True),
 ])
 def test_integ_banded_matches_dense(pz, variant):
-    """The bordered banded factors (pz_integ_banded(1), the default) and the
-    dense per-m inverses (pz_integ_banded(0)) solve the same systems: the two
-    handles agree to 1e-11 after 25 steps, and the banded one matches the
-    oracle at 1e-10."""
+    """The bordered banded factors (pz_integ_banded(1)) and the dense per-m
+    inverses (pz_integ_banded(0), the default) solve the same systems: the
+    two handles agree to 1e-11 after 25 steps, and the banded one matches
+    the oracle at 1e-10."""
     spec = dict(CI, **variant)
     temp0 = seeded(spec, 5, 1e-2 if spec["n_r_max"] < 97 else 1e-4)
-    prev = pz.integ_banded(False)
+    assert pz.integ_banded() is False
+    dense = pz.Ensemble(gpu_config(spec))
+    prev = pz.integ_banded(True)
     try:
-        dense = pz.Ensemble(gpu_config(spec))
+        band = pz.Ensemble(gpu_config(spec))
     finally:
         pz.integ_banded(prev)
-    assert pz.integ_banded() is True
-    band = pz.Ensemble(gpu_config(spec))
     sim = oracle(spec, temp0=temp0)
     for e in (dense, band):
         e.set_state(0, temp=temp0)
