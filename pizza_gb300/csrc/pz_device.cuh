@@ -150,14 +150,15 @@ __device__ __forceinline__ void mv3(const double* __restrict__ A, const double* 
 // phi-FFT: mixed-radix Stockham autosort on nb transforms in shared memory
 // ---------------------------------------------------------------------------
 // One stage of radix R with running product p (product of earlier radices).
-// tw[k] = exp(-2 pi i k / P) in global memory; `backward` selects the
-// conjugate twiddles.  Twiddles of the first stage (p = 1) are all 1.
+// tw[k] = exp(-2 pi i k / P) in global memory, tw[P + k] its conjugate;
+// `backward` selects the conjugate twiddles.  Twiddles of the first stage (p = 1) are all 1.
 __device__ void fft_stage(const double2* __restrict__ x, double2* __restrict__ y, int P, int R, int p,
                           const double2* __restrict__ tw, int nb, bool backward) {
   const int T = P / R;
   const int tstep = P / (p * R);
   const int rstep = P / R;
-  const double sg = backward ? -1.0 : 1.0;
+  // backward transforms read the conjugate table (tw + P): no FP64 sign flips
+  const double2* twd = backward ? tw + P : tw;
   for (int w = threadIdx.x; w < nb * T; w += blockDim.x) {
     const int b = w / T, i = w - b * T;
     const int k = i % p;
@@ -169,13 +170,7 @@ __device__ void fft_stage(const double2* __restrict__ x, double2* __restrict__ y
     for (int q = 1; q < PZ_MAX_RADIX; ++q) {
       if (q < R) {
         const double2 v = xb[i + q * T];
-        if (k == 0) {
-          u[q] = v;
-        } else {
-          double2 t = __ldg(tw + (q * k * tstep) % P);
-          t.y *= sg;
-          u[q] = cmul(v, t);
-        }
+        u[q] = k == 0 ? v : cmul(v, __ldg(twd + (q * k * tstep) % P));
       }
     }
     const int base = (i - k) * R + k;
@@ -194,7 +189,7 @@ __device__ void fft_stage(const double2* __restrict__ x, double2* __restrict__ y
     } else if (R == 3) {
       // W = c - i sg*sn with c = cos(2 pi/3), sn = sin(2 pi/3) from the table
       const double2 w1 = __ldg(tw + rstep);
-      const double c = w1.x, sn = -w1.y * sg;
+      const double c = w1.x, sn = backward ? w1.y : -w1.y;
       const double2 s12 = cadd(u[1], u[2]), d12 = csub(u[1], u[2]);
       const double2 m = make_double2(u[0].x + c * s12.x, u[0].y + c * s12.y);
       const double2 jd = make_double2(sn * d12.y, -sn * d12.x);   // -i sn d
@@ -204,11 +199,7 @@ __device__ void fft_stage(const double2* __restrict__ x, double2* __restrict__ y
     } else {
       for (int s2 = 0; s2 < R; ++s2) {
         double2 acc = u[0];
-        for (int q = 1; q < R; ++q) {
-          double2 t = __ldg(tw + ((s2 * q) % R) * rstep);
-          t.y *= sg;
-          acc = cadd(acc, cmul(u[q], t));
-        }
+        for (int q = 1; q < R; ++q) acc = cadd(acc, cmul(u[q], __ldg(twd + ((s2 * q) % R) * rstep)));
         yb[base + s2 * p] = acc;
       }
     }
@@ -341,6 +332,7 @@ __device__ void rloop_group(const PzInst& I, const View& V, int r0, int gmax, IO
     io.cfl(r, dtr, dth);
   }
   double2* f = fft_run(h, g1, I, tw, nt * G, false);
+  const double hP = 0.5 / (double)P;
   for (int t = threadIdx.x; t < G * M; t += blockDim.x) {
     const int g = t / M, m = t - g * M, r = r0 + g;
     const double or1 = V.rad(RV_OR1)[r];
@@ -350,10 +342,11 @@ __device__ void rloop_group(const PzInst& I, const View& V, int r0, int gmax, IO
     const double2* f2 = f1 + P;
     // split the two real transforms packed in one complex FFT
     const double2 Z = f1[m], Zc = f1[mc], Y = f2[m], Yc = f2[mc];
-    const double2 vsT = make_double2(0.5 * (Z.x + Zc.x) / (double)P, 0.5 * (Z.y - Zc.y) / (double)P);
-    const double2 upT = make_double2(0.5 * (Z.y + Zc.y) / (double)P, -0.5 * (Z.x - Zc.x) / (double)P);
-    const double2 vsOm = make_double2(0.5 * (Y.x + Yc.x) / (double)P, 0.5 * (Y.y - Yc.y) / (double)P);
-    const double2 upOm = make_double2(0.5 * (Y.y + Yc.y) / (double)P, -0.5 * (Y.x - Yc.x) / (double)P);
+    // (the forward transform's 1/P folded with the split's 1/2: one multiply each)
+    const double2 vsT = make_double2(hP * (Z.x + Zc.x), hP * (Z.y - Zc.y));
+    const double2 upT = make_double2(hP * (Z.y + Zc.y), -hP * (Z.x - Zc.x));
+    const double2 vsOm = make_double2(hP * (Y.x + Yc.x), hP * (Y.y - Yc.y));
+    const double2 upOm = make_double2(hP * (Y.y + Yc.y), -hP * (Y.x - Yc.x));
     const double tm = or1 * (double)(m * I.minc);
     io.out(m, r, make_double2(tm * upT.y - tfac * vsT.x, -tm * upT.x - tfac * vsT.y), vsT,
            (m == 0) ? make_double2(-usom[g], 0.0) : make_double2(tm * upOm.y, -tm * upOm.x), vsOm);
@@ -361,8 +354,8 @@ __device__ void rloop_group(const PzInst& I, const View& V, int r0, int gmax, IO
       // dxi/dt = -(i m / r) FFT(up xi), no beta term (radial_loop.f90:372-374)
       const double2* f3 = f2 + P;
       const double2 X = f3[m], Xc = f3[mc];
-      const double2 vsX = make_double2(0.5 * (X.x + Xc.x) / (double)P, 0.5 * (X.y - Xc.y) / (double)P);
-      const double2 upX = make_double2(0.5 * (X.y + Xc.y) / (double)P, -0.5 * (X.x - Xc.x) / (double)P);
+      const double2 vsX = make_double2(hP * (X.x + Xc.x), hP * (X.y - Xc.y));
+      const double2 upX = make_double2(hP * (X.y + Xc.y), -hP * (X.x - Xc.x));
       io.outx(m, r, make_double2(tm * upX.y, -tm * upX.x), vsX);
     }
   }

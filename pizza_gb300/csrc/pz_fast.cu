@@ -77,13 +77,9 @@ __device__ void split_col(const BOp& B, int j, const double* x, int step, int K)
   }
 }
 
-// zero the slices of columns [j0, C)
-__device__ void zero_cols(const BOp& B, int j0) {
-  for (int s = 0; s < PZ_OZ_S; ++s)
-    for (long long q = (long long)j0 * B.sw + threadIdx.x; q < (long long)B.C * B.sw; q += blockDim.x)
-      B.w[(long long)s * B.C * B.sw + q] = 0u;
-  for (int j = j0 + threadIdx.x; j < B.C; j += blockDim.x) B.ce[j] = 0;
-}
+// Columns of B that no split_col wrote this phase (inactive instances, the
+// padding to whole 8-column tiles) hold stale slices: a product column depends
+// on its own B column only, and those outputs are never stored or read.
 
 __device__ __forceinline__ void mma16816(float* c, const uint4& a, uint32_t b0, uint32_t b1) {
   asm("mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
@@ -279,8 +275,6 @@ __global__ void __launch_bounds__(256, 3) k_fast(PzDev d) {
   // ---- explicit terms: D1p of dVsT, then of dVsOm (2 columns per instance
   // each), into s.R and s.R + 2 G N
   for (int f = 0; f < 2; ++f) {
-    zero_cols(s.B, 0);
-    __syncthreads();
     for (int j = warp; j < 2 * ni; j += nw) {
       const int g = j >> 1, part = j & 1;
       if (!s.st[2 * g]) continue;
@@ -351,8 +345,6 @@ __global__ void __launch_bounds__(256, 3) k_fast(PzDev d) {
   __syncthreads();
 
   // ---- temperature: y = U^-1 rhs, z = y / (1 - w TdiffFac lam), [T; dT/dr] = [U; D1p U] z
-  zero_cols(s.B, 0);
-  __syncthreads();
   for (int j = warp; j < 2 * ni; j += nw)
     if (s.st[2 * (j >> 1)]) split_col(s.B, j, s.RT + (long long)j * n, 1, n);
   __syncthreads();
@@ -368,8 +360,6 @@ __global__ void __launch_bounds__(256, 3) k_fast(PzDev d) {
       s.R[(long long)(2 * g + 1) * n + k] *= D;
     }
   }
-  __syncthreads();
-  zero_cols(s.B, 0);
   __syncthreads();
   for (int j = warp; j < 2 * ni; j += nw)
     if (s.st[2 * (j >> 1)]) split_col(s.B, j, s.R + (long long)j * n, 1, n);
@@ -416,8 +406,6 @@ __global__ void __launch_bounds__(256, 3) k_fast(PzDev d) {
 
   // ---- vorticity (m > 0) or u_phi (m = 0): y = U^-1 rhs
   const PzOzOp& wuinv = (mi == 0) ? F.us[it.ucls].uinv : FM.uinv;
-  zero_cols(s.B, 0);
-  __syncthreads();
   for (int j = warp; j < 2 * ni; j += nw)
     if (s.st[2 * (j >> 1)]) split_col(s.B, j, s.RW + (long long)j * n, 1, n);
   __syncthreads();
@@ -481,8 +469,6 @@ __global__ void __launch_bounds__(256, 3) k_fast(PzDev d) {
       }
     }
   }
-  __syncthreads();
-  zero_cols(s.B, 0);
   __syncthreads();
   for (int j = warp; j < 2 * ni; j += nw)
     if (s.st[2 * (j >> 1)]) split_col(s.B, j, s.R + (long long)j * n, 1, n);

@@ -518,7 +518,7 @@ int validate(const pz_config& c, std::string* why) {
     if (dirk_tableau(c.time_scheme, &t) && t.assembly)
       return uns("cheb_method 'integ' has no assembly stage (mloop.f90:162-164 aborts)");
   } else if (c.matrix_solve == PZ_SOLVE_DIRECT && pz_build_smem_bytes(c.n_r_max, true, false) > PZ_SMEM_MAX) {
-    return uns("matrix_solve DIRECT needs n_r_max <= 97 (the coupled operator build is staged in shared memory)");
+    return uns("matrix_solve DIRECT: n_r_max too large for the operator builders");
   }
   if (c.dtMax <= 0.0) return bad("dtMax must be > 0");
   if (c.alpha <= 0.0 || c.alpha > 1.0) return bad("alpha must be in (0, 1]");
@@ -869,7 +869,7 @@ extern "C" int pz_create(const pz_config* cfgs, int n, pz_handle** out) {
         return fail(nullptr, PZ_E_UNSUPPORTED, "integration-method operator with a half band width above 8");
       }
     }
-    if (!tw_off.count(I.P)) tw_off[I.P] = take(2LL * I.P);
+    if (!tw_off.count(I.P)) tw_off[I.P] = take(4LL * I.P);
     I.o_tw = tw_off[I.P];
     // radial functions (radial.f90:115-282)
     const Basis& B = bases[N];
@@ -999,6 +999,8 @@ extern "C" int pz_create(const pz_config* cfgs, int n, pz_handle** out) {
     } else if (I.flags & PZF_DIRECT) {
       I.o_gsm = take(4 * M * N * N);
       I.o_gom = I.o_gpsi = I.o_aux = 0;   // influence-matrix operators unused
+      I.smat_ws_stride = pz_smat_ws_doubles((int)N);
+      I.o_smat_ws = I.smat_ws_stride ? take(M * I.smat_ws_stride) : 0;
     } else {
       I.o_gom = take(M * N * N);
       I.o_gpsi = take(M * N * N);
@@ -1029,7 +1031,7 @@ extern "C" int pz_create(const pz_config* cfgs, int n, pz_handle** out) {
   {
     long long hi = 0;
     for (auto& kv : basis_off) hi = std::max(hi, kv.second + (long long)BM_COUNT * kv.first * kv.first);
-    for (auto& kv : tw_off) hi = std::max(hi, kv.second + 2LL * kv.first);
+    for (auto& kv : tw_off) hi = std::max(hi, kv.second + 4LL * kv.first);
     for (auto& kv : integ_off) hi = std::max(hi, kv.second + (long long)IM_COUNT * kv.first.first * kv.first.first);
     for (int i = 0; i < n; ++i) hi = std::max(hi, h->inst[i].o_rad + (long long)RV_COUNT * h->inst[i].N);
     for (int i = 0; i < n; ++i)
@@ -1066,6 +1068,8 @@ extern "C" int pz_create(const pz_config* cfgs, int n, pz_handle** out) {
         const long double a = 2.0L * pi * (long double)k / (long double)P;
         dst[2 * k] = (double)cosl(a);
         dst[2 * k + 1] = -(double)sinl(a);
+        dst[2 * P + 2 * k] = dst[2 * k];          // the conjugates, for the backward transforms
+        dst[2 * P + 2 * k + 1] = (double)sinl(a);
       }
     }
     for (int i = 0; i < n; ++i) std::memcpy(img.data() + h->inst[i].o_rad, rad[i].data(), rad[i].size() * sizeof(double));

@@ -154,7 +154,7 @@ struct PzInst {
   double sh_vol_den;        // rInt_R(dxicond^2 height r), denominator of Sh_vol
   long long o_rad;          // RV_COUNT*N
   long long o_basis;        // BM_COUNT*N*N (shared by instances of equal N)
-  long long o_tw;           // 2*P: exp(-2 pi i k/P), shared by equal P
+  long long o_tw;           // 4*P: exp(-2 pi i k/P), then exp(+2 pi i k/P); shared by equal P
   long long o_gt;           // M*N*N   temperature operator per m
   long long o_gx;           // M*N*N   composition operator per m (get_xiMat / integ xi lhs)
   long long o_gom;          // M*N*N   vorticity operator per m (influence)
@@ -180,6 +180,9 @@ struct PzInst {
   // solve: 4 tau rows, complex)
   int bkw_t, bkl_t, bkw_p, bkl_p;
   long long bstr_t, bstr_p;
+  // direct solve with n_r_max above 97: the coupled build's workspace per m
+  // in the pool (o_smat_ws, 0 when it fits shared memory)
+  long long o_smat_ws, smat_ws_stride;
   int rg;                   // radii per k_rloop block
   double rerr_thr;          // rerror_fac * epsilon with l_rerror_fix, else 0
 };
@@ -287,6 +290,7 @@ cudaError_t pz_setup_kernels();
 // dynamic shared memory for G instances per block and grids up to maxN
 cudaError_t pz_launch_fast(const PzDev& d, cudaStream_t s);
 size_t pz_fast_smem_bytes(int G, int maxN);
+long long pz_smat_ws_doubles(int n);
 size_t pz_build_smem_bytes(int n, bool direct, bool integ);   // k_build shared memory for one instance
 size_t pz_rloop_smem_bytes(int P, int M, int G, int nt);     // k_rloop shared memory, G radii per block,
                                                              // nt transforms per radius (2, or 3 with composition)

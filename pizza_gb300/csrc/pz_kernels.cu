@@ -565,11 +565,12 @@ __device__ int gj_invert_c(double2* A, int n, int* piv, double2* colk, double* r
 // Shared memory: S (complex N^2) | E (N^2, padded to an even count) | f1, f2,
 // pivot column (2N each) | reductions | pivots; D^-1 occupies the first N^2
 // doubles before S is formed.
-__device__ int build_smat(double* G, const BuildCtx& B, const View& V, int m, double wlin) {
-  extern __shared__ double shb[];
+// ws: the workspace (build_smat_smem_bytes(n)): shared memory, or for
+// n_r_max above 97 the instance's global-memory workspace (PzInst::o_smat_ws)
+__device__ int build_smat(double* G, const BuildCtx& B, const View& V, int m, double wlin, double* ws) {
   const PzInst& I = *B.I;
   const int n = B.N, n2 = 2 * n;
-  double* X = shb;
+  double* X = ws;
   double2* Sx = reinterpret_cast<double2*>(X);
   double* E = X + 2LL * n * n;
   double* f1 = E + (((long long)n * n + 1) & ~1LL);   // even offset: colk below is read as double2
@@ -766,7 +767,9 @@ __device__ __forceinline__ void build_item(const PzDev& d, const PzItem it) {
   if (I.flags & PZF_DIRECT) {
     // coupled (omega, psi) operator of update_om_coll_smat
     __syncthreads();
-    if (build_smat(d.pool + I.o_gsm + 4LL * mi * n * n, B, V, m, wlin) != 0) flag_status(S, PZ_E_SINGULAR);
+    extern __shared__ double shb[];
+    double* ws = I.o_smat_ws ? d.pool + I.o_smat_ws + (long long)mi * I.smat_ws_stride : shb;
+    if (build_smat(d.pool + I.o_gsm + 4LL * mi * n * n, B, V, m, wlin, ws) != 0) flag_status(S, PZ_E_SINGULAR);
     return;
   }
   // omega (get_omMat: row and column scaling)
@@ -1908,6 +1911,14 @@ __global__ void k_gather_rows(PzDev d, double* out) {
 size_t build_smat_smem_bytes(int n) {
   return (3 * (size_t)n * n + 1 + 6 * (size_t)n + 32 + 16 + (size_t)(n + 1) / 2) * sizeof(double);
 }
+}  // namespace
+// the coupled operator build's workspace in doubles when it does not fit
+// shared memory (0 when it does): it then lives in the instance's pool slice
+long long pz_smat_ws_doubles(int n) {
+  const size_t b = build_smat_smem_bytes(n);
+  return b > PZ_SMEM_MAX ? (long long)((b / sizeof(double) + 1) & ~(size_t)1) : 0;
+}
+namespace {
 size_t build_smem_bytes(int n) {
   long long off = (long long)n * n + 3LL * n + 32 + 16 + (n + 1) / 2;
   off = (off + 1) & ~1LL;
@@ -1958,6 +1969,7 @@ size_t pz_build_smem_bytes(int n, bool direct, bool integ) {
   }
   if (!direct) return a;
   const size_t b = build_smat_smem_bytes(n);
+  if (b > PZ_SMEM_MAX) return a;     // the coupled build runs in global memory (pz_smat_ws_doubles)
   return a > b ? a : b;
 }
 

@@ -84,6 +84,17 @@ def test_direct_larger_grids(pz):
         check_fields(sim, out[-1][2], 1e-9, f"N={spec['n_r_max']}")
 
 
+def test_direct_beyond_shared_memory(pz):
+    """n_r_max = 113 and 128: the coupled operator's build (3 N^2 doubles) no
+    longer fits shared memory and runs on a global-memory workspace.  The
+    coupled system's conditioning grows like N^4, so the field bar follows the
+    per-solve agreement (1e-9 at N = 97) up to 1e-8."""
+    for spec in (dict(C0D, n_r_max=113, n_cheb_max=113, m_max=42, ek=1e-4, ra=1e6, dtMax=1e-5),
+                 dict(C0D, n_r_max=128, n_cheb_max=128, m_max=32, ek=1e-4, ra=1e6, dtMax=1e-5)):
+        sim, ens, out = run_pair(pz, spec, 8, seed=9)
+        check_fields(sim, out[-1][2], 1e-8, f"N={spec['n_r_max']}")
+
+
 def test_mixed_direct_and_influence_batch(pz):
     specs = [C0D, dict(C0D, matrix_solve="INFLUENCE"), dict(C0D, n_r_max=49, m_max=64, ek=1e-4, ra=1e6, dtMax=2e-5)]
     temps = [seeded(s, 20 + i) for i, s in enumerate(specs)]
