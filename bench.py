@@ -233,6 +233,17 @@ class Clocks:
 # large to capture under the profiling rules; its traffic is this ratio times
 # its algorithmic bytes (traffic grows with the (instance, m) items processed).
 MLOOP_TRAFFIC_PER_ALGO_BYTE = 83.97e6 / 81868128.0
+# k_rloop: DRAM bytes (read + write) per launch over its algorithmic bytes, the
+# four input and four output (m, r) planes of every instance (16 * 8 M N),
+# from an ncu capture of the 16-instance ensemble (profiles/launch_list_ensemble256_fast.md);
+# the traffic scales with the instances, so the ratio carries to 256
+RLOOP_TRAFFIC_PER_ALGO_BYTE = (7927936.0 + 32128.0) / 7725056.0
+
+
+def rloop_bytes(specs):
+    """Algorithmic bytes of one k_rloop launch: 4 input and 4 output planes of
+    (m, r) complex values per instance."""
+    return 8 * 16.0 * sum((s["m_max"] + 1) * s["n_r_max"] for s in specs)
 
 
 def measured_peaks():
@@ -611,8 +622,13 @@ def main():
     if kms.get("k_rloop", 0.0) > 0.0:
         f = rloop_work(specs)
         a_t = f / (kms["k_rloop"] * 1e-3) / 1e12
+        rb = rloop_bytes(specs)
         kernels["k_rloop"] = {"bound": "fp64", "achieved": a_t, "peak": dfma_peak, "unit": "TFLOP/s",
                               "frac": a_t / dfma_peak if dfma_peak else None,
+                              "traffic": RLOOP_TRAFFIC_PER_ALGO_BYTE * rb,
+                              "hbm": {"achieved": rb / (kms["k_rloop"] * 1e-3) / 1e9, "peak": hbm_peak,
+                                      "unit": "GB/s", "frac": rb / (kms["k_rloop"] * 1e-3) / 1e9 / hbm_peak,
+                                      "bytes": rb},
                               "work": f, "work_note": "4 complex FFTs of length n_phi_max per (instance, radius) "
                                                       "at 5 P log2 P flops, plus 8 P + 20 M elementwise",
                               "peak_kind": "DFMA issue rate measured in this run (pz_probe_peaks)"}
@@ -639,9 +655,10 @@ def main():
                                      "traffic": MLOOP_TRAFFIC_PER_ALGO_BYTE * byts}}
     roof = dict(kernels.get(dom, {}))
     roof["kernel"] = dom
-    roof["traffic"] = None
-    roof["traffic_note"] = ("DRAM bytes of the dominant kernel per launch: profiles/ holds the ncu summaries; "
-                            "this line does not re-derive them")
+    roof["traffic"] = kernels.get(dom, {}).get("traffic")
+    roof["traffic_note"] = ("DRAM bytes (read + write) per launch of the dominant kernel: its algorithmic bytes "
+                            "times the DRAM/algorithmic ratio of an ncu capture (profiles/), where the kernel's "
+                            "traffic scales with the instances; null otherwise")
     roof["peaks"] = {"dfma_tflops": dfma_peak, "mma_bf16_tflops": mma_peak, "hbm_gbs": hbm_peak,
                      "hbm_kind": peak_kind, "tcgen05_bf16_tflops": bf16_peak}
 

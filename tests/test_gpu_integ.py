@@ -150,9 +150,11 @@ def test_integ_influence_matrix(pz, variant):
 ])
 def test_integ_banded_matches_dense(pz, variant):
     """The bordered banded factors (pz_integ_banded(1)) and the dense per-m
-    inverses (pz_integ_banded(0), the default) solve the same systems: the
-    two handles agree to 1e-11 after 25 steps, and the banded one matches
-    the oracle at 1e-10."""
+    inverses (pz_integ_banded(0), the default) solve the same systems: after
+    25 steps both match the oracle at 1e-10 (1e-9 at n_r_max = 97 with the
+    rotating direct solve, whose tau-bordered system has rows ~n^6 apart; the
+    two solvers differ there by ~1e-9, the banded LU being the more accurate
+    of the two against a 40-digit solve)."""
     spec = dict(CI, **variant)
     temp0 = seeded(spec, 5, 1e-2 if spec["n_r_max"] < 97 else 1e-4)
     assert pz.integ_banded() is False
@@ -170,9 +172,9 @@ def test_integ_banded_matches_dense(pz, variant):
     dense.step(25)
     band.step(25)
     gd, gb = dense.get_state(0), band.get_state(0)
-    for f in ("temp", "us", "up", "om"):
-        assert rel_err(gb[f], gd[f]) < 1e-11, (f, rel_err(gb[f], gd[f]))
-    check_fields(sim, gb, 1e-10, f"banded {variant}")
+    tol = 1e-9 if spec["n_r_max"] >= 97 and spec.get("matrix_solve", "DIRECT") == "DIRECT" else 1e-10
+    check_fields(sim, gb, tol, f"banded {variant}")
+    check_fields(sim, gd, tol, f"dense {variant}")
     dense.close()
     band.close()
 
@@ -224,13 +226,16 @@ def test_integ_rejections(pz):
 
 C1 = dict(n_r_max=97, n_cheb_max=97, m_max=128, ek=1e-5, ra=3e7, pr=1.0, radratio=0.35,
           time_scheme="SBDF3", dtMax=2e-6, cheb_method="INTEG", matrix_solve="DIRECT", l_ek_pump=True)
-C1_CK = (20, 500, 1000, 2000)
+C1_CK = (20, 500, 1000, 1250)
 
 
 def _c1_oracle(pert):
     """Oracle run of the full-size integ workload to C1_CK; with `pert`,
-    fp64_noise of that level after every step (the size of the rounding
-    differences of another FP64 implementation)."""
+    fp64_noise of that level on the temperature after every step (the size of
+    the rounding differences of another FP64 implementation).  The unperturbed
+    run then goes on to its breakdown: its Courant step collapses below dtMin a
+    few steps after 1250 (at step 1272 on x86 with NumPy/SciPy), and it returns
+    that step and the dt of every step after 1250."""
     import sys
     sys.path.insert(0, os.path.dirname(HERE))
     from tests.helpers import fp64_noise, oracle as make, seeded as seed_of
@@ -244,19 +249,33 @@ def _c1_oracle(pert):
                 fp64_noise(sim, rng, pert, fields=("temp",))
         done = k
         out[k] = {f: getattr(sim, f).copy() for f in ("us", "up", "om", "temp", "psi")}
+    if not pert:
+        dts, k = [], done
+        try:
+            while k < 2000:
+                sim.advance()
+                k += 1
+                dts.append(sim.ts.dt[0])
+        except FloatingPointError:
+            out["fail"] = k + 1
+        out["dt"] = np.array(dts)
     return out
 
 
 def test_c1_integ_sbdf3_full_size(pz):
     """The integ workload at full size (n_r_max=97, n_phi_max=384, E=1e-5,
-    Ra=3e7, SBDF3, dt=2e-6, seeded amplitude 1e-4) over its 2000 steps
-    against the oracle at steps 20, 500, 1000 and 2000.  The bar is 1e-10
-    relative while the oracle's own spread (its run with fp64_noise of 1e-13
-    on the temperature after every step) stays below 1e-12, and 100x that
-    spread beyond.  The tau rows, which hold in Chebyshev space, are checked
-    on the final GPU state: for T and psi (m > 0) c_0/2 + sum_n c_n (+-1)^n = 0
-    at both walls (the physical wall value differs from it by the DCT-I's
-    half weight on c_{N-1})."""
+    Ra=3e7, SBDF3, dt=2e-6, seeded amplitude 1e-4) over its 2000 steps.  The
+    reference's algorithm does not finish them: the flow grows exponentially
+    (max |u_s| 0.65 at step 100, 121 at 1200) and the Courant step collapses
+    below dtMin soon after step 1250.  So the GPU is held to the oracle at steps
+    20, 500, 1000 and 1250 (1e-10 relative while the oracle's own spread, its
+    run with fp64_noise of 1e-13 on the temperature after every step, stays
+    below 1e-12, and 100x that spread beyond), then it must break down the same
+    way: the same dt sequence through the collapse (1e-6 relative) and the
+    dt < dtMin error within two steps of the oracle's.  The tau rows, which
+    hold in Chebyshev space, are checked on the step-1250 GPU state: for T and
+    psi (m > 0) c_0/2 + sum_n c_n (+-1)^n = 0 at both walls (the physical wall
+    value differs from it by the DCT-I's half weight on c_{N-1})."""
     import multiprocessing as mp
     with mp.get_context("spawn").Pool(2) as pool:
         ref, spread = pool.map(_c1_oracle, (0.0, 1e-13))
@@ -273,12 +292,6 @@ def test_c1_integ_sbdf3_full_size(pz):
         report.append((k, errs, fl))
         for f, e in errs.items():
             assert e < tol, f"c1 step {k} {f}: rel err {e:.3e} (oracle spread {fl:.2e})"
-    out_dir = os.path.join(os.path.dirname(HERE), "gpurun_out")
-    if os.path.isdir(out_dir):
-        with open(os.path.join(out_dir, "c1_integ_parity.txt"), "w") as f:
-            for k, errs, fl in report:
-                f.write(f"step {k}: " + " ".join(f"{a} {e:.2e}" for a, e in errs.items())
-                        + f" oracle-spread {fl:.2e}\n")
     g = ens.get_state(0)
     N = C1["n_r_max"]
     sg = np.where(np.arange(N) % 2 == 0, 1.0, -1.0)
@@ -289,3 +302,23 @@ def test_c1_integ_sbdf3_full_size(pz):
         bot = 0.5 * c[:, 0] + (c[:, 1:] * sg[1:]).sum(axis=1)
         scale = np.max(np.abs(c))
         assert np.max(np.abs(top)) < 1e-11 * scale and np.max(np.abs(bot)) < 1e-11 * scale, f
+    # the breakdown
+    assert "fail" in ref, "the oracle finished 2000 steps"
+    dts, fail = [], None
+    for k in range(done + 1, 2001):
+        try:
+            ens.step(1)
+        except pz.PizzaError:
+            fail = k
+            break
+        dts.append(ens.get_step_state(0)[1][0])
+    out_dir = os.path.join(os.path.dirname(HERE), "gpurun_out")
+    if os.path.isdir(out_dir):
+        with open(os.path.join(out_dir, "c1_integ_parity.txt"), "w") as f:
+            for k, errs, fl in report:
+                f.write(f"step {k}: " + " ".join(f"{a} {e:.2e}" for a, e in errs.items())
+                        + f" oracle-spread {fl:.2e}\n")
+            f.write(f"breakdown: oracle at step {ref['fail']}, GPU at step {fail}\n")
+    assert fail is not None and abs(fail - ref["fail"]) <= 2, (fail, ref["fail"])
+    n = min(len(dts), len(ref["dt"])) - 2
+    np.testing.assert_allclose(np.array(dts[:n]), ref["dt"][:n], rtol=1e-6)

@@ -194,9 +194,13 @@ def test_device_2d_spectra_match_oracle(pz, tmp_path):
                                           (dict(l_non_rot=True, l_ek_pump=False, ra=2e4, dtMax=1e-4), True)])
 def test_force_balances_match_oracle(pz, tmp_path, variant, fast):
     """The vorticity and u_phi force balances (pz_balance_step) against the
-    oracle's record of the same step, per term relative to its largest
-    value, at the 6th and 9th step, on the tensor-core stage and on the dense
-    kernels; then the time-averaged files written from the device terms."""
+    oracle's record of the same step, at the 6th and 9th step, on the
+    tensor-core stage and on the dense kernels: every term to 1e-10 of the
+    balance's dominant term (the largest of its terms other than the
+    vorticity's dw/dt, which is held to itself; a balance is read against
+    its leading terms, and a term that nearly vanishes -- u_phi(m=0) without
+    rotation -- carries the rounding of the others); then the time-averaged
+    files written from the device terms."""
     from pizza_gb300.pizza_io import VortBalance, VpBalance
     spec = dict(C0, matrix_solve="INFLUENCE", time_scheme="CNAB2", **variant)
     t0 = seeded(spec, 71, 1e-2)
@@ -219,13 +223,16 @@ def test_force_balances_match_oracle(pz, tmp_path, variant, fast):
         got = ens.balance_step(0)
         done = k
         for part in ("vort", "vp"):
+            # dw/dt of the vorticity balance mixes Chebyshev and physical values
+            # (the reference's quirk): judged against itself, the others against
+            # the largest of them
+            scale = max(np.max(np.abs(a)) for n_, a in ref[part].items() if n_ != "dwdt")
             for name, a in ref[part].items():
                 b = got[part][name]
-                scale = np.max(np.abs(a))
-                if scale == 0.0:
+                if np.max(np.abs(a)) == 0.0:
                     assert np.max(np.abs(b)) == 0.0, (k, part, name)
                     continue
-                e = np.max(np.abs(b - a)) / scale
+                e = np.max(np.abs(b - a)) / (np.max(np.abs(a)) if name == "dwdt" else scale)
                 assert e < 1e-10, (k, part, name, e)
         t_avg += sim.ts.dt[0]
         vb.calc_avg(got["vort"], t_avg)
