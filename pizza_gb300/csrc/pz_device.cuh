@@ -151,33 +151,45 @@ __device__ __forceinline__ void mv3(const double* __restrict__ A, const double* 
 // ---------------------------------------------------------------------------
 // One stage of radix R with running product p (product of earlier radices).
 // tw[k] = exp(-2 pi i k / P) in global memory, tw[P + k] its conjugate;
-// `backward` selects the conjugate twiddles.  Twiddles of the first stage (p = 1) are all 1.
-__device__ void fft_stage(const double2* __restrict__ x, double2* __restrict__ y, int P, int R, int p,
-                          const double2* __restrict__ tw, int nb, bool backward) {
+// `backward` selects the conjugate twiddles.  Twiddles of the first stage (p = 1)
+// are all 1.  RC = R for the radices with a specialised butterfly (2, 3, 4):
+// the butterfly values stay in registers; RC = 0 is the generic radix.
+template <int RC>
+__device__ void fft_stage_r(const double2* __restrict__ x, double2* __restrict__ y, int P, int Rrt, int p,
+                            const double2* __restrict__ tw, int nb, bool backward) {
+  constexpr int RU = RC ? RC : PZ_MAX_RADIX;
+  const int R = RC ? RC : Rrt;
   const int T = P / R;
   const int tstep = P / (p * R);
   const int rstep = P / R;
   // backward transforms read the conjugate table (tw + P): no FP64 sign flips
   const double2* twd = backward ? tw + P : tw;
+  // w / T and i / p by a float reciprocal and one correction step (w < 2^20:
+  // the float quotient is within one of the true one)
+  const float rT = 1.0f / (float)T, rp = 1.0f / (float)p;
   for (int w = threadIdx.x; w < nb * T; w += blockDim.x) {
-    const int b = w / T, i = w - b * T;
-    const int k = i % p;
+    int b = (int)((float)w * rT);
+    b += (w - b * T >= T) - (w < b * T);
+    const int i = w - b * T;
+    int ip = (int)((float)i * rp);
+    ip += (i - ip * p >= p) - (i < ip * p);
+    const int k = i - ip * p;
     const double2* xb = x + b * P;
     double2* yb = y + b * P;
-    double2 u[PZ_MAX_RADIX];
+    double2 u[RU];
     u[0] = xb[i];
 #pragma unroll
-    for (int q = 1; q < PZ_MAX_RADIX; ++q) {
+    for (int q = 1; q < RU; ++q) {
       if (q < R) {
         const double2 v = xb[i + q * T];
-        u[q] = k == 0 ? v : cmul(v, __ldg(twd + (q * k * tstep) % P));
+        u[q] = k == 0 ? v : cmul(v, __ldg(twd + q * k * tstep));   // q k tstep < R p P / (p R) = P
       }
     }
     const int base = (i - k) * R + k;
-    if (R == 2) {
+    if constexpr (RC == 2) {
       yb[base] = cadd(u[0], u[1]);
       yb[base + p] = csub(u[0], u[1]);
-    } else if (R == 4) {
+    } else if constexpr (RC == 4) {
       const double2 s02 = cadd(u[0], u[2]), d02 = csub(u[0], u[2]);
       const double2 s13 = cadd(u[1], u[3]), d13 = csub(u[1], u[3]);
       // forward: W = -i ; backward: W = +i
@@ -186,7 +198,7 @@ __device__ void fft_stage(const double2* __restrict__ x, double2* __restrict__ y
       yb[base + p] = cadd(d02, jd13);
       yb[base + 2 * p] = csub(s02, s13);
       yb[base + 3 * p] = csub(d02, jd13);
-    } else if (R == 3) {
+    } else if constexpr (RC == 3) {
       // W = c - i sg*sn with c = cos(2 pi/3), sn = sin(2 pi/3) from the table
       const double2 w1 = __ldg(tw + rstep);
       const double c = w1.x, sn = backward ? w1.y : -w1.y;
@@ -204,6 +216,13 @@ __device__ void fft_stage(const double2* __restrict__ x, double2* __restrict__ y
       }
     }
   }
+}
+__device__ void fft_stage(const double2* __restrict__ x, double2* __restrict__ y, int P, int R, int p,
+                          const double2* __restrict__ tw, int nb, bool backward) {
+  if (R == 4) fft_stage_r<4>(x, y, P, R, p, tw, nb, backward);
+  else if (R == 2) fft_stage_r<2>(x, y, P, R, p, tw, nb, backward);
+  else if (R == 3) fft_stage_r<3>(x, y, P, R, p, tw, nb, backward);
+  else fft_stage_r<0>(x, y, P, R, p, tw, nb, backward);
 }
 
 // Full transform; returns the buffer holding the result (a or b).
@@ -298,8 +317,11 @@ __device__ void rloop_group(const PzInst& I, const View& V, int r0, int gmax, IO
   // multiple of 32 the 32 points of a warp lie on one radius and every lane
   // runs every pass: one atomic per warp after a warp maximum.
   const bool warp_red = (P & 31) == 0 && (blockDim.x & 31) == 0;
+  const float rP = 1.0f / (float)P;
   for (int t = threadIdx.x; t < G * P; t += blockDim.x) {
-    const int g = t / P, j = t - g * P;
+    int g = (int)((float)t * rP);
+    g += (t - g * P >= P) - (t < g * P);     // t / P (t < 2^20)
+    const int j = t - g * P;
     const double rr = V.rad(RV_R)[r0 + g];
     const double2 z1 = g1[(nt * g) * P + j], z2 = g1[(nt * g + 1) * P + j];
     const double usg = z1.x, upg = z1.y, omg = z2.x, Tg = z2.y;
@@ -333,11 +355,14 @@ __device__ void rloop_group(const PzInst& I, const View& V, int r0, int gmax, IO
   }
   double2* f = fft_run(h, g1, I, tw, nt * G, false);
   const double hP = 0.5 / (double)P;
+  const float rM = 1.0f / (float)M;
   for (int t = threadIdx.x; t < G * M; t += blockDim.x) {
-    const int g = t / M, m = t - g * M, r = r0 + g;
+    int g = (int)((float)t * rM);
+    g += (t - g * M >= M) - (t < g * M);     // t / M (t < 2^20)
+    const int m = t - g * M, r = r0 + g;
     const double or1 = V.rad(RV_OR1)[r];
     const double tfac = (1.0 - I.tadvz) * V.rad(RV_BETA)[r] * or1;
-    const int mc = (P - m) % P;
+    const int mc = m == 0 ? 0 : P - m;
     const double2* f1 = f + (nt * g) * P;
     const double2* f2 = f1 + P;
     // split the two real transforms packed in one complex FFT
