@@ -314,11 +314,12 @@ int pz_explicit_terms_noalloc(pz_handle* h, int inst, const double* us, const do
  *       (us2_3D + up2_3D + uz2_3D)(k)          (e_kin_3D, outputs.f90:553-570)
  * and the gradient is taken with respect to the initial temperature
  * perturbation (the temp argument of pz_set_state) and Ra, for a fixed
- * time-step sequence.  The collocation step with the influence-matrix solve
- * is covered, with CNAB2 or a DIRK scheme (one scheme for all instances), and
- * with pizza's default direct solve (update_om_coll_smat, the coupled
+ * time-step sequence.  The collocation step is covered with the
+ * influence-matrix solve and any multistep or DIRK scheme, and with pizza's
+ * default direct solve (update_om_coll_smat, the coupled
  * vorticity-streamfunction system with implicit Ekman pumping and, with
- * corio_term='IMPLICIT', implicit Coriolis) with CNAB2.
+ * corio_term='IMPLICIT', implicit Coriolis) and any multistep scheme; one
+ * scheme for all instances of the handle.
  *
  * The objective is selected per sweep: PZ_OBJ_EKIN3D (above) or
  * PZ_OBJ_NUTOP, the mean of NuTop = 1 + dT/dr(m=0, r_cmb)/dtcond(r_cmb).

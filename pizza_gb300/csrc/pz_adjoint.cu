@@ -1,6 +1,6 @@
-// Discrete adjoint of the CNAB2 collocation step (influence-matrix solve, or
-// the direct solve of update_om_coll_smat, whose coupled solve transposes to
-// G^H and whose implicit Ekman pumping and Coriolis terms join L^T):
+// Discrete adjoint of the multistep collocation step (influence-matrix solve,
+// or the direct solve of update_om_coll_smat, whose coupled solve transposes
+// to G^H and whose implicit Ekman pumping and Coriolis terms join L^T):
 // gradient of a time-averaged 3-D kinetic energy or outer-boundary Nusselt
 // number with respect to the initial temperature perturbation and to BuoFac
 // (hence Ra).
@@ -8,12 +8,14 @@
 // The step of k_rloop/k_cfl/k_build/k_mloop is, per instance, a map of the
 // state S_n = (Tc, oc, pc, uc) -- the Chebyshev coefficients of temperature,
 // vorticity and streamfunction (m /= 0) and of u_phi (m = 0) -- plus the
-// explicit terms E_{n-1} of the previous step:
+// history of the earlier steps (old_{n-k}, impl_{n-k}, E_{n-k}, k >= 1, as the
+// scheme's nold, nimp, nexp slots hold them; CNAB2: E_{n-1} only):
 //   fields f_n   = L(S_n)                 T, us, up, om, implicit terms iT, iP
 //                                         (get_temp_rhs_imp_coll, get_psi_rhs_imp_coll_dmat)
 //   nonlinear    = NL(f_n)                radial_loop.f90:231-394
 //   E_n          = FIN(f_n, NL)           finish_exp_temp_coll / finish_exp_psi_coll_dmat
-//   S_{n+1}      = SOLVE(f_n, E_n, E_{n-1})   update_temp_co, update_om_coll_dmat
+//   S_{n+1}      = SOLVE(rhs_n),  rhs_n = sum_k wimp[k] old_{n-k} + sum_k wimp_lin[k+1]
+//                  impl_{n-k} + sum_k wexp[k] E_{n-k}   update_temp_co, update_om_coll_dmat
 // with SOLVE linear in its inputs for a fixed time-step sequence.  The backward
 // step is the exact transpose of each piece, in reverse order:
 //   k_adj_solve  (instance, m)  SOLVE^T and FIN^T (local part): influence
@@ -54,7 +56,13 @@ namespace {
 // planes of M*N complex per instance in the adjoint workspace
 enum {
   AP_TCB = 0, AP_OCB, AP_PCB, AP_UCB,   // adjoint of the state (row 0 of AP_UCB: u_phi, m = 0)
-  AP_CT, AP_CP,                          // adjoint of E_n carried from step n+1 (we1 * rhs adjoint)
+  AP_CT, AP_CP,                          // adjoint of E_n carried from the later steps (sum over k >= 1
+                                         // of wexp_{n+k}[k] times their rhs adjoints)
+  AP_C2T, AP_C2P, AP_C3T, AP_C3P,        // the same for E_{n-1}, E_{n-2} (multistep schemes with nexp > 2)
+  AP_O1T, AP_O1P, AP_O2T, AP_O2P, AP_O3T, AP_O3P,   // adjoint of old_{n-1..n-3} from the later steps
+  AP_OTB, AP_OPB,                        // adjoint of old_n (temperature; vorticity or u_phi), complete
+  AP_I1T, AP_I1P, AP_I2T, AP_I2P,        // adjoint of impl_{n-1..n-2} from the later steps (nimp > 1)
+  AP_ITB, AP_IPB,                        // adjoint of impl_n, complete
   AP_RTB, AP_RPB,                        // adjoint of the solve right-hand sides of step n
   AP_ETB, AP_EPB,                        // adjoint of E_n (temperature, vorticity)
   AP_VTB, AP_VOB,                        // adjoint of dVsT, dVsOm
@@ -371,16 +379,59 @@ __global__ void __launch_bounds__(256, 4) k_adj_solve(PzAdjDev a, int n, int slo
                                                          : a.d.pool + I.o_gt + (long long)mi * N * N;
   mvT_lanes(GT, N, Tc, rT);
   __syncthreads();
+  // IMEX weights (multistep_schemes.f90:308-316): rhs_n = sum_k wimp_n[k] old_{n-k}
+  // + wimp_lin_n[1] impl_n + sum_k wexp_n[k] E_{n-k}.  The adjoints of old_n and
+  // E_n collect wimp_{n+k}[k] and wexp_{n+k}[k] times the rhs adjoint of every
+  // later step n+k: shift registers of carry planes, one per k >= 1.
+  double wi[4], we[4], wl[3];
+  for (int k = 0; k < 4; ++k) {
+    wi[k] = k < I.nold ? S.wimp[k] : 0.0;
+    we[k] = k < I.nexp ? S.wexp[k] : 0.0;
+    if (k < 3) wl[k] = k < I.nimp ? S.wimp_lin[k + 1] : 0.0;
+  }
+  double2* i1T = A.plane(AP_I1T, mi);
+  double2* i1P = A.plane(AP_I1P, mi);
+  double2* i2T = A.plane(AP_I2T, mi);
+  double2* i2P = A.plane(AP_I2P, mi);
+  (void)we0; (void)we1;
   double2* cT = A.plane(AP_CT, mi);
   double2* cP = A.plane(AP_CP, mi);
+  double2* c2T = A.plane(AP_C2T, mi);
+  double2* c2P = A.plane(AP_C2P, mi);
+  double2* c3T = A.plane(AP_C3T, mi);
+  double2* c3P = A.plane(AP_C3P, mi);
+  double2* o1T = A.plane(AP_O1T, mi);
+  double2* o1P = A.plane(AP_O1P, mi);
+  double2* o2T = A.plane(AP_O2T, mi);
+  double2* o2P = A.plane(AP_O2P, mi);
+  double2* o3T = A.plane(AP_O3T, mi);
+  double2* o3P = A.plane(AP_O3P, mi);
   for (int i = threadIdx.x; i < N; i += blockDim.x) {
     const double2 rt = (i == 0 || i == N - 1) ? cz() : rT[i];
     const double2 rp = rP[i];
     rT[i] = rt;
-    const double2 et = caxpy(we0, rt, cT[i]), ep = caxpy(we0, rp, cP[i]);
+    const double2 et = caxpy(we[0], rt, cT[i]), ep = caxpy(we[0], rp, cP[i]);
     eT[i] = et; eP[i] = ep;
-    cT[i] = cscale(we1, rt);
-    cP[i] = cscale(we1, rp);
+    cT[i] = caxpy(we[1], rt, c2T[i]);
+    cP[i] = caxpy(we[1], rp, c2P[i]);
+    c2T[i] = caxpy(we[2], rt, c3T[i]);
+    c2P[i] = caxpy(we[2], rp, c3P[i]);
+    c3T[i] = cscale(we[3], rt);
+    c3P[i] = cscale(we[3], rp);
+    A.plane(AP_OTB, mi)[i] = caxpy(wi[0], rt, o1T[i]);
+    A.plane(AP_OPB, mi)[i] = caxpy(wi[0], rp, o1P[i]);
+    o1T[i] = caxpy(wi[1], rt, o2T[i]);
+    o1P[i] = caxpy(wi[1], rp, o2P[i]);
+    o2T[i] = caxpy(wi[2], rt, o3T[i]);
+    o2P[i] = caxpy(wi[2], rp, o3P[i]);
+    o3T[i] = cscale(wi[3], rt);
+    o3P[i] = cscale(wi[3], rp);
+    A.plane(AP_ITB, mi)[i] = caxpy(wl[0], rt, i1T[i]);
+    A.plane(AP_IPB, mi)[i] = caxpy(wl[0], rp, i1P[i]);
+    i1T[i] = caxpy(wl[1], rt, i2T[i]);
+    i1P[i] = caxpy(wl[1], rp, i2P[i]);
+    i2T[i] = cscale(wl[2], rt);
+    i2P[i] = cscale(wl[2], rp);
     A.plane(AP_RTB, mi)[i] = rt;
     A.plane(AP_RPB, mi)[i] = rp;
     A.plane(AP_ETB, mi)[i] = et;
@@ -407,7 +458,7 @@ __global__ void __launch_bounds__(256, 4) k_adj_solve(PzAdjDev a, int n, int slo
       const double c = rgrav[i] * or1[i];
       if (buo_imp) {
         acc += cdotr(rP[i], cscale(-wl0 * c, cim(dm, Tn1[i])));
-        acc += wl1 * cdotr(rP[i], cscale(-c, cim(dm, Tn[i])));
+        acc += cdotr(A.plane(AP_IPB, mi)[i], cscale(-c, cim(dm, Tn[i])));   // impl_n, all later steps
       } else {
         acc += cdotr(eP[i], cscale(-c, cim(dm, Tn[i])));
       }
@@ -602,8 +653,15 @@ __global__ void __launch_bounds__(256, 3) k_adj_lin(PzAdjDev a, int n, int slot,
       aus = A.plane(AP_AUS, mi)[i]; aup = A.plane(AP_AUP, mi)[i];
       aom = A.plane(AP_AOM, mi)[i]; aT = A.plane(AP_AT, mi)[i];
     }
-    double2 Tb = caxpy(w0, rT, aT);
-    const double2 iTb = cscale(wl1, rT), oldPb = cscale(w0, rP), iPb = cscale(wl1, rP);
+    // adjoints of old_n and impl_n, collected over every later step that reads them
+    double2 Tb = aT, oldPb = cz(), iTb = cz(), iPb = cz();
+    if (!terminal) {
+      Tb = cadd(Tb, A.plane(AP_OTB, mi)[i]);
+      oldPb = A.plane(AP_OPB, mi)[i];
+      iTb = A.plane(AP_ITB, mi)[i];
+      iPb = A.plane(AP_IPB, mi)[i];
+    }
+    (void)rT; (void)w0; (void)wl1;
     // FIN^T (update_temp_coll.f90:152-176, update_psi_coll_dmat.f90:468-552)
     const double gT = dtcond[i] - I.tadvz * beta[i] * tcond[i];
     double2 usb = caxpy(-gT, eT, aus), upb = aup, omb = aom;
@@ -1414,11 +1472,11 @@ extern "C" int pz_adjoint_forward(pz_handle* h, int objective, int n_steps, int 
   if (n_window < 0 || n_window > n_steps) return pz_fail(h, PZ_E_ARG, "pz_adjoint_forward: n_window outside [0, n_steps]");
   for (int i = 0; i < h->n_inst; ++i) {
     const PzInst& I = h->inst[i];
-    if ((I.scheme != PZ_CNAB2 && !I.dirk) || (I.flags & (PZF_INTEG | PZF_CHEM)) ||
-        (I.dirk && (I.flags & PZF_DIRECT)))
+    if ((I.flags & (PZF_INTEG | PZF_CHEM)) || (I.dirk && (I.flags & PZF_DIRECT)))
       return pz_fail(h, PZ_E_UNSUPPORTED,
                      "pz_adjoint_forward: the adjoint covers the collocation step with the influence-matrix solve "
-                     "(CNAB2 or a DIRK scheme) or with the direct solve (CNAB2), without composition");
+                     "(any multistep or DIRK scheme) or with the direct solve (multistep schemes), without "
+                     "composition");
     if (I.scheme != h->inst[0].scheme)
       return pz_fail(h, PZ_E_UNSUPPORTED, "pz_adjoint_forward: all instances must use the same time scheme");
     if (adj_rloop_smem_bytes(I.P, I.rg, false) > PZ_SMEM_MAX)

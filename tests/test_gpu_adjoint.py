@@ -333,3 +333,23 @@ def test_direct_solve_adjoint(pz, variant):
     ens.set_ra(0, ra)
     fd = (jp - jm) / (2 * h)
     assert abs(fd - dra[0]) <= GRAD_TOL * abs(fd), (fd, dra[0])
+
+
+@pytest.mark.parametrize("scheme,solve", [("SBDF2", "INFLUENCE"), ("SBDF3", "INFLUENCE"), ("SBDF4", "INFLUENCE"),
+                                          ("CNLF", "INFLUENCE"), ("MODCNAB", "INFLUENCE"), ("TVB33", "INFLUENCE"),
+                                          ("SBDF3", "DIRECT")])
+def test_multistep_scheme_adjoint(pz, scheme, solve):
+    """The adjoint of the other multistep schemes (multistep_schemes.f90:
+    up to four old, implicit and explicit slots, with the CNAB2 bridge of
+    their first steps, step_time.f90:417-516), both solves: J against the
+    oracle with the same step sequence (a dt change in the middle; 1e-10),
+    the temperature gradient against FD along 2 directions (1e-6)."""
+    spec = dict(SMALL, time_scheme=scheme, matrix_solve=solve)
+    t0 = seeded(spec, 4, 1e-2)
+    ens = pz.Ensemble(gpu_config(spec))
+    J, dt = fwd(ens, t0, 12, 7, SCHED, ck=4)
+    assert np.array_equal(dt, SCHED)
+    Jo = oracle_objective(spec, t0, SCHED, 7)
+    assert abs(J - Jo) <= 1e-10 * abs(Jo), (J, Jo)
+    g, _ = ens.adjoint_backward()
+    fd_check(ens, t0, g[0], 12, 7, SCHED, n_dir=2, seed=13)
