@@ -497,6 +497,32 @@ def batched_adjoint_leg(torch, reps=2, n_fd=4, checkpoint_every=BADJ_CK, fd=True
             "fd_rel_errs": errs}
 
 
+# ---------------------------------------------------------------------------
+# replicas (one process per GPU under torchrun): the instances are
+# independent, so every rank steps its own ensemble (a seed of its own) and
+# the only collective is the max of the timed windows
+# ---------------------------------------------------------------------------
+def rank_specs(n_inst, seed, rank):
+    """The ensemble of one rank: the same size mix, its own seeds."""
+    return ensemble_specs(n_inst, seed=seed + 7919 * rank)
+
+
+def max_over_ranks(ms, dist, device):
+    """The slowest rank's timed window (ms); dist None on one process."""
+    if dist is None:
+        return ms
+    import torch
+    t = torch.tensor([ms], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def aggregate_rate(world, n_inst, steps, ms):
+    """Instance-steps/s of the whole job: every rank advanced n_inst
+    instances by `steps` steps within the slowest rank's ms."""
+    return world * n_inst * steps / (ms * 1e-3)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -531,7 +557,7 @@ def main():
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
     local = int(os.environ.get("LOCAL_RANK", "0"))
-    specs = ensemble_specs(args.instances, seed=args.seed + 7919 * rank)
+    specs = rank_specs(args.instances, args.seed, rank)
 
     if args.impl == "reference":
         if rank == 0:
@@ -599,11 +625,8 @@ def main():
     clocks.start()
     ms = time_steps(ens, args.steps, torch)
     clk = clocks.stop()
-    if dist:
-        t = torch.tensor([ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
-    value = world * len(specs) * args.steps / (ms * 1e-3)
+    ms = max_over_ranks(ms, dist, "cuda")
+    value = aggregate_rate(world, len(specs), args.steps, ms)
 
     # ---- per-kernel device times over the same steps as the timed window:
     # the same start state and warm-up, then the timed window's steps with
