@@ -1377,9 +1377,9 @@ cudaError_t launch_ckpt(const PzAdjDev& a, int c, int dir, cudaStream_t s) {
 // to snapshots base + 1 .. base + s1 - 1 after their stages (base >= 0).
 // With grid snapshots (a.gs) and gbase >= 0, k_rloop of stage s stores the
 // grids of the state it transforms at grid slot gbase + s - 1.
-cudaError_t launch_fwd_plan(const pz_handle* h, const PzDev& d, const PzAdjDev& a, int base, int gbase,
-                            cudaStream_t s) {
-  for (const PzLaunch& L : h->plan) {
+cudaError_t launch_fwd_plan(const pz_handle* h, const std::vector<PzLaunch>& plan, const PzDev& d,
+                            const PzAdjDev& a, int base, int gbase, cudaStream_t s) {
+  for (const PzLaunch& L : plan) {
     if (L.kind == PZK_OBS) continue;
     cudaError_t e;
     if (L.kind == PZK_RLOOP && gbase >= 0 && a.gs) {
@@ -1398,9 +1398,20 @@ cudaError_t launch_fwd_plan(const pz_handle* h, const PzDev& d, const PzAdjDev& 
   }
   return cudaSuccess;
 }
-// a CNAB2 step; its state's grids go to grid slot gslot (>= 0)
+// a multistep step; its state's grids go to grid slot gslot (>= 0).  Handles
+// with tensor-core instances step with that stage (the plain step's plan):
+// the sweep only needs the states, and the backward sweep rebuilds the dense
+// operators it transposes.
 cudaError_t launch_fwd(const pz_handle* h, const PzDev& d, const PzAdjDev& a, int gslot, cudaStream_t s) {
-  return launch_fwd_plan(h, d, a, -1, gslot, s);
+  if (h->n_fast > 0) {
+    PzDev df = h->fdev;
+    df.dt_io = d.dt_io;
+    df.rec = d.rec;
+    df.sched_n = d.sched_n;
+    df.sched_mode = d.sched_mode;
+    return launch_fwd_plan(h, h->fplan, df, a, -1, gslot, s);
+  }
+  return launch_fwd_plan(h, h->plan, d, a, -1, gslot, s);
 }
 
 // one forward DIRK step without the time series, with the stage states
@@ -1408,7 +1419,7 @@ cudaError_t launch_fwd(const pz_handle* h, const PzDev& d, const PzAdjDev& a, in
 cudaError_t launch_fwd_dirk(const pz_handle* h, const PzDev& d, const PzAdjDev& a, int base, cudaStream_t s) {
   cudaError_t e;
   if (base >= 0 && (e = launch_snap(a, base, s))) return e;
-  return launch_fwd_plan(h, d, a, base, base, s);
+  return launch_fwd_plan(h, h->plan, d, a, base, base, s);
 }
 
 // NL^T of snapshot `slot`; `grid`: the forward stored the slot's grids
@@ -1737,7 +1748,9 @@ extern "C" int pz_adjoint_backward(pz_handle* h, double* dJ_dtemp, double* dJ_dr
       if ((e = launch_snap(a, k1 - k0, s))) return acuda(h, e, "recompute");
     }
     for (int n = k1 - 1; n >= k0; --n) {
-      bool rebuild = false;
+      // the tensor-core forward builds no dense operators: rebuild them for the
+      // segment's last step
+      bool rebuild = n == k1 - 1 && h->n_fast > 0;
       if (n < k1 - 1)
         for (int i = 0; i < h->n_inst && !rebuild; ++i) {
           const PzState* r = &A->h_rec[(size_t)i * n_steps];

@@ -145,7 +145,7 @@ def test_ragged_batch_matches_independent_runs(pz):
 
 def test_unsupported_and_invalid_configs_fail_loudly(pz):
     with pytest.raises(pz.PizzaError) as e:
-        pz.Ensemble(pz.Config(n_r_max=128, m_max=32, matrix_solve="DIRECT"))   # smat build > shared memory
+        pz.Ensemble(pz.Config(n_r_max=33, m_max=32, minc=2, matrix_solve="INFLUENCE"))   # minc /= 1
     assert e.value.code == -6
     with pytest.raises(pz.PizzaError) as e:
         pz.Ensemble(pz.Config(n_r_max=3, m_max=32, matrix_solve="INFLUENCE"))
