@@ -151,10 +151,12 @@ __device__ __forceinline__ void mv3(const double* __restrict__ A, const double* 
 // ---------------------------------------------------------------------------
 // One stage of radix R with running product p (product of earlier radices).
 // tw[k] = exp(-2 pi i k / P) in global memory, tw[P + k] its conjugate;
-// `backward` selects the conjugate twiddles.  Twiddles of the first stage (p = 1)
-// are all 1.  RC = R for the radices with a specialised butterfly (2, 3, 4):
-// the butterfly values stay in registers; RC = 0 is the generic radix.
-template <int RC>
+// `backward` selects the conjugate twiddles.  RC = R for the radices with a
+// specialised butterfly (2, 3, 4): the butterfly values stay in registers;
+// RC = 0 is the generic radix.  FIRST = (p == 1): the first stage's twiddles
+// are all 1 and its index within the stage is its butterfly index, so that
+// instantiation loads and multiplies no twiddles.
+template <int RC, bool FIRST>
 __device__ void fft_stage_r(const double2* __restrict__ x, double2* __restrict__ y, int P, int Rrt, int p,
                             const double2* __restrict__ tw, int nb, bool backward) {
   constexpr int RU = RC ? RC : PZ_MAX_RADIX;
@@ -164,16 +166,17 @@ __device__ void fft_stage_r(const double2* __restrict__ x, double2* __restrict__
   const int rstep = P / R;
   // backward transforms read the conjugate table (tw + P): no FP64 sign flips
   const double2* twd = backward ? tw + P : tw;
-  // w / T and i / p by a float reciprocal and one correction step (w < 2^20:
-  // the float quotient is within one of the true one)
-  const float rT = 1.0f / (float)T, rp = 1.0f / (float)p;
+  // radix 3: W = c - i sg*sn with c = cos(2 pi/3), sn = sin(2 pi/3) from the table
+  double c3 = 0.0, s3 = 0.0;
+  if constexpr (RC == 3) {
+    const double2 w1 = __ldg(tw + rstep);
+    c3 = w1.x;
+    s3 = backward ? w1.y : -w1.y;
+  }
   for (int w = threadIdx.x; w < nb * T; w += blockDim.x) {
-    int b = (int)((float)w * rT);
-    b += (w - b * T >= T) - (w < b * T);
-    const int i = w - b * T;
-    int ip = (int)((float)i * rp);
-    ip += (i - ip * p >= p) - (i < ip * p);
-    const int k = i - ip * p;
+    const int b = w / T, i = w - b * T;
+    int k = 0;
+    if constexpr (!FIRST) k = i % p;
     const double2* xb = x + b * P;
     double2* yb = y + b * P;
     double2 u[RU];
@@ -182,7 +185,8 @@ __device__ void fft_stage_r(const double2* __restrict__ x, double2* __restrict__
     for (int q = 1; q < RU; ++q) {
       if (q < R) {
         const double2 v = xb[i + q * T];
-        u[q] = k == 0 ? v : cmul(v, __ldg(twd + q * k * tstep));   // q k tstep < R p P / (p R) = P
+        if constexpr (FIRST) u[q] = v;
+        else u[q] = k == 0 ? v : cmul(v, __ldg(twd + q * k * tstep));   // q k tstep < R p P / (p R) = P
       }
     }
     const int base = (i - k) * R + k;
@@ -199,12 +203,9 @@ __device__ void fft_stage_r(const double2* __restrict__ x, double2* __restrict__
       yb[base + 2 * p] = csub(s02, s13);
       yb[base + 3 * p] = csub(d02, jd13);
     } else if constexpr (RC == 3) {
-      // W = c - i sg*sn with c = cos(2 pi/3), sn = sin(2 pi/3) from the table
-      const double2 w1 = __ldg(tw + rstep);
-      const double c = w1.x, sn = backward ? w1.y : -w1.y;
       const double2 s12 = cadd(u[1], u[2]), d12 = csub(u[1], u[2]);
-      const double2 m = make_double2(u[0].x + c * s12.x, u[0].y + c * s12.y);
-      const double2 jd = make_double2(sn * d12.y, -sn * d12.x);   // -i sn d
+      const double2 m = make_double2(u[0].x + c3 * s12.x, u[0].y + c3 * s12.y);
+      const double2 jd = make_double2(s3 * d12.y, -s3 * d12.x);   // -i sn d
       yb[base] = cadd(u[0], s12);
       yb[base + p] = cadd(m, jd);
       yb[base + 2 * p] = csub(m, jd);
@@ -219,10 +220,15 @@ __device__ void fft_stage_r(const double2* __restrict__ x, double2* __restrict__
 }
 __device__ void fft_stage(const double2* __restrict__ x, double2* __restrict__ y, int P, int R, int p,
                           const double2* __restrict__ tw, int nb, bool backward) {
-  if (R == 4) fft_stage_r<4>(x, y, P, R, p, tw, nb, backward);
-  else if (R == 2) fft_stage_r<2>(x, y, P, R, p, tw, nb, backward);
-  else if (R == 3) fft_stage_r<3>(x, y, P, R, p, tw, nb, backward);
-  else fft_stage_r<0>(x, y, P, R, p, tw, nb, backward);
+  if (p == 1) {
+    if (R == 4) fft_stage_r<4, true>(x, y, P, R, p, tw, nb, backward);
+    else if (R == 2) fft_stage_r<2, true>(x, y, P, R, p, tw, nb, backward);
+    else if (R == 3) fft_stage_r<3, true>(x, y, P, R, p, tw, nb, backward);
+    else fft_stage_r<0, true>(x, y, P, R, p, tw, nb, backward);
+  } else if (R == 4) fft_stage_r<4, false>(x, y, P, R, p, tw, nb, backward);
+  else if (R == 2) fft_stage_r<2, false>(x, y, P, R, p, tw, nb, backward);
+  else if (R == 3) fft_stage_r<3, false>(x, y, P, R, p, tw, nb, backward);
+  else fft_stage_r<0, false>(x, y, P, R, p, tw, nb, backward);
 }
 
 // Full transform; returns the buffer holding the result (a or b).
@@ -317,11 +323,8 @@ __device__ void rloop_group(const PzInst& I, const View& V, int r0, int gmax, IO
   // multiple of 32 the 32 points of a warp lie on one radius and every lane
   // runs every pass: one atomic per warp after a warp maximum.
   const bool warp_red = (P & 31) == 0 && (blockDim.x & 31) == 0;
-  const float rP = 1.0f / (float)P;
   for (int t = threadIdx.x; t < G * P; t += blockDim.x) {
-    int g = (int)((float)t * rP);
-    g += (t - g * P >= P) - (t < g * P);     // t / P (t < 2^20)
-    const int j = t - g * P;
+    const int g = t / P, j = t - g * P;
     const double rr = V.rad(RV_R)[r0 + g];
     const double2 z1 = g1[(nt * g) * P + j], z2 = g1[(nt * g + 1) * P + j];
     const double usg = z1.x, upg = z1.y, omg = z2.x, Tg = z2.y;
@@ -355,11 +358,8 @@ __device__ void rloop_group(const PzInst& I, const View& V, int r0, int gmax, IO
   }
   double2* f = fft_run(h, g1, I, tw, nt * G, false);
   const double hP = 0.5 / (double)P;
-  const float rM = 1.0f / (float)M;
   for (int t = threadIdx.x; t < G * M; t += blockDim.x) {
-    int g = (int)((float)t * rM);
-    g += (t - g * M >= M) - (t < g * M);     // t / M (t < 2^20)
-    const int m = t - g * M, r = r0 + g;
+    const int g = t / M, m = t - g * M, r = r0 + g;
     const double or1 = V.rad(RV_OR1)[r];
     const double tfac = (1.0 - I.tadvz) * V.rad(RV_BETA)[r] * or1;
     const int mc = m == 0 ? 0 : P - m;

@@ -125,7 +125,11 @@ __device__ __forceinline__ double scale2(double v, int e) {
 // B).  A warp takes a (16-row tile, NC 8-column tiles) task; for each k tile
 // it loads the NC x PZ_OZ_S B fragments once and every A slice once, and runs
 // the slice pairs kA + kx <= PZ_OZ_S - 1, accumulating the pair sums of equal
-// kA + kx in one fp32 register set (integers below 2^24: exact).
+// kA + kx in one fp32 register set (integers below 2^24: exact).  Each A
+// slice register is refilled with the next k tile's slice as soon as its
+// last product of this tile is issued, so the loads of tile kt + 1 overlap
+// the products of tile kt (the last tile re-reads itself: no read past the
+// operator).
 template <int NC>
 __device__ void oz_mma_t(const PzFastDev& F, const PzOzOp& op, const BOp& B, int C, double* Y, int ldy) {
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
@@ -142,6 +146,10 @@ __device__ void oz_mma_t(const PzFastDev& F, const PzOzOp& op, const BOp& B, int
       for (int g = 0; g < PZ_OZ_S; ++g)
 #pragma unroll
         for (int q = 0; q < 4; ++q) acc[c][g][q] = 0.0f;
+    const uint4* ap = Af + ((long long)rt * op.KT * PZ_OZ_S) * 32 + lane;
+    uint4 a[PZ_OZ_S];
+#pragma unroll
+    for (int ka = 0; ka < PZ_OZ_S; ++ka) a[ka] = __ldg(ap + ka * 32);
     for (int kt = 0; kt < op.KT; ++kt) {
       uint32_t b[NC][PZ_OZ_S][2];
 #pragma unroll
@@ -154,14 +162,14 @@ __device__ void oz_mma_t(const PzFastDev& F, const PzOzOp& op, const BOp& B, int
           b[c][s][1] = p[4];
         }
       }
-      const uint4* ap = Af + ((long long)(rt * op.KT + kt) * PZ_OZ_S) * 32 + lane;
+      const uint4* an = ap + (long long)(kt + 1 < op.KT ? kt + 1 : kt) * PZ_OZ_S * 32;
 #pragma unroll
       for (int ka = 0; ka < PZ_OZ_S; ++ka) {
-        const uint4 a = __ldg(ap + ka * 32);
 #pragma unroll
         for (int g = ka; g < PZ_OZ_S; ++g)
 #pragma unroll
-          for (int c = 0; c < NC; ++c) mma16816(acc[c][g], a, b[c][g - ka][0], b[c][g - ka][1]);
+          for (int c = 0; c < NC; ++c) mma16816(acc[c][g], a[ka], b[c][g - ka][0], b[c][g - ka][1]);
+        a[ka] = __ldg(an + ka * 32);
       }
     }
 #pragma unroll
@@ -184,26 +192,26 @@ __device__ __forceinline__ void oz_mma(const PzFastDev& F, const PzOzOp& op, con
   oz_mma_t<1>(F, op, B, C, Y, ldy);
 }
 
-__device__ __forceinline__ double2 imex_rhs_f(const View& V, const PzInst& I, const PzState& S, int f, int mi,
-                                               int i) {
-  double2 acc;
-  {
-    const double2 v = V.hist(f, 0, S.r_old, mi)[i];
-    acc = make_double2(S.wimp[0] * v.x, S.wimp[0] * v.y);
+// The IMEX right-hand side of one instance (multistep_schemes.f90:308-316)
+// as a list of history slots and weights: rhs = sum_j w[j] hist(slot[j])
+// with the old terms (wimp), the implicit terms (wimp_lin(2:)) and the
+// explicit terms (wexp) of the ring positions of this step.  off[j] is the
+// slot's offset from the first history slot of the field, in (m, r) planes.
+#define PZ_RHS_TERMS 12
+struct RhsTerms {
+  double w[PZ_RHS_TERMS];
+  int off[PZ_RHS_TERMS];
+  int n;
+};
+__device__ __forceinline__ void rhs_terms(const PzInst& I, const PzState& S, RhsTerms& T) {
+  int n = 0;
+  for (int k = 0; k < I.nold; ++k, ++n) { T.w[n] = S.wimp[k]; T.off[n] = (S.r_old + k) % I.nold; }
+  for (int k = 0; k < I.nimp; ++k, ++n) { T.w[n] = S.wimp_lin[k + 1]; T.off[n] = I.nold + (S.r_impl + k) % I.nimp; }
+  for (int k = 0; k < I.nexp; ++k, ++n) {
+    T.w[n] = S.wexp[k];
+    T.off[n] = I.nold + I.nimp + (S.r_expl + k) % I.nexp;
   }
-  for (int k = 1; k < I.nold; ++k) {
-    const double2 v = V.hist(f, 0, (S.r_old + k) % I.nold, mi)[i];
-    acc.x += S.wimp[k] * v.x; acc.y += S.wimp[k] * v.y;
-  }
-  for (int k = 0; k < I.nimp; ++k) {
-    const double2 v = V.hist(f, 1, (S.r_impl + k) % I.nimp, mi)[i];
-    acc.x += S.wimp_lin[k + 1] * v.x; acc.y += S.wimp_lin[k + 1] * v.y;
-  }
-  for (int k = 0; k < I.nexp; ++k) {
-    const double2 v = V.hist(f, 2, (S.r_expl + k) % I.nexp, mi)[i];
-    acc.x += S.wexp[k] * v.x; acc.y += S.wexp[k] * v.y;
-  }
-  return acc;
+  T.n = n;
 }
 
 // shared-memory layout of k_fast for G instances and grids up to N
@@ -212,11 +220,12 @@ struct FastSmem {
   double* R;     // product outputs, column-major
   double* RT;    // temperature right-hand sides (interior), then the new temperature (interior)
   double* RW;    // vorticity / u_phi right-hand sides (interior)
-  double* sc;    // per instance: c1 (re, im), c2 (re, im)
+  double* sc;    // per instance: c1 (re, im), c2 (re, im), w, 1/w, w TdiffFac, w ViscFac
+  RhsTerms* rh;  // per instance: IMEX right-hand-side terms
   int* st;       // per instance: active, bad
 };
 __host__ __device__ inline size_t fast_smem_layout(int G, int N, size_t* oR, size_t* oRT, size_t* oRW, size_t* osc,
-                                                   size_t* ost, size_t* oce, int* C, int* sw) {
+                                                   size_t* orh, size_t* ost, size_t* oce, int* C, int* sw) {
   const int n = N - 2;
   *C = ((2 * G + 15) / 16) * 16;
   *sw = ((N + 15) / 16) * 8 + 4;
@@ -230,6 +239,8 @@ __host__ __device__ inline size_t fast_smem_layout(int G, int N, size_t* oR, siz
   *oRT = o; o += (size_t)2 * G * n * 8;
   *oRW = o; o += (size_t)2 * G * n * 8;
   *osc = o; o += (size_t)G * 8 * 8;
+  *orh = o; o += (size_t)G * sizeof(RhsTerms);
+  o = (o + 15) & ~(size_t)15;
   *ost = o; o += (size_t)G * 2 * 4;
   return (o + 15) & ~(size_t)15;
 }
@@ -242,9 +253,9 @@ __global__ void __launch_bounds__(256, 3) k_fast(PzDev d) {
   const int N = cls.N, n = cls.n, mi = it.m, G = F.G, ni = it.ni;
   FastSmem s;
   {
-    size_t oR, oRT, oRW, osc, ost, oce;
+    size_t oR, oRT, oRW, osc, orh, ost, oce;
     int C, sw;
-    fast_smem_layout(G, d.fast_maxN, &oR, &oRT, &oRW, &osc, &ost, &oce, &C, &sw);
+    fast_smem_layout(G, d.fast_maxN, &oR, &oRT, &oRW, &osc, &orh, &ost, &oce, &C, &sw);
     s.B.w = reinterpret_cast<uint32_t*>(fsm);
     s.B.ce = reinterpret_cast<int*>(fsm + oce);
     s.B.C = C;
@@ -253,6 +264,7 @@ __global__ void __launch_bounds__(256, 3) k_fast(PzDev d) {
     s.RT = reinterpret_cast<double*>(fsm + oRT);
     s.RW = reinterpret_cast<double*>(fsm + oRW);
     s.sc = reinterpret_cast<double*>(fsm + osc);
+    s.rh = reinterpret_cast<RhsTerms*>(fsm + orh);
     s.st = reinterpret_cast<int*>(fsm + ost);
   }
   const int* fi = F.fi + it.i0;
@@ -268,6 +280,7 @@ __global__ void __launch_bounds__(256, 3) k_fast(PzDev d) {
       s.sc[8 * g + 5] = 1.0 / w;
       s.sc[8 * g + 6] = w * d.inst[fi[g]].TdiffFac;
       s.sc[8 * g + 7] = w * d.inst[fi[g]].ViscFac;
+      rhs_terms(d.inst[fi[g]], d.state[fi[g]], s.rh[g]);
     }
   }
   __syncthreads();
@@ -288,59 +301,88 @@ __global__ void __launch_bounds__(256, 3) k_fast(PzDev d) {
     __syncthreads();
   }
 
-  // ---- finish the explicit terms; IMEX right-hand sides (interior rows)
-  const double dm = (double)(mi * d.inst[fi[0]].minc), dm2 = dm * dm;
-  for (int t = threadIdx.x; t < ni * N; t += blockDim.x) {
-    const int g = t / N, i = t - g * N;
+  // ---- finish the explicit terms; IMEX right-hand sides (interior rows).
+  // One warp per instance: the instance's constants and row pointers are
+  // read once into registers, the lanes run over the radii.
+  const double dm = (double)(mi * d.inst[fi[0]].minc);
+  for (int g = warp; g < ni; g += nw) {
     if (!s.st[2 * g]) continue;
     const int inst = fi[g];
     const PzInst& I = d.inst[inst];
     const PzState& S = d.state[inst];
     const View V{&I, d.pool};
+    const int flags = I.flags;
+    const double tadvz = I.tadvz, cor = I.CorFac, buo = I.BuoFac;
     const double* or1 = V.rad(RV_OR1);
     const double* beta = V.rad(RV_BETA);
-    const double2 u = V.fld(F_US, mi)[i];
-    const double2 dT = make_double2(s.R[(2 * g + 0) * N + i], s.R[(2 * g + 1) * N + i]);
-    const double2 dO = make_double2(s.R[(long long)(2 * G + 2 * g) * N + i], s.R[(long long)(2 * G + 2 * g + 1) * N + i]);
+    const double* dtcond = V.rad(RV_DTCOND);
+    const double* tcond = V.rad(RV_TCOND);
+    const double* rgrav = V.rad(RV_RGRAV);
+    const double* ekp = V.rad(RV_EKPUMP);
+    const double* ekus = V.rad(RV_EKP_US);
+    const double* ekdp = V.rad(RV_EKP_DUSDP);
+    const double* ekup = V.rad(RV_EKP_UP);
+    const double2* us = V.fld(F_US, mi);
+    const double2* tf = V.fld(F_TEMP, mi);
+    const double2* om = V.fld(F_OM, mi);
+    const double2* up = V.fld(F_UP, mi);
     double2* eT = V.hist(0, 2, S.r_expl, mi);
-    double2 e = eT[i];
-    const double c = V.rad(RV_DTCOND)[i] - I.tadvz * beta[i] * V.rad(RV_TCOND)[i];
-    e.x = e.x - or1[i] * dT.x - u.x * c;
-    e.y = e.y - or1[i] * dT.y - u.y * c;
-    eT[i] = e;
-    if (mi != 0) {
-      double2* eP = V.hist(1, 2, S.r_expl, mi);
-      double2 p = eP[i];
-      p.x -= or1[i] * dO.x;
-      p.y -= or1[i] * dO.y;
-      if (!(I.flags & PZF_NON_ROT)) {
-        p.x += I.CorFac * beta[i] * u.x;
-        p.y += I.CorFac * beta[i] * u.y;
+    double2* eP = V.hist(1, 2, S.r_expl, mi);
+    const double2* h0 = V.hist(0, 0, 0, mi);      // first history slot, temperature
+    const double2* h1 = V.hist(1, 0, 0, mi);      // first history slot, vorticity / u_phi
+    const long long pl = (long long)I.M * I.N;    // one (m, r) plane
+    const RhsTerms& rh = s.rh[g];
+    const double* Rt = s.R + (long long)(2 * g) * N;
+    const double* Ro = s.R + (long long)(2 * G + 2 * g) * N;
+    for (int i = lane; i < N; i += 32) {
+      const double2 u = us[i];
+      const double2 dT = make_double2(Rt[i], Rt[N + i]);
+      double2 e = eT[i];
+      const double c = dtcond[i] - tadvz * beta[i] * tcond[i];
+      e.x = e.x - or1[i] * dT.x - u.x * c;
+      e.y = e.y - or1[i] * dT.y - u.y * c;
+      eT[i] = e;
+      if (mi != 0) {
+        const double2 dO = make_double2(Ro[i], Ro[N + i]);
+        double2 p = eP[i];
+        p.x -= or1[i] * dO.x;
+        p.y -= or1[i] * dO.y;
+        if (!(flags & PZF_NON_ROT)) {
+          p.x += cor * beta[i] * u.x;
+          p.y += cor * beta[i] * u.y;
+        }
+        if (!(flags & PZF_BUO_IMP)) {
+          const double2 b = cim(dm, tf[i]);
+          const double cb = buo * rgrav[i] * or1[i];
+          p.x -= cb * b.x; p.y -= cb * b.y;
+        }
+        if (flags & PZF_EK_PUMP) {
+          const double2 o = om[i], w = up[i];
+          const double eus = ekus[i], edp = ekdp[i];
+          const double2 q = make_double2(eus * u.x - edp * dm * u.y, eus * u.y + edp * dm * u.x);
+          const double ce = cor * ekp[i];
+          const double eup = ekup[i];
+          p.x -= ce * (o.x + eup * w.x + q.x);
+          p.y -= ce * (o.y + eup * w.y + q.y);
+        }
+        eP[i] = p;
       }
-      if (!(I.flags & PZF_BUO_IMP)) {
-        const double2 b = cim(dm, V.fld(F_TEMP, mi)[i]);
-        const double cb = I.BuoFac * V.rad(RV_RGRAV)[i] * or1[i];
-        p.x -= cb * b.x; p.y -= cb * b.y;
+      if (i == 0 || i == N - 1) continue;
+      // the explicit term of this step was stored above: read after the store
+      double2 rt = make_double2(0.0, 0.0), rw = make_double2(0.0, 0.0);
+      for (int k = 0; k < rh.n; ++k) {
+        const double w = rh.w[k];
+        const long long o = rh.off[k] * pl + i;
+        const double2 a = h0[o], b = h1[o];
+        rt.x += w * a.x; rt.y += w * a.y;
+        rw.x += w * b.x; rw.y += w * b.y;
       }
-      if (I.flags & PZF_EK_PUMP) {
-        const double2 o = V.fld(F_OM, mi)[i], w = V.fld(F_UP, mi)[i];
-        const double eus = V.rad(RV_EKP_US)[i], edp = V.rad(RV_EKP_DUSDP)[i];
-        const double2 q = make_double2(eus * u.x - edp * dm * u.y, eus * u.y + edp * dm * u.x);
-        const double ce = I.CorFac * V.rad(RV_EKPUMP)[i];
-        const double eup = V.rad(RV_EKP_UP)[i];
-        p.x -= ce * (o.x + eup * w.x + q.x);
-        p.y -= ce * (o.y + eup * w.y + q.y);
-      }
-      eP[i] = p;
+      if (mi == 0) rw.y = 0.0;
+      s.RT[(2 * g) * n + i - 1] = rt.x;
+      s.RT[(2 * g + 1) * n + i - 1] = rt.y;
+      s.RW[(2 * g) * n + i - 1] = rw.x;
+      s.RW[(2 * g + 1) * n + i - 1] = rw.y;
     }
-    if (i == 0 || i == N - 1) continue;
-    const double2 rt = imex_rhs_f(V, I, S, 0, mi, i);
-    double2 rw = imex_rhs_f(V, I, S, 1, mi, i);
-    if (mi == 0) rw.y = 0.0;
-    s.RT[(2 * g) * n + i - 1] = rt.x;
-    s.RT[(2 * g + 1) * n + i - 1] = rt.y;
-    s.RW[(2 * g) * n + i - 1] = rw.x;
-    s.RW[(2 * g + 1) * n + i - 1] = rw.y;
   }
   __syncthreads();
 
@@ -354,7 +396,6 @@ __global__ void __launch_bounds__(256, 3) k_fast(PzDev d) {
     const double* lam = F.vec + FM.vec;
     for (int t = threadIdx.x; t < ni * n; t += blockDim.x) {
       const int g = t / n, k = t - g * n;
-      const int inst = fi[g];
       const double D = 1.0 / (1.0 - s.sc[8 * g + 6] * lam[k]);
       s.R[(long long)(2 * g) * n + k] *= D;
       s.R[(long long)(2 * g + 1) * n + k] *= D;
@@ -367,40 +408,50 @@ __global__ void __launch_bounds__(256, 3) k_fast(PzDev d) {
   oz_mma(F, FM.s3t, s.B, 2 * ni, s.R, n + N);
   __syncthreads();
   // new temperature, dT/dr, history; the vorticity rhs gets the implicit buoyancy
-  for (int t = threadIdx.x; t < ni * N; t += blockDim.x) {
-    const int g = t / N, i = t - g * N;
+  // (one warp per instance, like the explicit terms)
+  for (int g = warp; g < ni; g += nw) {
     if (!s.st[2 * g]) continue;
     const int inst = fi[g];
     const PzInst& I = d.inst[inst];
     const PzState& S = d.state[inst];
     const View V{&I, d.pool};
     const int ld = n + N;
-    const bool edge = (i == 0 || i == N - 1);
-    const double2 T = edge ? make_double2(0.0, 0.0)
-                           : make_double2(s.R[(2 * g) * ld + i - 1], s.R[(2 * g + 1) * ld + i - 1]);
-    const double2 d1 = make_double2(s.R[(2 * g) * ld + n + i], s.R[(2 * g + 1) * ld + n + i]);
-    V.fld(F_TEMP, mi)[i] = T;
-    V.fld(F_DTEMP, mi)[i] = d1;
-    V.hist(0, 0, S.b_old, mi)[i] = T;
-    if (!isfinite(T.x) || !isfinite(T.y)) s.st[2 * g + 1] = 1;
-    const double w = S.wimp_lin[0];
-    if (S.l_calc_lin) {
-      double2 it = make_double2(0.0, 0.0);
-      if (!edge) {
-        const double iw = s.sc[8 * g + 5];
-        it = make_double2(iw * (T.x - s.RT[(2 * g) * n + i - 1]), iw * (T.y - s.RT[(2 * g + 1) * n + i - 1]));
+    const double w = S.wimp_lin[0], iw = s.sc[8 * g + 5];
+    const bool lin = S.l_calc_lin != 0;
+    const bool buo = mi != 0 && (I.flags & PZF_BUO_IMP);
+    const double cbuo = w * I.BuoFac;
+    const double* rgrav = V.rad(RV_RGRAV);
+    const double* or1 = V.rad(RV_OR1);
+    double2* tf = V.fld(F_TEMP, mi);
+    double2* dtf = V.fld(F_DTEMP, mi);
+    double2* ho = V.hist(0, 0, S.b_old, mi);
+    double2* hi = V.hist(0, 1, S.b_impl, mi);
+    const double* Rr = s.R + (long long)(2 * g) * ld;
+    const double* Ri = Rr + ld;
+    double* RTr = s.RT + (long long)(2 * g) * n;
+    double* RTi = RTr + n;
+    double* RWr = s.RW + (long long)(2 * g) * n;
+    double* RWi = RWr + n;
+    bool bad = false;
+    for (int i = lane; i < N; i += 32) {
+      const bool edge = (i == 0 || i == N - 1);
+      const double2 T = edge ? make_double2(0.0, 0.0) : make_double2(Rr[i - 1], Ri[i - 1]);
+      tf[i] = T;
+      dtf[i] = make_double2(Rr[n + i], Ri[n + i]);
+      ho[i] = T;
+      bad |= !isfinite(T.x) || !isfinite(T.y);
+      if (lin) hi[i] = edge ? make_double2(0.0, 0.0) : make_double2(iw * (T.x - RTr[i - 1]), iw * (T.y - RTi[i - 1]));
+      if (edge) continue;
+      RTr[i - 1] = T.x;       // the new temperature for the buoyancy below
+      RTi[i - 1] = T.y;
+      if (buo) {
+        const double2 b = cim(dm, T);
+        const double c = cbuo * rgrav[i] * or1[i];
+        RWr[i - 1] -= c * b.x;
+        RWi[i - 1] -= c * b.y;
       }
-      V.hist(0, 1, S.b_impl, mi)[i] = it;
     }
-    if (edge) continue;
-    s.RT[(2 * g) * n + i - 1] = T.x;       // the new temperature for the buoyancy below
-    s.RT[(2 * g + 1) * n + i - 1] = T.y;
-    if (mi != 0 && (I.flags & PZF_BUO_IMP)) {
-      const double2 b = cim(dm, T);
-      const double c = w * I.BuoFac * V.rad(RV_RGRAV)[i] * V.rad(RV_OR1)[i];
-      s.RW[(2 * g) * n + i - 1] -= c * b.x;
-      s.RW[(2 * g + 1) * n + i - 1] -= c * b.y;
-    }
+    if (bad) s.st[2 * g + 1] = 1;
   }
   __syncthreads();
 
@@ -431,38 +482,66 @@ __global__ void __launch_bounds__(256, 3) k_fast(PzDev d) {
     const double* qb = lam + 4 * n;
     for (int g = warp; g < ni; g += nw) {
       if (!s.st[2 * g]) continue;
-      const int inst = fi[g];
       const double wn = s.sc[8 * g + 7];
       double* zr = s.R + (long long)(2 * g) * n;
       double* zi = zr + n;
-      double t1r = 0.0, t1i = 0.0, b1r = 0.0, b1i = 0.0, t2 = 0.0, b2 = 0.0, t3 = 0.0, b3 = 0.0;
-      double wD[PZ_FAST_KPL];            // w nu / (1 - w nu lam) of this lane's k
+      // v = (t1r, t1i, b1r, b1i, t2, b2, t3, b3): the walls' dpsi/dr of z
+      // (t1, b1) and of the two homogeneous solutions (t2, b2; t3, b3)
+      double v[8] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
+      double hb[PZ_FAST_KPL], ht[PZ_FAST_KPL];   // h_bot, h_top at this lane's k
 #pragma unroll
       for (int u = 0; u < PZ_FAST_KPL; ++u) {
         const int k = lane + 32 * u;
-        wD[u] = 0.0;
+        hb[u] = 0.0; ht[u] = 0.0;
         if (k >= n) continue;
         const double D = 1.0 / (1.0 - wn * lam[k]);
-        wD[u] = wn * D;
+        const double wD = wn * D;
         const double yr = zr[k] * D, yi = zi[k] * D;
         zr[k] = yr; zi[k] = yi;
-        const double h2 = wD[u] * gbot[k], h3 = wD[u] * gtop[k];
-        t1r += qt[k] * yr; t1i += qt[k] * yi; b1r += qb[k] * yr; b1i += qb[k] * yi;
-        t2 += qt[k] * h2; b2 += qb[k] * h2; t3 += qt[k] * h3; b3 += qb[k] * h3;
+        hb[u] = wD * gbot[k]; ht[u] = wD * gtop[k];
+        const double a = qt[k], b = qb[k];
+        v[0] += a * yr; v[1] += a * yi; v[2] += b * yr; v[3] += b * yi;
+        v[4] += a * hb[u]; v[5] += b * hb[u]; v[6] += a * ht[u]; v[7] += b * ht[u];
       }
-      t1r = warp_sum(t1r); t1i = warp_sum(t1i); b1r = warp_sum(b1r); b1i = warp_sum(b1i);
-      t2 = warp_sum(t2); b2 = warp_sum(b2); t3 = warp_sum(t3); b3 = warp_sum(b3);
-      const double det = t2 * b3 - t3 * b2;
-      const double i00 = b3 / det, i01 = -t3 / det, i10 = -b2 / det, i11 = t2 / det;
+      // the eight warp sums as one transpose reduction: each exchange halves
+      // the values a lane carries (16: 8 -> 4, 8: 4 -> 2, 4: 2 -> 1), two
+      // more rounds finish the sums; lane 16 q2 + 8 q1 + 4 q0 then holds sum q
+      double r4[4], r2[2];
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        const bool hi = lane & 16;
+        const double send = hi ? v[q] : v[q + 4];
+        r4[q] = (hi ? v[q + 4] : v[q]) + __shfl_xor_sync(0xffffffffu, send, 16);
+      }
+#pragma unroll
+      for (int q = 0; q < 2; ++q) {
+        const bool hi = lane & 8;
+        const double send = hi ? r4[q] : r4[q + 2];
+        r2[q] = (hi ? r4[q + 2] : r4[q]) + __shfl_xor_sync(0xffffffffu, send, 8);
+      }
+      double r1;
+      {
+        const bool hi = lane & 4;
+        const double send = hi ? r2[0] : r2[1];
+        r1 = (hi ? r2[1] : r2[0]) + __shfl_xor_sync(0xffffffffu, send, 4);
+      }
+      r1 += __shfl_xor_sync(0xffffffffu, r1, 2);
+      r1 += __shfl_xor_sync(0xffffffffu, r1, 1);
+      double sum[8];
+#pragma unroll
+      for (int q = 0; q < 8; ++q) sum[q] = __shfl_sync(0xffffffffu, r1, 16 * (q >> 2) + 8 * ((q >> 1) & 1) + 4 * (q & 1));
+      const double t1r = sum[0], t1i = sum[1], b1r = sum[2], b1i = sum[3];
+      const double t2 = sum[4], b2 = sum[5], t3 = sum[6], b3 = sum[7];
+      const double idet = 1.0 / (t2 * b3 - t3 * b2);
+      const double i00 = b3 * idet, i01 = -t3 * idet, i10 = -b2 * idet, i11 = t2 * idet;
       const double c1r = -i00 * t1r - i01 * b1r, c1i = -i00 * t1i - i01 * b1i;
       const double c2r = -i10 * t1r - i11 * b1r, c2i = -i10 * t1i - i11 * b1i;
 #pragma unroll
       for (int u = 0; u < PZ_FAST_KPL; ++u) {
         const int k = lane + 32 * u;
         if (k >= n) continue;
-        const double h2 = wD[u] * gbot[k], h3 = wD[u] * gtop[k];
-        zr[k] += c1r * h2 + c2r * h3;
-        zi[k] += c1i * h2 + c2i * h3;
+        zr[k] += c1r * hb[u] + c2r * ht[u];
+        zi[k] += c1i * hb[u] + c2i * ht[u];
       }
       if (lane == 0) {
         s.sc[8 * g + 0] = c1r; s.sc[8 * g + 1] = c1i; s.sc[8 * g + 2] = c2r; s.sc[8 * g + 3] = c2i;
@@ -478,57 +557,71 @@ __global__ void __launch_bounds__(256, 3) k_fast(PzDev d) {
   oz_mma(F, w3, s.B, 2 * ni, s.R, ld3);
   __syncthreads();
 
-  // ---- new velocity, vorticity and streamfunction; history
-  for (int t = threadIdx.x; t < ni * N; t += blockDim.x) {
-    const int g = t / N, i = t - g * N;
+  // ---- new velocity, vorticity and streamfunction; history (one warp per instance)
+  for (int g = warp; g < ni; g += nw) {
     if (!s.st[2 * g]) continue;
     const int inst = fi[g];
     const PzInst& I = d.inst[inst];
     const PzState& S = d.state[inst];
     const View V{&I, d.pool};
     const double* or1 = V.rad(RV_OR1);
-    const bool edge = (i == 0 || i == N - 1);
+    const double* beta = V.rad(RV_BETA);
+    const double* rgrav = V.rad(RV_RGRAV);
     const double iw = s.sc[8 * g + 5];
+    const bool lin = S.l_calc_lin != 0;
+    const bool buo = (I.flags & PZF_BUO_IMP) != 0;
+    const double bf = I.BuoFac;
+    double2* us = V.fld(F_US, mi);
+    double2* up = V.fld(F_UP, mi);
+    double2* omf = V.fld(F_OM, mi);
+    double2* psi = V.fld(F_PSI, mi);
+    double2* ho = V.hist(1, 0, S.b_old, mi);
+    double2* hi = V.hist(1, 1, S.b_impl, mi);
     const double* Rr = s.R + (long long)(2 * g) * ld3;
     const double* Ri = s.R + (long long)(2 * g + 1) * ld3;
-    bool bad;
-    if (mi == 0) {
-      const double u = edge ? 0.0 : Rr[i - 1];
-      const double du = Rr[n + i];
-      V.fld(F_US, 0)[i] = make_double2(0.0, 0.0);
-      V.fld(F_UP, 0)[i] = make_double2(u, 0.0);
-      V.fld(F_OM, 0)[i] = make_double2(du + or1[i] * u, 0.0);
-      V.fld(F_PSI, 0)[i] = make_double2(0.0, 0.0);
-      V.hist(1, 0, S.b_old, 0)[i] = make_double2(u, 0.0);
-      if (S.l_calc_lin)
-        V.hist(1, 1, S.b_impl, 0)[i] = make_double2(edge ? 0.0 : iw * (u - s.RW[(2 * g) * n + i - 1]), 0.0);
-      bad = !isfinite(u);
-    } else {
-      double2 om, ps;
-      if (i == 0) om = make_double2(s.sc[8 * g + 2], s.sc[8 * g + 3]);
-      else if (i == N - 1) om = make_double2(s.sc[8 * g + 0], s.sc[8 * g + 1]);
-      else om = make_double2(Rr[i - 1], Ri[i - 1]);
-      ps = edge ? make_double2(0.0, 0.0) : make_double2(Rr[n + i - 1], Ri[n + i - 1]);
-      const double2 dp = make_double2(Rr[2 * n + i], Ri[2 * n + i]);
-      const double be = V.rad(RV_BETA)[i];
-      V.fld(F_PSI, mi)[i] = ps;
-      V.fld(F_US, mi)[i] = cscale(or1[i], cim(dm, ps));
-      V.fld(F_UP, mi)[i] = make_double2(-dp.x - be * ps.x, -dp.y - be * ps.y);
-      V.fld(F_OM, mi)[i] = om;
-      V.hist(1, 0, S.b_old, mi)[i] = om;
-      if (S.l_calc_lin) {
-        double2 v = make_double2(0.0, 0.0);
-        if (!edge) {
-          v = cscale(iw, csub(om, make_double2(s.RW[(2 * g) * n + i - 1], s.RW[(2 * g + 1) * n + i - 1])));
-          if (I.flags & PZF_BUO_IMP) {
-            const double2 b = cim(dm, make_double2(s.RT[(2 * g) * n + i - 1], s.RT[(2 * g + 1) * n + i - 1]));
-            const double c = V.rad(RV_RGRAV)[i] * or1[i] * I.BuoFac;
-            v.x -= c * b.x; v.y -= c * b.y;
+    const double* RWr = s.RW + (long long)(2 * g) * n;
+    const double* RWi = RWr + n;
+    const double* RTr = s.RT + (long long)(2 * g) * n;
+    const double* RTi = RTr + n;
+    const double2 om_bot = make_double2(s.sc[8 * g + 2], s.sc[8 * g + 3]);
+    const double2 om_top = make_double2(s.sc[8 * g + 0], s.sc[8 * g + 1]);
+    bool bad = false;
+    for (int i = lane; i < N; i += 32) {
+      const bool edge = (i == 0 || i == N - 1);
+      if (mi == 0) {
+        const double u = edge ? 0.0 : Rr[i - 1];
+        const double du = Rr[n + i];
+        us[i] = make_double2(0.0, 0.0);
+        up[i] = make_double2(u, 0.0);
+        omf[i] = make_double2(du + or1[i] * u, 0.0);
+        psi[i] = make_double2(0.0, 0.0);
+        ho[i] = make_double2(u, 0.0);
+        if (lin) hi[i] = make_double2(edge ? 0.0 : iw * (u - RWr[i - 1]), 0.0);
+        bad |= !isfinite(u);
+      } else {
+        const double2 om = i == 0 ? om_bot : (i == N - 1 ? om_top : make_double2(Rr[i - 1], Ri[i - 1]));
+        const double2 ps = edge ? make_double2(0.0, 0.0) : make_double2(Rr[n + i - 1], Ri[n + i - 1]);
+        const double2 dp = make_double2(Rr[2 * n + i], Ri[2 * n + i]);
+        const double be = beta[i];
+        psi[i] = ps;
+        us[i] = cscale(or1[i], cim(dm, ps));
+        up[i] = make_double2(-dp.x - be * ps.x, -dp.y - be * ps.y);
+        omf[i] = om;
+        ho[i] = om;
+        if (lin) {
+          double2 v = make_double2(0.0, 0.0);
+          if (!edge) {
+            v = cscale(iw, csub(om, make_double2(RWr[i - 1], RWi[i - 1])));
+            if (buo) {
+              const double2 b = cim(dm, make_double2(RTr[i - 1], RTi[i - 1]));
+              const double c = rgrav[i] * or1[i] * bf;
+              v.x -= c * b.x; v.y -= c * b.y;
+            }
           }
+          hi[i] = v;
         }
-        V.hist(1, 1, S.b_impl, mi)[i] = v;
+        bad |= !isfinite(om.x) || !isfinite(om.y);
       }
-      bad = !isfinite(om.x) || !isfinite(om.y);
     }
     if (bad) s.st[2 * g + 1] = 1;
   }
@@ -543,9 +636,9 @@ __global__ void __launch_bounds__(256, 3) k_fast(PzDev d) {
 }  // namespace
 
 size_t pz_fast_smem_bytes(int G, int maxN) {
-  size_t oR, oRT, oRW, osc, ost, oce;
+  size_t oR, oRT, oRW, osc, orh, ost, oce;
   int C, sw;
-  return fast_smem_layout(G, maxN, &oR, &oRT, &oRW, &osc, &ost, &oce, &C, &sw);
+  return fast_smem_layout(G, maxN, &oR, &oRT, &oRW, &osc, &orh, &ost, &oce, &C, &sw);
 }
 
 cudaError_t pz_launch_fast(const PzDev& d, cudaStream_t s) {

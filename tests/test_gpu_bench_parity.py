@@ -32,9 +32,12 @@ the fields by ~1e-9 or more, whatever the arithmetic.  The fields are held to
 the bar above up to the first such discrete split of the dt sequences (the
 first step whose dt differs by more than 1e-9 relative differs by more than
 1e-3: a branch taken differently, not drift); later checkpoints of that
-instance are only required to be finite, and at most two of the 14
-instances may split.  Without a split, the dt sequences drift apart only
-with the fields.
+instance are only required to be finite.  A split must come from chaotic
+growth, not from a wrong step: the oracle's own noise spread must exceed
+1e-6 at the first checkpoint at or after it (in the runs so far the splits
+fall between steps 270 and 330 of the Ra ~ 3e6-1e7, E = 1e-3 instances,
+where that spread is 1e-5 to 1).  Without a split, the dt sequences drift
+apart only with the fields.
 """
 import multiprocessing as mp
 import os
@@ -191,7 +194,15 @@ def test_batched_ensemble_matches_oracle_over_500_steps(pz):
                     f"Ra={specs[i]['ra']:.3g} step {k}: fast {e:.2e} dense {ed:.2e} series {rs:.2e} "
                     f"oracle-spread {fl:.2e} series-spread {rfl:.2e} dt-split {sp}\n")
     assert not fails, "\n".join(fails)
-    assert sum(v is not None for v in split.values()) <= 2, split
+    # a dt split (the Courant hysteresis taking the other branch) is a
+    # consequence of chaotic growth only: it may come no earlier than the
+    # oracle's own noise spread reaches 1e-6 at the next checkpoint, and the
+    # fields agreed at every checkpoint before it (checked above)
+    for i, sp in split.items():
+        if sp is None:
+            continue
+        nxt = [k for k in CK if k >= sp]
+        assert nxt and _err(spread[i][nxt[0]], ref[i][nxt[0]]) > 1e-6, (i, sp)
     # the strict bar holds over all 500 steps wherever the flow is predictable
     # at that level (the oracle's own spread stays below 1e-12) and dt did not split
     for i in sel:
