@@ -13,24 +13,28 @@ Every equation is multiplied by r^2 (r^4 for the streamfunction) and
 integrated twice (four times) in r, which makes the operators banded
 (oracle/chebsparse.py derives them); the first 2 (4) rows are replaced by
 tau rows carrying the boundary conditions.  The reference stores them as
-bordered band matrices and solves with a bordered LU; this restatement holds
-them dense and solves with LAPACK, which changes only rounding.  The row
-preconditioning of get_lhs_mat_tau (one over the largest entry of each row)
-is kept.
+bordered band matrices and solves with a bordered LU (oracle/bordered.py
+restates it: ``bordered=True``); by default this restatement holds them dense
+and solves with LAPACK's dense LU, which changes only rounding -- and on the
+ill-conditioned systems of n_r_max ~ 97 at small E the dense LU is the less
+accurate of the two.  The row preconditioning of get_lhs_mat_tau (one over
+the largest entry of each row) is kept.
 """
 from __future__ import annotations
 
 import numpy as np
 import scipy.linalg as sla
 
+from .bordered import BorderedLU
 from .chebsparse import IntegOperators
 
 
 class IntegScheme:
     """The integ operators and stage routines of one ``Pizza`` instance."""
 
-    def __init__(self, pz):
+    def __init__(self, pz, bordered: bool = False):
         self.pz = pz
+        self.bordered = bordered
         p, d, c = pz.p, pz.d, pz.cheb
         N = pz.N
         self.ops = ops = IntegOperators(N, d["r_icb"], d["r_cmb"], c.rnorm)
@@ -97,6 +101,8 @@ class IntegScheme:
         A[:ntau, 0] *= self.pz.cheb.boundary_fac
         fac = 1.0 / np.max(np.abs(A), axis=1)
         A = A * fac[:, None]
+        if self.bordered:
+            return BorderedLU(A, ntau), fac
         lu, piv = sla.lu_factor(A, check_finite=True)
         if np.any(np.diag(lu) == 0.0):
             raise np.linalg.LinAlgError("Singular matrix in the integ solve")
@@ -210,6 +216,8 @@ class IntegScheme:
 
     @staticmethod
     def _solve(lu_fac, rhs):
+        if isinstance(lu_fac[0], BorderedLU):
+            return lu_fac[0].solve(rhs * lu_fac[1])
         (lu, piv), fac = lu_fac
         b = rhs * fac
         if np.iscomplexobj(lu):

@@ -904,7 +904,7 @@ def seeded_temperature(n_m_max: int, r: np.ndarray, r_icb: float, amp: float, se
 class Pizza:
     """State and stage body of pizza's collocation time step for one instance."""
 
-    def __init__(self, p: Params):
+    def __init__(self, p: Params, integ_bordered: bool = False):
         self.p = p
         d = p.derived()
         self.d = d
@@ -965,7 +965,7 @@ class Pizza:
         self._dVsXi = np.zeros(shp, complex)
         if self.l_integ:
             from .pizza_integ import IntegScheme
-            self.integ = IntegScheme(self)
+            self.integ = IntegScheme(self, bordered=integ_bordered)
 
     # -- radial functions (src/radial.f90:115-282) ---------------------------
     def _radial(self):

@@ -14,8 +14,8 @@ def gpu_config(spec):
     return pz.Config(**kw)
 
 
-def oracle(spec, temp0=None, xi0=None):
-    sim = Pizza(Params(**spec))
+def oracle(spec, temp0=None, xi0=None, integ_bordered=False):
+    sim = Pizza(Params(**spec), integ_bordered=integ_bordered)
     sim.start(temp0=temp0, xi0=xi0)
     return sim
 

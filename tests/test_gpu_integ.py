@@ -149,14 +149,21 @@ def test_integ_influence_matrix(pz, variant):
     dict(n_r_max=97, n_cheb_max=97, m_max=32, ek=1e-5, ra=3e7, dtMax=2e-6, time_scheme="SBDF3", l_ek_pump=True),
 ])
 def test_integ_banded_matches_dense(pz, variant):
-    """The bordered banded factors (pz_integ_banded(1)) and the dense per-m
-    inverses (pz_integ_banded(0), the default) solve the same systems.  After
-    25 steps the dense path matches the oracle (which factorises the same
-    row-scaled tau systems with LAPACK's dense LU) at 1e-10, 1e-9 at
-    n_r_max = 97 with the rotating direct solve, whose tau rows are ~n^6 apart
-    in scale; the banded LU, pizza's own algorithm, rounds differently on
-    these ill-conditioned systems and is held to 10x those bars (a 40-digit
-    check of one N = 97 streamfunction solve put it at 8e-14)."""
+    """The bordered banded factors (pz_integ_banded(1), pizza's own algorithm:
+    band LU of the operator block, Schur complement of the tau rows) and the
+    dense per-m inverses (pz_integ_banded(0), the default) solve the same
+    systems.  After 25 steps the dense path matches the oracle (which
+    factorises the same row-scaled tau systems with LAPACK's dense LU) at
+    1e-10, 1e-9 at n_r_max = 97 with the rotating direct solve.  The bordered
+    elimination is less accurate than a pivoted dense LU on the four-tau-row
+    streamfunction systems (against a 40-digit solve of the row-scaled
+    N = 97, E = 1e-5 systems: 1e-12 relative per solve, the dense LU 2e-14),
+    and the flow amplifies that: the oracle's own restatement of the bordered
+    solve (oracle/bordered.py, LAPACK gbtrf/gbtrs/getrf as the reference
+    calls them) drifts from the dense oracle by up to 1.3e-7 in 25 steps of
+    that case.  So the banded path must stay as close to the dense oracle as
+    the reference's algorithm does: within 10x the larger of the dense bar
+    and the bordered oracle's distance, per field."""
     spec = dict(CI, **variant)
     temp0 = seeded(spec, 5, 1e-2 if spec["n_r_max"] < 97 else 1e-4)
     assert pz.integ_banded() is False
@@ -167,18 +174,23 @@ def test_integ_banded_matches_dense(pz, variant):
     finally:
         pz.integ_banded(prev)
     sim = oracle(spec, temp0=temp0)
+    bsim = oracle(spec, temp0=temp0, integ_bordered=True)
     for e in (dense, band):
         e.set_state(0, temp=temp0)
     for _ in range(25):
         sim.advance()
+        bsim.advance()
     dense.step(25)
     band.step(25)
     gd, gb = dense.get_state(0), band.get_state(0)
     big = spec["n_r_max"] >= 97 and spec.get("matrix_solve", "DIRECT") == "DIRECT"
-    check_fields(sim, gd, 1e-9 if big else 1e-10, f"dense {variant}")
-    # the banded LU rounds differently on these tau systems: measured 2.6e-10
-    # (N = 33, composition) and 2.4e-9 (N = 97) from the oracle's dense LU
-    check_fields(sim, gb, 1e-8 if big else 1e-9, f"banded {variant}")
+    bar = 1e-9 if big else 1e-10
+    check_fields(sim, gd, bar, f"dense {variant}")
+    for f in ("temp", "us", "up", "om"):
+        ref = getattr(sim, f)
+        drift = rel_err(getattr(bsim, f), ref)
+        e = rel_err(gb[f], ref)
+        assert e < 10.0 * max(bar, drift), f"banded {variant} {f}: rel err {e:.3e}, bordered oracle {drift:.3e}"
     dense.close()
     band.close()
 
