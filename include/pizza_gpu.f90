@@ -45,7 +45,7 @@ module pizza_gpu
    integer(c_int), parameter :: PZ_NOALLOC_MAX_MN = 32768
    integer(c_int), parameter :: PZ_OBJ_EKIN3D = 0, PZ_OBJ_NUTOP = 1
    integer(c_int), parameter :: PZ_INTEG_OPS = 19
-   integer(c_int), parameter :: PZ_TUNE_FAST_G = 0, PZ_TUNE_RLOOP_RG = 1
+   integer(c_int), parameter :: PZ_TUNE_FAST_G = 0, PZ_TUNE_RLOOP_RG = 1, PZ_TUNE_LANES = 2
 
    ! One instance's namelist values, the C struct pz_config field by field.
    type, bind(c) :: pz_config

@@ -403,11 +403,17 @@ int pz_integ_banded(int enable);
  *    tensor-core stage (key ignored; value 1..16, <= 0 restores the default 8);
  *  - PZ_TUNE_RLOOP_RG: radii per block of the phi-transform kernel for
  *    n_phi_max = key (value 1..16 within its shared memory; <= 0 restores the
- *    default clamp(576 / n_phi_max, 1, 8)).
+ *    default clamp(576 / n_phi_max, 1, 8));
+ *  - PZ_TUNE_LANES: parallel lanes of a step whose instances all run the
+ *    tensor-core stage (key ignored; value 1..4, <= 0 restores the default 2):
+ *    the instances are dealt to the lanes in turn and each lane's kernels
+ *    run on their own stream inside the step's graph; handles with fewer
+ *    than 16 instances per lane take one.
  * pizza_gb300.autotune times the candidates on the device and applies the
  * winners.  PZ_E_ARG for an unknown parameter or a value out of range. */
 #define PZ_TUNE_FAST_G   0
 #define PZ_TUNE_RLOOP_RG 1
+#define PZ_TUNE_LANES    2
 int pz_tune_set(int what, int key, int value);
 
 /* No counterpart in the reference.  Eigen-decomposition the tensor-core

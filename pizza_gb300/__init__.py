@@ -244,13 +244,14 @@ def fast_path(enable=None) -> bool:
     return bool(lib.pz_fast_path(-1 if enable is None else int(bool(enable))))
 
 
-TUNE_FAST_G, TUNE_RLOOP_RG = 0, 1
+TUNE_FAST_G, TUNE_RLOOP_RG, TUNE_LANES = 0, 1, 2
 
 
 def tune_set(what: int, key: int, value: int):
     """Process-wide launch-shape table for handles created afterwards
-    (pz_tune_set): TUNE_FAST_G (instances per tensor-core block) or
-    TUNE_RLOOP_RG (radii per transform block for n_phi_max = key); value <= 0
+    (pz_tune_set): TUNE_FAST_G (instances per tensor-core block),
+    TUNE_RLOOP_RG (radii per transform block for n_phi_max = key) or
+    TUNE_LANES (parallel lanes of an all-tensor-core step); value <= 0
     restores the default."""
     lib = load_library()
     rc = lib.pz_tune_set(int(what), int(key), int(value))

@@ -51,6 +51,16 @@ struct pz_handle {
   PzItem* d_mitems_std = nullptr;
   int* d_iorder_std = nullptr;
   void* d_fast = nullptr;      // one allocation: fragments, exponents, vectors, descriptors, items
+  // lanes of the plain step (every instance on the fast path): the instances
+  // split into n_lanes interleaved sets whose kernels run on their own
+  // streams inside the step's graph, so that one set's phi transforms
+  // (FP64-bound) overlap another's tensor-core stage (latency-bound)
+  int n_lanes = 1;
+  cudaStream_t lane_stream[PZ_LANES_MAX] = {};
+  cudaEvent_t lane_fork = nullptr;
+  cudaEvent_t lane_join[PZ_LANES_MAX] = {};
+  PzDev ldev[PZ_LANES_MAX] = {};
+  int* d_lane_inst = nullptr;  // the instances lane by lane (k_cfl's blocks)
 };
 
 // host helpers of pz_host.cu

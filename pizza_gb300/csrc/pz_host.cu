@@ -541,6 +541,7 @@ int g_integ_banded = 0;   // integration method: bordered banded factors (else d
 // process-wide tuning table (pz_tune_set): k_fast instances per block, and
 // k_rloop radii per block by n_phi_max; 0 = the built-in choice
 int g_tune_fast_g = 0;
+int g_tune_lanes = 2;
 std::map<int, int> g_tune_rloop_rg;
 
 namespace {
@@ -564,12 +565,13 @@ struct FastBuild {
   PzFastHost H;
   std::vector<PzFastItem> items;
   std::vector<int> fi;
+  std::vector<int> lane_item;   // items of lane l: [lane_item[l], lane_item[l + 1])
   int maxN = 0;
   int G = PZ_FAST_G;        // instances per block, within the shared-memory budget
 };
 
 void fast_classes(pz_handle* h, const std::map<int, Basis>& bases, const std::vector<std::vector<double>>& rad,
-                  int G, FastBuild& fb) {
+                  int G, std::vector<int>& lane_of, int n_lanes, FastBuild& fb) {
   const int n = h->n_inst;
   std::vector<int> cls_of(n, -1), ucls_of(n, -1);
   std::map<std::tuple<int, double, int>, std::vector<int>> classes;
@@ -607,11 +609,21 @@ void fast_classes(pz_handle* h, const std::map<int, Basis>& bases, const std::ve
   for (int c : cl) fb.maxN = std::max(fb.maxN, fb.H.cls[c].N);
   while (G > 1 && pz_fast_smem_bytes(G, fb.maxN) > PZ_SMEM_MAX) --G;
   fb.G = G;
+  // The lanes take a class's instances G at a time in turn, so the groups
+  // are the ones a single lane would form; then lane by lane: a group never
+  // mixes lanes, and a lane's items are contiguous.
   for (int c : cl) {
+    int k = 0;
+    for (int i = 0; i < n; ++i)
+      if (cls_of[i] == c) lane_of[i] = (k++ / G) % n_lanes;
+  }
+  for (int l = 0; l < n_lanes; ++l) {
+   fb.lane_item.push_back((int)fb.items.size());
+   for (int c : cl) {
     for (int m = 0; m < fb.H.cls[c].Mc; ++m) {
       std::map<int, std::vector<int>> groups;    // by u_phi class (m = 0), else one group
       for (int i = 0; i < n; ++i)
-        if (cls_of[i] == c && h->inst[i].M > m) groups[m == 0 ? ucls_of[i] : 0].push_back(i);
+        if (cls_of[i] == c && lane_of[i] == l && h->inst[i].M > m) groups[m == 0 ? ucls_of[i] : 0].push_back(i);
       for (auto& gv : groups)
         for (size_t a = 0; a < gv.second.size(); a += G) {
           PzFastItem it;
@@ -622,7 +634,9 @@ void fast_classes(pz_handle* h, const std::map<int, Basis>& bases, const std::ve
           fb.items.push_back(it);
         }
     }
+   }
   }
+  fb.lane_item.push_back((int)fb.items.size());
   for (int i = 0; i < n; ++i)
     if (cls_of[i] >= 0) h->inst[i].flags |= PZF_FAST;
 }
@@ -689,6 +703,11 @@ extern "C" int pz_tune_set(int what, int key, int value) {
   if (what == PZ_TUNE_FAST_G) {
     if (value > PZ_FAST_GMAX) return fail(nullptr, PZ_E_ARG, "pz_tune_set: k_fast takes at most 16 instances per block");
     g_tune_fast_g = value > 0 ? value : 0;
+    return PZ_OK;
+  }
+  if (what == PZ_TUNE_LANES) {
+    if (value > PZ_LANES_MAX) return fail(nullptr, PZ_E_ARG, "pz_tune_set: at most 4 lanes");
+    g_tune_lanes = value > 0 ? value : 2;
     return PZ_OK;
   }
   if (what == PZ_TUNE_RLOOP_RG) {
@@ -968,9 +987,21 @@ extern "C" int pz_create(const pz_config* cfgs, int n, pz_handle** out) {
     maxM = std::max(maxM, I.M);
   }
   // tensor-core stage: classes, eigen-bases and work items of the eligible instances
+  // lanes of the plain step: the instances in work-list order (largest
+  // first), dealt to the lanes in turn so that each lane gets the same mix
+  // (the tensor-core instances then by whole k_fast groups per class)
+  std::vector<int> order(n);
+  for (int i = 0; i < n; ++i) order[i] = i;
+  std::stable_sort(order.begin(), order.end(), [&](int a, int b) {
+    return (long long)h->inst[a].N * h->inst[a].M > (long long)h->inst[b].N * h->inst[b].M;
+  });
+  int n_lanes = std::min(std::max(g_tune_lanes, 1), PZ_LANES_MAX);
+  if (n < 16 * n_lanes) n_lanes = 1;
+  std::vector<int> lane_of(n, 0);    // fast_classes deals its instances by whole groups
+  for (int k = 0; k < n; ++k) lane_of[order[k]] = k % n_lanes;
   FastBuild fb;
   const int fast_g = g_tune_fast_g > 0 ? g_tune_fast_g : PZ_FAST_G;
-  fast_classes(h, bases, rad, fast_g, fb);
+  fast_classes(h, bases, rad, fast_g, lane_of, n_lanes, fb);
   // per-instance operators and state
   for (int i = 0; i < n; ++i) {
     PzInst& I = h->inst[i];
@@ -1085,17 +1116,24 @@ extern "C" int pz_create(const pz_config* cfgs, int n, pz_handle** out) {
     return PZ_E_CUDA;
   }
   // work lists: radii and m, largest instances first
-  std::vector<int> order(n);
-  for (int i = 0; i < n; ++i) order[i] = i;
-  std::stable_sort(order.begin(), order.end(), [&](int a, int b) {
-    return (long long)h->inst[a].N * h->inst[a].M > (long long)h->inst[b].N * h->inst[b].M;
-  });
   std::vector<PzItem> ritems, mitems, oitems;
-  for (int i : order) {
-    for (int r = 0; r < h->inst[i].N; r += h->inst[i].rg) ritems.push_back({i, r});
-    for (int m = 0; m < h->inst[i].M; ++m) mitems.push_back({i, m});
-    for (int r = 0; r < h->inst[i].N; r += PZ_OBS_RC) oitems.push_back({i, r});
+  std::vector<int> lane_r, lane_o, lane_i, linst;   // lane l's ranges of ritems, oitems, linst
+  for (int l = 0; l < n_lanes; ++l) {
+    lane_r.push_back((int)ritems.size());
+    lane_o.push_back((int)oitems.size());
+    lane_i.push_back((int)linst.size());
+    for (int i : order) {
+      if (lane_of[i] != l) continue;
+      for (int r = 0; r < h->inst[i].N; r += h->inst[i].rg) ritems.push_back({i, r});
+      for (int r = 0; r < h->inst[i].N; r += PZ_OBS_RC) oitems.push_back({i, r});
+      linst.push_back(i);
+    }
   }
+  lane_r.push_back((int)ritems.size());
+  lane_o.push_back((int)oitems.size());
+  lane_i.push_back((int)linst.size());
+  for (int i : order)
+    for (int m = 0; m < h->inst[i].M; ++m) mitems.push_back({i, m});
   if ((e = cudaMalloc(&h->d_inst, n * sizeof(PzInst))) || (e = cudaMalloc(&h->d_state, n * sizeof(PzState))) ||
       (e = cudaMalloc(&h->d_ritems, ritems.size() * sizeof(PzItem))) ||
       (e = cudaMalloc(&h->d_mitems, mitems.size() * sizeof(PzItem))) ||
@@ -1227,6 +1265,37 @@ extern "C" int pz_create(const pz_config* cfgs, int n, pz_handle** out) {
     }
     if (any_assembly) h->fplan.push_back({PZK_ASSEMBLE, 0});
     h->fplan.push_back({PZK_OBS, 0});
+    // lanes: every instance on the fast path and no assembly stage (the
+    // plan is then k_rloop, k_cfl, k_fast, k_obs, each over its own items)
+    if (n_lanes > 1 && ostd.empty() && !any_assembly) {
+      if ((e = cudaMalloc(&h->d_lane_inst, n * sizeof(int))) ||
+          (e = cudaMemcpyAsync(h->d_lane_inst, linst.data(), n * sizeof(int), cudaMemcpyHostToDevice, h->stream)) ||
+          (e = cudaEventCreateWithFlags(&h->lane_fork, cudaEventDisableTiming))) {
+        g_create_error = std::string("lanes: ") + cudaGetErrorString(e);
+        pz_destroy(h);
+        return PZ_E_NOMEM;
+      }
+      for (int l = 0; l < n_lanes; ++l) {
+        if ((e = cudaStreamCreateWithFlags(&h->lane_stream[l], cudaStreamNonBlocking)) ||
+            (e = cudaEventCreateWithFlags(&h->lane_join[l], cudaEventDisableTiming))) {
+          g_create_error = std::string("lanes: ") + cudaGetErrorString(e);
+          pz_destroy(h);
+          return PZ_E_NOMEM;
+        }
+        PzDev& L = h->ldev[l];
+        L = h->fdev;
+        L.ritems = h->d_ritems + lane_r[l];
+        L.n_ritems = lane_r[l + 1] - lane_r[l];
+        L.oitems = h->d_oitems + lane_o[l];
+        L.n_oitems = lane_o[l + 1] - lane_o[l];
+        L.obs_part = h->d_obs_part + (long long)lane_o[l] * PZ_OBS_NP;   // k_obs indexes it by block
+        L.cfl_inst = h->d_lane_inst + lane_i[l];
+        L.n_inst = lane_i[l + 1] - lane_i[l];
+        L.fast.items = h->fdev.fast.items + fb.lane_item[l];
+        L.fast.n_items = fb.lane_item[l + 1] - fb.lane_item[l];
+      }
+      h->n_lanes = n_lanes;
+    }
   }
   if ((e = pz_launch_init_state(h->dev, -1, h->stream)) || (e = pz_launch_build_static(h->dev, h->stream)) ||
       (e = cudaStreamSynchronize(h->stream))) {
@@ -1337,8 +1406,20 @@ extern "C" int pz_step(pz_handle* h, int n_steps) {
     cudaGraph_t g;
     if ((e = cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal))) return cuda_fail(h, e, "capture");
     const bool fast = h->n_fast > 0;
-    for (const PzLaunch& L : fast ? h->fplan : h->plan)
-      if (!e) e = pz_launch_step_kernel(fast ? h->fdev : h->dev, L.kind, L.stage, h->stream);
+    if (fast && h->n_lanes > 1) {
+      // fork the lanes from the capturing stream, join them back into it
+      e = cudaEventRecord(h->lane_fork, h->stream);
+      for (int l = 0; l < h->n_lanes && !e; ++l) {
+        e = cudaStreamWaitEvent(h->lane_stream[l], h->lane_fork, 0);
+        for (const PzLaunch& L : h->fplan)
+          if (!e) e = pz_launch_step_kernel(h->ldev[l], L.kind, L.stage, h->lane_stream[l]);
+        if (!e) e = cudaEventRecord(h->lane_join[l], h->lane_stream[l]);
+        if (!e) e = cudaStreamWaitEvent(h->stream, h->lane_join[l], 0);
+      }
+    } else {
+      for (const PzLaunch& L : fast ? h->fplan : h->plan)
+        if (!e) e = pz_launch_step_kernel(fast ? h->fdev : h->dev, L.kind, L.stage, h->stream);
+    }
     cudaError_t e2 = cudaStreamEndCapture(h->stream, &g);
     if (e || e2) return cuda_fail(h, e ? e : e2, "capture");
     e = cudaGraphInstantiate(&h->graph, g, 0);
@@ -1619,7 +1700,7 @@ extern "C" int pz_get_dims(pz_handle* h, int inst, int* n_r_max, int* n_m_max, i
 
 extern "C" int pz_launches_per_step(pz_handle* h) {
   if (!h) return 0;
-  return (int)(h->n_fast > 0 ? h->fplan.size() : h->plan.size());
+  return (int)(h->n_fast > 0 ? h->fplan.size() * h->n_lanes : h->plan.size());
 }
 
 extern "C" int pz_latest_rows(pz_handle* h, double* rows) {
@@ -1759,6 +1840,12 @@ extern "C" int pz_destroy(pz_handle* h) {
   cudaFree(h->d_fast);
   cudaFree(h->d_mitems_std);
   cudaFree(h->d_iorder_std);
+  cudaFree(h->d_lane_inst);
+  for (int l = 0; l < PZ_LANES_MAX; ++l) {
+    if (h->lane_stream[l]) cudaStreamDestroy(h->lane_stream[l]);
+    if (h->lane_join[l]) cudaEventDestroy(h->lane_join[l]);
+  }
+  if (h->lane_fork) cudaEventDestroy(h->lane_fork);
   if (h->stream) cudaStreamDestroy(h->stream);
   delete h;
   return PZ_OK;

@@ -26,6 +26,7 @@
 #define PZ_SMEM_MAX (227 * 1024)
 #define PZ_OBS_RC 16        // k_obs: radii per block
 #define PZ_OBS_NP 10        // k_obs: partial sums per block
+#define PZ_LANES_MAX 4      // parallel lanes of the plain step's graph
 #define PZ_MAX_STAGES 8     // DIRK stages
 #define PZ_BT_LD (PZ_MAX_STAGES + 1)
 // DIRK tables at o_bt (unscaled, row-major with leading dimension PZ_BT_LD):
@@ -242,6 +243,7 @@ struct PzDev {
                                           // contiguous in mitems, m ascending)
   int n_iorder;                           // instances of the per-m work list (mitems)
   int n_inst;
+  const int* cfl_inst;      // instances of k_cfl's n_inst blocks (null: the block index)
   int any_chem;             // some instance has composition: the step launches the
                             // kernels' composition instantiations
   int maxN, maxP, maxM;

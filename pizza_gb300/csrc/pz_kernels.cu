@@ -224,7 +224,7 @@ __global__ void __launch_bounds__(256, CHEM ? 3 : 4) k_rloop(PzDev d, int stage)
 // (src/courant.f90:78-167, src/step_time.f90:281-329)
 // ---------------------------------------------------------------------------
 __global__ void k_cfl(PzDev d) {
-  const int inst = blockIdx.x;
+  const int inst = d.cfl_inst ? d.cfl_inst[blockIdx.x] : (int)blockIdx.x;
   const PzInst& I = d.inst[inst];
   PzState& S = d.state[inst];
   if (S.status != 0) return;

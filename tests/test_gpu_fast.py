@@ -6,6 +6,7 @@ CNAB2 take the fast path by default; pz_fast_path(0) keeps a handle created
 afterwards on the dense kernels.  Both must give the oracle's step to FP64
 rounding, so they agree with each other far below the 1e-10 parity bar.
 """
+import os
 import numpy as np
 import pytest
 
@@ -91,3 +92,29 @@ def test_mixed_fast_and_dense_instances_in_one_graph(pz):
         g = ens.get_state(i)
         for f in ("temp", "us", "up", "om"):
             assert rel_err(g[f], getattr(sim, f)) < 1e-10, (i, f)
+
+
+@pytest.mark.gpu
+def test_lanes_change_nothing_but_the_schedule(pz):
+    """The 256-instance bench handle stepped as two lanes (the default) and as
+    one: the same kernels over the same instances, so the same bits."""
+    import sys
+    sys.path.insert(0, os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
+    import bench
+    specs = bench.ensemble_specs(256)
+    temps = [bench.seeded_temp(s) for s in specs]
+    states = []
+    for lanes in (2, 1):
+        pz.tune_set(pz.TUNE_LANES, 0, lanes)
+        try:
+            e = pz.Ensemble([bench.gpu_cfg(s) for s in specs])
+        finally:
+            pz.tune_set(pz.TUNE_LANES, 0, 0)
+        assert e.launches_per_step() == 4 * lanes
+        e.set_state_all(temps)
+        e.step(40)
+        states.append(([e.get_state(i)["om"] for i in (0, 77, 255)], e.latest_rows()))
+        e.close()
+    for a, b in zip(states[0][0], states[1][0]):
+        assert np.array_equal(a, b)
+    assert np.array_equal(states[0][1], states[1][1])
