@@ -52,11 +52,12 @@ struct pz_handle {
   int* d_iorder_std = nullptr;
   void* d_fast = nullptr;      // one allocation: fragments, exponents, vectors, descriptors, items
   // lanes of the plain step (every instance on the fast path): the instances
-  // split into n_lanes interleaved sets whose kernels run on their own
-  // streams inside the step's graph, so that one set's phi transforms
-  // (FP64-bound) overlap another's tensor-core stage (latency-bound)
+  // split into n_lanes sets, each stepped by its own graph on its own
+  // stream, so that one set's phi transforms (FP64-bound) overlap another's
+  // tensor-core stage (latency-bound)
   int n_lanes = 1;
   cudaStream_t lane_stream[PZ_LANES_MAX] = {};
+  cudaGraphExec_t lane_graph[PZ_LANES_MAX] = {};
   cudaEvent_t lane_fork = nullptr;
   cudaEvent_t lane_join[PZ_LANES_MAX] = {};
   PzDev ldev[PZ_LANES_MAX] = {};

@@ -1401,25 +1401,42 @@ extern "C" int pz_step(pz_handle* h, int n_steps) {
   if (!h) return fail(nullptr, PZ_E_ARG, "pz_step: null handle");
   pz_adjoint_invalidate(h);
   if (n_steps < 0) return fail(h, PZ_E_ARG, "pz_step: n_steps < 0");
-  cudaError_t e;
+  cudaError_t e = cudaSuccess;
+  const bool fast = h->n_fast > 0;
+  if (fast && h->n_lanes > 1) {
+    // one graph per lane on the lane's own stream; the lanes start after the
+    // work already on the handle's stream and the handle's stream waits for
+    // all of them at the end, so the lanes run their steps independently
+    // in between (one lane's transforms beside another's stage)
+    for (int l = 0; l < h->n_lanes && !h->lane_graph[l]; ++l) {
+      cudaGraph_t g;
+      if ((e = cudaStreamBeginCapture(h->lane_stream[l], cudaStreamCaptureModeThreadLocal)))
+        return cuda_fail(h, e, "capture");
+      for (const PzLaunch& L : h->fplan)
+        if (!e) e = pz_launch_step_kernel(h->ldev[l], L.kind, L.stage, h->lane_stream[l]);
+      cudaError_t e2 = cudaStreamEndCapture(h->lane_stream[l], &g);
+      if (e || e2) return cuda_fail(h, e ? e : e2, "capture");
+      e = cudaGraphInstantiate(&h->lane_graph[l], g, 0);
+      cudaGraphDestroy(g);
+      if (e) { h->lane_graph[l] = nullptr; return cuda_fail(h, e, "graph instantiate"); }
+    }
+    if ((e = cudaEventRecord(h->lane_fork, h->stream))) return cuda_fail(h, e, "lanes");
+    for (int l = 0; l < h->n_lanes; ++l)
+      if ((e = cudaStreamWaitEvent(h->lane_stream[l], h->lane_fork, 0))) return cuda_fail(h, e, "lanes");
+    for (int s = 0; s < n_steps; ++s)
+      for (int l = 0; l < h->n_lanes; ++l)
+        if ((e = cudaGraphLaunch(h->lane_graph[l], h->lane_stream[l]))) return cuda_fail(h, e, "graph launch");
+    for (int l = 0; l < h->n_lanes; ++l)
+      if ((e = cudaEventRecord(h->lane_join[l], h->lane_stream[l])) ||
+          (e = cudaStreamWaitEvent(h->stream, h->lane_join[l], 0)))
+        return cuda_fail(h, e, "lanes");
+    return PZ_OK;
+  }
   if (!h->graph) {
     cudaGraph_t g;
     if ((e = cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal))) return cuda_fail(h, e, "capture");
-    const bool fast = h->n_fast > 0;
-    if (fast && h->n_lanes > 1) {
-      // fork the lanes from the capturing stream, join them back into it
-      e = cudaEventRecord(h->lane_fork, h->stream);
-      for (int l = 0; l < h->n_lanes && !e; ++l) {
-        e = cudaStreamWaitEvent(h->lane_stream[l], h->lane_fork, 0);
-        for (const PzLaunch& L : h->fplan)
-          if (!e) e = pz_launch_step_kernel(h->ldev[l], L.kind, L.stage, h->lane_stream[l]);
-        if (!e) e = cudaEventRecord(h->lane_join[l], h->lane_stream[l]);
-        if (!e) e = cudaStreamWaitEvent(h->stream, h->lane_join[l], 0);
-      }
-    } else {
-      for (const PzLaunch& L : fast ? h->fplan : h->plan)
-        if (!e) e = pz_launch_step_kernel(fast ? h->fdev : h->dev, L.kind, L.stage, h->stream);
-    }
+    for (const PzLaunch& L : fast ? h->fplan : h->plan)
+      if (!e) e = pz_launch_step_kernel(fast ? h->fdev : h->dev, L.kind, L.stage, h->stream);
     cudaError_t e2 = cudaStreamEndCapture(h->stream, &g);
     if (e || e2) return cuda_fail(h, e ? e : e2, "capture");
     e = cudaGraphInstantiate(&h->graph, g, 0);
@@ -1823,6 +1840,8 @@ extern "C" int pz_destroy(pz_handle* h) {
   if (h->stream) cudaStreamSynchronize(h->stream);
   pz_adjoint_free(h);
   if (h->graph) cudaGraphExecDestroy(h->graph);
+  for (int l = 0; l < PZ_LANES_MAX; ++l)
+    if (h->lane_graph[l]) cudaGraphExecDestroy(h->lane_graph[l]);
   cudaFree(h->pool);
   cudaFree(h->d_inst);
   cudaFree(h->d_state);
