@@ -606,8 +606,8 @@ def main():
         else:
             table = autotune.tune([gpu_cfg(s) for s in specs], temps)
             source = "tuned in this run on this workload"
-            out_dir = os.path.join(os.path.dirname(os.path.abspath(__file__)), "gpurun_out")
-            if os.path.isdir(out_dir):
+            out_dir = os.environ.get("PZ_REPORT_DIR", "")
+            if out_dir and os.path.isdir(out_dir):
                 autotune.save(table, os.path.join(out_dir, "tuning_gb300.json"))
         autotune.apply(table)
         tuning = {"source": source, "k_fast_G": table.get("k_fast_G"), "k_rloop_rg": table.get("k_rloop_rg"),

@@ -187,8 +187,9 @@ def test_batched_ensemble_matches_oracle_over_500_steps(pz):
                 fails.append(f"instance {i} step {k}: series rel err {rs:.2e}, oracle spread {rfl:.2e}")
             if e <= 1e-10 and strict_until[i] == (CK[CK.index(k) - 1] if k != CK[0] else 0):
                 strict_until[i] = k
-    out_dir = os.path.join(ROOT, "gpurun_out")
-    with open(os.path.join(out_dir, "bench_parity.txt") if os.path.isdir(out_dir) else os.devnull, "w") as f:
+    out_dir = os.environ.get("PZ_REPORT_DIR", "")
+    with open(os.path.join(out_dir, "bench_parity.txt") if out_dir and os.path.isdir(out_dir) else os.devnull,
+              "w") as f:
         for i, k, e, ed, fl, rs, rfl, sp in report:
             f.write(f"inst {i} N={specs[i]['n_r_max']} P={3 * specs[i]['m_max']} ek={specs[i]['ek']} "
                     f"Ra={specs[i]['ra']:.3g} step {k}: fast {e:.2e} dense {ed:.2e} series {rs:.2e} "

@@ -329,8 +329,8 @@ def test_c1_integ_sbdf3_full_size(pz):
             fail = k
             break
         dts.append(ens.get_step_state(0)[1][0])
-    out_dir = os.path.join(os.path.dirname(HERE), "gpurun_out")
-    if os.path.isdir(out_dir):
+    out_dir = os.environ.get("PZ_REPORT_DIR", "")
+    if out_dir and os.path.isdir(out_dir):
         with open(os.path.join(out_dir, "c1_integ_parity.txt"), "w") as f:
             for k, errs, fl in report:
                 f.write(f"step {k}: " + " ".join(f"{a} {e:.2e}" for a, e in errs.items())
