@@ -291,27 +291,62 @@ def cpu_baseline(specs, nsteps=4):
                       f"({len(classes)} classes), scaled by the class counts of the {len(specs)}-instance batch"}
 
 
+def workload_config(specs):
+    return {"workload": f"batched ensemble of {len(specs)} annulus instances per GPU: "
+                        "n_r_max in {33,49,65}, n_phi_max in {96,192,288}, Ra log-uniform [1e5, Ra_max(N)] "
+                        "with Ra_max = 1e6/3e6/1e7 for N = 33/49/65, E in {1e-3,1e-4}, CNAB2, CFL 0.5, "
+                        "collocation + influence matrix",
+            "instances": len(specs), "l2": "working set (operators + state, GBs) far larger than L2",
+            "solve": "INFLUENCE"}
+
+
+def _cpu_instance_time(args):
+    """One instance of the workload on one core: start, `warmup` untimed
+    steps (the first builds the matrices), then `steps` timed steps."""
+    spec, warmup, steps = args
+    from oracle.pizza_oracle import Params, Pizza
+    kw = {k: v for k, v in spec.items() if k != "seed"}
+    sim = Pizza(Params(**kw))
+    sim.start(temp0=seeded_temp(spec))
+    for _ in range(max(1, warmup)):
+        sim.advance()
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        sim.advance()
+    return time.perf_counter() - t0
+
+
+# a bound on the reference arm's CPU work: instance-steps it may run in all
+# (about a minute on 16 host cores at the workload's ~7 ms per instance-step)
+REF_MAX_INSTANCE_STEPS = 256 * 520
+
+
 def reference_arm(args, specs):
-    """--impl reference: the oracle port of the reference's CPU algorithm on all host cores."""
+    """--impl reference: the oracle port of the reference's CPU algorithm on
+    all host cores, one process per core, over the same workload as the GPU
+    arm (every instance, W warm-up and K timed steps each) unless that
+    exceeds REF_MAX_INSTANCE_STEPS, in which case the steps are cut to fit
+    and the line says so."""
     import multiprocessing as mp
     cores = os.cpu_count() or 1
-    sample = specs[: min(len(specs), max(cores, 32))]
-    steps = max(1, min(args.steps, 3))
+    warmup = max(3, args.warmup)
+    steps = max(1, min(args.steps, REF_MAX_INSTANCE_STEPS // max(1, len(specs)) - warmup))
     ctx = mp.get_context("spawn")
     t0 = time.perf_counter()
     with ctx.Pool(cores) as pool:
-        per = pool.map(_cpu_class_time, [(s, steps) for s in sample])
+        per = pool.map(_cpu_instance_time, [(s, warmup, steps) for s in specs])
     wall = time.perf_counter() - t0
-    # aggregate rate of `cores` workers each stepping its own instances
-    rate = len(sample) / (sum(per) / cores)
+    # aggregate rate of `cores` workers each stepping its share of the instances
+    rate = len(specs) * steps / (sum(per) / cores)
+    same = steps == args.steps
     line = {"impl": "reference", "metric": METRIC, "value": rate, "unit": UNIT, "n_gpus": 0,
-            "steps": steps, "warmup": 1, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-            "dtype": "f64", "data": "synthetic",
-            "config": {"workload": f"batched ensemble of {len(specs)} annulus instances",
-                       "instances_sampled": len(sample)},
+            "steps": steps, "warmup": warmup, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f64", "data": "synthetic", "config": workload_config(specs),
             "cpu_baseline": {"value": rate, "unit": UNIT, "cores": cores, "kind": "port",
-                             "sample": f"{len(sample)} instances x {steps} steps of the oracle port, one process "
-                                       f"per core; wall {wall:.1f}s incl. matrix set-up"},
+                             "sample": f"all {len(specs)} instances x {steps} timed steps (after {warmup} "
+                                       f"untimed) of the oracle port, one process per core; wall {wall:.1f}s "
+                                       "incl. matrix set-up" + ("" if same else
+                                       f"; steps cut from {args.steps} to bound the run")},
             "e2e": {"value": rate, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line))
 
@@ -726,12 +761,7 @@ def main():
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": f"batched ensemble of {len(specs)} annulus instances per GPU: "
-                               "n_r_max in {33,49,65}, n_phi_max in {96,192,288}, Ra log-uniform [1e5, Ra_max(N)] "
-                               "with Ra_max = 1e6/3e6/1e7 for N = 33/49/65, E in {1e-3,1e-4}, CNAB2, CFL 0.5, "
-                               "collocation + influence matrix",
-                   "instances": len(specs), "l2": "working set (operators + state, GBs) far larger than L2",
-                   "solve": "INFLUENCE"},
+        "config": workload_config(specs),
         "plain_steps_per_s": plain["value"] if plain else None,
         "batched_over_plain": (value / world / plain["value"]) if plain else None,
         "plain_detail": plain,
