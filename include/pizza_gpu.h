@@ -162,6 +162,11 @@ int pz_get_state_xi(pz_handle* h, int inst, double* xi, double* dxi);
 /* Advance every instance by n_steps time steps: for each step the stage body
  * of time_loop, with the CFL decision, weight update and matrix rebuild done
  * on the device.  The step is captured once in a CUDA graph and replayed.
+ * A handle whose instances all run the tensor-core stage steps them in lanes
+ * (PZ_TUNE_LANES), each through its own graph on its own stream; the lanes
+ * start after the work already on the handle's stream (pz_stream) and that
+ * stream waits for them before anything enqueued after pz_step, so callers
+ * order their work on pz_stream exactly as with one graph.
  * Asynchronous: returns after enqueueing; pz_sync() waits and reports
  * device-side errors. */
 int pz_step(pz_handle* h, int n_steps);
