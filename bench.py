@@ -646,6 +646,7 @@ def main():
                 autotune.save(table, os.path.join(out_dir, "tuning_gb300.json"))
         autotune.apply(table)
         tuning = {"source": source, "k_fast_G": table.get("k_fast_G"), "k_rloop_rg": table.get("k_rloop_rg"),
+                  "lanes": table.get("lanes"),
                   "gain_over_defaults": autotune.gain(table), "candidates_ms_per_step": table.get("ms"),
                   "seconds": time.perf_counter() - t0}
     ens = pz.Ensemble([gpu_cfg(s) for s in specs])

@@ -8,11 +8,15 @@ best value depends on the workload's grids:
   share each operator fragment loaded from L2, fewer blocks fill the GPU;
 - the phi-transform kernel's radii per block for each n_phi_max (k_rloop):
   more radii per block give the FFT stages more parallel work per barrier,
-  fewer resident blocks per SM.
+  fewer resident blocks per SM;
+- the lanes of a step whose instances all run the tensor-core stage: more
+  lanes overlap one lane's transforms with another's stage, but split the
+  classes into more partly filled k_fast groups.
 
 ``tune(configs, ...)`` builds handles of the given instances (a workload's own
-configurations), times every candidate with CUDA events over the kernels
-launched one by one (pz_step_profile), and returns the table; ``apply``
+configurations), times every launch-shape candidate with CUDA events over the
+kernels launched one by one (pz_step_profile) and every lane count over whole
+steps (the lanes exist only in the step's graphs), and returns the table; ``apply``
 installs a table for handles created afterwards (pz_tune_set) and
 ``save``/``load`` persist it as JSON.
 """
@@ -22,10 +26,14 @@ import json
 
 import numpy as np
 
-from . import Ensemble, TUNE_FAST_G, TUNE_RLOOP_RG, tune_set
+import time
+
+from . import Ensemble, TUNE_FAST_G, TUNE_LANES, TUNE_RLOOP_RG, tune_set
 
 FAST_G = (4, 8, 12, 16)
 RLOOP_RG = (1, 2, 3, 4, 6, 8)
+LANES = (1, 2, 4)
+DEFAULT_LANES = 2
 
 
 def _time(configs, temps, kernel, steps, warmup):
@@ -38,12 +46,26 @@ def _time(configs, temps, kernel, steps, warmup):
         ens.close()
 
 
-def tune(configs, temps, steps=10, warmup=3, fast_g=FAST_G, rloop_rg=RLOOP_RG, log=None):
+def _time_steps(configs, temps, steps, warmup):
+    """ms per whole step of a handle (host clock around pz_step(steps) and
+    pz_sync, after the warm-up): the lanes run only inside pz_step."""
+    ens = Ensemble(configs)
+    try:
+        ens.set_state_all(temps)
+        ens.step(warmup)
+        t0 = time.perf_counter()
+        ens.step(steps)
+        return (time.perf_counter() - t0) * 1e3 / steps
+    finally:
+        ens.close()
+
+
+def tune(configs, temps, steps=10, warmup=3, fast_g=FAST_G, rloop_rg=RLOOP_RG, lanes=LANES, log=None):
     """Time the candidates for `configs` (a list of pizza_gb300.Config) started
     from `temps` (their initial temperature perturbations); returns
-    {"k_fast_G": g, "k_rloop_rg": {n_phi_max: rg}, "ms": {...}} with the
-    per-step device ms of every candidate and of the built-in defaults."""
-    table = {"k_fast_G": None, "k_rloop_rg": {}, "ms": {"k_fast": {}, "k_rloop": {}}}
+    {"k_fast_G": g, "k_rloop_rg": {n_phi_max: rg}, "lanes": l, "ms": {...}}
+    with the per-step ms of every candidate and of the built-in defaults."""
+    table = {"k_fast_G": None, "k_rloop_rg": {}, "lanes": None, "ms": {"k_fast": {}, "k_rloop": {}, "lanes": {}}}
     # k_fast: all instances together (its blocks mix classes)
     best = None
     for g in fast_g:
@@ -80,6 +102,20 @@ def tune(configs, temps, steps=10, warmup=3, fast_g=FAST_G, rloop_rg=RLOOP_RG, l
         table["ms"]["k_rloop"][str(P)]["default"] = _time(cf, tp, "k_rloop", steps, warmup)
         if best is not None:
             table["k_rloop_rg"][str(P)] = best[0]
+    # lanes: whole steps of the whole workload (its own G and radii per block)
+    apply({k: table[k] for k in ("k_fast_G", "k_rloop_rg")})
+    best = None
+    for n in lanes:
+        tune_set(TUNE_LANES, 0, n)
+        ms = _time_steps(configs, temps, 4 * steps, warmup)
+        table["ms"]["lanes"][str(n)] = ms
+        if log:
+            log(f"lanes {n}: {ms:.4f} ms/step")
+        if best is None or ms < best[1]:
+            best = (n, ms)
+    reset(table)
+    if best is not None:
+        table["lanes"] = best[0]
     return table
 
 
@@ -89,11 +125,14 @@ def apply(table):
         tune_set(TUNE_FAST_G, 0, int(table["k_fast_G"]))
     for P, rg in table.get("k_rloop_rg", {}).items():
         tune_set(TUNE_RLOOP_RG, int(P), int(rg))
+    if table.get("lanes"):
+        tune_set(TUNE_LANES, 0, int(table["lanes"]))
 
 
 def reset(table=None):
     """Back to the built-in launch shapes."""
     tune_set(TUNE_FAST_G, 0, 0)
+    tune_set(TUNE_LANES, 0, 0)
     for P in (table or {}).get("k_rloop_rg", {}):
         tune_set(TUNE_RLOOP_RG, int(P), 0)
 
@@ -121,5 +160,8 @@ def gain(table):
         tot_t += d[str(rg)]
     if tot_t > 0:
         out["k_rloop"] = tot_d / tot_t
+    lm = ms.get("lanes", {})
+    if table.get("lanes") and str(DEFAULT_LANES) in lm and str(table["lanes"]) in lm:
+        out["lanes"] = lm[str(DEFAULT_LANES)] / lm[str(table["lanes"])]
     return {k: float(np.round(v, 4)) for k, v in out.items()}
 

@@ -48,3 +48,4 @@ def test_two_gloo_replicas():
     assert v0 == v1 == 2 * 8 * 5 / 11.0e-3          # both ranks' instances against it
     assert [x[3] for x in s0] != [x[3] for x in s1]  # seeds of their own
     assert sorted((a, b) for a, b, _, _ in s0) != [] and all(a in (33, 49, 65) for a, _, _, _ in s0 + s1)
+
