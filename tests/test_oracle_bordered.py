@@ -71,19 +71,38 @@ def test_bordered_against_exact_n97():
     assert ed < 1e-13 and 1e-13 < eb < 1e-10, errs
 
 
-@pytest.mark.parametrize("case", ["RotInteg", "FingConv"])
-def test_bordered_oracle_matches_reference_fixture(case):
-    """pizza.exe solved these integration-method runs with its bordered LU;
-    the oracle with the restated bordered solve reproduces their time series
-    at the reference harness's rtol 1e-8 as the dense-LU oracle does."""
+_BORDERED_RUNS = {}
+
+
+def _bordered_run(case):
+    """The bordered-solve oracle's run of a fixture case (a continuation case
+    restarts from its first run's final state, as in test_oracle_golden)."""
     import json
     import os
+    from tests.test_oracle_golden import checkpoint_of
+    if case not in _BORDERED_RUNS:
+        here = os.path.dirname(os.path.abspath(__file__))
+        with open(os.path.join(here, "golden", "cases.json")) as f:
+            spec = json.load(f)[case]
+        sim = Pizza(Params(**spec["params"]), integ_bordered=True)
+        if "restart_from" in spec:
+            sim.start_from_checkpoint(checkpoint_of(_bordered_run(spec["restart_from"])[0]))
+        else:
+            sim.start()
+        _BORDERED_RUNS[case] = (sim, sim.run()[spec["series"]])
+    return _BORDERED_RUNS[case]
+
+
+@pytest.mark.parametrize("case", ["RotInteg", "RotIntegContinue", "FingConv"])
+def test_bordered_oracle_matches_reference_fixture(case):
+    """pizza.exe solved these integration-method runs (the direct solve, and
+    the influence-matrix solve of the continuation on N = 97) with its
+    bordered LU; the oracle with the restated bordered solve reproduces their
+    time series at the reference harness's rtol 1e-8 as the dense-LU oracle
+    does."""
+    import os
     here = os.path.dirname(os.path.abspath(__file__))
-    with open(os.path.join(here, "golden", "cases.json")) as f:
-        spec = json.load(f)[case]
     ref = np.loadtxt(os.path.join(here, "golden", f"{case}.txt"))
-    sim = Pizza(Params(**spec["params"]), integ_bordered=True)
-    sim.start()
-    rows = sim.run()[spec["series"]]
+    rows = _bordered_run(case)[1]
     assert rows.shape == ref.shape
     np.testing.assert_allclose(rows, ref, rtol=1e-8, atol=1e-20)
