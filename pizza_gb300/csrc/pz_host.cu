@@ -1423,13 +1423,15 @@ extern "C" int pz_step(pz_handle* h, int n_steps) {
     if ((e = cudaEventRecord(h->lane_fork, h->stream))) return cuda_fail(h, e, "lanes");
     for (int l = 0; l < h->n_lanes; ++l)
       if ((e = cudaStreamWaitEvent(h->lane_stream[l], h->lane_fork, 0))) return cuda_fail(h, e, "lanes");
-    for (int s = 0; s < n_steps; ++s)
-      for (int l = 0; l < h->n_lanes; ++l)
-        if ((e = cudaGraphLaunch(h->lane_graph[l], h->lane_stream[l]))) return cuda_fail(h, e, "graph launch");
-    for (int l = 0; l < h->n_lanes; ++l)
-      if ((e = cudaEventRecord(h->lane_join[l], h->lane_stream[l])) ||
-          (e = cudaStreamWaitEvent(h->stream, h->lane_join[l], 0)))
-        return cuda_fail(h, e, "lanes");
+    for (int s = 0; s < n_steps && !e; ++s)
+      for (int l = 0; l < h->n_lanes && !e; ++l) e = cudaGraphLaunch(h->lane_graph[l], h->lane_stream[l]);
+    // join whatever was launched, also after a failed launch, so that work
+    // enqueued on the handle's stream afterwards still follows the lanes
+    cudaError_t ej = cudaSuccess;
+    for (int l = 0; l < h->n_lanes && !ej; ++l)
+      if (!(ej = cudaEventRecord(h->lane_join[l], h->lane_stream[l]))) ej = cudaStreamWaitEvent(h->stream, h->lane_join[l], 0);
+    if (e) return cuda_fail(h, e, "graph launch");
+    if (ej) return cuda_fail(h, ej, "lanes");
     return PZ_OK;
   }
   if (!h->graph) {
